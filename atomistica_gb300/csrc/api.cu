@@ -1,0 +1,525 @@
+// C-ABI of the potentials (replaces the generated shims
+// python_<mod>_{new,free,bind_to,energy_and_forces}, src/python/gen_factory.py:98-356,
+// and COMPUTE_FUNC / BIND_TO_FUNC, src/potentials/bop/default_compute_func.f90:25-100,
+// default_bind_to_func.f90:25-146, src/potentials/eam/tabulated_alloy_eam.f90:297-415).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "bop_math.h"
+#include "potential.h"
+
+using namespace gb;
+
+struct gb_potential {
+  Potential pot;
+};
+
+namespace gb {
+namespace {
+
+// Default parameter sets: Tersoff_PRB_39_5566_SiC (tersoff_params.f90:99-138)
+// and Kumagai_CompMaterSci_39_457_Si (kumagai_params.f90:97-132).
+gb_tersoff_params_t default_tersoff() {
+  gb_tersoff_params_t p{};
+  p.nel = 2;
+  p.Z[0] = 6;
+  p.Z[1] = 14;
+  const double A[3] = {1.3936e3, std::sqrt(1.3936e3 * 1.8308e3), 1.8308e3};
+  const double B[3] = {3.4674e2, std::sqrt(3.4674e2 * 4.7118e2), 4.7118e2};
+  const double xi[3] = {1.0, 0.9776e0, 1.0};
+  const double lam[3] = {3.4879e0, (3.4879e0 + 2.4799e0) / 2, 2.4799e0};
+  const double mu[3] = {2.2119e0, (2.2119e0 + 1.7322e0) / 2, 1.7322e0};
+  const double r1[3] = {1.80, std::sqrt(1.80 * 2.70), 2.70};
+  const double r2[3] = {2.10, std::sqrt(2.10 * 3.00), 3.00};
+  for (int q = 0; q < 3; q++) {
+    p.A[q] = A[q];
+    p.B[q] = B[q];
+    p.xi[q] = xi[q];
+    p.lambda[q] = lam[q];
+    p.mu[q] = mu[q];
+    p.omega[q] = 1.0;
+    p.mubo[q] = 0.0;
+    p.m[q] = 1;
+    p.r1[q] = r1[q];
+    p.r2[q] = r2[q];
+  }
+  const double beta[2] = {1.5724e-7, 1.1000e-6}, n[2] = {7.2751e-1, 7.8734e-1},
+               c[2] = {3.8049e4, 1.0039e5}, d[2] = {4.3484e0, 1.6217e1},
+               h[2] = {-5.7058e-1, -5.9825e-1};
+  for (int q = 0; q < 2; q++) {
+    p.beta[q] = beta[q];
+    p.n[q] = n[q];
+    p.c[q] = c[q];
+    p.d[q] = d[q];
+    p.h[q] = h[q];
+  }
+  return p;
+}
+
+gb_kumagai_params_t default_kumagai() {
+  gb_kumagai_params_t p{};
+  p.nel = 1;
+  p.Z[0] = 14;
+  p.A[0] = 3281.5905;
+  p.B[0] = 121.00047;
+  p.lambda1[0] = 3.2300135;
+  p.lambda2[0] = 1.3457970;
+  p.eta[0] = 1.0000000;
+  p.delta[0] = 0.53298909;
+  p.alpha[0] = 2.3890327;
+  p.beta[0] = 1;
+  p.c1[0] = 0.20173476;
+  p.c2[0] = 730418.72;
+  p.c3[0] = 1000000.0;
+  p.c4[0] = 1.0000000;
+  p.c5[0] = 26.000000;
+  p.h[0] = -0.36500000;
+  p.r1[0] = 2.70;
+  p.r2[0] = 3.30;
+  return p;
+}
+
+int check_tersoff(const gb_tersoff_params_t &p) {
+  if (p.nel < 1 || p.nel > 3) {
+    set_error("Tersoff: nel must be 1..3");
+    return GB_ERROR_ARGUMENT;
+  }
+  const int np = p.nel * (p.nel + 1) / 2;
+  for (int q = 0; q < np; q++) {
+    if (!(p.r2[q] > p.r1[q]) || !(p.r1[q] >= 0)) {
+      set_error("Tersoff: need 0 <= r1 < r2 for every pair");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (p.mubo[q] != 0.0 && p.m[q] < 1) {
+      set_error("Tersoff: m must be >= 1 when mubo != 0");
+      return GB_ERROR_ARGUMENT;
+    }
+  }
+  for (int q = 0; q < p.nel; q++)
+    if (!(p.n[q] != 0.0) || !(p.d[q] != 0.0)) {
+      set_error("Tersoff: n and d must be nonzero");
+      return GB_ERROR_ARGUMENT;
+    }
+  return 0;
+}
+
+int check_kumagai(const gb_kumagai_params_t &p) {
+  if (p.nel != 1) {
+    set_error("Kumagai: exactly one element is supported (KUMAGAI_MAX_EL = 1)");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (!(p.r2[0] > p.r1[0]) || !(p.r1[0] >= 0)) {
+    set_error("Kumagai: need 0 <= r1 < r2");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (p.alpha[0] != 0.0 && p.beta[0] < 1) {
+    set_error("Kumagai: beta must be >= 1");
+    return GB_ERROR_ARGUMENT;
+  }
+  return 0;
+}
+
+int pot_nel(const Potential &pot) {
+  if (pot.kind == kTersoff) return pot.tp.nel;
+  if (pot.kind == kKumagai) return 1;
+  return pot.eam->nel;
+}
+int pot_Z(const Potential &pot, int q) {
+  if (pot.kind == kTersoff) return pot.tp.Z[q];
+  if (pot.kind == kKumagai) return pot.kp.Z[q];
+  return pot.eam->Z[q];
+}
+
+cudaStream_t pot_stream(Potential &pot) {
+  if (!pot.stream) {
+    cudaStreamCreateWithFlags(&pot.stream, cudaStreamNonBlocking);
+    pot.own_stream = true;
+  }
+  if (!pot.ev[0])
+    for (int q = 0; q < 4; q++) cudaEventCreate(&pot.ev[q]);
+  return pot.stream;
+}
+
+// Z -> internal element index (Z2db, default_compute_func.f90:62-66).
+int update_element_map(Potential &pot, const Particles &p) {
+  if (pot.el_for == &p && pot.el_zrev == p.z_rev && pot.el.p) return 0;
+  const int nel = pot_nel(pot);
+  std::vector<int> el(std::max(p.nat, 1), -1);
+  for (int i = 0; i < p.nat; i++)
+    for (int q = 0; q < nel; q++)
+      if (p.hZ[i] == pot_Z(pot, q)) el[i] = q;
+  GB_CHECK(pot.el.ensure(sizeof(int) * el.size()));
+  GB_CUDA(cudaMemcpyAsync(pot.el.p, el.data(), sizeof(int) * el.size(), cudaMemcpyHostToDevice,
+                          pot_stream(pot)));
+  GB_CUDA(cudaStreamSynchronize(pot.stream));
+  pot.el_for = &p;
+  pot.el_zrev = p.z_rev;
+  return 0;
+}
+
+struct Stage {
+  double *caller = nullptr;
+  double *dev = nullptr;
+  size_t n = 0;
+  bool host = false;
+};
+
+int stage_in(double *caller, size_t n, DevBuf &tmp, cudaStream_t s, Stage &st) {
+  st.caller = caller;
+  st.n = n;
+  st.dev = nullptr;
+  st.host = false;
+  if (!caller) return 0;
+  if (is_device_ptr(caller)) {
+    st.dev = caller;
+    return 0;
+  }
+  GB_CHECK(tmp.ensure(sizeof(double) * std::max<size_t>(n, 1)));
+  st.dev = tmp.as<double>();
+  st.host = true;
+  if (n) GB_CUDA(cudaMemcpyAsync(st.dev, caller, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  return 0;
+}
+
+int stage_out(const Stage &st, cudaStream_t s) {
+  if (st.host && st.n)
+    GB_CUDA(cudaMemcpyAsync(st.caller, st.dev, sizeof(double) * st.n, cudaMemcpyDeviceToHost, s));
+  return 0;
+}
+
+__global__ void add_arrays(double *__restrict__ dst, const double *__restrict__ src, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    dst[k] += src[k];
+}
+
+int add_into(double *dst, const double *src, size_t n, cudaStream_t s) {
+  if (!n) return 0;
+  const int T = 256;
+  const size_t blocks = std::min<size_t>((n + T - 1) / T, 65535);
+  add_arrays<<<(unsigned)blocks, T, 0, s>>>(dst, src, n);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot, double *f,
+                      double *wpot, const int *mask, double *epa, double *epb, double *fpb,
+                      double *wpa, double *wpb) {
+  if (!epot || !f || !wpot) {
+    set_error("energy_and_forces: epot, f and wpot are required");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (pot.kind == kEAM && (epb || fpb || wpb)) {
+    set_error("Per-bond properties are not supported by TabulatedAlloyEAM.");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (pot.kind == kEAM && pot.precision != GB_PRECISION_FP64) {
+    set_error("TabulatedAlloyEAM has only the FP64 form.");
+    return GB_ERROR_ARGUMENT;
+  }
+  cudaStream_t s = pot_stream(pot);
+  if (p.stream && p.stream != s) {
+    GB_CUDA(cudaEventRecord(pot.ev[3], p.stream));
+    GB_CUDA(cudaStreamWaitEvent(s, pot.ev[3], 0));
+  }
+  GB_CUDA(cudaEventRecord(pot.ev[0], s));
+  GB_CHECK(update_element_map(pot, p));
+  nl.stream = s;
+  GB_CHECK(neighbors_update(nl, p, s));
+  GB_CUDA(cudaEventRecord(pot.ev[1], s));
+
+  const int nat = p.nat;
+  const size_t nb = (size_t)nl.nentries;
+  Stage sf, sepa, swpa, sepb, sfpb, swpb;
+  GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, s, sf));
+  GB_CHECK(stage_in(epa, nat, pot.out_epa, s, sepa));
+  GB_CHECK(stage_in(wpa, 9 * (size_t)nat, pot.out_wpa, s, swpa));
+  GB_CHECK(stage_in(epb, nb, pot.out_epb, s, sepb));
+  GB_CHECK(stage_in(fpb, 3 * nb, pot.out_fpb, s, sfpb));
+  GB_CHECK(stage_in(wpb, 9 * nb, pot.out_wpb, s, swpb));
+  Outputs o;
+  o.f = sf.dev;
+  o.epot_per_at = sepa.dev;
+  o.wpot_per_at = swpa.dev;
+  o.epot_per_bond = sepb.dev;
+  o.f_per_bond = sfpb.dev;
+  o.wpot_per_bond = swpb.dev;
+  if (mask) {
+    if (is_device_ptr(mask)) {
+      o.mask = mask;
+    } else {
+      GB_CHECK(pot.mask_d.ensure(sizeof(int) * std::max(nat, 1)));
+      if (nat)
+        GB_CUDA(cudaMemcpyAsync(pot.mask_d.p, mask, sizeof(int) * nat, cudaMemcpyHostToDevice, s));
+      o.mask = pot.mask_d.as<int>();
+    }
+  }
+  GB_CHECK(pot.red.ensure(sizeof(double) * 16));
+  o.red = pot.red.as<double>();
+  o.status = reinterpret_cast<int *>(o.red + 12);
+  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 2, s));
+
+  const bool want_wat = wpa != nullptr || wpb != nullptr;
+  const bool want_pb = epb || fpb || wpb;
+  if (pot.kind == kEAM) {
+    GB_CHECK(eam_compute(pot, p, nl, o, want_wat));
+  } else {
+    GB_CHECK(bop_compute(pot, p, nl, o, want_wat, want_pb));
+    if (epb) GB_CHECK(add_into(sepb.dev, pot.bond_e.as<double>(), nb, s));
+    if (fpb) GB_CHECK(add_into(sfpb.dev, pot.bond_fr.as<double>(), 3 * nb, s));
+    if (wpb) GB_CHECK(add_into(swpb.dev, pot.bond_w.as<double>(), 9 * nb, s));
+  }
+  GB_CUDA(cudaEventRecord(pot.ev[2], s));
+  GB_CHECK(stage_out(sf, s));
+  GB_CHECK(stage_out(sepa, s));
+  GB_CHECK(stage_out(swpa, s));
+  GB_CHECK(stage_out(sepb, s));
+  GB_CHECK(stage_out(sfpb, s));
+  GB_CHECK(stage_out(swpb, s));
+  GB_CHECK(pot.hred.ensure(sizeof(double) * 16));
+  double *hr = pot.hred.as<double>();
+  GB_CUDA(cudaMemcpyAsync(hr, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaEventRecord(pot.ev[3], s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  GB_CUDA(cudaGetLastError());
+  float ms[3];
+  cudaEventElapsedTime(&ms[0], pot.ev[0], pot.ev[1]);
+  cudaEventElapsedTime(&ms[1], pot.ev[1], pot.ev[2]);
+  cudaEventElapsedTime(&ms[2], pot.ev[0], pot.ev[3]);
+  for (int q = 0; q < 3; q++) pot.timing[q] = ms[q];
+  const int st = reinterpret_cast<const int *>(hr + 12)[0];
+  pot.last_status = st;
+  if (st & 1) {
+    set_error("Spline argument outside of the defined interval (EAM density table).");
+    return GB_ERROR_DOMAIN;
+  }
+  if (st & 2) {
+    set_error("Internal error: bond-order tile plan mismatch.");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  // epot is set; wpot accumulated (gen_factory.py:283, potential.c:468-479).
+  if (is_device_ptr(epot)) {
+    GB_CUDA(cudaMemcpy(epot, hr, sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    *epot = hr[0];
+  }
+  if (is_device_ptr(wpot)) {
+    double w[9];
+    GB_CUDA(cudaMemcpy(w, wpot, sizeof(w), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < 9; q++) w[q] += hr[1 + q];
+    GB_CUDA(cudaMemcpy(wpot, w, sizeof(w), cudaMemcpyHostToDevice));
+  } else {
+    for (int q = 0; q < 9; q++) wpot[q] += hr[1 + q];
+  }
+  return 0;
+}
+
+int bind_to(Potential &pot, Particles &p, Neighbors &nl) {
+  // Elements present in the particles (p%nel / el2Z).
+  std::vector<int> zs(p.hZ.begin(), p.hZ.end());
+  std::sort(zs.begin(), zs.end());
+  zs.erase(std::unique(zs.begin(), zs.end()), zs.end());
+  const int nel = pot_nel(pot);
+  auto dbidx = [&](int Z) {
+    for (int q = 0; q < nel; q++)
+      if (pot_Z(pot, q) == Z) return q;
+    return -1;
+  };
+  if (pot.kind == kEAM) {
+    // tabulated_alloy_eam_bind_to (:297-350): the cutoff for every pair.
+    if (!zs.empty() && pot.eam->cutoff > nl.interaction_range) {
+      nl.interaction_range = pot.eam->cutoff;
+      nl.valid = false;
+    }
+  } else {
+    // default_bind_to_func.f90:123-144: cut_in_h of each present pair.
+    for (int zi : zs)
+      for (int zj : zs) {
+        const int ii = dbidx(zi), jj = dbidx(zj);
+        if (ii < 0 || jj < 0) continue;
+        const int t = pair_index(ii, jj, nel);
+        const double c = pot.kind == kTersoff ? pot.tp.r2[t] : pot.kp.r2[t];
+        if (c > nl.interaction_range) {
+          nl.interaction_range = c;
+          nl.valid = false;
+        }
+      }
+  }
+  pot.el_for = nullptr;
+  return update_element_map(pot, p);
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" {
+
+int gb_tersoff_new(gb_potential_t **h, const gb_tersoff_params_t *params) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_tersoff_params_t p = params ? *params : default_tersoff();
+  GB_CHECK(check_tersoff(p));
+  *h = new gb_potential;
+  (*h)->pot.kind = kTersoff;
+  (*h)->pot.tp = p;
+  return 0;
+}
+
+int gb_kumagai_new(gb_potential_t **h, const gb_kumagai_params_t *params) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_kumagai_params_t p = params ? *params : default_kumagai();
+  GB_CHECK(check_kumagai(p));
+  *h = new gb_potential;
+  (*h)->pot.kind = kKumagai;
+  (*h)->pot.kp = p;
+  return 0;
+}
+
+int gb_tabulated_alloy_eam_new(gb_potential_t **h, const char *fn) {
+  clear_error();
+  if (!h || !fn) return GB_ERROR_ARGUMENT;
+  std::unique_ptr<EamTables> t(new EamTables);
+  GB_CHECK(eam_read_setfl(fn, *t));
+  GB_CHECK(eam_upload(*t));
+  *h = new gb_potential;
+  (*h)->pot.kind = kEAM;
+  (*h)->pot.eam = std::move(t);
+  return 0;
+}
+
+void gb_potential_free(gb_potential_t *h) {
+  if (!h) return;
+  Potential &pot = h->pot;
+  for (int q = 0; q < 4; q++)
+    if (pot.ev[q]) cudaEventDestroy(pot.ev[q]);
+  if (pot.own_stream && pot.stream) cudaStreamDestroy(pot.stream);
+  delete h;
+}
+
+int gb_potential_set_precision(gb_potential_t *h, int precision) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  if (precision != GB_PRECISION_FP64 && precision != GB_PRECISION_MIXED) {
+    set_error("precision must be GB_PRECISION_FP64 or GB_PRECISION_MIXED");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (h->pot.kind == kEAM && precision != GB_PRECISION_FP64) {
+    set_error("TabulatedAlloyEAM has only the FP64 form.");
+    return GB_ERROR_ARGUMENT;
+  }
+  h->pot.precision = precision;
+  return 0;
+}
+
+int gb_potential_set_stream(gb_potential_t *h, void *stream) {
+  if (!h) return GB_ERROR_ARGUMENT;
+  Potential &pot = h->pot;
+  if (pot.own_stream && pot.stream) cudaStreamDestroy(pot.stream);
+  pot.own_stream = false;
+  pot.stream = (cudaStream_t)stream;
+  if (!stream) pot_stream(pot);
+  return 0;
+}
+
+double gb_potential_get_cutoff(const gb_potential_t *h) {
+  if (!h) return -1.0;
+  const Potential &pot = h->pot;
+  if (pot.kind == kEAM) return pot.eam->cutoff;
+  double c = 0.0;
+  const int np = pot_nel(pot) * (pot_nel(pot) + 1) / 2;
+  for (int q = 0; q < np; q++)
+    c = std::max(c, pot.kind == kTersoff ? pot.tp.r2[q] : pot.kp.r2[q]);
+  return c;
+}
+
+int gb_potential_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl, int *ierror) {
+  clear_error();
+  int rc = (h && p && nl) ? bind_to(h->pot, p->p, nl->nl) : GB_ERROR_ARGUMENT;
+  if (ierror) *ierror = rc;
+  return rc;
+}
+
+int gb_potential_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                   const double *q, double *epot, double *f, double *wpot,
+                                   const int *mask, double *epa, double *epb, double *fpb,
+                                   double *wpa, double *wpb, int *ierror) {
+  (void)q;
+  clear_error();
+  int rc = (h && p && nl)
+               ? energy_and_forces(h->pot, p->p, nl->nl, epot, f, wpot, mask, epa, epb, fpb, wpa,
+                                   wpb)
+               : GB_ERROR_ARGUMENT;
+  if (ierror) *ierror = rc;
+  return rc;
+}
+
+int gb_tersoff_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl, int *ierror) {
+  return gb_potential_bind_to(h, p, nl, ierror);
+}
+int gb_tersoff_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                 const double *q, double *epot, double *f, double *wpot,
+                                 const int *mask, double *epa, double *epb, double *fpb,
+                                 double *wpa, double *wpb, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
+                                        ierror);
+}
+int gb_kumagai_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl, int *ierror) {
+  return gb_potential_bind_to(h, p, nl, ierror);
+}
+int gb_kumagai_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                 const double *q, double *epot, double *f, double *wpot,
+                                 const int *mask, double *epa, double *epb, double *fpb,
+                                 double *wpa, double *wpb, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
+                                        ierror);
+}
+int gb_tabulated_alloy_eam_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                   int *ierror) {
+  return gb_potential_bind_to(h, p, nl, ierror);
+}
+int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *h, gb_particles_t *p,
+                                             gb_neighbors_t *nl, const double *q, double *epot,
+                                             double *f, double *wpot, const int *mask,
+                                             double *epa, double *wpa, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, nullptr, nullptr,
+                                        wpa, nullptr, ierror);
+}
+
+int gb_tabulated_alloy_eam_table(const gb_potential_t *h, int which, int idx, double *x0dx,
+                                 double *coef) {
+  clear_error();
+  if (!h || h->pot.kind != kEAM) return GB_ERROR_ARGUMENT;
+  const EamTables &t = *h->pot.eam;
+  const SplineHost *s = nullptr;
+  if (which == 0 && idx >= 0 && idx < t.nel) s = &t.F[idx];
+  if (which == 1 && idx >= 0 && idx < t.nel) s = &t.rho[idx];
+  if (which == 2 && idx >= 0 && idx < t.nel * t.nel) s = &t.phi[idx];
+  if (!s) return GB_ERROR_ARGUMENT;
+  if (x0dx) {
+    x0dx[0] = s->x0;
+    x0dx[1] = s->dx;
+    x0dx[2] = s->cut;
+  }
+  if (coef) {
+    const std::vector<double> *arr[8] = {&s->y, &s->d2y, &s->c1, &s->c2,
+                                         &s->c3, &s->d1, &s->d2, &s->d3};
+    for (int c = 0; c < 8; c++)
+      for (int k = 0; k < s->n; k++)
+        coef[(size_t)c * s->n + k] = k < (int)arr[c]->size() ? (*arr[c])[k] : 0.0;
+  }
+  return s->n;
+}
+
+int gb_potential_last_timing(const gb_potential_t *h, double *ms3) {
+  if (!h || !ms3) return GB_ERROR_ARGUMENT;
+  for (int q = 0; q < 3; q++) ms3[q] = h->pot.timing[q];
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,627 @@
+// Tersoff / Kumagai energy, force and virial on GB300 (replaces BOP_KERNEL,
+// src/potentials/bop/bop_kernel.f90:420-1628, non-screened branch).
+//
+// Work decomposition (one launch of bop_tile per call, then one gather):
+//
+//   bop_tile   one CTA per tile of `apt` consecutive atoms; a thread per bond
+//              (directed neighbour entry), strided over the tile's bonds.
+//     phase 1  bond geometry from positions and integer image shifts, with
+//              r^2 evaluated exactly as the neighbour test (FP64, no FMA), the
+//              cutoff regions of pass 1 (:627-680, :997-1058) and trig_off.
+//              Unit vectors, lengths and cutoff values go to shared memory.
+//     phase 2  per bond ij: the k loop over the other bonds of i (:1171-1343)
+//              gives zeta_ij, d zeta/d r_j and, per (ij, ik), d zeta/d r_k,
+//              which is kept in shared memory (no per-triplet global
+//              storage).  Then b_ij, P_ij = d E / d zeta_ij (bo, :1356),
+//              the pair energy (:1366) and the radial force (:1376-1402).
+//     phase 3  per bond ik: G_ik = force that centre i exerts on the end atom
+//              of bond ik = (its own j-role term) - sum_j P_ij d zeta_ij/d r_k.
+//   bop_gather one thread per atom a: F_a = sum_{b in out(a)} (G[rev b] - G[b]),
+//              using the reverse-entry index of the symmetric list.  The self
+//              term -sum G[b] equals the reference's f_i by translation
+//              invariance.  No atomics anywhere: results are bitwise
+//              reproducible run to run.
+//
+// The total virial is -sum_b r_b (x) G_b (equal to sum_ij w_ij of :1404); the
+// per-atom virial (requested) follows the reference exactly: w_ij = r_ij (x)
+// df - P_ij wijb_ij, half to i and half to j (:1510-1518).
+//
+// Precision forms: R = double (drop-in) or R = float (mixed: three-body terms
+// and the bond order in FP32; bond geometry, pair terms VA/VR, cutoff and all
+// accumulation of E, F, W in FP64).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "bop_math.h"
+#include "potential.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int kBopThreads = 128;
+constexpr int kMaxApt = 64;
+
+// Bond meta word: owner local atom (bits 0-7), pair type (8-11), flags
+// (12: in short list, 13: active as ij, 14: usable as k), maskfac (16-17).
+constexpr int kFlagShort = 1 << 12;
+constexpr int kFlagIJ = 1 << 13;
+constexpr int kFlagK = 1 << 14;
+
+struct BopArgs {
+  int nat;
+  int apt;
+  const Pos4 *pos;
+  const int *el;
+  const int *seed;
+  const int *nbr;
+  const int *shift;
+  const int *mask;
+  double A[3][3];
+  double *G;        // 3 per bond
+  double *ebond;    // 1 per bond
+  double *wbond;    // 9 per bond (per-atom virial only)
+  double *frbond;   // 3 per bond (f_per_bond only)
+  double *tile_part;  // 10 per tile
+};
+
+template <class R>
+struct SmemLayout {
+  int *aseed, *toff, *el, *meta;
+  double *rn64, *r64, *fc64, *dfc64, *P, *G;
+  R *rn, *rl, *rinv, *fc, *dfc;
+  R *t;  // 3 * ntrip
+  int nbt, ntrip;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+template <class R>
+__host__ __device__ inline size_t bop_smem_bytes(int nbt, int ntrip) {
+  size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + nbt));
+  o += align16(sizeof(double) * (size_t)nbt * 10);
+  o += align16(sizeof(R) * (size_t)nbt * 7);
+  o += align16(sizeof(R) * (size_t)ntrip * 3);
+  return o + 64;
+}
+
+template <class R>
+__device__ inline SmemLayout<R> carve(unsigned char *sm, int nbt, int ntrip) {
+  SmemLayout<R> L;
+  L.nbt = nbt;
+  L.ntrip = ntrip;
+  int *ip = reinterpret_cast<int *>(sm);
+  L.aseed = ip;
+  L.toff = ip + kMaxApt + 1;
+  L.el = ip + 2 * kMaxApt + 2;
+  L.meta = ip + 3 * kMaxApt + 2;
+  size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + nbt));
+  double *dp = reinterpret_cast<double *>(sm + o);
+  L.rn64 = dp;
+  L.r64 = dp + 3 * nbt;
+  L.fc64 = dp + 4 * nbt;
+  L.dfc64 = dp + 5 * nbt;
+  L.P = dp + 6 * nbt;
+  L.G = dp + 7 * nbt;
+  o += align16(sizeof(double) * (size_t)nbt * 10);
+  R *rp = reinterpret_cast<R *>(sm + o);
+  L.rn = rp;
+  L.rl = rp + 3 * nbt;
+  L.rinv = rp + 4 * nbt;
+  L.fc = rp + 5 * nbt;
+  L.dfc = rp + 6 * nbt;
+  o += align16(sizeof(R) * (size_t)nbt * 7);
+  L.t = reinterpret_cast<R *>(sm + o);
+  return L;
+}
+
+// Deterministic block sum of NC doubles per thread into out[0..NC).
+template <int NC>
+__device__ inline void block_sum(double (&v)[NC], double *out, double *scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int nw = kBopThreads / 32;
+#pragma unroll
+  for (int c = 0; c < NC; c++) {
+    double x = v[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) scratch[wid * NC + c] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    double s = 0.0;
+    for (int w = 0; w < nw; w++) s += scratch[w * NC + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+template <class Pot, class R, bool kWat, bool kPB>
+__global__ void __launch_bounds__(kBopThreads)
+    bop_tile(const BopArgs a, const Pot pot, int max_nbt, int max_ntrip, int *status) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ double red_scratch[(kBopThreads / 32) * 9];
+  const int tid = threadIdx.x;
+  const int a0 = blockIdx.x * a.apt;
+  const int a1 = min(a0 + a.apt, a.nat);
+  const int na = a1 - a0;
+  const int b0 = a.seed[a0];
+  const int nbt = a.seed[a1] - b0;
+
+  // Tile bookkeeping: local atom seeds, triplet offsets, owners.
+  int ntrip = 0;
+  {
+    int *aseed = reinterpret_cast<int *>(sm);
+    int *toff = aseed + kMaxApt + 1;
+    int *el = aseed + 2 * kMaxApt + 2;
+    for (int q = tid; q <= na; q += kBopThreads) aseed[q] = a.seed[a0 + q] - b0;
+    for (int q = tid; q < na; q += kBopThreads) el[q] = a.el[a0 + q];
+    __syncthreads();
+    if (tid == 0) {
+      int s = 0;
+      for (int q = 0; q < na; q++) {
+        toff[q] = s;
+        const int z = aseed[q + 1] - aseed[q];
+        s += z * z;
+      }
+      toff[na] = s;
+    }
+    __syncthreads();
+    ntrip = toff[na];
+  }
+  if (nbt > max_nbt || ntrip > max_ntrip) {
+    // Plan mismatch: report and leave this tile's outputs untouched.
+    if (tid == 0) atomicOr(status, 2);
+    return;
+  }
+  SmemLayout<R> L = carve<R>(sm, nbt, ntrip);
+  for (int q = tid; q < na; q += kBopThreads)
+    for (int lb = L.aseed[q]; lb < L.aseed[q + 1]; lb++) L.meta[lb] = q;
+  __syncthreads();
+
+  const int nel = pot.nel();
+
+  // ---- Phase 1: bond geometry (pass 1, bop_kernel.f90:562-1068). ----
+  for (int lb = tid; lb < nbt; lb += kBopThreads) {
+    const int ai = L.meta[lb];
+    const int i = a0 + ai;
+    const int b = b0 + lb;
+    const int j = a.nbr[b];
+    const int eli = L.el[ai];
+    const int elj = a.el[j];
+    int meta = ai;
+    double fc = 0.0, dfc = 0.0, r = 1.0;
+    double rn[3] = {0.0, 0.0, 0.0};
+    if (eli >= 0 && elj >= 0) {
+      const Pos4 pi = a.pos[i], pj = a.pos[j];
+      int s0, s1, s2;
+      unpack_shift(a.shift[b], s0, s1, s2);
+      // rij = r_j - r_i - matmul(cell, dc) (:593), reference order, no FMA.
+      double rij[3] = {__dsub_rn(pj.x, pi.x), __dsub_rn(pj.y, pi.y), __dsub_rn(pj.z, pi.z)};
+      if (s0 | s1 | s2) {
+        const double sx = s0, sy = s1, sz = s2;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          double as = __dmul_rn(a.A[c][0], sx);
+          as = __dadd_rn(as, __dmul_rn(a.A[c][1], sy));
+          as = __dadd_rn(as, __dmul_rn(a.A[c][2], sz));
+          rij[c] = __dsub_rn(rij[c], as);
+        }
+      }
+      double r2 = __dmul_rn(rij[0], rij[0]);
+      r2 = __dadd_rn(r2, __dmul_rn(rij[1], rij[1]));
+      r2 = __dadd_rn(r2, __dmul_rn(rij[2], rij[2]));
+      const int t = pair_index(eli, elj, nel);
+      meta |= t << 8;
+      bool in_short = false;
+      if (r2 < pot.r1sq(t)) {
+        fc = 1.0;
+        dfc = 0.0;
+        in_short = true;
+      } else if (r2 < pot.r2sq(t)) {
+        trig_off(__dsqrt_rn(r2), pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
+        in_short = true;
+      }
+      if (in_short) {
+        r = __dsqrt_rn(r2);
+#pragma unroll
+        for (int c = 0; c < 3; c++) rn[c] = rij[c] / r;
+        int mf = 2;
+        if (a.mask) {
+          const int mi = a.mask[i], mj = a.mask[j];
+          if (mi == 0 && mj == 0)
+            mf = 0;
+          else if (mi == 0 || mj == 0)
+            mf = 1;
+        }
+        meta |= kFlagShort | (mf << 16);
+        if (r < pot.r2(t)) {
+          meta |= kFlagK;
+          if (mf > 0) meta |= kFlagIJ;
+        }
+      }
+    }
+    L.meta[lb] = meta;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      L.rn64[c * nbt + lb] = rn[c];
+      L.rn[c * nbt + lb] = (R)rn[c];
+    }
+    L.r64[lb] = r;
+    L.fc64[lb] = fc;
+    L.dfc64[lb] = dfc;
+    L.rl[lb] = (R)r;
+    L.rinv[lb] = (R)(1.0 / r);
+    L.fc[lb] = (R)fc;
+    L.dfc[lb] = (R)dfc;
+  }
+  __syncthreads();
+
+  // ---- Phase 2: zeta, bond order, pair terms (pass 2, :1074-1529). ----
+  double eacc[1] = {0.0};
+  for (int lb = tid; lb < nbt; lb += kBopThreads) {
+    const int b = b0 + lb;
+    const int meta = L.meta[lb];
+    if (!(meta & kFlagIJ)) {
+      L.P[lb] = 0.0;
+      L.G[lb] = 0.0;
+      L.G[nbt + lb] = 0.0;
+      L.G[2 * nbt + lb] = 0.0;
+      a.ebond[b] = 0.0;
+      if (kPB) {
+        a.frbond[3 * (size_t)b] = 0.0;
+        a.frbond[3 * (size_t)b + 1] = 0.0;
+        a.frbond[3 * (size_t)b + 2] = 0.0;
+      }
+      if (kWat)
+        for (int c = 0; c < 9; c++) a.wbond[9 * (size_t)b + c] = 0.0;
+      continue;
+    }
+    const int ai = meta & 0xff;
+    const int t = (meta >> 8) & 0xf;
+    const int mf = (meta >> 16) & 3;
+    const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
+    R *trow = L.t + L.toff[ai] + p * z;  // component c at trow[c*ntrip + q]
+    const int eli = L.el[ai];
+    const R rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
+    const R rlij = L.rl[lb], rinvj = L.rinv[lb];
+    R zeta = R(0);
+    R dbj[3] = {R(0), R(0), R(0)};
+    R wk[9];
+    if (kWat)
+#pragma unroll
+      for (int c = 0; c < 9; c++) wk[c] = R(0);
+    for (int q = 0; q < z; q++) {
+      const int lk = s + q;
+      if (lk == lb) continue;
+      const int mk = L.meta[lk];
+      if (!(mk & kFlagK)) {
+        trow[q] = R(0);
+        trow[ntrip + q] = R(0);
+        trow[2 * ntrip + q] = R(0);
+        continue;
+      }
+      const int ikpot = (mk >> 8) & 0xf;
+      const R rnik[3] = {L.rn[lk], L.rn[nbt + lk], L.rn[2 * nbt + lk]};
+      const R rlik = L.rl[lk], rinvk = L.rinv[lk], fcik = L.fc[lk], dfcik = L.dfc[lk];
+      R hv, dh;
+      pot.template h<R>(ikpot, rlij - rlik, hv, dh);
+      const R cs = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
+      R gv, dg;
+      pot.template g<R>(eli, ikpot, cs, gv, dg);
+      const R dzfac = fcik * dg * hv;
+      zeta += fcik * gv * hv;
+      const R dzdrij = gv * fcik * dh;
+      const R dzdrik = gv * (dfcik * hv - fcik * dh);
+      R dk[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        // d cos / d r_j = (rn_ik - cos rn_ij)/r_ij ; d cos / d r_k = (rn_ij - cos rn_ik)/r_ik
+        const R dcj = (rnik[c] - cs * rnij[c]) * rinvj;
+        const R dck = (rnij[c] - cs * rnik[c]) * rinvk;
+        dbj[c] += dzdrij * rnij[c] + dzfac * dcj;
+        dk[c] = dzdrik * rnik[c] + dzfac * dck;
+        trow[c * ntrip + q] = dk[c];
+      }
+      if (kWat) {
+#pragma unroll
+        for (int c1 = 0; c1 < 3; c1++)
+#pragma unroll
+          for (int c2 = 0; c2 < 3; c2++) wk[3 * c1 + c2] += rnik[c1] * rlik * dk[c2];
+      }
+    }
+    // Pair terms in FP64 (tersoff_func.f90:32-78), scaled by maskfac/2.
+    const double r = L.r64[lb];
+    double VA, dVA, VR, dVR;
+    pot.VA(t, r, VA, dVA);
+    pot.VR(t, r, VR, dVR);
+    const double hm = 0.5 * mf;
+    VA *= hm;
+    dVA *= hm;
+    VR *= hm;
+    dVR *= hm;
+    const double fcij = L.fc64[lb], dfcij = L.dfc64[lb];
+    double bij, P;
+    {
+      R bR, PR;
+      pot.template bo<R>(eli, t, zeta, (R)fcij, (R)VA, bR, PR);
+      bij = bR;
+      P = PR;
+    }
+    const double e_b = 0.5 * fcij * (VR + bij * VA);
+    const double dff = 0.5 * (dVR * fcij + bij * dVA * fcij + VR * dfcij + bij * VA * dfcij);
+    const double rn64[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
+    double dfr[3], Gp[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      dfr[c] = dff * rn64[c];
+      Gp[c] = -dfr[c] - P * (double)dbj[c];
+    }
+    L.P[lb] = P;
+    L.G[lb] = Gp[0];
+    L.G[nbt + lb] = Gp[1];
+    L.G[2 * nbt + lb] = Gp[2];
+    a.ebond[b] = e_b;
+    eacc[0] += e_b;
+    if (kPB) {
+      a.frbond[3 * (size_t)b] = dfr[0];
+      a.frbond[3 * (size_t)b + 1] = dfr[1];
+      a.frbond[3 * (size_t)b + 2] = dfr[2];
+    }
+    if (kWat) {
+      // w_ij = r_ij (x) df - P wijb, wijb = -r_ij (x) dbidj - sum_k r_ik (x) dbidk
+      const double rij[3] = {r * rn64[0], r * rn64[1], r * rn64[2]};
+#pragma unroll
+      for (int c1 = 0; c1 < 3; c1++)
+#pragma unroll
+        for (int c2 = 0; c2 < 3; c2++) {
+          const double w = rij[c1] * dfr[c2] + P * (rij[c1] * (double)dbj[c2]) +
+                           P * (double)wk[3 * c1 + c2];
+          a.wbond[9 * (size_t)b + c1 + 3 * c2] = w;  // Fortran (c1, c2)
+        }
+    }
+  }
+  __syncthreads();
+
+  // ---- Phase 3: forces on the end atoms (k-role), total virial. ----
+  double wacc[9];
+#pragma unroll
+  for (int c = 0; c < 9; c++) wacc[c] = 0.0;
+  for (int lb = tid; lb < nbt; lb += kBopThreads) {
+    const int b = b0 + lb;
+    const int meta = L.meta[lb];
+    double G[3] = {L.G[lb], L.G[nbt + lb], L.G[2 * nbt + lb]};
+    if (meta & kFlagK) {
+      const int ai = meta & 0xff;
+      const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, q = lb - s;
+      const R *tcol = L.t + L.toff[ai] + q;
+      for (int p = 0; p < z; p++) {
+        const int lp = s + p;
+        if (lp == lb) continue;
+        if (!(L.meta[lp] & kFlagIJ)) continue;
+        const double P = L.P[lp];
+        const R *tv = tcol + p * z;
+#pragma unroll
+        for (int c = 0; c < 3; c++) G[c] -= P * (double)tv[c * ntrip];
+      }
+      const double r = L.r64[lb];
+      const double rb[3] = {r * L.rn64[lb], r * L.rn64[nbt + lb], r * L.rn64[2 * nbt + lb]};
+#pragma unroll
+      for (int c1 = 0; c1 < 3; c1++)
+#pragma unroll
+        for (int c2 = 0; c2 < 3; c2++) wacc[c1 + 3 * c2] -= rb[c1] * G[c2];
+    }
+    a.G[3 * (size_t)b] = G[0];
+    a.G[3 * (size_t)b + 1] = G[1];
+    a.G[3 * (size_t)b + 2] = G[2];
+  }
+  double *part = a.tile_part + 10 * (size_t)blockIdx.x;
+  block_sum<1>(eacc, part, red_scratch);
+  block_sum<9>(wacc, part + 1, red_scratch);
+}
+
+// Per-atom gather through the reverse-entry index.
+template <bool kEpa, bool kWat>
+__global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__restrict__ rev,
+                           const double *__restrict__ G, const double *__restrict__ ebond,
+                           const double *__restrict__ wbond, double *__restrict__ f,
+                           double *__restrict__ epa, double *__restrict__ wpa) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  double F[3] = {0.0, 0.0, 0.0};
+  double E = 0.0;
+  double W[9];
+  if (kWat)
+#pragma unroll
+    for (int c = 0; c < 9; c++) W[c] = 0.0;
+  const int s = seed[i], e = seed[i + 1];
+  for (int b = s; b < e; b++) {
+    const int rb = rev[b];
+#pragma unroll
+    for (int c = 0; c < 3; c++) F[c] += G[3 * (size_t)rb + c] - G[3 * (size_t)b + c];
+    if (kEpa) E += ebond[b] + ebond[rb];
+    if (kWat)
+#pragma unroll
+      for (int c = 0; c < 9; c++) W[c] += wbond[9 * (size_t)b + c] + wbond[9 * (size_t)rb + c];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) f[3 * (size_t)i + c] += F[c];
+  if (kEpa) epa[i] += 0.5 * E;
+  if (kWat)
+#pragma unroll
+    for (int c = 0; c < 9; c++) wpa[9 * (size_t)i + c] += 0.5 * W[c];
+}
+
+// Tile plan: per tile bond count and sum of z^2.
+__global__ void bop_plan(int nat, int apt, const int *__restrict__ seed, int *__restrict__ out) {
+  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a0 = tile * apt;
+  if (a0 >= nat) return;
+  const int a1 = min(a0 + apt, nat);
+  int ntrip = 0;
+  for (int q = a0; q < a1; q++) {
+    const int z = seed[q + 1] - seed[q];
+    ntrip += z * z;
+  }
+  atomicMax(&out[0], seed[a1] - seed[a0]);
+  atomicMax(&out[1], ntrip);
+}
+
+__global__ void reduce_partials_kernel(const double *__restrict__ part, int ntiles, int nc,
+                                       double *__restrict__ red) {
+  __shared__ double sh[1024];
+  for (int c = 0; c < nc; c++) {
+    double s = 0.0;
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) s += part[(size_t)t * nc + c];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) red[c] = sh[0];
+    __syncthreads();
+  }
+}
+
+template <class Pot, class R, bool kWat, bool kPB>
+int launch_tile(const BopArgs &args, const Pot &pot, int ntiles, int max_nbt, int max_ntrip,
+                int *status, cudaStream_t s) {
+  const size_t smem = bop_smem_bytes<R>(max_nbt, max_ntrip);
+  auto kern = bop_tile<Pot, R, kWat, kPB>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) {
+      set_error(std::string("bop: shared memory request too large: ") + cudaGetErrorString(e));
+      return GB_ERROR_CAPACITY;
+    }
+  }
+  kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, max_nbt, max_ntrip, status);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <class Pot, class R>
+int dispatch_tile(const BopArgs &args, const Pot &pot, int ntiles, int max_nbt, int max_ntrip,
+                  int *status, bool wat, bool pb, cudaStream_t s) {
+  if (wat && pb) return launch_tile<Pot, R, true, true>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
+  if (wat) return launch_tile<Pot, R, true, false>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
+  if (pb) return launch_tile<Pot, R, false, true>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
+  return launch_tile<Pot, R, false, false>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
+}
+
+}  // namespace
+
+int reduce_partials(const double *part, int ntiles, int nc, double *red, cudaStream_t s) {
+  reduce_partials_kernel<<<1, 1024, 0, s>>>(part, ntiles, nc, red);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static const size_t kSmemBudget = 200 * 1024;
+
+int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
+                bool want_wat, bool want_pb) {
+  cudaStream_t s = pot.stream;
+  const int nat = p.nat;
+  if (nat == 0) {
+    GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
+    return 0;
+  }
+  GB_CHECK(neighbors_build_reverse(nl, p, s));
+  const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  const size_t rsz = mixed ? sizeof(float) : sizeof(double);
+  // Atoms per tile: largest power of two <= kMaxApt whose worst tile fits.
+  const int maxz = std::max(nl.maxz, 1);
+  int apt = kMaxApt;
+  auto fits = [&](int aptc) {
+    const size_t worst = bop_smem_bytes<double>(aptc * maxz, aptc * maxz * maxz);
+    return worst <= kSmemBudget;
+  };
+  while (apt > 1 && !fits(apt)) apt >>= 1;
+  // Keep roughly one bond per thread.
+  while (apt > 1 && (int64_t)apt * std::max(1, (int)(nl.nentries / std::max(nat, 1))) >
+                        2 * kBopThreads)
+    apt >>= 1;
+  if (!fits(apt)) {
+    set_error("Internal neighbor list exhausted: an atom has " + std::to_string(maxz) +
+              " neighbours within the cutoff, more than the bond-order kernel supports.");
+    return GB_ERROR_CAPACITY;
+  }
+  const int ntiles = (nat + apt - 1) / apt;
+  const int64_t nb = std::max<int64_t>(nl.nentries, 1);
+  GB_CHECK(pot.bond_G.ensure(sizeof(double) * 3 * nb));
+  GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
+  if (want_wat) GB_CHECK(pot.bond_w.ensure(sizeof(double) * 9 * nb));
+  if (want_pb) GB_CHECK(pot.bond_fr.ensure(sizeof(double) * 3 * nb));
+  GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * ntiles + 64));
+  // Plan: exact max bonds / triplets per tile.
+  int *plan = reinterpret_cast<int *>(pot.tile_part.as<double>() + 10 * (size_t)ntiles);
+  GB_CUDA(cudaMemsetAsync(plan, 0, sizeof(int) * 4, s));
+  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, nl.seed.as<int>(), plan);
+  GB_CHECK(pot.hred.ensure(64));
+  int *hplan = pot.hred.as<int>();
+  GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  const int max_nbt = hplan[0], max_ntrip = hplan[1];
+  (void)rsz;
+
+  BopArgs args;
+  args.nat = nat;
+  args.apt = apt;
+  args.pos = nl.pos4.as<Pos4>();
+  args.el = pot.el.as<int>();
+  args.seed = nl.seed.as<int>();
+  args.nbr = nl.nbr.as<int>();
+  args.shift = nl.shift.as<int>();
+  args.mask = o.mask;
+  std::memcpy(args.A, p.A, sizeof(args.A));
+  args.G = pot.bond_G.as<double>();
+  args.ebond = pot.bond_e.as<double>();
+  args.wbond = want_wat ? pot.bond_w.as<double>() : nullptr;
+  args.frbond = want_pb ? pot.bond_fr.as<double>() : nullptr;
+  args.tile_part = pot.tile_part.as<double>();
+  int *status = o.status;
+  int rc;
+  if (pot.kind == kTersoff) {
+    TersoffPot tp{make_tersoff_dev(pot.tp)};
+    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, ntiles, max_nbt, max_ntrip, status,
+                                                  want_wat, want_pb, s)
+               : dispatch_tile<TersoffPot, double>(args, tp, ntiles, max_nbt, max_ntrip,
+                                                   status, want_wat, want_pb, s);
+  } else {
+    KumagaiPot kp{make_kumagai_dev(pot.kp)};
+    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, ntiles, max_nbt, max_ntrip, status,
+                                                  want_wat, want_pb, s)
+               : dispatch_tile<KumagaiPot, double>(args, kp, ntiles, max_nbt, max_ntrip,
+                                                   status, want_wat, want_pb, s);
+  }
+  GB_CHECK(rc);
+  const int T = 128;
+  const bool epa = o.epot_per_at != nullptr;
+  const int gb = (nat + T - 1) / T;
+  if (epa && want_wat)
+    bop_gather<true, true><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
+                                            args.ebond, args.wbond, o.f, o.epot_per_at,
+                                            o.wpot_per_at);
+  else if (epa)
+    bop_gather<true, false><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
+                                             args.ebond, nullptr, o.f, o.epot_per_at, nullptr);
+  else if (want_wat)
+    bop_gather<false, true><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
+                                             args.ebond, args.wbond, o.f, nullptr,
+                                             o.wpot_per_at);
+  else
+    bop_gather<false, false><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
+                                              args.ebond, nullptr, o.f, nullptr, nullptr);
+  GB_CUDA(cudaGetLastError());
+  GB_CHECK(reduce_partials(args.tile_part, ntiles, 10, o.red, s));
+  pot.tile_atoms = apt;
+  return 0;
+}
+
+}  // namespace gb

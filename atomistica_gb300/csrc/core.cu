@@ -1,0 +1,915 @@
+// Particles, neighbour list and shared utilities of libatomistica_gb300.
+//
+// Neighbour build (replaces python_neighbors.f90:430-959):
+//   K1  nl_assign_cells   per atom: FP64 cell coordinate floor(rec . r) with the
+//                         reference operation order, pbc wrap / clamp, padded
+//                         Pos4 copy of the position, cell histogram.
+//   K1b exclusive scan    cell offsets.
+//   K1c nl_scatter        atoms into their cell slots (atomic slot claim).
+//   K1d nl_sort_cells     per-cell sort by atom id, so that every cell lists its
+//                         atoms in increasing id as the reference's linked
+//                         list does (binning_update, :904-959).
+//   K2  nl_pairs<count>   per atom (cell-sorted thread order): stencil loop in
+//                         the reference order, FP64 test |r_i - r_j + A s|^2 <
+//                         cutoff^2 evaluated without FMA contraction in the
+//                         reference's order (:708-711) -> per-atom counts.
+//   K2b exclusive scan    CSR offsets.
+//   K2c nl_pairs<fill>    same loop, writes j and the packed image shift.
+// The resulting per-atom entry order equals the reference's (stencil offset
+// x-major/z-minor, then atom id), so pair sets and per-bond indices match.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "internal.h"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// Error state.
+// ---------------------------------------------------------------------------
+static thread_local std::string g_error;
+void set_error(const std::string &msg) { g_error = msg; }
+void clear_error() { g_error.clear(); }
+
+int DevBuf::ensure(size_t n) {
+  if (n <= bytes && p) return 0;
+  size_t nb = std::max<size_t>(n, 256);
+  nb = std::max(nb, bytes + bytes / 2);
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, nb);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc(") + std::to_string(nb) + ") failed: " +
+              cudaGetErrorString(e));
+    return GB_ERROR_CUDA;
+  }
+  if (p) cudaFree(p);
+  p = q;
+  bytes = nb;
+  return 0;
+}
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+int HostBuf::ensure(size_t n) {
+  if (n <= bytes && p) return 0;
+  size_t nb = std::max<size_t>(n, 256);
+  nb = std::max(nb, bytes + bytes / 2);
+  void *q = nullptr;
+  cudaError_t e = cudaMallocHost(&q, nb);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMallocHost failed: ") + cudaGetErrorString(e));
+    return GB_ERROR_CUDA;
+  }
+  if (p) cudaFreeHost(p);
+  p = q;
+  bytes = nb;
+  return 0;
+}
+void HostBuf::release() {
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+bool is_device_ptr(const void *ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+Cell make_cell(const Particles &p) {
+  Cell c;
+  std::memcpy(c.A, p.A, sizeof(c.A));
+  for (int k = 0; k < 3; k++) c.pbc[k] = p.pbc[k];
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of int32: block-local scans, recursive scan of block sums.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanPerThread = 8;
+constexpr int kScanTile = kScanThreads * kScanPerThread;
+
+__global__ void scan_tiles(const int *__restrict__ in, int *__restrict__ out, int n,
+                           int *__restrict__ tile_sums) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
+  int v[kScanPerThread];
+  int s = 0;
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; q++) {
+    int idx = base + q;
+    v[q] = idx < n ? in[idx] : 0;
+    s += v[q];
+  }
+  // Warp-inclusive scan of per-thread sums.
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < kScanThreads / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < kScanThreads / 32) warp_tot[lane] = w;
+  }
+  __syncthreads();
+  int run = incl - s + (wid > 0 ? warp_tot[wid - 1] : 0);
+#pragma unroll
+  for (int q = 0; q < kScanPerThread; q++) {
+    int idx = base + q;
+    if (idx < n) out[idx] = run;
+    run += v[q];
+  }
+  if (threadIdx.x == kScanThreads - 1) tile_sums[blockIdx.x] = run;
+}
+
+__global__ void scan_add(int *__restrict__ out, int n, const int *__restrict__ tile_offs) {
+  const int idx = blockIdx.x * kScanTile + threadIdx.x;
+  const int add = tile_offs[blockIdx.x];
+  for (int q = 0; q < kScanPerThread; q++) {
+    int k = idx + q * kScanThreads;
+    if (k < n && k < (blockIdx.x + 1) * kScanTile) out[k] += add;
+  }
+}
+
+__global__ void scan_total(const int *__restrict__ in, int *__restrict__ out, int n) {
+  // out[n] = out[n-1] + in[n-1]
+  if (n == 0)
+    out[0] = 0;
+  else
+    out[n] = out[n - 1] + in[n - 1];
+}
+
+int scan_rec(const int *in, int *out, int n, int *tmp, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const int tiles = (n + kScanTile - 1) / kScanTile;
+  int *sums = tmp;
+  int *offs = tmp + tiles + 1;
+  scan_tiles<<<tiles, kScanThreads, 0, s>>>(in, out, n, sums);
+  if (tiles > 1) {
+    scan_rec(sums, offs, tiles, tmp + 2 * (tiles + 1), s);
+    scan_add<<<tiles, kScanThreads, 0, s>>>(out, n, offs);
+  }
+  return 0;
+}
+
+size_t scan_tmp_ints(int n) {
+  size_t t = 0;
+  while (n > 0) {
+    int tiles = (n + kScanTile - 1) / kScanTile;
+    t += 2 * (size_t)(tiles + 1);
+    if (tiles <= 1) break;
+    n = tiles;
+  }
+  return t + 64;
+}
+
+}  // namespace
+
+int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t stream) {
+  GB_CHECK(tmp.ensure(scan_tmp_ints(n) * sizeof(int)));
+  scan_rec(in, out, n, tmp.as<int>(), stream);
+  scan_total<<<1, 1, 0, stream>>>(in, out, n);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side cell inverse (gauss(), f_linearalgebra.f90:505-552).
+// ---------------------------------------------------------------------------
+static int gauss_solve3(const double Ain[3][3], const double b[3], double x[3]) {
+  double A[3][4];
+  for (int j = 0; j < 3; j++) {
+    for (int k = 0; k < 3; k++) A[j][k] = Ain[j][k];
+    A[j][3] = b[j];
+  }
+  int indx[3] = {0, 0, 0};
+  for (int i = 0; i < 3; i++) {
+    int mi = -1;
+    double mv = -1.0;
+    for (int j = 0; j < 3; j++) {
+      if (indx[j]) continue;
+      double v = std::fabs(A[j][i]);
+      if (v > mv) {
+        mv = v;
+        mi = j;
+      }
+    }
+    indx[mi] = i + 1;
+    if (A[mi][i] == 0.0) return -1;
+    double fac[3], row[4];
+    for (int j = 0; j < 3; j++) fac[j] = A[j][i] / A[mi][i];
+    for (int k = 0; k < 4; k++) row[k] = A[mi][k];
+    for (int j = 0; j < 3; j++) {
+      if (indx[j]) continue;
+      for (int k = i; k < 4; k++) A[j][k] = A[j][k] - fac[j] * row[k];
+    }
+  }
+  double Ap[3][4];
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 4; k++) Ap[indx[j] - 1][k] = A[j][k];
+  for (int j = 2; j >= 0; j--) {
+    if (Ap[j][j] == 0.0) return -1;
+    x[j] = Ap[j][3] / Ap[j][j];
+    for (int m = 0; m < j; m++) Ap[m][3] = Ap[m][3] - Ap[m][j] * x[j];
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour build kernels.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct BinParams {
+  double rec[3][3];
+  double A[3][3];
+  int n[3];
+  int pbc[3];
+  int dx, dy, dz;
+  double cutoff_sq;
+};
+
+__device__ __forceinline__ int floor_div(int a, int n) {
+  int q = a / n;
+  if ((a % n != 0) && ((a < 0) != (n < 0))) q--;
+  return q;
+}
+
+// floor(matmul(rec_cell_size, r)) with the reference's summation order and no
+// FMA contraction (python_neighbors.f90:641).
+__device__ __forceinline__ void raw_cell(const BinParams &bp, double x, double y, double z,
+                                         int c[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double s = __dmul_rn(bp.rec[k][0], x);
+    s = __dadd_rn(s, __dmul_rn(bp.rec[k][1], y));
+    s = __dadd_rn(s, __dmul_rn(bp.rec[k][2], z));
+    double f = floor(s);
+    f = fmin(fmax(f, -1.0e9), 1.0e9);
+    c[k] = (int)f;
+  }
+}
+
+__device__ __forceinline__ int pack_wrap(int q0, int q1, int q2) {
+  return pack_shift(q0, q1, q2);
+}
+
+__global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams bp,
+                                Pos4 *__restrict__ pos4, int *__restrict__ atom_cell,
+                                int *__restrict__ atom_wrap, int *__restrict__ cell_count,
+                                int *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+  pos4[i] = Pos4{x, y, z, 0.0};
+  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+    atomicOr(&status[1], 1);  // non-finite position
+    atom_cell[i] = 0;
+    atom_wrap[i] = pack_wrap(0, 0, 0);
+    atomicAdd(&cell_count[0], 1);
+    return;
+  }
+  int c[3], q[3];
+  raw_cell(bp, x, y, z, c);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    q[k] = 0;
+    if (bp.pbc[k]) {
+      q[k] = floor_div(c[k], bp.n[k]);
+      c[k] -= q[k] * bp.n[k];
+    } else {
+      c[k] = min(max(c[k], 0), bp.n[k] - 1);
+    }
+    if (q[k] > kMaxShift || q[k] < -kMaxShift) atomicOr(&status[1], 2);
+  }
+  const int ci = (c[2] * bp.n[1] + c[1]) * bp.n[0] + c[0];
+  atom_cell[i] = ci;
+  atom_wrap[i] = pack_wrap(max(min(q[0], kMaxShift), -kMaxShift),
+                           max(min(q[1], kMaxShift), -kMaxShift),
+                           max(min(q[2], kMaxShift), -kMaxShift));
+  atomicAdd(&cell_count[ci], 1);
+}
+
+__global__ void nl_scatter(int nat, const int *__restrict__ atom_cell,
+                           const int *__restrict__ cell_start, int *__restrict__ cell_fill,
+                           int *__restrict__ cell_atoms) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const int c = atom_cell[i];
+  const int slot = cell_start[c] + atomicAdd(&cell_fill[c], 1);
+  cell_atoms[slot] = i;
+}
+
+// Sort each cell's atoms by id: insertion sort for small cells, a
+// rank-by-count pass (one block per cell) for the rare crowded cell.
+constexpr int kSmallCell = 48;
+
+__global__ void nl_sort_cells(int ncells, const int *__restrict__ cell_start,
+                              int *__restrict__ cell_atoms, int *__restrict__ big_cells,
+                              int *__restrict__ n_big) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int s = cell_start[c], e = cell_start[c + 1];
+  const int m = e - s;
+  if (m <= 1) return;
+  if (m > kSmallCell) {
+    big_cells[atomicAdd(n_big, 1)] = c;
+    return;
+  }
+  int v[kSmallCell];
+  for (int q = 0; q < m; q++) v[q] = cell_atoms[s + q];
+  for (int q = 1; q < m; q++) {
+    int key = v[q];
+    int p = q - 1;
+    while (p >= 0 && v[p] > key) {
+      v[p + 1] = v[p];
+      p--;
+    }
+    v[p + 1] = key;
+  }
+  for (int q = 0; q < m; q++) cell_atoms[s + q] = v[q];
+}
+
+__global__ void nl_sort_big_cells(const int *__restrict__ big_cells, const int *__restrict__ n_big,
+                                  const int *__restrict__ cell_start, const int *__restrict__ src,
+                                  int *__restrict__ dst) {
+  for (int bc = blockIdx.x; bc < *n_big; bc += gridDim.x) {
+    const int c = big_cells[bc];
+    const int s = cell_start[c], e = cell_start[c + 1];
+    for (int q = s + threadIdx.x; q < e; q += blockDim.x) {
+      const int me = src[q];
+      int rank = 0;
+      for (int t = s; t < e; t++) rank += src[t] < me;
+      dst[s + rank] = me;
+    }
+  }
+}
+
+__global__ void nl_copy_big_cells(const int *__restrict__ big_cells, const int *__restrict__ n_big,
+                                  const int *__restrict__ cell_start, const int *__restrict__ src,
+                                  int *__restrict__ dst) {
+  for (int bc = blockIdx.x; bc < *n_big; bc += gridDim.x) {
+    const int c = big_cells[bc];
+    for (int q = cell_start[c] + threadIdx.x; q < cell_start[c + 1]; q += blockDim.x)
+      dst[q] = src[q];
+  }
+}
+
+template <bool kFill>
+__global__ void __launch_bounds__(128)
+    nl_pairs(int nat, BinParams bp, const Pos4 *__restrict__ pos4,
+             const int *__restrict__ atom_cell, const int *__restrict__ atom_wrap,
+             const int *__restrict__ cell_start, const int *__restrict__ cell_atoms,
+             int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
+             int *__restrict__ shift, int *__restrict__ status) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nat) return;
+  const int i = cell_atoms[t];
+  const Pos4 ri = pos4[i];
+  int ci = atom_cell[i];
+  int cell[3];
+  cell[0] = ci % bp.n[0];
+  ci /= bp.n[0];
+  cell[1] = ci % bp.n[1];
+  cell[2] = ci / bp.n[1];
+  int q0, q1, q2;
+  unpack_shift(atom_wrap[i], q0, q1, q2);
+  const int shi[3] = {-q0, -q1, -q2};
+  int cur = kFill ? seed[i] : 0;
+  int cnt = 0;
+  for (int x = -bp.dx; x <= bp.dx; x++) {
+    for (int y = -bp.dy; y <= bp.dy; y++) {
+      for (int z = -bp.dz; z <= bp.dz; z++) {
+        int cc[3] = {cell[0] + x, cell[1] + y, cell[2] + z};
+        int s1[3] = {shi[0], shi[1], shi[2]};
+        bool exists = true;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          if (bp.pbc[k]) {
+            const int q = floor_div(cc[k], bp.n[k]);
+            cc[k] -= q * bp.n[k];
+            s1[k] -= q;
+          } else if (cc[k] < 0 || cc[k] >= bp.n[k]) {
+            exists = false;
+          }
+        }
+        if (!exists) continue;
+        const int c = (cc[2] * bp.n[1] + cc[1]) * bp.n[0] + cc[0];
+        const int js = cell_start[c], je = cell_start[c + 1];
+        for (int jq = js; jq < je; jq++) {
+          const int j = cell_atoms[jq];
+          int w0, w1, w2;
+          unpack_shift(atom_wrap[j], w0, w1, w2);
+          const int s2x = s1[0] + w0, s2y = s1[1] + w1, s2z = s1[2] + w2;
+          if (j == i && s2x == 0 && s2y == 0 && s2z == 0) continue;
+          const Pos4 rj = pos4[j];
+          const double sx = (double)s2x, sy = (double)s2y, sz = (double)s2z;
+          double d[3];
+          const double rij[3] = {__dsub_rn(ri.x, rj.x), __dsub_rn(ri.y, rj.y),
+                                 __dsub_rn(ri.z, rj.z)};
+#pragma unroll
+          for (int a = 0; a < 3; a++) {
+            double as = __dmul_rn(bp.A[a][0], sx);
+            as = __dadd_rn(as, __dmul_rn(bp.A[a][1], sy));
+            as = __dadd_rn(as, __dmul_rn(bp.A[a][2], sz));
+            d[a] = __dadd_rn(rij[a], as);
+          }
+          double d2 = __dmul_rn(d[0], d[0]);
+          d2 = __dadd_rn(d2, __dmul_rn(d[1], d[1]));
+          d2 = __dadd_rn(d2, __dmul_rn(d[2], d[2]));
+          if (d2 < bp.cutoff_sq) {
+            if (kFill) {
+              nbr[cur] = j;
+              shift[cur] = pack_shift(s2x, s2y, s2z);
+              cur++;
+            } else {
+              cnt++;
+              if (s2x > kMaxShift || s2x < -kMaxShift || s2y > kMaxShift ||
+                  s2y < -kMaxShift || s2z > kMaxShift || s2z < -kMaxShift)
+                atomicOr(&status[1], 2);
+            }
+          }
+        }
+      }
+    }
+  }
+  if (!kFill) {
+    counts[i] = cnt;
+    atomicMax(&status[0], cnt);
+  }
+}
+
+// rev[b] = entry (j -> i, -s) of the entry b = (i -> j, s).
+__global__ void nl_reverse(int nat, const int *__restrict__ seed, const int *__restrict__ nbr,
+                           const int *__restrict__ shift, int *__restrict__ rev,
+                           int *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  for (int b = seed[i]; b < seed[i + 1]; b++) {
+    const int j = nbr[b];
+    int s0, s1, s2;
+    unpack_shift(shift[b], s0, s1, s2);
+    const int want = pack_shift(-s0, -s1, -s2);
+    int found = -1;
+    for (int c = seed[j]; c < seed[j + 1]; c++) {
+      if (nbr[c] == i && shift[c] == want) {
+        found = c;
+        break;
+      }
+    }
+    if (found < 0) atomicOr(&status[1], 4);
+    rev[b] = found;
+  }
+}
+
+}  // namespace
+
+// Host-side binning_init (python_neighbors.f90:765-871).
+static void binning_init(Neighbors &nl, const Particles &p, double cutoff) {
+  const double bin_size = cutoff;
+  double box_size[3];
+  for (int x = 0; x < 3; x++) {
+    double s = 0.0;
+    for (int a = 0; a < 3; a++) s = s + p.A[a][x] * p.A[a][x];
+    box_size[x] = std::sqrt(s);
+  }
+  for (int x = 0; x < 3; x++) {
+    double v = box_size[x] / bin_size;
+    int nc = v > 1e6 ? 1000000 : (int)v;
+    nl.n_cells[x] = nc < 3 ? 3 : nc;
+  }
+  double cs[3][3];
+  for (int x = 0; x < 3; x++) {
+    for (int a = 0; a < 3; a++) cs[a][x] = p.A[a][x] / nl.n_cells[x];
+    for (int k = 0; k < 3; k++) nl.rec[x][k] = p.B[x][k] * nl.n_cells[x];
+  }
+  auto cross = [](const double u[3], const double v[3], double w[3]) {
+    w[0] = u[1] * v[2] - u[2] * v[1];
+    w[1] = u[2] * v[0] - u[0] * v[2];
+    w[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  auto dot = [](const double u[3], const double v[3]) {
+    double s = u[0] * v[0];
+    s = s + u[1] * v[1];
+    s = s + u[2] * v[2];
+    return s;
+  };
+  double c1[3], c2[3], c3[3], nx[3], ny[3], nz[3];
+  for (int a = 0; a < 3; a++) {
+    c1[a] = cs[a][0];
+    c2[a] = cs[a][1];
+    c3[a] = cs[a][2];
+  }
+  cross(c2, c3, nx);
+  cross(c3, c1, ny);
+  cross(c1, c2, nz);
+  const double cv = dot(c1, nx);
+  const double dnx = dot(nx, nx), dny = dot(ny, ny), dnz = dot(nz, nz);
+  for (int a = 0; a < 3; a++) {
+    nx[a] = cv * nx[a] / dnx;
+    ny[a] = cv * ny[a] / dny;
+    nz[a] = cv * nz[a] / dnz;
+  }
+  nl.dx = (int)(cutoff / std::sqrt(dot(nx, nx))) + 1;
+  nl.dy = (int)(cutoff / std::sqrt(dot(ny, ny))) + 1;
+  nl.dz = (int)(cutoff / std::sqrt(dot(nz, nz))) + 1;
+}
+
+int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
+  if (!p.cell_set) {
+    set_error("neighbors_update: cell not set");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (p.nat > 0 && !p.r.p) {
+    set_error("neighbors_update: positions not set");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (nl.valid && nl.built_for == &p && nl.built_pos_rev == p.pos_rev &&
+      nl.built_cell_rev == p.cell_rev && nl.built_nat == p.nat && nl.cutoff == nl.interaction_range)
+    return 0;
+  // cutoff = interaction_range + verlet_shell (0 on the Python path, :478)
+  const double cutoff = nl.interaction_range;
+  if (!(cutoff > 0.0)) {
+    set_error("Cutoff needs to be larger than zero.");
+    return GB_ERROR_ARGUMENT;
+  }
+  nl.valid = false;
+  nl.rev_valid = false;
+  const int nat = p.nat;
+  binning_init(nl, p, cutoff);
+  const int ncells = nl.n_cells[0] * nl.n_cells[1] * nl.n_cells[2];
+  if ((long long)nl.n_cells[0] * nl.n_cells[1] * nl.n_cells[2] > (1ll << 28)) {
+    set_error("neighbors_update: too many cells (cell or cutoff out of range)");
+    return GB_ERROR_DOMAIN;
+  }
+  if ((2ll * nl.dx + 1) * (2ll * nl.dy + 1) * (2ll * nl.dz + 1) > 100000000ll) {
+    set_error("neighbors_update: cutoff too large for this cell");
+    return GB_ERROR_DOMAIN;
+  }
+  BinParams bp;
+  std::memcpy(bp.rec, nl.rec, sizeof(bp.rec));
+  std::memcpy(bp.A, p.A, sizeof(bp.A));
+  for (int k = 0; k < 3; k++) {
+    bp.n[k] = nl.n_cells[k];
+    bp.pbc[k] = p.pbc[k];
+  }
+  bp.dx = nl.dx;
+  bp.dy = nl.dy;
+  bp.dz = nl.dz;
+  bp.cutoff_sq = cutoff * cutoff;
+
+  GB_CHECK(nl.pos4.ensure(sizeof(Pos4) * std::max(nat, 1)));
+  GB_CHECK(nl.atom_cell.ensure(sizeof(int) * std::max(nat, 1)));
+  GB_CHECK(nl.atom_wrap.ensure(sizeof(int) * std::max(nat, 1)));
+  GB_CHECK(nl.cell_count.ensure(sizeof(int) * (ncells + 1)));
+  GB_CHECK(nl.cell_start.ensure(sizeof(int) * (ncells + 1)));
+  GB_CHECK(nl.cell_atoms.ensure(sizeof(int) * 2 * std::max(nat, 1)));
+  GB_CHECK(nl.counts.ensure(sizeof(int) * (nat + 1)));
+  GB_CHECK(nl.seed.ensure(sizeof(int) * (nat + 1)));
+  GB_CHECK(nl.stats.ensure(sizeof(int) * 8 + sizeof(int) * (size_t)(ncells + 1)));
+  GB_CHECK(nl.hstats.ensure(sizeof(int) * 8));
+  int *status = nl.stats.as<int>();  // [0] maxz [1] flags [2] n_big
+  int *big_cells = status + 8;
+  GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 8, stream));
+  GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
+  const int T = 256;
+  const int nb = (nat + T - 1) / T;
+  if (nat > 0) {
+    nl_assign_cells<<<nb, T, 0, stream>>>(nat, p.r.as<double>(), bp, nl.pos4.as<Pos4>(),
+                                          nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
+                                          nl.cell_count.as<int>(), status);
+  }
+  GB_CHECK(exclusive_scan_i32(nl.cell_count.as<int>(), nl.cell_start.as<int>(), ncells,
+                              nl.scan_tmp, stream));
+  GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
+  int *cell_atoms = nl.cell_atoms.as<int>();
+  if (nat > 0) {
+    nl_scatter<<<nb, T, 0, stream>>>(nat, nl.atom_cell.as<int>(), nl.cell_start.as<int>(),
+                                     nl.cell_count.as<int>(), cell_atoms);
+    nl_sort_cells<<<(ncells + T - 1) / T, T, 0, stream>>>(ncells, nl.cell_start.as<int>(),
+                                                         cell_atoms, big_cells, &status[2]);
+    // Crowded cells (rare): rank-by-count into the second half, copy back.
+    nl_sort_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
+        big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms, cell_atoms + nat);
+    nl_copy_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
+        big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms + nat, cell_atoms);
+    nl_pairs<false><<<(nat + 127) / 128, 128, 0, stream>>>(
+        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
+        nl.cell_start.as<int>(), cell_atoms, nl.counts.as<int>(), nullptr, nullptr, nullptr,
+        status);
+  }
+  GB_CHECK(exclusive_scan_i32(nl.counts.as<int>(), nl.seed.as<int>(), nat, nl.scan_tmp, stream));
+  // Read back: maxz, flags, n_big, total entries.
+  int *hs = nl.hstats.as<int>();
+  GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
+  GB_CUDA(cudaMemcpyAsync(hs + 4, nl.seed.as<int>() + nat, sizeof(int), cudaMemcpyDeviceToHost,
+                          stream));
+  GB_CUDA(cudaStreamSynchronize(stream));
+  GB_CUDA(cudaGetLastError());
+  if (hs[1] & 1) {
+    set_error("Non-finite particle position.");
+    return GB_ERROR_DOMAIN;
+  }
+  if (hs[1] & 2) {
+    set_error("Particle or image shift outside the supported range (|shift| <= 511 cells).");
+    return GB_ERROR_DOMAIN;
+  }
+  const int64_t total = hs[4];
+  if (total < 0) {
+    set_error("Neighbor list overflow (more than 2^31 entries).");
+    return GB_ERROR_CAPACITY;
+  }
+  GB_CHECK(nl.nbr.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
+  GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
+  if (nat > 0) {
+    nl_pairs<true><<<(nat + 127) / 128, 128, 0, stream>>>(
+        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
+        nl.cell_start.as<int>(), cell_atoms, nullptr, nl.seed.as<int>(), nl.nbr.as<int>(),
+        nl.shift.as<int>(), status);
+  }
+  GB_CUDA(cudaGetLastError());
+  nl.nentries = total;
+  nl.maxz = hs[0];
+  nl.cutoff = cutoff;
+  nl.valid = true;
+  nl.built_for = &p;
+  nl.built_pos_rev = p.pos_rev;
+  nl.built_cell_rev = p.cell_rev;
+  nl.built_nat = nat;
+  return 0;
+}
+
+int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream) {
+  if (nl.rev_valid) return 0;
+  const int nat = p.nat;
+  GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(nl.nentries, 1)));
+  int *status = nl.stats.as<int>();
+  GB_CUDA(cudaMemsetAsync(status + 1, 0, sizeof(int), stream));
+  if (nat > 0)
+    nl_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.seed.as<int>(), nl.nbr.as<int>(),
+                                                     nl.shift.as<int>(), nl.rev.as<int>(),
+                                                     status);
+  int *hs = nl.hstats.as<int>();
+  GB_CUDA(cudaMemcpyAsync(hs + 1, status + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  GB_CUDA(cudaStreamSynchronize(stream));
+  if (hs[1] & 4) {
+    set_error("Internal error: neighbour list is not symmetric.");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  nl.rev_valid = true;
+  return 0;
+}
+
+}  // namespace gb
+
+// ===========================================================================
+// C-ABI: particles and neighbours.
+// ===========================================================================
+using namespace gb;
+
+
+static cudaStream_t particles_stream(Particles &p) {
+  if (!p.stream) {
+    cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking);
+    p.own_stream = true;
+  }
+  return p.stream;
+}
+
+extern "C" {
+
+const char *gb_get_error(void) { return g_error.c_str(); }
+const char *gb_version(void) { return "atomistica_gb300 0.1.0 (sm_103a)"; }
+
+int gb_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int gb_particles_new(gb_particles_t **p) {
+  clear_error();
+  if (!p) return GB_ERROR_ARGUMENT;
+  *p = new gb_particles;
+  return 0;
+}
+
+void gb_particles_free(gb_particles_t *p) {
+  if (!p) return;
+  if (p->p.own_stream && p->p.stream) cudaStreamDestroy(p->p.stream);
+  delete p;
+}
+
+int gb_particles_allocate(gb_particles_t *h, int nat) {
+  clear_error();
+  if (!h || nat < 0) {
+    set_error("particles_allocate: invalid arguments");
+    return GB_ERROR_ARGUMENT;
+  }
+  Particles &p = h->p;
+  GB_CHECK(p.r.ensure(sizeof(double) * 3 * std::max(nat, 1)));
+  GB_CHECK(p.Z.ensure(sizeof(int) * std::max(nat, 1)));
+  p.nat = nat;
+  p.hZ.assign(nat, 0);
+  GB_CUDA(cudaMemsetAsync(p.r.p, 0, sizeof(double) * 3 * std::max(nat, 1), particles_stream(p)));
+  GB_CUDA(cudaMemsetAsync(p.Z.p, 0, sizeof(int) * std::max(nat, 1), particles_stream(p)));
+  GB_CUDA(cudaStreamSynchronize(particles_stream(p)));
+  p.pos_rev++;
+  p.z_rev++;
+  return 0;
+}
+
+int gb_particles_get_nat(const gb_particles_t *h) { return h ? h->p.nat : -1; }
+
+int gb_particles_set_cell(gb_particles_t *h, const double *cell, const int *pbc) {
+  clear_error();
+  if (!h || !cell) return GB_ERROR_ARGUMENT;
+  Particles &p = h->p;
+  double A[3][3];
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 3; k++) A[a][k] = cell[3 * k + a];
+  double B[3][3];
+  for (int c = 0; c < 3; c++) {
+    double e[3] = {0, 0, 0}, x[3];
+    e[c] = 1.0;
+    if (gauss_solve3(A, e, x) != 0) {
+      set_error("Gauss elimination failed (singular cell).");
+      return GB_ERROR_ARGUMENT;
+    }
+    for (int a = 0; a < 3; a++) B[a][c] = x[a];
+  }
+  bool changed = !p.cell_set || std::memcmp(A, p.A, sizeof(A)) != 0;
+  std::memcpy(p.A, A, sizeof(A));
+  std::memcpy(p.B, B, sizeof(B));
+  for (int k = 0; k < 3; k++) {
+    int v = pbc ? (pbc[k] != 0) : 1;
+    if (v != p.pbc[k]) changed = true;
+    p.pbc[k] = v;
+  }
+  p.cell_set = true;
+  if (changed) p.cell_rev++;
+  return 0;
+}
+
+int gb_particles_set_positions(gb_particles_t *h, const double *r) {
+  clear_error();
+  if (!h || (!r && h->p.nat > 0)) return GB_ERROR_ARGUMENT;
+  Particles &p = h->p;
+  if (p.nat == 0) {
+    p.pos_rev++;
+    return 0;
+  }
+  cudaStream_t s = particles_stream(p);
+  const size_t bytes = sizeof(double) * 3 * p.nat;
+  GB_CUDA(cudaMemcpyAsync(p.r.p, r, bytes, cudaMemcpyDefault, s));
+  if (!is_device_ptr(r)) GB_CUDA(cudaStreamSynchronize(s));
+  p.pos_rev++;
+  return 0;
+}
+
+int gb_particles_set_Z(gb_particles_t *h, const int *Z) {
+  clear_error();
+  if (!h || (!Z && h->p.nat > 0)) return GB_ERROR_ARGUMENT;
+  Particles &p = h->p;
+  if (p.nat == 0) return 0;
+  cudaStream_t s = particles_stream(p);
+  GB_CUDA(cudaMemcpyAsync(p.hZ.data(), Z, sizeof(int) * p.nat, cudaMemcpyDefault, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  GB_CUDA(cudaMemcpyAsync(p.Z.p, p.hZ.data(), sizeof(int) * p.nat, cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  p.z_rev++;
+  return 0;
+}
+
+int gb_particles_set_stream(gb_particles_t *h, void *stream) {
+  if (!h) return GB_ERROR_ARGUMENT;
+  Particles &p = h->p;
+  if (p.own_stream && p.stream) cudaStreamDestroy(p.stream);
+  p.own_stream = false;
+  p.stream = (cudaStream_t)stream;
+  if (!stream) particles_stream(p);
+  return 0;
+}
+
+int gb_neighbors_new(gb_neighbors_t **nl, int avgn) {
+  clear_error();
+  if (!nl) return GB_ERROR_ARGUMENT;
+  *nl = new gb_neighbors;
+  (*nl)->nl.avgn = avgn > 0 ? avgn : 100;
+  return 0;
+}
+
+void gb_neighbors_free(gb_neighbors_t *nl) { delete nl; }
+
+int gb_neighbors_request_interaction_range(gb_neighbors_t *h, double cutoff) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  if (cutoff > h->nl.interaction_range) {
+    h->nl.interaction_range = cutoff;
+    h->nl.valid = false;
+  }
+  return 0;
+}
+
+double gb_neighbors_get_interaction_range(const gb_neighbors_t *h) {
+  return h ? h->nl.interaction_range : -1.0;
+}
+
+int gb_neighbors_update(gb_neighbors_t *h, gb_particles_t *p) {
+  clear_error();
+  if (!h || !p) return GB_ERROR_ARGUMENT;
+  cudaStream_t s = h->nl.stream ? h->nl.stream : particles_stream(p->p);
+  if (p->p.stream && p->p.stream != s) GB_CUDA(cudaStreamSynchronize(p->p.stream));
+  return neighbors_update(h->nl, p->p, s);
+}
+
+int64_t gb_neighbors_get_size(const gb_neighbors_t *h) {
+  return (h && h->nl.valid) ? h->nl.nentries : -1;
+}
+
+namespace gb {
+namespace {
+__global__ void nl_export(int nat, const int *__restrict__ seed, const int *__restrict__ nbr,
+                          const int *__restrict__ shift, int64_t *__restrict__ oseed,
+                          int *__restrict__ oj, int *__restrict__ odc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nat) return;
+  if (oseed) oseed[i] = seed[i];
+  if (i == nat) return;
+  for (int b = seed[i]; b < seed[i + 1]; b++) {
+    if (oj) oj[b] = nbr[b];
+    if (odc) {
+      int s0, s1, s2;
+      unpack_shift(shift[b], s0, s1, s2);
+      odc[3 * b] = s0;
+      odc[3 * b + 1] = s1;
+      odc[3 * b + 2] = s2;
+    }
+  }
+}
+}  // namespace
+}  // namespace gb
+
+int gb_neighbors_get(gb_neighbors_t *h, gb_particles_t *ph, int64_t *seed, int *j, int *dc) {
+  clear_error();
+  if (!h || !ph) return GB_ERROR_ARGUMENT;
+  Neighbors &nl = h->nl;
+  Particles &p = ph->p;
+  cudaStream_t s = nl.stream ? nl.stream : particles_stream(p);
+  GB_CHECK(neighbors_update(nl, p, s));
+  const int nat = p.nat;
+  const int64_t n = nl.nentries;
+  DevBuf tmp;
+  const size_t bs = sizeof(int64_t) * (nat + 1), bj = sizeof(int) * n, bd = sizeof(int) * 3 * n;
+  GB_CHECK(tmp.ensure(bs + bj + bd + 64));
+  char *base = tmp.as<char>();
+  int64_t *dseed = (seed && is_device_ptr(seed)) ? seed : (int64_t *)base;
+  int *dj = (j && is_device_ptr(j)) ? j : (int *)(base + bs);
+  int *ddc = (dc && is_device_ptr(dc)) ? dc : (int *)(base + bs + bj);
+  nl_export<<<(nat + 1 + 127) / 128, 128, 0, s>>>(nat, nl.seed.as<int>(), nl.nbr.as<int>(),
+                                                 nl.shift.as<int>(), seed ? dseed : nullptr,
+                                                 j ? dj : nullptr, dc ? ddc : nullptr);
+  GB_CUDA(cudaGetLastError());
+  if (seed && dseed != seed) GB_CUDA(cudaMemcpyAsync(seed, dseed, bs, cudaMemcpyDeviceToHost, s));
+  if (j && dj != j && n) GB_CUDA(cudaMemcpyAsync(j, dj, bj, cudaMemcpyDeviceToHost, s));
+  if (dc && ddc != dc && n) GB_CUDA(cudaMemcpyAsync(dc, ddc, bd, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int gb_neighbors_set_stream(gb_neighbors_t *h, void *stream) {
+  if (!h) return GB_ERROR_ARGUMENT;
+  h->nl.stream = (cudaStream_t)stream;
+  return 0;
+}
+
+}  // extern "C"

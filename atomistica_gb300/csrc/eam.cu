@@ -1,0 +1,525 @@
+// Tabulated alloy EAM on GB300 (replaces
+// src/potentials/eam/tabulated_alloy_eam.f90:147-259 (setfl reader) and
+// :423-627 (kernel), with the natural cubic spline of
+// src/support/simple_spline.f90:127-195, 373-614).
+//
+//   eam_density  one warp per atom i (lanes strided over its list entries):
+//                rho_i = sum_j rho_{el j}(r_ij) (no extrapolation: an argument
+//                outside the table raises an error as in the serial reference),
+//                rho clamped at 0, F_i and F'_i with index-clamped
+//                extrapolation (:506-554).
+//   eam_pair     one warp per atom i: for each entry (i->j) the i-side term of
+//                the reference (:561-607) and the j-side term of the mirror
+//                entry (j->i) (same r, exactly negated pair vector), so that
+//                f_i = sum_j [df_ij - df_ji] is a gather: no atomics, no
+//                reverse index.  The mask applies to the i side of each entry
+//                as in the reference (:488).
+// Spline coefficients are built on the host in FP64 with the reference's
+// operation order and uploaded as 8 doubles per interval
+// {y, c1, c2, c3, d1, d2, d3, 0}: a value gather is one 32-byte sector.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+
+#include "potential.h"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// Host spline builder (simple_spline_init, :127-195; scale_y_axis :756-773).
+// ---------------------------------------------------------------------------
+void SplineHost::init(int n_, double x0_, double dx_, const double *yy) {
+  const double sig = 0.5;
+  n = n_;
+  x0 = x0_;
+  dx = dx_;
+  y.assign(yy, yy + n);
+  d2y.assign(n, 0.0);
+  std::vector<double> u(n, 0.0);
+  c1.assign(n - 1, 0.0);
+  c2.assign(n - 1, 0.0);
+  c3.assign(n - 1, 0.0);
+  d1.assign(n - 1, 0.0);
+  d2.assign(n - 1, 0.0);
+  d3.assign(n - 1, 0.0);
+  for (int i = 1; i < n - 1; i++) {
+    const double p = sig * d2y[i - 1] + 2;
+    d2y[i] = (sig - 1) / p;
+    u[i] = (6.0 * ((y[i + 1] - y[i]) / dx - (y[i] - y[i - 1]) / dx) / (2 * dx) - sig * u[i - 1]) / p;
+  }
+  const double qn = 0.0, un = 0.0;
+  d2y[n - 1] = (un - qn * u[n - 2]) / (qn * d2y[n - 2] + 1.0);
+  for (int k = n - 2; k >= 0; k--) d2y[k] = d2y[k] * d2y[k + 1] + u[k];
+  const double dx2 = dx * dx;
+  for (int k = 0; k < n - 1; k++) {
+    c1[k] = y[k + 1] - y[k] - (2 * d2y[k] + d2y[k + 1]) * dx2 / 6;
+    c2[k] = d2y[k] * dx2 / 2;
+    c3[k] = (d2y[k + 1] - d2y[k]) * dx2 / 6;
+  }
+  for (int k = 0; k < n - 1; k++) {
+    d1[k] = c1[k] / dx;
+    d2[k] = 2 * c2[k] / dx;
+    d3[k] = 3 * c3[k] / dx;
+  }
+  cut = x0 + dx * (n - 1);
+}
+
+void SplineHost::scale_y(double fac) {
+  for (auto *v : {&y, &d2y, &c1, &c2, &c3, &d1, &d2, &d3})
+    for (auto &x : *v) x = fac * x;
+}
+
+// setfl reader (tabulated_alloy_eam.f90:178-253).
+int eam_read_setfl(const char *fn, EamTables &t) {
+  std::ifstream in(fn);
+  if (!in) {
+    set_error(std::string("Could not open file '") + fn + "'.");
+    return GB_ERROR_FILE_NOT_FOUND;
+  }
+  std::string line;
+  for (int i = 0; i < 3; i++)
+    if (!std::getline(in, line)) {
+      set_error("setfl: premature end of file in header");
+      return GB_ERROR_IO_EOF;
+    }
+  if (!std::getline(in, line)) {
+    set_error("setfl: premature end of file");
+    return GB_ERROR_IO_EOF;
+  }
+  {
+    std::istringstream ss(line);
+    ss >> t.nel;
+    if (!ss || t.nel <= 0 || t.nel > 10) {
+      set_error("setfl: bad element count line: " + line);
+      return GB_ERROR_IO;
+    }
+  }
+  int nF = 0, nr = 0;
+  double dF = 0, dr = 0;
+  if (!std::getline(in, line)) {
+    set_error("setfl: premature end of file");
+    return GB_ERROR_IO_EOF;
+  }
+  {
+    std::istringstream ss(line);
+    ss >> nF >> dF >> nr >> dr >> t.cutoff;
+    if (!ss || nF < 2 || nr < 2 || !(dF > 0) || !(dr > 0)) {
+      set_error("setfl: bad grid line: " + line);
+      return GB_ERROR_IO;
+    }
+  }
+  auto read_values = [&](int n, std::vector<double> &v) {
+    v.clear();
+    v.reserve(n + 2);
+    std::string tok;
+    while ((int)v.size() < n && (in >> tok)) v.push_back(std::strtod(tok.c_str(), nullptr));
+    std::getline(in, line);
+    return (int)v.size() == n;
+  };
+  t.Z.assign(t.nel, 0);
+  t.F.assign(t.nel, SplineHost());
+  t.rho.assign(t.nel, SplineHost());
+  t.phi.assign((size_t)t.nel * t.nel, SplineHost());
+  std::vector<double> v;
+  for (int e = 0; e < t.nel; e++) {
+    if (!std::getline(in, line)) {
+      set_error("setfl: premature end of file");
+      return GB_ERROR_IO_EOF;
+    }
+    std::istringstream ss(line);
+    ss >> t.Z[e];
+    if (!ss || t.Z[e] <= 0) {
+      set_error("setfl: bad element line: " + line);
+      return GB_ERROR_IO;
+    }
+    if (!read_values(nF, v)) {
+      set_error("setfl: premature end of file in F(rho)");
+      return GB_ERROR_IO_EOF;
+    }
+    t.F[e].init(nF, 0.0, dF, v.data());
+    if (!read_values(nr, v)) {
+      set_error("setfl: premature end of file in rho(r)");
+      return GB_ERROR_IO_EOF;
+    }
+    v.push_back(0.0);
+    v.push_back(0.0);
+    t.rho[e].init(nr + 2, 0.0, dr, v.data());
+  }
+  for (int i = 0; i < t.nel; i++)
+    for (int j = 0; j <= i; j++) {
+      if (!read_values(nr, v)) {
+        set_error("setfl: premature end of file in r*phi(r)");
+        return GB_ERROR_IO_EOF;
+      }
+      v.push_back(0.0);
+      v.push_back(0.0);
+      SplineHost s;
+      s.init(nr + 2, 0.0, dr, v.data());
+      s.scale_y(0.5);
+      t.phi[(size_t)i * t.nel + j] = s;
+      t.phi[(size_t)j * t.nel + i] = s;
+    }
+  return 0;
+}
+
+int eam_upload(EamTables &t) {
+  std::vector<const SplineHost *> all;
+  for (auto &s : t.F) all.push_back(&s);
+  for (auto &s : t.rho) all.push_back(&s);
+  for (auto &s : t.phi) all.push_back(&s);
+  size_t total = 0;
+  for (auto *s : all) total += 8 * (size_t)(s->n - 1);
+  std::vector<double> h(total);
+  std::vector<size_t> offs;
+  size_t o = 0;
+  for (auto *s : all) {
+    offs.push_back(o);
+    for (int k = 0; k < s->n - 1; k++) {
+      double *d = &h[o + 8 * (size_t)k];
+      d[0] = s->y[k];
+      d[1] = s->c1[k];
+      d[2] = s->c2[k];
+      d[3] = s->c3[k];
+      d[4] = s->d1[k];
+      d[5] = s->d2[k];
+      d[6] = s->d3[k];
+      d[7] = 0.0;
+    }
+    o += 8 * (size_t)(s->n - 1);
+  }
+  GB_CHECK(t.dev.ensure(sizeof(double) * std::max<size_t>(total, 1)));
+  GB_CUDA(cudaMemcpy(t.dev.p, h.data(), sizeof(double) * total, cudaMemcpyHostToDevice));
+  auto mk = [&](const SplineHost &s, size_t off) {
+    SplineDev d;
+    d.tab = t.dev.as<double>() + off;
+    d.n = s.n;
+    d.x0 = s.x0;
+    d.dx = s.dx;
+    d.cut = s.cut;
+    return d;
+  };
+  t.dF.clear();
+  t.drho.clear();
+  t.dphi.clear();
+  size_t q = 0;
+  for (auto &s : t.F) t.dF.push_back(mk(s, offs[q++]));
+  for (auto &s : t.rho) t.drho.push_back(mk(s, offs[q++]));
+  for (auto &s : t.phi) t.dphi.push_back(mk(s, offs[q++]));
+  return 0;
+}
+
+namespace {
+
+constexpr int kMaxEamEl = 4;
+
+struct EamArgs {
+  int nat;
+  int nel;
+  const Pos4 *pos;
+  const int *el;  // table index or -1
+  const int *seed, *nbr, *shift, *mask;
+  double A[3][3];
+  double cutoff_sq;
+  SplineDev F[kMaxEamEl], rho[kMaxEamEl], phi[kMaxEamEl * kMaxEamEl];
+  double *Fi, *dFi;      // per atom
+  double *f, *epa, *wpa;  // outputs (device, accumulated)
+  double *part;           // 10 per block
+  int *status;
+};
+
+// simple_spline_f / _df without extrapolation (:373-528): 1-based interval
+// index i = floor((x-x0)/dx + 1), or n-1 at x == cut; out of range -> error.
+__device__ __forceinline__ bool spline_index(const SplineDev &s, double x, double &B, int &k) {
+  double xf;
+  int i;
+  if (x == s.cut) {
+    xf = s.n;
+    i = s.n - 1;
+  } else {
+    xf = (x - s.x0) / s.dx + 1;
+    const double fl = floor(xf);
+    i = (fl < -1e9) ? -1000000000 : (fl > 1e9 ? 1000000000 : (int)fl);
+  }
+  if (i < 1 || i >= s.n) return false;
+  B = xf - i;
+  k = i - 1;
+  return true;
+}
+
+__device__ __forceinline__ double spline_f(const SplineDev &s, double x, int *err) {
+  double B;
+  int k;
+  if (!spline_index(s, x, B, k)) {
+    *err = 1;
+    return 1.0;
+  }
+  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k);
+  const double2 a = __ldg(t), b = __ldg(t + 1);
+  return a.x + B * (a.y + B * (b.x + B * b.y));
+}
+
+__device__ __forceinline__ double spline_df(const SplineDev &s, double x, int *err) {
+  double B;
+  int k;
+  if (!spline_index(s, x, B, k)) {
+    *err = 1;
+    return 1.0;
+  }
+  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k + 4);
+  const double2 c = __ldg(t), d = __ldg(t + 1);
+  return c.x + B * (c.y + B * d.x);
+}
+
+// simple_spline_f_and_df with extrapolate=.true. (:536-614).
+__device__ __forceinline__ void spline_fdf_extrap(const SplineDev &s, double x, double &f,
+                                                  double &df) {
+  const double xf = (x - s.x0) / s.dx + 1;
+  const double fl = floor(xf);
+  int i = (fl < -1e9) ? -1000000000 : (fl > 1e9 ? 1000000000 : (int)fl);
+  if (i < 1)
+    i = 1;
+  else if (i >= s.n)
+    i = s.n - 1;
+  const double B = xf - i;
+  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)(i - 1));
+  const double2 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2), d = __ldg(t + 3);
+  f = a.x + B * (a.y + B * (b.x + B * b.y));
+  df = c.x + B * (c.y + B * d.x);
+}
+
+// GET_DRJ (macros.inc:76): r_i - r_j + matmul(Abox, dc), reference order.
+__device__ __forceinline__ void get_drj(const EamArgs &a, const Pos4 &pi, const Pos4 &pj,
+                                        int sh, double d[3]) {
+  int s0, s1, s2;
+  unpack_shift(sh, s0, s1, s2);
+  d[0] = __dsub_rn(pi.x, pj.x);
+  d[1] = __dsub_rn(pi.y, pj.y);
+  d[2] = __dsub_rn(pi.z, pj.z);
+  if (s0 | s1 | s2) {
+    const double sx = s0, sy = s1, sz = s2;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double as = __dmul_rn(a.A[c][0], sx);
+      as = __dadd_rn(as, __dmul_rn(a.A[c][1], sy));
+      as = __dadd_rn(as, __dmul_rn(a.A[c][2], sz));
+      d[c] = __dadd_rn(d[c], as);
+    }
+  }
+}
+
+__device__ __forceinline__ double norm2_ref(const double d[3]) {
+  double s = __dmul_rn(d[0], d[0]);
+  s = __dadd_rn(s, __dmul_rn(d[1], d[1]));
+  s = __dadd_rn(s, __dmul_rn(d[2], d[2]));
+  return s;
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+constexpr int kEamThreads = 256;
+
+__global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
+  const int warp = (blockIdx.x * kEamThreads + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= a.nat) return;
+  const int i = warp;
+  const int eli = a.el[i];
+  if (eli < 0 || (a.mask && a.mask[i] == 0)) {
+    if (lane == 0) {
+      a.Fi[i] = 0.0;
+      a.dFi[i] = 0.0;
+    }
+    return;
+  }
+  const Pos4 pi = a.pos[i];
+  double rho = 0.0;
+  int err = 0;
+  const int s = a.seed[i], e = a.seed[i + 1];
+  for (int b = s + lane; b < e; b += 32) {
+    const int j = a.nbr[b];
+    const int elj = a.el[j];
+    if (elj < 0) continue;
+    double d[3];
+    get_drj(a, pi, a.pos[j], a.shift[b], d);
+    const double r2 = norm2_ref(d);
+    if (r2 < a.cutoff_sq) rho += spline_f(a.rho[elj], sqrt(r2), &err);
+  }
+  rho = warp_sum(rho);
+  if (err) atomicOr(a.status, 1);
+  if (lane == 0) {
+    if (rho < 0.0) rho = 0.0;
+    double F, dF;
+    spline_fdf_extrap(a.F[eli], rho, F, dF);
+    a.Fi[i] = F;
+    a.dFi[i] = dF;
+  }
+}
+
+template <bool kEpa, bool kWat>
+__global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
+  __shared__ double sred[kEamThreads / 32][10];
+  const int wib = threadIdx.x >> 5;
+  const int warp = (blockIdx.x * kEamThreads + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  double e_tot = 0.0;
+  double w_tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (warp < a.nat) {
+    const int i = warp;
+    const int eli = a.el[i];
+    double F3[3] = {0.0, 0.0, 0.0};
+    double Wa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double Ei = 0.0;
+    if (eli >= 0) {
+      const bool mi = !(a.mask && a.mask[i] == 0);
+      const double dFi = mi ? a.dFi[i] : 0.0;
+      const Pos4 pi = a.pos[i];
+      int err = 0;
+      const int s = a.seed[i], e = a.seed[i + 1];
+      for (int b = s + lane; b < e; b += 32) {
+        const int j = a.nbr[b];
+        const int elj = a.el[j];
+        if (elj < 0) continue;
+        double d[3];
+        get_drj(a, pi, a.pos[j], a.shift[b], d);
+        const double r2 = norm2_ref(d);
+        if (!(r2 < a.cutoff_sq)) continue;
+        const bool mj = !(a.mask && a.mask[j] == 0);
+        const double r = sqrt(r2);
+        const double rinv = 1.0 / r;
+        double phi, dphi;
+        spline_fdf_extrap(a.phi[eli * a.nel + elj], r, phi, dphi);
+        const double pair = (dphi - phi * rinv) * rinv;
+        if (mi) {
+          // i-side of entry (i->j), :577-607
+          const double fac = spline_df(a.rho[elj], r, &err);
+          const double sc = -(dFi * fac + pair) * rinv;
+          Ei += phi * rinv;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const double df = sc * d[c];
+            F3[c] += df;
+#pragma unroll
+            for (int c2 = 0; c2 < 3; c2++) {
+              const double w = -d[c2] * df;  // (c2, c) Fortran
+              w_tot[c2 + 3 * c] += w;
+              if (kWat) Wa[c2 + 3 * c] += 0.5 * w;
+            }
+          }
+        }
+        if (mj) {
+          // j-side of the mirror entry (j->i): dr' = -d, acts on i with -df'.
+          const double fac = spline_df(a.rho[eli], r, &err);
+          const double sc = -(a.dFi[j] * fac + pair) * rinv;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const double dfp = sc * (-d[c]);
+            F3[c] -= dfp;
+            if (kWat)
+#pragma unroll
+              for (int c2 = 0; c2 < 3; c2++) Wa[c2 + 3 * c] += 0.5 * (d[c2] * dfp);
+          }
+        }
+      }
+      if (err) atomicOr(a.status, 1);
+#pragma unroll
+      for (int c = 0; c < 3; c++) F3[c] = warp_sum(F3[c]);
+      Ei = warp_sum(Ei);
+      if (kWat)
+#pragma unroll
+        for (int c = 0; c < 9; c++) Wa[c] = warp_sum(Wa[c]);
+      if (mi) Ei += a.Fi[i];
+      if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) a.f[3 * (size_t)i + c] += F3[c];
+        if (kEpa && mi) a.epa[i] += Ei;
+        if (kWat)
+#pragma unroll
+          for (int c = 0; c < 9; c++) a.wpa[9 * (size_t)i + c] += Wa[c];
+      }
+      e_tot = (lane == 0 && mi) ? Ei : 0.0;
+    }
+  }
+  // Block partials: energy (lane 0 of each warp holds it) and virial.
+#pragma unroll
+  for (int c = 0; c < 9; c++) w_tot[c] = warp_sum(w_tot[c]);
+  e_tot = warp_sum(e_tot);
+  if (lane == 0) {
+    sred[wib][0] = e_tot;
+#pragma unroll
+    for (int c = 0; c < 9; c++) sred[wib][1 + c] = w_tot[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < 10) {
+    double s = 0.0;
+    for (int w = 0; w < kEamThreads / 32; w++) s += sred[w][threadIdx.x];
+    a.part[10 * (size_t)blockIdx.x + threadIdx.x] = s;
+  }
+}
+
+}  // namespace
+
+int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
+                bool want_wat) {
+  cudaStream_t s = pot.stream;
+  const int nat = p.nat;
+  EamTables &t = *pot.eam;
+  if (nat == 0) {
+    GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
+    return 0;
+  }
+  if (t.nel > kMaxEamEl) {
+    set_error("TabulatedAlloyEAM: more than 4 elements in the setfl file are not supported.");
+    return GB_ERROR_ARGUMENT;
+  }
+  EamArgs a;
+  a.nat = nat;
+  a.nel = t.nel;
+  a.pos = nl.pos4.as<Pos4>();
+  a.el = pot.el.as<int>();
+  a.seed = nl.seed.as<int>();
+  a.nbr = nl.nbr.as<int>();
+  a.shift = nl.shift.as<int>();
+  a.mask = o.mask;
+  std::memcpy(a.A, p.A, sizeof(a.A));
+  a.cutoff_sq = t.cutoff * t.cutoff;
+  for (int q = 0; q < t.nel; q++) {
+    a.F[q] = t.dF[q];
+    a.rho[q] = t.drho[q];
+  }
+  for (int q = 0; q < t.nel * t.nel; q++) a.phi[q] = t.dphi[q];
+  GB_CHECK(pot.atom_dF.ensure(sizeof(double) * 2 * nat));
+  a.Fi = pot.atom_dF.as<double>();
+  a.dFi = a.Fi + nat;
+  a.f = o.f;
+  a.epa = o.epot_per_at;
+  a.wpa = o.wpot_per_at;
+  const int blocks = (nat * 32 + kEamThreads - 1) / kEamThreads;
+  GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * blocks + 64));
+  a.part = pot.tile_part.as<double>();
+  a.status = o.status;
+  eam_density<<<blocks, kEamThreads, 0, s>>>(a);
+  const bool epa = o.epot_per_at != nullptr;
+  if (epa && want_wat)
+    eam_pair<true, true><<<blocks, kEamThreads, 0, s>>>(a);
+  else if (epa)
+    eam_pair<true, false><<<blocks, kEamThreads, 0, s>>>(a);
+  else if (want_wat)
+    eam_pair<false, true><<<blocks, kEamThreads, 0, s>>>(a);
+  else
+    eam_pair<false, false><<<blocks, kEamThreads, 0, s>>>(a);
+  GB_CUDA(cudaGetLastError());
+  GB_CHECK(reduce_partials(a.part, blocks, 10, o.red, s));
+  return 0;
+}
+
+}  // namespace gb

@@ -1,0 +1,166 @@
+// Internal types shared by the CUDA translation units of libatomistica_gb300.
+// Nothing here crosses the C-ABI; the public surface is include/atomistica_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/atomistica_gb300.h"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// Error state.  The C-ABI returns an int code (error.f90:81-86 convention:
+// 0 = none, negative = error) and keeps the message in a thread-local buffer.
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+void clear_error();
+
+#define GB_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      ::gb::set_error(std::string("CUDA error in " #call ": ") +                   \
+                      cudaGetErrorString(e_));                                     \
+      return GB_ERROR_CUDA;                                                        \
+    }                                                                              \
+  } while (0)
+
+#define GB_CHECK(expr)        \
+  do {                        \
+    int rc_ = (expr);         \
+    if (rc_ != 0) return rc_; \
+  } while (0)
+
+// Growable device buffer (grows, never shrinks — like the reference's
+// internal neighbour buffers, bop_kernel.f90:307-414).
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t n);
+  void release();
+  template <class T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+  ~DevBuf() { release(); }
+};
+
+// Pinned host staging buffer.
+struct HostBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t n);
+  void release();
+  template <class T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+  ~HostBuf() { release(); }
+};
+
+// Does the pointer refer to device (or managed) memory?
+bool is_device_ptr(const void *ptr);
+
+// ---------------------------------------------------------------------------
+// Particles (python_particles.f90:85-140, set_cell :286-346).
+// ---------------------------------------------------------------------------
+struct Particles {
+  int nat = 0;
+  double A[3][3] = {{0}};  // A[a][k] = Abox(a,k): column k = lattice vector k
+  double B[3][3] = {{0}};  // Bbox = A^-1 (Gauss elimination, gauss() order)
+  int pbc[3] = {1, 1, 1};
+  bool cell_set = false;
+  uint64_t pos_rev = 0, cell_rev = 0, z_rev = 0;
+  DevBuf r;      // double[3*nat], caller layout (nat,3)
+  DevBuf Z;      // int[nat]
+  std::vector<int> hZ;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+};
+
+// Packed integer image shift: three 10-bit signed fields (range +-511).
+__host__ __device__ inline int32_t pack_shift(int s0, int s1, int s2) {
+  return (int32_t)((uint32_t)(s0 + 512) | ((uint32_t)(s1 + 512) << 10) |
+                   ((uint32_t)(s2 + 512) << 20));
+}
+__host__ __device__ inline void unpack_shift(int32_t p, int &s0, int &s1, int &s2) {
+  uint32_t u = (uint32_t)p;
+  s0 = (int)(u & 1023u) - 512;
+  s1 = (int)((u >> 10) & 1023u) - 512;
+  s2 = (int)((u >> 20) & 1023u) - 512;
+}
+constexpr int kMaxShift = 511;
+
+// Position padded to 32 bytes: one DRAM sector per gather.
+struct __align__(32) Pos4 {
+  double x, y, z, w;
+};
+
+struct Cell {
+  double A[3][3];
+  int pbc[3];
+};
+
+// ---------------------------------------------------------------------------
+// Neighbour list (python_neighbors.f90:51-139) — full directed CSR with
+// per-entry image shifts, rebuilt when positions or cell changed.
+// ---------------------------------------------------------------------------
+struct Neighbors {
+  int avgn = 100;
+  double interaction_range = 0.0;
+  double cutoff = 0.0;
+  bool valid = false;
+  const Particles *built_for = nullptr;
+  uint64_t built_pos_rev = ~0ull, built_cell_rev = ~0ull;
+  int built_nat = -1;
+
+  // Binning (neighbors_binning_init, :765-871).
+  int n_cells[3] = {0, 0, 0};
+  double rec[3][3] = {{0}};
+  int dx = 0, dy = 0, dz = 0;
+
+  DevBuf pos4;        // Pos4[nat]: positions padded for one-sector gathers
+  DevBuf atom_cell;   // int[nat]: wrapped linear cell index
+  DevBuf atom_wrap;   // int[nat]: packed wrap counts q (pbc dims)
+  DevBuf cell_count;  // int[ncells+1]
+  DevBuf cell_start;  // int[ncells+1]
+  DevBuf cell_atoms;  // int[nat]: atoms sorted by (cell, id)
+  DevBuf counts;      // int[nat+1]
+  DevBuf seed;        // int[nat+1] CSR offsets
+  DevBuf nbr;         // int[capacity]
+  DevBuf shift;       // int32 packed shifts [capacity]
+  DevBuf rev;         // int[capacity]: reverse entry (built on demand)
+  DevBuf scan_tmp;
+  DevBuf stats;       // device-side status words
+  HostBuf hstats;
+  bool rev_valid = false;
+  int64_t nentries = 0;
+  int maxz = 0;
+  cudaStream_t stream = nullptr;
+};
+
+// Builds/refreshes the list for p if positions or cell changed
+// (neighbors_update, :430-456).
+int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream);
+int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream);
+
+// Device-wide exclusive scan of int32 (n+1 outputs, out[n] = total).
+int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t stream);
+
+// Cell for kernels.
+Cell make_cell(const Particles &p);
+
+}  // namespace gb
+
+// Opaque handle types of the C-ABI.
+struct gb_particles {
+  gb::Particles p;
+};
+struct gb_neighbors {
+  gb::Neighbors nl;
+};

@@ -1,0 +1,100 @@
+// Internal potential object shared by bop.cu, eam.cu and api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace gb {
+
+enum PotKind { kTersoff = 0, kKumagai = 1, kEAM = 2 };
+
+// Uniform natural cubic spline tables (simple_spline.f90:127-195) built on the
+// host.  Device layout: 8 doubles per interval k = {y_k, c1_k, c2_k, c3_k,
+// d1_k, d2_k, d3_k, 0} so that one value-gather is one 32-byte sector and a
+// value+derivative gather is two.
+struct SplineHost {
+  int n = 0;
+  double x0 = 0, dx = 1, cut = 0;
+  std::vector<double> y, d2y, c1, c2, c3, d1, d2, d3;
+  void init(int n, double x0, double dx, const double *yy);
+  void scale_y(double fac);
+};
+
+struct SplineDev {
+  const double *tab;  // 8*(n-1) doubles
+  int n;
+  double x0, dx, cut;
+};
+
+struct EamTables {
+  int nel = 0;
+  std::vector<int> Z;
+  double cutoff = 0;
+  std::vector<SplineHost> F, rho, phi;  // phi[i*nel+j]
+  DevBuf dev;                           // all tables, packed
+  std::vector<SplineDev> dF, drho, dphi;
+};
+
+int eam_read_setfl(const char *fn, EamTables &t);
+int eam_upload(EamTables &t);
+
+struct Outputs {
+  // Device pointers (accumulated into); NULL when not requested.
+  double *f = nullptr;
+  double *epot_per_at = nullptr;
+  double *wpot_per_at = nullptr;
+  double *epot_per_bond = nullptr;
+  double *f_per_bond = nullptr;
+  double *wpot_per_bond = nullptr;
+  const int *mask = nullptr;
+  // Device result of the reductions: [0] epot, [1..9] wpot Fortran order.
+  double *red = nullptr;
+  // Device status word: bit 0 spline argument out of range, bit 1 tile plan
+  // mismatch.
+  int *status = nullptr;
+};
+
+struct Potential {
+  PotKind kind = kTersoff;
+  int precision = GB_PRECISION_FP64;
+  gb_tersoff_params_t tp{};
+  gb_kumagai_params_t kp{};
+  std::unique_ptr<EamTables> eam;
+
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+
+  // Element map for the bound particles.
+  DevBuf el;
+  const Particles *el_for = nullptr;
+  uint64_t el_zrev = ~0ull;
+
+  // Scratch.
+  DevBuf bond_G, bond_e, bond_w, bond_fr, tile_part, red;
+  DevBuf atom_dF;
+  DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
+  HostBuf hred;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double timing[3] = {0, 0, 0};
+  int tile_atoms = 32;
+  int last_status = 0;
+};
+
+// Interaction range requested by bind_to for the given element pair set.
+double bop_pair_cutoff(const Potential &pot, int zi, int zj);
+
+// Kernel launches (on pot.stream) for an up-to-date neighbour list.
+int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
+                bool want_wat, bool want_per_bond);
+int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
+                bool want_wat);
+
+// Deterministic fixed-order sum of tile partials: red[c] = sum_t part[t*nc+c].
+int reduce_partials(const double *part, int ntiles, int nc, double *red, cudaStream_t s);
+
+}  // namespace gb

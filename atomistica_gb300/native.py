@@ -1,0 +1,396 @@
+"""
+Native objects with the interface of Atomistica's Python extension
+``_atomistica`` (src/python/c/particles.c, neighbors.c, potential.c):
+
+    p = Particles(); p.allocate(nat); p.set_cell(cell, pbc)
+    p.coordinates[:] = r; p.I_changed_positions()
+    p.Z[:] = numbers; p.update_elements()
+    nl = Neighbors(avgn)
+    pot = Tersoff(**params); pot.bind_to(p, nl)
+    epot, f, wpot, ... = pot.energy_and_forces(p, nl, forces=..., mask=...,
+                          epot_per_at=True, epot_per_bond=..., f_per_bond=...,
+                          wpot_per_at=..., wpot_per_bond=...)
+
+Return layouts follow potential.c:622-657: f (nat,3); wpot (3,3) with
+wpot[a,c] = W(a,c); wpot_per_at (nat,3,3) and wpot_per_bond (n,3,3) with
+[i,x,y] = W_i(y,x) (the Fortran (3,3,n) buffer viewed C-ordered); per-bond
+arrays follow the neighbour-list order of Neighbors.get_neighbors.
+
+Arrays may be numpy (host) or torch CUDA tensors (used in place).  All
+computation runs in libatomistica_gb300 on the GPU; there is no CPU path.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GB_PRECISION_FP64, GB_PRECISION_MIXED, check, load
+from .parameters import (Kumagai_CompMaterSci_39_457_Si, Tersoff_PRB_39_5566_Si_C,
+                         atomic_numbers)
+
+try:  # PyTorch is optional: only for device-resident inputs/outputs.
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_torch(x):
+    return torch is not None and isinstance(x, torch.Tensor)
+
+
+def _ptr(x, dtype):
+    """(pointer, keepalive) for a numpy array or torch tensor."""
+    if x is None:
+        return None, None
+    if _is_torch(x):
+        want = torch.float64 if dtype == np.float64 else torch.int32
+        if x.dtype != want or not x.is_contiguous():
+            raise TypeError("tensor must be contiguous %s" % want)
+        return x.data_ptr(), x
+    a = np.ascontiguousarray(x, dtype=dtype)
+    return a.ctypes.data, a
+
+
+def _to_numpy(x):
+    if _is_torch(x):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
+class Particles:
+    """particles_t: positions (nat,3), cell (rows = lattice vectors), pbc,
+    atomic numbers (python_particles.f90:85-140)."""
+
+    def __init__(self):
+        self._L = load()
+        self._h = ctypes.c_void_p()
+        check(self._L.gb_particles_new(ctypes.byref(self._h)), "particles_new")
+        self.nat = 0
+        self.coordinates = np.zeros((0, 3))
+        self.Z = np.zeros(0, dtype=np.int32)
+        self.cell = np.eye(3)
+        self.pbc = np.array([True, True, True])
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gb_particles_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __len__(self):
+        return self.nat
+
+    def allocate(self, nat):
+        check(self._L.gb_particles_allocate(self._h, int(nat)), "particles_allocate")
+        self.nat = int(nat)
+        self.coordinates = np.zeros((self.nat, 3))
+        self.Z = np.zeros(self.nat, dtype=np.int32)
+
+    def set_cell(self, cell, pbc=True):
+        cell = np.asarray(cell, dtype=np.float64)
+        if cell.shape == (3,):
+            cell = np.diag(cell)
+        pbc = np.broadcast_to(np.asarray(pbc, dtype=bool), (3,)).copy()
+        c = np.ascontiguousarray(cell)
+        pb = np.ascontiguousarray(pbc.astype(np.int32))
+        check(self._L.gb_particles_set_cell(self._h, c.ctypes.data, pb.ctypes.data),
+              "particles_set_cell")
+        self.cell = cell.copy()
+        self.pbc = pbc
+
+    def I_changed_positions(self):
+        """Upload ``coordinates`` (particles_I_changed_positions)."""
+        self.set_positions(self.coordinates)
+
+    def set_positions(self, r):
+        """Positions (nat,3): numpy array or torch CUDA tensor (float64)."""
+        ptr, keep = _ptr(r, np.float64)
+        if not _is_torch(r):
+            if keep is not self.coordinates:
+                self.coordinates = np.array(keep)
+        check(self._L.gb_particles_set_positions(self._h, ptr), "particles_set_positions")
+
+    def update_elements(self):
+        z = np.ascontiguousarray(self.Z, dtype=np.int32)
+        check(self._L.gb_particles_set_Z(self._h, z.ctypes.data), "particles_set_Z")
+
+    def set_Z(self, Z):
+        self.Z = np.ascontiguousarray(_to_numpy(Z), dtype=np.int32)
+        self.update_elements()
+
+    def set_stream(self, stream):
+        check(self._L.gb_particles_set_stream(self._h, stream), "particles_set_stream")
+
+
+def from_atoms(atoms):
+    """Particles from an ASE-like object (positions, cell, pbc, numbers)."""
+    p = Particles()
+    pos = atoms.get_positions() if hasattr(atoms, "get_positions") else atoms.positions
+    cell = atoms.get_cell() if hasattr(atoms, "get_cell") else atoms.cell
+    pbc = atoms.get_pbc() if hasattr(atoms, "get_pbc") else atoms.pbc
+    numbers = atoms.get_atomic_numbers() if hasattr(atoms, "get_atomic_numbers") else \
+        atoms.numbers
+    p.allocate(len(pos))
+    p.set_cell(np.asarray(cell), pbc)
+    p.Z[:] = numbers
+    p.update_elements()
+    p.coordinates[:] = pos
+    p.I_changed_positions()
+    return p
+
+
+class Neighbors:
+    """neighbors_t: full directed cell-list neighbour list."""
+
+    def __init__(self, avgn=100):
+        self._L = load()
+        self._h = ctypes.c_void_p()
+        check(self._L.gb_neighbors_new(ctypes.byref(self._h), int(avgn)), "neighbors_new")
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gb_neighbors_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def request_interaction_range(self, cutoff):
+        check(self._L.gb_neighbors_request_interaction_range(self._h, float(cutoff)),
+              "request_interaction_range")
+
+    @property
+    def interaction_range(self):
+        return self._L.gb_neighbors_get_interaction_range(self._h)
+
+    def update(self, p):
+        check(self._L.gb_neighbors_update(self._h, p._h), "neighbors_update")
+
+    def get_list(self, p):
+        """(seed (nat+1), j (n), dc (n,3)): CSR list in reference order."""
+        self.update(p)
+        n = self._L.gb_neighbors_get_size(self._h)
+        seed = np.zeros(len(p) + 1, dtype=np.int64)
+        j = np.zeros(max(n, 1), dtype=np.int32)
+        dc = np.zeros((max(n, 1), 3), dtype=np.int32)
+        check(self._L.gb_neighbors_get(self._h, p._h, seed.ctypes.data, j.ctypes.data,
+                                       dc.ctypes.data), "neighbors_get")
+        return seed, j[:n], dc[:n]
+
+    def get_neighbors(self, p, vec=False):
+        """(i, j, [dr], abs_dr) with dr = r_i - r_j + cell^T dc
+        (f_get_all_neighbors[_vec], neighbors_wrap.f90:425-492)."""
+        seed, j, dc = self.get_list(p)
+        i = np.repeat(np.arange(len(p), dtype=np.int32), np.diff(seed))
+        r = p.coordinates
+        dr = r[i] - r[j] + dc @ p.cell
+        abs_dr = np.sqrt(np.sum(dr * dr, axis=1))
+        if vec:
+            return i, j, dr, abs_dr
+        return i, j, abs_dr
+
+    def get_coordination_numbers(self, p, cutoff):
+        i, j, r = self.get_neighbors(p)
+        return np.bincount(i[r < cutoff], minlength=len(p))
+
+
+def _fill(arr, vals, n):
+    for q in range(n):
+        arr[q] = vals[q]
+
+
+def tersoff_params(params):
+    """gb_tersoff_params_t from a parameter dict (parameters.py format);
+    keys not given keep the values of the default Si-C set."""
+    d = dict(Tersoff_PRB_39_5566_Si_C)
+    d.update({k: v for k, v in params.items() if not k.startswith("__")})
+    p = _lib.TersoffParams()
+    els = d["el"]
+    p.nel = len(els)
+    if not 1 <= p.nel <= 3:
+        raise ValueError("Tersoff supports 1..3 elements")
+    for q, s in enumerate(els):
+        p.Z[q] = atomic_numbers[s]
+    npair = p.nel * (p.nel + 1) // 2
+    for k in ("A", "B", "xi", "lambda", "mu", "omega", "mubo", "r1", "r2"):
+        vals = d.get(k)
+        if vals is None or len(vals) < npair:
+            vals = list(vals or []) + [{"xi": 1.0, "omega": 1.0, "mubo": 0.0}.get(k, 1.0)] * npair
+        _fill(getattr(p, "lambda_" if k == "lambda" else k), [float(v) for v in vals], npair)
+    ms = list(d.get("m", [1] * npair)) + [1] * npair
+    _fill(p.m, [int(v) for v in ms], npair)
+    for k in ("beta", "n", "c", "d", "h"):
+        _fill(getattr(p, k), [float(v) for v in d[k]], p.nel)
+    return p
+
+
+def kumagai_params(params):
+    d = dict(Kumagai_CompMaterSci_39_457_Si)
+    d.update({k: v for k, v in params.items() if not k.startswith("__")})
+    p = _lib.KumagaiParams()
+    if len(d["el"]) != 1:
+        raise ValueError("Kumagai supports exactly one element")
+    p.nel = 1
+    p.Z[0] = atomic_numbers[d["el"][0]]
+    for k in ("A", "B", "lambda1", "lambda2", "eta", "delta", "alpha", "c1", "c2", "c3",
+              "c4", "c5", "h", "r1", "r2"):
+        getattr(p, k)[0] = float(d[k][0])
+    p.beta[0] = int(d["beta"][0])
+    return p
+
+
+class _Potential:
+    """Common energy_and_forces front-end (src/python/c/potential.c:347-666)."""
+
+    features = ("mask", "per_at", "per_bond")
+
+    def __init__(self):
+        self._L = load()
+        self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gb_potential_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    @property
+    def precision(self):
+        return self._precision
+
+    def set_precision(self, precision):
+        code = {"fp64": GB_PRECISION_FP64, "mixed": GB_PRECISION_MIXED,
+                GB_PRECISION_FP64: GB_PRECISION_FP64,
+                GB_PRECISION_MIXED: GB_PRECISION_MIXED}[precision]
+        check(self._L.gb_potential_set_precision(self._h, code), "set_precision")
+        self._precision = "fp64" if code == GB_PRECISION_FP64 else "mixed"
+
+    def set_stream(self, stream):
+        check(self._L.gb_potential_set_stream(self._h, stream), "set_stream")
+
+    def get_cutoff(self):
+        return self._L.gb_potential_get_cutoff(self._h)
+
+    def bind_to(self, p, nl):
+        err = ctypes.c_int(0)
+        check(self._L.gb_potential_bind_to(self._h, p._h, nl._h, ctypes.byref(err)), "bind_to")
+
+    def last_timing(self):
+        """(neighbour ms, force ms, total ms) of the last call (CUDA events)."""
+        t = (ctypes.c_double * 3)()
+        self._L.gb_potential_last_timing(self._h, t)
+        return tuple(t)
+
+    def energy_and_forces(self, particles, neighbors, forces=None, mask=None, charges=None,
+                          epot_per_at=None, epot_per_bond=None, f_per_bond=None,
+                          wpot_per_at=None, wpot_per_bond=None):
+        nat = len(particles)
+        dev = _is_torch(forces) and forces.is_cuda
+
+        def zeros(shape):
+            if dev:
+                return torch.zeros(shape, dtype=torch.float64, device=forces.device)
+            return np.zeros(shape)
+
+        if forces is None:
+            forces = zeros((nat, 3))
+        elif tuple(forces.shape) != (nat, 3):
+            raise RuntimeError("Length of force array (= %d) does not equal  number of atoms "
+                               "(= %d)." % (forces.shape[0], nat))
+        if mask is not None:
+            if len(mask) != nat:
+                raise RuntimeError("Length of mask array (= %d) does not equal number of "
+                                   "atoms (= %d)." % (len(mask), nat))
+            if _is_torch(mask):
+                mask = mask.to(torch.int32).contiguous()
+            else:
+                mask = np.ascontiguousarray(np.asarray(mask).astype(np.int32))
+        if "per_bond" not in self.features and (epot_per_bond or f_per_bond or wpot_per_bond):
+            raise RuntimeError("Per-bond properties are not supported by %s."
+                               % type(self).__name__)
+        nb = 0
+        if epot_per_bond or f_per_bond or wpot_per_bond:
+            neighbors.update(particles)
+            nb = self._L.gb_neighbors_get_size(neighbors._h)
+        wpot = np.zeros((3, 3), order="F")
+        out = {}
+        if epot_per_at:
+            out["epot_per_at"] = zeros((nat,))
+        if epot_per_bond:
+            out["epot_per_bond"] = zeros((nb,))
+        if f_per_bond:
+            out["f_per_bond"] = zeros((nb, 3))
+        if wpot_per_at:
+            out["wpot_per_at"] = zeros((nat, 3, 3))
+        if wpot_per_bond:
+            out["wpot_per_bond"] = zeros((nb, 3, 3))
+        fp, fkeep = _ptr(forces, np.float64)
+        mp, mkeep = _ptr(mask, np.int32)
+        ptrs = {k: _ptr(v, np.float64) for k, v in out.items()}
+        epot = ctypes.c_double(0.0)
+        err = ctypes.c_int(0)
+        g = lambda k: ptrs[k][0] if k in ptrs else None  # noqa: E731
+        rc = self._L.gb_potential_energy_and_forces(
+            self._h, particles._h, neighbors._h, None, ctypes.byref(epot), fp,
+            wpot.ctypes.data, mp, g("epot_per_at"), g("epot_per_bond"), g("f_per_bond"),
+            g("wpot_per_at"), g("wpot_per_bond"), ctypes.byref(err))
+        check(rc, "%s.energy_and_forces" % type(self).__name__)
+        if fkeep is not forces and not _is_torch(forces):
+            forces[...] = fkeep
+        for k, (ptr, keep) in ptrs.items():
+            out[k] = keep
+        res = [epot.value, forces, np.ascontiguousarray(wpot)]
+        for k, flag in (("epot_per_at", epot_per_at), ("epot_per_bond", epot_per_bond),
+                        ("f_per_bond", f_per_bond), ("wpot_per_at", wpot_per_at),
+                        ("wpot_per_bond", wpot_per_bond)):
+            if flag is not None:
+                res.append(out.get(k) if flag else None)
+        return tuple(res)
+
+
+class Tersoff(_Potential):
+    """Tersoff bond-order potential (src/potentials/bop/tersoff/)."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        if params:
+            p = tersoff_params(params)
+            check(self._L.gb_tersoff_new(ctypes.byref(self._h), ctypes.byref(p)), "Tersoff")
+        else:
+            check(self._L.gb_tersoff_new(ctypes.byref(self._h), None), "Tersoff")
+        self.set_precision(precision)
+
+
+class Kumagai(_Potential):
+    """Kumagai bond-order potential (src/potentials/bop/kumagai/)."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        if params:
+            p = kumagai_params(params)
+            check(self._L.gb_kumagai_new(ctypes.byref(self._h), ctypes.byref(p)), "Kumagai")
+        else:
+            check(self._L.gb_kumagai_new(ctypes.byref(self._h), None), "Kumagai")
+        self.set_precision(precision)
+
+
+class TabulatedAlloyEAM(_Potential):
+    """Tabulated alloy EAM from a DYNAMO setfl file
+    (src/potentials/eam/tabulated_alloy_eam.f90)."""
+
+    features = ("mask", "per_at")
+
+    def __init__(self, fn, elements="*"):
+        super().__init__()
+        if elements not in ("*", None):
+            raise NotImplementedError("element filters other than '*' are not supported")
+        check(self._L.gb_tabulated_alloy_eam_new(ctypes.byref(self._h),
+                                                 str(fn).encode()), "TabulatedAlloyEAM")
+        self._precision = "fp64"
+
+    def table(self, which, idx):
+        """((x0, dx, cut), coefficients (8, n)) of a spline table:
+        which = 0 F(rho), 1 rho(r), 2 phi(r) (index i*nel+j)."""
+        x = np.zeros(3)
+        n = self._L.gb_tabulated_alloy_eam_table(self._h, which, idx, x.ctypes.data, None)
+        if n < 0:
+            check(n, "table")
+        c = np.zeros((8, n))
+        self._L.gb_tabulated_alloy_eam_table(self._h, which, idx, x.ctypes.data, c.ctypes.data)
+        return x, c

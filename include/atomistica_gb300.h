@@ -1,0 +1,218 @@
+/*
+ * atomistica_gb300 — C-ABI of the GB300-native per-step force path.
+ *
+ * Drop-in replacement for the ISO_C_BINDING shims that Atomistica generates
+ * for every potential (src/python/gen_factory.py:98-356, C prototypes
+ * :380-401, function table src/python/c/factory.template.h:36-52) and for the
+ * particles / neighbour-list objects they operate on
+ * (src/python/f90/particles_wrap.f90, src/python/f90/neighbors_wrap.f90).
+ *
+ * Conventions kept from the reference:
+ *   - every call returns an int error code; 0 = ERROR_NONE, negative = error
+ *     (src/support/error.f90:81-86); the message is available from
+ *     gb_get_error() (the reference pushes it on its error stack and converts
+ *     it with error_to_py, src/python/c/py_f.c:36);
+ *   - `epot` is set (zeroed, then accumulated; gen_factory.py:283), while `f`,
+ *     `wpot` and every optional per-atom / per-bond output are ACCUMULATED into
+ *     (the caller zeroes them, src/python/c/potential.c:468-479);
+ *   - array layouts are those the Python extension hands to Fortran:
+ *     positions and forces (nat,3) C-order (= Fortran (3,nat)); cell rows are
+ *     the lattice vectors (particles.c:436-461); wpot is Fortran (3,3)
+ *     (element (a,c) at wpot[a + 3c]); wpot_per_at / wpot_per_bond are Fortran
+ *     (3,3,n) (element (a,c,i) at [a + 3c + 9i]); f_per_bond is (n,3);
+ *   - optional outputs are NULL when not requested; a potential that does not
+ *     support one (EAM: per-bond) returns an error (gen_factory.py:302-351);
+ *   - per-bond arrays are indexed by the compact neighbour-list entry, in the
+ *     order of gb_neighbors_get (the reference's f_pack_per_bond_* order,
+ *     neighbors_wrap.f90:498-547).
+ *
+ * Pointers may be host or device (CUDA) memory; device pointers are used in
+ * place, host pointers are staged through pinned buffers.  All device work
+ * of one object runs on its CUDA stream (gb_*_set_stream).  Calls on one
+ * handle are not re-entrant (as in the reference, tls.f90:45-49).
+ *
+ * There is no CPU fallback: without a CUDA device every compute entry point
+ * returns GB_ERROR_CUDA.
+ */
+#ifndef ATOMISTICA_GB300_H
+#define ATOMISTICA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes (src/support/error.f90:81-86 plus this library's own). */
+#define GB_ERROR_NONE 0
+#define GB_ERROR_UNSPECIFIED (-1)
+#define GB_ERROR_FILE_NOT_FOUND (-2)
+#define GB_ERROR_IO (-3)
+#define GB_ERROR_IO_EOF (-4)
+#define GB_ERROR_CUDA (-10)
+#define GB_ERROR_ARGUMENT (-11)
+#define GB_ERROR_CAPACITY (-12)
+#define GB_ERROR_DOMAIN (-13)
+
+/* Precision forms of the BOP kernels. */
+#define GB_PRECISION_FP64 0  /* drop-in: FP64 throughout */
+#define GB_PRECISION_MIXED 1 /* FP32 bond arithmetic, FP64 accumulation */
+
+typedef struct gb_particles gb_particles_t;
+typedef struct gb_neighbors gb_neighbors_t;
+typedef struct gb_potential gb_potential_t;
+
+/* Last error message of the calling thread ("" if none). */
+const char *gb_get_error(void);
+/* Library version string. */
+const char *gb_version(void);
+/* Number of CUDA devices visible (0 without a GPU). */
+int gb_device_count(void);
+
+/* ------------------------------------------------------------------------
+ * Particles — replaces particles_t (src/python/f90/python_particles.f90:85-140)
+ * and its Python binding (src/python/c/particles.c).
+ * ---------------------------------------------------------------------- */
+/* particles_new (particles_wrap.f90) */
+int gb_particles_new(gb_particles_t **p);
+void gb_particles_free(gb_particles_t *p);
+/* particles_allocate (python_particles.f90:524-555) */
+int gb_particles_allocate(gb_particles_t *p, int nat);
+int gb_particles_get_nat(const gb_particles_t *p);
+/* particles_set_cell (python_particles.f90:286-346): cell rows = lattice
+ * vectors (3x3 row-major), pbc[3] nonzero = periodic. */
+int gb_particles_set_cell(gb_particles_t *p, const double *cell, const int *pbc);
+/* Writes the coordinates (nat,3) and marks positions changed
+ * (I_changed_positions, python_particles.f90:768-777). */
+int gb_particles_set_positions(gb_particles_t *p, const double *r);
+/* Atomic numbers (nat); update_elements (python_particles.f90:617-658). */
+int gb_particles_set_Z(gb_particles_t *p, const int *Z);
+/* Stream used for the particles' uploads (NULL = a stream owned by p). */
+int gb_particles_set_stream(gb_particles_t *p, void *cuda_stream);
+
+/* ------------------------------------------------------------------------
+ * Neighbour list — replaces neighbors_t (python_neighbors.f90:51-139).
+ * ---------------------------------------------------------------------- */
+/* neighbors_new(avgn) (neighbors_wrap.f90) */
+int gb_neighbors_new(gb_neighbors_t **nl, int avgn);
+void gb_neighbors_free(gb_neighbors_t *nl);
+/* request_interaction_range (python_neighbors.f90:381-403) */
+int gb_neighbors_request_interaction_range(gb_neighbors_t *nl, double cutoff);
+double gb_neighbors_get_interaction_range(const gb_neighbors_t *nl);
+/* neighbors_update (python_neighbors.f90:430-456): rebuilds the full
+ * directed list if positions or cell changed. */
+int gb_neighbors_update(gb_neighbors_t *nl, gb_particles_t *p);
+/* Number of list entries after the last update (get_number_of_all_neighbors). */
+int64_t gb_neighbors_get_size(const gb_neighbors_t *nl);
+/* Copies the list (f_get_all_neighbors, neighbors_wrap.f90:425-455):
+ * seed (nat+1 CSR offsets, int64), j (n, 0-based) and integer image shifts
+ * dc (n,3) such that r_i - r_j + cell^T dc is the pair vector.  Any pointer
+ * may be NULL; host or device memory. */
+int gb_neighbors_get(gb_neighbors_t *nl, gb_particles_t *p, int64_t *seed, int *j,
+                     int *dc);
+int gb_neighbors_set_stream(gb_neighbors_t *nl, void *cuda_stream);
+
+/* ------------------------------------------------------------------------
+ * Potentials — replace the generated shims python_<mod>_{new, free,
+ * init_without_parameters, bind_to, energy_and_forces}
+ * (gen_factory.py:98-356; prototypes :380-401).
+ * ---------------------------------------------------------------------- */
+
+/* Tersoff parameter set: layout of BOP_DB_TYPE
+ * (src/potentials/bop/tersoff/tersoff_params.f90:27-97), 0-based element and
+ * symmetric pair indices (src/macros.inc:123). */
+typedef struct gb_tersoff_params {
+  int nel;
+  int Z[3];
+  double A[6], B[6], xi[6], lambda[6], mu[6], omega[6], mubo[6];
+  int m[6];
+  double beta[3], n[3], c[3], d[3], h[3];
+  double r1[6], r2[6];
+} gb_tersoff_params_t;
+
+/* Kumagai parameter set (src/potentials/bop/kumagai/kumagai_params.f90:27-96). */
+typedef struct gb_kumagai_params {
+  int nel;
+  int Z[1];
+  double A[1], B[1], lambda1[1], lambda2[1];
+  double eta[1], delta[1], alpha[1];
+  int beta[1];
+  double c1[1], c2[1], c3[1], c4[1], c5[1], h[1];
+  double r1[1], r2[1];
+} gb_kumagai_params_t;
+
+/* python_tersoff_new + register (parameters set through a struct instead of
+ * the ptrdict config tree, tersoff_registry.f90:22-115). params may be NULL
+ * for the default Tersoff_PRB_39_5566_SiC set (tersoff_params.f90:99-138). */
+int gb_tersoff_new(gb_potential_t **pot, const gb_tersoff_params_t *params);
+/* python_kumagai_new; NULL = Kumagai_CompMaterSci_39_457_Si
+ * (kumagai_params.f90:97-132). */
+int gb_kumagai_new(gb_potential_t **pot, const gb_kumagai_params_t *params);
+/* python_tabulated_alloy_eam_new + init(fn=...) (tabulated_alloy_eam.f90:147-259):
+ * reads a DYNAMO setfl file. */
+int gb_tabulated_alloy_eam_new(gb_potential_t **pot, const char *fn);
+/* python_<mod>_free */
+void gb_potential_free(gb_potential_t *pot);
+/* GB_PRECISION_FP64 (default) or GB_PRECISION_MIXED (BOP only). */
+int gb_potential_set_precision(gb_potential_t *pot, int precision);
+int gb_potential_set_stream(gb_potential_t *pot, void *cuda_stream);
+/* Interaction cutoff the potential requests for the pair (Z1, Z2). */
+double gb_potential_get_cutoff(const gb_potential_t *pot);
+
+/* python_<mod>_bind_to (gen_factory.py:219-237 -> BIND_TO_FUNC,
+ * default_bind_to_func.f90:25-146; tabulated_alloy_eam.f90:297-350):
+ * maps elements and requests the interaction range on nl. */
+int gb_potential_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                         int *ierror);
+
+/* python_<mod>_energy_and_forces (gen_factory.py:239-356 -> COMPUTE_FUNC,
+ * default_compute_func.f90:25-100; tabulated_alloy_eam.f90:360-415).
+ * q (charges) is accepted and ignored, as by these potentials. */
+int gb_potential_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                                   const double *q, double *epot, double *f, double *wpot,
+                                   const int *mask, double *epot_per_at, double *epot_per_bond,
+                                   double *f_per_bond, double *wpot_per_at,
+                                   double *wpot_per_bond, int *ierror);
+
+/* Per-class aliases with the reference's shim names' shape. */
+int gb_tersoff_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                       int *ierror);
+int gb_tersoff_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                                 const double *q, double *epot, double *f, double *wpot,
+                                 const int *mask, double *epot_per_at, double *epot_per_bond,
+                                 double *f_per_bond, double *wpot_per_at,
+                                 double *wpot_per_bond, int *ierror);
+int gb_kumagai_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                       int *ierror);
+int gb_kumagai_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                                 const double *q, double *epot, double *f, double *wpot,
+                                 const int *mask, double *epot_per_at, double *epot_per_bond,
+                                 double *f_per_bond, double *wpot_per_at,
+                                 double *wpot_per_bond, int *ierror);
+int gb_tabulated_alloy_eam_bind_to(gb_potential_t *pot, gb_particles_t *p,
+                                   gb_neighbors_t *nl, int *ierror);
+int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *pot, gb_particles_t *p,
+                                             gb_neighbors_t *nl, const double *q, double *epot,
+                                             double *f, double *wpot, const int *mask,
+                                             double *epot_per_at, double *wpot_per_at,
+                                             int *ierror);
+
+/* Spline table export of an EAM potential (for parity checks of the host
+ * setfl reader and spline builder against simple_spline_init,
+ * simple_spline.f90:127-195): which = 0 F(rho), 1 rho(r), 2 phi(r) (index
+ * i*nel+j).  Returns the number of points n; x0dx = {x0, dx, cut}; coef is
+ * (8, n): y, d2y, c1, c2, c3, d1, d2, d3 (last column of the 6 interval
+ * arrays is 0).  coef may be NULL. */
+int gb_tabulated_alloy_eam_table(const gb_potential_t *pot, int which, int idx, double *x0dx,
+                                 double *coef);
+
+/* Timing of the last energy_and_forces call's phases in milliseconds
+ * (CUDA events on the potential's stream): [0] neighbour build,
+ * [1] force kernels, [2] total device time.  Returns 0. */
+int gb_potential_last_timing(const gb_potential_t *pot, double *ms3);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATOMISTICA_GB300_H */

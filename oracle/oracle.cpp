@@ -1,0 +1,1303 @@
+// ============================================================================
+// TEST INFRASTRUCTURE ONLY — the CPU FP64 oracle.
+//
+// A plain C++17 (+OpenMP) restatement of Atomistica's per-step force path, used
+// by tests/ as the checker and by bench.py as the timed CPU baseline.  Nothing
+// in the atomistica_gb300 product links, loads or calls this file.
+//
+// Every routine follows the reference loop structure and operation order:
+//   * neighbour list      src/python/f90/python_neighbors.f90:570-959
+//   * reciprocal cell     src/support/f_linearalgebra.f90:505-552 (gauss)
+//   * BOP kernel          src/potentials/bop/bop_kernel.f90:420-1068, 1074-1529,
+//                         1613-1628 (non-screened branch)
+//   * BOP glue            src/potentials/bop/default_bind_to_func.f90:73-144,
+//                         src/potentials/bop/default_compute_func.f90:54-95
+//   * Tersoff functions   src/potentials/bop/tersoff/tersoff_func.f90:32-232
+//   * Kumagai functions   src/potentials/bop/kumagai/kumagai_func.f90:32-242
+//   * trig_off cutoff     src/support/cutoff.f90:152-196
+//   * cubic spline        src/support/simple_spline.f90:127-195, 373-651, 756-773
+//   * alloy EAM           src/potentials/eam/tabulated_alloy_eam.f90:147-259,
+//                         423-627
+//   * pair index          src/macros.inc:123
+//
+// Parity pins: the reference ships no golden energy/force vectors and its
+// Fortran cannot be compiled here (no Fortran compiler).  The oracle is pinned
+// by the reference's own known-answer tests re-expressed without ASE (see
+// tests/test_oracle_pins.py): FD force/virial consistency, the Si(100)
+// surface energy 2.309 J/m^2, bulk Ec/a0/elastic constants within 5 %, mask
+// additivity, the pbc bit-equality and the neighbour-list tests.
+//
+// Build with -ffp-contract=off so that the FP64 distance tests follow the
+// reference operation order exactly (no fused multiply-add).
+// ============================================================================
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Cell geometry.  A[a][k] is Fortran Abox(a,k): column k is lattice vector k.
+// ---------------------------------------------------------------------------
+
+struct Box {
+  double A[3][3];
+  double B[3][3];  // A^-1 (Bbox)
+  int pbc[3];
+};
+
+// Gauss elimination with the pivot choice of gauss() in
+// src/support/f_linearalgebra.f90:505-552, applied to each unit vector as in
+// gaussn (:599-637, the non-LAPACK branch).
+int gauss_solve(const double Ain[3][3], const double b[3], double x[3]) {
+  const int n = 3;
+  double A[3][4];
+  for (int j = 0; j < n; j++) {
+    for (int k = 0; k < n; k++) A[j][k] = Ain[j][k];
+    A[j][n] = b[j];
+  }
+  int indx[3] = {0, 0, 0};  // 0 = not yet used as pivot, else pivot step (1-based)
+  for (int i = 0; i < n; i++) {
+    int max_indx = -1;
+    double maxv = -1.0;
+    for (int j = 0; j < n; j++) {
+      if (indx[j] != 0) continue;
+      double v = std::fabs(A[j][i]);
+      if (v > maxv) {
+        maxv = v;
+        max_indx = j;
+      }
+    }
+    indx[max_indx] = i + 1;
+    if (A[max_indx][i] == 0.0) return -1;
+    double fac[3], row[4];
+    for (int j = 0; j < n; j++) fac[j] = A[j][i] / A[max_indx][i];
+    for (int k = 0; k < n + 1; k++) row[k] = A[max_indx][k];
+    for (int j = 0; j < n; j++) {
+      if (indx[j] != 0) continue;
+      for (int k = i; k < n + 1; k++) A[j][k] = A[j][k] - fac[j] * row[k];
+    }
+  }
+  double Ap[3][4];
+  for (int j = 0; j < n; j++)
+    for (int k = 0; k < n + 1; k++) Ap[indx[j] - 1][k] = A[j][k];
+  for (int j = n - 1; j >= 0; j--) {
+    if (Ap[j][j] == 0.0) return -1;
+    x[j] = Ap[j][n] / Ap[j][j];
+    for (int m = 0; m < j; m++) Ap[m][n] = Ap[m][n] - Ap[m][j] * x[j];
+  }
+  return 0;
+}
+
+int make_box(const double *cell_rows, const int *pbc, Box &box) {
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 3; k++) box.A[a][k] = cell_rows[3 * k + a];
+  for (int c = 0; c < 3; c++) {
+    double e[3] = {0, 0, 0}, x[3];
+    e[c] = 1.0;
+    if (gauss_solve(box.A, e, x) != 0) return -1;
+    for (int a = 0; a < 3; a++) box.B[a][c] = x[a];
+  }
+  for (int k = 0; k < 3; k++) box.pbc[k] = pbc[k] != 0;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour list: python_neighbors.f90 binning_init (:765-871), binning_update
+// (:904-959) and fill_neighbor_list (:570-754).  Compact CSR instead of the
+// sentinel-separated per-thread chunks; same per-atom entry order.
+// ---------------------------------------------------------------------------
+
+struct NList {
+  std::vector<int64_t> seed;  // nat+1 CSR offsets
+  std::vector<int> nbr;
+  std::vector<int> dc;  // 3 ints per entry
+};
+
+struct Binning {
+  int n_cells[3];
+  double rec[3][3];
+  int dx, dy, dz;
+  std::vector<int> d;  // 3 per stencil entry
+};
+
+void binning_init(const Box &box, double cutoff, double bin_size, Binning &bn) {
+  double box_size[3];
+  for (int x = 0; x < 3; x++) {
+    double s = 0.0;
+    for (int a = 0; a < 3; a++) s = s + box.A[a][x] * box.A[a][x];
+    box_size[x] = std::sqrt(s);
+  }
+  for (int x = 0; x < 3; x++) {
+    int nc = (int)(box_size[x] / bin_size);
+    bn.n_cells[x] = nc < 3 ? 3 : nc;
+  }
+  double cs[3][3];  // cs[a][x] = cell_size(a, x)
+  for (int x = 0; x < 3; x++) {
+    for (int a = 0; a < 3; a++) cs[a][x] = box.A[a][x] / bn.n_cells[x];
+    for (int k = 0; k < 3; k++) bn.rec[x][k] = box.B[x][k] * bn.n_cells[x];
+  }
+  auto col = [&](int x, double v[3]) {
+    for (int a = 0; a < 3; a++) v[a] = cs[a][x];
+  };
+  auto cross = [](const double u[3], const double v[3], double w[3]) {
+    w[0] = u[1] * v[2] - u[2] * v[1];
+    w[1] = u[2] * v[0] - u[0] * v[2];
+    w[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  auto dot = [](const double u[3], const double v[3]) {
+    double s = u[0] * v[0];
+    s = s + u[1] * v[1];
+    s = s + u[2] * v[2];
+    return s;
+  };
+  double c1[3], c2[3], c3[3], nx[3], ny[3], nz[3];
+  col(0, c1);
+  col(1, c2);
+  col(2, c3);
+  cross(c2, c3, nx);
+  cross(c3, c1, ny);
+  cross(c1, c2, nz);
+  double cv = dot(c1, nx);
+  // nx = cv*nx/dot_product(nx, nx) etc. (python_neighbors.f90:838-840); the
+  // right-hand side uses the old vector.
+  const double dnx = dot(nx, nx), dny = dot(ny, ny), dnz = dot(nz, nz);
+  for (int a = 0; a < 3; a++) {
+    nx[a] = cv * nx[a] / dnx;
+    ny[a] = cv * ny[a] / dny;
+    nz[a] = cv * nz[a] / dnz;
+  }
+  bn.dx = (int)(cutoff / std::sqrt(dot(nx, nx))) + 1;
+  bn.dy = (int)(cutoff / std::sqrt(dot(ny, ny))) + 1;
+  bn.dz = (int)(cutoff / std::sqrt(dot(nz, nz))) + 1;
+  bn.d.clear();
+  for (int x = -bn.dx; x <= bn.dx; x++)
+    for (int y = -bn.dy; y <= bn.dy; y++)
+      for (int z = -bn.dz; z <= bn.dz; z++) {
+        bn.d.push_back(x);
+        bn.d.push_back(y);
+        bn.d.push_back(z);
+      }
+}
+
+// floor(matmul(rec_cell_size, r)) (0-based), python_neighbors.f90:641.
+inline void raw_cell(const Binning &bn, const double *ri, int c[3]) {
+  for (int x = 0; x < 3; x++) {
+    double s = bn.rec[x][0] * ri[0];
+    s = s + bn.rec[x][1] * ri[1];
+    s = s + bn.rec[x][2] * ri[2];
+    c[x] = (int)std::floor(s);
+  }
+}
+
+int build_neighbors(int nat, const double *r, const Box &box, double cutoff,
+                    NList &nl) {
+  Binning bn;
+  binning_init(box, cutoff, cutoff, bn);
+  const int ncx = bn.n_cells[0], ncy = bn.n_cells[1], ncz = bn.n_cells[2];
+  // binning_update: singly linked list per cell in increasing atom id.
+  std::vector<int> seed((size_t)ncx * ncy * ncz, -1), last(seed.size(), -1),
+      next(nat, -1);
+  for (int i = 0; i < nat; i++) {
+    int c[3];
+    raw_cell(bn, &r[3 * i], c);
+    for (int k = 0; k < 3; k++) {
+      const int n = bn.n_cells[k];
+      if (box.pbc[k]) {
+        while (c[k] < 0) c[k] += n;
+        while (c[k] > n - 1) c[k] -= n;
+      } else {
+        if (c[k] < 0) c[k] = 0;
+        if (c[k] > n - 1) c[k] = n - 1;
+      }
+    }
+    size_t ci = ((size_t)c[2] * ncy + c[1]) * ncx + c[0];
+    if (seed[ci] == -1) {
+      seed[ci] = i;
+      last[ci] = i;
+    } else {
+      next[last[ci]] = i;
+      last[ci] = i;
+    }
+  }
+  const double cutoff_sq = cutoff * cutoff;
+  const int n_d = (int)bn.d.size() / 3;
+  // Per-atom lists are built independently, then concatenated in atom order.
+  std::vector<std::vector<int>> lj(nat), ls(nat);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < nat; i++) {
+    int celli[3], shift[3] = {0, 0, 0};
+    raw_cell(bn, &r[3 * i], celli);
+    for (int k = 0; k < 3; k++) {
+      const int n = bn.n_cells[k];
+      if (box.pbc[k]) {
+        while (celli[k] < 0) {
+          celli[k] += n;
+          shift[k] += 1;
+        }
+        while (celli[k] > n - 1) {
+          celli[k] -= n;
+          shift[k] -= 1;
+        }
+      } else {
+        if (celli[k] < 0) celli[k] = 0;
+        if (celli[k] > n - 1) celli[k] = n - 1;
+      }
+    }
+    for (int x = 0; x < n_d; x++) {
+      int cur[3], shift1[3];
+      for (int k = 0; k < 3; k++) {
+        cur[k] = celli[k] + bn.d[3 * x + k];
+        shift1[k] = shift[k];
+      }
+      bool exists = true;
+      for (int k = 0; k < 3; k++) {
+        const int n = bn.n_cells[k];
+        if (box.pbc[k]) {
+          while (cur[k] < 0) {
+            cur[k] += n;
+            shift1[k] += 1;
+          }
+          while (cur[k] > n - 1) {
+            cur[k] -= n;
+            shift1[k] -= 1;
+          }
+        }
+        if (cur[k] < 0 || cur[k] > n - 1) exists = false;
+      }
+      if (!exists) continue;
+      int j = seed[((size_t)cur[2] * ncy + cur[1]) * ncx + cur[0]];
+      while (j != -1) {
+        int cellj[3], shift2[3];
+        raw_cell(bn, &r[3 * j], cellj);
+        for (int k = 0; k < 3; k++) {
+          shift2[k] = shift1[k];
+          const int n = bn.n_cells[k];
+          if (box.pbc[k]) {
+            while (cellj[k] < 0) {
+              cellj[k] += n;
+              shift2[k] -= 1;
+            }
+            while (cellj[k] > n - 1) {
+              cellj[k] -= n;
+              shift2[k] += 1;
+            }
+          }
+        }
+        if (i != j || shift2[0] != 0 || shift2[1] != 0 || shift2[2] != 0) {
+          // delta_r = r_i - r_j + matmul(Abox, shift2)   (:708)
+          double dr[3];
+          for (int a = 0; a < 3; a++) {
+            double as = box.A[a][0] * (double)shift2[0];
+            as = as + box.A[a][1] * (double)shift2[1];
+            as = as + box.A[a][2] * (double)shift2[2];
+            dr[a] = (r[3 * i + a] - r[3 * j + a]) + as;
+          }
+          double d2 = dr[0] * dr[0];
+          d2 = d2 + dr[1] * dr[1];
+          d2 = d2 + dr[2] * dr[2];
+          if (d2 < cutoff_sq) {
+            lj[i].push_back(j);
+            ls[i].push_back(shift2[0]);
+            ls[i].push_back(shift2[1]);
+            ls[i].push_back(shift2[2]);
+          }
+        }
+        j = next[j];
+      }
+    }
+  }
+  nl.seed.assign(nat + 1, 0);
+  for (int i = 0; i < nat; i++) nl.seed[i + 1] = nl.seed[i] + (int64_t)lj[i].size();
+  nl.nbr.resize(nl.seed[nat]);
+  nl.dc.resize(3 * nl.seed[nat]);
+  for (int i = 0; i < nat; i++) {
+    std::copy(lj[i].begin(), lj[i].end(), nl.nbr.begin() + nl.seed[i]);
+    std::copy(ls[i].begin(), ls[i].end(), nl.dc.begin() + 3 * nl.seed[i]);
+  }
+  return 0;
+}
+
+// Pair index, src/macros.inc:123 (0-based in and out).
+inline int pair_index(int i, int j, int nel) {
+  int a = std::min(i + j * nel, j + i * nel);
+  int b = std::min(i * (i + 1) / 2, j * (j + 1) / 2);
+  return a - b;
+}
+
+// trig_off cutoff, src/support/cutoff.f90:152-196.
+struct TrigOff {
+  double r1, r2, fac;
+  void init(double a, double b) {
+    r1 = a;
+    r2 = b;
+    fac = M_PI / (r2 - r1);
+  }
+  void f(double r, double &val, double &dval) const {
+    if (r <= r1) {
+      val = 1.0;
+      dval = 0.0;
+    } else if (r >= r2) {
+      val = 0.0;
+      dval = 0.0;
+    } else {
+      double x = fac * (r - r1);
+      val = 0.5 * (1.0 + std::cos(x));
+      dval = -0.5 * fac * std::sin(x);
+    }
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Parameter sets (layout of BOP_DB_TYPE, tersoff_params.f90:27-97 and
+// kumagai_params.f90:27-96; 0-based element/pair indices).
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+struct orc_tersoff_params {
+  int nel;
+  int Z[3];
+  double A[6], B[6], xi[6], lambda[6], mu[6], omega[6], mubo[6];
+  int m[6];
+  double beta[3], n[3], c[3], d[3], h[3];
+  double r1[6], r2[6];
+};
+
+struct orc_kumagai_params {
+  int nel;
+  int Z[1];
+  double A[1], B[1], lambda1[1], lambda2[1];
+  double eta[1], delta[1], alpha[1];
+  int beta[1];
+  double c1[1], c2[1], c3[1], c4[1], c5[1], h[1];
+  double r1[1], r2[1];
+};
+
+}  // extern "C"
+
+namespace {
+
+// Tersoff functional form, tersoff_func.f90:32-232.
+struct TersoffFn {
+  const orc_tersoff_params &p;
+  explicit TersoffFn(const orc_tersoff_params &q) : p(q) {}
+  int nel() const { return p.nel; }
+  double r1(int ij) const { return p.r1[ij]; }
+  double r2(int ij) const { return p.r2[ij]; }
+  void VA(int ij, double dr, double &val, double &dval) const {
+    double e = std::exp(-p.mu[ij] * dr);
+    val = -p.B[ij] * e;
+    dval = p.B[ij] * p.mu[ij] * e;
+  }
+  void VR(int ij, double dr, double &val, double &dval) const {
+    double e = std::exp(-p.lambda[ij] * dr);
+    val = p.A[ij] * e;
+    dval = -p.A[ij] * p.lambda[ij] * e;
+  }
+  void g(int ktypi, int ikpot, double costh, double &val, double &dval) const {
+    double omega = p.omega[ikpot];
+    double h_c = p.h[ktypi] - costh;
+    double c_sq = p.c[ktypi] * p.c[ktypi];
+    double d_sq = p.d[ktypi] * p.d[ktypi];
+    double h = d_sq + h_c * h_c;
+    val = omega * (1.0 + c_sq / d_sq - c_sq / h);
+    dval = -2 * omega * c_sq * h_c / (h * h);
+  }
+  void bo(int ktypi, int ijpot, double zij, double fcij, double faij, double &bij,
+          double &dfbij) const {
+    if (zij > 0.0) {
+      double e = -0.5 / p.n[ktypi];
+      double b = std::pow(p.beta[ktypi], p.n[ktypi]);
+      double arg = 1.0 + b * std::pow(zij, p.n[ktypi]);
+      bij = p.xi[ijpot] * std::pow(arg, e);
+      dfbij = -0.25 * fcij * faij * p.xi[ijpot] * b * std::pow(zij, p.n[ktypi] - 1.0) *
+              std::pow(arg, e - 1.0);
+    } else {
+      bij = 1.0;
+      dfbij = 0.0;
+    }
+  }
+  void h(int ikpot, double dr, double &val, double &dval) const {
+    double mu = p.mubo[ikpot];
+    if (mu == 0.0) {
+      val = 1.0;
+      dval = 0.0;
+    } else {
+      int m = p.m[ikpot];
+      if (m == 1) {
+        val = std::exp(2 * mu * dr);
+        dval = 2 * mu * val;
+      } else if (m == 3) {
+        double arg = 2 * mu * dr;
+        val = std::exp(arg * arg * arg);
+        dval = 2 * mu * m * arg * arg * val;
+      } else {
+        val = std::exp(std::pow(2 * mu * dr, m));
+        dval = 2 * mu * m * std::pow(2 * mu * dr, m - 1) * val;
+      }
+    }
+  }
+};
+
+// Kumagai functional form, kumagai_func.f90:32-242.
+struct KumagaiFn {
+  const orc_kumagai_params &p;
+  explicit KumagaiFn(const orc_kumagai_params &q) : p(q) {}
+  int nel() const { return p.nel; }
+  double r1(int ij) const { return p.r1[ij]; }
+  double r2(int ij) const { return p.r2[ij]; }
+  void VA(int ij, double dr, double &val, double &dval) const {
+    double e = std::exp(-p.lambda2[ij] * dr);
+    val = -p.B[ij] * e;
+    dval = p.B[ij] * p.lambda2[ij] * e;
+  }
+  void VR(int ij, double dr, double &val, double &dval) const {
+    double e = std::exp(-p.lambda1[ij] * dr);
+    val = p.A[ij] * e;
+    dval = -p.A[ij] * p.lambda1[ij] * e;
+  }
+  void g(int ktypi, int /*ikpot*/, double costh, double &val, double &dval) const {
+    double c1 = p.c1[ktypi], c2 = p.c2[ktypi], c3 = p.c3[ktypi], c4 = p.c4[ktypi],
+           c5 = p.c5[ktypi], h = p.h[ktypi];
+    double h_cos = h - costh;
+    double h_cos_sq = h_cos * h_cos;
+    double tmp = h_cos / (c3 + h_cos_sq);
+    double go = c2 * tmp;
+    double ga1 = c4 * std::exp(-c5 * h_cos_sq);
+    double v = go * (1.0 + ga1);
+    dval = -2 * (1.0 - h_cos * tmp) * v + 2 * c5 * h_cos_sq * go * ga1;
+    val = c1 + h_cos * v;
+  }
+  void bo(int ktypi, int /*ijpot*/, double zij, double fcij, double faij, double &bij,
+          double &dfbij) const {
+    if (zij > 0.0) {
+      double eta = p.eta[ktypi];
+      double delta = -p.delta[ktypi];
+      double arg = 1.0 + std::pow(zij, eta);
+      bij = std::pow(arg, delta);
+      dfbij = 0.5 * fcij * faij * eta * std::pow(zij, eta - 1.0) * delta *
+              std::pow(arg, delta - 1.0);
+    } else {
+      bij = 1.0;
+      dfbij = 0.0;
+    }
+  }
+  void h(int ikpot, double dr, double &val, double &dval) const {
+    double alpha = p.alpha[ikpot];
+    if (alpha == 0.0) {
+      val = 1.0;
+      dval = 0.0;
+    } else {
+      int beta = p.beta[ikpot];
+      if (beta == 1) {
+        val = std::exp(alpha * dr);
+        dval = alpha * val;
+      } else if (beta == 3) {
+        // kumagai_func.f90:211-213 omits alpha in the exponent; kept as is.
+        val = std::exp(dr * dr * dr);
+        dval = 3 * alpha * dr * dr * val;
+      } else {
+        val = std::exp(alpha * std::pow(dr, beta));
+        dval = beta * alpha * std::pow(dr, beta - 1) * val;
+      }
+    }
+  }
+};
+
+struct BopOut {
+  double *epot, *f, *wpot, *epot_per_at, *epot_per_bond, *f_per_bond, *wpot_per_at,
+      *wpot_per_bond;
+};
+
+// BOP_KERNEL, bop_kernel.f90 (non-screened, PYTHON build).  el[i] is the
+// 0-based database index or -1.  Per-bond outputs are indexed by the compact
+// neighbour-list slot (the reference's nbb).
+template <class Fn>
+int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int *el,
+               const NList &nl, const int *mask, const BopOut &o, int nthreads) {
+  const int nel = fn.nel();
+  const int npairs = nel * (nel + 1) / 2;
+  std::vector<TrigOff> cut_in(npairs);
+  std::vector<double> cut_in_l(npairs), cut_in_h(npairs), cut_in_h2(npairs);
+  for (int i = 0; i < npairs; i++) {
+    cut_in[i].init(fn.r1(i), fn.r2(i));
+    cut_in_l[i] = fn.r1(i);
+    cut_in_h[i] = fn.r2(i);
+    cut_in_h2[i] = fn.r2(i) * fn.r2(i);
+  }
+  // Pass 1 (bop_kernel.f90:562-1068): internal short bond list.
+  struct Bond {
+    int j, nbb, typ;
+    int dc[3];
+    double len, nm[3], fc, dfc;
+  };
+  std::vector<int64_t> neb_seed(nat + 1, 0);
+  std::vector<std::vector<Bond>> bonds_of(nat);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+  for (int i = 0; i < nat; i++) {
+    const int eli = el[i];
+    if (eli < 0) continue;
+    for (int64_t jn = nl.seed[i]; jn < nl.seed[i + 1]; jn++) {
+      const int j = nl.nbr[jn];
+      const int elj = el[j];
+      if (elj < 0) continue;
+      const int *dc = &nl.dc[3 * jn];
+      double rij[3];
+      for (int a = 0; a < 3; a++) {
+        double as = box.A[a][0] * (double)dc[0];
+        as = as + box.A[a][1] * (double)dc[1];
+        as = as + box.A[a][2] * (double)dc[2];
+        rij[a] = (r[3 * j + a] - r[3 * i + a]) - as;
+      }
+      double rlij = rij[0] * rij[0];
+      rlij = rlij + rij[1] * rij[1];
+      rlij = rlij + rij[2] * rij[2];
+      const int el2ij = pair_index(eli, elj, nel);
+      Bond b;
+      b.j = j;
+      b.nbb = (int)jn;
+      b.typ = el2ij;
+      b.dc[0] = dc[0];
+      b.dc[1] = dc[1];
+      b.dc[2] = dc[2];
+      if (rlij < cut_in_l[el2ij] * cut_in_l[el2ij]) {
+        b.fc = 1.0;
+        b.dfc = 0.0;
+      } else if (rlij < cut_in_h2[el2ij]) {
+        double rl = std::sqrt(rlij);
+        cut_in[el2ij].f(rl, b.fc, b.dfc);
+      } else {
+        continue;
+      }
+      rlij = std::sqrt(rlij);
+      b.len = rlij;
+      for (int a = 0; a < 3; a++) b.nm[a] = rij[a] / rlij;
+      bonds_of[i].push_back(b);
+    }
+  }
+  int nebmax = 0;
+  for (int i = 0; i < nat; i++) nebmax = std::max(nebmax, (int)bonds_of[i].size());
+
+  // Pass 2 (bop_kernel.f90:1074-1529) with thread-private pe/f/wpot_per_at
+  // (tls.f90) reduced in thread order at the end.
+  int nt = nthreads;
+  std::vector<std::vector<double>> tpe(nt), tf(nt), twat(nt);
+  std::vector<double> twpot(9 * nt, 0.0);
+  const bool want_wat = o.wpot_per_at != nullptr;
+#pragma omp parallel num_threads(nthreads)
+  {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#else
+    const int tid = 0;
+#endif
+    std::vector<double> &pe = tpe[tid];
+    std::vector<double> &f = tf[tid];
+    std::vector<double> &wat = twat[tid];
+    pe.assign(nat, 0.0);
+    f.assign(3 * (size_t)nat, 0.0);
+    if (want_wat) wat.assign(9 * (size_t)nat, 0.0);
+    double wpot[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    std::vector<double> dbidk(3 * (size_t)std::max(nebmax, 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < nat; i++) {
+      const int eli = el[i];
+      if (eli < 0) continue;
+      double fi[3] = {0, 0, 0};
+      const std::vector<Bond> &bi = bonds_of[i];
+      const int nb = (int)bi.size();
+      for (int ij = 0; ij < nb; ij++) {
+        const Bond &B = bi[ij];
+        const int j = B.j;
+        int maskfac = 2;
+        if (mask) {
+          if (mask[i] == 0 && mask[j] == 0)
+            maskfac = 0;
+          else if (mask[i] == 0 || mask[j] == 0)
+            maskfac = 1;
+        }
+        const int el2ij = B.typ;
+        double rlij = B.len;
+        if (!(maskfac > 0 && rlij < cut_in_h[el2ij])) continue;
+        double fj[3] = {0, 0, 0};
+        const int elj = el[j];
+        (void)elj;
+        const double rlijr = 1.0 / rlij;
+        double rnij[3] = {B.nm[0], B.nm[1], B.nm[2]};
+        double rij[3] = {rlij * rnij[0], rlij * rnij[1], rlij * rnij[2]};
+        const double fcarij = B.fc, dfcarijr = B.dfc;
+        double VAij, dVAij, VRij, dVRij;
+        fn.VA(el2ij, rlij, VAij, dVAij);
+        fn.VR(el2ij, rlij, VRij, dVRij);
+        VAij = 0.5 * maskfac * VAij;
+        dVAij = 0.5 * maskfac * dVAij;
+        VRij = 0.5 * maskfac * VRij;
+        dVRij = 0.5 * maskfac * dVRij;
+        double wij[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double wijb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double zij = 0.0;
+        double dbidi[3] = {0, 0, 0}, dbidj[3] = {0, 0, 0};
+        for (int ik = 0; ik < nb; ik++) {
+          if (ik == ij) continue;
+          const Bond &K = bi[ik];
+          const int ikpot = K.typ;
+          const double rlik = K.len;
+          if (!(rlik < cut_in_h[ikpot])) {
+            dbidk[3 * ik] = dbidk[3 * ik + 1] = dbidk[3 * ik + 2] = 0.0;
+            continue;
+          }
+          const double *rnik = K.nm;
+          double rik[3] = {rlik * rnik[0], rlik * rnik[1], rlik * rnik[2]};
+          const double fcik = K.fc, dfcikr = K.dfc;
+          double h_Dr, dh_dDr;
+          fn.h(ikpot, rlij - rlik, h_Dr, dh_dDr);
+          double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
+          double g_costh, dg_dcosth;
+          fn.g(eli, ikpot, costh, g_costh, dg_dcosth);
+          double dkc[3];
+          for (int a = 0; a < 3; a++) dkc[a] = rnik[a] * rlik - rnij[a] * rlij;
+          double disjk = std::sqrt(dkc[0] * dkc[0] + dkc[1] * dkc[1] + dkc[2] * dkc[2]);
+          for (int a = 0; a < 3; a++) dkc[a] = dkc[a] / disjk;
+          const double dcsdij = 1.0 / rlik - costh * rlijr;
+          const double dcsdik = rlijr - costh / rlik;
+          const double dcsdjk = -disjk * rlijr / rlik;
+          double dcsdi[3], dcsdj[3], dcsdk[3];
+          for (int a = 0; a < 3; a++) {
+            dcsdi[a] = -dcsdij * rnij[a] - dcsdik * rnik[a];
+            dcsdj[a] = dcsdij * rnij[a] - dcsdjk * dkc[a];
+            dcsdk[a] = dcsdik * rnik[a] + dcsdjk * dkc[a];
+          }
+          const double dzfac = fcik * dg_dcosth * h_Dr;
+          double dgdi[3], dgdj[3], dgdk[3];
+          for (int a = 0; a < 3; a++) {
+            dgdi[a] = dzfac * dcsdi[a];
+            dgdj[a] = dzfac * dcsdj[a];
+            dgdk[a] = dzfac * dcsdk[a];
+          }
+          zij = zij + fcik * g_costh * h_Dr;
+          const double dzdrij = g_costh * fcik * dh_dDr;
+          const double dzdrik = g_costh * (dfcikr * h_Dr - fcik * dh_dDr);
+          double df[3];
+          for (int a = 0; a < 3; a++) {
+            dbidi[a] = dbidi[a] - dzdrij * rnij[a] - dzdrik * rnik[a] + dgdi[a];
+            df[a] = dzdrij * rnij[a] + dgdj[a];
+            dbidj[a] = dbidj[a] + df[a];
+            dbidk[3 * ik + a] = dzdrik * rnik[a] + dgdk[a];
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++)
+              wijb[a][c] = wijb[a][c] - rij[a] * df[c] - rik[a] * dbidk[3 * ik + c];
+        }
+        double bij, dbij_dzij;
+        fn.bo(eli, el2ij, zij, fcarij, VAij, bij, dbij_dzij);
+        double dffac = 0.5 * fcarij * (VRij + bij * VAij);
+        pe[i] = pe[i] + dffac;
+        pe[j] = pe[j] + dffac;
+        if (o.epot_per_bond) o.epot_per_bond[B.nbb] += dffac;
+        dffac = 0.5 * (dVRij * fcarij + bij * dVAij * fcarij + VRij * dfcarijr +
+                       bij * VAij * dfcarijr);
+        double df[3];
+        for (int a = 0; a < 3; a++) {
+          df[a] = dffac * rnij[a];
+          fi[a] = fi[a] + df[a];
+          fj[a] = fj[a] - df[a];
+        }
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++)
+            wij[a][c] = wij[a][c] + rij[a] * df[c] - dbij_dzij * wijb[a][c];
+        if (o.f_per_bond)
+          for (int a = 0; a < 3; a++) o.f_per_bond[3 * (size_t)B.nbb + a] += df[a];
+        for (int a = 0; a < 3; a++) fi[a] = fi[a] - dbij_dzij * dbidi[a];
+        for (int a = 0; a < 3; a++) fj[a] = fj[a] - dbij_dzij * dbidj[a];
+        for (int ik = 0; ik < nb; ik++) {
+          if (ik == ij) continue;  // k == j and kdc == jdc (:1459)
+          const int k = bi[ik].j;
+          for (int a = 0; a < 3; a++)
+            f[3 * (size_t)k + a] += -dbij_dzij * dbidk[3 * ik + a];
+        }
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++) wpot[a][c] += wij[a][c];
+        if (o.wpot_per_bond)
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++)
+              o.wpot_per_bond[9 * (size_t)B.nbb + 3 * c + a] += wij[a][c];
+        if (want_wat)
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) {
+              wat[9 * (size_t)i + 3 * c + a] += wij[a][c] / 2;
+              wat[9 * (size_t)j + 3 * c + a] += wij[a][c] / 2;
+            }
+        for (int a = 0; a < 3; a++) f[3 * (size_t)j + a] += fj[a];
+      }
+      for (int a = 0; a < 3; a++) f[3 * (size_t)i + a] += fi[a];
+    }
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) twpot[9 * tid + 3 * a + c] = wpot[a][c];
+  }
+  // Reductions (bop_kernel.f90:1613-1628, tls_reduce).
+  double esum = 0.0;
+  for (int t = 0; t < nt; t++) {
+    if (tpe[t].empty()) continue;
+    double s = 0.0;
+    for (int i = 0; i < nat; i++) s += tpe[t][i];
+    esum += 0.5 * s;
+    for (size_t q = 0; q < 3 * (size_t)nat; q++) o.f[q] += tf[t][q];
+    if (o.epot_per_at)
+      for (int i = 0; i < nat; i++) o.epot_per_at[i] += 0.5 * tpe[t][i];
+    if (want_wat)
+      for (size_t q = 0; q < 9 * (size_t)nat; q++) o.wpot_per_at[q] += twat[t][q];
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) o.wpot[3 * c + a] += twpot[9 * t + 3 * a + c];
+  }
+  *o.epot += esum;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Natural cubic spline on a uniform grid, simple_spline.f90.
+// ---------------------------------------------------------------------------
+
+struct Spline {
+  int n = 0;
+  double x0 = 0, dx = 1, cut = 0;
+  std::vector<double> y, d2y, c1, c2, c3, d1, d2, d3;
+
+  void init(int n_, double x0_, double dx_, const double *yy) {
+    const double sig = 0.5;
+    n = n_;
+    x0 = x0_;
+    dx = dx_;
+    y.assign(yy, yy + n);
+    d2y.assign(n, 0.0);
+    std::vector<double> u(n, 0.0);
+    c1.assign(n - 1, 0.0);
+    c2.assign(n - 1, 0.0);
+    c3.assign(n - 1, 0.0);
+    d1.assign(n - 1, 0.0);
+    d2.assign(n - 1, 0.0);
+    d3.assign(n - 1, 0.0);
+    d2y[0] = 0.0;
+    u[0] = 0.0;
+    for (int i = 1; i < n - 1; i++) {
+      double p = sig * d2y[i - 1] + 2;
+      d2y[i] = (sig - 1) / p;
+      u[i] = (6.0 * ((y[i + 1] - y[i]) / dx - (y[i] - y[i - 1]) / dx) / (2 * dx) -
+              sig * u[i - 1]) /
+             p;
+    }
+    const double qn = 0.0, un = 0.0;
+    d2y[n - 1] = (un - qn * u[n - 2]) / (qn * d2y[n - 2] + 1.0);
+    for (int k = n - 2; k >= 0; k--) d2y[k] = d2y[k] * d2y[k + 1] + u[k];
+    for (int k = 0; k < n - 1; k++) {
+      c1[k] = y[k + 1] - y[k] - (2 * d2y[k] + d2y[k + 1]) * (dx * dx) / 6;
+      c2[k] = d2y[k] * (dx * dx) / 2;
+      c3[k] = (d2y[k + 1] - d2y[k]) * (dx * dx) / 6;
+    }
+    for (int k = 0; k < n - 1; k++) {
+      d1[k] = c1[k] / dx;
+      d2[k] = 2 * c2[k] / dx;
+      d3[k] = 3 * c3[k] / dx;
+    }
+    cut = x0 + dx * (n - 1);
+  }
+  void scale_y(double fac) {
+    for (auto &v : y) v = fac * v;
+    for (auto &v : d2y) v = fac * v;
+    for (auto &v : c1) v = fac * v;
+    for (auto &v : c2) v = fac * v;
+    for (auto &v : c3) v = fac * v;
+    for (auto &v : d1) v = fac * v;
+    for (auto &v : d2) v = fac * v;
+    for (auto &v : d3) v = fac * v;
+  }
+  // simple_spline_f (:373-434); 1-based interval index as in the reference.
+  double f(double x, int *err) const {
+    double xf;
+    int i;
+    if (x == cut) {
+      xf = n;
+      i = n - 1;
+    } else {
+      xf = (x - x0) / dx + 1;
+      i = (int)std::floor(xf);
+    }
+    if (i < 1 || i >= n) {
+      if (err) *err = -1;
+      return 1.0;
+    }
+    double B = xf - i;
+    int k = i - 1;
+    return y[k] + B * (c1[k] + B * (c2[k] + B * c3[k]));
+  }
+  double df(double x, int *err) const {
+    double xf;
+    int i;
+    if (x == cut) {
+      xf = n;
+      i = n - 1;
+    } else {
+      xf = (x - x0) / dx + 1;
+      i = (int)std::floor(xf);
+    }
+    if (i < 1 || i >= n) {
+      if (err) *err = -1;
+      return 1.0;
+    }
+    double B = xf - i;
+    int k = i - 1;
+    return d1[k] + B * (d2[k] + B * d3[k]);
+  }
+  void f_and_df_extrap(double x, double &fv, double &dfv) const {
+    double xf = (x - x0) / dx + 1;
+    int i = (int)std::floor(xf);
+    if (i < 1)
+      i = 1;
+    else if (i >= n)
+      i = n - 1;
+    double B = xf - i;
+    int k = i - 1;
+    fv = y[k] + B * (c1[k] + B * (c2[k] + B * c3[k]));
+    dfv = d1[k] + B * (d2[k] + B * d3[k]);
+  }
+};
+
+struct EAM {
+  int nel = 0;
+  std::vector<int> Z;
+  double cutoff = 0;
+  std::vector<Spline> F, rho, phi;  // phi[i*nel+j], symmetric copies
+};
+
+// setfl reader, tabulated_alloy_eam.f90:147-259 (read_ascii takes
+// whitespace-separated values across lines).
+int eam_read(const char *fn, EAM &e) {
+  std::ifstream in(fn);
+  if (!in) return -1;
+  std::string line;
+  for (int i = 0; i < 3; i++)
+    if (!std::getline(in, line)) return -2;
+  if (!std::getline(in, line)) return -2;
+  {
+    std::istringstream ss(line);
+    ss >> e.nel;
+    if (!ss || e.nel <= 0) return -3;
+  }
+  int nF, nr;
+  double dF, dr;
+  if (!std::getline(in, line)) return -2;
+  {
+    std::istringstream ss(line);
+    ss >> nF >> dF >> nr >> dr >> e.cutoff;
+    if (!ss) return -3;
+  }
+  auto read_values = [&](int n, std::vector<double> &v) {
+    v.clear();
+    std::string tok;
+    while ((int)v.size() < n && (in >> tok)) v.push_back(std::strtod(tok.c_str(), nullptr));
+    std::getline(in, line);  // rest of the last line
+    return (int)v.size() == n;
+  };
+  e.Z.resize(e.nel);
+  e.F.resize(e.nel);
+  e.rho.resize(e.nel);
+  e.phi.resize((size_t)e.nel * e.nel);
+  std::vector<double> v;
+  for (int i = 0; i < e.nel; i++) {
+    if (!std::getline(in, line)) return -2;
+    std::istringstream ss(line);
+    ss >> e.Z[i];
+    if (!read_values(nF, v)) return -4;
+    e.F[i].init(nF, 0.0, dF, v.data());
+    if (!read_values(nr, v)) return -4;
+    v.push_back(0.0);
+    v.push_back(0.0);
+    e.rho[i].init(nr + 2, 0.0, dr, v.data());
+  }
+  for (int i = 0; i < e.nel; i++)
+    for (int j = 0; j <= i; j++) {
+      if (!read_values(nr, v)) return -4;
+      v.push_back(0.0);
+      v.push_back(0.0);
+      Spline s;
+      s.init(nr + 2, 0.0, dr, v.data());
+      s.scale_y(0.5);
+      e.phi[(size_t)i * e.nel + j] = s;
+      e.phi[(size_t)j * e.nel + i] = s;
+    }
+  return 0;
+}
+
+// tabulated_alloy_eam_energy_and_forces_kernel (:423-627).  db[i] is the
+// 0-based table index of atom i or -1.
+int eam_kernel(const EAM &e, int nat, const double *r, const Box &box, const int *db,
+               const NList &nl, const int *mask, double *epot, double *fout, double *wpot,
+               double *epot_per_at, double *wpot_per_at, int nthreads) {
+  const double cutoff_sq = e.cutoff * e.cutoff;
+  int nt = nthreads;
+  std::vector<std::vector<double>> tsca(nt), tvec(nt), twat(nt);
+  std::vector<double> tw(9 * nt, 0.0), te(nt, 0.0);
+  int err_all = 0;
+  const bool want_wat = wpot_per_at != nullptr;
+#pragma omp parallel num_threads(nthreads) reduction(| : err_all)
+  {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#else
+    const int tid = 0;
+#endif
+    auto &sca = tsca[tid];
+    auto &vec = tvec[tid];
+    auto &wat = twat[tid];
+    sca.assign(nat, 0.0);
+    vec.assign(3 * (size_t)nat, 0.0);
+    if (want_wat) wat.assign(9 * (size_t)nat, 0.0);
+    double w[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    std::vector<int> neb;
+    std::vector<double> neb_dr, neb_abs;
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < nat; i++) {
+      if (mask && mask[i] == 0) continue;
+      const int dbi = db[i];
+      if (dbi < 0) continue;
+      double rho = 0.0;
+      neb.clear();
+      neb_dr.clear();
+      neb_abs.clear();
+      for (int64_t ni = nl.seed[i]; ni < nl.seed[i + 1]; ni++) {
+        const int j = nl.nbr[ni];
+        const int dbj = db[j];
+        if (dbj < 0) continue;
+        const int *dc = &nl.dc[3 * ni];
+        double dr[3];
+        for (int a = 0; a < 3; a++) {
+          double as = box.A[a][0] * (double)dc[0];
+          as = as + box.A[a][1] * (double)dc[1];
+          as = as + box.A[a][2] * (double)dc[2];
+          dr[a] = (r[3 * i + a] - r[3 * j + a]) + as;
+        }
+        double abs_dr = dr[0] * dr[0];
+        abs_dr = abs_dr + dr[1] * dr[1];
+        abs_dr = abs_dr + dr[2] * dr[2];
+        if (abs_dr < cutoff_sq) {
+          abs_dr = std::sqrt(abs_dr);
+          int err = 0;
+          double drho = e.rho[dbj].f(abs_dr, &err);
+          if (err) err_all |= 1;
+          rho = rho + drho;
+          neb.push_back(j);
+          neb_dr.insert(neb_dr.end(), dr, dr + 3);
+          neb_abs.push_back(abs_dr);
+        }
+      }
+      if (rho < 0.0) rho = 0.0;
+      double Fi, dFi;
+      e.F[dbi].f_and_df_extrap(rho, Fi, dFi);
+      sca[i] = sca[i] + Fi;
+      double fori[3] = {0, 0, 0};
+      for (size_t q = 0; q < neb.size(); q++) {
+        const int j = neb[q];
+        const int dbj = db[j];
+        const double *dr = &neb_dr[3 * q];
+        const double abs_dr = neb_abs[q];
+        double phi, dphi;
+        e.phi[(size_t)dbi * e.nel + dbj].f_and_df_extrap(abs_dr, phi, dphi);
+        const double r_abs_dr = 1.0 / abs_dr;
+        sca[i] = sca[i] + phi * r_abs_dr;
+        int err = 0;
+        const double fac = e.rho[dbj].df(abs_dr, &err);
+        if (err) err_all |= 1;
+        double df[3];
+        for (int a = 0; a < 3; a++)
+          df[a] = -(dFi * fac + (dphi - phi * r_abs_dr) * r_abs_dr) * r_abs_dr * dr[a];
+        for (int a = 0; a < 3; a++) {
+          fori[a] = fori[a] + df[a];
+          vec[3 * (size_t)j + a] = vec[3 * (size_t)j + a] - df[a];
+        }
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++) {
+            double wij = -dr[a] * df[c];
+            w[a][c] = w[a][c] + wij;
+            if (want_wat) {
+              wat[9 * (size_t)i + 3 * c + a] += wij / 2;
+              wat[9 * (size_t)j + 3 * c + a] += wij / 2;
+            }
+          }
+      }
+      for (int a = 0; a < 3; a++) vec[3 * (size_t)i + a] += fori[a];
+    }
+    double s = 0.0;
+    for (int i = 0; i < nat; i++) s += sca[i];
+    te[tid] = s;
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) tw[9 * tid + 3 * a + c] = w[a][c];
+  }
+  double esum = 0.0;
+  for (int t = 0; t < nt; t++) {
+    if (tsca[t].empty()) continue;
+    esum += te[t];
+    for (size_t q = 0; q < 3 * (size_t)nat; q++) fout[q] += tvec[t][q];
+    if (epot_per_at)
+      for (int i = 0; i < nat; i++) epot_per_at[i] += tsca[t][i];
+    if (want_wat)
+      for (size_t q = 0; q < 9 * (size_t)nat; q++) wpot_per_at[q] += twat[t][q];
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) wpot[3 * c + a] += tw[9 * t + 3 * a + c];
+  }
+  *epot += esum;
+  return err_all ? -2 : 0;
+}
+
+int resolve_threads(int nthreads) {
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  return nthreads < 1 ? 1 : nthreads;
+}
+
+// View an externally supplied CSR list as an NList (copying).
+void nl_from_arrays(int nat, const int64_t *seed, const int *nbr, const int *dc, NList &nl) {
+  nl.seed.assign(seed, seed + nat + 1);
+  nl.nbr.assign(nbr, nbr + seed[nat]);
+  nl.dc.assign(dc, dc + 3 * seed[nat]);
+}
+
+}  // namespace
+
+// ============================================================================
+// C entry points (ctypes, tests and bench.py's CPU baseline only).
+// ============================================================================
+
+extern "C" {
+
+struct orc_nlist {
+  NList nl;
+};
+
+// Builds the full directed neighbour list.  Returns a handle or NULL.
+orc_nlist *orc_neighbors_build(int nat, const double *r, const double *cell, const int *pbc,
+                               double cutoff) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return nullptr;
+  orc_nlist *h = new orc_nlist;
+  build_neighbors(nat, r, box, cutoff, h->nl);
+  return h;
+}
+
+int64_t orc_neighbors_size(const orc_nlist *h) { return (int64_t)h->nl.nbr.size(); }
+
+void orc_neighbors_copy(const orc_nlist *h, int64_t *seed, int *nbr, int *dc) {
+  std::copy(h->nl.seed.begin(), h->nl.seed.end(), seed);
+  std::copy(h->nl.nbr.begin(), h->nl.nbr.end(), nbr);
+  std::copy(h->nl.dc.begin(), h->nl.dc.end(), dc);
+}
+
+void orc_neighbors_free(orc_nlist *h) { delete h; }
+
+void orc_cell_inverse(const double *cell, double *Bbox_rowmajor) {
+  Box box;
+  int pbc[3] = {1, 1, 1};
+  make_box(cell, pbc, box);
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 3; k++) Bbox_rowmajor[3 * a + k] = box.B[a][k];
+}
+
+static int map_elements(int nat, const int *Z, int nel, const int *dbZ, std::vector<int> &el) {
+  el.assign(nat, -1);
+  for (int i = 0; i < nat; i++)
+    for (int q = 0; q < nel; q++)
+      if (Z[i] == dbZ[q]) el[i] = q;
+  return 0;
+}
+
+// Interaction range requested by BIND_TO_FUNC for the elements present
+// (default_bind_to_func.f90:123-144).
+static double bop_range(int nat, const std::vector<int> &el, int nel, const double *r2) {
+  std::vector<int> present(nel, 0);
+  for (int i = 0; i < nat; i++)
+    if (el[i] >= 0) present[el[i]] = 1;
+  double range = 0.0;
+  for (int a = 0; a < nel; a++)
+    for (int b = 0; b < nel; b++)
+      if (present[a] && present[b]) range = std::max(range, r2[pair_index(a, b, nel)]);
+  return range;
+}
+
+double orc_tersoff_cutoff(const orc_tersoff_params *p, int nat, const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return bop_range(nat, el, p->nel, p->r2);
+}
+
+double orc_kumagai_cutoff(const orc_kumagai_params *p, int nat, const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return bop_range(nat, el, p->nel, p->r2);
+}
+
+// energy_and_forces on an explicit neighbour list.  Outputs are accumulated
+// into (f, wpot, per-atom, per-bond) as the reference does; epot is set.
+int orc_tersoff_kernel(const orc_tersoff_params *p, int nat, const double *r,
+                       const double *cell, const int *pbc, const int *Z,
+                       const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                       double *epot, double *f, double *wpot, double *epot_per_at,
+                       double *epot_per_bond, double *f_per_bond, double *wpot_per_at,
+                       double *wpot_per_bond, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  NList nl;
+  nl_from_arrays(nat, seed, nbr, dc, nl);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return bop_kernel(TersoffFn(*p), nat, r, box, el.data(), nl, mask, o,
+                    resolve_threads(nthreads));
+}
+
+int orc_kumagai_kernel(const orc_kumagai_params *p, int nat, const double *r,
+                       const double *cell, const int *pbc, const int *Z,
+                       const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                       double *epot, double *f, double *wpot, double *epot_per_at,
+                       double *epot_per_bond, double *f_per_bond, double *wpot_per_at,
+                       double *wpot_per_bond, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  NList nl;
+  nl_from_arrays(nat, seed, nbr, dc, nl);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return bop_kernel(KumagaiFn(*p), nat, r, box, el.data(), nl, mask, o,
+                    resolve_threads(nthreads));
+}
+
+// Full COMPUTE_FUNC: neighbour build + kernel (no per-bond outputs).
+int orc_tersoff_compute(const orc_tersoff_params *p, int nat, const double *r,
+                        const double *cell, const int *pbc, const int *Z, const int *mask,
+                        double *epot, double *f, double *wpot, double *epot_per_at,
+                        double *wpot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  double cutoff = bop_range(nat, el, p->nel, p->r2);
+  NList nl;
+  if (cutoff > 0) build_neighbors(nat, r, box, cutoff, nl);
+  else nl.seed.assign(nat + 1, 0);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return bop_kernel(TersoffFn(*p), nat, r, box, el.data(), nl, mask, o,
+                    resolve_threads(nthreads));
+}
+
+int orc_kumagai_compute(const orc_kumagai_params *p, int nat, const double *r,
+                        const double *cell, const int *pbc, const int *Z, const int *mask,
+                        double *epot, double *f, double *wpot, double *epot_per_at,
+                        double *wpot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  double cutoff = bop_range(nat, el, p->nel, p->r2);
+  NList nl;
+  if (cutoff > 0) build_neighbors(nat, r, box, cutoff, nl);
+  else nl.seed.assign(nat + 1, 0);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return bop_kernel(KumagaiFn(*p), nat, r, box, el.data(), nl, mask, o,
+                    resolve_threads(nthreads));
+}
+
+struct orc_eam {
+  EAM e;
+};
+
+orc_eam *orc_eam_load(const char *fn, int *ierr) {
+  orc_eam *h = new orc_eam;
+  int rc = eam_read(fn, h->e);
+  if (ierr) *ierr = rc;
+  if (rc != 0) {
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+
+void orc_eam_free(orc_eam *h) { delete h; }
+double orc_eam_cutoff(const orc_eam *h) { return h->e.cutoff; }
+int orc_eam_nel(const orc_eam *h) { return h->e.nel; }
+
+// Spline table export: which = 0 (F), 1 (rho), 2 (phi, i*nel+j).
+// Returns n; fills x0dx[3] = {x0, dx, cut} and coef (8*n slots: y, d2y, then
+// c1,c2,c3,d1,d2,d3 each n-1 long, padded to n) when coef != NULL.
+int orc_eam_table(const orc_eam *h, int which, int idx, double *x0dx, double *coef) {
+  const Spline *s = nullptr;
+  if (which == 0) s = &h->e.F[idx];
+  else if (which == 1) s = &h->e.rho[idx];
+  else s = &h->e.phi[idx];
+  if (x0dx) {
+    x0dx[0] = s->x0;
+    x0dx[1] = s->dx;
+    x0dx[2] = s->cut;
+  }
+  if (coef) {
+    const int n = s->n;
+    const std::vector<double> *arr[8] = {&s->y, &s->d2y, &s->c1, &s->c2,
+                                         &s->c3, &s->d1, &s->d2, &s->d3};
+    for (int q = 0; q < 8; q++) {
+      for (int k = 0; k < n; k++) coef[(size_t)q * n + k] = k < (int)arr[q]->size() ? (*arr[q])[k] : 0.0;
+    }
+  }
+  return s->n;
+}
+
+int orc_eam_kernel(const orc_eam *h, int nat, const double *r, const double *cell,
+                   const int *pbc, const int *Z, const int64_t *seed, const int *nbr,
+                   const int *dc, const int *mask, double *epot, double *f, double *wpot,
+                   double *epot_per_at, double *wpot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> db;
+  map_elements(nat, Z, h->e.nel, h->e.Z.data(), db);
+  NList nl;
+  nl_from_arrays(nat, seed, nbr, dc, nl);
+  *epot = 0.0;
+  return eam_kernel(h->e, nat, r, box, db.data(), nl, mask, epot, f, wpot, epot_per_at,
+                    wpot_per_at, resolve_threads(nthreads));
+}
+
+int orc_eam_compute(const orc_eam *h, int nat, const double *r, const double *cell,
+                    const int *pbc, const int *Z, const int *mask, double *epot, double *f,
+                    double *wpot, double *epot_per_at, double *wpot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> db;
+  map_elements(nat, Z, h->e.nel, h->e.Z.data(), db);
+  NList nl;
+  build_neighbors(nat, r, box, h->e.cutoff, nl);
+  *epot = 0.0;
+  return eam_kernel(h->e, nat, r, box, db.data(), nl, mask, epot, f, wpot, epot_per_at,
+                    wpot_per_at, resolve_threads(nthreads));
+}
+
+int orc_max_threads(void) { return resolve_threads(0); }
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+"""Shared helpers of the test-suite: run the GPU path and the oracle on the
+same structure and compare."""
+
+import numpy as np
+
+from atomistica_gb300 import parameters as P
+from atomistica_gb300 import structures as S
+
+TERSOFF = P.Tersoff_PRB_39_5566_Si_C
+KUMAGAI = P.Kumagai_CompMaterSci_39_457_Si
+
+# Tolerances of the FP64 drop-in against the FP64 oracle (per atom energy,
+# force and virial components), and of the mixed form's forces.
+E_TOL = 1e-10      # eV/atom
+F_TOL = 1e-9       # eV/A
+W_TOL = 1e-9       # eV per atom of virial magnitude (scaled by nat below)
+MIXED_F_TOL = 1e-5  # eV/A
+
+
+def gpu_bop(kind, s, precision="fp64", params=None, mask=None, per_at=True, per_bond=False,
+            repeat=1):
+    from atomistica_gb300 import native
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    cls = native.Tersoff if kind == "tersoff" else native.Kumagai
+    pot = cls(precision=precision, **(params or {}))
+    pot.bind_to(p, nl)
+    out = None
+    for _ in range(repeat):
+        kw = dict(mask=mask)
+        if per_at:
+            kw.update(epot_per_at=True, wpot_per_at=True)
+        if per_bond:
+            kw.update(epot_per_bond=True, f_per_bond=True, wpot_per_bond=True)
+        res = pot.energy_and_forces(p, nl, **kw)
+        out = {"epot": res[0], "f": res[1], "wpot": res[2]}
+        k = 3
+        if per_at:
+            out["epot_per_at"] = res[k]
+            out["wpot_per_at"] = res[k + 1] if not per_bond else res[k + 3]
+            if per_bond:
+                out["epot_per_bond"] = res[k + 1]
+                out["f_per_bond"] = res[k + 2]
+                out["wpot_per_bond"] = res[k + 4]
+        elif per_bond:
+            out["epot_per_bond"], out["f_per_bond"], out["wpot_per_bond"] = res[k:k + 3]
+    out["nl"] = nl.get_list(p)
+    out["timing"] = pot.last_timing()
+    return out
+
+
+def gpu_eam(fn, s, mask=None, per_at=True):
+    from atomistica_gb300 import native
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    pot = native.TabulatedAlloyEAM(fn)
+    pot.bind_to(p, nl)
+    kw = dict(mask=mask)
+    if per_at:
+        kw.update(epot_per_at=True, wpot_per_at=True)
+    res = pot.energy_and_forces(p, nl, **kw)
+    out = {"epot": res[0], "f": res[1], "wpot": res[2]}
+    if per_at:
+        out["epot_per_at"], out["wpot_per_at"] = res[3], res[4]
+    out["nl"] = nl.get_list(p)
+    return out
+
+
+def compare(ref, got, nat, etol=E_TOL, ftol=F_TOL, wtol=W_TOL, per_at=True):
+    """Max deviations; asserts they are within tolerance."""
+    de = abs(ref["epot"] - got["epot"]) / max(nat, 1)
+    df = float(np.max(np.abs(ref["f"] - got["f"]))) if nat else 0.0
+    dw = float(np.max(np.abs(ref["wpot"] - got["wpot"])))
+    wscale = max(1.0, nat)
+    assert de < etol, "energy per atom differs by %g" % de
+    assert df < ftol, "forces differ by %g" % df
+    assert dw < wtol * wscale, "virial differs by %g" % dw
+    if per_at and "epot_per_at" in got and nat:
+        assert np.max(np.abs(ref["epot_per_at"] - got["epot_per_at"])) < etol * 10
+        assert np.max(np.abs(ref["wpot_per_at"] - got["wpot_per_at"])) < wtol * 10
+    return de, df, dw
+
+
+def rattled_diamond(symbol="Si", a=5.431, size=(2, 2, 2), amp=0.3, seed=0):
+    rng = np.random.default_rng(seed)
+    s = S.diamond(symbol, a, size)
+    s.positions += rng.uniform(-amp, amp, s.positions.shape)
+    return s
+
+
+def random_carbon(nat=128, density=3.0, seed=0, dmin=1.2):
+    """Amorphous-carbon-like random packing (a stand-in for aC.cfg)."""
+    rng = np.random.default_rng(seed)
+    mass = 12.011
+    L = (nat * mass / (density * 6.02214076e23) * 1e24) ** (1.0 / 3.0)
+    cell = np.eye(3) * L
+    pos = S._random_packing(rng, nat, cell, dmin)
+    return S.Structure(pos, cell, np.array([True, True, True]),
+                       np.full(nat, 6, dtype=np.int32))
+
+
+def triclinic_si(nat=24, seed=0, strain=0.08, dmin=2.0):
+    rng = np.random.default_rng(seed)
+    n = S.si_number_density()
+    L = (nat / n) ** (1.0 / 3.0)
+    eps = rng.uniform(-strain, strain, size=(3, 3))
+    cell = (np.eye(3) * L) @ (np.eye(3) + eps).T
+    pos = S._random_packing(rng, nat, cell, dmin)
+    return S.Structure(pos, cell, np.array([True, True, True]),
+                       np.full(nat, 14, dtype=np.int32))
+
+
+def sorted_triples(seed, j, dc):
+    i = np.repeat(np.arange(len(seed) - 1), np.diff(seed))
+    t = np.column_stack([i, j, dc]).astype(np.int64)
+    return t[np.lexsort(t.T[::-1])]

@@ -1,0 +1,92 @@
+"""Host-side logic on CPU: workload generators, file formats, parameter
+conversion and the Python front-end's behaviour without a GPU."""
+
+import numpy as np
+import pytest
+
+import oracle
+from atomistica_gb300 import io as gio
+from atomistica_gb300 import parameters as P
+from atomistica_gb300 import structures as S
+
+
+def test_workload_sizes_and_density():
+    s = S.tersoff_si_4096()
+    assert len(s) == 4096 and np.allclose(np.diag(s.cell), 8 * 5.431)
+    assert np.max(np.abs(s.positions - S.diamond("Si", 5.431, (8, 8, 8)).positions)) <= 0.1
+    c = S.tersoff_si_amorphous(natoms=4096, seed=3)
+    assert len(c) == 4096
+    rho = len(c) * S.MASS_SI / S.AVOGADRO / c.get_volume() * 1e24
+    assert abs(rho - 2.33) < 1e-9
+
+
+def test_full_size_amorphous_construction():
+    c = S.tersoff_si_amorphous()
+    assert len(c) == 1048576
+    assert c.info["sites"] == 8 * 51 ** 3 and c.info["deleted"] == 12632
+    assert abs(c.info["a"] - 5.4086) < 1e-3
+
+
+def test_batch_and_fit_sets():
+    b = S.si_batch(nstruct=6, seed=1)
+    for s in b:
+        assert 8 <= len(s) <= 512
+        d = s.positions[:, None, :] - s.positions[None, :, :]
+        frac = d @ np.linalg.inv(s.cell)
+        frac -= np.round(frac)
+        r = np.sqrt(((frac @ s.cell) ** 2).sum(-1)) + np.eye(len(s)) * 10
+        assert r.min() >= 2.0 - 1e-9
+    f = S.si_fit_set(nstruct=10)
+    assert all(len(s) in (64, 96, 144, 216) for s in f)
+
+
+def test_setfl_round_trip(tmp_path):
+    fn = gio.cu_analytic_setfl(str(tmp_path / "cu.setfl"), nr=500, nrho=400)
+    e = oracle.EAM(fn)
+    assert e.nel == 1 and abs(e.cutoff - 5.0) < 1e-15
+    x, c = e.table(1, 0)
+    r = np.arange(502) * x[1]
+    expect = np.exp(-3.0 * (r[:500] / 2.556 - 1.0))
+    assert np.allclose(c[0, :500], expect, rtol=0, atol=1e-15)
+    assert c[0, 500] == 0 and c[0, 501] == 0  # two zero pads (tabulated_alloy_eam.f90:222)
+    x, c = e.table(2, 0)
+    rr = np.arange(500) * x[1]
+    phi = 0.35 * (np.exp(-2.8 * (rr - 2.556)) - 2 * np.exp(-1.4 * (rr - 2.556)))
+    assert np.allclose(c[0, :500], 0.5 * rr * phi, atol=1e-14)  # r*phi scaled by 1/2
+
+
+def test_parameter_conversion():
+    from atomistica_gb300 import _lib, native
+    p = native.tersoff_params(P.Tersoff_PRB_39_5566_Si_C)
+    assert p.nel == 2 and list(p.Z)[:2] == [6, 14]
+    assert p.A[2] == 1.8308e3 and p.r2[2] == 3.0 and p.lambda_[1] == (3.4879 + 2.4799) / 2
+    q = native.kumagai_params(P.Kumagai_CompMaterSci_39_457_Si)
+    assert q.Z[0] == 14 and q.beta[0] == 1 and q.r2[0] == 3.3
+    si = P.tersoff_single_element(P.Tersoff_PRB_39_5566_Si_C, "Si")
+    assert si["A"] == [1.8308e3] and si["n"] == [7.8734e-1]
+    assert isinstance(p, _lib.TersoffParams)
+
+
+def test_pair_index_matches_reference_table():
+    # src/macros.inc:110-123 table for maxval=4 (1-based): row i, col j>=i
+    expect = {(1, 1): 1, (1, 2): 2, (1, 3): 3, (1, 4): 4, (2, 2): 5, (2, 3): 6, (2, 4): 7,
+              (3, 3): 8, (3, 4): 9, (4, 4): 10}
+    for (i, j), v in expect.items():
+        assert P.pair_index(i - 1, j - 1, 4) + 1 == v
+        assert P.pair_index(j - 1, i - 1, 4) + 1 == v
+
+
+def test_cfg_reader(reference_tests_dir):
+    import os
+    s = gio.read_cfg(os.path.join(reference_tests_dir, "aC_small.cfg"))
+    assert len(s) == 128 and np.all(s.numbers == 6)
+    assert np.allclose(np.diag(s.cell), 9.584001)
+
+
+def test_frontend_fails_loudly_without_gpu():
+    from atomistica_gb300 import _lib, native
+    _lib.load()
+    if _lib.device_count() > 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(_lib.AtomisticaError):
+        native.from_atoms(S.diamond("Si", 5.431))
