@@ -16,11 +16,14 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libatomistica_gb300.so")
-SOURCES = ["core.cu", "bop.cu", "eam.cu", "api.cu"]
+SOURCES = ["core.cu", "bop.cu", "eam.cu", "api.cu", "diag.cu"]
 HEADERS = ["internal.h", "potential.h", "bop_math.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code is compiled without FP contraction so that the cell inverse, the
+# binning set-up and the spline tables are bit-identical on x86 and Arm hosts.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-diag-suppress", "1444",
               "-I" + os.path.join(ROOT, "include")]
 

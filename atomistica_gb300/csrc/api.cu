@@ -140,8 +140,10 @@ cudaStream_t pot_stream(Potential &pot) {
     cudaStreamCreateWithFlags(&pot.stream, cudaStreamNonBlocking);
     pot.own_stream = true;
   }
-  if (!pot.ev[0])
+  if (!pot.ev[0]) {
     for (int q = 0; q < 4; q++) cudaEventCreate(&pot.ev[q]);
+    for (int q = 0; q < 2; q++) cudaEventCreate(&pot.kev[q]);
+  }
   return pot.stream;
 }
 
@@ -203,6 +205,7 @@ int add_into(double *dst, const double *src, size_t n, cudaStream_t s) {
   const int T = 256;
   const size_t blocks = std::min<size_t>((n + T - 1) / T, 65535);
   add_arrays<<<(unsigned)blocks, T, 0, s>>>(dst, src, n);
+  note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -287,11 +290,13 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CUDA(cudaEventRecord(pot.ev[3], s));
   GB_CUDA(cudaStreamSynchronize(s));
   GB_CUDA(cudaGetLastError());
-  float ms[3];
+  float ms[4] = {0, 0, 0, 0};
   cudaEventElapsedTime(&ms[0], pot.ev[0], pot.ev[1]);
   cudaEventElapsedTime(&ms[1], pot.ev[1], pot.ev[2]);
   cudaEventElapsedTime(&ms[2], pot.ev[0], pot.ev[3]);
-  for (int q = 0; q < 3; q++) pot.timing[q] = ms[q];
+  if (nat > 0) cudaEventElapsedTime(&ms[3], pot.kev[0], pot.kev[1]);
+  cudaGetLastError();
+  for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
   const int st = reinterpret_cast<const int *>(hr + 12)[0];
   pot.last_status = st;
   if (st & 1) {
@@ -398,6 +403,8 @@ void gb_potential_free(gb_potential_t *h) {
   Potential &pot = h->pot;
   for (int q = 0; q < 4; q++)
     if (pot.ev[q]) cudaEventDestroy(pot.ev[q]);
+  for (int q = 0; q < 2; q++)
+    if (pot.kev[q]) cudaEventDestroy(pot.kev[q]);
   if (pot.own_stream && pot.stream) cudaStreamDestroy(pot.stream);
   delete h;
 }
@@ -516,9 +523,9 @@ int gb_tabulated_alloy_eam_table(const gb_potential_t *h, int which, int idx, do
   return s->n;
 }
 
-int gb_potential_last_timing(const gb_potential_t *h, double *ms3) {
-  if (!h || !ms3) return GB_ERROR_ARGUMENT;
-  for (int q = 0; q < 3; q++) ms3[q] = h->pot.timing[q];
+int gb_potential_last_timing(const gb_potential_t *h, double *ms) {
+  if (!h || !ms) return GB_ERROR_ARGUMENT;
+  for (int q = 0; q < 4; q++) ms[q] = h->pot.timing[q];
   return 0;
 }
 

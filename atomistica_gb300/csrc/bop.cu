@@ -501,6 +501,7 @@ int launch_tile(const BopArgs &args, const Pot &pot, int ntiles, int max_nbt, in
     }
   }
   kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, max_nbt, max_ntrip, status);
+  note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -518,6 +519,7 @@ int dispatch_tile(const BopArgs &args, const Pot &pot, int ntiles, int max_nbt, 
 
 int reduce_partials(const double *part, int ntiles, int nc, double *red, cudaStream_t s) {
   reduce_partials_kernel<<<1, 1024, 0, s>>>(part, ntiles, nc, red);
+  note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -563,6 +565,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   int *plan = reinterpret_cast<int *>(pot.tile_part.as<double>() + 10 * (size_t)ntiles);
   GB_CUDA(cudaMemsetAsync(plan, 0, sizeof(int) * 4, s));
   bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, nl.seed.as<int>(), plan);
+  note_launch();
   GB_CHECK(pot.hred.ensure(64));
   int *hplan = pot.hred.as<int>();
   GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
@@ -587,6 +590,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   args.tile_part = pot.tile_part.as<double>();
   int *status = o.status;
   int rc;
+  GB_CUDA(cudaEventRecord(pot.kev[0], s));
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};
     rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, ntiles, max_nbt, max_ntrip, status,
@@ -601,23 +605,32 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
                                                    status, want_wat, want_pb, s);
   }
   GB_CHECK(rc);
+  GB_CUDA(cudaEventRecord(pot.kev[1], s));
   const int T = 128;
   const bool epa = o.epot_per_at != nullptr;
   const int gb = (nat + T - 1) / T;
-  if (epa && want_wat)
+  if (epa && want_wat) {
     bop_gather<true, true><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                                             args.ebond, args.wbond, o.f, o.epot_per_at,
                                             o.wpot_per_at);
-  else if (epa)
+    note_launch();
+  }
+  else if (epa) {
     bop_gather<true, false><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                                              args.ebond, nullptr, o.f, o.epot_per_at, nullptr);
-  else if (want_wat)
+    note_launch();
+  }
+  else if (want_wat) {
     bop_gather<false, true><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                                              args.ebond, args.wbond, o.f, nullptr,
                                              o.wpot_per_at);
-  else
+    note_launch();
+  }
+  else {
     bop_gather<false, false><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                                               args.ebond, nullptr, o.f, nullptr, nullptr);
+    note_launch();
+  }
   GB_CUDA(cudaGetLastError());
   GB_CHECK(reduce_partials(args.tile_part, ntiles, 10, o.red, s));
   pot.tile_atoms = apt;

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -33,6 +34,8 @@ namespace gb {
 // Error state.
 // ---------------------------------------------------------------------------
 static thread_local std::string g_error;
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 void set_error(const std::string &msg) { g_error = msg; }
 void clear_error() { g_error.clear(); }
 
@@ -171,9 +174,11 @@ int scan_rec(const int *in, int *out, int n, int *tmp, cudaStream_t s) {
   int *sums = tmp;
   int *offs = tmp + tiles + 1;
   scan_tiles<<<tiles, kScanThreads, 0, s>>>(in, out, n, sums);
+  note_launch();
   if (tiles > 1) {
     scan_rec(sums, offs, tiles, tmp + 2 * (tiles + 1), s);
     scan_add<<<tiles, kScanThreads, 0, s>>>(out, n, offs);
+    note_launch();
   }
   return 0;
 }
@@ -195,6 +200,7 @@ int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t
   GB_CHECK(tmp.ensure(scan_tmp_ints(n) * sizeof(int)));
   scan_rec(in, out, n, tmp.as<int>(), stream);
   scan_total<<<1, 1, 0, stream>>>(in, out, n);
+  note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -604,6 +610,7 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
     nl_assign_cells<<<nb, T, 0, stream>>>(nat, p.r.as<double>(), bp, nl.pos4.as<Pos4>(),
                                           nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
                                           nl.cell_count.as<int>(), status);
+    note_launch();
   }
   GB_CHECK(exclusive_scan_i32(nl.cell_count.as<int>(), nl.cell_start.as<int>(), ncells,
                               nl.scan_tmp, stream));
@@ -612,17 +619,22 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   if (nat > 0) {
     nl_scatter<<<nb, T, 0, stream>>>(nat, nl.atom_cell.as<int>(), nl.cell_start.as<int>(),
                                      nl.cell_count.as<int>(), cell_atoms);
+    note_launch();
     nl_sort_cells<<<(ncells + T - 1) / T, T, 0, stream>>>(ncells, nl.cell_start.as<int>(),
                                                          cell_atoms, big_cells, &status[2]);
+    note_launch();
     // Crowded cells (rare): rank-by-count into the second half, copy back.
     nl_sort_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
         big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms, cell_atoms + nat);
+    note_launch();
     nl_copy_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
         big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms + nat, cell_atoms);
+    note_launch();
     nl_pairs<false><<<(nat + 127) / 128, 128, 0, stream>>>(
         nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
         nl.cell_start.as<int>(), cell_atoms, nl.counts.as<int>(), nullptr, nullptr, nullptr,
         status);
+    note_launch();
   }
   GB_CHECK(exclusive_scan_i32(nl.counts.as<int>(), nl.seed.as<int>(), nat, nl.scan_tmp, stream));
   // Read back: maxz, flags, n_big, total entries.
@@ -652,6 +664,7 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
         nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
         nl.cell_start.as<int>(), cell_atoms, nullptr, nl.seed.as<int>(), nl.nbr.as<int>(),
         nl.shift.as<int>(), status);
+    note_launch();
   }
   GB_CUDA(cudaGetLastError());
   nl.nentries = total;
@@ -671,10 +684,12 @@ int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stre
   GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(nl.nentries, 1)));
   int *status = nl.stats.as<int>();
   GB_CUDA(cudaMemsetAsync(status + 1, 0, sizeof(int), stream));
-  if (nat > 0)
+  if (nat > 0) {
     nl_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.seed.as<int>(), nl.nbr.as<int>(),
                                                      nl.shift.as<int>(), nl.rev.as<int>(),
                                                      status);
+    note_launch();
+  }
   int *hs = nl.hstats.as<int>();
   GB_CUDA(cudaMemcpyAsync(hs + 1, status + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
   GB_CUDA(cudaStreamSynchronize(stream));
@@ -706,6 +721,8 @@ extern "C" {
 
 const char *gb_get_error(void) { return g_error.c_str(); }
 const char *gb_version(void) { return "atomistica_gb300 0.1.0 (sm_103a)"; }
+
+uint64_t gb_kernel_launches(void) { return g_launches.load(); }
 
 int gb_device_count(void) {
   int n = 0;
@@ -898,6 +915,7 @@ int gb_neighbors_get(gb_neighbors_t *h, gb_particles_t *ph, int64_t *seed, int *
   nl_export<<<(nat + 1 + 127) / 128, 128, 0, s>>>(nat, nl.seed.as<int>(), nl.nbr.as<int>(),
                                                  nl.shift.as<int>(), seed ? dseed : nullptr,
                                                  j ? dj : nullptr, dc ? ddc : nullptr);
+  note_launch();
   GB_CUDA(cudaGetLastError());
   if (seed && dseed != seed) GB_CUDA(cudaMemcpyAsync(seed, dseed, bs, cudaMemcpyDeviceToHost, s));
   if (j && dj != j && n) GB_CUDA(cudaMemcpyAsync(j, dj, bj, cudaMemcpyDeviceToHost, s));

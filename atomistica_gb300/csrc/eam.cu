@@ -508,15 +508,26 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   a.part = pot.tile_part.as<double>();
   a.status = o.status;
   eam_density<<<blocks, kEamThreads, 0, s>>>(a);
+  note_launch();
   const bool epa = o.epot_per_at != nullptr;
-  if (epa && want_wat)
+  GB_CUDA(cudaEventRecord(pot.kev[0], s));
+  if (epa && want_wat) {
     eam_pair<true, true><<<blocks, kEamThreads, 0, s>>>(a);
-  else if (epa)
+    note_launch();
+  }
+  else if (epa) {
     eam_pair<true, false><<<blocks, kEamThreads, 0, s>>>(a);
-  else if (want_wat)
+    note_launch();
+  }
+  else if (want_wat) {
     eam_pair<false, true><<<blocks, kEamThreads, 0, s>>>(a);
-  else
+    note_launch();
+  }
+  else {
     eam_pair<false, false><<<blocks, kEamThreads, 0, s>>>(a);
+    note_launch();
+  }
+  GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CUDA(cudaGetLastError());
   GB_CHECK(reduce_partials(a.part, blocks, 10, o.red, s));
   return 0;

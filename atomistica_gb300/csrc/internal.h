@@ -63,6 +63,9 @@ struct HostBuf {
   ~HostBuf() { release(); }
 };
 
+// Host-side count of kernel launches issued by this library (diagnostics).
+void note_launch(int n = 1);
+
 // Does the pointer refer to device (or managed) memory?
 bool is_device_ptr(const void *ptr);
 

@@ -80,7 +80,8 @@ struct Potential {
   DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
   HostBuf hred;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  double timing[3] = {0, 0, 0};
+  cudaEvent_t kev[2] = {nullptr, nullptr};  // around the dominant force kernel
+  double timing[4] = {0, 0, 0, 0};
   int tile_atoms = 32;
   int last_status = 0;
 };

@@ -272,8 +272,9 @@ class _Potential:
         check(self._L.gb_potential_bind_to(self._h, p._h, nl._h, ctypes.byref(err)), "bind_to")
 
     def last_timing(self):
-        """(neighbour ms, force ms, total ms) of the last call (CUDA events)."""
-        t = (ctypes.c_double * 3)()
+        """(neighbour-list ms, force ms, total ms, dominant kernel ms) of the
+        last call (CUDA events on the potential's stream)."""
+        t = (ctypes.c_double * 4)()
         self._L.gb_potential_last_timing(self._h, t)
         return tuple(t)
 

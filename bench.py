@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""
+Benchmark of the per-step Tersoff force path on GB300.
+
+Workload (the configuration the headline metric is quoted on): Si block of
+1,048,576 atoms at 2.33 g/cm^3 in a cubic periodic box, diamond sites with
+Gaussian sigma = 0.25 A (seeded; atomistica_gb300.structures.
+tersoff_si_amorphous).  One step = one energy_and_forces call: full
+neighbour-list rebuild (positions are marked changed every step, as on the
+reference's ASE path with a zero Verlet shell) + energy, forces and virial.
+
+  value   atom-evals/s of the FP32-mixed form, inputs resident in HBM,
+          CUDA events on the launching stream, L2 flushed between steps
+          (256 MB write, outside the timed events); the FP64 drop-in is
+          timed the same way and reported beside it.
+  e2e     the same metric through the public API with pinned HOST buffers:
+          per step the position upload, the force upload (accumulate
+          semantics) and the force/energy/virial download are timed.
+  roofline  the dominant kernel (bond-order tile kernel, mixed form):
+          algorithmic FP32/FP64 flops per launch / kernel time against the
+          FP32 and FP64 FMA peaks measured in this run.
+  cpu_baseline  the C++ FP64 oracle (the reference algorithm restated;
+          reference binary unavailable: no Fortran compiler) with OpenMP on
+          all host cores, full workload, median of 3 calls.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun (N > 1) every rank evaluates its own replica (no exchange).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Tersoff atom-evals/s: FP32-mixed vs FP64 GPU at ≤1e-5 eV/Å force error"
+UNIT = "atom-evals/s"
+
+# Algorithmic flop model per directed bond and per triplet (+,-,*,/,sqrt and
+# each exp/pow/cos/sin counted as one flop), counted from the reference's
+# non-screened BOP code.  In the mixed form the triplet terms and the bond
+# order run in FP32, the bond geometry and pair terms in FP64.
+FLOPS_BOND = 150.0
+FLOPS_TRIPLET = 165.0
+FLOPS_BO = 14.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--natoms", type=int, default=1048576)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--cpu-runs", type=int, default=3)
+    ap.add_argument("--skip-oracle", action="store_true",
+                    help="skip the FP64 oracle error check and CPU baseline")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flop_model(z):
+    """Algorithmic FP32 / FP64 flops per call of the mixed and FP64 forms."""
+    import numpy as np
+    z = np.asarray(z, dtype=np.float64)
+    nb = float(z.sum())
+    nt = float((z * (z - 1)).sum())
+    return {
+        "bonds": nb, "triplets": nt,
+        "fp64_form_fp64": FLOPS_BOND * nb + FLOPS_TRIPLET * nt,
+        "mixed_fp32": FLOPS_TRIPLET * nt + FLOPS_BO * nb,
+        "mixed_fp64": (FLOPS_BOND - FLOPS_BO) * nb,
+    }
+
+
+def cpu_baseline(structure, params, runs):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # CPU baseline leg: the reference algorithm on the host cores
+    oracle.build()
+    nthreads = oracle.max_threads()
+    oracle.bop_compute("tersoff", params, structure, nthreads=nthreads)
+    ts = []
+    for _ in range(runs):
+        t0 = time.perf_counter()
+        oracle.bop_compute("tersoff", params, structure, nthreads=nthreads)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return {"value": len(structure) / t, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "full %d-atom workload incl. neighbour build, median of %d calls "
+                      "(C++ FP64 restatement of the reference algorithm, OpenMP)"
+                      % (len(structure), runs),
+            "seconds_per_call": t}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from atomistica_gb300 import parameters, structures
+    s = structures.tersoff_si_amorphous(args.natoms, seed=args.seed)
+    params = parameters.Tersoff_PRB_39_5566_Si_C
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    nthreads = oracle.max_threads()
+    for _ in range(max(args.warmup, 1)):
+        oracle.bop_compute("tersoff", params, s, nthreads=nthreads)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.bop_compute("tersoff", params, s, nthreads=nthreads)
+        ts.append(time.perf_counter() - t0)
+    total = sum(ts)
+    value = len(s) * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "tersoff_si_amorphous_%d" % len(s), "natoms": len(s),
+                   "seed": args.seed, "density_gcc": 2.33, "sigma_A": 0.25},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "full workload per step incl. neighbour build (C++ FP64 "
+                                   "restatement of the reference algorithm, OpenMP; reference "
+                                   "binary unavailable: no Fortran compiler)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    from atomistica_gb300 import _lib, native, parameters, structures
+    from atomistica_gb300 import build as gbuild
+    gbuild.build()
+    L = _lib.load()
+    params = parameters.Tersoff_PRB_39_5566_Si_C
+    s = structures.tersoff_si_amorphous(args.natoms, seed=args.seed)
+    nat = len(s)
+
+    stream = torch.cuda.Stream(device=dev)
+    p = native.from_atoms(s)
+    p.set_stream(stream.cuda_stream)
+    nl = native.Neighbors(100)
+    pots = {}
+    for prec in ("mixed", "fp64"):
+        pot = native.Tersoff(precision=prec)
+        pot.set_stream(stream.cuda_stream)
+        pot.bind_to(p, nl)
+        pots[prec] = pot
+
+    d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+    d_f = torch.zeros((nat, 3), dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step(pot):
+        with torch.cuda.stream(stream):
+            d_f.zero_()
+        p.set_positions(d_pos)   # marks positions changed -> full neighbour rebuild
+        return pot.energy_and_forces(p, nl, forces=d_f)
+
+    def timed(pot, k, sampler=None):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k)]
+        parts = []
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        n0 = L.gb_kernel_launches()
+        if sampler:
+            sampler.start()
+        for q in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[q][0].record(stream)
+            step(pot)
+            with torch.cuda.stream(stream):
+                ev[q][1].record(stream)
+            parts.append(pot.last_timing())
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        launches = L.gb_kernel_launches() - n0
+        if ws > 1:
+            torch.distributed.barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return ms, parts, launches, clocks
+
+    for prec in ("fp64", "mixed"):
+        for _ in range(max(args.warmup, 3)):
+            step(pots[prec])
+    torch.cuda.synchronize()
+
+    ms64, parts64, _, _ = timed(pots["fp64"], args.steps)
+    sampler = ClockSampler(torch.cuda.current_device())
+    msmx, partsmx, launches, clocks = timed(pots["mixed"], args.steps, sampler)
+
+    def tmax(x):
+        if ws > 1:
+            t = torch.tensor([x], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    t_mx = tmax(sum(msmx) / 1e3)
+    t_64 = tmax(sum(ms64) / 1e3)
+    value = ws * nat * args.steps / t_mx
+    value64 = ws * nat * args.steps / t_64
+    nl_mx = statistics.mean(q[0] for q in partsmx)
+    kern_mx = statistics.mean(q[3] for q in partsmx)
+    kern_64 = statistics.mean(q[3] for q in parts64)
+    nl_64 = statistics.mean(q[0] for q in parts64)
+
+    # Accuracy of both forms at the workload against each other and the oracle.
+    res = {}
+    for prec in ("fp64", "mixed"):
+        e, f, w = step(pots[prec])
+        res[prec] = (e, f.cpu().numpy().copy(), np.array(w))
+    seed_np, _, _ = nl.get_list(p)
+    fm = flop_model(np.diff(seed_np))
+
+    # e2e through the public API with pinned host buffers.
+    pos_h = torch.empty((nat, 3), dtype=torch.float64).pin_memory()
+    pos_h.copy_(torch.from_numpy(s.positions))
+    f_h = torch.zeros((nat, 3), dtype=torch.float64).pin_memory()
+    pos_np, f_np = pos_h.numpy(), f_h.numpy()
+    pot = pots["mixed"]
+    for _ in range(2):
+        p.set_positions(pos_np)
+        pot.energy_and_forces(p, nl, forces=f_np)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        f_np[...] = 0.0
+        p.set_positions(pos_np)
+        e2e_e, _, e2e_w = pot.energy_and_forces(p, nl, forces=f_np)
+    torch.cuda.synchronize()
+    t_e2e = tmax(time.perf_counter() - t0)
+    e2e = {"value": ws * nat * args.steps / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": 2 * 24 * nat, "d2h_bytes_per_step": 24 * nat + 80,
+           "api": "native.Particles.set_positions + Tersoff.energy_and_forces (C-ABI "
+                  "gb_particles_set_positions / gb_potential_energy_and_forces), pinned "
+                  "host numpy buffers"}
+
+    # Roofline of the dominant kernel (mixed bond-order tile kernel).
+    p32 = _peak(L, 0)
+    p64 = _peak(L, 1)
+    t_k = kern_mx * 1e-3
+    t_roof = max(fm["mixed_fp32"] / (p32 * 1e12), fm["mixed_fp64"] / (p64 * 1e12))
+    bound = "fp32" if fm["mixed_fp32"] / p32 >= fm["mixed_fp64"] / p64 else "fp64"
+    achieved = (fm["mixed_fp32"] if bound == "fp32" else fm["mixed_fp64"]) / t_k / 1e12
+    peak = p32 if bound == "fp32" else p64
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": t_roof / t_k, "traffic": None,
+                "kernel": "bop_tile<Tersoff, float> (mixed form)",
+                "kernel_ms": kern_mx,
+                "peak_source": "FMA-chain microbenchmark in this run (MEASURED_PEAKS.json has "
+                               "no FP32/FP64 peak; no tensor cores on this path)",
+                "fp32_peak_tflops": p32, "fp64_peak_tflops": p64,
+                "fp64_form": {"kernel": "bop_tile<Tersoff, double>", "kernel_ms": kern_64,
+                              "achieved_tflops": fm["fp64_form_fp64"] / (kern_64 * 1e-3) / 1e12,
+                              "frac_of_fp64_peak": fm["fp64_form_fp64"] / (kern_64 * 1e-3)
+                              / (p64 * 1e12)},
+                "flop_model": {"per_bond": FLOPS_BOND, "per_triplet": FLOPS_TRIPLET,
+                               "bonds": fm["bonds"], "triplets": fm["triplets"]}}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_mx / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 three-body/bond-order + fp64 geometry, pair terms, accumulation",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "tersoff_si_amorphous_%d" % nat, "natoms": nat,
+                   "seed": args.seed, "density_gcc": 2.33, "sigma_A": 0.25,
+                   "potential": "Tersoff_PRB_39_5566_Si_C", "parallelism": "replicas" if ws > 1
+                   else "single GPU", "l2": "flushed between steps (256 MB write outside the "
+                                            "timed events)",
+                   "step": "set_positions (D2D) + energy_and_forces incl. full neighbour "
+                           "rebuild"},
+        "fp64_dropin": {"value": value64, "unit": UNIT, "ms_per_step": 1e3 * t_64 / args.steps,
+                        "neighbour_ms": nl_64, "kernel_ms": kern_64},
+        "mixed_over_fp64": value / value64,
+        "value_without_neighbour_build": ws * nat / ((1e3 * t_mx / args.steps - nl_mx) * 1e-3),
+        "neighbour_ms": nl_mx,
+        "e2e": e2e,
+        "roofline": roofline,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    emx, fmx, wmx = res["mixed"]
+    e64, f64, w64 = res["fp64"]
+    line["accuracy"] = {"mixed_vs_fp64_gpu": {"max_abs_dF": float(np.max(np.abs(fmx - f64))),
+                                              "abs_dE_per_atom": abs(emx - e64) / nat,
+                                              "max_abs_dW": float(np.max(np.abs(wmx - w64)))}}
+    if rank == 0 and not args.skip_oracle:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle  # the FP64 checker and the CPU baseline
+        oracle.build()
+        ref = oracle.bop_compute("tersoff", params, s, nthreads=oracle.max_threads())
+        for prec, (e, f, w) in res.items():
+            line["accuracy"][prec + "_vs_oracle"] = {
+                "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
+                "abs_dE_per_atom": abs(e - ref["epot"]) / nat,
+                "max_abs_dW": float(np.max(np.abs(w - ref["wpot"])))}
+        line["cpu_baseline"] = cpu_baseline(s, params, args.cpu_runs)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+_peaks = {}
+
+
+def _peak(L, fp64):
+    import ctypes
+    if fp64 not in _peaks:
+        v = ctypes.c_double(0.0)
+        _lib_check = L.gb_bench_fma_peak(int(fp64), ctypes.byref(v))
+        if _lib_check != 0:
+            raise RuntimeError("FMA peak microbenchmark failed")
+        _peaks[fp64] = v.value
+    return _peaks[fp64]
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -206,10 +206,19 @@ int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *pot, gb_particles_t
 int gb_tabulated_alloy_eam_table(const gb_potential_t *pot, int which, int idx, double *x0dx,
                                  double *coef);
 
-/* Timing of the last energy_and_forces call's phases in milliseconds
- * (CUDA events on the potential's stream): [0] neighbour build,
- * [1] force kernels, [2] total device time.  Returns 0. */
-int gb_potential_last_timing(const gb_potential_t *pot, double *ms3);
+/* ------------------------------------------------------------------------
+ * Diagnostics (no counterpart in the reference; used by the benchmark).
+ * ---------------------------------------------------------------------- */
+/* Timing of the last energy_and_forces call in milliseconds (CUDA events on
+ * the potential's stream): [0] neighbour-list update, [1] force evaluation,
+ * [2] total, [3] the dominant force kernel alone (bond-order tile kernel or
+ * EAM pair kernel).  ms must hold 4 doubles. */
+int gb_potential_last_timing(const gb_potential_t *pot, double *ms);
+/* Number of kernel launches this library has issued since it was loaded. */
+uint64_t gb_kernel_launches(void);
+/* FMA-chain microbenchmark on the current device: sustained FP64 (fp64=1)
+ * or FP32 (fp64=0) throughput in TFLOP/s (2 flops per FMA). */
+int gb_bench_fma_peak(int fp64, double *tflops);
 
 #ifdef __cplusplus
 }
