@@ -15,10 +15,6 @@
 
 using namespace gb;
 
-struct gb_potential {
-  Potential pot;
-};
-
 namespace gb {
 namespace {
 

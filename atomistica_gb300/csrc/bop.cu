@@ -638,3 +638,288 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 }
 
 }  // namespace gb
+
+// ===========================================================================
+// Allocation-free variant of the bond-order evaluation.
+//
+// Some callers cannot call cudaMalloc: codes embedded in a host framework that
+// has already reserved the device memory for its own pool (so cudaMalloc
+// fails or would fragment that pool), and MD loops that must not allocate —
+// or implicitly synchronise the device — inside a time step.  For them
+// gb_bop_energy_and_forces_noalloc evaluates Tersoff or Kumagai on a
+// neighbour list the caller supplies, using only the file-scope scratch array
+// below for every intermediate buffer.  The array is sized for at most
+// kNoallocMaxAtoms atoms and kNoallocMaxEntries list entries; every GPU that
+// loads this library holds it (about 12.5 MB) until the process exits.
+// ===========================================================================
+
+namespace gb {
+namespace {
+
+constexpr int kNoallocMaxAtoms = 16384;
+constexpr int kNoallocMaxEntries = 262144;
+
+constexpr size_t na_align(size_t x) { return (x + 255) & ~size_t(255); }
+// Scratch layout (byte offsets).
+constexpr size_t kNaStatus = 0;                                            // 64 ints
+constexpr size_t kNaRed = kNaStatus + 256;                                 // 16 doubles
+constexpr size_t kNaPos = kNaRed + 256;                                    // Pos4[A]
+constexpr size_t kNaEl = na_align(kNaPos + 32 * (size_t)kNoallocMaxAtoms);  // int[A]
+constexpr size_t kNaSeed = na_align(kNaEl + 4 * (size_t)kNoallocMaxAtoms);  // int[A+1]
+constexpr size_t kNaShift = na_align(kNaSeed + 4 * ((size_t)kNoallocMaxAtoms + 1));
+constexpr size_t kNaRev = na_align(kNaShift + 4 * (size_t)kNoallocMaxEntries);
+constexpr size_t kNaG = na_align(kNaRev + 4 * (size_t)kNoallocMaxEntries);   // 3 doubles/entry
+constexpr size_t kNaE = na_align(kNaG + 24 * (size_t)kNoallocMaxEntries);    // 1 double/entry
+constexpr size_t kNaPart = na_align(kNaE + 8 * (size_t)kNoallocMaxEntries);  // 10 doubles/tile
+constexpr size_t kNoallocBytes = na_align(kNaPart + 80 * (size_t)kNoallocMaxAtoms);
+
+}  // namespace
+}  // namespace gb
+
+// The scratch itself.  Host code must not use this name as an address (on the
+// host it is only a stand-in): the device address is obtained with
+// cudaGetSymbolAddress, once per device, in noalloc_scratch() below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[gb::kNoallocBytes];
+
+namespace gb {
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+unsigned char *g_noalloc_ptr[kNoallocMaxDevices] = {nullptr};
+
+// Device address of the scratch for the current device (set-up on the first
+// call per device).
+int noalloc_scratch(unsigned char **out) {
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocMaxDevices) {
+    set_error("noalloc: device index out of range");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (!g_noalloc_ptr[dev]) {
+    void *ptr = nullptr;
+    GB_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = static_cast<unsigned char *>(ptr);
+  }
+  *out = g_noalloc_ptr[dev];
+  return 0;
+}
+
+// Per atom: padded position, element index (Z -> parameter-set index), int32
+// offsets, max neighbour count.  status[0] = max z, status[1] = flags.
+__global__ void noalloc_prepare(int nat, const double *__restrict__ r, const int *__restrict__ Z,
+                                int nel, int z0, int z1, int z2, const int64_t *__restrict__ seed,
+                                Pos4 *__restrict__ pos, int *__restrict__ el,
+                                int *__restrict__ seed32, int *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nat) return;
+  seed32[i] = (int)seed[i];
+  if (i == nat) return;
+  pos[i] = Pos4{r[3 * i], r[3 * i + 1], r[3 * i + 2], 0.0};
+  const int z = Z[i];
+  el[i] = (nel > 0 && z == z0) ? 0 : (nel > 1 && z == z1) ? 1 : (nel > 2 && z == z2) ? 2 : -1;
+  const int64_t cnt = seed[i + 1] - seed[i];
+  if (cnt < 0) atomicOr(&status[1], 1);
+  atomicMax(&status[0], (int)(cnt > 0 ? cnt : 0));
+}
+
+// Per entry: packed image shift; neighbour index range check.
+__global__ void noalloc_pack(int nat, int n, const int *__restrict__ j, const int *__restrict__ dc,
+                             int *__restrict__ shift, int *__restrict__ status) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const int s0 = dc[3 * b], s1 = dc[3 * b + 1], s2 = dc[3 * b + 2];
+  if (s0 > kMaxShift || s0 < -kMaxShift || s1 > kMaxShift || s1 < -kMaxShift ||
+      s2 > kMaxShift || s2 < -kMaxShift)
+    atomicOr(&status[1], 2);
+  const int jj = j[b];
+  if (jj < 0 || jj >= nat) atomicOr(&status[1], 4);
+  shift[b] = pack_shift(s0, s1, s2);
+}
+
+// rev[b] = entry (j -> i, -s) of entry b = (i -> j, s); the list must be the
+// full symmetric list of gb_neighbors_get.
+__global__ void noalloc_reverse(int nat, const int *__restrict__ seed, const int *__restrict__ nbr,
+                                const int *__restrict__ shift, int *__restrict__ rev,
+                                int *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  for (int b = seed[i]; b < seed[i + 1]; b++) {
+    const int jj = nbr[b];
+    int found = -1;
+    if (jj >= 0 && jj < nat) {
+      int s0, s1, s2;
+      unpack_shift(shift[b], s0, s1, s2);
+      const int want = pack_shift(-s0, -s1, -s2);
+      for (int c = seed[jj]; c < seed[jj + 1]; c++)
+        if (nbr[c] == i && shift[c] == want) {
+          found = c;
+          break;
+        }
+    }
+    if (found < 0) {
+      atomicOr(&status[1], 8);
+      found = b;  // keeps the gather in bounds; the call reports an error
+    }
+    rev[b] = found;
+  }
+}
+
+__global__ void noalloc_finish(const double *__restrict__ red, double *__restrict__ epot,
+                               double *__restrict__ wpot) {
+  if (threadIdx.x == 0) epot[0] = red[0];
+  if (threadIdx.x < 9) wpot[threadIdx.x] += red[1 + threadIdx.x];
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, const double *r,
+                                                const double *cell, const int *Z,
+                                                const int64_t *seed, const int *j, const int *dc,
+                                                double *epot, double *f, double *wpot,
+                                                void *stream) {
+  using namespace gb;
+  clear_error();
+  if (!h || !cell || !epot || !f || !wpot || (nat > 0 && (!r || !Z || !seed))) {
+    set_error("noalloc: missing argument");
+    return GB_ERROR_ARGUMENT;
+  }
+  Potential &pot = h->pot;
+  if (pot.kind != kTersoff && pot.kind != kKumagai) {
+    set_error("noalloc: only the bond-order potentials (Tersoff, Kumagai) are supported");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (nat < 0 || nat > kNoallocMaxAtoms) {
+    set_error("noalloc: nat = " + std::to_string(nat) + " exceeds the maximum of " +
+              std::to_string(kNoallocMaxAtoms) + " atoms");
+    return GB_ERROR_CAPACITY;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char *base = nullptr;
+  GB_CHECK(noalloc_scratch(&base));
+  int *status = reinterpret_cast<int *>(base + kNaStatus);
+  double *red = reinterpret_cast<double *>(base + kNaRed);
+  // The status words and reduction slots keep the previous call's values:
+  // clear them.
+  GB_CUDA(cudaMemsetAsync(status, 0, 256 + 256, s));
+  if (nat == 0) {
+    noalloc_finish<<<1, 32, 0, s>>>(red, epot, wpot);
+    note_launch();
+    GB_CUDA(cudaGetLastError());
+    return 0;
+  }
+  int64_t n64 = 0;
+  GB_CUDA(cudaMemcpyAsync(&n64, seed + nat, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (n64 < 0 || n64 > kNoallocMaxEntries) {
+    set_error("noalloc: the neighbour list has " + std::to_string(n64) +
+              " entries, more than the maximum of " + std::to_string(kNoallocMaxEntries));
+    return GB_ERROR_CAPACITY;
+  }
+  const int n = (int)n64;
+  if (n > 0 && (!j || !dc)) {
+    set_error("noalloc: missing neighbour list arrays");
+    return GB_ERROR_ARGUMENT;
+  }
+  Pos4 *pos = reinterpret_cast<Pos4 *>(base + kNaPos);
+  int *el = reinterpret_cast<int *>(base + kNaEl);
+  int *seed32 = reinterpret_cast<int *>(base + kNaSeed);
+  int *shift = reinterpret_cast<int *>(base + kNaShift);
+  int *rev = reinterpret_cast<int *>(base + kNaRev);
+  double *G = reinterpret_cast<double *>(base + kNaG);
+  double *ebond = reinterpret_cast<double *>(base + kNaE);
+  double *part = reinterpret_cast<double *>(base + kNaPart);
+  const int nel = pot.kind == kTersoff ? pot.tp.nel : 1;
+  const int *pz = pot.kind == kTersoff ? pot.tp.Z : pot.kp.Z;
+  const int z0 = pz[0], z1 = nel > 1 ? pz[1] : -1, z2 = nel > 2 ? pz[2] : -1;
+  noalloc_prepare<<<(nat + 1 + 127) / 128, 128, 0, s>>>(nat, r, Z, nel, z0, z1, z2, seed, pos, el,
+                                                       seed32, status);
+  note_launch();
+  if (n > 0) {
+    noalloc_pack<<<(n + 255) / 256, 256, 0, s>>>(nat, n, j, dc, shift, status);
+    note_launch();
+  }
+  noalloc_reverse<<<(nat + 127) / 128, 128, 0, s>>>(nat, seed32, j, shift, rev, status);
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  int hs[2] = {0, 0};
+  GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (hs[1]) {
+    set_error(std::string("noalloc: invalid neighbour list (") +
+              ((hs[1] & 1) ? "decreasing offsets " : "") +
+              ((hs[1] & 2) ? "image shift beyond +-511 " : "") +
+              ((hs[1] & 4) ? "neighbour index out of range " : "") +
+              ((hs[1] & 8) ? "list not symmetric" : "") + ")");
+    return GB_ERROR_ARGUMENT;
+  }
+  // Tile size as in bop_compute.
+  const int maxz = std::max(hs[0], 1);
+  int apt = kMaxApt;
+  auto fits = [&](int aptc) {
+    return bop_smem_bytes<double>(aptc * maxz, aptc * maxz * maxz) <= kSmemBudget;
+  };
+  while (apt > 1 && !fits(apt)) apt >>= 1;
+  while (apt > 1 && (int64_t)apt * std::max(1, n / nat) > 2 * kBopThreads) apt >>= 1;
+  if (!fits(apt)) {
+    set_error("noalloc: an atom has " + std::to_string(maxz) +
+              " neighbours, more than the bond-order kernel supports");
+    return GB_ERROR_CAPACITY;
+  }
+  const int ntiles = (nat + apt - 1) / apt;
+  int *plan = status + 4;
+  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, seed32, plan);
+  note_launch();
+  int hp[2] = {0, 0};
+  GB_CUDA(cudaMemcpyAsync(hp, plan, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+
+  BopArgs args;
+  args.nat = nat;
+  args.apt = apt;
+  args.pos = pos;
+  args.el = el;
+  args.seed = seed32;
+  args.nbr = j;
+  args.shift = shift;
+  args.mask = nullptr;
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 3; k++) args.A[a][k] = cell[3 * k + a];
+  args.G = G;
+  args.ebond = ebond;
+  args.wbond = nullptr;
+  args.frbond = nullptr;
+  args.tile_part = part;
+  const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  int rc;
+  if (pot.kind == kTersoff) {
+    TersoffPot tp{make_tersoff_dev(pot.tp)};
+    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, ntiles, hp[0], hp[1], status + 2,
+                                                  false, false, s)
+               : dispatch_tile<TersoffPot, double>(args, tp, ntiles, hp[0], hp[1], status + 2,
+                                                   false, false, s);
+  } else {
+    KumagaiPot kp{make_kumagai_dev(pot.kp)};
+    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, ntiles, hp[0], hp[1], status + 2,
+                                                  false, false, s)
+               : dispatch_tile<KumagaiPot, double>(args, kp, ntiles, hp[0], hp[1], status + 2,
+                                                   false, false, s);
+  }
+  GB_CHECK(rc);
+  bop_gather<false, false><<<(nat + 127) / 128, 128, 0, s>>>(nat, seed32, rev, G, ebond, nullptr,
+                                                              f, nullptr, nullptr);
+  note_launch();
+  GB_CHECK(reduce_partials(part, ntiles, 10, red, s));
+  noalloc_finish<<<1, 32, 0, s>>>(red, epot, wpot);
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  int hst = 0;
+  GB_CUDA(cudaMemcpyAsync(&hst, status + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (hst) {
+    set_error("noalloc: internal error (tile plan mismatch)");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  return 0;
+}

@@ -99,3 +99,8 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 int reduce_partials(const double *part, int ntiles, int nc, double *red, cudaStream_t s);
 
 }  // namespace gb
+
+// Opaque handle type of the C-ABI.
+struct gb_potential {
+  gb::Potential pot;
+};

@@ -207,6 +207,40 @@ int gb_tabulated_alloy_eam_table(const gb_potential_t *pot, int which, int idx, 
                                  double *coef);
 
 /* ------------------------------------------------------------------------
+ * Allocation-free evaluation.  This entry point has no counterpart in the
+ * reference.  It is meant for callers that cannot call cudaMalloc: codes
+ * embedded in a host framework that has already reserved the device memory
+ * for its own pool, and MD loops that must not allocate (nor implicitly
+ * synchronise the device) during a time step.  It evaluates a Tersoff or
+ * Kumagai potential (FP64 or mixed, as set on `pot`) on a neighbour list the
+ * caller supplies and allocates nothing: all intermediate buffers live in one
+ * static device array of about 12.5 MB that every GPU loading this library
+ * holds until the process exits.
+ *
+ *   limits: nat <= 16384 atoms and at most 262144 list entries; larger
+ *           inputs are rejected with GB_ERROR_CAPACITY and a message.
+ *   device memory: r (nat,3), Z (nat), seed (nat+1, int64), j (n), dc (n,3)
+ *           — the full symmetric list in the layout of gb_neighbors_get —
+ *           and the outputs epot (1 double, set), f (nat,3) and wpot (9,
+ *           Fortran order), both accumulated into, as in
+ *           gb_potential_energy_and_forces.
+ *   host memory: cell (3x3, rows = lattice vectors).
+ *   stream: the CUDA stream all work is issued on (NULL = default stream);
+ *           the call returns after that stream has finished its work.
+ *   set-up: the first call on a device looks up the device address of the
+ *           static array (cudaGetSymbolAddress); make that first call before
+ *           any stream capture.
+ *   sharing: every call uses the same array and finds it holding the
+ *           previous call's data (the call clears what must start at zero);
+ *           calls that overlap on the GPU — from several host threads or
+ *           streams — race on it and must be serialised by the caller.
+ * ---------------------------------------------------------------------- */
+int gb_bop_energy_and_forces_noalloc(gb_potential_t *pot, int nat, const double *r,
+                                     const double *cell, const int *Z, const int64_t *seed,
+                                     const int *j, const int *dc, double *epot, double *f,
+                                     double *wpot, void *cuda_stream);
+
+/* ------------------------------------------------------------------------
  * Diagnostics (no counterpart in the reference; used by the benchmark).
  * ---------------------------------------------------------------------- */
 /* Timing of the last energy_and_forces call in milliseconds (CUDA events on
