@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "bop_math.h"
 #include "potential.h"
@@ -68,12 +69,12 @@ struct BopArgs {
   double *tile_part;  // 10 per tile
 };
 
-template <class R>
+// Shared-memory layout of one tile (nbt bonds, ntrip (ij, ik) slots).
 struct SmemLayout {
-  int *aseed, *toff, *el, *meta;
-  double *rn64, *r64, *fc64, *dfc64, *P, *G;
-  R *rn, *rl, *rinv, *fc, *dfc;
-  R *t;  // 3 * ntrip
+  int *aseed, *toff, *el, *meta, *hot;
+  double *rn64, *r64, *rinv64, *fc64, *dfc64, *P, *G, *E;  // per bond
+  float *rnf, *rlf, *rinvf, *fcf, *dfcf;                   // per bond (mixed form)
+  double *t;                                               // 3 per (ij, ik) slot
   int nbt, ntrip;
 };
 
@@ -81,16 +82,15 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 
 template <class R>
 __host__ __device__ inline size_t bop_smem_bytes(int nbt, int ntrip) {
-  size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + nbt));
-  o += align16(sizeof(double) * (size_t)nbt * 10);
-  o += align16(sizeof(R) * (size_t)nbt * 7);
-  o += align16(sizeof(R) * (size_t)ntrip * 3);
+  size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + 2 * (size_t)nbt));
+  o += align16(sizeof(double) * (size_t)nbt * 12);
+  o += align16(sizeof(float) * (size_t)nbt * 7);
+  o += align16(sizeof(double) * (size_t)ntrip * 3);
   return o + 64;
 }
 
-template <class R>
-__device__ inline SmemLayout<R> carve(unsigned char *sm, int nbt, int ntrip) {
-  SmemLayout<R> L;
+__device__ inline SmemLayout carve(unsigned char *sm, int nbt, int ntrip) {
+  SmemLayout L;
   L.nbt = nbt;
   L.ntrip = ntrip;
   int *ip = reinterpret_cast<int *>(sm);
@@ -98,23 +98,26 @@ __device__ inline SmemLayout<R> carve(unsigned char *sm, int nbt, int ntrip) {
   L.toff = ip + kMaxApt + 1;
   L.el = ip + 2 * kMaxApt + 2;
   L.meta = ip + 3 * kMaxApt + 2;
-  size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + nbt));
+  L.hot = L.meta + nbt;
+  size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + 2 * (size_t)nbt));
   double *dp = reinterpret_cast<double *>(sm + o);
   L.rn64 = dp;
   L.r64 = dp + 3 * nbt;
-  L.fc64 = dp + 4 * nbt;
-  L.dfc64 = dp + 5 * nbt;
-  L.P = dp + 6 * nbt;
-  L.G = dp + 7 * nbt;
-  o += align16(sizeof(double) * (size_t)nbt * 10);
-  R *rp = reinterpret_cast<R *>(sm + o);
-  L.rn = rp;
-  L.rl = rp + 3 * nbt;
-  L.rinv = rp + 4 * nbt;
-  L.fc = rp + 5 * nbt;
-  L.dfc = rp + 6 * nbt;
-  o += align16(sizeof(R) * (size_t)nbt * 7);
-  L.t = reinterpret_cast<R *>(sm + o);
+  L.rinv64 = dp + 4 * nbt;
+  L.fc64 = dp + 5 * nbt;
+  L.dfc64 = dp + 6 * nbt;
+  L.P = dp + 7 * nbt;
+  L.G = dp + 8 * nbt;
+  L.E = dp + 11 * nbt;
+  o += align16(sizeof(double) * (size_t)nbt * 12);
+  float *fp = reinterpret_cast<float *>(sm + o);
+  L.rnf = fp;
+  L.rlf = fp + 3 * nbt;
+  L.rinvf = fp + 4 * nbt;
+  L.fcf = fp + 5 * nbt;
+  L.dfcf = fp + 6 * nbt;
+  o += align16(sizeof(float) * (size_t)nbt * 7);
+  L.t = reinterpret_cast<double *>(sm + o);
   return L;
 }
 
@@ -139,12 +142,161 @@ __device__ inline void block_sum(double (&v)[NC], double *out, double *scratch) 
   __syncthreads();
 }
 
+// k loop of bond ij = lb in FP64 (bop_kernel.f90:1171-1343): zeta_ij,
+// d zeta/d r_j (dbj), d zeta_ij/d r_k into trow (component c at
+// trow[c*ntrip + q]) and, for the per-atom virial, sum_k r_ik (x) dzeta/dr_k.
+template <class Pot, bool kWat>
+__device__ __forceinline__ void kloop64(const Pot &pot, const SmemLayout &L, int lb, int s, int z,
+                                        int eli, double *trow, double &zeta, double dbj[3],
+                                        double wk[9]) {
+  const int nbt = L.nbt, ntrip = L.ntrip;
+  const double rnij[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
+  const double rlij = L.r64[lb], rinvj = L.rinv64[lb];
+  for (int q = 0; q < z; q++) {
+    const int lk = s + q;
+    if (lk == lb) continue;
+    const int mk = L.meta[lk];
+    if (!(mk & kFlagK)) {
+      trow[q] = 0.0;
+      trow[ntrip + q] = 0.0;
+      trow[2 * ntrip + q] = 0.0;
+      continue;
+    }
+    const int ikpot = (mk >> 8) & 0xf;
+    const double rnik[3] = {L.rn64[lk], L.rn64[nbt + lk], L.rn64[2 * nbt + lk]};
+    const double rlik = L.r64[lk], rinvk = L.rinv64[lk], fcik = L.fc64[lk], dfcik = L.dfc64[lk];
+    double hv, dh;
+    pot.template h<double>(ikpot, rlij - rlik, hv, dh);
+    const double cs = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
+    double gv, dg;
+    pot.template g<double>(eli, ikpot, cs, gv, dg);
+    const double dzfac = fcik * dg * hv;
+    zeta += fcik * gv * hv;
+    const double dzdrij = gv * fcik * dh;
+    const double dzdrik = gv * (dfcik * hv - fcik * dh);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      // d cos/d r_j = (n_ik - cos n_ij)/r_ij ; d cos/d r_k = (n_ij - cos n_ik)/r_ik
+      const double dcj = (rnik[c] - cs * rnij[c]) * rinvj;
+      const double dck = (rnij[c] - cs * rnik[c]) * rinvk;
+      dbj[c] += dzdrij * rnij[c] + dzfac * dcj;
+      const double dk = dzdrik * rnik[c] + dzfac * dck;
+      trow[c * ntrip + q] = dk;
+      if (kWat)
+#pragma unroll
+        for (int c1 = 0; c1 < 3; c1++) wk[3 * c1 + c] += rnik[c1] * rlik * dk;
+    }
+  }
+}
+
+// The same k loop with FP32 three-body arithmetic (mixed form).  h - cos
+// theta is formed from the FP64 unit vectors: g' ~ 1e5 amplifies any error of
+// cos theta.  Also returns sum |d zeta/d r_k| for the error estimate.
+template <class Pot, bool kWat>
+__device__ __forceinline__ void kloop32(const Pot &pot, const SmemLayout &L, int lb, int s, int z,
+                                        int eli, double *trow, float &zeta, float dbj[3],
+                                        float wk[9], float &sumdk) {
+  const int nbt = L.nbt, ntrip = L.ntrip;
+  const float rnij[3] = {L.rnf[lb], L.rnf[nbt + lb], L.rnf[2 * nbt + lb]};
+  const float rlij = L.rlf[lb], rinvj = L.rinvf[lb];
+  const double rn64j[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
+  const double hpar = pot.hpar(eli);
+  for (int q = 0; q < z; q++) {
+    const int lk = s + q;
+    if (lk == lb) continue;
+    const int mk = L.meta[lk];
+    if (!(mk & kFlagK)) {
+      trow[q] = 0.0;
+      trow[ntrip + q] = 0.0;
+      trow[2 * ntrip + q] = 0.0;
+      continue;
+    }
+    const int ikpot = (mk >> 8) & 0xf;
+    const float rnik[3] = {L.rnf[lk], L.rnf[nbt + lk], L.rnf[2 * nbt + lk]};
+    const float rlik = L.rlf[lk], rinvk = L.rinvf[lk], fcik = L.fcf[lk], dfcik = L.dfcf[lk];
+    float hv, dh;
+    pot.template h<float>(ikpot, rlij - rlik, hv, dh);
+    const double cs64 = L.rn64[lk] * rn64j[0] + L.rn64[nbt + lk] * rn64j[1] +
+                        L.rn64[2 * nbt + lk] * rn64j[2];
+    const float cs = (float)cs64;
+    float gv, dg;
+    pot.template g_hc<float>(eli, ikpot, (float)(hpar - cs64), gv, dg);
+    const float dzfac = fcik * dg * hv;
+    zeta += fcik * gv * hv;
+    const float dzdrij = gv * fcik * dh;
+    const float dzdrik = gv * (dfcik * hv - fcik * dh);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float dcj = (rnik[c] - cs * rnij[c]) * rinvj;
+      const float dck = (rnij[c] - cs * rnik[c]) * rinvk;
+      dbj[c] += dzdrij * rnij[c] + dzfac * dcj;
+      const float dk = dzdrik * rnik[c] + dzfac * dck;
+      trow[c * ntrip + q] = (double)dk;
+      sumdk += fabsf(dk);
+      if (kWat)
+#pragma unroll
+        for (int c1 = 0; c1 < 3; c1++) wk[3 * c1 + c] += rnik[c1] * rlik * dk;
+    }
+  }
+}
+
+// Energy, radial force, G partial and per-bond outputs of bond ij
+// (bop_kernel.f90:1356-1518).  The energy goes to L.E (summed later in a
+// fixed order).
+template <bool kWat, bool kPB>
+__device__ __forceinline__ void finalize_bond(const BopArgs &a, const SmemLayout &L, int lb, int b,
+                                              double bij, double P, const double dbj[3],
+                                              const double wk[9], double VA, double dVA,
+                                              double VR, double dVR) {
+  const int nbt = L.nbt;
+  const double fcij = L.fc64[lb], dfcij = L.dfc64[lb];
+  const double e_b = 0.5 * fcij * (VR + bij * VA);
+  const double dff = 0.5 * (dVR * fcij + bij * dVA * fcij + VR * dfcij + bij * VA * dfcij);
+  const double rn64[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
+  double dfr[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    dfr[c] = dff * rn64[c];
+    L.G[c * nbt + lb] = -dfr[c] - P * dbj[c];
+  }
+  L.P[lb] = P;
+  L.E[lb] = e_b;
+  a.ebond[b] = e_b;
+  if (kPB) {
+    a.frbond[3 * (size_t)b] = dfr[0];
+    a.frbond[3 * (size_t)b + 1] = dfr[1];
+    a.frbond[3 * (size_t)b + 2] = dfr[2];
+  }
+  if (kWat) {
+    // w_ij = r_ij (x) df - P wijb, wijb = -r_ij (x) dbidj - sum_k r_ik (x) dbidk
+    const double r = L.r64[lb];
+    const double rij[3] = {r * rn64[0], r * rn64[1], r * rn64[2]};
+#pragma unroll
+    for (int c1 = 0; c1 < 3; c1++)
+#pragma unroll
+      for (int c2 = 0; c2 < 3; c2++)
+        a.wbond[9 * (size_t)b + c1 + 3 * c2] =
+            rij[c1] * dfr[c2] + P * (rij[c1] * dbj[c2]) + P * wk[3 * c1 + c2];
+  }
+}
+
+// Mixed form: bonds whose estimated FP32 error exceeds this (eV/A) are
+// recomputed in FP64 (about 6 % of the bonds at the 2.33 g/cm^3, sigma =
+// 0.25 A workload).
+constexpr float kHotThreshold = 1.0e-6f;
+
 template <class Pot, class R, bool kWat, bool kPB>
 __global__ void __launch_bounds__(kBopThreads)
     bop_tile(const BopArgs a, const Pot pot, int max_nbt, int max_ntrip, int *status) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ double red_scratch[(kBopThreads / 32) * 9];
+  __shared__ double s_exp2[256];
+  __shared__ int s_nhot;
+  constexpr bool kMix = std::is_same<R, float>::value;
   const int tid = threadIdx.x;
+  if (kMix)
+    for (int q = tid; q < 256; q += kBopThreads) s_exp2[q] = kExp2Tab[q];
+  if (tid == 0) s_nhot = 0;
   const int a0 = blockIdx.x * a.apt;
   const int a1 = min(a0 + a.apt, a.nat);
   const int na = a1 - a0;
@@ -177,7 +329,7 @@ __global__ void __launch_bounds__(kBopThreads)
     if (tid == 0) atomicOr(status, 2);
     return;
   }
-  SmemLayout<R> L = carve<R>(sm, nbt, ntrip);
+  SmemLayout L = carve(sm, nbt, ntrip);
   for (int q = tid; q < na; q += kBopThreads)
     for (int lb = L.aseed[q]; lb < L.aseed[q + 1]; lb++) L.meta[lb] = q;
   __syncthreads();
@@ -193,7 +345,7 @@ __global__ void __launch_bounds__(kBopThreads)
     const int eli = L.el[ai];
     const int elj = a.el[j];
     int meta = ai;
-    double fc = 0.0, dfc = 0.0, r = 1.0;
+    double fc = 0.0, dfc = 0.0, r = 1.0, rinv = 1.0;
     double rn[3] = {0.0, 0.0, 0.0};
     if (eli >= 0 && elj >= 0) {
       const Pos4 pi = a.pos[i], pj = a.pos[j];
@@ -222,13 +374,27 @@ __global__ void __launch_bounds__(kBopThreads)
         dfc = 0.0;
         in_short = true;
       } else if (r2 < pot.r2sq(t)) {
-        trig_off(__dsqrt_rn(r2), pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
         in_short = true;
       }
       if (in_short) {
-        r = __dsqrt_rn(r2);
+        if (kMix) {
+          // r and 1/r from an FP32 rsqrt seed and one FP64 Newton step (~48
+          // bits); FP64 trig cutoff (its derivative is multiplied by g ~ 1e4).
+          double y = (double)rsqrtf((float)r2);
+          y = y * fma(-0.5 * r2, y * y, 1.5);
+          r = r2 * y;
 #pragma unroll
-        for (int c = 0; c < 3; c++) rn[c] = rij[c] / r;
+          for (int c = 0; c < 3; c++) rn[c] = rij[c] * y;
+          rinv = y;
+          if (!(r2 < pot.r1sq(t))) trig_off(r, pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
+        } else {
+          if (!(r2 < pot.r1sq(t)))
+            trig_off(__dsqrt_rn(r2), pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
+          r = __dsqrt_rn(r2);
+#pragma unroll
+          for (int c = 0; c < 3; c++) rn[c] = rij[c] / r;
+          rinv = 1.0 / r;
+        }
         int mf = 2;
         if (a.mask) {
           const int mi = a.mask[i], mj = a.mask[j];
@@ -246,22 +412,23 @@ __global__ void __launch_bounds__(kBopThreads)
     }
     L.meta[lb] = meta;
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      L.rn64[c * nbt + lb] = rn[c];
-      L.rn[c * nbt + lb] = (R)rn[c];
-    }
+    for (int c = 0; c < 3; c++) L.rn64[c * nbt + lb] = rn[c];
     L.r64[lb] = r;
+    L.rinv64[lb] = rinv;
     L.fc64[lb] = fc;
     L.dfc64[lb] = dfc;
-    L.rl[lb] = (R)r;
-    L.rinv[lb] = (R)(1.0 / r);
-    L.fc[lb] = (R)fc;
-    L.dfc[lb] = (R)dfc;
+    if (kMix) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) L.rnf[c * nbt + lb] = (float)rn[c];
+      L.rlf[lb] = (float)r;
+      L.rinvf[lb] = (float)rinv;
+      L.fcf[lb] = (float)fc;
+      L.dfcf[lb] = (float)dfc;
+    }
   }
   __syncthreads();
 
   // ---- Phase 2: zeta, bond order, pair terms (pass 2, :1074-1529). ----
-  double eacc[1] = {0.0};
   for (int lb = tid; lb < nbt; lb += kBopThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
@@ -270,6 +437,7 @@ __global__ void __launch_bounds__(kBopThreads)
       L.G[lb] = 0.0;
       L.G[nbt + lb] = 0.0;
       L.G[2 * nbt + lb] = 0.0;
+      L.E[lb] = 0.0;
       a.ebond[b] = 0.0;
       if (kPB) {
         a.frbond[3 * (size_t)b] = 0.0;
@@ -284,128 +452,119 @@ __global__ void __launch_bounds__(kBopThreads)
     const int t = (meta >> 8) & 0xf;
     const int mf = (meta >> 16) & 3;
     const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-    R *trow = L.t + L.toff[ai] + p * z;  // component c at trow[c*ntrip + q]
+    double *trow = L.t + L.toff[ai] + p * z;
     const int eli = L.el[ai];
-    const R rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
-    const R rlij = L.rl[lb], rinvj = L.rinv[lb];
-    R zeta = R(0);
-    R dbj[3] = {R(0), R(0), R(0)};
-    R wk[9];
-    if (kWat)
-#pragma unroll
-      for (int c = 0; c < 9; c++) wk[c] = R(0);
-    for (int q = 0; q < z; q++) {
-      const int lk = s + q;
-      if (lk == lb) continue;
-      const int mk = L.meta[lk];
-      if (!(mk & kFlagK)) {
-        trow[q] = R(0);
-        trow[ntrip + q] = R(0);
-        trow[2 * ntrip + q] = R(0);
-        continue;
-      }
-      const int ikpot = (mk >> 8) & 0xf;
-      const R rnik[3] = {L.rn[lk], L.rn[nbt + lk], L.rn[2 * nbt + lk]};
-      const R rlik = L.rl[lk], rinvk = L.rinv[lk], fcik = L.fc[lk], dfcik = L.dfc[lk];
-      R hv, dh;
-      pot.template h<R>(ikpot, rlij - rlik, hv, dh);
-      const R cs = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
-      R gv, dg;
-      pot.template g<R>(eli, ikpot, cs, gv, dg);
-      const R dzfac = fcik * dg * hv;
-      zeta += fcik * gv * hv;
-      const R dzdrij = gv * fcik * dh;
-      const R dzdrik = gv * (dfcik * hv - fcik * dh);
-      R dk[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        // d cos / d r_j = (rn_ik - cos rn_ij)/r_ij ; d cos / d r_k = (rn_ij - cos rn_ik)/r_ik
-        const R dcj = (rnik[c] - cs * rnij[c]) * rinvj;
-        const R dck = (rnij[c] - cs * rnik[c]) * rinvk;
-        dbj[c] += dzdrij * rnij[c] + dzfac * dcj;
-        dk[c] = dzdrik * rnik[c] + dzfac * dck;
-        trow[c * ntrip + q] = dk[c];
-      }
-      if (kWat) {
-#pragma unroll
-        for (int c1 = 0; c1 < 3; c1++)
-#pragma unroll
-          for (int c2 = 0; c2 < 3; c2++) wk[3 * c1 + c2] += rnik[c1] * rlik * dk[c2];
-      }
-    }
-    // Pair terms in FP64 (tersoff_func.f90:32-78), scaled by maskfac/2.
     const double r = L.r64[lb];
-    double VA, dVA, VR, dVR;
-    pot.VA(t, r, VA, dVA);
-    pot.VR(t, r, VR, dVR);
     const double hm = 0.5 * mf;
+    const double fcij = L.fc64[lb];
+    double VA, dVA, VR, dVR;
+    if (kMix) {
+      VA = -pot.Bc(t) * exp_acc(-pot.cA(t) * r, s_exp2);
+      dVA = -pot.cA(t) * VA;
+      VR = pot.Ac(t) * exp_acc(-pot.cR(t) * r, s_exp2);
+      dVR = -pot.cR(t) * VR;
+    } else {
+      // VA, VR (tersoff_func.f90:32-78) scaled by maskfac/2 (:1133-1139)
+      pot.VA(t, r, VA, dVA);
+      pot.VR(t, r, VR, dVR);
+    }
     VA *= hm;
     dVA *= hm;
     VR *= hm;
     dVR *= hm;
-    const double fcij = L.fc64[lb], dfcij = L.dfc64[lb];
-    double bij, P;
-    {
-      R bR, PR;
-      pot.template bo<R>(eli, t, zeta, (R)fcij, (R)VA, bR, PR);
-      bij = bR;
-      P = PR;
-    }
-    const double e_b = 0.5 * fcij * (VR + bij * VA);
-    const double dff = 0.5 * (dVR * fcij + bij * dVA * fcij + VR * dfcij + bij * VA * dfcij);
-    const double rn64[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
-    double dfr[3], Gp[3];
+    if (!kMix) {
+      double zeta = 0.0, dbj[3] = {0.0, 0.0, 0.0}, wk[9];
+      if (kWat)
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      dfr[c] = dff * rn64[c];
-      Gp[c] = -dfr[c] - P * (double)dbj[c];
-    }
-    L.P[lb] = P;
-    L.G[lb] = Gp[0];
-    L.G[nbt + lb] = Gp[1];
-    L.G[2 * nbt + lb] = Gp[2];
-    a.ebond[b] = e_b;
-    eacc[0] += e_b;
-    if (kPB) {
-      a.frbond[3 * (size_t)b] = dfr[0];
-      a.frbond[3 * (size_t)b + 1] = dfr[1];
-      a.frbond[3 * (size_t)b + 2] = dfr[2];
-    }
-    if (kWat) {
-      // w_ij = r_ij (x) df - P wijb, wijb = -r_ij (x) dbidj - sum_k r_ik (x) dbidk
-      const double rij[3] = {r * rn64[0], r * rn64[1], r * rn64[2]};
+        for (int c = 0; c < 9; c++) wk[c] = 0.0;
+      kloop64<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk);
+      double bij, P;
+      pot.template bo<double>(eli, t, zeta, fcij, VA, bij, P);
+      finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
+    } else {
+      float zeta = 0.0f, dbj[3] = {0.0f, 0.0f, 0.0f}, wk[9], sumdk = 0.0f;
+      if (kWat)
 #pragma unroll
-      for (int c1 = 0; c1 < 3; c1++)
+        for (int c = 0; c < 9; c++) wk[c] = 0.0f;
+      kloop32<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
+      double bij, P;
+      pot.bo_mixed(eli, t, zeta, fcij, VA, s_exp2, bij, P);
+      // Estimated FP32 error of this bond's force contributions: zeta (and
+      // hence b) to ~2.4e-7 relative, the three-body derivatives to ~3e-7.
+      const float sens = pot.bsens(eli, zeta);
+      const float est = 2.4e-7f * fabsf((float)dVA) * (float)fcij * sens +
+                        3.0e-7f * fabsf((float)P) *
+                            (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
+      if (est > kHotThreshold) {
+        L.hot[atomicAdd(&s_nhot, 1)] = lb;
+      } else {
+        const double dbjd[3] = {dbj[0], dbj[1], dbj[2]};
+        double wkd[9];
+        if (kWat)
 #pragma unroll
-        for (int c2 = 0; c2 < 3; c2++) {
-          const double w = rij[c1] * dfr[c2] + P * (rij[c1] * (double)dbj[c2]) +
-                           P * (double)wk[3 * c1 + c2];
-          a.wbond[9 * (size_t)b + c1 + 3 * c2] = w;  // Fortran (c1, c2)
-        }
+          for (int c = 0; c < 9; c++) wkd[c] = wk[c];
+        finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbjd, wkd, VA, dVA, VR, dVR);
+      }
+    }
+  }
+  if (kMix) {
+    __syncthreads();
+    // ---- Phase 2b (mixed form): FP64 recomputation of the hot bonds. ----
+    const int nhot = s_nhot;
+    for (int h = tid; h < nhot; h += kBopThreads) {
+      const int lb = L.hot[h];
+      const int b = b0 + lb;
+      const int meta = L.meta[lb];
+      const int ai = meta & 0xff;
+      const int t = (meta >> 8) & 0xf;
+      const int mf = (meta >> 16) & 3;
+      const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
+      double *trow = L.t + L.toff[ai] + p * z;
+      const int eli = L.el[ai];
+      const double r = L.r64[lb];
+      const double hm = 0.5 * mf;
+      double VA = -pot.Bc(t) * exp_acc(-pot.cA(t) * r, s_exp2);
+      double dVA = -pot.cA(t) * VA;
+      double VR = pot.Ac(t) * exp_acc(-pot.cR(t) * r, s_exp2);
+      double dVR = -pot.cR(t) * VR;
+      VA *= hm;
+      dVA *= hm;
+      VR *= hm;
+      dVR *= hm;
+      double zeta = 0.0, dbj[3] = {0.0, 0.0, 0.0}, wk[9];
+      if (kWat)
+#pragma unroll
+        for (int c = 0; c < 9; c++) wk[c] = 0.0;
+      kloop64<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk);
+      double bij, P;
+      pot.template bo<double>(eli, t, zeta, L.fc64[lb], VA, bij, P);
+      finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
     }
   }
   __syncthreads();
 
   // ---- Phase 3: forces on the end atoms (k-role), total virial. ----
+  double eacc[1] = {0.0};
   double wacc[9];
 #pragma unroll
   for (int c = 0; c < 9; c++) wacc[c] = 0.0;
   for (int lb = tid; lb < nbt; lb += kBopThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
+    eacc[0] += L.E[lb];
     double G[3] = {L.G[lb], L.G[nbt + lb], L.G[2 * nbt + lb]};
     if (meta & kFlagK) {
       const int ai = meta & 0xff;
       const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, q = lb - s;
-      const R *tcol = L.t + L.toff[ai] + q;
+      const double *tcol = L.t + L.toff[ai] + q;
       for (int p = 0; p < z; p++) {
         const int lp = s + p;
         if (lp == lb) continue;
         if (!(L.meta[lp] & kFlagIJ)) continue;
         const double P = L.P[lp];
-        const R *tv = tcol + p * z;
+        const double *tv = tcol + p * z;
 #pragma unroll
-        for (int c = 0; c < 3; c++) G[c] -= P * (double)tv[c * ntrip];
+        for (int c = 0; c < 3; c++) G[c] -= P * tv[c * ntrip];
       }
       const double r = L.r64[lb];
       const double rb[3] = {r * L.rn64[lb], r * L.rn64[nbt + lb], r * L.rn64[2 * nbt + lb]};

@@ -9,10 +9,14 @@
 //   K1d nl_sort_cells     per-cell sort by atom id, so that every cell lists its
 //                         atoms in increasing id as the reference's linked
 //                         list does (binning_update, :904-959).
+//   K1e nl_gather_sorted  float positions (+ id, wrap) in cell-sorted order.
 //   K2  nl_pairs<count>   per atom (cell-sorted thread order): stencil loop in
-//                         the reference order, FP64 test |r_i - r_j + A s|^2 <
-//                         cutoff^2 evaluated without FMA contraction in the
-//                         reference's order (:708-711) -> per-atom counts.
+//                         the reference order; each candidate is decided by an
+//                         FP32 test with a rigorous error bound, and only the
+//                         few inside the uncertainty band take the reference's
+//                         FP64 test |r_i - r_j + A s|^2 < cutoff^2 (no FMA
+//                         contraction, reference order, :708-711), so the
+//                         decision always equals the reference's -> counts.
 //   K2b exclusive scan    CSR offsets.
 //   K2c nl_pairs<fill>    same loop, writes j and the packed image shift.
 // The resulting per-atom entry order equals the reference's (stencil offset
@@ -259,6 +263,8 @@ struct BinParams {
   int pbc[3];
   int dx, dy, dz;
   double cutoff_sq;
+  float cutoff_f;                    // cutoff rounded up to float
+  float cutoff_sq_lo, cutoff_sq_hi;  // float bracket of cutoff^2
 };
 
 __device__ __forceinline__ int floor_div(int a, int n) {
@@ -300,6 +306,10 @@ __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams
     atom_wrap[i] = pack_wrap(0, 0, 0);
     atomicAdd(&cell_count[0], 1);
     return;
+  }
+  {
+    const float m = fmaxf(fabsf((float)x), fmaxf(fabsf((float)y), fabsf((float)z)));
+    atomicMax(&status[3], __float_as_int(m * (1.0f + 1.2e-7f)));
   }
   int c[3], q[3];
   raw_cell(bp, x, y, z, c);
@@ -387,17 +397,61 @@ __global__ void nl_copy_big_cells(const int *__restrict__ big_cells, const int *
   }
 }
 
+// Per sorted slot: float copy of the position with the atom id in .w and the
+// atom's wrap counts, so that the candidate loop reads one 16-byte record.
+__global__ void nl_gather_sorted(int nat, const int *__restrict__ cell_atoms,
+                                 const Pos4 *__restrict__ pos4, const int *__restrict__ atom_wrap,
+                                 float4 *__restrict__ spos, int *__restrict__ swrap) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nat) return;
+  const int i = cell_atoms[t];
+  const Pos4 p = pos4[i];
+  spos[t] = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(i));
+  swrap[t] = atom_wrap[i];
+}
+
+// Exact reference test |r_i - r_j + A s|^2 < cutoff^2: FP64, no FMA
+// contraction, reference operation order (python_neighbors.f90:708-711).
+__device__ __forceinline__ bool exact_pair_test(const BinParams &bp, const Pos4 &ri,
+                                                const Pos4 &rj, int s0, int s1, int s2) {
+  const double sx = (double)s0, sy = (double)s1, sz = (double)s2;
+  const double rij[3] = {__dsub_rn(ri.x, rj.x), __dsub_rn(ri.y, rj.y), __dsub_rn(ri.z, rj.z)};
+  double d[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    double as = __dmul_rn(bp.A[a][0], sx);
+    as = __dadd_rn(as, __dmul_rn(bp.A[a][1], sy));
+    as = __dadd_rn(as, __dmul_rn(bp.A[a][2], sz));
+    d[a] = __dadd_rn(rij[a], as);
+  }
+  double d2 = __dmul_rn(d[0], d[0]);
+  d2 = __dadd_rn(d2, __dmul_rn(d[1], d[1]));
+  d2 = __dadd_rn(d2, __dmul_rn(d[2], d[2]));
+  return d2 < bp.cutoff_sq;
+}
+
+// Candidate loop.  Every candidate is first tested in FP32 against a
+// rigorous error bound of the FP32 evaluation (positions rounded to float,
+// the image term and the squared norm); only candidates whose FP32 distance
+// falls inside the uncertainty band around the cutoff take the exact FP64
+// test.  The decision is therefore always the reference's, while almost all
+// arithmetic runs on the FP32 pipe.
+//
+// Error bound: with u = 2^-24, X = max |coordinate| and T = sum_k |A_ak s_k|,
+// each component of the FP32 difference vector is within
+// E = u (4X + 8T + 4 cutoff + 4) of the exact one, and
+// |d2_f - d2| <= 2 E (3.47 |d| + 9 E) + 12 u d2 (a factor-2 margin included).
 template <bool kFill>
 __global__ void __launch_bounds__(128)
     nl_pairs(int nat, BinParams bp, const Pos4 *__restrict__ pos4,
-             const int *__restrict__ atom_cell, const int *__restrict__ atom_wrap,
-             const int *__restrict__ cell_start, const int *__restrict__ cell_atoms,
+             const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
+             const int *__restrict__ swrap, const int *__restrict__ cell_start,
              int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
              int *__restrict__ shift, int *__restrict__ status) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nat) return;
-  const int i = cell_atoms[t];
-  const Pos4 ri = pos4[i];
+  const float4 pi = spos[t];
+  const int i = __float_as_int(pi.w);
   int ci = atom_cell[i];
   int cell[3];
   cell[0] = ci % bp.n[0];
@@ -405,10 +459,23 @@ __global__ void __launch_bounds__(128)
   cell[1] = ci % bp.n[1];
   cell[2] = ci / bp.n[1];
   int q0, q1, q2;
-  unpack_shift(atom_wrap[i], q0, q1, q2);
+  unpack_shift(swrap[t], q0, q1, q2);
   const int shi[3] = {-q0, -q1, -q2};
+  const float u = 5.9604645e-8f;
+  const float X = __int_as_float(status[3]);
+  const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
+  float Af[3][3], Amax = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      Af[a][k] = (float)bp.A[a][k];
+      Amax = fmaxf(Amax, fabsf(Af[a][k]));
+    }
   int cur = kFill ? seed[i] : 0;
   int cnt = 0;
+  bool have_ri = false;
+  Pos4 ri;
   for (int x = -bp.dx; x <= bp.dx; x++) {
     for (int y = -bp.dy; y <= bp.dy; y++) {
       for (int z = -bp.dz; z <= bp.dz; z++) {
@@ -429,27 +496,37 @@ __global__ void __launch_bounds__(128)
         const int c = (cc[2] * bp.n[1] + cc[1]) * bp.n[0] + cc[0];
         const int js = cell_start[c], je = cell_start[c + 1];
         for (int jq = js; jq < je; jq++) {
-          const int j = cell_atoms[jq];
+          const float4 pj = spos[jq];
+          const int j = __float_as_int(pj.w);
           int w0, w1, w2;
-          unpack_shift(atom_wrap[j], w0, w1, w2);
+          unpack_shift(swrap[jq], w0, w1, w2);
           const int s2x = s1[0] + w0, s2y = s1[1] + w1, s2z = s1[2] + w2;
-          if (j == i && s2x == 0 && s2y == 0 && s2z == 0) continue;
-          const Pos4 rj = pos4[j];
-          const double sx = (double)s2x, sy = (double)s2y, sz = (double)s2z;
-          double d[3];
-          const double rij[3] = {__dsub_rn(ri.x, rj.x), __dsub_rn(ri.y, rj.y),
-                                 __dsub_rn(ri.z, rj.z)};
-#pragma unroll
-          for (int a = 0; a < 3; a++) {
-            double as = __dmul_rn(bp.A[a][0], sx);
-            as = __dadd_rn(as, __dmul_rn(bp.A[a][1], sy));
-            as = __dadd_rn(as, __dmul_rn(bp.A[a][2], sz));
-            d[a] = __dadd_rn(rij[a], as);
+          const bool zero_shift = (s2x | s2y | s2z) == 0;
+          if (j == i && zero_shift) continue;
+          float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+          float E = Ebase;
+          if (!zero_shift) {
+            const float fx = (float)s2x, fy = (float)s2y, fz = (float)s2z;
+            dx += Af[0][0] * fx + Af[0][1] * fy + Af[0][2] * fz;
+            dy += Af[1][0] * fx + Af[1][1] * fy + Af[1][2] * fz;
+            dz += Af[2][0] * fx + Af[2][1] * fy + Af[2][2] * fz;
+            E += 8.0f * u * Amax * (fabsf(fx) + fabsf(fy) + fabsf(fz));
           }
-          double d2 = __dmul_rn(d[0], d[0]);
-          d2 = __dadd_rn(d2, __dmul_rn(d[1], d[1]));
-          d2 = __dadd_rn(d2, __dmul_rn(d[2], d[2]));
-          if (d2 < bp.cutoff_sq) {
+          const float d2f = dx * dx + dy * dy + dz * dz;
+          const float B = 2.0f * E * (3.47f * sqrtf(d2f) + 9.0f * E) + 12.0f * u * d2f;
+          bool accept;
+          if (d2f + B < bp.cutoff_sq_lo) {
+            accept = true;
+          } else if (d2f - B > bp.cutoff_sq_hi) {
+            accept = false;
+          } else {
+            if (!have_ri) {
+              ri = pos4[i];
+              have_ri = true;
+            }
+            accept = exact_pair_test(bp, ri, pos4[j], s2x, s2y, s2z);
+          }
+          if (accept) {
             if (kFill) {
               nbr[cur] = j;
               shift[cur] = pack_shift(s2x, s2y, s2z);
@@ -589,6 +666,9 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   bp.dy = nl.dy;
   bp.dz = nl.dz;
   bp.cutoff_sq = cutoff * cutoff;
+  bp.cutoff_f = (float)(cutoff * (1.0 + 1e-6));
+  bp.cutoff_sq_lo = (float)(bp.cutoff_sq * (1.0 - 1e-6));
+  bp.cutoff_sq_hi = (float)(bp.cutoff_sq * (1.0 + 1e-6));
 
   GB_CHECK(nl.pos4.ensure(sizeof(Pos4) * std::max(nat, 1)));
   GB_CHECK(nl.atom_cell.ensure(sizeof(int) * std::max(nat, 1)));
@@ -597,6 +677,8 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   GB_CHECK(nl.cell_start.ensure(sizeof(int) * (ncells + 1)));
   GB_CHECK(nl.cell_atoms.ensure(sizeof(int) * 2 * std::max(nat, 1)));
   GB_CHECK(nl.counts.ensure(sizeof(int) * (nat + 1)));
+  GB_CHECK(nl.spos.ensure(sizeof(float4) * std::max(nat, 1)));
+  GB_CHECK(nl.swrap.ensure(sizeof(int) * std::max(nat, 1)));
   GB_CHECK(nl.seed.ensure(sizeof(int) * (nat + 1)));
   GB_CHECK(nl.stats.ensure(sizeof(int) * 8 + sizeof(int) * (size_t)(ncells + 1)));
   GB_CHECK(nl.hstats.ensure(sizeof(int) * 8));
@@ -630,10 +712,14 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
     nl_copy_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
         big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms + nat, cell_atoms);
     note_launch();
+    nl_gather_sorted<<<nb, T, 0, stream>>>(nat, cell_atoms, nl.pos4.as<Pos4>(),
+                                           nl.atom_wrap.as<int>(), nl.spos.as<float4>(),
+                                           nl.swrap.as<int>());
+    note_launch();
     nl_pairs<false><<<(nat + 127) / 128, 128, 0, stream>>>(
-        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
-        nl.cell_start.as<int>(), cell_atoms, nl.counts.as<int>(), nullptr, nullptr, nullptr,
-        status);
+        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
+        nl.swrap.as<int>(), nl.cell_start.as<int>(), nl.counts.as<int>(), nullptr, nullptr,
+        nullptr, status);
     note_launch();
   }
   GB_CHECK(exclusive_scan_i32(nl.counts.as<int>(), nl.seed.as<int>(), nat, nl.scan_tmp, stream));
@@ -661,9 +747,9 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
   if (nat > 0) {
     nl_pairs<true><<<(nat + 127) / 128, 128, 0, stream>>>(
-        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
-        nl.cell_start.as<int>(), cell_atoms, nullptr, nl.seed.as<int>(), nl.nbr.as<int>(),
-        nl.shift.as<int>(), status);
+        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
+        nl.swrap.as<int>(), nl.cell_start.as<int>(), nullptr, nl.seed.as<int>(),
+        nl.nbr.as<int>(), nl.shift.as<int>(), status);
     note_launch();
   }
   GB_CUDA(cudaGetLastError());

@@ -134,6 +134,8 @@ struct Neighbors {
   DevBuf cell_start;  // int[ncells+1]
   DevBuf cell_atoms;  // int[nat]: atoms sorted by (cell, id)
   DevBuf counts;      // int[nat+1]
+  DevBuf spos;        // float4[nat]: cell-sorted float positions, .w = atom id
+  DevBuf swrap;       // int[nat]: wrap counts in cell-sorted order
   DevBuf seed;        // int[nat+1] CSR offsets
   DevBuf nbr;         // int[capacity]
   DevBuf shift;       // int32 packed shifts [capacity]

@@ -231,3 +231,22 @@ def test_eam_mask(gpu, tmp_path):
     g0 = gpu_eam(fn, s)
     assert abs(g0["epot"] - got["epot"] - g2["epot"]) < 1e-6
     assert np.max(np.abs(g0["f"] - got["f"] - g2["f"])) < 1e-6
+
+
+@pytest.mark.parametrize("natoms", [65536, 1048576])
+def test_mixed_precision_amorphous_workload(gpu, natoms):
+    # The bench workload (2.33 g/cm^3, sigma = 0.25 A, close contacts down to
+    # ~0.5 A with forces of several hundred eV/A): the mixed form must stay
+    # within 1e-5 eV/A of the FP64 oracle; the FP64 drop-in within 1e-9.
+    s = S.tersoff_si_amorphous(natoms, seed=3)
+    ref = oracle.bop_compute("tersoff", TERSOFF, s)
+    g64 = gpu_bop("tersoff", s, per_at=False)
+    gmx = gpu_bop("tersoff", s, precision="mixed", per_at=False)
+    assert np.max(np.abs(g64["f"] - ref["f"])) < 1e-9
+    assert abs(g64["epot"] - ref["epot"]) / natoms < 1e-10
+    dfm = np.max(np.abs(gmx["f"] - ref["f"]))
+    assert dfm <= MIXED_F_TOL, dfm
+    assert abs(gmx["epot"] - ref["epot"]) / natoms < 1e-6
+    # size-independent properties: no net force (translation invariance)
+    assert np.max(np.abs(gmx["f"].sum(axis=0))) < 1e-6 * natoms ** 0.5
+    assert np.max(np.abs(g64["f"].sum(axis=0))) < 1e-9 * natoms ** 0.5
