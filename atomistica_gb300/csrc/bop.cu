@@ -26,9 +26,10 @@
 // per-atom virial (requested) follows the reference exactly: w_ij = r_ij (x)
 // df - P_ij wijb_ij, half to i and half to j (:1510-1518).
 //
-// Precision forms: R = double (drop-in) or R = float (mixed: three-body terms
-// and the bond order in FP32; bond geometry, pair terms VA/VR, cutoff and all
-// accumulation of E, F, W in FP64).
+// Precision forms: bop_tile (FP64 drop-in, this file) and bop_tile_mx (mixed:
+// FP32 three-body terms, float-float geometry, pair terms, bond order and
+// accumulation on the FP32 pipe, FP64 recomputation of the bonds whose
+// estimated error is large; bop_mixed.cuh).
 
 #include <cuda_runtime.h>
 
@@ -37,6 +38,8 @@
 #include <type_traits>
 
 #include "bop_math.h"
+#include "ff.h"
+#include "ff_tables.h"
 #include "potential.h"
 
 namespace gb {
@@ -73,7 +76,6 @@ struct BopArgs {
 struct SmemLayout {
   int *aseed, *toff, *el, *meta, *hot;
   double *rn64, *r64, *rinv64, *fc64, *dfc64, *P, *G, *E;  // per bond
-  float *rnf, *rlf, *rinvf, *fcf, *dfcf;                   // per bond (mixed form)
   double *t;                                               // 3 per (ij, ik) slot
   int nbt, ntrip;
 };
@@ -84,7 +86,6 @@ template <class R>
 __host__ __device__ inline size_t bop_smem_bytes(int nbt, int ntrip) {
   size_t o = align16(sizeof(int) * (3 * kMaxApt + 2 + 2 * (size_t)nbt));
   o += align16(sizeof(double) * (size_t)nbt * 12);
-  o += align16(sizeof(float) * (size_t)nbt * 7);
   o += align16(sizeof(double) * (size_t)ntrip * 3);
   return o + 64;
 }
@@ -110,13 +111,6 @@ __device__ inline SmemLayout carve(unsigned char *sm, int nbt, int ntrip) {
   L.G = dp + 8 * nbt;
   L.E = dp + 11 * nbt;
   o += align16(sizeof(double) * (size_t)nbt * 12);
-  float *fp = reinterpret_cast<float *>(sm + o);
-  L.rnf = fp;
-  L.rlf = fp + 3 * nbt;
-  L.rinvf = fp + 4 * nbt;
-  L.fcf = fp + 5 * nbt;
-  L.dfcf = fp + 6 * nbt;
-  o += align16(sizeof(float) * (size_t)nbt * 7);
   L.t = reinterpret_cast<double *>(sm + o);
   return L;
 }
@@ -189,57 +183,6 @@ __device__ __forceinline__ void kloop64(const Pot &pot, const SmemLayout &L, int
   }
 }
 
-// The same k loop with FP32 three-body arithmetic (mixed form).  h - cos
-// theta is formed from the FP64 unit vectors: g' ~ 1e5 amplifies any error of
-// cos theta.  Also returns sum |d zeta/d r_k| for the error estimate.
-template <class Pot, bool kWat>
-__device__ __forceinline__ void kloop32(const Pot &pot, const SmemLayout &L, int lb, int s, int z,
-                                        int eli, double *trow, float &zeta, float dbj[3],
-                                        float wk[9], float &sumdk) {
-  const int nbt = L.nbt, ntrip = L.ntrip;
-  const float rnij[3] = {L.rnf[lb], L.rnf[nbt + lb], L.rnf[2 * nbt + lb]};
-  const float rlij = L.rlf[lb], rinvj = L.rinvf[lb];
-  const double rn64j[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
-  const double hpar = pot.hpar(eli);
-  for (int q = 0; q < z; q++) {
-    const int lk = s + q;
-    if (lk == lb) continue;
-    const int mk = L.meta[lk];
-    if (!(mk & kFlagK)) {
-      trow[q] = 0.0;
-      trow[ntrip + q] = 0.0;
-      trow[2 * ntrip + q] = 0.0;
-      continue;
-    }
-    const int ikpot = (mk >> 8) & 0xf;
-    const float rnik[3] = {L.rnf[lk], L.rnf[nbt + lk], L.rnf[2 * nbt + lk]};
-    const float rlik = L.rlf[lk], rinvk = L.rinvf[lk], fcik = L.fcf[lk], dfcik = L.dfcf[lk];
-    float hv, dh;
-    pot.template h<float>(ikpot, rlij - rlik, hv, dh);
-    const double cs64 = L.rn64[lk] * rn64j[0] + L.rn64[nbt + lk] * rn64j[1] +
-                        L.rn64[2 * nbt + lk] * rn64j[2];
-    const float cs = (float)cs64;
-    float gv, dg;
-    pot.template g_hc<float>(eli, ikpot, (float)(hpar - cs64), gv, dg);
-    const float dzfac = fcik * dg * hv;
-    zeta += fcik * gv * hv;
-    const float dzdrij = gv * fcik * dh;
-    const float dzdrik = gv * (dfcik * hv - fcik * dh);
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float dcj = (rnik[c] - cs * rnij[c]) * rinvj;
-      const float dck = (rnij[c] - cs * rnik[c]) * rinvk;
-      dbj[c] += dzdrij * rnij[c] + dzfac * dcj;
-      const float dk = dzdrik * rnik[c] + dzfac * dck;
-      trow[c * ntrip + q] = (double)dk;
-      sumdk += fabsf(dk);
-      if (kWat)
-#pragma unroll
-        for (int c1 = 0; c1 < 3; c1++) wk[3 * c1 + c] += rnik[c1] * rlik * dk;
-    }
-  }
-}
-
 // Energy, radial force, G partial and per-bond outputs of bond ij
 // (bop_kernel.f90:1356-1518).  The energy goes to L.E (summed later in a
 // fixed order).
@@ -290,13 +233,8 @@ __global__ void __launch_bounds__(kBopThreads)
     bop_tile(const BopArgs a, const Pot pot, int max_nbt, int max_ntrip, int *status) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ double red_scratch[(kBopThreads / 32) * 9];
-  __shared__ double s_exp2[256];
-  __shared__ int s_nhot;
-  constexpr bool kMix = std::is_same<R, float>::value;
+  static_assert(std::is_same<R, double>::value, "bop_tile is the FP64 form");
   const int tid = threadIdx.x;
-  if (kMix)
-    for (int q = tid; q < 256; q += kBopThreads) s_exp2[q] = kExp2Tab[q];
-  if (tid == 0) s_nhot = 0;
   const int a0 = blockIdx.x * a.apt;
   const int a1 = min(a0 + a.apt, a.nat);
   const int na = a1 - a0;
@@ -377,24 +315,12 @@ __global__ void __launch_bounds__(kBopThreads)
         in_short = true;
       }
       if (in_short) {
-        if (kMix) {
-          // r and 1/r from an FP32 rsqrt seed and one FP64 Newton step (~48
-          // bits); FP64 trig cutoff (its derivative is multiplied by g ~ 1e4).
-          double y = (double)rsqrtf((float)r2);
-          y = y * fma(-0.5 * r2, y * y, 1.5);
-          r = r2 * y;
+        if (!(r2 < pot.r1sq(t)))
+          trig_off(__dsqrt_rn(r2), pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
+        r = __dsqrt_rn(r2);
 #pragma unroll
-          for (int c = 0; c < 3; c++) rn[c] = rij[c] * y;
-          rinv = y;
-          if (!(r2 < pot.r1sq(t))) trig_off(r, pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
-        } else {
-          if (!(r2 < pot.r1sq(t)))
-            trig_off(__dsqrt_rn(r2), pot.r1(t), pot.r2(t), pot.fac(t), fc, dfc);
-          r = __dsqrt_rn(r2);
-#pragma unroll
-          for (int c = 0; c < 3; c++) rn[c] = rij[c] / r;
-          rinv = 1.0 / r;
-        }
+        for (int c = 0; c < 3; c++) rn[c] = rij[c] / r;
+        rinv = 1.0 / r;
         int mf = 2;
         if (a.mask) {
           const int mi = a.mask[i], mj = a.mask[j];
@@ -417,14 +343,6 @@ __global__ void __launch_bounds__(kBopThreads)
     L.rinv64[lb] = rinv;
     L.fc64[lb] = fc;
     L.dfc64[lb] = dfc;
-    if (kMix) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) L.rnf[c * nbt + lb] = (float)rn[c];
-      L.rlf[lb] = (float)r;
-      L.rinvf[lb] = (float)rinv;
-      L.fcf[lb] = (float)fc;
-      L.dfcf[lb] = (float)dfc;
-    }
   }
   __syncthreads();
 
@@ -458,88 +376,21 @@ __global__ void __launch_bounds__(kBopThreads)
     const double hm = 0.5 * mf;
     const double fcij = L.fc64[lb];
     double VA, dVA, VR, dVR;
-    if (kMix) {
-      VA = -pot.Bc(t) * exp_acc(-pot.cA(t) * r, s_exp2);
-      dVA = -pot.cA(t) * VA;
-      VR = pot.Ac(t) * exp_acc(-pot.cR(t) * r, s_exp2);
-      dVR = -pot.cR(t) * VR;
-    } else {
-      // VA, VR (tersoff_func.f90:32-78) scaled by maskfac/2 (:1133-1139)
-      pot.VA(t, r, VA, dVA);
-      pot.VR(t, r, VR, dVR);
-    }
+    // VA, VR (tersoff_func.f90:32-78) scaled by maskfac/2 (:1133-1139)
+    pot.VA(t, r, VA, dVA);
+    pot.VR(t, r, VR, dVR);
     VA *= hm;
     dVA *= hm;
     VR *= hm;
     dVR *= hm;
-    if (!kMix) {
-      double zeta = 0.0, dbj[3] = {0.0, 0.0, 0.0}, wk[9];
-      if (kWat)
+    double zeta = 0.0, dbj[3] = {0.0, 0.0, 0.0}, wk[9];
+    if (kWat)
 #pragma unroll
-        for (int c = 0; c < 9; c++) wk[c] = 0.0;
-      kloop64<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk);
-      double bij, P;
-      pot.template bo<double>(eli, t, zeta, fcij, VA, bij, P);
-      finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
-    } else {
-      float zeta = 0.0f, dbj[3] = {0.0f, 0.0f, 0.0f}, wk[9], sumdk = 0.0f;
-      if (kWat)
-#pragma unroll
-        for (int c = 0; c < 9; c++) wk[c] = 0.0f;
-      kloop32<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
-      double bij, P;
-      pot.bo_mixed(eli, t, zeta, fcij, VA, s_exp2, bij, P);
-      // Estimated FP32 error of this bond's force contributions: zeta (and
-      // hence b) to ~2.4e-7 relative, the three-body derivatives to ~3e-7.
-      const float sens = pot.bsens(eli, zeta);
-      const float est = 2.4e-7f * fabsf((float)dVA) * (float)fcij * sens +
-                        3.0e-7f * fabsf((float)P) *
-                            (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
-      if (est > kHotThreshold) {
-        L.hot[atomicAdd(&s_nhot, 1)] = lb;
-      } else {
-        const double dbjd[3] = {dbj[0], dbj[1], dbj[2]};
-        double wkd[9];
-        if (kWat)
-#pragma unroll
-          for (int c = 0; c < 9; c++) wkd[c] = wk[c];
-        finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbjd, wkd, VA, dVA, VR, dVR);
-      }
-    }
-  }
-  if (kMix) {
-    __syncthreads();
-    // ---- Phase 2b (mixed form): FP64 recomputation of the hot bonds. ----
-    const int nhot = s_nhot;
-    for (int h = tid; h < nhot; h += kBopThreads) {
-      const int lb = L.hot[h];
-      const int b = b0 + lb;
-      const int meta = L.meta[lb];
-      const int ai = meta & 0xff;
-      const int t = (meta >> 8) & 0xf;
-      const int mf = (meta >> 16) & 3;
-      const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-      double *trow = L.t + L.toff[ai] + p * z;
-      const int eli = L.el[ai];
-      const double r = L.r64[lb];
-      const double hm = 0.5 * mf;
-      double VA = -pot.Bc(t) * exp_acc(-pot.cA(t) * r, s_exp2);
-      double dVA = -pot.cA(t) * VA;
-      double VR = pot.Ac(t) * exp_acc(-pot.cR(t) * r, s_exp2);
-      double dVR = -pot.cR(t) * VR;
-      VA *= hm;
-      dVA *= hm;
-      VR *= hm;
-      dVR *= hm;
-      double zeta = 0.0, dbj[3] = {0.0, 0.0, 0.0}, wk[9];
-      if (kWat)
-#pragma unroll
-        for (int c = 0; c < 9; c++) wk[c] = 0.0;
-      kloop64<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk);
-      double bij, P;
-      pot.template bo<double>(eli, t, zeta, L.fc64[lb], VA, bij, P);
-      finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
-    }
+      for (int c = 0; c < 9; c++) wk[c] = 0.0;
+    kloop64<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk);
+    double bij, P;
+    pot.template bo<double>(eli, t, zeta, fcij, VA, bij, P);
+    finalize_bond<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
   }
   __syncthreads();
 
@@ -581,6 +432,14 @@ __global__ void __launch_bounds__(kBopThreads)
   block_sum<1>(eacc, part, red_scratch);
   block_sum<9>(wacc, part + 1, red_scratch);
 }
+
+}  // namespace
+}  // namespace gb
+
+#include "bop_mixed.cuh"
+
+namespace gb {
+namespace {
 
 // Per-atom gather through the reverse-entry index.
 template <bool kEpa, bool kWat>
@@ -647,31 +506,71 @@ __global__ void reduce_partials_kernel(const double *__restrict__ part, int ntil
 }
 
 template <class Pot, class R, bool kWat, bool kPB>
-int launch_tile(const BopArgs &args, const Pot &pot, int ntiles, int max_nbt, int max_ntrip,
-                int *status, cudaStream_t s) {
-  const size_t smem = bop_smem_bytes<R>(max_nbt, max_ntrip);
-  auto kern = bop_tile<Pot, R, kWat, kPB>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) {
-      set_error(std::string("bop: shared memory request too large: ") + cudaGetErrorString(e));
-      return GB_ERROR_CAPACITY;
+int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int ntiles, int max_nbt,
+                int max_ntrip, int *status, cudaStream_t s) {
+  constexpr bool kMix = std::is_same<R, float>::value;
+  const size_t smem =
+      kMix ? bop_smem_bytes_mx(max_nbt, max_ntrip) : bop_smem_bytes<R>(max_nbt, max_ntrip);
+  cudaError_t e = cudaSuccess;
+  if (kMix) {
+    auto kern = bop_tile_mx<Pot, kWat, kPB>;
+    if (smem > 48 * 1024)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+      const MxParams mp = make_mx(pot.p, args.A);
+      kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
+      note_launch();
+    }
+  } else {
+    auto kern = bop_tile<Pot, double, kWat, kPB>;
+    if (smem > 48 * 1024)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+      kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, max_nbt, max_ntrip, status);
+      note_launch();
     }
   }
-  kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, max_nbt, max_ntrip, status);
-  note_launch();
+  if (e != cudaSuccess) {
+    set_error(std::string("bop: shared memory request too large: ") + cudaGetErrorString(e));
+    return GB_ERROR_CAPACITY;
+  }
   GB_CUDA(cudaGetLastError());
   return 0;
 }
 
+// R = double: FP64 drop-in; R = float: mixed form (posff: ff positions).
 template <class Pot, class R>
-int dispatch_tile(const BopArgs &args, const Pot &pot, int ntiles, int max_nbt, int max_ntrip,
-                  int *status, bool wat, bool pb, cudaStream_t s) {
-  if (wat && pb) return launch_tile<Pot, R, true, true>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
-  if (wat) return launch_tile<Pot, R, true, false>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
-  if (pb) return launch_tile<Pot, R, false, true>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
-  return launch_tile<Pot, R, false, false>(args, pot, ntiles, max_nbt, max_ntrip, status, s);
+int dispatch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int ntiles,
+                  int max_nbt, int max_ntrip, int *status, bool wat, bool pb, cudaStream_t s) {
+  if (wat && pb)
+    return launch_tile<Pot, R, true, true>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+  if (wat)
+    return launch_tile<Pot, R, true, false>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+  if (pb)
+    return launch_tile<Pot, R, false, true>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+  return launch_tile<Pot, R, false, false>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+}
+
+// Per-atom gather of the bond forces (FP64 G, or ff G for the mixed form).
+int launch_gather(bool mixed, int nat, const int *seed, const int *rev, const double *G,
+                  const double *ebond, const double *wbond, double *f, double *epa, double *wpa,
+                  cudaStream_t s) {
+  const int T = 128, nb = (nat + T - 1) / T;
+  const float2 *Gf = reinterpret_cast<const float2 *>(G);
+  if (mixed) {
+    if (epa && wpa) bop_gather_mx<true, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
+    else if (epa) bop_gather_mx<true, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
+    else if (wpa) bop_gather_mx<false, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
+    else bop_gather_mx<false, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
+  } else {
+    if (epa && wpa) bop_gather<true, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
+    else if (epa) bop_gather<true, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
+    else if (wpa) bop_gather<false, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
+    else bop_gather<false, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
+  }
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
 }
 
 }  // namespace
@@ -695,7 +594,6 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   }
   GB_CHECK(neighbors_build_reverse(nl, p, s));
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
-  const size_t rsz = mixed ? sizeof(float) : sizeof(double);
   // Atoms per tile: largest power of two <= kMaxApt whose worst tile fits.
   const int maxz = std::max(nl.maxz, 1);
   int apt = kMaxApt;
@@ -730,7 +628,6 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
   const int max_nbt = hplan[0], max_ntrip = hplan[1];
-  (void)rsz;
 
   BopArgs args;
   args.nat = nat;
@@ -749,48 +646,31 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   args.tile_part = pot.tile_part.as<double>();
   int *status = o.status;
   int rc;
+  const float4 *posff = nullptr;
+  if (mixed) {
+    GB_CHECK(pot.posff.ensure(sizeof(float4) * 2 * (size_t)nat));
+    bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, args.pos, pot.posff.as<float4>());
+    note_launch();
+    posff = pot.posff.as<float4>();
+  }
   GB_CUDA(cudaEventRecord(pot.kev[0], s));
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};
-    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, ntiles, max_nbt, max_ntrip, status,
-                                                  want_wat, want_pb, s)
-               : dispatch_tile<TersoffPot, double>(args, tp, ntiles, max_nbt, max_ntrip,
+    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, max_nbt, max_ntrip,
+                                                  status, want_wat, want_pb, s)
+               : dispatch_tile<TersoffPot, double>(args, tp, posff, ntiles, max_nbt, max_ntrip,
                                                    status, want_wat, want_pb, s);
   } else {
     KumagaiPot kp{make_kumagai_dev(pot.kp)};
-    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, ntiles, max_nbt, max_ntrip, status,
-                                                  want_wat, want_pb, s)
-               : dispatch_tile<KumagaiPot, double>(args, kp, ntiles, max_nbt, max_ntrip,
+    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, posff, ntiles, max_nbt, max_ntrip,
+                                                  status, want_wat, want_pb, s)
+               : dispatch_tile<KumagaiPot, double>(args, kp, posff, ntiles, max_nbt, max_ntrip,
                                                    status, want_wat, want_pb, s);
   }
   GB_CHECK(rc);
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
-  const int T = 128;
-  const bool epa = o.epot_per_at != nullptr;
-  const int gb = (nat + T - 1) / T;
-  if (epa && want_wat) {
-    bop_gather<true, true><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
-                                            args.ebond, args.wbond, o.f, o.epot_per_at,
-                                            o.wpot_per_at);
-    note_launch();
-  }
-  else if (epa) {
-    bop_gather<true, false><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
-                                             args.ebond, nullptr, o.f, o.epot_per_at, nullptr);
-    note_launch();
-  }
-  else if (want_wat) {
-    bop_gather<false, true><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
-                                             args.ebond, args.wbond, o.f, nullptr,
-                                             o.wpot_per_at);
-    note_launch();
-  }
-  else {
-    bop_gather<false, false><<<gb, T, 0, s>>>(nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
-                                              args.ebond, nullptr, o.f, nullptr, nullptr);
-    note_launch();
-  }
-  GB_CUDA(cudaGetLastError());
+  GB_CHECK(launch_gather(mixed, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
+                         args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
   GB_CHECK(reduce_partials(args.tile_part, ntiles, 10, o.red, s));
   pot.tile_atoms = apt;
   return 0;
@@ -809,7 +689,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 // neighbour list the caller supplies, using only the file-scope scratch array
 // below for every intermediate buffer.  The array is sized for at most
 // kNoallocMaxAtoms atoms and kNoallocMaxEntries list entries; every GPU that
-// loads this library holds it (about 12.5 MB) until the process exits.
+// loads this library holds it (about 13 MB) until the process exits.
 // ===========================================================================
 
 namespace gb {
@@ -830,7 +710,8 @@ constexpr size_t kNaRev = na_align(kNaShift + 4 * (size_t)kNoallocMaxEntries);
 constexpr size_t kNaG = na_align(kNaRev + 4 * (size_t)kNoallocMaxEntries);   // 3 doubles/entry
 constexpr size_t kNaE = na_align(kNaG + 24 * (size_t)kNoallocMaxEntries);    // 1 double/entry
 constexpr size_t kNaPart = na_align(kNaE + 8 * (size_t)kNoallocMaxEntries);  // 10 doubles/tile
-constexpr size_t kNoallocBytes = na_align(kNaPart + 80 * (size_t)kNoallocMaxAtoms);
+constexpr size_t kNaPosff = na_align(kNaPart + 80 * (size_t)kNoallocMaxAtoms);  // 2 float4/atom
+constexpr size_t kNoallocBytes = na_align(kNaPosff + 32 * (size_t)kNoallocMaxAtoms);
 
 }  // namespace
 }  // namespace gb
@@ -1051,24 +932,27 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   args.frbond = nullptr;
   args.tile_part = part;
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  float4 *posff = reinterpret_cast<float4 *>(base + kNaPosff);
+  if (mixed) {
+    bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, pos, posff);
+    note_launch();
+  }
   int rc;
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};
-    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, ntiles, hp[0], hp[1], status + 2,
-                                                  false, false, s)
-               : dispatch_tile<TersoffPot, double>(args, tp, ntiles, hp[0], hp[1], status + 2,
-                                                   false, false, s);
+    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, hp[0], hp[1],
+                                                  status + 2, false, false, s)
+               : dispatch_tile<TersoffPot, double>(args, tp, posff, ntiles, hp[0], hp[1],
+                                                   status + 2, false, false, s);
   } else {
     KumagaiPot kp{make_kumagai_dev(pot.kp)};
-    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, ntiles, hp[0], hp[1], status + 2,
-                                                  false, false, s)
-               : dispatch_tile<KumagaiPot, double>(args, kp, ntiles, hp[0], hp[1], status + 2,
-                                                   false, false, s);
+    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, posff, ntiles, hp[0], hp[1],
+                                                  status + 2, false, false, s)
+               : dispatch_tile<KumagaiPot, double>(args, kp, posff, ntiles, hp[0], hp[1],
+                                                   status + 2, false, false, s);
   }
   GB_CHECK(rc);
-  bop_gather<false, false><<<(nat + 127) / 128, 128, 0, s>>>(nat, seed32, rev, G, ebond, nullptr,
-                                                              f, nullptr, nullptr);
-  note_launch();
+  GB_CHECK(launch_gather(mixed, nat, seed32, rev, G, ebond, nullptr, f, nullptr, nullptr, s));
   GB_CHECK(reduce_partials(part, ntiles, 10, red, s));
   noalloc_finish<<<1, 32, 0, s>>>(red, epot, wpot);
   note_launch();

@@ -77,6 +77,7 @@ struct Potential {
   // Scratch.
   DevBuf bond_G, bond_e, bond_w, bond_fr, tile_part, red;
   DevBuf atom_dF;
+  DevBuf posff;  // ff positions (mixed form)
   DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
   HostBuf hred;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
