@@ -488,20 +488,33 @@ __global__ void bop_plan(int nat, int apt, const int *__restrict__ seed, int *__
   atomicMax(&out[1], ntrip);
 }
 
-__global__ void reduce_partials_kernel(const double *__restrict__ part, int ntiles, int nc,
-                                       double *__restrict__ red) {
-  __shared__ double sh[1024];
-  for (int c = 0; c < nc; c++) {
-    double s = 0.0;
-    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) s += part[(size_t)t * nc + c];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) red[c] = sh[0];
-    __syncthreads();
+// Deterministic sum of rows of kRedCols doubles: block q sums rows
+// [q*rpb, min((q+1)*rpb, nrows)) into out[q*kRedCols ..] (coalesced row
+// reads, fixed shuffle tree, then the warps in order).
+constexpr int kRedCols = 10;
+__global__ void reduce_rows_kernel(const double *__restrict__ part, int nrows, int rpb,
+                                   double *__restrict__ out) {
+  __shared__ double sh[32 * kRedCols];
+  const int r0 = blockIdx.x * rpb, r1 = min(r0 + rpb, nrows);
+  double acc[kRedCols];
+#pragma unroll
+  for (int c = 0; c < kRedCols; c++) acc[c] = 0.0;
+  for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < kRedCols; c++) acc[c] += part[(size_t)t * kRedCols + c];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int c = 0; c < kRedCols; c++) {
+    double x = acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[wid * kRedCols + c] = x;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < kRedCols) {
+    double x = 0.0;
+    for (int w = 0; w < nw; w++) x += sh[w * kRedCols + threadIdx.x];
+    out[(size_t)blockIdx.x * kRedCols + threadIdx.x] = x;
   }
 }
 
@@ -575,9 +588,26 @@ int launch_gather(bool mixed, int nat, const int *seed, const int *rev, const do
 
 }  // namespace
 
-int reduce_partials(const double *part, int ntiles, int nc, double *red, cudaStream_t s) {
-  reduce_partials_kernel<<<1, 1024, 0, s>>>(part, ntiles, nc, red);
-  note_launch();
+size_t reduce_stage_bytes(int nrows) {
+  return sizeof(double) * kRedCols * (size_t)((nrows + kRedRowsPerBlock - 1) / kRedRowsPerBlock);
+}
+
+int reduce_partials(const double *part, int nrows, int nc, double *red, double *stage,
+                    cudaStream_t s) {
+  if (nc != kRedCols) {
+    set_error("reduce_partials: unsupported column count");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (stage == nullptr || nrows <= 2 * kRedRowsPerBlock) {
+    reduce_rows_kernel<<<1, 1024, 0, s>>>(part, nrows, std::max(nrows, 1), red);
+    note_launch();
+  } else {
+    const int nb = (nrows + kRedRowsPerBlock - 1) / kRedRowsPerBlock;
+    reduce_rows_kernel<<<nb, 256, 0, s>>>(part, nrows, kRedRowsPerBlock, stage);
+    note_launch();
+    reduce_rows_kernel<<<1, 1024, 0, s>>>(stage, nb, nb, red);
+    note_launch();
+  }
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -671,7 +701,8 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
                          args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
-  GB_CHECK(reduce_partials(args.tile_part, ntiles, 10, o.red, s));
+  GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(ntiles) + 64));
+  GB_CHECK(reduce_partials(args.tile_part, ntiles, 10, o.red, pot.red_stage.as<double>(), s));
   pot.tile_atoms = apt;
   return 0;
 }
@@ -953,7 +984,7 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   }
   GB_CHECK(rc);
   GB_CHECK(launch_gather(mixed, nat, seed32, rev, G, ebond, nullptr, f, nullptr, nullptr, s));
-  GB_CHECK(reduce_partials(part, ntiles, 10, red, s));
+  GB_CHECK(reduce_partials(part, ntiles, 10, red, nullptr, s));
   noalloc_finish<<<1, 32, 0, s>>>(red, epot, wpot);
   note_launch();
   GB_CUDA(cudaGetLastError());

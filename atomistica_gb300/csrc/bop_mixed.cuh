@@ -21,9 +21,20 @@ namespace {
 
 struct MxPair {
   ff cA, cR, Ac, Bc, xi, r1, fac;
+  float r1sq, r2sq, r2;  // cutoff tests in FP32
+  // h(dr) = exp(hae (hs dr)^hm), dh/d dr = had hm hs (hs dr)^(hm-1) h;
+  // hm = 0: h = 1.  Tersoff: hae = had = 1, hs = 2 mubo, hm = m; Kumagai:
+  // hae = alpha (1 for beta = 3, kumagai_func.f90:211-213), had = alpha,
+  // hs = 1, hm = beta.
+  ff hae, had, hs;
+  int hm;
+  ff om;  // Tersoff omega of the (i,k) pair
 };
 struct MxElem {
   ff n, lbetan, e, h, eta, delta;
+  ff c2, d2, c2d2;                 // Tersoff g
+  ff c1, kc2, c3, c4, c5;          // Kumagai g
+  float sens;                      // |d ln b / d ln x| prefactor (|e n|, |delta eta|)
 };
 struct MxParams {
   int kind;  // 0 Tersoff, 1 Kumagai
@@ -34,24 +45,42 @@ struct MxParams {
 
 inline ff ffh(double d) { return ff_from_double(d); }
 
+inline void mx_cutoffs(MxPair &q, double r1, double r2, double fac) {
+  q.r1 = ffh(r1);
+  q.fac = ffh(fac);
+  q.r1sq = (float)(r1 * r1);
+  q.r2sq = (float)(r2 * r2);
+  q.r2 = (float)r2;
+}
+
 inline MxParams make_mx(const TersoffDev &d, const double A[3][3]) {
   MxParams m{};
   m.kind = 0;
   const int np = d.nel * (d.nel + 1) / 2;
   for (int q = 0; q < np; q++) {
-    m.pr[q].cA = ffh(d.mu[q]);
-    m.pr[q].cR = ffh(d.lambda[q]);
-    m.pr[q].Ac = ffh(d.A[q]);
-    m.pr[q].Bc = ffh(d.B[q]);
-    m.pr[q].xi = ffh(d.xi[q]);
-    m.pr[q].r1 = ffh(d.r1[q]);
-    m.pr[q].fac = ffh(d.fac[q]);
+    MxPair &pq = m.pr[q];
+    pq.cA = ffh(d.mu[q]);
+    pq.cR = ffh(d.lambda[q]);
+    pq.Ac = ffh(d.A[q]);
+    pq.Bc = ffh(d.B[q]);
+    pq.xi = ffh(d.xi[q]);
+    mx_cutoffs(pq, d.r1[q], d.r2[q], d.fac[q]);
+    pq.hae = ffh(1.0);
+    pq.had = ffh(1.0);
+    pq.hs = ffh(2.0 * d.mubo[q]);
+    pq.hm = d.mubo[q] == 0.0 ? 0 : d.m[q];
+    pq.om = ffh(d.omega[q]);
   }
   for (int q = 0; q < d.nel; q++) {
-    m.el[q].n = ffh(d.n[q]);
-    m.el[q].lbetan = ffh(d.lbetan[q]);
-    m.el[q].e = ffh(d.e[q]);
-    m.el[q].h = ffh(d.h[q]);
+    MxElem &e = m.el[q];
+    e.n = ffh(d.n[q]);
+    e.lbetan = ffh(d.lbetan[q]);
+    e.e = ffh(d.e[q]);
+    e.h = ffh(d.h[q]);
+    e.c2 = ffh(d.c2[q]);
+    e.d2 = ffh(d.d2[q]);
+    e.c2d2 = ffh(d.c2d2inv[q]);
+    e.sens = (float)std::fabs(d.e[q] * d.n[q]);
   }
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) m.A[a][k] = ffh(A[a][k]);
@@ -61,16 +90,30 @@ inline MxParams make_mx(const TersoffDev &d, const double A[3][3]) {
 inline MxParams make_mx(const KumagaiDev &d, const double A[3][3]) {
   MxParams m{};
   m.kind = 1;
-  m.pr[0].cA = ffh(d.lambda2[0]);
-  m.pr[0].cR = ffh(d.lambda1[0]);
-  m.pr[0].Ac = ffh(d.A[0]);
-  m.pr[0].Bc = ffh(d.B[0]);
-  m.pr[0].xi = ffh(1.0);
-  m.pr[0].r1 = ffh(d.r1[0]);
-  m.pr[0].fac = ffh(d.fac[0]);
-  m.el[0].eta = ffh(d.eta[0]);
-  m.el[0].delta = ffh(d.delta[0]);
-  m.el[0].h = ffh(d.h[0]);
+  MxPair &p0 = m.pr[0];
+  p0.cA = ffh(d.lambda2[0]);
+  p0.cR = ffh(d.lambda1[0]);
+  p0.Ac = ffh(d.A[0]);
+  p0.Bc = ffh(d.B[0]);
+  p0.xi = ffh(1.0);
+  mx_cutoffs(p0, d.r1[0], d.r2[0], d.fac[0]);
+  p0.hae = ffh(d.beta[0] == 3 ? 1.0 : d.alpha[0]);
+  p0.had = ffh(d.alpha[0]);
+  p0.hs = ffh(1.0);
+  p0.hm = d.alpha[0] == 0.0 ? 0 : d.beta[0];
+  p0.om = ffh(1.0);
+  MxElem &e = m.el[0];
+  e.n = ffh(d.eta[0]);
+  e.lbetan = ffh(0.0);
+  e.eta = ffh(d.eta[0]);
+  e.delta = ffh(d.delta[0]);
+  e.h = ffh(d.h[0]);
+  e.c1 = ffh(d.c1[0]);
+  e.kc2 = ffh(d.c2[0]);
+  e.c3 = ffh(d.c3[0]);
+  e.c4 = ffh(d.c4[0]);
+  e.c5 = ffh(d.c5[0]);
+  e.sens = (float)std::fabs(d.delta[0] * d.eta[0]);
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) m.A[a][k] = ffh(A[a][k]);
   return m;
@@ -124,41 +167,137 @@ __device__ inline MxLayout carve_mx(unsigned char *sm, int nbt, int ntrip) {
   return L;
 }
 
-// Bond order in ff from an FP32 zeta (Tersoff: b = xi (1 + beta^n z^n)^e,
-// P = -1/4 fc VA xi beta^n z^(n-1) (1+x)^(e-1); Kumagai: b = (1 + z^eta)^-delta,
-// P = 1/2 fc VA eta z^(eta-1) (-delta) (1+x)^(-delta-1)).
-__device__ __forceinline__ void bo_ff(const MxParams &mp, int eli, int t, float zeta, ff fc,
-                                      ff VA, const ff *etab, ff &b, ff &P) {
-  if (!(zeta > 0.0f)) {
+// ln z for an ff z > 0: one Newton step on logf(z.hi).
+__device__ __forceinline__ ff ff_log(ff z, const ff *etab) {
+  const float l0 = logf(z.hi);
+  const ff e = ff_exp(ff_make(-l0, 0.0f), etab);  // e^-l0
+  const ff w = ff_addf(ff_mul(e, z), -1.0f);      // z e^-l0 - 1
+  return ff_addf(w, l0);
+}
+
+// ---- Three-body functions on the MxParams copies of the parameters. ----
+// g as a function of hc = h - cos theta, and d g / d cos theta
+// (tersoff_func.f90:86-114 in the stable form g = omega (1 + c^2 hc^2 /
+// (d^2 (d^2 + hc^2))); kumagai_func.f90:86-131).
+__device__ __forceinline__ void g_f(const MxParams &mp, int eli, int ikpot, float hc, float &val,
+                                    float &dval) {
+  const MxElem &E = mp.el[eli];
+  const float hc2 = hc * hc;
+  if (mp.kind == 0) {
+    const float om = mp.pr[ikpot].om.hi;
+    const float inv = 1.0f / (E.d2.hi + hc2);
+    val = om * (1.0f + E.c2d2.hi * hc2 * inv);
+    dval = -2.0f * om * E.c2.hi * hc * inv * inv;
+  } else {
+    const float tmp = hc / (E.c3.hi + hc2);
+    const float go = E.kc2.hi * tmp;
+    const float ga1 = E.c4.hi * expf(-E.c5.hi * hc2);
+    const float v = go * (1.0f + ga1);
+    dval = -2.0f * (1.0f - hc * tmp) * v + 2.0f * E.c5.hi * hc2 * go * ga1;
+    val = E.c1.hi + hc * v;
+  }
+}
+
+__device__ __forceinline__ void g_ff(const MxParams &mp, int eli, int ikpot, ff hc,
+                                     const ff *etab, ff &val, ff &dval) {
+  const MxElem &E = mp.el[eli];
+  const ff hc2 = ff_mul(hc, hc);
+  if (mp.kind == 0) {
+    const ff om = mp.pr[ikpot].om;
+    const ff inv = ff_rcp(ff_add_fast(E.d2, hc2));
+    val = ff_mul(om, ff_addf(ff_mul(ff_mul(E.c2d2, hc2), inv), 1.0f));
+    dval = ff_mulf(ff_mul(ff_mul(ff_mul(om, E.c2), hc), ff_mul(inv, inv)), -2.0f);
+  } else {
+    const ff tmp = ff_div(hc, ff_add_fast(E.c3, hc2));
+    const ff go = ff_mul(E.kc2, tmp);
+    const ff ga1 = ff_mul(E.c4, ff_exp(ff_neg(ff_mul(E.c5, hc2)), etab));
+    const ff v = ff_mul(go, ff_addf(ga1, 1.0f));
+    const ff t1 = ff_mulf(ff_mul(ff_addf(ff_neg(ff_mul(hc, tmp)), 1.0f), v), -2.0f);
+    const ff t2 = ff_mulf(ff_mul(ff_mul(E.c5, hc2), ff_mul(go, ga1)), 2.0f);
+    dval = ff_add(t1, t2);
+    val = ff_add(E.c1, ff_mul(hc, v));
+  }
+}
+
+// h(dr), dr = r_ij - r_ik (tersoff_func.f90:168-211, kumagai_func.f90:179-221).
+__device__ __forceinline__ void h_f(const MxPair &q, float dr, float &val, float &dval) {
+  if (q.hm == 0) {
+    val = 1.0f;
+    dval = 0.0f;
+    return;
+  }
+  const float x = q.hs.hi * dr;
+  float pw = 1.0f;
+  for (int k = 1; k < q.hm; k++) pw *= x;
+  val = expf(q.hae.hi * pw * x);
+  dval = q.had.hi * (float)q.hm * q.hs.hi * pw * val;
+}
+
+__device__ __forceinline__ void h_ff(const MxPair &q, ff dr, const ff *etab, ff &val, ff &dval) {
+  if (q.hm == 0) {
+    val = ff_make(1.0f, 0.0f);
+    dval = ff_make(0.0f, 0.0f);
+    return;
+  }
+  const ff x = ff_mul(q.hs, dr);
+  ff pw = ff_make(1.0f, 0.0f);
+  for (int k = 1; k < q.hm; k++) pw = ff_mul(pw, x);
+  val = ff_exp(ff_mul(q.hae, ff_mul(pw, x)), etab);
+  dval = ff_mul(ff_mulf(ff_mul(q.had, q.hs), (float)q.hm), ff_mul(pw, val));
+}
+
+// |d ln b / d ln zeta| = sens x / (1 + x), x = beta^n zeta^n (Kumagai: zeta^eta).
+__device__ __forceinline__ float bsens_f(const MxParams &mp, int eli, float zeta) {
+  if (!(zeta > 0.0f)) return 0.0f;
+  const MxElem &E = mp.el[eli];
+  const float x = __expf(E.n.hi * __logf(zeta) + E.lbetan.hi);
+  return E.sens * x / (1.0f + x);
+}
+
+// Bond order in ff (Tersoff: b = xi (1 + beta^n z^n)^e, P = -1/4 fc VA xi
+// beta^n z^(n-1) (1+x)^(e-1); Kumagai: b = (1 + z^eta)^-delta, P = 1/2 fc VA
+// eta z^(eta-1) (-delta) (1+x)^(-delta-1)).  kAcc: ln(1+x) and b in ff (the
+// hot-bond path); otherwise ln(1+x) in FP32 (error counted by bsens).
+template <bool kAcc>
+__device__ __forceinline__ void bo_ff(const MxParams &mp, int eli, int t, ff zeta, ff fc, ff VA,
+                                      const ff *etab, ff &b, ff &P) {
+  if (!(zeta.hi > 0.0f)) {
     b = ff_make(1.0f, 0.0f);
     P = ff_make(0.0f, 0.0f);
     return;
   }
   const MxElem &E = mp.el[eli];
-  const ff lnz = ff_log_f(zeta, etab);
+  const ff lnz = ff_log(zeta, etab);
+  const ff tx = ff_add(ff_mul(E.n, lnz), E.lbetan);  // ln x
+  const ff x = ff_exp(tx, etab);
+  ff L;
+  if (kAcc)
+    L = ff_log(ff_addf(x, 1.0f), etab);
+  else
+    L = ff_make(log1pf(x.hi + x.lo), 0.0f);
   if (mp.kind == 0) {
-    const ff tx = ff_add(ff_mul(E.n, lnz), E.lbetan);
-    const ff x = ff_exp(tx, etab);
-    const float L = log1pf(x.hi + x.lo);
-    const float u = E.e.hi * L;
-    b = ff_mul(mp.pr[t].xi, two_sum(1.0f, expm1f(u)));
-    const ff arg = ff_addf(ff_sub(tx, lnz), (E.e.hi - 1.0f) * L);
+    const ff eL = ff_mul(E.e, L);
+    b = ff_mul(mp.pr[t].xi,
+               kAcc ? ff_exp(eL, etab) : two_sum(1.0f, expm1f(eL.hi)));
+    const ff arg = ff_add(ff_sub(tx, lnz), ff_mul(ff_addf(E.e, -1.0f), L));
     P = ff_mul(ff_mulf(ff_mul(ff_mul(fc, VA), mp.pr[t].xi), -0.25f), ff_exp(arg, etab));
   } else {
-    const ff x = ff_exp(ff_mul(E.eta, lnz), etab);
-    const float L = log1pf(x.hi + x.lo);
-    b = two_sum(1.0f, expm1f(-E.delta.hi * L));
-    const ff arg = ff_addf(ff_mul(ff_addf(E.eta, -1.0f), lnz), (-E.delta.hi - 1.0f) * L);
+    const ff dL = ff_mul(ff_neg(E.delta), L);
+    b = kAcc ? ff_exp(dL, etab) : two_sum(1.0f, expm1f(dL.hi));
+    const ff arg = ff_add(ff_mul(ff_addf(E.eta, -1.0f), lnz),
+                          ff_mul(ff_addf(ff_neg(E.delta), -1.0f), L));
     P = ff_mul(ff_mul(ff_mul(ff_mul(fc, VA), E.eta), ff_neg(E.delta)),
                ff_mulf(ff_exp(arg, etab), 0.5f));
   }
 }
 
-// Three-body k loop in FP32 (h - cos theta from an ff dot product).
-template <class Pot, bool kWat>
-__device__ __forceinline__ void kloop_mx(const Pot &pot, const MxParams &mp, const MxLayout &L,
-                                         int lb, int s, int z, int eli, ff *trow, float &zeta,
-                                         float dbj[3], float wk[9], float &sumdk) {
+// Three-body k loop of bond lb in FP32 (h - cos theta from an ff dot
+// product, bop_kernel.f90:1171-1343).  Also returns sum_k |d zeta/d r_k| for
+// the error estimate.
+template <bool kWat>
+__device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, int lb, int s,
+                                         int z, int eli, ff *trow, float &zeta, float dbj[3],
+                                         float wk[9], float &sumdk) {
   const int nbt = L.nbt, ntrip = L.ntrip;
   const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
   const float rlij = L.r[lb].hi, rinvj = L.rinv[lb].hi;
@@ -186,9 +325,9 @@ __device__ __forceinline__ void kloop_mx(const Pot &pot, const MxParams &mp, con
     const ff hc = ff_sub(h, csf);
     const float cs = csf.hi + csf.lo;
     float hv, dh;
-    pot.template h<float>(ikpot, rlij - rlik, hv, dh);
+    h_f(mp.pr[ikpot], rlij - rlik, hv, dh);
     float gv, dg;
-    pot.template g_hc<float>(eli, ikpot, hc.hi + hc.lo, gv, dg);
+    g_f(mp, eli, ikpot, hc.hi + hc.lo, gv, dg);
     const float dzfac = fcik * dg * hv;
     zeta += fcik * gv * hv;
     const float dzdrij = gv * fcik * dh;
@@ -210,15 +349,15 @@ __device__ __forceinline__ void kloop_mx(const Pot &pot, const MxParams &mp, con
   }
 }
 
-// FP64 k loop for the hot bonds, from the ff geometry.
-template <class Pot, bool kWat>
-__device__ __forceinline__ void kloop_mx64(const Pot &pot, const MxLayout &L, int lb, int s, int z,
-                                           int eli, ff *trow, double &zeta, double dbj[3],
-                                           double wk[9]) {
+// The same k loop in ff arithmetic for the hot bonds.
+template <bool kWat>
+__device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, int lb, int s,
+                                         int z, int eli, ff *trow, const ff *etab, ff &zeta,
+                                         ff dbj[3], ff wk[9]) {
   const int nbt = L.nbt, ntrip = L.ntrip;
-  const double rnij[3] = {ff_to_double(L.rn[lb]), ff_to_double(L.rn[nbt + lb]),
-                          ff_to_double(L.rn[2 * nbt + lb])};
-  const double rlij = ff_to_double(L.r[lb]), rinvj = ff_to_double(L.rinv[lb]);
+  const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
+  const ff rlij = L.r[lb], rinvj = L.rinv[lb];
+  const ff h = mp.el[eli].h;
   for (int q = 0; q < z; q++) {
     const int lk = s + q;
     if (lk == lb) continue;
@@ -230,29 +369,31 @@ __device__ __forceinline__ void kloop_mx64(const Pot &pot, const MxLayout &L, in
       continue;
     }
     const int ikpot = (mk >> 8) & 0xf;
-    const double rnik[3] = {ff_to_double(L.rn[lk]), ff_to_double(L.rn[nbt + lk]),
-                            ff_to_double(L.rn[2 * nbt + lk])};
-    const double rlik = ff_to_double(L.r[lk]), rinvk = ff_to_double(L.rinv[lk]);
-    const double fcik = ff_to_double(L.fc[lk]), dfcik = ff_to_double(L.dfc[lk]);
-    double hv, dh;
-    pot.template h<double>(ikpot, rlij - rlik, hv, dh);
-    const double cs = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
-    double gv, dg;
-    pot.template g<double>(eli, ikpot, cs, gv, dg);
-    const double dzfac = fcik * dg * hv;
-    zeta += fcik * gv * hv;
-    const double dzdrij = gv * fcik * dh;
-    const double dzdrik = gv * (dfcik * hv - fcik * dh);
+    const ff rnik[3] = {L.rn[lk], L.rn[nbt + lk], L.rn[2 * nbt + lk]};
+    const ff rlik = L.r[lk], rinvk = L.rinv[lk], fcik = L.fc[lk], dfcik = L.dfc[lk];
+    ff hv, dh;
+    h_ff(mp.pr[ikpot], ff_sub(rlij, rlik), etab, hv, dh);
+    ff cs = ff_mul(rnik[0], rnij[0]);
+    cs = ff_add(cs, ff_mul(rnik[1], rnij[1]));
+    cs = ff_add(cs, ff_mul(rnik[2], rnij[2]));
+    ff gv, dg;
+    g_ff(mp, eli, ikpot, ff_sub(h, cs), etab, gv, dg);
+    const ff fh = ff_mul(fcik, hv);
+    const ff dzfac = ff_mul(fh, dg);
+    zeta = ff_add_fast(zeta, ff_mul(fh, gv));
+    const ff dzdrij = ff_mul(ff_mul(gv, fcik), dh);
+    const ff dzdrik = ff_mul(gv, ff_sub(ff_mul(dfcik, hv), ff_mul(fcik, dh)));
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      const double dcj = (rnik[c] - cs * rnij[c]) * rinvj;
-      const double dck = (rnij[c] - cs * rnik[c]) * rinvk;
-      dbj[c] += dzdrij * rnij[c] + dzfac * dcj;
-      const double dk = dzdrik * rnik[c] + dzfac * dck;
-      trow[c * ntrip + q] = ff_from_double(dk);
+      const ff dcj = ff_mul(ff_sub(rnik[c], ff_mul(cs, rnij[c])), rinvj);
+      const ff dck = ff_mul(ff_sub(rnij[c], ff_mul(cs, rnik[c])), rinvk);
+      dbj[c] = ff_add_fast(dbj[c], ff_add_fast(ff_mul(dzdrij, rnij[c]), ff_mul(dzfac, dcj)));
+      const ff dk = ff_add_fast(ff_mul(dzdrik, rnik[c]), ff_mul(dzfac, dck));
+      trow[c * ntrip + q] = dk;
       if (kWat)
 #pragma unroll
-        for (int c1 = 0; c1 < 3; c1++) wk[3 * c1 + c] += rnik[c1] * rlik * dk;
+        for (int c1 = 0; c1 < 3; c1++)
+          wk[3 * c1 + c] = ff_add_fast(wk[3 * c1 + c], ff_mul(ff_mul(rnik[c1], rlik), dk));
     }
   }
 }
@@ -260,44 +401,68 @@ __device__ __forceinline__ void kloop_mx64(const Pot &pot, const MxLayout &L, in
 // Energy, radial force and G partial in ff; FP64 per-bond outputs.
 template <bool kWat, bool kPB>
 __device__ __forceinline__ void finalize_mx(const BopArgs &a, const MxLayout &L, int lb, int b,
-                                            ff bij, ff P, const ff dbj[3], const double wk[9],
+                                            ff bij, ff P, const ff dbj[3], const ff wk[9],
                                             ff VA, ff dVA, ff VR, ff dVR) {
   const int nbt = L.nbt;
   const ff fc = L.fc[lb], dfc = L.dfc[lb];
   const ff v = ff_add(VR, ff_mul(bij, VA));    // VR + b VA
   const ff dv = ff_add(dVR, ff_mul(bij, dVA));  // dVR + b dVA
   const ff e_b = ff_mulf(ff_mul(fc, v), 0.5f);
-  const ff dff = ff_mulf(ff_add(ff_mul(fc, dv), ff_mul(dfc, v)), 0.5f);
+  const ff dff = ff_mulf(ff_add_fast(ff_mul(fc, dv), ff_mul(dfc, v)), 0.5f);
   ff dfr[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     dfr[c] = ff_mul(dff, L.rn[c * nbt + lb]);
-    L.G[c * nbt + lb] = ff_neg(ff_add(dfr[c], ff_mul(P, dbj[c])));
+    L.G[c * nbt + lb] = ff_neg(ff_add_fast(dfr[c], ff_mul(P, dbj[c])));
   }
   L.P[lb] = P;
   L.E[lb] = e_b;
-  a.ebond[b] = ff_to_double(e_b);
+  a.ebond[b] = (double)e_b.hi + (double)e_b.lo;
   if (kPB) {
     a.frbond[3 * (size_t)b] = ff_to_double(dfr[0]);
     a.frbond[3 * (size_t)b + 1] = ff_to_double(dfr[1]);
     a.frbond[3 * (size_t)b + 2] = ff_to_double(dfr[2]);
   }
   if (kWat) {
-    const double r = ff_to_double(L.r[lb]);
-    const double P64 = ff_to_double(P);
-    double rij[3], dfr64[3], dbj64[3];
+    // w_ij = r_ij (x) df + P (r_ij (x) dbj + sum_k r_ik (x) dk) (bop_kernel.f90:1404)
+    const ff r = L.r[lb];
+    ff rij[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      rij[c] = r * ff_to_double(L.rn[c * nbt + lb]);
-      dfr64[c] = ff_to_double(dfr[c]);
-      dbj64[c] = ff_to_double(dbj[c]);
-    }
+    for (int c = 0; c < 3; c++) rij[c] = ff_mul(r, L.rn[c * nbt + lb]);
 #pragma unroll
     for (int c1 = 0; c1 < 3; c1++)
 #pragma unroll
-      for (int c2 = 0; c2 < 3; c2++)
-        a.wbond[9 * (size_t)b + c1 + 3 * c2] =
-            rij[c1] * dfr64[c2] + P64 * (rij[c1] * dbj64[c2]) + P64 * wk[3 * c1 + c2];
+      for (int c2 = 0; c2 < 3; c2++) {
+        const ff w = ff_add_fast(ff_mul(rij[c1], dfr[c2]),
+                                 ff_mul(P, ff_add_fast(ff_mul(rij[c1], dbj[c2]), wk[3 * c1 + c2])));
+        a.wbond[9 * (size_t)b + c1 + 3 * c2] = ff_to_double(w);
+      }
+  }
+}
+
+// Deterministic block sum of NC ff values per thread (fixed shuffle tree,
+// then the warps in order); one thread per component writes it as FP64.
+template <int NC>
+__device__ inline void block_sum_ff(const ff (&v)[NC], double *out, ff *scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int nw = kBopThreads / 32;
+#pragma unroll
+  for (int c = 0; c < NC; c++) {
+    ff x = v[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ff y;
+      y.hi = __shfl_down_sync(0xffffffffu, x.hi, o);
+      y.lo = __shfl_down_sync(0xffffffffu, x.lo, o);
+      x = ff_add_fast(x, y);
+    }
+    if (lane == 0) scratch[wid * NC + c] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    ff s = scratch[threadIdx.x];
+    for (int w = 1; w < nw; w++) s = ff_add_fast(s, scratch[w * NC + threadIdx.x]);
+    out[threadIdx.x] = ff_to_double(s);
   }
 }
 
@@ -306,7 +471,7 @@ __global__ void __launch_bounds__(kBopThreads)
     bop_tile_mx(const BopArgs a, const Pot pot, const MxParams mp, const float4 *__restrict__ posff,
                 int max_nbt, int max_ntrip, int *status) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ double red_scratch[(kBopThreads / 32) * 10];
+  __shared__ ff red_scratch[(kBopThreads / 32) * 10];
   __shared__ ff s_exp[256], s_sin[257], s_cos[257];
   __shared__ int s_nhot;
   const int tid = threadIdx.x;
@@ -388,15 +553,15 @@ __global__ void __launch_bounds__(kBopThreads)
       const int t = pair_index(eli, elj, nel);
       meta |= t << 8;
       const float r2f = r2.hi + r2.lo;
-      if (r2f < (float)pot.r2sq(t)) {
+      const MxPair &pp = mp.pr[t];
+      if (r2f < pp.r2sq) {
         ff_sqrt_rsqrt(r2, r, rinv);
 #pragma unroll
         for (int c = 0; c < 3; c++) rn[c] = ff_mul(rij[c], rinv);
         const float rf = r.hi + r.lo;
-        if (r2f < (float)pot.r1sq(t) || rf <= (float)pot.r1(t)) {
+        if (r2f < pp.r1sq || rf <= pp.r1.hi) {
           fc = ff_make(1.0f, 0.0f);
-        } else if (rf < (float)pot.r2(t)) {
-          const MxPair &pp = mp.pr[t];
+        } else if (rf < pp.r2) {
           const ff x = ff_mul(pp.fac, ff_sub(r, pp.r1));
           ff sx, cx;
           ff_sincos(x, s_sin, s_cos, sx, cx);
@@ -412,7 +577,7 @@ __global__ void __launch_bounds__(kBopThreads)
             mf = 1;
         }
         meta |= kFlagShort | (mf << 16);
-        if (rf < (float)pot.r2(t)) {
+        if (rf < pp.r2) {
           meta |= kFlagK;
           if (mf > 0) meta |= kFlagIJ;
         }
@@ -465,28 +630,28 @@ __global__ void __launch_bounds__(kBopThreads)
     if (kWat)
 #pragma unroll
       for (int c = 0; c < 9; c++) wk[c] = 0.0f;
-    kloop_mx<Pot, kWat>(pot, mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
+    kloop_mx<kWat>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
     // A zeta below 1e-30 would overflow the FP32 range inside ln/exp: such a
-    // bond (and any non-finite estimate) takes the FP64 path.
+    // bond (and any non-finite estimate) takes the accurate path.
     const bool tiny = zeta > 0.0f && zeta < 1.0e-30f;
     ff bij, P;
-    bo_ff(mp, eli, t, tiny ? 1.0f : zeta, L.fc[lb], VA, s_exp, bij, P);
-    const float est = 2.4e-7f * fabsf(dVA.hi) * L.fc[lb].hi * pot.bsens(eli, zeta) +
+    bo_ff<false>(mp, eli, t, ff_make(tiny ? 1.0f : zeta, 0.0f), L.fc[lb], VA, s_exp, bij, P);
+    const float est = 2.4e-7f * fabsf(dVA.hi) * L.fc[lb].hi * bsens_f(mp, eli, zeta) +
                       3.0e-7f * fabsf(P.hi) *
                           (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
     if (tiny || !(est <= kHotThreshold)) {
       L.hot[atomicAdd(&s_nhot, 1)] = lb;
     } else {
       const ff dbjf[3] = {ff_make(dbj[0], 0.0f), ff_make(dbj[1], 0.0f), ff_make(dbj[2], 0.0f)};
-      double wkd[9];
+      ff wkf[9];
       if (kWat)
 #pragma unroll
-        for (int c = 0; c < 9; c++) wkd[c] = wk[c];
-      finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbjf, wkd, VA, dVA, VR, dVR);
+        for (int c = 0; c < 9; c++) wkf[c] = ff_make(wk[c], 0.0f);
+      finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbjf, wkf, VA, dVA, VR, dVR);
     }
   }
   __syncthreads();
-  // ---- Phase 2b: FP64 recomputation of the hot bonds. ----
+  // ---- Phase 2b: the hot bonds again, k loop and bond order in ff. ----
   {
     const int nhot = s_nhot;
     for (int hq = tid; hq < nhot; hq += kBopThreads) {
@@ -506,16 +671,24 @@ __global__ void __launch_bounds__(kBopThreads)
       const ff dVA = ff_neg(ff_mul(pp.cA, VA));
       const ff VR = ff_mulf(ff_mul(pp.Ac, ff_exp(ff_neg(ff_mul(pp.cR, r)), s_exp)), hm);
       const ff dVR = ff_neg(ff_mul(pp.cR, VR));
-      double zeta = 0.0, dbj[3] = {0.0, 0.0, 0.0}, wk[9];
+      ff zeta = ff_make(0.0f, 0.0f), wk[9];
+      ff dbj[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
       if (kWat)
 #pragma unroll
-        for (int c = 0; c < 9; c++) wk[c] = 0.0;
-      kloop_mx64<Pot, kWat>(pot, L, lb, s, z, eli, trow, zeta, dbj, wk);
-      double b64, P64;
-      pot.template bo<double>(eli, t, zeta, ff_to_double(L.fc[lb]), ff_to_double(VA), b64, P64);
-      const ff dbjf[3] = {ff_from_double(dbj[0]), ff_from_double(dbj[1]), ff_from_double(dbj[2])};
-      finalize_mx<kWat, kPB>(a, L, lb, b, ff_from_double(b64), ff_from_double(P64), dbjf, wk, VA,
-                             dVA, VR, dVR);
+        for (int c = 0; c < 9; c++) wk[c] = ff_make(0.0f, 0.0f);
+      kloop_ff<kWat>(mp, L, lb, s, z, eli, trow, s_exp, zeta, dbj, wk);
+      ff bij, P;
+      if (zeta.hi > 1.0e-30f) {
+        bo_ff<true>(mp, eli, t, zeta, L.fc[lb], VA, s_exp, bij, P);
+      } else {
+        // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
+        double b64, P64;
+        pot.template bo<double>(eli, t, ff_to_double(zeta), ff_to_double(L.fc[lb]),
+                                ff_to_double(VA), b64, P64);
+        bij = ff_from_double(b64);
+        P = ff_from_double(P64);
+      }
+      finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
     }
   }
   __syncthreads();
@@ -528,7 +701,7 @@ __global__ void __launch_bounds__(kBopThreads)
   for (int lb = tid; lb < nbt; lb += kBopThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
-    eacc = ff_add(eacc, L.E[lb]);
+    eacc = ff_add_fast(eacc, L.E[lb]);
     ff G[3] = {L.G[lb], L.G[nbt + lb], L.G[2 * nbt + lb]};
     if (meta & kFlagK) {
       const int ai = meta & 0xff;
@@ -541,7 +714,7 @@ __global__ void __launch_bounds__(kBopThreads)
         const ff P = L.P[lp];
         const ff *tv = tcol + pq * z;
 #pragma unroll
-        for (int c = 0; c < 3; c++) G[c] = ff_sub(G[c], ff_mul(P, tv[c * ntrip]));
+        for (int c = 0; c < 3; c++) G[c] = ff_add_fast(G[c], ff_neg(ff_mul(P, tv[c * ntrip])));
       }
       const ff r = L.r[lb];
       ff rb[3];
@@ -551,18 +724,18 @@ __global__ void __launch_bounds__(kBopThreads)
       for (int c1 = 0; c1 < 3; c1++)
 #pragma unroll
         for (int c2 = 0; c2 < 3; c2++)
-          wacc[c1 + 3 * c2] = ff_sub(wacc[c1 + 3 * c2], ff_mul(rb[c1], G[c2]));
+          wacc[c1 + 3 * c2] = ff_add_fast(wacc[c1 + 3 * c2], ff_neg(ff_mul(rb[c1], G[c2])));
     }
     float2 *Gout = reinterpret_cast<float2 *>(a.G) + 3 * (size_t)b;
     Gout[0] = make_float2(G[0].hi, G[0].lo);
     Gout[1] = make_float2(G[1].hi, G[1].lo);
     Gout[2] = make_float2(G[2].hi, G[2].lo);
   }
-  double part_v[10];
-  part_v[0] = ff_to_double(eacc);
+  ff part_v[10];
+  part_v[0] = eacc;
 #pragma unroll
-  for (int c = 0; c < 9; c++) part_v[1 + c] = ff_to_double(wacc[c]);
-  block_sum<10>(part_v, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
+  for (int c = 0; c < 9; c++) part_v[1 + c] = wacc[c];
+  block_sum_ff<10>(part_v, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
 }
 
 // Gather of the ff bond forces: F_a = sum_b (G[rev b] - G[b]) in ff.

@@ -529,7 +529,8 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   }
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CUDA(cudaGetLastError());
-  GB_CHECK(reduce_partials(a.part, blocks, 10, o.red, s));
+  GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(blocks) + 64));
+  GB_CHECK(reduce_partials(a.part, blocks, 10, o.red, pot.red_stage.as<double>(), s));
   return 0;
 }
 

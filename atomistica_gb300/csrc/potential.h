@@ -77,7 +77,8 @@ struct Potential {
   // Scratch.
   DevBuf bond_G, bond_e, bond_w, bond_fr, tile_part, red;
   DevBuf atom_dF;
-  DevBuf posff;  // ff positions (mixed form)
+  DevBuf posff;      // ff positions (mixed form)
+  DevBuf red_stage;  // first-stage sums of the tile partials
   DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
   HostBuf hred;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -97,7 +98,12 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
                 bool want_wat);
 
 // Deterministic fixed-order sum of tile partials: red[c] = sum_t part[t*nc+c].
-int reduce_partials(const double *part, int ntiles, int nc, double *red, cudaStream_t s);
+// Deterministic sum of nrows rows of nc (= 10) doubles into red[0..nc); with a
+// stage buffer of reduce_stage_bytes(nrows) bytes large inputs use two passes.
+constexpr int kRedRowsPerBlock = 2048;
+size_t reduce_stage_bytes(int nrows);
+int reduce_partials(const double *part, int nrows, int nc, double *red, double *stage,
+                    cudaStream_t s);
 
 }  // namespace gb
 
