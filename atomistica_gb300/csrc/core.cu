@@ -258,6 +258,7 @@ namespace {
 
 struct BinParams {
   double rec[3][3];
+  float recf[3][3];  // rec rounded to float (cell prefilter)
   double A[3][3];
   int n[3];
   int pbc[3];
@@ -274,18 +275,37 @@ __device__ __forceinline__ int floor_div(int a, int n) {
 }
 
 // floor(matmul(rec_cell_size, r)) with the reference's summation order and no
-// FMA contraction (python_neighbors.f90:641).
+// FMA contraction (python_neighbors.f90:641).  The FP32 value s_f of each row
+// is within 8 u S (S = sum |rec_a x_a|, u = 2^-24; 5.1 u S is the bound of the
+// FP32 and FP64 roundings) of the FP64 value, so floor(s_f -/+ e) agreeing
+// decides the cell; otherwise (an atom within ~1e-5 cells of a boundary) the
+// FP64 evaluation does.
 __device__ __forceinline__ void raw_cell(const BinParams &bp, double x, double y, double z,
-                                         int c[3]) {
+                                         float xf, float yf, float zf, int c[3]) {
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    double s = __dmul_rn(bp.rec[k][0], x);
-    s = __dadd_rn(s, __dmul_rn(bp.rec[k][1], y));
-    s = __dadd_rn(s, __dmul_rn(bp.rec[k][2], z));
-    double f = floor(s);
-    f = fmin(fmax(f, -1.0e9), 1.0e9);
-    c[k] = (int)f;
+    const float p0 = __fmul_rn(bp.recf[k][0], xf), p1 = __fmul_rn(bp.recf[k][1], yf),
+                p2 = __fmul_rn(bp.recf[k][2], zf);
+    const float sf = __fadd_rn(__fadd_rn(p0, p1), p2);
+    const float e = 4.8e-7f * (fabsf(p0) + fabsf(p1) + fabsf(p2)) + 1.0e-37f;
+    const float fl = floorf(sf - e);
+    if (fl == floorf(sf + e) && fabsf(fl) < 1.0e9f) {
+      c[k] = (int)fl;
+    } else {
+      double sd = __dmul_rn(bp.rec[k][0], x);
+      sd = __dadd_rn(sd, __dmul_rn(bp.rec[k][1], y));
+      sd = __dadd_rn(sd, __dmul_rn(bp.rec[k][2], z));
+      double f = floor(sd);
+      f = fmin(fmax(f, -1.0e9), 1.0e9);
+      c[k] = (int)f;
+    }
   }
+}
+
+// Linear cell index, z fastest: the 2 dz + 1 cells of one (x, y) stencil row
+// are contiguous in the cell-sorted atom order.
+__device__ __forceinline__ int cell_linear(const BinParams &bp, int cx, int cy, int cz) {
+  return (cx * bp.n[1] + cy) * bp.n[2] + cz;
 }
 
 __device__ __forceinline__ int pack_wrap(int q0, int q1, int q2) {
@@ -296,23 +316,36 @@ __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams
                                 Pos4 *__restrict__ pos4, int *__restrict__ atom_cell,
                                 int *__restrict__ atom_wrap, int *__restrict__ cell_count,
                                 int *__restrict__ status) {
+  // (blockDim.x is a multiple of 32: every lane reaches the warp reduction)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nat) return;
-  const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+  const bool in = i < nat;
+  double x = 0.0, y = 0.0, z = 0.0;
+  if (in) {
+    x = r[3 * i];
+    y = r[3 * i + 1];
+    z = r[3 * i + 2];
+  }
+  const bool finite = isfinite(x) && isfinite(y) && isfinite(z);
+  const float xf = (float)x, yf = (float)y, zf = (float)z;
+  {
+    // max |coordinate| (rounded up) for the pair prefilter's error bound: one
+    // atomic per warp.
+    const float m = finite ? fmaxf(fabsf(xf), fmaxf(fabsf(yf), fabsf(zf))) * (1.0f + 1.2e-7f)
+                           : 0.0f;
+    const unsigned mw = __reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(m));
+    if ((threadIdx.x & 31) == 0) atomicMax(&status[3], (int)mw);
+  }
+  if (!in) return;
   pos4[i] = Pos4{x, y, z, 0.0};
-  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+  if (!finite) {
     atomicOr(&status[1], 1);  // non-finite position
     atom_cell[i] = 0;
     atom_wrap[i] = pack_wrap(0, 0, 0);
     atomicAdd(&cell_count[0], 1);
     return;
   }
-  {
-    const float m = fmaxf(fabsf((float)x), fmaxf(fabsf((float)y), fabsf((float)z)));
-    atomicMax(&status[3], __float_as_int(m * (1.0f + 1.2e-7f)));
-  }
   int c[3], q[3];
-  raw_cell(bp, x, y, z, c);
+  raw_cell(bp, x, y, z, xf, yf, zf, c);
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     q[k] = 0;
@@ -324,7 +357,7 @@ __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams
     }
     if (q[k] > kMaxShift || q[k] < -kMaxShift) atomicOr(&status[1], 2);
   }
-  const int ci = (c[2] * bp.n[1] + c[1]) * bp.n[0] + c[0];
+  const int ci = cell_linear(bp, c[0], c[1], c[2]);
   atom_cell[i] = ci;
   atom_wrap[i] = pack_wrap(max(min(q[0], kMaxShift), -kMaxShift),
                            max(min(q[1], kMaxShift), -kMaxShift),
@@ -440,27 +473,48 @@ __device__ __forceinline__ bool exact_pair_test(const BinParams &bp, const Pos4 
 // Error bound: with u = 2^-24, X = max |coordinate| and T = sum_k |A_ak s_k|,
 // each component of the FP32 difference vector is within
 // E = u (4X + 8T + 4 cutoff + 4) of the exact one, and
-// |d2_f - d2| <= 2 E (3.47 |d| + 9 E) + 12 u d2 (a factor-2 margin included).
-template <bool kFill>
+// |d2_f - d2| <= 2 E (3.47 |d| + 9 E) + 12 u d2 (a factor-2 margin included);
+// |d| <= (d2 + 1) / 2 replaces the square root.
+//
+// Stencil order (python_neighbors.f90:862-869): x, then y, then z offsets,
+// each cell's atoms by increasing id.  With the z-fastest cell layout the z
+// offsets of one (x, y) row that do not cross the periodic boundary form one
+// contiguous run of the cell-sorted atoms, visited in that same order.
+//
+// kMode: kPairsCount (counts), kPairsFill (CSR j and packed shift at seed[i]),
+// kPairsCountStage (counts, and the first `cap` entries of each atom into
+// stage[i * cap ..], compacted afterwards when no atom has more).
+constexpr int kPairsCount = 0, kPairsFill = 1, kPairsCountStage = 2;
+
+__device__ __forceinline__ bool wrap_cell(const BinParams &bp, int k, int &c, int &s) {
+  const int n = bp.n[k];
+  if (c >= 0 && c < n) return true;
+  if (!bp.pbc[k]) return false;
+  const int q = floor_div(c, n);
+  c -= q * n;
+  s -= q;
+  return true;
+}
+
+template <int kMode>
 __global__ void __launch_bounds__(128)
     nl_pairs(int nat, BinParams bp, const Pos4 *__restrict__ pos4,
              const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
              const int *__restrict__ swrap, const int *__restrict__ cell_start,
              int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
-             int *__restrict__ shift, int *__restrict__ status) {
+             int *__restrict__ shift, int2 *__restrict__ stage, int cap,
+             int *__restrict__ status) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nat) return;
   const float4 pi = spos[t];
   const int i = __float_as_int(pi.w);
   int ci = atom_cell[i];
-  int cell[3];
-  cell[0] = ci % bp.n[0];
-  ci /= bp.n[0];
-  cell[1] = ci % bp.n[1];
-  cell[2] = ci / bp.n[1];
+  const int cz0 = ci % bp.n[2];
+  ci /= bp.n[2];
+  const int cy0 = ci % bp.n[1];
+  const int cx0 = ci / bp.n[1];
   int q0, q1, q2;
   unpack_shift(swrap[t], q0, q1, q2);
-  const int shi[3] = {-q0, -q1, -q2};
   const float u = 5.9604645e-8f;
   const float X = __int_as_float(status[3]);
   const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
@@ -472,35 +526,33 @@ __global__ void __launch_bounds__(128)
       Af[a][k] = (float)bp.A[a][k];
       Amax = fmaxf(Amax, fabsf(Af[a][k]));
     }
-  int cur = kFill ? seed[i] : 0;
+  int cur = kMode == kPairsFill ? seed[i] : 0;
   int cnt = 0;
   bool have_ri = false;
   Pos4 ri;
   for (int x = -bp.dx; x <= bp.dx; x++) {
+    int cx = cx0 + x, sx = -q0;
+    if (!wrap_cell(bp, 0, cx, sx)) continue;
     for (int y = -bp.dy; y <= bp.dy; y++) {
-      for (int z = -bp.dz; z <= bp.dz; z++) {
-        int cc[3] = {cell[0] + x, cell[1] + y, cell[2] + z};
-        int s1[3] = {shi[0], shi[1], shi[2]};
-        bool exists = true;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          if (bp.pbc[k]) {
-            const int q = floor_div(cc[k], bp.n[k]);
-            cc[k] -= q * bp.n[k];
-            s1[k] -= q;
-          } else if (cc[k] < 0 || cc[k] >= bp.n[k]) {
-            exists = false;
-          }
+      int cy = cy0 + y, sy = -q1;
+      if (!wrap_cell(bp, 1, cy, sy)) continue;
+      const int row = cell_linear(bp, cx, cy, 0);
+      int z = -bp.dz;
+      while (z <= bp.dz) {
+        int cz = cz0 + z, sz = -q2;
+        if (!wrap_cell(bp, 2, cz, sz)) {
+          z++;
+          continue;
         }
-        if (!exists) continue;
-        const int c = (cc[2] * bp.n[1] + cc[1]) * bp.n[0] + cc[0];
-        const int js = cell_start[c], je = cell_start[c + 1];
+        const int run = min(bp.dz - z + 1, bp.n[2] - cz);
+        const int js = cell_start[row + cz], je = cell_start[row + cz + run];
+        z += run;
         for (int jq = js; jq < je; jq++) {
           const float4 pj = spos[jq];
           const int j = __float_as_int(pj.w);
           int w0, w1, w2;
           unpack_shift(swrap[jq], w0, w1, w2);
-          const int s2x = s1[0] + w0, s2y = s1[1] + w1, s2z = s1[2] + w2;
+          const int s2x = sx + w0, s2y = sy + w1, s2z = sz + w2;
           const bool zero_shift = (s2x | s2y | s2z) == 0;
           if (j == i && zero_shift) continue;
           float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -513,7 +565,7 @@ __global__ void __launch_bounds__(128)
             E += 8.0f * u * Amax * (fabsf(fx) + fabsf(fy) + fabsf(fz));
           }
           const float d2f = dx * dx + dy * dy + dz * dz;
-          const float B = 2.0f * E * (3.47f * sqrtf(d2f) + 9.0f * E) + 12.0f * u * d2f;
+          const float B = 2.0f * E * (1.735f * (d2f + 1.0f) + 9.0f * E) + 12.0f * u * d2f;
           bool accept;
           if (d2f + B < bp.cutoff_sq_lo) {
             accept = true;
@@ -527,11 +579,13 @@ __global__ void __launch_bounds__(128)
             accept = exact_pair_test(bp, ri, pos4[j], s2x, s2y, s2z);
           }
           if (accept) {
-            if (kFill) {
+            if (kMode == kPairsFill) {
               nbr[cur] = j;
               shift[cur] = pack_shift(s2x, s2y, s2z);
               cur++;
             } else {
+              if (kMode == kPairsCountStage && cnt < cap)
+                stage[(size_t)i * cap + cnt] = make_int2(j, pack_shift(s2x, s2y, s2z));
               cnt++;
               if (s2x > kMaxShift || s2x < -kMaxShift || s2y > kMaxShift ||
                   s2y < -kMaxShift || s2z > kMaxShift || s2z < -kMaxShift)
@@ -542,9 +596,24 @@ __global__ void __launch_bounds__(128)
       }
     }
   }
-  if (!kFill) {
+  if (kMode != kPairsFill) {
     counts[i] = cnt;
     atomicMax(&status[0], cnt);
+  }
+}
+
+// CSR from the staged entries (every atom has at most cap of them).
+__global__ void nl_compact(int nat, int cap, const int *__restrict__ seed,
+                           const int2 *__restrict__ stage, int *__restrict__ nbr,
+                           int *__restrict__ shift) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const int s = seed[i], n = seed[i + 1] - s;
+  const int2 *src = stage + (size_t)i * cap;
+  for (int k = 0; k < n; k++) {
+    const int2 v = src[k];
+    nbr[s + k] = v.x;
+    shift[s + k] = v.y;
   }
 }
 
@@ -657,6 +726,8 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   }
   BinParams bp;
   std::memcpy(bp.rec, nl.rec, sizeof(bp.rec));
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 3; k++) bp.recf[a][k] = (float)nl.rec[a][k];
   std::memcpy(bp.A, p.A, sizeof(bp.A));
   for (int k = 0; k < 3; k++) {
     bp.n[k] = nl.n_cells[k];
@@ -716,10 +787,20 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
                                            nl.atom_wrap.as<int>(), nl.spos.as<float4>(),
                                            nl.swrap.as<int>());
     note_launch();
-    nl_pairs<false><<<(nat + 127) / 128, 128, 0, stream>>>(
-        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
-        nl.swrap.as<int>(), nl.cell_start.as<int>(), nl.counts.as<int>(), nullptr, nullptr,
-        nullptr, status);
+    // Single pass (count + staged entries) once a previous build has sized
+    // the per-atom capacity; count-only pass otherwise.
+    if (nl.stage_cap > 0) {
+      GB_CHECK(nl.stage.ensure(sizeof(int2) * (size_t)nat * nl.stage_cap));
+      nl_pairs<kPairsCountStage><<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
+          nl.swrap.as<int>(), nl.cell_start.as<int>(), nl.counts.as<int>(), nullptr, nullptr,
+          nullptr, nl.stage.as<int2>(), nl.stage_cap, status);
+    } else {
+      nl_pairs<kPairsCount><<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
+          nl.swrap.as<int>(), nl.cell_start.as<int>(), nl.counts.as<int>(), nullptr, nullptr,
+          nullptr, nullptr, 0, status);
+    }
     note_launch();
   }
   GB_CHECK(exclusive_scan_i32(nl.counts.as<int>(), nl.seed.as<int>(), nat, nl.scan_tmp, stream));
@@ -745,16 +826,29 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   }
   GB_CHECK(nl.nbr.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
   GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
+  const int maxz = hs[0];
   if (nat > 0) {
-    nl_pairs<true><<<(nat + 127) / 128, 128, 0, stream>>>(
-        nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
-        nl.swrap.as<int>(), nl.cell_start.as<int>(), nullptr, nl.seed.as<int>(),
-        nl.nbr.as<int>(), nl.shift.as<int>(), status);
+    if (nl.stage_cap > 0 && maxz <= nl.stage_cap) {
+      nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
+                                                        nl.stage.as<int2>(), nl.nbr.as<int>(),
+                                                        nl.shift.as<int>());
+    } else {
+      nl_pairs<kPairsFill><<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
+          nl.swrap.as<int>(), nl.cell_start.as<int>(), nullptr, nl.seed.as<int>(),
+          nl.nbr.as<int>(), nl.shift.as<int>(), nullptr, 0, status);
+    }
     note_launch();
+  }
+  // Capacity of the next build's single pass: this build's maximum plus a
+  // margin, while the stage stays below kStageMaxBytes.
+  {
+    const int cap = ((maxz + maxz / 4 + 4) + 3) & ~3;
+    nl.stage_cap = (size_t)nat * cap * sizeof(int2) <= kStageMaxBytes ? cap : 0;
   }
   GB_CUDA(cudaGetLastError());
   nl.nentries = total;
-  nl.maxz = hs[0];
+  nl.maxz = maxz;
   nl.cutoff = cutoff;
   nl.valid = true;
   nl.built_for = &p;

@@ -98,6 +98,8 @@ __host__ __device__ inline void unpack_shift(int32_t p, int &s0, int &s1, int &s
   s2 = (int)((u >> 20) & 1023u) - 512;
 }
 constexpr int kMaxShift = 511;
+// Largest staging buffer of the single-pass neighbour build (bytes).
+constexpr size_t kStageMaxBytes = size_t(2) << 30;
 
 // Position padded to 32 bytes: one DRAM sector per gather.
 struct __align__(32) Pos4 {
@@ -140,6 +142,8 @@ struct Neighbors {
   DevBuf nbr;         // int[capacity]
   DevBuf shift;       // int32 packed shifts [capacity]
   DevBuf rev;         // int[capacity]: reverse entry (built on demand)
+  DevBuf stage;       // int2[nat * stage_cap]: staged entries of the single pass
+  int stage_cap = 0;  // per-atom capacity of the single pass (0: two passes)
   DevBuf scan_tmp;
   DevBuf stats;       // device-side status words
   HostBuf hstats;
