@@ -55,6 +55,7 @@ SIGNATURES = [
     ("gb_tabulated_alloy_eam_energy_and_forces", _I, [_P] * 10 + [_P]),
     ("gb_tabulated_alloy_eam_table", _I, [_P, _I, _I, _P, _P]),
     ("gb_potential_last_timing", _I, [_P, _P]),
+    ("gb_potential_last_stats", _I, [_P, _P]),
     ("gb_bop_energy_and_forces_noalloc", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                               _P]),
     ("gb_kernel_launches", ctypes.c_uint64, []),

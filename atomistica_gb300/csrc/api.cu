@@ -261,7 +261,7 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CHECK(pot.red.ensure(sizeof(double) * 16));
   o.red = pot.red.as<double>();
   o.status = reinterpret_cast<int *>(o.red + 12);
-  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 2, s));
+  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s));
 
   const bool want_wat = wpa != nullptr || wpb != nullptr;
   const bool want_pb = epb || fpb || wpb;
@@ -295,6 +295,8 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
   const int st = reinterpret_cast<const int *>(hr + 12)[0];
   pot.last_status = st;
+  pot.last_hot = reinterpret_cast<const int *>(hr + 12)[2];
+  pot.last_bonds = pot.kind == kEAM ? 0 : nl.nentries;
   if (st & 1) {
     set_error("Spline argument outside of the defined interval (EAM density table).");
     return GB_ERROR_DOMAIN;
@@ -522,6 +524,15 @@ int gb_tabulated_alloy_eam_table(const gb_potential_t *h, int which, int idx, do
 int gb_potential_last_timing(const gb_potential_t *h, double *ms) {
   if (!h || !ms) return GB_ERROR_ARGUMENT;
   for (int q = 0; q < 4; q++) ms[q] = h->pot.timing[q];
+  return 0;
+}
+
+int gb_potential_last_stats(const gb_potential_t *h, int64_t *stats) {
+  if (!h || !stats) return GB_ERROR_ARGUMENT;
+  stats[0] = h->pot.last_bonds;
+  stats[1] = h->pot.last_hot;
+  stats[2] = h->pot.tile_atoms;
+  stats[3] = 0;
   return 0;
 }
 

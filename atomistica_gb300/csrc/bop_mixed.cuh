@@ -126,6 +126,22 @@ __device__ __forceinline__ ff ff_add_fast(ff a, ff b) {
   return quick_two_sum(s.hi, s.lo);
 }
 
+// acc += a b with an unnormalised accumulator (hi: running FP32 sum, lo:
+// its rounding errors and the low parts); ff_norm before use.
+__device__ __forceinline__ void ff_acc_mul(ff &acc, ff a, ff b) {
+  ff p = two_prod(a.hi, b.hi);
+  p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+  const ff s = two_sum(acc.hi, p.hi);
+  acc.hi = s.hi;
+  acc.lo += s.lo + p.lo;
+}
+__device__ __forceinline__ void ff_acc(ff &acc, ff a) {
+  const ff s = two_sum(acc.hi, a.hi);
+  acc.hi = s.hi;
+  acc.lo += s.lo + a.lo;
+}
+__device__ __forceinline__ ff ff_norm(ff a) { return two_sum(a.hi, a.lo); }
+
 struct MxLayout {
   int *aseed, *toff, *el, *meta, *hot;
   ff *rn;  // 3 * nbt (component-major)
@@ -165,14 +181,6 @@ __device__ inline MxLayout carve_mx(unsigned char *sm, int nbt, int ntrip) {
   o += align16(sizeof(ff) * (size_t)nbt * 12);
   L.t = reinterpret_cast<ff *>(sm + o);
   return L;
-}
-
-// ln z for an ff z > 0: one Newton step on logf(z.hi).
-__device__ __forceinline__ ff ff_log(ff z, const ff *etab) {
-  const float l0 = logf(z.hi);
-  const ff e = ff_exp(ff_make(-l0, 0.0f), etab);  // e^-l0
-  const ff w = ff_addf(ff_mul(e, z), -1.0f);      // z e^-l0 - 1
-  return ff_addf(w, l0);
 }
 
 // ---- Three-body functions on the MxParams copies of the parameters. ----
@@ -254,11 +262,40 @@ __device__ __forceinline__ float bsens_f(const MxParams &mp, int eli, float zeta
   return E.sens * x / (1.0f + x);
 }
 
-// Bond order in ff (Tersoff: b = xi (1 + beta^n z^n)^e, P = -1/4 fc VA xi
-// beta^n z^(n-1) (1+x)^(e-1); Kumagai: b = (1 + z^eta)^-delta, P = 1/2 fc VA
-// eta z^(eta-1) (-delta) (1+x)^(-delta-1)).  kAcc: ln(1+x) and b in ff (the
-// hot-bond path); otherwise ln(1+x) in FP32 (error counted by bsens).
-template <bool kAcc>
+// Bond order of a bond on the FP32 path, from its FP32 zeta (tersoff_func.f90
+// :122-160, kumagai_func.f90:139-171): ln zeta, x = beta^n zeta^n and the
+// exponent of P in ff, so that b and P carry only the error of zeta (the
+// error estimate's first term); log1p(x) and expm1 in FP32, where their
+// error is of the order of zeta's.
+__device__ __forceinline__ void bo_f(const MxParams &mp, int eli, int t, float zeta, ff fc, ff VA,
+                                     const ff *etab, ff &b, ff &P) {
+  if (!(zeta > 0.0f)) {
+    b = ff_make(1.0f, 0.0f);
+    P = ff_make(0.0f, 0.0f);
+    return;
+  }
+  const MxElem &E = mp.el[eli];
+  const ff lnz = ff_log_f(zeta, etab);
+  if (mp.kind == 0) {
+    const ff tx = ff_add(ff_mul(E.n, lnz), E.lbetan);  // ln x
+    const ff x = ff_exp(tx, etab);
+    const float L = log1pf(x.hi + x.lo);
+    b = ff_mul(mp.pr[t].xi, two_sum(1.0f, expm1f(E.e.hi * L)));
+    const ff arg = ff_addf(ff_sub(tx, lnz), (E.e.hi - 1.0f) * L);
+    P = ff_mul(ff_mulf(ff_mul(ff_mul(fc, VA), mp.pr[t].xi), -0.25f), ff_exp(arg, etab));
+  } else {
+    const ff x = ff_exp(ff_mul(E.eta, lnz), etab);
+    const float L = log1pf(x.hi + x.lo);
+    b = two_sum(1.0f, expm1f(-E.delta.hi * L));
+    const ff arg = ff_addf(ff_mul(ff_addf(E.eta, -1.0f), lnz), (-E.delta.hi - 1.0f) * L);
+    P = ff_mul(ff_mul(ff_mul(ff_mul(fc, VA), E.eta), ff_neg(E.delta)),
+               ff_mulf(ff_exp(arg, etab), 0.5f));
+  }
+}
+
+// Bond order in ff from an ff zeta (the hot-bond path; Tersoff: b = xi
+// (1 + beta^n z^n)^e, P = -1/4 fc VA xi beta^n z^(n-1) (1+x)^(e-1); Kumagai:
+// b = (1 + z^eta)^-delta, P = 1/2 fc VA eta z^(eta-1) (-delta) (1+x)^(-delta-1)).
 __device__ __forceinline__ void bo_ff(const MxParams &mp, int eli, int t, ff zeta, ff fc, ff VA,
                                       const ff *etab, ff &b, ff &P) {
   if (!(zeta.hi > 0.0f)) {
@@ -270,20 +307,13 @@ __device__ __forceinline__ void bo_ff(const MxParams &mp, int eli, int t, ff zet
   const ff lnz = ff_log(zeta, etab);
   const ff tx = ff_add(ff_mul(E.n, lnz), E.lbetan);  // ln x
   const ff x = ff_exp(tx, etab);
-  ff L;
-  if (kAcc)
-    L = ff_log(ff_addf(x, 1.0f), etab);
-  else
-    L = ff_make(log1pf(x.hi + x.lo), 0.0f);
+  const ff L = ff_log(ff_addf(x, 1.0f), etab);
   if (mp.kind == 0) {
-    const ff eL = ff_mul(E.e, L);
-    b = ff_mul(mp.pr[t].xi,
-               kAcc ? ff_exp(eL, etab) : two_sum(1.0f, expm1f(eL.hi)));
+    b = ff_mul(mp.pr[t].xi, ff_exp(ff_mul(E.e, L), etab));
     const ff arg = ff_add(ff_sub(tx, lnz), ff_mul(ff_addf(E.e, -1.0f), L));
     P = ff_mul(ff_mulf(ff_mul(ff_mul(fc, VA), mp.pr[t].xi), -0.25f), ff_exp(arg, etab));
   } else {
-    const ff dL = ff_mul(ff_neg(E.delta), L);
-    b = kAcc ? ff_exp(dL, etab) : two_sum(1.0f, expm1f(dL.hi));
+    b = ff_exp(ff_mul(ff_neg(E.delta), L), etab);
     const ff arg = ff_add(ff_mul(ff_addf(E.eta, -1.0f), lnz),
                           ff_mul(ff_addf(ff_neg(E.delta), -1.0f), L));
     P = ff_mul(ff_mul(ff_mul(ff_mul(fc, VA), E.eta), ff_neg(E.delta)),
@@ -440,29 +470,46 @@ __device__ __forceinline__ void finalize_mx(const BopArgs &a, const MxLayout &L,
   }
 }
 
-// Deterministic block sum of NC ff values per thread (fixed shuffle tree,
-// then the warps in order); one thread per component writes it as FP64.
+// Deterministic block sum of NC <= 16 ff values per thread.  Within a warp a
+// reduce-scatter butterfly (lanes l, l ^ m exchange half of their components
+// for m = 16, 8, 4, 2; then m = 1) leaves component
+// c = 8 b4 + 4 b3 + 2 b2 + b1 (b_k: bit k of the lane) summed over the warp in
+// lanes 2c and 2c+1; the warps' sums are then added in order and written as
+// FP64 by one thread per component.
 template <int NC>
 __device__ inline void block_sum_ff(const ff (&v)[NC], double *out, ff *scratch) {
+  static_assert(NC <= 16, "block_sum_ff: at most 16 components");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int nw = kBopThreads / 32;
+  ff x[16];
 #pragma unroll
-  for (int c = 0; c < NC; c++) {
-    ff x = v[c];
+  for (int c = 0; c < 16; c++) x[c] = c < NC ? v[c] : ff_make(0.0f, 0.0f);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ff y;
-      y.hi = __shfl_down_sync(0xffffffffu, x.hi, o);
-      y.lo = __shfl_down_sync(0xffffffffu, x.lo, o);
-      x = ff_add_fast(x, y);
+  for (int lev = 0; lev < 4; lev++) {
+    const int m = 16 >> lev, H = 8 >> lev;
+    const bool up = (lane & m) != 0;
+#pragma unroll
+    for (int q = 0; q < H; q++) {
+      const ff send = up ? x[q] : x[q + H];
+      const ff keep = up ? x[q + H] : x[q];
+      ff recv;
+      recv.hi = __shfl_xor_sync(0xffffffffu, send.hi, m);
+      recv.lo = __shfl_xor_sync(0xffffffffu, send.lo, m);
+      x[q] = ff_add_fast(keep, recv);
     }
-    if (lane == 0) scratch[wid * NC + c] = x;
   }
+  ff recv;
+  recv.hi = __shfl_xor_sync(0xffffffffu, x[0].hi, 1);
+  recv.lo = __shfl_xor_sync(0xffffffffu, x[0].lo, 1);
+  const ff r = ff_add_fast(x[0], recv);
+  const int c = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
+                ((lane >> 1) & 1);
+  if ((lane & 1) == 0 && c < NC) scratch[wid * NC + c] = r;
   __syncthreads();
   if (threadIdx.x < NC) {
-    ff s = scratch[threadIdx.x];
-    for (int w = 1; w < nw; w++) s = ff_add_fast(s, scratch[w * NC + threadIdx.x]);
-    out[threadIdx.x] = ff_to_double(s);
+    ff sum = scratch[threadIdx.x];
+    for (int w = 1; w < nw; w++) sum = ff_add_fast(sum, scratch[w * NC + threadIdx.x]);
+    out[threadIdx.x] = ff_to_double(sum);
   }
 }
 
@@ -635,7 +682,10 @@ __global__ void __launch_bounds__(kBopThreads)
     // bond (and any non-finite estimate) takes the accurate path.
     const bool tiny = zeta > 0.0f && zeta < 1.0e-30f;
     ff bij, P;
-    bo_ff<false>(mp, eli, t, ff_make(tiny ? 1.0f : zeta, 0.0f), L.fc[lb], VA, s_exp, bij, P);
+    bo_f(mp, eli, t, tiny ? 1.0f : zeta, L.fc[lb], VA, s_exp, bij, P);
+    // Error estimate (eV/A) of this bond's forces on the FP32 path: the FP32
+    // zeta through d b / d ln zeta, and the FP32 three-body derivatives
+    // multiplied by P.
     const float est = 2.4e-7f * fabsf(dVA.hi) * L.fc[lb].hi * bsens_f(mp, eli, zeta) +
                       3.0e-7f * fabsf(P.hi) *
                           (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
@@ -654,6 +704,7 @@ __global__ void __launch_bounds__(kBopThreads)
   // ---- Phase 2b: the hot bonds again, k loop and bond order in ff. ----
   {
     const int nhot = s_nhot;
+    if (tid == 0 && nhot > 0) atomicAdd(&status[2], nhot);  // diagnostic count
     for (int hq = tid; hq < nhot; hq += kBopThreads) {
       const int lb = L.hot[hq];
       const int b = b0 + lb;
@@ -679,7 +730,7 @@ __global__ void __launch_bounds__(kBopThreads)
       kloop_ff<kWat>(mp, L, lb, s, z, eli, trow, s_exp, zeta, dbj, wk);
       ff bij, P;
       if (zeta.hi > 1.0e-30f) {
-        bo_ff<true>(mp, eli, t, zeta, L.fc[lb], VA, s_exp, bij, P);
+        bo_ff(mp, eli, t, zeta, L.fc[lb], VA, s_exp, bij, P);
       } else {
         // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
         double b64, P64;
@@ -701,7 +752,7 @@ __global__ void __launch_bounds__(kBopThreads)
   for (int lb = tid; lb < nbt; lb += kBopThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
-    eacc = ff_add_fast(eacc, L.E[lb]);
+    ff_acc(eacc, L.E[lb]);
     ff G[3] = {L.G[lb], L.G[nbt + lb], L.G[2 * nbt + lb]};
     if (meta & kFlagK) {
       const int ai = meta & 0xff;
@@ -711,20 +762,21 @@ __global__ void __launch_bounds__(kBopThreads)
         const int lp = s + pq;
         if (lp == lb) continue;
         if (!(L.meta[lp] & kFlagIJ)) continue;
-        const ff P = L.P[lp];
+        const ff mP = ff_neg(L.P[lp]);
         const ff *tv = tcol + pq * z;
 #pragma unroll
-        for (int c = 0; c < 3; c++) G[c] = ff_add_fast(G[c], ff_neg(ff_mul(P, tv[c * ntrip])));
+        for (int c = 0; c < 3; c++) ff_acc_mul(G[c], mP, tv[c * ntrip]);
       }
-      const ff r = L.r[lb];
-      ff rb[3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) rb[c] = ff_mul(r, L.rn[c * nbt + lb]);
+      for (int c = 0; c < 3; c++) G[c] = ff_norm(G[c]);
+      const ff r = L.r[lb];
+      ff mrb[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) mrb[c] = ff_neg(ff_mul(r, L.rn[c * nbt + lb]));
 #pragma unroll
       for (int c1 = 0; c1 < 3; c1++)
 #pragma unroll
-        for (int c2 = 0; c2 < 3; c2++)
-          wacc[c1 + 3 * c2] = ff_add_fast(wacc[c1 + 3 * c2], ff_neg(ff_mul(rb[c1], G[c2])));
+        for (int c2 = 0; c2 < 3; c2++) ff_acc_mul(wacc[c1 + 3 * c2], mrb[c1], G[c2]);
     }
     float2 *Gout = reinterpret_cast<float2 *>(a.G) + 3 * (size_t)b;
     Gout[0] = make_float2(G[0].hi, G[0].lo);
@@ -732,9 +784,9 @@ __global__ void __launch_bounds__(kBopThreads)
     Gout[2] = make_float2(G[2].hi, G[2].lo);
   }
   ff part_v[10];
-  part_v[0] = eacc;
+  part_v[0] = ff_norm(eacc);
 #pragma unroll
-  for (int c = 0; c < 9; c++) part_v[1 + c] = wacc[c];
+  for (int c = 0; c < 9; c++) part_v[1 + c] = ff_norm(wacc[c]);
   block_sum_ff<10>(part_v, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
 }
 

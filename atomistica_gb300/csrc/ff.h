@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define FF_HD __host__ __device__ __forceinline__
@@ -26,6 +27,16 @@ namespace gb {
 struct ff {
   float hi, lo;
 };
+
+FF_HD float __int_as_float_hd(int i) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(i);
+#else
+  float f;
+  std::memcpy(&f, &i, sizeof f);
+  return f;
+#endif
+}
 
 FF_HD ff ff_make(float hi, float lo) {
   ff r;
@@ -116,29 +127,49 @@ constexpr float kFfC_mid = -7.4400555e-12f;
 FF_HD ff ff_exp(ff t, const ff *tab) {
   const float kf = floorf(t.hi * kFfInvC);
   const int k = (int)kf;
-  // rho = t - kf * C with C in two parts; kf*C_hi exact via two_prod.
+  // rho = t - kf * C, C = C_hi + C_mid: kf * C_hi exact via two_prod, the
+  // leading difference exact via two_sum, then the small parts; the tail
+  // polynomial takes rho.lo to first order.
   const ff kc = two_prod(kf, kFfC_hi);
-  ff rho = ff_sub(t, kc);
-  rho = ff_addf(rho, -kf * kFfC_mid);
-  const float r = rho.hi;
-  const float tail = rho.lo * (1.0f + r) +
+  const ff rh = two_sum(t.hi, -kc.hi);
+  const ff rho = two_sum(rh.hi, rh.lo + ((t.lo - kc.lo) - kf * kFfC_mid));
+  const float r = rho.hi, lo = rho.lo;
+  const float tail = lo * (1.0f + r) +
                      r * r * (0.5f + r * (0.16666667f + r * (0.041666668f + r * 0.0083333338f)));
   const ff eps = two_sum(r, tail);  // e^rho - 1
   const ff T = tab[k & 255];
-  ff v = ff_add(T, ff_mul(T, eps));
+  const ff Te = ff_mul(T, eps);  // |T eps| < 0.006 T: no cancellation below
+  ff v = two_sum(T.hi, Te.hi);
+  v.lo += T.lo + Te.lo;
+  v = quick_two_sum(v.hi, v.lo);
   const int e = k >> 8;
-  v.hi = ldexpf(v.hi, e);
-  v.lo = ldexpf(v.lo, e);
+  if (e > -120 && e < 120) {
+    const float sc = __int_as_float_hd((e + 127) << 23);  // 2^e, exact scaling
+    v.hi *= sc;
+    v.lo *= sc;
+  } else {
+    v.hi = ldexpf(v.hi, e);
+    v.lo = ldexpf(v.lo, e);
+  }
   return v;
 }
 
-// ln z for a positive FP32 z: one Newton step on logf, accurate to ~1e-12.
-FF_HD ff ff_log_f(float z, const ff *exptab) {
-  const float l0 = logf(z);
+// ln z for an ff z > 0: a start value l0 ~ ln z.hi, then
+// ln z = l0 + log1p(w), w = z e^-l0 - 1, with log1p(w) = w - w^2/2 (|w| < 1e-5).
+FF_HD ff ff_log(ff z, const ff *exptab) {
+#ifdef __CUDA_ARCH__
+  const float l0 = __logf(z.hi);
+#else
+  const float l0 = logf(z.hi);
+#endif
   const ff e = ff_exp(ff_make(-l0, 0.0f), exptab);  // e^-l0
-  const ff w = ff_addf(ff_mulf(e, z), -1.0f);      // z e^-l0 - 1
-  return ff_addf(w, l0);
+  const ff w = ff_addf(ff_mul(e, z), -1.0f);      // z e^-l0 - 1
+  const ff lw = ff_addf(w, -0.5f * w.hi * w.hi);
+  return ff_addf(lw, l0);
 }
+
+// ln z for a positive FP32 z.
+FF_HD ff ff_log_f(float z, const ff *exptab) { return ff_log(ff_make(z, 0.0f), exptab); }
 
 // ---------------------------------------------------------------------------
 // sin, cos of x in [0, pi]: x = j (pi/256) + d, |d| <= pi/512;

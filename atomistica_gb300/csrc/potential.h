@@ -86,6 +86,8 @@ struct Potential {
   double timing[4] = {0, 0, 0, 0};
   int tile_atoms = 32;
   int last_status = 0;
+  int last_hot = 0;         // bonds recomputed on the accurate path (mixed form)
+  int64_t last_bonds = 0;   // directed bonds of the last bond-order call
 };
 
 // Interaction range requested by bind_to for the given element pair set.

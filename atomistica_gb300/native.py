@@ -278,6 +278,13 @@ class _Potential:
         self._L.gb_potential_last_timing(self._h, t)
         return tuple(t)
 
+    def last_stats(self):
+        """(directed bonds, bonds recomputed on the accurate path of the mixed
+        form, atoms per tile) of the last call."""
+        v = (ctypes.c_int64 * 4)()
+        self._L.gb_potential_last_stats(self._h, v)
+        return tuple(v[:3])
+
     def energy_and_forces(self, particles, neighbors, forces=None, mask=None, charges=None,
                           epot_per_at=None, epot_per_bond=None, f_per_bond=None,
                           wpot_per_at=None, wpot_per_bond=None):

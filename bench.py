@@ -44,11 +44,16 @@ UNIT = "atom-evals/s"
 
 # Algorithmic flop model per directed bond and per triplet (+,-,*,/,sqrt and
 # each exp/pow/cos/sin counted as one flop), counted from the reference's
-# non-screened BOP code.  In the mixed form the triplet terms and the bond
-# order run in FP32, the bond geometry and pair terms in FP64.
+# non-screened BOP code.  Both forms execute all of it: the FP64 drop-in on
+# the FP64 pipe, the mixed form on the FP32 pipe (FP32 three-body terms,
+# float-float geometry, pair terms and accumulation).
 FLOPS_BOND = 150.0
 FLOPS_TRIPLET = 165.0
-FLOPS_BO = 14.0
+# Compulsory DRAM bytes of one bond-order tile launch: per atom positions
+# (32 B), element (4 B) and CSR offset (4 B); per directed bond the neighbour
+# index and packed shift (8 B) in, the bond force G (24 B) and energy (8 B) out.
+BYTES_ATOM = 40.0
+BYTES_BOND = 40.0
 
 
 def parse_args():
@@ -124,17 +129,13 @@ class ClockSampler:
 
 
 def flop_model(z):
-    """Algorithmic FP32 / FP64 flops per call of the mixed and FP64 forms."""
+    """Algorithmic flops and compulsory bytes of one bond-order evaluation."""
     import numpy as np
     z = np.asarray(z, dtype=np.float64)
     nb = float(z.sum())
     nt = float((z * (z - 1)).sum())
-    return {
-        "bonds": nb, "triplets": nt,
-        "fp64_form_fp64": FLOPS_BOND * nb + FLOPS_TRIPLET * nt,
-        "mixed_fp32": FLOPS_TRIPLET * nt + FLOPS_BO * nb,
-        "mixed_fp64": (FLOPS_BOND - FLOPS_BO) * nb,
-    }
+    return {"bonds": nb, "triplets": nt, "flops": FLOPS_BOND * nb + FLOPS_TRIPLET * nt,
+            "bytes": BYTES_ATOM * len(z) + BYTES_BOND * nb}
 
 
 def cpu_baseline(structure, params, runs):
@@ -289,6 +290,7 @@ def run_ours(args):
     for prec in ("fp64", "mixed"):
         e, f, w = step(pots[prec])
         res[prec] = (e, f.cpu().numpy().copy(), np.array(w))
+    hot = pots["mixed"].last_stats()
     seed_np, _, _ = nl.get_list(p)
     fm = flop_model(np.diff(seed_np))
 
@@ -317,24 +319,28 @@ def run_ours(args):
                   "gb_particles_set_positions / gb_potential_energy_and_forces), pinned "
                   "host numpy buffers"}
 
-    # Roofline of the dominant kernel (mixed bond-order tile kernel).
+    # Roofline of the dominant kernel (mixed bond-order tile kernel):
+    # T_roof = max(flops / FP32 peak, bytes / HBM peak), frac = T_roof / t.
     p32 = _peak(L, 0)
     p64 = _peak(L, 1)
+    hbm = _hbm_peak()
     t_k = kern_mx * 1e-3
-    t_roof = max(fm["mixed_fp32"] / (p32 * 1e12), fm["mixed_fp64"] / (p64 * 1e12))
-    bound = "fp32" if fm["mixed_fp32"] / p32 >= fm["mixed_fp64"] / p64 else "fp64"
-    achieved = (fm["mixed_fp32"] if bound == "fp32" else fm["mixed_fp64"]) / t_k / 1e12
-    peak = p32 if bound == "fp32" else p64
-    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": t_roof / t_k, "traffic": None,
-                "kernel": "bop_tile<Tersoff, float> (mixed form)",
+    t_flop = fm["flops"] / (p32 * 1e12)
+    t_byte = fm["bytes"] / (hbm * 1e9)
+    roofline = {"bound": "fp32" if t_flop >= t_byte else "hbm",
+                "achieved": fm["flops"] / t_k / 1e12, "peak": p32, "unit": "TFLOP/s",
+                "frac": max(t_flop, t_byte) / t_k, "traffic": None,
+                "kernel": "bop_tile_mx<Tersoff> (mixed form)",
                 "kernel_ms": kern_mx,
-                "peak_source": "FMA-chain microbenchmark in this run (MEASURED_PEAKS.json has "
-                               "no FP32/FP64 peak; no tensor cores on this path)",
+                "t_roof_ms": 1e3 * max(t_flop, t_byte),
+                "bytes_per_launch": fm["bytes"], "hbm_gbs": hbm,
+                "peak_source": "FP32/FP64 FMA-chain microbenchmark in this run (MEASURED_PEAKS.json "
+                               "has no FP32/FP64 peak; no tensor cores on this path); HBM from "
+                               "MEASURED_PEAKS.json",
                 "fp32_peak_tflops": p32, "fp64_peak_tflops": p64,
                 "fp64_form": {"kernel": "bop_tile<Tersoff, double>", "kernel_ms": kern_64,
-                              "achieved_tflops": fm["fp64_form_fp64"] / (kern_64 * 1e-3) / 1e12,
-                              "frac_of_fp64_peak": fm["fp64_form_fp64"] / (kern_64 * 1e-3)
+                              "achieved_tflops": fm["flops"] / (kern_64 * 1e-3) / 1e12,
+                              "frac_of_fp64_peak": fm["flops"] / (kern_64 * 1e-3)
                               / (p64 * 1e12)},
                 "flop_model": {"per_bond": FLOPS_BOND, "per_triplet": FLOPS_TRIPLET,
                                "bonds": fm["bonds"], "triplets": fm["triplets"]}}
@@ -343,7 +349,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_mx / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 three-body/bond-order + fp64 geometry, pair terms, accumulation",
+        "dtype": "fp32 three-body terms + float-float (2 x fp32) geometry, pair terms, "
+                 "bond order, accumulation; fp64 tile sums",
         "data": "synthetic (seeded)",
         "config": {"workload": "tersoff_si_amorphous_%d" % nat, "natoms": nat,
                    "seed": args.seed, "density_gcc": 2.33, "sigma_A": 0.25,
@@ -355,6 +362,8 @@ def run_ours(args):
         "fp64_dropin": {"value": value64, "unit": UNIT, "ms_per_step": 1e3 * t_64 / args.steps,
                         "neighbour_ms": nl_64, "kernel_ms": kern_64},
         "mixed_over_fp64": value / value64,
+        "mixed_accurate_path": {"bonds": hot[0], "recomputed": hot[1],
+                                "fraction": hot[1] / max(hot[0], 1), "atoms_per_tile": hot[2]},
         "value_without_neighbour_build": ws * nat / ((1e3 * t_mx / args.steps - nl_mx) * 1e-3),
         "neighbour_ms": nl_mx,
         "e2e": e2e,
@@ -382,6 +391,16 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) from MEASURED_PEAKS.json, else the
+    profiling fallback 6800 GB/s."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
 
 
 _peaks = {}

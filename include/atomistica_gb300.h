@@ -248,6 +248,11 @@ int gb_bop_energy_and_forces_noalloc(gb_potential_t *pot, int nat, const double 
  * [2] total, [3] the dominant force kernel alone (bond-order tile kernel or
  * EAM pair kernel).  ms must hold 4 doubles. */
 int gb_potential_last_timing(const gb_potential_t *pot, double *ms);
+/* Work counts of the last energy_and_forces call: stats[0] directed bonds
+ * (bond-order potentials), stats[1] bonds of the mixed form whose estimated
+ * FP32 error sent them through the float-float recomputation, stats[2] atoms
+ * per bond-order tile, stats[3] reserved (0).  stats must hold 4 int64_t. */
+int gb_potential_last_stats(const gb_potential_t *pot, int64_t *stats);
 /* Number of kernel launches this library has issued since it was loaded. */
 uint64_t gb_kernel_launches(void);
 /* FMA-chain microbenchmark on the current device: sustained FP64 (fp64=1)
