@@ -43,7 +43,10 @@ def _stale(target, deps):
 
 
 def build(force=False, verbose=False):
-    """Compile (if needed) and return the path of libatomistica_gb300.so."""
+    """Compile (if needed) and return the path of libatomistica_gb300.so.
+
+    Extra nvcc flags (e.g. -D tuning macros) may be given in the environment
+    variable GB_NVCC_FLAGS; changing them needs force=True."""
     os.makedirs(BUILD, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + \
         [os.path.join(ROOT, "include", "atomistica_gb300.h")]
@@ -55,7 +58,8 @@ def build(force=False, verbose=False):
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + os.environ.get("GB_NVCC_FLAGS", "").split() +
+                        ["-c", s, "-o", o])
 
     def run(cmd):
         if verbose:

@@ -527,6 +527,12 @@ int gb_potential_last_timing(const gb_potential_t *h, double *ms) {
   return 0;
 }
 
+int gb_potential_set_tile_atoms(gb_potential_t *h, int atoms) {
+  if (!h || atoms < 0) return GB_ERROR_ARGUMENT;
+  h->pot.tile_request = atoms;
+  return 0;
+}
+
 int gb_potential_last_stats(const gb_potential_t *h, int64_t *stats) {
   if (!h || !stats) return GB_ERROR_ARGUMENT;
   stats[0] = h->pot.last_bonds;

@@ -223,10 +223,15 @@ __device__ __forceinline__ void finalize_bond(const BopArgs &a, const SmemLayout
   }
 }
 
-// Mixed form: bonds whose estimated FP32 error exceeds this (eV/A) are
-// recomputed in FP64 (about 6 % of the bonds at the 2.33 g/cm^3, sigma =
-// 0.25 A workload).
-constexpr float kHotThreshold = 1.0e-6f;
+// Mixed form: bonds whose estimated FP32 force error exceeds this (eV/A) are
+// recomputed in float-float arithmetic.  At the 2.33 g/cm^3, sigma = 0.25 A
+// amorphous Si workload (1,048,576 atoms) 2e-6 sends 1.7 % of the bonds
+// there and gives a largest force error of 1.6e-6 eV/A against FP64 (1e-6:
+// 7.3 %, 1.1e-6 eV/A; 4e-6: 0.46 %, 2.3e-6 eV/A).
+#ifndef GB_MX_HOT_THRESHOLD
+#define GB_MX_HOT_THRESHOLD 2.0e-6f
+#endif
+constexpr float kHotThreshold = GB_MX_HOT_THRESHOLD;
 
 template <class Pot, class R, bool kWat, bool kPB>
 __global__ void __launch_bounds__(kBopThreads)
@@ -531,7 +536,7 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) {
       const MxParams mp = make_mx(pot.p, args.A);
-      kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
+      kern<<<ntiles, kMxThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
       note_launch();
     }
   } else {
@@ -631,11 +636,16 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
     const size_t worst = bop_smem_bytes<double>(aptc * maxz, aptc * maxz * maxz);
     return worst <= kSmemBudget;
   };
-  while (apt > 1 && !fits(apt)) apt >>= 1;
-  // Keep roughly one bond per thread.
-  while (apt > 1 && (int64_t)apt * std::max(1, (int)(nl.nentries / std::max(nat, 1))) >
-                        2 * kBopThreads)
-    apt >>= 1;
+  if (pot.tile_request > 0) {
+    apt = std::min(pot.tile_request, kMaxApt);
+    while (apt > 1 && !fits(apt)) apt >>= 1;
+  } else {
+    while (apt > 1 && !fits(apt)) apt >>= 1;
+    // Keep roughly one bond per thread.
+    while (apt > 1 && (int64_t)apt * std::max(1, (int)(nl.nentries / std::max(nat, 1))) >
+                          2 * kBopThreads)
+      apt >>= 1;
+  }
   if (!fits(apt)) {
     set_error("Internal neighbor list exhausted: an atom has " + std::to_string(maxz) +
               " neighbours within the cutoff, more than the bond-order kernel supports.");

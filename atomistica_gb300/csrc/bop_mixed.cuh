@@ -16,8 +16,18 @@
 // of per-bond energies and per-atom forces to FP64 and the tile reductions.
 // Run-to-run results are bitwise reproducible (no atomics in any sum).
 
+#ifndef GB_MX_THREADS
+#define GB_MX_THREADS 256
+#endif
+#ifndef GB_MX_MIN_BLOCKS
+#define GB_MX_MIN_BLOCKS 3
+#endif
+
 namespace gb {
 namespace {
+
+constexpr int kMxThreads = GB_MX_THREADS;  // threads per tile (mixed form)
+static_assert(kMaxApt <= 64, "the triplet-offset scan takes two atoms per lane");
 
 struct MxPair {
   ff cA, cR, Ac, Bc, xi, r1, fac;
@@ -379,16 +389,18 @@ __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, 
   }
 }
 
-// The same k loop in ff arithmetic for the hot bonds.
+// The same k loop in ff arithmetic for the hot bonds, over the slots
+// q = q0, q0 + dq, ... of bond lb's row (the partial sums of zeta, d zeta /
+// d r_j and the virial term are added up across the lanes afterwards).
 template <bool kWat>
 __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, int lb, int s,
-                                         int z, int eli, ff *trow, const ff *etab, ff &zeta,
-                                         ff dbj[3], ff wk[9]) {
+                                         int z, int eli, ff *trow, const ff *etab, int q0,
+                                         int dq, ff &zeta, ff dbj[3], ff wk[9]) {
   const int nbt = L.nbt, ntrip = L.ntrip;
   const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
   const ff rlij = L.r[lb], rinvj = L.rinv[lb];
   const ff h = mp.el[eli].h;
-  for (int q = 0; q < z; q++) {
+  for (int q = q0; q < z; q += dq) {
     const int lk = s + q;
     if (lk == lb) continue;
     const int mk = L.meta[lk];
@@ -426,6 +438,13 @@ __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, 
           wk[3 * c1 + c] = ff_add_fast(wk[3 * c1 + c], ff_mul(ff_mul(rnik[c1], rlik), dk));
     }
   }
+}
+
+__device__ __forceinline__ ff ff_shfl_xor(ff v, int o) {
+  ff r;
+  r.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+  r.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+  return r;
 }
 
 // Energy, radial force and G partial in ff; FP64 per-bond outputs.
@@ -480,7 +499,7 @@ template <int NC>
 __device__ inline void block_sum_ff(const ff (&v)[NC], double *out, ff *scratch) {
   static_assert(NC <= 16, "block_sum_ff: at most 16 components");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  constexpr int nw = kBopThreads / 32;
+  constexpr int nw = kMxThreads / 32;
   ff x[16];
 #pragma unroll
   for (int c = 0; c < 16; c++) x[c] = c < NC ? v[c] : ff_make(0.0f, 0.0f);
@@ -514,17 +533,17 @@ __device__ inline void block_sum_ff(const ff (&v)[NC], double *out, ff *scratch)
 }
 
 template <class Pot, bool kWat, bool kPB>
-__global__ void __launch_bounds__(kBopThreads)
+__global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
     bop_tile_mx(const BopArgs a, const Pot pot, const MxParams mp, const float4 *__restrict__ posff,
                 int max_nbt, int max_ntrip, int *status) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ ff red_scratch[(kBopThreads / 32) * 10];
+  __shared__ ff red_scratch[(kMxThreads / 32) * 10];
   __shared__ ff s_exp[256], s_sin[257], s_cos[257];
   __shared__ int s_nhot;
   const int tid = threadIdx.x;
-  for (int q = tid; q < 256; q += kBopThreads)
+  for (int q = tid; q < 256; q += kMxThreads)
     s_exp[q] = ff_make(kFfExp2Tab[2 * q], kFfExp2Tab[2 * q + 1]);
-  for (int q = tid; q < 257; q += kBopThreads) {
+  for (int q = tid; q < 257; q += kMxThreads) {
     s_sin[q] = ff_make(kFfSinTab[2 * q], kFfSinTab[2 * q + 1]);
     s_cos[q] = ff_make(kFfCosTab[2 * q], kFfCosTab[2 * q + 1]);
   }
@@ -539,17 +558,26 @@ __global__ void __launch_bounds__(kBopThreads)
     int *aseed = reinterpret_cast<int *>(sm);
     int *toff = aseed + kMaxApt + 1;
     int *el = aseed + 2 * kMaxApt + 2;
-    for (int q = tid; q <= na; q += kBopThreads) aseed[q] = a.seed[a0 + q] - b0;
-    for (int q = tid; q < na; q += kBopThreads) el[q] = a.el[a0 + q];
+    for (int q = tid; q <= na; q += kMxThreads) aseed[q] = a.seed[a0 + q] - b0;
+    for (int q = tid; q < na; q += kMxThreads) el[q] = a.el[a0 + q];
     __syncthreads();
-    if (tid == 0) {
-      int s = 0;
-      for (int q = 0; q < na; q++) {
-        toff[q] = s;
-        const int z = aseed[q + 1] - aseed[q];
-        s += z * z;
+    if (tid < 32) {
+      // triplet-slot offsets: exclusive scan of z^2 over the tile's atoms
+      // (na <= 64: two atoms per lane)
+      const int q0 = 2 * tid, q1 = 2 * tid + 1;
+      const int z0 = q0 < na ? aseed[q0 + 1] - aseed[q0] : 0;
+      const int z1 = q1 < na ? aseed[q1 + 1] - aseed[q1] : 0;
+      const int own = z0 * z0 + z1 * z1;
+      int inc = own;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (tid >= o) inc += v;
       }
-      toff[na] = s;
+      const int ex = inc - own;
+      if (q0 < na) toff[q0] = ex;
+      if (q1 < na) toff[q1] = ex + z0 * z0;
+      if (tid == 31) toff[na] = inc;
     }
     __syncthreads();
     ntrip = toff[na];
@@ -559,13 +587,13 @@ __global__ void __launch_bounds__(kBopThreads)
     return;
   }
   MxLayout L = carve_mx(sm, nbt, ntrip);
-  for (int q = tid; q < na; q += kBopThreads)
+  for (int q = tid; q < na; q += kMxThreads)
     for (int lb = L.aseed[q]; lb < L.aseed[q + 1]; lb++) L.meta[lb] = q;
   __syncthreads();
   const int nel = pot.nel();
 
   // ---- Phase 1: bond geometry in ff. ----
-  for (int lb = tid; lb < nbt; lb += kBopThreads) {
+  for (int lb = tid; lb < nbt; lb += kMxThreads) {
     const int ai = L.meta[lb];
     const int i = a0 + ai;
     const int b = b0 + lb;
@@ -641,7 +669,7 @@ __global__ void __launch_bounds__(kBopThreads)
   __syncthreads();
 
   // ---- Phase 2: FP32 three-body terms, ff scalar chain. ----
-  for (int lb = tid; lb < nbt; lb += kBopThreads) {
+  for (int lb = tid; lb < nbt; lb += kMxThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
     if (!(meta & kFlagIJ)) {
@@ -702,44 +730,66 @@ __global__ void __launch_bounds__(kBopThreads)
   }
   __syncthreads();
   // ---- Phase 2b: the hot bonds again, k loop and bond order in ff. ----
+  // kHotLanes lanes per hot bond share its k loop; the partial sums are added
+  // by a fixed xor tree, then the group's first lane finishes the bond.
   {
+    constexpr int kHotLanes = 8;
+    constexpr int kGroups = kMxThreads / kHotLanes;
     const int nhot = s_nhot;
     if (tid == 0 && nhot > 0) atomicAdd(&status[2], nhot);  // diagnostic count
-    for (int hq = tid; hq < nhot; hq += kBopThreads) {
-      const int lb = L.hot[hq];
-      const int b = b0 + lb;
-      const int meta = L.meta[lb];
-      const int ai = meta & 0xff;
-      const int t = (meta >> 8) & 0xf;
-      const int mf = (meta >> 16) & 3;
-      const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-      ff *trow = L.t + L.toff[ai] + p * z;
-      const int eli = L.el[ai];
-      const MxPair &pp = mp.pr[t];
-      const float hm = 0.5f * mf;
-      const ff r = L.r[lb];
-      const ff VA = ff_mulf(ff_mul(pp.Bc, ff_exp(ff_neg(ff_mul(pp.cA, r)), s_exp)), -hm);
-      const ff dVA = ff_neg(ff_mul(pp.cA, VA));
-      const ff VR = ff_mulf(ff_mul(pp.Ac, ff_exp(ff_neg(ff_mul(pp.cR, r)), s_exp)), hm);
-      const ff dVR = ff_neg(ff_mul(pp.cR, VR));
+    const int gl = tid & (kHotLanes - 1);
+    for (int base = 0; base < nhot; base += kGroups) {
+      const int hq = base + tid / kHotLanes;
+      const bool act = hq < nhot;
       ff zeta = ff_make(0.0f, 0.0f), wk[9];
       ff dbj[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
       if (kWat)
 #pragma unroll
         for (int c = 0; c < 9; c++) wk[c] = ff_make(0.0f, 0.0f);
-      kloop_ff<kWat>(mp, L, lb, s, z, eli, trow, s_exp, zeta, dbj, wk);
-      ff bij, P;
-      if (zeta.hi > 1.0e-30f) {
-        bo_ff(mp, eli, t, zeta, L.fc[lb], VA, s_exp, bij, P);
-      } else {
-        // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
-        double b64, P64;
-        pot.template bo<double>(eli, t, ff_to_double(zeta), ff_to_double(L.fc[lb]),
-                                ff_to_double(VA), b64, P64);
-        bij = ff_from_double(b64);
-        P = ff_from_double(P64);
+      int lb = 0;
+      if (act) {
+        lb = L.hot[hq];
+        const int ai = L.meta[lb] & 0xff;
+        const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
+        kloop_ff<kWat>(mp, L, lb, s, z, L.el[ai], L.t + L.toff[ai] + p * z, s_exp, gl,
+                       kHotLanes, zeta, dbj, wk);
       }
-      finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
+#pragma unroll
+      for (int o = 1; o < kHotLanes; o <<= 1) {
+        zeta = ff_add_fast(zeta, ff_shfl_xor(zeta, o));
+#pragma unroll
+        for (int c = 0; c < 3; c++) dbj[c] = ff_add_fast(dbj[c], ff_shfl_xor(dbj[c], o));
+        if (kWat)
+#pragma unroll
+          for (int c = 0; c < 9; c++) wk[c] = ff_add_fast(wk[c], ff_shfl_xor(wk[c], o));
+      }
+      if (act && gl == 0) {
+        const int b = b0 + lb;
+        const int meta = L.meta[lb];
+        const int ai = meta & 0xff;
+        const int t = (meta >> 8) & 0xf;
+        const int mf = (meta >> 16) & 3;
+        const int eli = L.el[ai];
+        const MxPair &pp = mp.pr[t];
+        const float hm = 0.5f * mf;
+        const ff r = L.r[lb];
+        const ff VA = ff_mulf(ff_mul(pp.Bc, ff_exp(ff_neg(ff_mul(pp.cA, r)), s_exp)), -hm);
+        const ff dVA = ff_neg(ff_mul(pp.cA, VA));
+        const ff VR = ff_mulf(ff_mul(pp.Ac, ff_exp(ff_neg(ff_mul(pp.cR, r)), s_exp)), hm);
+        const ff dVR = ff_neg(ff_mul(pp.cR, VR));
+        ff bij, P;
+        if (zeta.hi > 1.0e-30f) {
+          bo_ff(mp, eli, t, zeta, L.fc[lb], VA, s_exp, bij, P);
+        } else {
+          // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
+          double b64, P64;
+          pot.template bo<double>(eli, t, ff_to_double(zeta), ff_to_double(L.fc[lb]),
+                                  ff_to_double(VA), b64, P64);
+          bij = ff_from_double(b64);
+          P = ff_from_double(P64);
+        }
+        finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
+      }
     }
   }
   __syncthreads();
@@ -749,7 +799,7 @@ __global__ void __launch_bounds__(kBopThreads)
   ff wacc[9];
 #pragma unroll
   for (int c = 0; c < 9; c++) wacc[c] = ff_make(0.0f, 0.0f);
-  for (int lb = tid; lb < nbt; lb += kBopThreads) {
+  for (int lb = tid; lb < nbt; lb += kMxThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
     ff_acc(eacc, L.E[lb]);

@@ -85,6 +85,7 @@ struct Potential {
   cudaEvent_t kev[2] = {nullptr, nullptr};  // around the dominant force kernel
   double timing[4] = {0, 0, 0, 0};
   int tile_atoms = 32;
+  int tile_request = 0;     // atoms per tile requested (0: automatic)
   int last_status = 0;
   int last_hot = 0;         // bonds recomputed on the accurate path (mixed form)
   int64_t last_bonds = 0;   // directed bonds of the last bond-order call

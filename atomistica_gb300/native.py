@@ -278,6 +278,10 @@ class _Potential:
         self._L.gb_potential_last_timing(self._h, t)
         return tuple(t)
 
+    def set_tile_atoms(self, atoms):
+        """Atoms per bond-order tile (power of two <= 64; 0: automatic)."""
+        check(self._L.gb_potential_set_tile_atoms(self._h, int(atoms)), "set_tile_atoms")
+
     def last_stats(self):
         """(directed bonds, bonds recomputed on the accurate path of the mixed
         form, atoms per tile) of the last call."""

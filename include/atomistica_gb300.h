@@ -253,6 +253,10 @@ int gb_potential_last_timing(const gb_potential_t *pot, double *ms);
  * FP32 error sent them through the float-float recomputation, stats[2] atoms
  * per bond-order tile, stats[3] reserved (0).  stats must hold 4 int64_t. */
 int gb_potential_last_stats(const gb_potential_t *pot, int64_t *stats);
+/* Atoms per bond-order tile (a power of two <= 64, reduced until the worst
+ * tile fits in shared memory); 0 restores the automatic choice.  A tuning
+ * knob: results do not depend on it beyond FP rounding of the tile sums. */
+int gb_potential_set_tile_atoms(gb_potential_t *pot, int atoms);
 /* Number of kernel launches this library has issued since it was loaded. */
 uint64_t gb_kernel_launches(void);
 /* FMA-chain microbenchmark on the current device: sustained FP64 (fp64=1)
