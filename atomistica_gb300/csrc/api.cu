@@ -228,14 +228,30 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   }
   GB_CUDA(cudaEventRecord(pot.ev[0], s));
   GB_CHECK(update_element_map(pot, p));
+  const int nat = p.nat;
+  // Host forces (accumulated into): their upload runs on a second stream
+  // while the neighbour list is built.
+  Stage sf, sepa, swpa, sepb, sfpb, swpb;
+  const bool f_host = nat > 0 && !is_device_ptr(f);
+  if (f_host) {
+    if (!pot.aux) {
+      GB_CUDA(cudaStreamCreateWithFlags(&pot.aux, cudaStreamNonBlocking));
+      GB_CUDA(cudaEventCreateWithFlags(&pot.aux_ev, cudaEventDisableTiming));
+    }
+    GB_CUDA(cudaEventRecord(pot.aux_ev, s));  // the buffer's previous use is done
+    GB_CUDA(cudaStreamWaitEvent(pot.aux, pot.aux_ev, 0));
+    GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, pot.aux, sf));
+    GB_CUDA(cudaEventRecord(pot.aux_ev, pot.aux));
+  }
   nl.stream = s;
   GB_CHECK(neighbors_update(nl, p, s));
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
 
-  const int nat = p.nat;
   const size_t nb = (size_t)nl.nentries;
-  Stage sf, sepa, swpa, sepb, sfpb, swpb;
-  GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, s, sf));
+  if (f_host)
+    GB_CUDA(cudaStreamWaitEvent(s, pot.aux_ev, 0));
+  else
+    GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, s, sf));
   GB_CHECK(stage_in(epa, nat, pot.out_epa, s, sepa));
   GB_CHECK(stage_in(wpa, 9 * (size_t)nat, pot.out_wpa, s, swpa));
   GB_CHECK(stage_in(epb, nb, pot.out_epb, s, sepb));
@@ -403,6 +419,8 @@ void gb_potential_free(gb_potential_t *h) {
     if (pot.ev[q]) cudaEventDestroy(pot.ev[q]);
   for (int q = 0; q < 2; q++)
     if (pot.kev[q]) cudaEventDestroy(pot.kev[q]);
+  if (pot.aux_ev) cudaEventDestroy(pot.aux_ev);
+  if (pot.aux) cudaStreamDestroy(pot.aux);
   if (pot.own_stream && pot.stream) cudaStreamDestroy(pot.stream);
   delete h;
 }

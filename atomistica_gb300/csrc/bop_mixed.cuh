@@ -129,12 +129,6 @@ inline MxParams make_mx(const KumagaiDev &d, const double A[3][3]) {
   return m;
 }
 
-// Fast ff addition (no special care for catastrophic cancellation).
-__device__ __forceinline__ ff ff_add_fast(ff a, ff b) {
-  ff s = two_sum(a.hi, b.hi);
-  s.lo += a.lo + b.lo;
-  return quick_two_sum(s.hi, s.lo);
-}
 
 // acc += a b with an unnormalised accumulator (hi: running FP32 sum, lo:
 // its rounding errors and the low parts); ff_norm before use.
@@ -222,11 +216,11 @@ __device__ __forceinline__ void g_ff(const MxParams &mp, int eli, int ikpot, ff 
   const ff hc2 = ff_mul(hc, hc);
   if (mp.kind == 0) {
     const ff om = mp.pr[ikpot].om;
-    const ff inv = ff_rcp(ff_add_fast(E.d2, hc2));
+    const ff inv = ff_rcp(ff_add(E.d2, hc2));
     val = ff_mul(om, ff_addf(ff_mul(ff_mul(E.c2d2, hc2), inv), 1.0f));
     dval = ff_mulf(ff_mul(ff_mul(ff_mul(om, E.c2), hc), ff_mul(inv, inv)), -2.0f);
   } else {
-    const ff tmp = ff_div(hc, ff_add_fast(E.c3, hc2));
+    const ff tmp = ff_div(hc, ff_add(E.c3, hc2));
     const ff go = ff_mul(E.kc2, tmp);
     const ff ga1 = ff_mul(E.c4, ff_exp(ff_neg(ff_mul(E.c5, hc2)), etab));
     const ff v = ff_mul(go, ff_addf(ga1, 1.0f));
@@ -356,18 +350,25 @@ __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, 
     const ff rnik[3] = {L.rn[lk], L.rn[nbt + lk], L.rn[2 * nbt + lk]};
     const float rlik = L.r[lk].hi, rinvk = L.rinv[lk].hi, fcik = L.fc[lk].hi,
                 dfcik = L.dfc[lk].hi;
-    // cos theta in ff
-    ff csf = two_prod(rnik[0].hi, rnij[0].hi);
-    csf = ff_add_fast(csf, two_prod(rnik[1].hi, rnij[1].hi));
-    csf = ff_add_fast(csf, two_prod(rnik[2].hi, rnij[2].hi));
-    csf.lo += rnik[0].hi * rnij[0].lo + rnik[0].lo * rnij[0].hi + rnik[1].hi * rnij[1].lo +
-              rnik[1].lo * rnij[1].hi + rnik[2].hi * rnij[2].lo + rnik[2].lo * rnij[2].hi;
-    const ff hc = ff_sub(h, csf);
-    const float cs = csf.hi + csf.lo;
+    // cos theta = s2.hi + clo and h - cos theta, both to ~1e-14 absolute
+    const ff p0 = two_prod(rnik[0].hi, rnij[0].hi), p1 = two_prod(rnik[1].hi, rnij[1].hi),
+             p2 = two_prod(rnik[2].hi, rnij[2].hi);
+    const ff s1 = two_sum(p0.hi, p1.hi);
+    const ff s2 = two_sum(s1.hi, p2.hi);
+    float clo = ((s1.lo + s2.lo) + (p0.lo + p1.lo + p2.lo));
+    clo = fmaf(rnik[0].hi, rnij[0].lo, clo);
+    clo = fmaf(rnik[0].lo, rnij[0].hi, clo);
+    clo = fmaf(rnik[1].hi, rnij[1].lo, clo);
+    clo = fmaf(rnik[1].lo, rnij[1].hi, clo);
+    clo = fmaf(rnik[2].hi, rnij[2].lo, clo);
+    clo = fmaf(rnik[2].lo, rnij[2].hi, clo);
+    const float cs = s2.hi + clo;
+    const ff dh0 = two_sum(h.hi, -s2.hi);
+    const float hcf = dh0.hi + ((dh0.lo + h.lo) - clo);
     float hv, dh;
     h_f(mp.pr[ikpot], rlij - rlik, hv, dh);
     float gv, dg;
-    g_f(mp, eli, ikpot, hc.hi + hc.lo, gv, dg);
+    g_f(mp, eli, ikpot, hcf, gv, dg);
     const float dzfac = fcik * dg * hv;
     zeta += fcik * gv * hv;
     const float dzdrij = gv * fcik * dh;
@@ -422,20 +423,20 @@ __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, 
     g_ff(mp, eli, ikpot, ff_sub(h, cs), etab, gv, dg);
     const ff fh = ff_mul(fcik, hv);
     const ff dzfac = ff_mul(fh, dg);
-    zeta = ff_add_fast(zeta, ff_mul(fh, gv));
+    zeta = ff_add(zeta, ff_mul(fh, gv));
     const ff dzdrij = ff_mul(ff_mul(gv, fcik), dh);
     const ff dzdrik = ff_mul(gv, ff_sub(ff_mul(dfcik, hv), ff_mul(fcik, dh)));
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const ff dcj = ff_mul(ff_sub(rnik[c], ff_mul(cs, rnij[c])), rinvj);
       const ff dck = ff_mul(ff_sub(rnij[c], ff_mul(cs, rnik[c])), rinvk);
-      dbj[c] = ff_add_fast(dbj[c], ff_add_fast(ff_mul(dzdrij, rnij[c]), ff_mul(dzfac, dcj)));
-      const ff dk = ff_add_fast(ff_mul(dzdrik, rnik[c]), ff_mul(dzfac, dck));
+      dbj[c] = ff_add(dbj[c], ff_add(ff_mul(dzdrij, rnij[c]), ff_mul(dzfac, dcj)));
+      const ff dk = ff_add(ff_mul(dzdrik, rnik[c]), ff_mul(dzfac, dck));
       trow[c * ntrip + q] = dk;
       if (kWat)
 #pragma unroll
         for (int c1 = 0; c1 < 3; c1++)
-          wk[3 * c1 + c] = ff_add_fast(wk[3 * c1 + c], ff_mul(ff_mul(rnik[c1], rlik), dk));
+          wk[3 * c1 + c] = ff_add(wk[3 * c1 + c], ff_mul(ff_mul(rnik[c1], rlik), dk));
     }
   }
 }
@@ -457,12 +458,12 @@ __device__ __forceinline__ void finalize_mx(const BopArgs &a, const MxLayout &L,
   const ff v = ff_add(VR, ff_mul(bij, VA));    // VR + b VA
   const ff dv = ff_add(dVR, ff_mul(bij, dVA));  // dVR + b dVA
   const ff e_b = ff_mulf(ff_mul(fc, v), 0.5f);
-  const ff dff = ff_mulf(ff_add_fast(ff_mul(fc, dv), ff_mul(dfc, v)), 0.5f);
+  const ff dff = ff_mulf(ff_add(ff_mul(fc, dv), ff_mul(dfc, v)), 0.5f);
   ff dfr[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     dfr[c] = ff_mul(dff, L.rn[c * nbt + lb]);
-    L.G[c * nbt + lb] = ff_neg(ff_add_fast(dfr[c], ff_mul(P, dbj[c])));
+    L.G[c * nbt + lb] = ff_neg(ff_add(dfr[c], ff_mul(P, dbj[c])));
   }
   L.P[lb] = P;
   L.E[lb] = e_b;
@@ -482,53 +483,48 @@ __device__ __forceinline__ void finalize_mx(const BopArgs &a, const MxLayout &L,
     for (int c1 = 0; c1 < 3; c1++)
 #pragma unroll
       for (int c2 = 0; c2 < 3; c2++) {
-        const ff w = ff_add_fast(ff_mul(rij[c1], dfr[c2]),
-                                 ff_mul(P, ff_add_fast(ff_mul(rij[c1], dbj[c2]), wk[3 * c1 + c2])));
+        const ff w = ff_add(ff_mul(rij[c1], dfr[c2]),
+                                 ff_mul(P, ff_add(ff_mul(rij[c1], dbj[c2]), wk[3 * c1 + c2])));
         a.wbond[9 * (size_t)b + c1 + 3 * c2] = ff_to_double(w);
       }
   }
 }
 
-// Deterministic block sum of NC <= 16 ff values per thread.  Within a warp a
-// reduce-scatter butterfly (lanes l, l ^ m exchange half of their components
-// for m = 16, 8, 4, 2; then m = 1) leaves component
-// c = 8 b4 + 4 b3 + 2 b2 + b1 (b_k: bit k of the lane) summed over the warp in
-// lanes 2c and 2c+1; the warps' sums are then added in order and written as
-// FP64 by one thread per component.
-template <int NC>
-__device__ inline void block_sum_ff(const ff (&v)[NC], double *out, ff *scratch) {
-  static_assert(NC <= 16, "block_sum_ff: at most 16 components");
+// Deterministic tile sums: the energy in ff (warp xor tree), the nine virial
+// components in FP32 (a warp reduce-scatter butterfly: lanes l, l ^ m swap
+// half of their components for m = 16, 8, 4, 2, then m = 1, leaving
+// component c = 8 b4 + 4 b3 + 2 b2 + b1 (b_k: bit k of the lane) in lanes 2c,
+// 2c + 1), then the warps in order; written as FP64 (out[0] energy, out[1..9]
+// the virial).  The FP32 virial is accurate to ~1e-7 of sum |r (x) G|.
+__device__ inline void block_sum_tile(ff e, const float (&w)[9], double *out, ff *scratch) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int nw = kMxThreads / 32;
-  ff x[16];
 #pragma unroll
-  for (int c = 0; c < 16; c++) x[c] = c < NC ? v[c] : ff_make(0.0f, 0.0f);
+  for (int o = 16; o > 0; o >>= 1) e = ff_add(e, ff_shfl_xor(e, o));
+  float x[16];
+#pragma unroll
+  for (int c = 0; c < 16; c++) x[c] = c < 9 ? w[c] : 0.0f;
 #pragma unroll
   for (int lev = 0; lev < 4; lev++) {
     const int m = 16 >> lev, H = 8 >> lev;
     const bool up = (lane & m) != 0;
 #pragma unroll
     for (int q = 0; q < H; q++) {
-      const ff send = up ? x[q] : x[q + H];
-      const ff keep = up ? x[q + H] : x[q];
-      ff recv;
-      recv.hi = __shfl_xor_sync(0xffffffffu, send.hi, m);
-      recv.lo = __shfl_xor_sync(0xffffffffu, send.lo, m);
-      x[q] = ff_add_fast(keep, recv);
+      const float send = up ? x[q] : x[q + H];
+      const float keep = up ? x[q + H] : x[q];
+      x[q] = keep + __shfl_xor_sync(0xffffffffu, send, m);
     }
   }
-  ff recv;
-  recv.hi = __shfl_xor_sync(0xffffffffu, x[0].hi, 1);
-  recv.lo = __shfl_xor_sync(0xffffffffu, x[0].lo, 1);
-  const ff r = ff_add_fast(x[0], recv);
+  const float r = x[0] + __shfl_xor_sync(0xffffffffu, x[0], 1);
   const int c = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
                 ((lane >> 1) & 1);
-  if ((lane & 1) == 0 && c < NC) scratch[wid * NC + c] = r;
+  if ((lane & 1) == 0 && c < 9) scratch[wid * 10 + 1 + c] = ff_make(r, 0.0f);
+  if (lane == 0) scratch[wid * 10] = e;
   __syncthreads();
-  if (threadIdx.x < NC) {
-    ff sum = scratch[threadIdx.x];
-    for (int w = 1; w < nw; w++) sum = ff_add_fast(sum, scratch[w * NC + threadIdx.x]);
-    out[threadIdx.x] = ff_to_double(sum);
+  if (threadIdx.x < 10) {
+    double sum = 0.0;
+    for (int q = 0; q < nw; q++) sum += ff_to_double(scratch[q * 10 + threadIdx.x]);
+    out[threadIdx.x] = sum;
   }
 }
 
@@ -623,8 +619,8 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
         }
       }
       ff r2 = ff_mul(rij[0], rij[0]);
-      r2 = ff_add_fast(r2, ff_mul(rij[1], rij[1]));
-      r2 = ff_add_fast(r2, ff_mul(rij[2], rij[2]));
+      r2 = ff_add(r2, ff_mul(rij[1], rij[1]));
+      r2 = ff_add(r2, ff_mul(rij[2], rij[2]));
       const int t = pair_index(eli, elj, nel);
       meta |= t << 8;
       const float r2f = r2.hi + r2.lo;
@@ -756,12 +752,12 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       }
 #pragma unroll
       for (int o = 1; o < kHotLanes; o <<= 1) {
-        zeta = ff_add_fast(zeta, ff_shfl_xor(zeta, o));
+        zeta = ff_add(zeta, ff_shfl_xor(zeta, o));
 #pragma unroll
-        for (int c = 0; c < 3; c++) dbj[c] = ff_add_fast(dbj[c], ff_shfl_xor(dbj[c], o));
+        for (int c = 0; c < 3; c++) dbj[c] = ff_add(dbj[c], ff_shfl_xor(dbj[c], o));
         if (kWat)
 #pragma unroll
-          for (int c = 0; c < 9; c++) wk[c] = ff_add_fast(wk[c], ff_shfl_xor(wk[c], o));
+          for (int c = 0; c < 9; c++) wk[c] = ff_add(wk[c], ff_shfl_xor(wk[c], o));
       }
       if (act && gl == 0) {
         const int b = b0 + lb;
@@ -794,11 +790,11 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
   }
   __syncthreads();
 
-  // ---- Phase 3: k-role forces and the virial in ff. ----
+  // ---- Phase 3: k-role forces (ff) and the virial (FP32 per thread). ----
   ff eacc = ff_make(0.0f, 0.0f);
-  ff wacc[9];
+  float wacc[9];
 #pragma unroll
-  for (int c = 0; c < 9; c++) wacc[c] = ff_make(0.0f, 0.0f);
+  for (int c = 0; c < 9; c++) wacc[c] = 0.0f;
   for (int lb = tid; lb < nbt; lb += kMxThreads) {
     const int b = b0 + lb;
     const int meta = L.meta[lb];
@@ -819,25 +815,22 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) G[c] = ff_norm(G[c]);
-      const ff r = L.r[lb];
-      ff mrb[3];
+      const float r = L.r[lb].hi;
+      float rb[3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) mrb[c] = ff_neg(ff_mul(r, L.rn[c * nbt + lb]));
+      for (int c = 0; c < 3; c++) rb[c] = r * L.rn[c * nbt + lb].hi;
 #pragma unroll
       for (int c1 = 0; c1 < 3; c1++)
 #pragma unroll
-        for (int c2 = 0; c2 < 3; c2++) ff_acc_mul(wacc[c1 + 3 * c2], mrb[c1], G[c2]);
+        for (int c2 = 0; c2 < 3; c2++)
+          wacc[c1 + 3 * c2] = fmaf(-rb[c1], G[c2].hi + G[c2].lo, wacc[c1 + 3 * c2]);
     }
     float2 *Gout = reinterpret_cast<float2 *>(a.G) + 3 * (size_t)b;
     Gout[0] = make_float2(G[0].hi, G[0].lo);
     Gout[1] = make_float2(G[1].hi, G[1].lo);
     Gout[2] = make_float2(G[2].hi, G[2].lo);
   }
-  ff part_v[10];
-  part_v[0] = ff_norm(eacc);
-#pragma unroll
-  for (int c = 0; c < 9; c++) part_v[1 + c] = ff_norm(wacc[c]);
-  block_sum_ff<10>(part_v, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
+  block_sum_tile(ff_norm(eacc), wacc, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
 }
 
 // Gather of the ff bond forces: F_a = sum_b (G[rev b] - G[b]) in ff.

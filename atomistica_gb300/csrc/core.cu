@@ -260,6 +260,8 @@ struct BinParams {
   double rec[3][3];
   float recf[3][3];  // rec rounded to float (cell prefilter)
   double A[3][3];
+  float Af[3][3];  // A rounded to float, and max |A_ak|
+  float Amax;
   int n[3];
   int pbc[3];
   int dx, dy, dz;
@@ -518,14 +520,8 @@ __global__ void __launch_bounds__(128)
   const float u = 5.9604645e-8f;
   const float X = __int_as_float(status[3]);
   const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
-  float Af[3][3], Amax = 0.0f;
-#pragma unroll
-  for (int a = 0; a < 3; a++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      Af[a][k] = (float)bp.A[a][k];
-      Amax = fmaxf(Amax, fabsf(Af[a][k]));
-    }
+  const float eA = 8.0f * u * bp.Amax;
+  const int kZeroWrap = pack_shift(0, 0, 0);
   int cur = kMode == kPairsFill ? seed[i] : 0;
   int cnt = 0;
   bool have_ri = false;
@@ -547,23 +543,43 @@ __global__ void __launch_bounds__(128)
         const int run = min(bp.dz - z + 1, bp.n[2] - cz);
         const int js = cell_start[row + cz], je = cell_start[row + cz + run];
         z += run;
+        // image offset A s1 of this run (atoms j with zero wrap use it as is)
+        const bool s1zero = (sx | sy | sz) == 0;
+        float ox = 0.0f, oy = 0.0f, oz = 0.0f, Erun = Ebase;
+        if (!s1zero) {
+          const float fx = (float)sx, fy = (float)sy, fz = (float)sz;
+          ox = bp.Af[0][0] * fx + bp.Af[0][1] * fy + bp.Af[0][2] * fz;
+          oy = bp.Af[1][0] * fx + bp.Af[1][1] * fy + bp.Af[1][2] * fz;
+          oz = bp.Af[2][0] * fx + bp.Af[2][1] * fy + bp.Af[2][2] * fz;
+          Erun += eA * (fabsf(fx) + fabsf(fy) + fabsf(fz));
+        }
+        const int packed1 = pack_shift(sx, sy, sz);
         for (int jq = js; jq < je; jq++) {
           const float4 pj = spos[jq];
           const int j = __float_as_int(pj.w);
-          int w0, w1, w2;
-          unpack_shift(swrap[jq], w0, w1, w2);
-          const int s2x = sx + w0, s2y = sy + w1, s2z = sz + w2;
-          const bool zero_shift = (s2x | s2y | s2z) == 0;
-          if (j == i && zero_shift) continue;
+          const int wj = swrap[jq];
+          int s2x = sx, s2y = sy, s2z = sz;
+          bool zero_shift = s1zero;
           float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-          float E = Ebase;
-          if (!zero_shift) {
+          float E = Erun;
+          if (wj == kZeroWrap) {
+            dx += ox;
+            dy += oy;
+            dz += oz;
+          } else {
+            int w0, w1, w2;
+            unpack_shift(wj, w0, w1, w2);
+            s2x += w0;
+            s2y += w1;
+            s2z += w2;
+            zero_shift = (s2x | s2y | s2z) == 0;
             const float fx = (float)s2x, fy = (float)s2y, fz = (float)s2z;
-            dx += Af[0][0] * fx + Af[0][1] * fy + Af[0][2] * fz;
-            dy += Af[1][0] * fx + Af[1][1] * fy + Af[1][2] * fz;
-            dz += Af[2][0] * fx + Af[2][1] * fy + Af[2][2] * fz;
-            E += 8.0f * u * Amax * (fabsf(fx) + fabsf(fy) + fabsf(fz));
+            dx += bp.Af[0][0] * fx + bp.Af[0][1] * fy + bp.Af[0][2] * fz;
+            dy += bp.Af[1][0] * fx + bp.Af[1][1] * fy + bp.Af[1][2] * fz;
+            dz += bp.Af[2][0] * fx + bp.Af[2][1] * fy + bp.Af[2][2] * fz;
+            E = Ebase + eA * (fabsf(fx) + fabsf(fy) + fabsf(fz));
           }
+          if (j == i && zero_shift) continue;
           const float d2f = dx * dx + dy * dy + dz * dz;
           const float B = 2.0f * E * (1.735f * (d2f + 1.0f) + 9.0f * E) + 12.0f * u * d2f;
           bool accept;
@@ -579,13 +595,14 @@ __global__ void __launch_bounds__(128)
             accept = exact_pair_test(bp, ri, pos4[j], s2x, s2y, s2z);
           }
           if (accept) {
+            const int packed = wj == kZeroWrap ? packed1 : pack_shift(s2x, s2y, s2z);
             if (kMode == kPairsFill) {
               nbr[cur] = j;
-              shift[cur] = pack_shift(s2x, s2y, s2z);
+              shift[cur] = packed;
               cur++;
             } else {
               if (kMode == kPairsCountStage && cnt < cap)
-                stage[(size_t)i * cap + cnt] = make_int2(j, pack_shift(s2x, s2y, s2z));
+                stage[(size_t)i * cap + cnt] = make_int2(j, packed);
               cnt++;
               if (s2x > kMaxShift || s2x < -kMaxShift || s2y > kMaxShift ||
                   s2y < -kMaxShift || s2z > kMaxShift || s2z < -kMaxShift)
@@ -726,8 +743,13 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   }
   BinParams bp;
   std::memcpy(bp.rec, nl.rec, sizeof(bp.rec));
+  bp.Amax = 0.0f;
   for (int a = 0; a < 3; a++)
-    for (int k = 0; k < 3; k++) bp.recf[a][k] = (float)nl.rec[a][k];
+    for (int k = 0; k < 3; k++) {
+      bp.recf[a][k] = (float)nl.rec[a][k];
+      bp.Af[a][k] = (float)p.A[a][k];
+      bp.Amax = std::max(bp.Amax, std::fabs(bp.Af[a][k]));
+    }
   std::memcpy(bp.A, p.A, sizeof(bp.A));
   for (int k = 0; k < 3; k++) {
     bp.n[k] = nl.n_cells[k];

@@ -66,8 +66,17 @@ FF_HD ff ff_from_double(double d) {
 }
 FF_HD double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 FF_HD ff ff_neg(ff a) { return ff_make(-a.hi, -a.lo); }
-// Accurate addition (handles cancellation): two_sum of both parts.
+// Addition with an absolute error of a few u^2 (|a| + |b|) (u = 2^-24): the
+// leading parts exactly by two_sum, the low parts in FP32.  Under heavy
+// cancellation the relative error of the result grows, its absolute error
+// does not; every use in the kernels needs only the absolute bound.
 FF_HD ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+// Addition with a relative error of a few u^2 even under cancellation.
+FF_HD ff ff_add_accurate(ff a, ff b) {
   ff s = two_sum(a.hi, b.hi);
   const ff t = two_sum(a.lo, b.lo);
   s.lo += t.hi;
@@ -138,8 +147,8 @@ FF_HD ff ff_exp(ff t, const ff *tab) {
                      r * r * (0.5f + r * (0.16666667f + r * (0.041666668f + r * 0.0083333338f)));
   const ff eps = two_sum(r, tail);  // e^rho - 1
   const ff T = tab[k & 255];
-  const ff Te = ff_mul(T, eps);  // |T eps| < 0.006 T: no cancellation below
-  ff v = two_sum(T.hi, Te.hi);
+  const ff Te = ff_mul(T, eps);  // |T eps| < 0.006 T: fast two-sum below
+  ff v = quick_two_sum(T.hi, Te.hi);
   v.lo += T.lo + Te.lo;
   v = quick_two_sum(v.hi, v.lo);
   const int e = k >> 8;

@@ -83,6 +83,8 @@ struct Potential {
   HostBuf hred;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t kev[2] = {nullptr, nullptr};  // around the dominant force kernel
+  cudaStream_t aux = nullptr;   // host->device force upload, overlapped with the list build
+  cudaEvent_t aux_ev = nullptr;
   double timing[4] = {0, 0, 0, 0};
   int tile_atoms = 32;
   int tile_request = 0;     // atoms per tile requested (0: automatic)

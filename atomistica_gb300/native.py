@@ -103,11 +103,13 @@ class Particles:
         self.set_positions(self.coordinates)
 
     def set_positions(self, r):
-        """Positions (nat,3): numpy array or torch CUDA tensor (float64)."""
+        """Positions (nat,3): numpy array or torch CUDA tensor (float64).  A
+        C-contiguous float64 numpy array becomes ``coordinates`` itself (no
+        copy), as the reference's coordinates array is the particles'
+        storage; later writes to it take effect on I_changed_positions()."""
         ptr, keep = _ptr(r, np.float64)
         if not _is_torch(r):
-            if keep is not self.coordinates:
-                self.coordinates = np.array(keep)
+            self.coordinates = keep
         check(self._L.gb_particles_set_positions(self._h, ptr), "particles_set_positions")
 
     def update_elements(self):
