@@ -244,6 +244,7 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
     GB_CUDA(cudaEventRecord(pot.aux_ev, pot.aux));
   }
   nl.stream = s;
+  if (pot.precision == GB_PRECISION_MIXED) nl.want_posff = true;
   GB_CHECK(neighbors_update(nl, p, s));
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
 

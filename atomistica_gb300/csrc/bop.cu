@@ -608,7 +608,7 @@ int reduce_partials(const double *part, int nrows, int nc, double *red, double *
     note_launch();
   } else {
     const int nb = (nrows + kRedRowsPerBlock - 1) / kRedRowsPerBlock;
-    reduce_rows_kernel<<<nb, 256, 0, s>>>(part, nrows, kRedRowsPerBlock, stage);
+    reduce_rows_kernel<<<nb, kRedRowsPerBlock, 0, s>>>(part, nrows, kRedRowsPerBlock, stage);
     note_launch();
     reduce_rows_kernel<<<1, 1024, 0, s>>>(stage, nb, nb, red);
     note_launch();
@@ -627,7 +627,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
     GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
     return 0;
   }
-  GB_CHECK(neighbors_build_reverse(nl, p, s));
+  GB_CHECK(neighbors_build_reverse(nl, p, s, false));  // checked after the plan read-back
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
   // Atoms per tile: largest power of two <= kMaxApt whose worst tile fits.
   const int maxz = std::max(nl.maxz, 1);
@@ -667,6 +667,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   int *hplan = pot.hred.as<int>();
   GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
+  GB_CHECK(neighbors_check_reverse(nl, nullptr));
   const int max_nbt = hplan[0], max_ntrip = hplan[1];
 
   BopArgs args;
@@ -686,13 +687,13 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   args.tile_part = pot.tile_part.as<double>();
   int *status = o.status;
   int rc;
-  const float4 *posff = nullptr;
-  if (mixed) {
-    GB_CHECK(pot.posff.ensure(sizeof(float4) * 2 * (size_t)nat));
-    bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, args.pos, pot.posff.as<float4>());
+  if (mixed && !nl.posff_valid) {
+    GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * (size_t)nat));
+    bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, args.pos, nl.posff.as<float4>());
     note_launch();
-    posff = pot.posff.as<float4>();
+    nl.posff_valid = true;
   }
+  const float4 *posff = mixed ? nl.posff.as<float4>() : nullptr;
   GB_CUDA(cudaEventRecord(pot.kev[0], s));
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};

@@ -315,7 +315,8 @@ __device__ __forceinline__ int pack_wrap(int q0, int q1, int q2) {
 }
 
 __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams bp,
-                                Pos4 *__restrict__ pos4, int *__restrict__ atom_cell,
+                                Pos4 *__restrict__ pos4, float4 *__restrict__ posff,
+                                int *__restrict__ atom_cell,
                                 int *__restrict__ atom_wrap, int *__restrict__ cell_count,
                                 int *__restrict__ status) {
   // (blockDim.x is a multiple of 32: every lane reaches the warp reduction)
@@ -339,6 +340,12 @@ __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams
   }
   if (!in) return;
   pos4[i] = Pos4{x, y, z, 0.0};
+  if (posff) {
+    // float-float copy (hi, lo) for the mixed-precision kernels
+    posff[2 * i] = make_float4(xf, yf, zf, 0.0f);
+    posff[2 * i + 1] = make_float4((float)(x - (double)xf), (float)(y - (double)yf),
+                                   (float)(z - (double)zf), 0.0f);
+  }
   if (!finite) {
     atomicOr(&status[1], 1);  // non-finite position
     atom_cell[i] = 0;
@@ -627,30 +634,47 @@ __global__ void nl_compact(int nat, int cap, const int *__restrict__ seed,
   if (i >= nat) return;
   const int s = seed[i], n = seed[i + 1] - s;
   const int2 *src = stage + (size_t)i * cap;
-  for (int k = 0; k < n; k++) {
-    const int2 v = src[k];
-    nbr[s + k] = v.x;
-    shift[s + k] = v.y;
+  // four independent loads in flight per thread
+  for (int k = 0; k < n; k += 4) {
+    int2 v[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (k + q < n) v[q] = src[k + q];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (k + q < n) {
+        nbr[s + k + q] = v[q].x;
+        shift[s + k + q] = v[q].y;
+      }
   }
 }
 
 // rev[b] = entry (j -> i, -s) of the entry b = (i -> j, s).
+// One thread per atom i: each entry b = (i -> j, s) searches atom j's entries
+// for (j -> i, -s), four candidates per step.
 __global__ void nl_reverse(int nat, const int *__restrict__ seed, const int *__restrict__ nbr,
                            const int *__restrict__ shift, int *__restrict__ rev,
                            int *__restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nat) return;
-  for (int b = seed[i]; b < seed[i + 1]; b++) {
+  const int b1 = seed[i + 1];
+  for (int b = seed[i]; b < b1; b++) {
     const int j = nbr[b];
     int s0, s1, s2;
     unpack_shift(shift[b], s0, s1, s2);
     const int want = pack_shift(-s0, -s1, -s2);
+    const int c0 = seed[j], c1 = seed[j + 1];
     int found = -1;
-    for (int c = seed[j]; c < seed[j + 1]; c++) {
-      if (nbr[c] == i && shift[c] == want) {
-        found = c;
-        break;
+    for (int c = c0; c < c1 && found < 0; c += 4) {
+      int nj[4], sj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        nj[q] = c + q < c1 ? nbr[c + q] : -1;
+        sj[q] = c + q < c1 ? shift[c + q] : 0;
       }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (found < 0 && nj[q] == i && sj[q] == want) found = c + q;
     }
     if (found < 0) atomicOr(&status[1], 4);
     rev[b] = found;
@@ -730,6 +754,7 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   }
   nl.valid = false;
   nl.rev_valid = false;
+  nl.rev_pending = false;
   const int nat = p.nat;
   binning_init(nl, p, cutoff);
   const int ncells = nl.n_cells[0] * nl.n_cells[1] * nl.n_cells[2];
@@ -764,6 +789,8 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   bp.cutoff_sq_hi = (float)(bp.cutoff_sq * (1.0 + 1e-6));
 
   GB_CHECK(nl.pos4.ensure(sizeof(Pos4) * std::max(nat, 1)));
+  if (nl.want_posff) GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * std::max(nat, 1)));
+  nl.posff_valid = nl.want_posff;
   GB_CHECK(nl.atom_cell.ensure(sizeof(int) * std::max(nat, 1)));
   GB_CHECK(nl.atom_wrap.ensure(sizeof(int) * std::max(nat, 1)));
   GB_CHECK(nl.cell_count.ensure(sizeof(int) * (ncells + 1)));
@@ -783,6 +810,7 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   const int nb = (nat + T - 1) / T;
   if (nat > 0) {
     nl_assign_cells<<<nb, T, 0, stream>>>(nat, p.r.as<double>(), bp, nl.pos4.as<Pos4>(),
+                                          nl.want_posff ? nl.posff.as<float4>() : nullptr,
                                           nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
                                           nl.cell_count.as<int>(), status);
     note_launch();
@@ -880,8 +908,8 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   return 0;
 }
 
-int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream) {
-  if (nl.rev_valid) return 0;
+int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream, bool sync) {
+  if (nl.rev_valid || nl.rev_pending) return sync ? neighbors_check_reverse(nl, stream) : 0;
   const int nat = p.nat;
   GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(nl.nentries, 1)));
   int *status = nl.stats.as<int>();
@@ -894,8 +922,15 @@ int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stre
   }
   int *hs = nl.hstats.as<int>();
   GB_CUDA(cudaMemcpyAsync(hs + 1, status + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
-  GB_CUDA(cudaStreamSynchronize(stream));
-  if (hs[1] & 4) {
+  nl.rev_pending = true;
+  return sync ? neighbors_check_reverse(nl, stream) : 0;
+}
+
+int neighbors_check_reverse(Neighbors &nl, cudaStream_t stream) {
+  if (!nl.rev_pending) return 0;
+  if (stream) GB_CUDA(cudaStreamSynchronize(stream));
+  nl.rev_pending = false;
+  if (nl.hstats.as<int>()[1] & 4) {
     set_error("Internal error: neighbour list is not symmetric.");
     return GB_ERROR_UNSPECIFIED;
   }

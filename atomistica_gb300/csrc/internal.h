@@ -130,6 +130,9 @@ struct Neighbors {
   int dx = 0, dy = 0, dz = 0;
 
   DevBuf pos4;        // Pos4[nat]: positions padded for one-sector gathers
+  DevBuf posff;       // float4[2 nat]: positions as float-float (hi, lo)
+  bool want_posff = false;  // written by the build (a mixed-form potential uses the list)
+  bool posff_valid = false;
   DevBuf atom_cell;   // int[nat]: wrapped linear cell index
   DevBuf atom_wrap;   // int[nat]: packed wrap counts q (pbc dims)
   DevBuf cell_count;  // int[ncells+1]
@@ -148,6 +151,7 @@ struct Neighbors {
   DevBuf stats;       // device-side status words
   HostBuf hstats;
   bool rev_valid = false;
+  bool rev_pending = false;  // reverse index built, symmetry flag not yet read
   int64_t nentries = 0;
   int maxz = 0;
   cudaStream_t stream = nullptr;
@@ -156,7 +160,12 @@ struct Neighbors {
 // Builds/refreshes the list for p if positions or cell changed
 // (neighbors_update, :430-456).
 int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream);
-int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream);
+// Reverse-entry index of the list.  With sync = false the symmetry check is
+// deferred: call neighbors_check_reverse (stream = nullptr once the caller
+// has synchronised the stream itself) before rev is read.
+int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream,
+                            bool sync = true);
+int neighbors_check_reverse(Neighbors &nl, cudaStream_t stream);
 
 // Device-wide exclusive scan of int32 (n+1 outputs, out[n] = total).
 int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t stream);

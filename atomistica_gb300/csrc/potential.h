@@ -77,7 +77,6 @@ struct Potential {
   // Scratch.
   DevBuf bond_G, bond_e, bond_w, bond_fr, tile_part, red;
   DevBuf atom_dF;
-  DevBuf posff;      // ff positions (mixed form)
   DevBuf red_stage;  // first-stage sums of the tile partials
   DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
   HostBuf hred;
@@ -105,7 +104,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 // Deterministic fixed-order sum of tile partials: red[c] = sum_t part[t*nc+c].
 // Deterministic sum of nrows rows of nc (= 10) doubles into red[0..nc); with a
 // stage buffer of reduce_stage_bytes(nrows) bytes large inputs use two passes.
-constexpr int kRedRowsPerBlock = 2048;
+constexpr int kRedRowsPerBlock = 256;
 size_t reduce_stage_bytes(int nrows);
 int reduce_partials(const double *part, int nrows, int nc, double *red, double *stage,
                     cudaStream_t s);
