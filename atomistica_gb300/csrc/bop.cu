@@ -204,7 +204,7 @@ __device__ __forceinline__ void finalize_bond(const BopArgs &a, const SmemLayout
   }
   L.P[lb] = P;
   L.E[lb] = e_b;
-  a.ebond[b] = e_b;
+  if (a.ebond) a.ebond[b] = e_b;
   if (kPB) {
     a.frbond[3 * (size_t)b] = dfr[0];
     a.frbond[3 * (size_t)b + 1] = dfr[1];
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(kBopThreads)
       L.G[nbt + lb] = 0.0;
       L.G[2 * nbt + lb] = 0.0;
       L.E[lb] = 0.0;
-      a.ebond[b] = 0.0;
+      if (a.ebond) a.ebond[b] = 0.0;
       if (kPB) {
         a.frbond[3 * (size_t)b] = 0.0;
         a.frbond[3 * (size_t)b + 1] = 0.0;
@@ -681,7 +681,8 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   args.mask = o.mask;
   std::memcpy(args.A, p.A, sizeof(args.A));
   args.G = pot.bond_G.as<double>();
-  args.ebond = pot.bond_e.as<double>();
+  // per-bond energies only when per-atom or per-bond energies are requested
+  args.ebond = (o.epot_per_at || o.epot_per_bond) ? pot.bond_e.as<double>() : nullptr;
   args.wbond = want_wat ? pot.bond_w.as<double>() : nullptr;
   args.frbond = want_pb ? pot.bond_fr.as<double>() : nullptr;
   args.tile_part = pot.tile_part.as<double>();

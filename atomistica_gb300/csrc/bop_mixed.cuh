@@ -467,7 +467,7 @@ __device__ __forceinline__ void finalize_mx(const BopArgs &a, const MxLayout &L,
   }
   L.P[lb] = P;
   L.E[lb] = e_b;
-  a.ebond[b] = (double)e_b.hi + (double)e_b.lo;
+  if (a.ebond) a.ebond[b] = (double)e_b.hi + (double)e_b.lo;
   if (kPB) {
     a.frbond[3 * (size_t)b] = ff_to_double(dfr[0]);
     a.frbond[3 * (size_t)b + 1] = ff_to_double(dfr[1]);
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       L.G[lb] = ff_make(0.0f, 0.0f);
       L.G[nbt + lb] = ff_make(0.0f, 0.0f);
       L.G[2 * nbt + lb] = ff_make(0.0f, 0.0f);
-      a.ebond[b] = 0.0;
+      if (a.ebond) a.ebond[b] = 0.0;
       if (kPB) {
         a.frbond[3 * (size_t)b] = 0.0;
         a.frbond[3 * (size_t)b + 1] = 0.0;

@@ -126,16 +126,31 @@ FF_HD void ff_sqrt_rsqrt(ff x, ff &r, ff &rinv) {
 }
 
 // ---------------------------------------------------------------------------
-// exp: e^t = 2^(k/256) e^rho, k = floor(256 t / ln 2), 0 <= rho < ln 2/256.
+// exp: e^t = 2^(k/256) e^rho, k = round(256 t / ln 2), |rho| <= ln 2/512.
 // tab[j] = 2^(j/256) as ff.  Relative error ~1e-12 for |t| < 80.
 // ---------------------------------------------------------------------------
 constexpr float kFfInvC = 369.32993f;               // 256 / ln 2 (only selects k)
 constexpr float kFfC_hi = 0.0027076062f;            // ln 2 / 256 = hi + mid (+ 3e-19)
 constexpr float kFfC_mid = -7.4400555e-12f;
 
+// k = round(t / C) without conversion instructions: adding 1.5 * 2^23 leaves
+// the rounded integer in the low mantissa bits (|t| < 1e4).
+FF_HD int __float_as_int_hd(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_int(f);
+#else
+  int i;
+  std::memcpy(&i, &f, sizeof i);
+  return i;
+#endif
+}
+constexpr float kFfRoundMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kFfRoundMagicBits = 0x4B400000;
+
 FF_HD ff ff_exp(ff t, const ff *tab) {
-  const float kf = floorf(t.hi * kFfInvC);
-  const int k = (int)kf;
+  const float rv = fmaf(t.hi, kFfInvC, kFfRoundMagic);
+  const float kf = rv - kFfRoundMagic;
+  const int k = __float_as_int_hd(rv) - kFfRoundMagicBits;
   // rho = t - kf * C, C = C_hi + C_mid: kf * C_hi exact via two_prod, the
   // leading difference exact via two_sum, then the small parts; the tail
   // polynomial takes rho.lo to first order.
@@ -189,8 +204,9 @@ constexpr float kFfPiOver256_lo = -3.4149522e-10f;
 constexpr float kFf256OverPi = 81.48733f;
 
 FF_HD void ff_sincos(ff x, const ff *stab_sin, const ff *stab_cos, ff &sx, ff &cx) {
-  const float jf = rintf(x.hi * kFf256OverPi);
-  const int j = (int)jf;
+  const float rv = fmaf(x.hi, kFf256OverPi, kFfRoundMagic);
+  const float jf = rv - kFfRoundMagic;
+  const int j = __float_as_int_hd(rv) - kFfRoundMagicBits;
   const ff jc = two_prod(jf, kFfPiOver256_hi);
   ff d = ff_sub(x, jc);
   d = ff_addf(d, -jf * kFfPiOver256_lo);
