@@ -523,9 +523,23 @@ __global__ void reduce_rows_kernel(const double *__restrict__ part, int nrows, i
   }
 }
 
+// Resident CTAs of a kernel on this device (for the persistent grid).
+template <class K>
+int resident_ctas(K kern, int threads, size_t smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess)
+    return 0;
+  return sms * std::max(per_sm, 1);
+}
+
+// Launches the tile kernel; *rows = number of energy/virial partial rows
+// written to args.tile_part (one per tile, or one per CTA of the persistent
+// mixed kernel).
 template <class Pot, class R, bool kWat, bool kPB>
 int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int ntiles, int max_nbt,
-                int max_ntrip, int *status, cudaStream_t s) {
+                int max_ntrip, int *status, cudaStream_t s, int *rows) {
   constexpr bool kMix = std::is_same<R, float>::value;
   const size_t smem =
       kMix ? bop_smem_bytes_mx(max_nbt, max_ntrip) : bop_smem_bytes<R>(max_nbt, max_ntrip);
@@ -535,9 +549,12 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
     if (smem > 48 * 1024)
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) {
+      const int resident = resident_ctas(kern, kMxThreads, smem);
+      const int grid = resident > 0 ? std::min(ntiles, resident) : ntiles;
       const MxParams mp = make_mx(pot.p, args.A);
-      kern<<<ntiles, kMxThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
+      kern<<<grid, kMxThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
       note_launch();
+      *rows = grid;
     }
   } else {
     auto kern = bop_tile<Pot, double, kWat, kPB>;
@@ -546,6 +563,7 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
     if (e == cudaSuccess) {
       kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, max_nbt, max_ntrip, status);
       note_launch();
+      *rows = ntiles;
     }
   }
   if (e != cudaSuccess) {
@@ -559,14 +577,19 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
 // R = double: FP64 drop-in; R = float: mixed form (posff: ff positions).
 template <class Pot, class R>
 int dispatch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int ntiles,
-                  int max_nbt, int max_ntrip, int *status, bool wat, bool pb, cudaStream_t s) {
+                  int max_nbt, int max_ntrip, int *status, bool wat, bool pb, cudaStream_t s,
+                  int *rows) {
   if (wat && pb)
-    return launch_tile<Pot, R, true, true>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+    return launch_tile<Pot, R, true, true>(args, pot, posff, ntiles, max_nbt, max_ntrip, status,
+                                           s, rows);
   if (wat)
-    return launch_tile<Pot, R, true, false>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+    return launch_tile<Pot, R, true, false>(args, pot, posff, ntiles, max_nbt, max_ntrip, status,
+                                            s, rows);
   if (pb)
-    return launch_tile<Pot, R, false, true>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
-  return launch_tile<Pot, R, false, false>(args, pot, posff, ntiles, max_nbt, max_ntrip, status, s);
+    return launch_tile<Pot, R, false, true>(args, pot, posff, ntiles, max_nbt, max_ntrip, status,
+                                            s, rows);
+  return launch_tile<Pot, R, false, false>(args, pot, posff, ntiles, max_nbt, max_ntrip, status,
+                                           s, rows);
 }
 
 // Per-atom gather of the bond forces (FP64 G, or ff G for the mixed form).
@@ -687,7 +710,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   args.frbond = want_pb ? pot.bond_fr.as<double>() : nullptr;
   args.tile_part = pot.tile_part.as<double>();
   int *status = o.status;
-  int rc;
+  int rc, rows = ntiles;
   if (mixed && !nl.posff_valid) {
     GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * (size_t)nat));
     bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, args.pos, nl.posff.as<float4>());
@@ -699,22 +722,22 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};
     rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, max_nbt, max_ntrip,
-                                                  status, want_wat, want_pb, s)
+                                                  status, want_wat, want_pb, s, &rows)
                : dispatch_tile<TersoffPot, double>(args, tp, posff, ntiles, max_nbt, max_ntrip,
-                                                   status, want_wat, want_pb, s);
+                                                   status, want_wat, want_pb, s, &rows);
   } else {
     KumagaiPot kp{make_kumagai_dev(pot.kp)};
     rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, posff, ntiles, max_nbt, max_ntrip,
-                                                  status, want_wat, want_pb, s)
+                                                  status, want_wat, want_pb, s, &rows)
                : dispatch_tile<KumagaiPot, double>(args, kp, posff, ntiles, max_nbt, max_ntrip,
-                                                   status, want_wat, want_pb, s);
+                                                   status, want_wat, want_pb, s, &rows);
   }
   GB_CHECK(rc);
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
                          args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
-  GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(ntiles) + 64));
-  GB_CHECK(reduce_partials(args.tile_part, ntiles, 10, o.red, pot.red_stage.as<double>(), s));
+  GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(rows) + 64));
+  GB_CHECK(reduce_partials(args.tile_part, rows, 10, o.red, pot.red_stage.as<double>(), s));
   pot.tile_atoms = apt;
   return 0;
 }
@@ -980,23 +1003,23 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
     bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, pos, posff);
     note_launch();
   }
-  int rc;
+  int rc, rows = ntiles;
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};
     rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, hp[0], hp[1],
-                                                  status + 2, false, false, s)
+                                                  status + 2, false, false, s, &rows)
                : dispatch_tile<TersoffPot, double>(args, tp, posff, ntiles, hp[0], hp[1],
-                                                   status + 2, false, false, s);
+                                                   status + 2, false, false, s, &rows);
   } else {
     KumagaiPot kp{make_kumagai_dev(pot.kp)};
     rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, posff, ntiles, hp[0], hp[1],
-                                                  status + 2, false, false, s)
+                                                  status + 2, false, false, s, &rows)
                : dispatch_tile<KumagaiPot, double>(args, kp, posff, ntiles, hp[0], hp[1],
-                                                   status + 2, false, false, s);
+                                                   status + 2, false, false, s, &rows);
   }
   GB_CHECK(rc);
   GB_CHECK(launch_gather(mixed, nat, seed32, rev, G, ebond, nullptr, f, nullptr, nullptr, s));
-  GB_CHECK(reduce_partials(part, ntiles, 10, red, nullptr, s));
+  GB_CHECK(reduce_partials(part, rows, 10, red, nullptr, s));
   noalloc_finish<<<1, 32, 0, s>>>(red, epot, wpot);
   note_launch();
   GB_CUDA(cudaGetLastError());

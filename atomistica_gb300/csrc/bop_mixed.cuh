@@ -272,7 +272,9 @@ __device__ __forceinline__ float bsens_f(const MxParams &mp, int eli, float zeta
 // error estimate's first term); log1p(x) and expm1 in FP32, where their
 // error is of the order of zeta's.
 __device__ __forceinline__ void bo_f(const MxParams &mp, int eli, int t, float zeta, ff fc, ff VA,
-                                     const ff *etab, ff &b, ff &P) {
+                                     const ff *etab, ff &b, ff &P, ff &x, float &L) {
+  x = ff_make(0.0f, 0.0f);
+  L = 0.0f;
   if (!(zeta > 0.0f)) {
     b = ff_make(1.0f, 0.0f);
     P = ff_make(0.0f, 0.0f);
@@ -282,14 +284,14 @@ __device__ __forceinline__ void bo_f(const MxParams &mp, int eli, int t, float z
   const ff lnz = ff_log_f(zeta, etab);
   if (mp.kind == 0) {
     const ff tx = ff_add(ff_mul(E.n, lnz), E.lbetan);  // ln x
-    const ff x = ff_exp(tx, etab);
-    const float L = log1pf(x.hi + x.lo);
+    x = ff_exp(tx, etab);
+    L = log1pf(x.hi + x.lo);
     b = ff_mul(mp.pr[t].xi, two_sum(1.0f, expm1f(E.e.hi * L)));
     const ff arg = ff_addf(ff_sub(tx, lnz), (E.e.hi - 1.0f) * L);
     P = ff_mul(ff_mulf(ff_mul(ff_mul(fc, VA), mp.pr[t].xi), -0.25f), ff_exp(arg, etab));
   } else {
-    const ff x = ff_exp(ff_mul(E.eta, lnz), etab);
-    const float L = log1pf(x.hi + x.lo);
+    x = ff_exp(ff_mul(E.eta, lnz), etab);
+    L = log1pf(x.hi + x.lo);
     b = two_sum(1.0f, expm1f(-E.delta.hi * L));
     const ff arg = ff_addf(ff_mul(ff_addf(E.eta, -1.0f), lnz), (-E.delta.hi - 1.0f) * L);
     P = ff_mul(ff_mul(ff_mul(ff_mul(fc, VA), E.eta), ff_neg(E.delta)),
@@ -297,31 +299,26 @@ __device__ __forceinline__ void bo_f(const MxParams &mp, int eli, int t, float z
   }
 }
 
-// Bond order in ff from an ff zeta (the hot-bond path; Tersoff: b = xi
-// (1 + beta^n z^n)^e, P = -1/4 fc VA xi beta^n z^(n-1) (1+x)^(e-1); Kumagai:
-// b = (1 + z^eta)^-delta, P = 1/2 fc VA eta z^(eta-1) (-delta) (1+x)^(-delta-1)).
-__device__ __forceinline__ void bo_ff(const MxParams &mp, int eli, int t, ff zeta, ff fc, ff VA,
-                                      const ff *etab, ff &b, ff &P) {
-  if (!(zeta.hi > 0.0f)) {
-    b = ff_make(1.0f, 0.0f);
-    P = ff_make(0.0f, 0.0f);
-    return;
-  }
+// b and P of a hot bond at zeta0 + dz, from the FP32 pass's x0 = x(zeta0),
+// L0 = log1p(x0) (FP32) and P0 (exact for zeta0 and L0): x to first order in
+// dz / zeta0 (~1e-7), then L = ln(1 + x) and b in ff, and
+// P = P0 (1 + (n - 1) dz / zeta0 + (e - 1) (L - L0)) (Kumagai: n -> eta,
+// e -> -delta); the neglected terms are ~1e-14 relative.
+__device__ __forceinline__ void bo_hot(const MxParams &mp, int eli, int t, ff P0, ff x0,
+                                       float zeta0, float L0, float dz, const ff *etab, ff &b,
+                                       ff &P) {
   const MxElem &E = mp.el[eli];
-  const ff lnz = ff_log(zeta, etab);
-  const ff tx = ff_add(ff_mul(E.n, lnz), E.lbetan);  // ln x
-  const ff x = ff_exp(tx, etab);
+  const float dzr = dz / zeta0;
+  const float n = E.n.hi;  // x ~ zeta^n (Kumagai: n = eta)
+  const ff x = ff_add(x0, ff_mulf(x0, n * dzr));
   const ff L = ff_log(ff_addf(x, 1.0f), etab);
+  const float dL = (L.hi - L0) + L.lo;
   if (mp.kind == 0) {
     b = ff_mul(mp.pr[t].xi, ff_exp(ff_mul(E.e, L), etab));
-    const ff arg = ff_add(ff_sub(tx, lnz), ff_mul(ff_addf(E.e, -1.0f), L));
-    P = ff_mul(ff_mulf(ff_mul(ff_mul(fc, VA), mp.pr[t].xi), -0.25f), ff_exp(arg, etab));
+    P = ff_add(P0, ff_mulf(P0, (n - 1.0f) * dzr + (E.e.hi - 1.0f) * dL));
   } else {
     b = ff_exp(ff_mul(ff_neg(E.delta), L), etab);
-    const ff arg = ff_add(ff_mul(ff_addf(E.eta, -1.0f), lnz),
-                          ff_mul(ff_addf(ff_neg(E.delta), -1.0f), L));
-    P = ff_mul(ff_mul(ff_mul(ff_mul(fc, VA), E.eta), ff_neg(E.delta)),
-               ff_mulf(ff_exp(arg, etab), 0.5f));
+    P = ff_add(P0, ff_mulf(P0, (n - 1.0f) * dzr + (-E.delta.hi - 1.0f) * dL));
   }
 }
 
@@ -543,293 +540,306 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
     s_sin[q] = ff_make(kFfSinTab[2 * q], kFfSinTab[2 * q + 1]);
     s_cos[q] = ff_make(kFfCosTab[2 * q], kFfCosTab[2 * q + 1]);
   }
-  if (tid == 0) s_nhot = 0;
-  const int a0 = blockIdx.x * a.apt;
-  const int a1 = min(a0 + a.apt, a.nat);
-  const int na = a1 - a0;
-  const int b0 = a.seed[a0];
-  const int nbt = a.seed[a1] - b0;
-  int ntrip = 0;
-  {
-    int *aseed = reinterpret_cast<int *>(sm);
-    int *toff = aseed + kMaxApt + 1;
-    int *el = aseed + 2 * kMaxApt + 2;
-    for (int q = tid; q <= na; q += kMxThreads) aseed[q] = a.seed[a0 + q] - b0;
-    for (int q = tid; q < na; q += kMxThreads) el[q] = a.el[a0 + q];
-    __syncthreads();
-    if (tid < 32) {
-      // triplet-slot offsets: exclusive scan of z^2 over the tile's atoms
-      // (na <= 64: two atoms per lane)
-      const int q0 = 2 * tid, q1 = 2 * tid + 1;
-      const int z0 = q0 < na ? aseed[q0 + 1] - aseed[q0] : 0;
-      const int z1 = q1 < na ? aseed[q1 + 1] - aseed[q1] : 0;
-      const int own = z0 * z0 + z1 * z1;
-      int inc = own;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, inc, o);
-        if (tid >= o) inc += v;
-      }
-      const int ex = inc - own;
-      if (q0 < na) toff[q0] = ex;
-      if (q1 < na) toff[q1] = ex + z0 * z0;
-      if (tid == 31) toff[na] = inc;
-    }
-    __syncthreads();
-    ntrip = toff[na];
-  }
-  if (nbt > max_nbt || ntrip > max_ntrip) {
-    if (tid == 0) atomicOr(status, 2);
-    return;
-  }
-  MxLayout L = carve_mx(sm, nbt, ntrip);
-  for (int q = tid; q < na; q += kMxThreads)
-    for (int lb = L.aseed[q]; lb < L.aseed[q + 1]; lb++) L.meta[lb] = q;
-  __syncthreads();
-  const int nel = pot.nel();
-
-  // ---- Phase 1: bond geometry in ff. ----
-  for (int lb = tid; lb < nbt; lb += kMxThreads) {
-    const int ai = L.meta[lb];
-    const int i = a0 + ai;
-    const int b = b0 + lb;
-    const int j = a.nbr[b];
-    const int eli = L.el[ai];
-    const int elj = a.el[j];
-    int meta = ai;
-    ff fc = ff_make(0.0f, 0.0f), dfc = ff_make(0.0f, 0.0f), r = ff_make(1.0f, 0.0f),
-       rinv = ff_make(1.0f, 0.0f);
-    ff rn[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
-    if (eli >= 0 && elj >= 0) {
-      const float4 pih = posff[2 * i], pil = posff[2 * i + 1];
-      const float4 pjh = posff[2 * j], pjl = posff[2 * j + 1];
-      ff rij[3] = {ff_sub(ff_make(pjh.x, pjl.x), ff_make(pih.x, pil.x)),
-                   ff_sub(ff_make(pjh.y, pjl.y), ff_make(pih.y, pil.y)),
-                   ff_sub(ff_make(pjh.z, pjl.z), ff_make(pih.z, pil.z))};
-      int s0, s1, s2;
-      unpack_shift(a.shift[b], s0, s1, s2);
-      if (s0 | s1 | s2) {
-        const float sx = (float)s0, sy = (float)s1, sz = (float)s2;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          ff as = ff_mulf(mp.A[c][0], sx);
-          as = ff_add(as, ff_mulf(mp.A[c][1], sy));
-          as = ff_add(as, ff_mulf(mp.A[c][2], sz));
-          rij[c] = ff_sub(rij[c], as);
-        }
-      }
-      ff r2 = ff_mul(rij[0], rij[0]);
-      r2 = ff_add(r2, ff_mul(rij[1], rij[1]));
-      r2 = ff_add(r2, ff_mul(rij[2], rij[2]));
-      const int t = pair_index(eli, elj, nel);
-      meta |= t << 8;
-      const float r2f = r2.hi + r2.lo;
-      const MxPair &pp = mp.pr[t];
-      if (r2f < pp.r2sq) {
-        ff_sqrt_rsqrt(r2, r, rinv);
-#pragma unroll
-        for (int c = 0; c < 3; c++) rn[c] = ff_mul(rij[c], rinv);
-        const float rf = r.hi + r.lo;
-        if (r2f < pp.r1sq || rf <= pp.r1.hi) {
-          fc = ff_make(1.0f, 0.0f);
-        } else if (rf < pp.r2) {
-          const ff x = ff_mul(pp.fac, ff_sub(r, pp.r1));
-          ff sx, cx;
-          ff_sincos(x, s_sin, s_cos, sx, cx);
-          fc = ff_mulf(ff_addf(cx, 1.0f), 0.5f);
-          dfc = ff_mulf(ff_mul(pp.fac, sx), -0.5f);
-        }
-        int mf = 2;
-        if (a.mask) {
-          const int mi = a.mask[i], mj = a.mask[j];
-          if (mi == 0 && mj == 0)
-            mf = 0;
-          else if (mi == 0 || mj == 0)
-            mf = 1;
-        }
-        meta |= kFlagShort | (mf << 16);
-        if (rf < pp.r2) {
-          meta |= kFlagK;
-          if (mf > 0) meta |= kFlagIJ;
-        }
-      }
-    }
-    L.meta[lb] = meta;
-#pragma unroll
-    for (int c = 0; c < 3; c++) L.rn[c * nbt + lb] = rn[c];
-    L.r[lb] = r;
-    L.rinv[lb] = rinv;
-    L.fc[lb] = fc;
-    L.dfc[lb] = dfc;
-  }
-  __syncthreads();
-
-  // ---- Phase 2: FP32 three-body terms, ff scalar chain. ----
-  for (int lb = tid; lb < nbt; lb += kMxThreads) {
-    const int b = b0 + lb;
-    const int meta = L.meta[lb];
-    if (!(meta & kFlagIJ)) {
-      L.P[lb] = ff_make(0.0f, 0.0f);
-      L.E[lb] = ff_make(0.0f, 0.0f);
-      L.G[lb] = ff_make(0.0f, 0.0f);
-      L.G[nbt + lb] = ff_make(0.0f, 0.0f);
-      L.G[2 * nbt + lb] = ff_make(0.0f, 0.0f);
-      if (a.ebond) a.ebond[b] = 0.0;
-      if (kPB) {
-        a.frbond[3 * (size_t)b] = 0.0;
-        a.frbond[3 * (size_t)b + 1] = 0.0;
-        a.frbond[3 * (size_t)b + 2] = 0.0;
-      }
-      if (kWat)
-        for (int c = 0; c < 9; c++) a.wbond[9 * (size_t)b + c] = 0.0;
-      continue;
-    }
-    const int ai = meta & 0xff;
-    const int t = (meta >> 8) & 0xf;
-    const int mf = (meta >> 16) & 3;
-    const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-    ff *trow = L.t + L.toff[ai] + p * z;
-    const int eli = L.el[ai];
-    const MxPair &pp = mp.pr[t];
-    const float hm = 0.5f * mf;
-    const ff r = L.r[lb];
-    const ff VA = ff_mulf(ff_mul(pp.Bc, ff_exp(ff_neg(ff_mul(pp.cA, r)), s_exp)), -hm);
-    const ff dVA = ff_neg(ff_mul(pp.cA, VA));
-    const ff VR = ff_mulf(ff_mul(pp.Ac, ff_exp(ff_neg(ff_mul(pp.cR, r)), s_exp)), hm);
-    const ff dVR = ff_neg(ff_mul(pp.cR, VR));
-    float zeta = 0.0f, dbj[3] = {0.0f, 0.0f, 0.0f}, wk[9], sumdk = 0.0f;
-    if (kWat)
-#pragma unroll
-      for (int c = 0; c < 9; c++) wk[c] = 0.0f;
-    kloop_mx<kWat>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
-    // A zeta below 1e-30 would overflow the FP32 range inside ln/exp: such a
-    // bond (and any non-finite estimate) takes the accurate path.
-    const bool tiny = zeta > 0.0f && zeta < 1.0e-30f;
-    ff bij, P;
-    bo_f(mp, eli, t, tiny ? 1.0f : zeta, L.fc[lb], VA, s_exp, bij, P);
-    // Error estimate (eV/A) of this bond's forces on the FP32 path: the FP32
-    // zeta through d b / d ln zeta, and the FP32 three-body derivatives
-    // multiplied by P.
-    const float est = 2.4e-7f * fabsf(dVA.hi) * L.fc[lb].hi * bsens_f(mp, eli, zeta) +
-                      3.0e-7f * fabsf(P.hi) *
-                          (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
-    if (tiny || !(est <= kHotThreshold)) {
-      L.hot[atomicAdd(&s_nhot, 1)] = lb;
-    } else {
-      const ff dbjf[3] = {ff_make(dbj[0], 0.0f), ff_make(dbj[1], 0.0f), ff_make(dbj[2], 0.0f)};
-      ff wkf[9];
-      if (kWat)
-#pragma unroll
-        for (int c = 0; c < 9; c++) wkf[c] = ff_make(wk[c], 0.0f);
-      finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbjf, wkf, VA, dVA, VR, dVR);
-    }
-  }
-  __syncthreads();
-  // ---- Phase 2b: the hot bonds again, k loop and bond order in ff. ----
-  // kHotLanes lanes per hot bond share its k loop; the partial sums are added
-  // by a fixed xor tree, then the group's first lane finishes the bond.
-  {
-    constexpr int kHotLanes = 8;
-    constexpr int kGroups = kMxThreads / kHotLanes;
-    const int nhot = s_nhot;
-    if (tid == 0 && nhot > 0) atomicAdd(&status[2], nhot);  // diagnostic count
-    const int gl = tid & (kHotLanes - 1);
-    for (int base = 0; base < nhot; base += kGroups) {
-      const int hq = base + tid / kHotLanes;
-      const bool act = hq < nhot;
-      ff zeta = ff_make(0.0f, 0.0f), wk[9];
-      ff dbj[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
-      if (kWat)
-#pragma unroll
-        for (int c = 0; c < 9; c++) wk[c] = ff_make(0.0f, 0.0f);
-      int lb = 0;
-      if (act) {
-        lb = L.hot[hq];
-        const int ai = L.meta[lb] & 0xff;
-        const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-        kloop_ff<kWat>(mp, L, lb, s, z, L.el[ai], L.t + L.toff[ai] + p * z, s_exp, gl,
-                       kHotLanes, zeta, dbj, wk);
-      }
-#pragma unroll
-      for (int o = 1; o < kHotLanes; o <<= 1) {
-        zeta = ff_add(zeta, ff_shfl_xor(zeta, o));
-#pragma unroll
-        for (int c = 0; c < 3; c++) dbj[c] = ff_add(dbj[c], ff_shfl_xor(dbj[c], o));
-        if (kWat)
-#pragma unroll
-          for (int c = 0; c < 9; c++) wk[c] = ff_add(wk[c], ff_shfl_xor(wk[c], o));
-      }
-      if (act && gl == 0) {
-        const int b = b0 + lb;
-        const int meta = L.meta[lb];
-        const int ai = meta & 0xff;
-        const int t = (meta >> 8) & 0xf;
-        const int mf = (meta >> 16) & 3;
-        const int eli = L.el[ai];
-        const MxPair &pp = mp.pr[t];
-        const float hm = 0.5f * mf;
-        const ff r = L.r[lb];
-        const ff VA = ff_mulf(ff_mul(pp.Bc, ff_exp(ff_neg(ff_mul(pp.cA, r)), s_exp)), -hm);
-        const ff dVA = ff_neg(ff_mul(pp.cA, VA));
-        const ff VR = ff_mulf(ff_mul(pp.Ac, ff_exp(ff_neg(ff_mul(pp.cR, r)), s_exp)), hm);
-        const ff dVR = ff_neg(ff_mul(pp.cR, VR));
-        ff bij, P;
-        if (zeta.hi > 1.0e-30f) {
-          bo_ff(mp, eli, t, zeta, L.fc[lb], VA, s_exp, bij, P);
-        } else {
-          // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
-          double b64, P64;
-          pot.template bo<double>(eli, t, ff_to_double(zeta), ff_to_double(L.fc[lb]),
-                                  ff_to_double(VA), b64, P64);
-          bij = ff_from_double(b64);
-          P = ff_from_double(P64);
-        }
-        finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
-      }
-    }
-  }
-  __syncthreads();
-
-  // ---- Phase 3: k-role forces (ff) and the virial (FP32 per thread). ----
+  // Persistent CTAs: tiles blockIdx.x, blockIdx.x + gridDim.x, ... (a static
+  // schedule, so the per-CTA energy and virial sums are reproducible).
   ff eacc = ff_make(0.0f, 0.0f);
   float wacc[9];
 #pragma unroll
   for (int c = 0; c < 9; c++) wacc[c] = 0.0f;
-  for (int lb = tid; lb < nbt; lb += kMxThreads) {
-    const int b = b0 + lb;
-    const int meta = L.meta[lb];
-    ff_acc(eacc, L.E[lb]);
-    ff G[3] = {L.G[lb], L.G[nbt + lb], L.G[2 * nbt + lb]};
-    if (meta & kFlagK) {
-      const int ai = meta & 0xff;
-      const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, q = lb - s;
-      const ff *tcol = L.t + L.toff[ai] + q;
-      for (int pq = 0; pq < z; pq++) {
-        const int lp = s + pq;
-        if (lp == lb) continue;
-        if (!(L.meta[lp] & kFlagIJ)) continue;
-        const ff mP = ff_neg(L.P[lp]);
-        const ff *tv = tcol + pq * z;
+  const int ntiles = (a.nat + a.apt - 1) / a.apt;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    __syncthreads();  // the previous tile is done with shared memory
+    if (tid == 0) s_nhot = 0;
+    const int a0 = tile * a.apt;
+    const int a1 = min(a0 + a.apt, a.nat);
+    const int na = a1 - a0;
+    const int b0 = a.seed[a0];
+    const int nbt = a.seed[a1] - b0;
+    int ntrip = 0;
+    {
+      int *aseed = reinterpret_cast<int *>(sm);
+      int *toff = aseed + kMaxApt + 1;
+      int *el = aseed + 2 * kMaxApt + 2;
+      for (int q = tid; q <= na; q += kMxThreads) aseed[q] = a.seed[a0 + q] - b0;
+      for (int q = tid; q < na; q += kMxThreads) el[q] = a.el[a0 + q];
+      __syncthreads();
+      if (tid < 32) {
+        // triplet-slot offsets: exclusive scan of z^2 over the tile's atoms
+        // (na <= 64: two atoms per lane)
+        const int q0 = 2 * tid, q1 = 2 * tid + 1;
+        const int z0 = q0 < na ? aseed[q0 + 1] - aseed[q0] : 0;
+        const int z1 = q1 < na ? aseed[q1 + 1] - aseed[q1] : 0;
+        const int own = z0 * z0 + z1 * z1;
+        int inc = own;
 #pragma unroll
-        for (int c = 0; c < 3; c++) ff_acc_mul(G[c], mP, tv[c * ntrip]);
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, inc, o);
+          if (tid >= o) inc += v;
+        }
+        const int ex = inc - own;
+        if (q0 < na) toff[q0] = ex;
+        if (q1 < na) toff[q1] = ex + z0 * z0;
+        if (tid == 31) toff[na] = inc;
       }
-#pragma unroll
-      for (int c = 0; c < 3; c++) G[c] = ff_norm(G[c]);
-      const float r = L.r[lb].hi;
-      float rb[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) rb[c] = r * L.rn[c * nbt + lb].hi;
-#pragma unroll
-      for (int c1 = 0; c1 < 3; c1++)
-#pragma unroll
-        for (int c2 = 0; c2 < 3; c2++)
-          wacc[c1 + 3 * c2] = fmaf(-rb[c1], G[c2].hi + G[c2].lo, wacc[c1 + 3 * c2]);
+      __syncthreads();
+      ntrip = toff[na];
     }
-    float2 *Gout = reinterpret_cast<float2 *>(a.G) + 3 * (size_t)b;
-    Gout[0] = make_float2(G[0].hi, G[0].lo);
-    Gout[1] = make_float2(G[1].hi, G[1].lo);
-    Gout[2] = make_float2(G[2].hi, G[2].lo);
-  }
+    if (nbt > max_nbt || ntrip > max_ntrip) {  // uniform over the block
+      if (tid == 0) atomicOr(status, 2);
+      continue;
+    }
+    MxLayout L = carve_mx(sm, nbt, ntrip);
+    for (int q = tid; q < na; q += kMxThreads)
+      for (int lb = L.aseed[q]; lb < L.aseed[q + 1]; lb++) L.meta[lb] = q;
+    __syncthreads();
+    const int nel = pot.nel();
+
+    // ---- Phase 1: bond geometry in ff. ----
+    for (int lb = tid; lb < nbt; lb += kMxThreads) {
+      const int ai = L.meta[lb];
+      const int i = a0 + ai;
+      const int b = b0 + lb;
+      const int j = a.nbr[b];
+      const int eli = L.el[ai];
+      const int elj = a.el[j];
+      int meta = ai;
+      ff fc = ff_make(0.0f, 0.0f), dfc = ff_make(0.0f, 0.0f), r = ff_make(1.0f, 0.0f),
+         rinv = ff_make(1.0f, 0.0f);
+      ff rn[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
+      if (eli >= 0 && elj >= 0) {
+        const float4 pih = posff[2 * i], pil = posff[2 * i + 1];
+        const float4 pjh = posff[2 * j], pjl = posff[2 * j + 1];
+        ff rij[3] = {ff_sub(ff_make(pjh.x, pjl.x), ff_make(pih.x, pil.x)),
+                     ff_sub(ff_make(pjh.y, pjl.y), ff_make(pih.y, pil.y)),
+                     ff_sub(ff_make(pjh.z, pjl.z), ff_make(pih.z, pil.z))};
+        int s0, s1, s2;
+        unpack_shift(a.shift[b], s0, s1, s2);
+        if (s0 | s1 | s2) {
+          const float sx = (float)s0, sy = (float)s1, sz = (float)s2;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            ff as = ff_mulf(mp.A[c][0], sx);
+            as = ff_add(as, ff_mulf(mp.A[c][1], sy));
+            as = ff_add(as, ff_mulf(mp.A[c][2], sz));
+            rij[c] = ff_sub(rij[c], as);
+          }
+        }
+        ff r2 = ff_mul(rij[0], rij[0]);
+        r2 = ff_add(r2, ff_mul(rij[1], rij[1]));
+        r2 = ff_add(r2, ff_mul(rij[2], rij[2]));
+        const int t = pair_index(eli, elj, nel);
+        meta |= t << 8;
+        const float r2f = r2.hi + r2.lo;
+        const MxPair &pp = mp.pr[t];
+        if (r2f < pp.r2sq) {
+          ff_sqrt_rsqrt(r2, r, rinv);
+#pragma unroll
+          for (int c = 0; c < 3; c++) rn[c] = ff_mul(rij[c], rinv);
+          const float rf = r.hi + r.lo;
+          if (r2f < pp.r1sq || rf <= pp.r1.hi) {
+            fc = ff_make(1.0f, 0.0f);
+          } else if (rf < pp.r2) {
+            const ff x = ff_mul(pp.fac, ff_sub(r, pp.r1));
+            ff sx, cx;
+            ff_sincos(x, s_sin, s_cos, sx, cx);
+            fc = ff_mulf(ff_addf(cx, 1.0f), 0.5f);
+            dfc = ff_mulf(ff_mul(pp.fac, sx), -0.5f);
+          }
+          int mf = 2;
+          if (a.mask) {
+            const int mi = a.mask[i], mj = a.mask[j];
+            if (mi == 0 && mj == 0)
+              mf = 0;
+            else if (mi == 0 || mj == 0)
+              mf = 1;
+          }
+          meta |= kFlagShort | (mf << 16);
+          if (rf < pp.r2) {
+            meta |= kFlagK;
+            if (mf > 0) meta |= kFlagIJ;
+          }
+        }
+      }
+      L.meta[lb] = meta;
+#pragma unroll
+      for (int c = 0; c < 3; c++) L.rn[c * nbt + lb] = rn[c];
+      L.r[lb] = r;
+      L.rinv[lb] = rinv;
+      L.fc[lb] = fc;
+      L.dfc[lb] = dfc;
+    }
+    __syncthreads();
+
+    // ---- Phase 2: FP32 three-body terms, ff scalar chain. ----
+    for (int lb = tid; lb < nbt; lb += kMxThreads) {
+      const int b = b0 + lb;
+      const int meta = L.meta[lb];
+      if (!(meta & kFlagIJ)) {
+        L.P[lb] = ff_make(0.0f, 0.0f);
+        L.E[lb] = ff_make(0.0f, 0.0f);
+        L.G[lb] = ff_make(0.0f, 0.0f);
+        L.G[nbt + lb] = ff_make(0.0f, 0.0f);
+        L.G[2 * nbt + lb] = ff_make(0.0f, 0.0f);
+        if (a.ebond) a.ebond[b] = 0.0;
+        if (kPB) {
+          a.frbond[3 * (size_t)b] = 0.0;
+          a.frbond[3 * (size_t)b + 1] = 0.0;
+          a.frbond[3 * (size_t)b + 2] = 0.0;
+        }
+        if (kWat)
+          for (int c = 0; c < 9; c++) a.wbond[9 * (size_t)b + c] = 0.0;
+        continue;
+      }
+      const int ai = meta & 0xff;
+      const int t = (meta >> 8) & 0xf;
+      const int mf = (meta >> 16) & 3;
+      const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
+      ff *trow = L.t + L.toff[ai] + p * z;
+      const int eli = L.el[ai];
+      const MxPair &pp = mp.pr[t];
+      const float hm = 0.5f * mf;
+      const ff r = L.r[lb];
+      const ff VA = ff_mulf(ff_mul(pp.Bc, ff_exp(ff_neg(ff_mul(pp.cA, r)), s_exp)), -hm);
+      const ff dVA = ff_neg(ff_mul(pp.cA, VA));
+      const ff VR = ff_mulf(ff_mul(pp.Ac, ff_exp(ff_neg(ff_mul(pp.cR, r)), s_exp)), hm);
+      const ff dVR = ff_neg(ff_mul(pp.cR, VR));
+      float zeta = 0.0f, dbj[3] = {0.0f, 0.0f, 0.0f}, wk[9], sumdk = 0.0f;
+      if (kWat)
+#pragma unroll
+        for (int c = 0; c < 9; c++) wk[c] = 0.0f;
+      kloop_mx<kWat>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
+      // A zeta below 1e-30 would overflow the FP32 range inside ln/exp: such a
+      // bond (and any non-finite estimate) takes the accurate path.
+      const bool tiny = zeta > 0.0f && zeta < 1.0e-30f;
+      ff bij, P, x0;
+      float L0;
+      bo_f(mp, eli, t, tiny ? 1.0f : zeta, L.fc[lb], VA, s_exp, bij, P, x0, L0);
+      // Error estimate (eV/A) of this bond's forces on the FP32 path: the FP32
+      // zeta through d b / d ln zeta, the FP32 log1p/expm1 of b, and the FP32
+      // three-body derivatives multiplied by P.
+      const float fva = fabsf(dVA.hi) * L.fc[lb].hi;
+      const float est = fva * (2.4e-7f * bsens_f(mp, eli, zeta) +
+                               1.5e-7f * fabsf(bij.hi - mp.pr[t].xi.hi)) +
+                        3.0e-7f * fabsf(P.hi) *
+                            (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
+      if (tiny || !(est <= kHotThreshold)) {
+        L.hot[atomicAdd(&s_nhot, 1)] = lb;
+        // kept for the accurate pass (which overwrites these slots)
+        L.P[lb] = VA;
+        L.E[lb] = VR;
+        L.G[lb] = P;
+        L.G[nbt + lb] = x0;
+        L.G[2 * nbt + lb] = ff_make(tiny ? 0.0f : zeta, L0);
+      } else {
+        const ff dbjf[3] = {ff_make(dbj[0], 0.0f), ff_make(dbj[1], 0.0f), ff_make(dbj[2], 0.0f)};
+        ff wkf[9];
+        if (kWat)
+#pragma unroll
+          for (int c = 0; c < 9; c++) wkf[c] = ff_make(wk[c], 0.0f);
+        finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbjf, wkf, VA, dVA, VR, dVR);
+      }
+    }
+    __syncthreads();
+    // ---- Phase 2b: the hot bonds again, k loop and bond order in ff. ----
+    // kHotLanes lanes per hot bond share its k loop; the partial sums are added
+    // by a fixed xor tree, then the group's first lane finishes the bond.
+    {
+      constexpr int kHotLanes = 8;
+      constexpr int kGroups = kMxThreads / kHotLanes;
+      const int nhot = s_nhot;
+      if (tid == 0 && nhot > 0) atomicAdd(&status[2], nhot);  // diagnostic count
+      const int gl = tid & (kHotLanes - 1);
+      for (int base = 0; base < nhot; base += kGroups) {
+        const int hq = base + tid / kHotLanes;
+        const bool act = hq < nhot;
+        ff zeta = ff_make(0.0f, 0.0f), wk[9];
+        ff dbj[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
+        if (kWat)
+#pragma unroll
+          for (int c = 0; c < 9; c++) wk[c] = ff_make(0.0f, 0.0f);
+        int lb = 0;
+        if (act) {
+          lb = L.hot[hq];
+          const int ai = L.meta[lb] & 0xff;
+          const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
+          kloop_ff<kWat>(mp, L, lb, s, z, L.el[ai], L.t + L.toff[ai] + p * z, s_exp, gl,
+                         kHotLanes, zeta, dbj, wk);
+        }
+#pragma unroll
+        for (int o = 1; o < kHotLanes; o <<= 1) {
+          zeta = ff_add(zeta, ff_shfl_xor(zeta, o));
+#pragma unroll
+          for (int c = 0; c < 3; c++) dbj[c] = ff_add(dbj[c], ff_shfl_xor(dbj[c], o));
+          if (kWat)
+#pragma unroll
+            for (int c = 0; c < 9; c++) wk[c] = ff_add(wk[c], ff_shfl_xor(wk[c], o));
+        }
+        if (act && gl == 0) {
+          const int b = b0 + lb;
+          const int meta = L.meta[lb];
+          const int ai = meta & 0xff;
+          const int t = (meta >> 8) & 0xf;
+          const int eli = L.el[ai];
+          const MxPair &pp = mp.pr[t];
+          const ff VA = L.P[lb], VR = L.E[lb];  // from the FP32 pass
+          const ff dVA = ff_neg(ff_mul(pp.cA, VA));
+          const ff dVR = ff_neg(ff_mul(pp.cR, VR));
+          ff bij, P;
+          const ff zl = L.G[2 * nbt + lb];  // (FP32-pass zeta, L0)
+          if (zl.hi > 0.0f && zeta.hi > 1.0e-30f) {
+            bo_hot(mp, eli, t, L.G[lb], L.G[nbt + lb], zl.hi, zl.lo, (zeta.hi - zl.hi) + zeta.lo,
+                   s_exp, bij, P);
+          } else {
+            // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
+            double b64, P64;
+            pot.template bo<double>(eli, t, ff_to_double(zeta), ff_to_double(L.fc[lb]),
+                                    ff_to_double(VA), b64, P64);
+            bij = ff_from_double(b64);
+            P = ff_from_double(P64);
+          }
+          finalize_mx<kWat, kPB>(a, L, lb, b, bij, P, dbj, wk, VA, dVA, VR, dVR);
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- Phase 3: k-role forces (ff) and the virial (FP32 per thread). ----
+    for (int lb = tid; lb < nbt; lb += kMxThreads) {
+      const int b = b0 + lb;
+      const int meta = L.meta[lb];
+      ff_acc(eacc, L.E[lb]);
+      ff G[3] = {L.G[lb], L.G[nbt + lb], L.G[2 * nbt + lb]};
+      if (meta & kFlagK) {
+        const int ai = meta & 0xff;
+        const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, q = lb - s;
+        const ff *tcol = L.t + L.toff[ai] + q;
+        for (int pq = 0; pq < z; pq++) {
+          const int lp = s + pq;
+          if (lp == lb) continue;
+          if (!(L.meta[lp] & kFlagIJ)) continue;
+          const ff mP = ff_neg(L.P[lp]);
+          const ff *tv = tcol + pq * z;
+#pragma unroll
+          for (int c = 0; c < 3; c++) ff_acc_mul(G[c], mP, tv[c * ntrip]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) G[c] = ff_norm(G[c]);
+        const float r = L.r[lb].hi;
+        float rb[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) rb[c] = r * L.rn[c * nbt + lb].hi;
+#pragma unroll
+        for (int c1 = 0; c1 < 3; c1++)
+#pragma unroll
+          for (int c2 = 0; c2 < 3; c2++)
+            wacc[c1 + 3 * c2] = fmaf(-rb[c1], G[c2].hi + G[c2].lo, wacc[c1 + 3 * c2]);
+      }
+      float2 *Gout = reinterpret_cast<float2 *>(a.G) + 3 * (size_t)b;
+      Gout[0] = make_float2(G[0].hi, G[0].lo);
+      Gout[1] = make_float2(G[1].hi, G[1].lo);
+      Gout[2] = make_float2(G[2].hi, G[2].lo);
+    }
+  }  // tiles
   block_sum_tile(ff_norm(eacc), wacc, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
 }
 
