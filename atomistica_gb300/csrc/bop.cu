@@ -626,14 +626,16 @@ int reduce_partials(const double *part, int nrows, int nc, double *red, double *
     set_error("reduce_partials: unsupported column count");
     return GB_ERROR_ARGUMENT;
   }
+  // 64 threads per block: the shuffle tree's FP64 adds run on one SM's FP64
+  // units, so a wide block would be bound by them.
   if (stage == nullptr || nrows <= 2 * kRedRowsPerBlock) {
-    reduce_rows_kernel<<<1, 1024, 0, s>>>(part, nrows, std::max(nrows, 1), red);
+    reduce_rows_kernel<<<1, 64, 0, s>>>(part, nrows, std::max(nrows, 1), red);
     note_launch();
   } else {
     const int nb = (nrows + kRedRowsPerBlock - 1) / kRedRowsPerBlock;
-    reduce_rows_kernel<<<nb, kRedRowsPerBlock, 0, s>>>(part, nrows, kRedRowsPerBlock, stage);
+    reduce_rows_kernel<<<nb, 64, 0, s>>>(part, nrows, kRedRowsPerBlock, stage);
     note_launch();
-    reduce_rows_kernel<<<1, 1024, 0, s>>>(stage, nb, nb, red);
+    reduce_rows_kernel<<<1, 64, 0, s>>>(stage, nb, nb, red);
     note_launch();
   }
   GB_CUDA(cudaGetLastError());

@@ -332,11 +332,18 @@ __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams
   const float xf = (float)x, yf = (float)y, zf = (float)z;
   {
     // max |coordinate| (rounded up) for the pair prefilter's error bound: one
-    // atomic per warp.
+    // atomic per block (a single address: per-warp atomics serialised there).
+    __shared__ unsigned wmax[32];
     const float m = finite ? fmaxf(fabsf(xf), fmaxf(fabsf(yf), fabsf(zf))) * (1.0f + 1.2e-7f)
                            : 0.0f;
     const unsigned mw = __reduce_max_sync(0xffffffffu, (unsigned)__float_as_int(m));
-    if ((threadIdx.x & 31) == 0) atomicMax(&status[3], (int)mw);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mw;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const unsigned v = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0u;
+      const unsigned bm = __reduce_max_sync(0xffffffffu, v);
+      if (threadIdx.x == 0) atomicMax(&status[3], (int)bm);
+    }
   }
   if (!in) return;
   pos4[i] = Pos4{x, y, z, 0.0};
