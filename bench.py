@@ -51,9 +51,12 @@ FLOPS_BOND = 150.0
 FLOPS_TRIPLET = 165.0
 # Compulsory DRAM bytes of one bond-order tile launch: per atom positions
 # (32 B), element (4 B) and CSR offset (4 B); per directed bond the neighbour
-# index and packed shift (8 B) in, the bond force G (24 B) and energy (8 B) out.
+# index and packed shift (8 B) in, the bond force G (24 B) out.
 BYTES_ATOM = 40.0
-BYTES_BOND = 40.0
+BYTES_BOND = 32.0
+# DRAM bytes (read + write) of one launch of the mixed tile kernel at this
+# workload, from ncu (profiles/bop_tile_mx_tersoff_si_1048576.md).
+TRAFFIC_MX = 75.56e6 + 48.86e6
 
 
 def parse_args():
@@ -329,7 +332,10 @@ def run_ours(args):
     t_byte = fm["bytes"] / (hbm * 1e9)
     roofline = {"bound": "fp32" if t_flop >= t_byte else "hbm",
                 "achieved": fm["flops"] / t_k / 1e12, "peak": p32, "unit": "TFLOP/s",
-                "frac": max(t_flop, t_byte) / t_k, "traffic": None,
+                "frac": max(t_flop, t_byte) / t_k,
+                "traffic": TRAFFIC_MX if nat == 1048576 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                                  "(profiles/bop_tile_mx_tersoff_si_1048576.md)",
                 "kernel": "bop_tile_mx<Tersoff> (mixed form)",
                 "kernel_ms": kern_mx,
                 "t_roof_ms": 1e3 * max(t_flop, t_byte),
