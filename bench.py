@@ -160,6 +160,93 @@ def cpu_baseline(structure, params, runs):
             "seconds_per_call": t}
 
 
+def _gpu_step_ms(pot, p, nl, d_pos, d_f, steps=20):
+    """Mean device time (ms) of set_positions + energy_and_forces."""
+    import torch
+    for _ in range(3):
+        d_f.zero_()
+        p.set_positions(d_pos)
+        pot.energy_and_forces(p, nl, forces=d_f)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        d_f.zero_()
+        p.set_positions(d_pos)
+        pot.energy_and_forces(p, nl, forces=d_f)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def other_configs(dev, oracle):
+    """The 4096-atom Tersoff crystal (FP64 and mixed) and the 131,072-atom
+    alloy-EAM Cu block (FP64): GPU atom-evals/s through the public API with
+    device-resident inputs (default stream, no L2 flush: both fit in L2),
+    the oracle on all host cores, and the GPU-oracle deviations."""
+    import numpy as np
+    import torch
+    from atomistica_gb300 import io as gio, native, parameters, structures
+    out = {}
+    nth = oracle.max_threads()
+
+    def cpu_time(fn, runs=5):
+        fn()
+        ts = []
+        for _ in range(runs):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    s = structures.tersoff_si_4096(seed=1)
+    params = parameters.Tersoff_PRB_39_5566_Si_C
+    ref = oracle.bop_compute("tersoff", params, s, nthreads=nth)
+    t_cpu = cpu_time(lambda: oracle.bop_compute("tersoff", params, s, nthreads=nth))
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+    d_f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+    entry = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu, "cpu_cores": nth}
+    for prec in ("fp64", "mixed"):
+        pot = native.Tersoff(precision=prec)
+        pot.bind_to(p, nl)
+        ms = _gpu_step_ms(pot, p, nl, d_pos, d_f)
+        d_f.zero_()
+        p.set_positions(d_pos)
+        e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
+        f = d_f.cpu().numpy()
+        entry[prec] = {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
+                       "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
+                       "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}
+    out["tersoff_si_4096"] = entry
+
+    s = structures.eam_cu_131072(seed=2)
+    with tempfile.TemporaryDirectory() as td:
+        fn = os.path.join(td, "cu.setfl")
+        gio.cu_analytic_setfl(fn)
+        eo = oracle.EAM(fn)
+        ref = eo.compute_full(s, nthreads=nth)
+        t_cpu = cpu_time(lambda: eo.compute_full(s, nthreads=nth))
+        p = native.from_atoms(s)
+        nl = native.Neighbors(100)
+        pot = native.TabulatedAlloyEAM(fn)
+        pot.bind_to(p, nl)
+        d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+        d_f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+        ms = _gpu_step_ms(pot, p, nl, d_pos, d_f)
+        d_f.zero_()
+        p.set_positions(d_pos)
+        e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
+        f = d_f.cpu().numpy()
+    out["eam_cu_131072"] = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu,
+                            "cpu_cores": nth,
+                            "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
+                                     "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
+                                     "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -393,6 +480,7 @@ def run_ours(args):
                 "abs_dE_per_atom": abs(e - ref["epot"]) / nat,
                 "max_abs_dW": float(np.max(np.abs(w - ref["wpot"])))}
         line["cpu_baseline"] = cpu_baseline(s, params, args.cpu_runs)
+        line["other_configs"] = other_configs(dev, oracle)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
