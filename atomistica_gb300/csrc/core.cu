@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "internal.h"
 
@@ -251,24 +252,21 @@ static int gauss_solve3(const double Ain[3][3], const double b[3], double x[3]) 
   return 0;
 }
 
+int cell_inverse(const double A[3][3], double B[3][3]) {
+  for (int c = 0; c < 3; c++) {
+    double e[3] = {0, 0, 0}, x[3];
+    e[c] = 1.0;
+    if (gauss_solve3(A, e, x) != 0) return -1;
+    for (int a = 0; a < 3; a++) B[a][c] = x[a];
+  }
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // Neighbour build kernels.
 // ---------------------------------------------------------------------------
 namespace {
 
-struct BinParams {
-  double rec[3][3];
-  float recf[3][3];  // rec rounded to float (cell prefilter)
-  double A[3][3];
-  float Af[3][3];  // A rounded to float, and max |A_ak|
-  float Amax;
-  int n[3];
-  int pbc[3];
-  int dx, dy, dz;
-  double cutoff_sq;
-  float cutoff_f;                    // cutoff rounded up to float
-  float cutoff_sq_lo, cutoff_sq_hi;  // float bracket of cutoff^2
-};
 
 __device__ __forceinline__ int floor_div(int a, int n) {
   int q = a / n;
@@ -307,14 +305,18 @@ __device__ __forceinline__ void raw_cell(const BinParams &bp, double x, double y
 // Linear cell index, z fastest: the 2 dz + 1 cells of one (x, y) stencil row
 // are contiguous in the cell-sorted atom order.
 __device__ __forceinline__ int cell_linear(const BinParams &bp, int cx, int cy, int cz) {
-  return (cx * bp.n[1] + cy) * bp.n[2] + cz;
+  return bp.cell_base + (cx * bp.n[1] + cy) * bp.n[2] + cz;
 }
 
 __device__ __forceinline__ int pack_wrap(int q0, int q1, int q2) {
   return pack_shift(q0, q1, q2);
 }
 
-__global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams bp,
+// kBatch: atom i belongs to structure sid[i] with binning parameters
+// bps[sid[i]] (cells of all structures numbered consecutively).
+template <bool kBatch>
+__global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams bp0,
+                                const BinParams *__restrict__ bps, const int *__restrict__ sid,
                                 Pos4 *__restrict__ pos4, float4 *__restrict__ posff,
                                 int *__restrict__ atom_cell,
                                 int *__restrict__ atom_wrap, int *__restrict__ cell_count,
@@ -346,6 +348,7 @@ __global__ void nl_assign_cells(int nat, const double *__restrict__ r, BinParams
     }
   }
   if (!in) return;
+  const BinParams &bp = kBatch ? bps[sid[i]] : bp0;
   pos4[i] = Pos4{x, y, z, 0.0};
   if (posff) {
     // float-float copy (hi, lo) for the mixed-precision kernels
@@ -512,9 +515,10 @@ __device__ __forceinline__ bool wrap_cell(const BinParams &bp, int k, int &c, in
   return true;
 }
 
-template <int kMode>
+template <int kMode, bool kBatch>
 __global__ void __launch_bounds__(128)
-    nl_pairs(int nat, BinParams bp, const Pos4 *__restrict__ pos4,
+    nl_pairs(int nat, BinParams bp0, const BinParams *__restrict__ bps,
+             const int *__restrict__ sid, const Pos4 *__restrict__ pos4,
              const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
              const int *__restrict__ swrap, const int *__restrict__ cell_start,
              int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
@@ -524,7 +528,8 @@ __global__ void __launch_bounds__(128)
   if (t >= nat) return;
   const float4 pi = spos[t];
   const int i = __float_as_int(pi.w);
-  int ci = atom_cell[i];
+  const BinParams &bp = kBatch ? bps[sid[i]] : bp0;
+  int ci = atom_cell[i] - bp.cell_base;
   const int cz0 = ci % bp.n[2];
   ci /= bp.n[2];
   const int cy0 = ci % bp.n[1];
@@ -690,24 +695,28 @@ __global__ void nl_reverse(int nat, const int *__restrict__ seed, const int *__r
 
 }  // namespace
 
-// Host-side binning_init (python_neighbors.f90:765-871).
-static void binning_init(Neighbors &nl, const Particles &p, double cutoff) {
+// Host-side binning_init (python_neighbors.f90:765-871) for one cell:
+// n_cells = max(3, int(|a_k| / cutoff)), rec_cell_size = n_cells * Bbox,
+// stencil half-widths from the cell's plane spacings; plus the derived
+// fields of the pair search.  cell_base offsets the cell numbers (batches).
+int bin_params(const double A[3][3], const double B[3][3], const int pbc[3], double cutoff,
+               int cell_base, BinParams &bp) {
   const double bin_size = cutoff;
   double box_size[3];
   for (int x = 0; x < 3; x++) {
     double s = 0.0;
-    for (int a = 0; a < 3; a++) s = s + p.A[a][x] * p.A[a][x];
+    for (int a = 0; a < 3; a++) s = s + A[a][x] * A[a][x];
     box_size[x] = std::sqrt(s);
   }
   for (int x = 0; x < 3; x++) {
     double v = box_size[x] / bin_size;
     int nc = v > 1e6 ? 1000000 : (int)v;
-    nl.n_cells[x] = nc < 3 ? 3 : nc;
+    bp.n[x] = nc < 3 ? 3 : nc;
   }
   double cs[3][3];
   for (int x = 0; x < 3; x++) {
-    for (int a = 0; a < 3; a++) cs[a][x] = p.A[a][x] / nl.n_cells[x];
-    for (int k = 0; k < 3; k++) nl.rec[x][k] = p.B[x][k] * nl.n_cells[x];
+    for (int a = 0; a < 3; a++) cs[a][x] = A[a][x] / bp.n[x];
+    for (int k = 0; k < 3; k++) bp.rec[x][k] = B[x][k] * bp.n[x];
   }
   auto cross = [](const double u[3], const double v[3], double w[3]) {
     w[0] = u[1] * v[2] - u[2] * v[1];
@@ -736,65 +745,40 @@ static void binning_init(Neighbors &nl, const Particles &p, double cutoff) {
     ny[a] = cv * ny[a] / dny;
     nz[a] = cv * nz[a] / dnz;
   }
-  nl.dx = (int)(cutoff / std::sqrt(dot(nx, nx))) + 1;
-  nl.dy = (int)(cutoff / std::sqrt(dot(ny, ny))) + 1;
-  nl.dz = (int)(cutoff / std::sqrt(dot(nz, nz))) + 1;
-}
-
-int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
-  if (!p.cell_set) {
-    set_error("neighbors_update: cell not set");
-    return GB_ERROR_ARGUMENT;
-  }
-  if (p.nat > 0 && !p.r.p) {
-    set_error("neighbors_update: positions not set");
-    return GB_ERROR_ARGUMENT;
-  }
-  if (nl.valid && nl.built_for == &p && nl.built_pos_rev == p.pos_rev &&
-      nl.built_cell_rev == p.cell_rev && nl.built_nat == p.nat && nl.cutoff == nl.interaction_range)
-    return 0;
-  // cutoff = interaction_range + verlet_shell (0 on the Python path, :478)
-  const double cutoff = nl.interaction_range;
-  if (!(cutoff > 0.0)) {
-    set_error("Cutoff needs to be larger than zero.");
-    return GB_ERROR_ARGUMENT;
-  }
-  nl.valid = false;
-  nl.rev_valid = false;
-  nl.rev_pending = false;
-  const int nat = p.nat;
-  binning_init(nl, p, cutoff);
-  const int ncells = nl.n_cells[0] * nl.n_cells[1] * nl.n_cells[2];
-  if ((long long)nl.n_cells[0] * nl.n_cells[1] * nl.n_cells[2] > (1ll << 28)) {
+  bp.dx = (int)(cutoff / std::sqrt(dot(nx, nx))) + 1;
+  bp.dy = (int)(cutoff / std::sqrt(dot(ny, ny))) + 1;
+  bp.dz = (int)(cutoff / std::sqrt(dot(nz, nz))) + 1;
+  if ((long long)bp.n[0] * bp.n[1] * bp.n[2] > (1ll << 28)) {
     set_error("neighbors_update: too many cells (cell or cutoff out of range)");
     return GB_ERROR_DOMAIN;
   }
-  if ((2ll * nl.dx + 1) * (2ll * nl.dy + 1) * (2ll * nl.dz + 1) > 100000000ll) {
+  if ((2ll * bp.dx + 1) * (2ll * bp.dy + 1) * (2ll * bp.dz + 1) > 100000000ll) {
     set_error("neighbors_update: cutoff too large for this cell");
     return GB_ERROR_DOMAIN;
   }
-  BinParams bp;
-  std::memcpy(bp.rec, nl.rec, sizeof(bp.rec));
+  bp.cell_base = cell_base;
   bp.Amax = 0.0f;
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) {
-      bp.recf[a][k] = (float)nl.rec[a][k];
-      bp.Af[a][k] = (float)p.A[a][k];
+      bp.recf[a][k] = (float)bp.rec[a][k];
+      bp.A[a][k] = A[a][k];
+      bp.Af[a][k] = (float)A[a][k];
       bp.Amax = std::max(bp.Amax, std::fabs(bp.Af[a][k]));
     }
-  std::memcpy(bp.A, p.A, sizeof(bp.A));
-  for (int k = 0; k < 3; k++) {
-    bp.n[k] = nl.n_cells[k];
-    bp.pbc[k] = p.pbc[k];
-  }
-  bp.dx = nl.dx;
-  bp.dy = nl.dy;
-  bp.dz = nl.dz;
+  for (int k = 0; k < 3; k++) bp.pbc[k] = pbc[k];
   bp.cutoff_sq = cutoff * cutoff;
   bp.cutoff_f = (float)(cutoff * (1.0 + 1e-6));
   bp.cutoff_sq_lo = (float)(bp.cutoff_sq * (1.0 - 1e-6));
   bp.cutoff_sq_hi = (float)(bp.cutoff_sq * (1.0 + 1e-6));
+  return 0;
+}
 
+// Builds the list of nat atoms at r (device, (nat,3)) on the stream.  A
+// batch passes per-structure parameters bps (device) and the atoms'
+// structure ids sid; bp0 is then unused.
+int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
+             const BinParams *bps, const int *sid, int ncells, cudaStream_t stream) {
+  const bool batch = bps != nullptr;
   GB_CHECK(nl.pos4.ensure(sizeof(Pos4) * std::max(nat, 1)));
   if (nl.want_posff) GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * std::max(nat, 1)));
   nl.posff_valid = nl.want_posff;
@@ -809,23 +793,43 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   GB_CHECK(nl.seed.ensure(sizeof(int) * (nat + 1)));
   GB_CHECK(nl.stats.ensure(sizeof(int) * 8 + sizeof(int) * (size_t)(ncells + 1)));
   GB_CHECK(nl.hstats.ensure(sizeof(int) * 8));
-  int *status = nl.stats.as<int>();  // [0] maxz [1] flags [2] n_big
+  int *status = nl.stats.as<int>();  // [0] maxz [1] flags [2] n_big [3] max |coordinate|
   int *big_cells = status + 8;
   GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 8, stream));
   GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
   const int T = 256;
   const int nb = (nat + T - 1) / T;
+  float4 *posff = nl.want_posff ? nl.posff.as<float4>() : nullptr;
   if (nat > 0) {
-    nl_assign_cells<<<nb, T, 0, stream>>>(nat, p.r.as<double>(), bp, nl.pos4.as<Pos4>(),
-                                          nl.want_posff ? nl.posff.as<float4>() : nullptr,
-                                          nl.atom_cell.as<int>(), nl.atom_wrap.as<int>(),
-                                          nl.cell_count.as<int>(), status);
+    if (batch)
+      nl_assign_cells<true><<<nb, T, 0, stream>>>(
+          nat, r, bp0, bps, sid, nl.pos4.as<Pos4>(), posff, nl.atom_cell.as<int>(),
+          nl.atom_wrap.as<int>(), nl.cell_count.as<int>(), status);
+    else
+      nl_assign_cells<false><<<nb, T, 0, stream>>>(
+          nat, r, bp0, nullptr, nullptr, nl.pos4.as<Pos4>(), posff, nl.atom_cell.as<int>(),
+          nl.atom_wrap.as<int>(), nl.cell_count.as<int>(), status);
     note_launch();
   }
   GB_CHECK(exclusive_scan_i32(nl.cell_count.as<int>(), nl.cell_start.as<int>(), ncells,
                               nl.scan_tmp, stream));
   GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
   int *cell_atoms = nl.cell_atoms.as<int>();
+  auto pairs = [&](auto mode_tag, int *counts, const int *seed, int *nbr, int *shift,
+                   int2 *stage, int cap) {
+    constexpr int kMode = decltype(mode_tag)::value;
+    if (batch)
+      nl_pairs<kMode, true><<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, bp0, bps, sid, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
+          nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr, shift, stage, cap,
+          status);
+    else
+      nl_pairs<kMode, false><<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, bp0, nullptr, nullptr, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(),
+          nl.spos.as<float4>(), nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr,
+          shift, stage, cap, status);
+    note_launch();
+  };
   if (nat > 0) {
     nl_scatter<<<nb, T, 0, stream>>>(nat, nl.atom_cell.as<int>(), nl.cell_start.as<int>(),
                                      nl.cell_count.as<int>(), cell_atoms);
@@ -848,17 +852,12 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
     // the per-atom capacity; count-only pass otherwise.
     if (nl.stage_cap > 0) {
       GB_CHECK(nl.stage.ensure(sizeof(int2) * (size_t)nat * nl.stage_cap));
-      nl_pairs<kPairsCountStage><<<(nat + 127) / 128, 128, 0, stream>>>(
-          nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
-          nl.swrap.as<int>(), nl.cell_start.as<int>(), nl.counts.as<int>(), nullptr, nullptr,
-          nullptr, nl.stage.as<int2>(), nl.stage_cap, status);
+      pairs(std::integral_constant<int, kPairsCountStage>(), nl.counts.as<int>(), nullptr,
+            nullptr, nullptr, nl.stage.as<int2>(), nl.stage_cap);
     } else {
-      nl_pairs<kPairsCount><<<(nat + 127) / 128, 128, 0, stream>>>(
-          nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
-          nl.swrap.as<int>(), nl.cell_start.as<int>(), nl.counts.as<int>(), nullptr, nullptr,
-          nullptr, nullptr, 0, status);
+      pairs(std::integral_constant<int, kPairsCount>(), nl.counts.as<int>(), nullptr, nullptr,
+            nullptr, nullptr, 0);
     }
-    note_launch();
   }
   GB_CHECK(exclusive_scan_i32(nl.counts.as<int>(), nl.seed.as<int>(), nat, nl.scan_tmp, stream));
   // Read back: maxz, flags, n_big, total entries.
@@ -889,13 +888,11 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
       nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
                                                         nl.stage.as<int2>(), nl.nbr.as<int>(),
                                                         nl.shift.as<int>());
+      note_launch();
     } else {
-      nl_pairs<kPairsFill><<<(nat + 127) / 128, 128, 0, stream>>>(
-          nat, bp, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
-          nl.swrap.as<int>(), nl.cell_start.as<int>(), nullptr, nl.seed.as<int>(),
-          nl.nbr.as<int>(), nl.shift.as<int>(), nullptr, 0, status);
+      pairs(std::integral_constant<int, kPairsFill>(), nullptr, nl.seed.as<int>(),
+            nl.nbr.as<int>(), nl.shift.as<int>(), nullptr, 0);
     }
-    note_launch();
   }
   // Capacity of the next build's single pass: this build's maximum plus a
   // margin, while the stage stays below kStageMaxBytes.
@@ -906,12 +903,45 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   GB_CUDA(cudaGetLastError());
   nl.nentries = total;
   nl.maxz = maxz;
+  return 0;
+}
+
+int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
+  if (!p.cell_set) {
+    set_error("neighbors_update: cell not set");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (p.nat > 0 && !p.r.p) {
+    set_error("neighbors_update: positions not set");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (nl.valid && nl.built_for == &p && nl.built_pos_rev == p.pos_rev &&
+      nl.built_cell_rev == p.cell_rev && nl.built_nat == p.nat && nl.cutoff == nl.interaction_range)
+    return 0;
+  // cutoff = interaction_range + verlet_shell (0 on the Python path, :478)
+  const double cutoff = nl.interaction_range;
+  if (!(cutoff > 0.0)) {
+    set_error("Cutoff needs to be larger than zero.");
+    return GB_ERROR_ARGUMENT;
+  }
+  nl.valid = false;
+  nl.rev_valid = false;
+  nl.rev_pending = false;
+  BinParams bp;
+  GB_CHECK(bin_params(p.A, p.B, p.pbc, cutoff, 0, bp));
+  for (int k = 0; k < 3; k++) nl.n_cells[k] = bp.n[k];
+  std::memcpy(nl.rec, bp.rec, sizeof(nl.rec));
+  nl.dx = bp.dx;
+  nl.dy = bp.dy;
+  nl.dz = bp.dz;
+  const int ncells = bp.n[0] * bp.n[1] * bp.n[2];
+  GB_CHECK(nl_build(nl, p.nat, p.r.as<double>(), bp, nullptr, nullptr, ncells, stream));
   nl.cutoff = cutoff;
   nl.valid = true;
   nl.built_for = &p;
   nl.built_pos_rev = p.pos_rev;
   nl.built_cell_rev = p.cell_rev;
-  nl.built_nat = nat;
+  nl.built_nat = p.nat;
   return 0;
 }
 
@@ -1019,14 +1049,9 @@ int gb_particles_set_cell(gb_particles_t *h, const double *cell, const int *pbc)
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) A[a][k] = cell[3 * k + a];
   double B[3][3];
-  for (int c = 0; c < 3; c++) {
-    double e[3] = {0, 0, 0}, x[3];
-    e[c] = 1.0;
-    if (gauss_solve3(A, e, x) != 0) {
-      set_error("Gauss elimination failed (singular cell).");
-      return GB_ERROR_ARGUMENT;
-    }
-    for (int a = 0; a < 3; a++) B[a][c] = x[a];
+  if (cell_inverse(A, B) != 0) {
+    set_error("Gauss elimination failed (singular cell).");
+    return GB_ERROR_ARGUMENT;
   }
   bool changed = !p.cell_set || std::memcmp(A, p.A, sizeof(A)) != 0;
   std::memcpy(p.A, A, sizeof(A));

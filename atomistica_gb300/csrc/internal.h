@@ -101,6 +101,22 @@ constexpr int kMaxShift = 511;
 // Largest staging buffer of the single-pass neighbour build (bytes).
 constexpr size_t kStageMaxBytes = size_t(2) << 30;
 
+// Binning and pair-search parameters of one periodic cell.
+struct BinParams {
+  double rec[3][3];
+  float recf[3][3];  // rec rounded to float (cell prefilter)
+  double A[3][3];
+  float Af[3][3];  // A rounded to float, and max |A_ak|
+  float Amax;
+  int n[3];
+  int pbc[3];
+  int dx, dy, dz;
+  int cell_base;  // first cell of this structure in a batch (0 otherwise)
+  double cutoff_sq;
+  float cutoff_f;                    // cutoff rounded up to float
+  float cutoff_sq_lo, cutoff_sq_hi;  // float bracket of cutoff^2
+};
+
 // Position padded to 32 bytes: one DRAM sector per gather.
 struct __align__(32) Pos4 {
   double x, y, z, w;
@@ -160,6 +176,16 @@ struct Neighbors {
 // Builds/refreshes the list for p if positions or cell changed
 // (neighbors_update, :430-456).
 int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream);
+// Binning parameters of one cell (rows of A: Abox(a, k) with column k the
+// lattice vector k; B = A^-1); cell_base offsets the cell numbers.
+int bin_params(const double A[3][3], const double B[3][3], const int pbc[3], double cutoff,
+               int cell_base, BinParams &bp);
+// 3x3 inverse by the reference's Gauss elimination (0 on success).
+int cell_inverse(const double A[3][3], double B[3][3]);
+// List build of nat atoms at r (device (nat,3)); a batch passes per-structure
+// parameters bps (device) and per-atom structure ids sid.
+int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
+             const BinParams *bps, const int *sid, int ncells, cudaStream_t stream);
 // Reverse-entry index of the list.  With sync = false the symmetry check is
 // deferred: call neighbors_check_reverse (stream = nullptr once the caller
 // has synchronised the stream itself) before rev is read.
