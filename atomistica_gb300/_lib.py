@@ -54,6 +54,13 @@ SIGNATURES = [
     ("gb_tabulated_alloy_eam_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_tabulated_alloy_eam_energy_and_forces", _I, [_P] * 10 + [_P]),
     ("gb_tabulated_alloy_eam_table", _I, [_P, _I, _I, _P, _P]),
+    ("gb_batch_new", _I, [_P]),
+    ("gb_batch_free", None, [_P]),
+    ("gb_batch_set_stream", _I, [_P, _P]),
+    ("gb_batch_set_structures", _I, [_P, _I, _P, _P, _P, _P]),
+    ("gb_batch_set_positions", _I, [_P, _P]),
+    ("gb_batch_get_nat", _I, [_P]),
+    ("gb_batch_energy_and_forces", _I, [_P, _P, _P, _P, _P]),
     ("gb_potential_last_timing", _I, [_P, _P]),
     ("gb_potential_last_stats", _I, [_P, _P]),
     ("gb_potential_set_tile_atoms", _I, [_P, _I]),

@@ -120,6 +120,8 @@ int check_kumagai(const gb_kumagai_params_t &p) {
   return 0;
 }
 
+}  // namespace
+
 int pot_nel(const Potential &pot) {
   if (pot.kind == kTersoff) return pot.tp.nel;
   if (pot.kind == kKumagai) return 1;
@@ -142,6 +144,9 @@ cudaStream_t pot_stream(Potential &pot) {
   }
   return pot.stream;
 }
+
+namespace {
+
 
 // Z -> internal element index (Z2db, default_compute_func.f90:62-66).
 int update_element_map(Potential &pot, const Particles &p) {

@@ -1,0 +1,411 @@
+// Batched bond-order evaluation: many independent periodic structures of
+// uneven size and shape (each with its own triclinic cell and pbc flags) in
+// one neighbour build and one tile-kernel launch.
+//
+//   * atoms of all structures are concatenated; sid[i] is the structure of
+//     atom i; each structure has its own binning parameters (its cells are
+//     numbered consecutively after the previous structure's), so the cell
+//     lists are segmented and one pair-search launch covers every structure;
+//   * bond-order tiles never cross a structure and carry their structure's
+//     cell; the per-tile energy/virial rows are summed per structure;
+//   * forces come from the same gather as a single structure.
+//
+// Per structure the results equal a separate evaluation of that structure
+// (the same neighbour entries in the same order, the same kernels); the
+// reference has no batched entry point.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bop_math.h"
+#include "potential.h"
+
+namespace gb {
+
+struct Batch {
+  int nstruct = 0, nat = 0;
+  std::vector<int> atom_off;  // nstruct + 1
+  std::vector<double> A;      // 9 per structure: A[a][k], column k = lattice vector k
+  std::vector<double> B;      // inverses
+  std::vector<int> pbc;       // 3 per structure
+  std::vector<int> hZ;        // nat
+  uint64_t geom_rev = 0, pos_rev = 0;
+  DevBuf r, sid, bps, Acells, Acells_ff, tiles, red_seg, el;
+  HostBuf hseg;
+  // cached derived state
+  uint64_t built_geom = ~0ull, built_pos = ~0ull, el_geom = ~0ull;
+  const Potential *el_pot = nullptr;
+  double built_cutoff = -1.0;
+  int ncells = 0, tiles_apt = 0, ntiles = 0;
+  int64_t tiles_nentries = -1;
+  Neighbors nl;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+};
+
+namespace {
+
+cudaStream_t batch_stream(Batch &b) {
+  if (!b.stream) {
+    cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking);
+    b.own_stream = true;
+  }
+  return b.stream;
+}
+
+// Element index of every atom for this potential (Z2db).
+int batch_elements(Batch &b, Potential &pot, cudaStream_t s) {
+  if (b.el_pot == &pot && b.el_geom == b.geom_rev && b.el.p) return 0;
+  const int nel = pot_nel(pot);
+  std::vector<int> el(std::max(b.nat, 1), -1);
+  for (int i = 0; i < b.nat; i++)
+    for (int q = 0; q < nel; q++)
+      if (b.hZ[i] == pot_Z(pot, q)) el[i] = q;
+  GB_CHECK(b.el.ensure(sizeof(int) * el.size()));
+  GB_CUDA(cudaMemcpyAsync(b.el.p, el.data(), sizeof(int) * el.size(), cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  b.el_pot = &pot;
+  b.el_geom = b.geom_rev;
+  return 0;
+}
+
+// Interaction range: the largest r2 over the element pairs present
+// (default_bind_to_func.f90:123-144).
+double batch_cutoff(const Batch &b, const Potential &pot) {
+  std::vector<int> zs(b.hZ.begin(), b.hZ.end());
+  std::sort(zs.begin(), zs.end());
+  zs.erase(std::unique(zs.begin(), zs.end()), zs.end());
+  const int nel = pot_nel(pot);
+  auto dbidx = [&](int Z) {
+    for (int q = 0; q < nel; q++)
+      if (pot_Z(pot, q) == Z) return q;
+    return -1;
+  };
+  double cut = 0.0;
+  for (int zi : zs)
+    for (int zj : zs) {
+      const int ii = dbidx(zi), jj = dbidx(zj);
+      if (ii < 0 || jj < 0) continue;
+      const int t = pair_index(ii, jj, nel);
+      cut = std::max(cut, pot.kind == kTersoff ? pot.tp.r2[t] : pot.kp.r2[t]);
+    }
+  return cut;
+}
+
+// Per-structure binning parameters for the cutoff (cells numbered in
+// structure order).
+int batch_binning(Batch &b, double cutoff, cudaStream_t s) {
+  if (b.built_geom == b.geom_rev && b.built_cutoff == cutoff) return 0;
+  std::vector<BinParams> h(std::max(b.nstruct, 1));
+  long long base = 0;
+  for (int q = 0; q < b.nstruct; q++) {
+    double A[3][3], B[3][3];
+    std::memcpy(A, &b.A[9 * q], sizeof(A));
+    std::memcpy(B, &b.B[9 * q], sizeof(B));
+    GB_CHECK(bin_params(A, B, &b.pbc[3 * q], cutoff, (int)base, h[q]));
+    base += (long long)h[q].n[0] * h[q].n[1] * h[q].n[2];
+    if (base > (1ll << 28)) {
+      set_error("batch: too many cells in total (cells or cutoff out of range)");
+      return GB_ERROR_DOMAIN;
+    }
+  }
+  GB_CHECK(b.bps.ensure(sizeof(BinParams) * h.size()));
+  GB_CUDA(cudaMemcpyAsync(b.bps.p, h.data(), sizeof(BinParams) * h.size(),
+                          cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  b.ncells = (int)base;
+  b.built_geom = b.geom_rev;
+  b.built_cutoff = cutoff;
+  b.nl.valid = false;
+  return 0;
+}
+
+// Tiles of at most apt atoms inside each structure; per-structure tile
+// offsets for the energy/virial sums.
+int batch_tiles(Batch &b, int apt, cudaStream_t s) {
+  if (b.tiles_apt == apt && b.tiles_nentries == b.nl.nentries && b.ntiles > 0 &&
+      b.built_geom == b.geom_rev)
+    return 0;
+  std::vector<int> atom0, strct, seg(b.nstruct + 1, 0);
+  for (int q = 0; q < b.nstruct; q++) {
+    seg[q] = (int)strct.size();
+    for (int a = b.atom_off[q]; a < b.atom_off[q + 1]; a += apt) {
+      atom0.push_back(a);
+      strct.push_back(q);
+    }
+  }
+  seg[b.nstruct] = (int)strct.size();
+  const int nt = (int)strct.size();
+  atom0.push_back(b.nat);
+  // layout: tile_atom0 [nt + 1] | tile_struct [nt] | seg [nstruct + 1]
+  const size_t n = atom0.size() + strct.size() + seg.size();
+  GB_CHECK(b.tiles.ensure(sizeof(int) * n));
+  int *d = b.tiles.as<int>();
+  GB_CUDA(cudaMemcpyAsync(d, atom0.data(), sizeof(int) * atom0.size(), cudaMemcpyHostToDevice, s));
+  if (nt)
+    GB_CUDA(cudaMemcpyAsync(d + atom0.size(), strct.data(), sizeof(int) * strct.size(),
+                            cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaMemcpyAsync(d + atom0.size() + strct.size(), seg.data(), sizeof(int) * seg.size(),
+                          cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  b.tiles_apt = apt;
+  b.ntiles = nt;
+  b.tiles_nentries = b.nl.nentries;
+  return 0;
+}
+
+}  // namespace
+
+int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, double *wpot) {
+  if (!epot || !f || !wpot) {
+    set_error("batch_energy_and_forces: epot, f and wpot are required");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (pot.kind == kEAM) {
+    set_error("batch_energy_and_forces: batches support the bond-order potentials");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (b.nstruct == 0) return 0;
+  if (b.nat > 0 && !b.r.p) {
+    set_error("batch_energy_and_forces: positions not set");
+    return GB_ERROR_ARGUMENT;
+  }
+  cudaStream_t s = pot_stream(pot);
+  if (b.stream && b.stream != s) {
+    GB_CUDA(cudaEventRecord(pot.ev[3], b.stream));
+    GB_CUDA(cudaStreamWaitEvent(s, pot.ev[3], 0));
+  }
+  GB_CUDA(cudaEventRecord(pot.ev[0], s));
+  const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  GB_CHECK(batch_elements(b, pot, s));
+  const double cutoff = batch_cutoff(b, pot);
+  if (!(cutoff > 0.0)) {
+    set_error("batch_energy_and_forces: no element of the batch is known to the potential");
+    return GB_ERROR_ARGUMENT;
+  }
+  GB_CHECK(batch_binning(b, cutoff, s));
+  if (mixed) b.nl.want_posff = true;
+  if (!(b.nl.valid && b.built_pos == b.pos_rev && b.nl.posff_valid == b.nl.want_posff)) {
+    b.nl.valid = false;
+    b.nl.rev_valid = false;
+    b.nl.rev_pending = false;
+    BinParams dummy{};
+    GB_CHECK(nl_build(b.nl, b.nat, b.r.as<double>(), dummy, b.bps.as<BinParams>(),
+                      b.sid.as<int>(), b.ncells, s));
+    b.nl.cutoff = cutoff;
+    b.nl.valid = true;
+    b.built_pos = b.pos_rev;
+  }
+  GB_CUDA(cudaEventRecord(pot.ev[1], s));
+  GB_CHECK(batch_tiles(b, bop_batch_apt(b.nl.maxz), s));
+
+  // Outputs: forces accumulated (host arrays staged), per-structure sums.
+  const size_t nf = 3 * (size_t)b.nat;
+  double *fd = f;
+  const bool f_host = b.nat > 0 && !is_device_ptr(f);
+  if (f_host) {
+    GB_CHECK(pot.out_f.ensure(sizeof(double) * std::max<size_t>(nf, 1)));
+    fd = pot.out_f.as<double>();
+    GB_CUDA(cudaMemcpyAsync(fd, f, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
+  }
+  GB_CHECK(pot.red.ensure(sizeof(double) * 16));
+  GB_CHECK(b.red_seg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1)));
+  Outputs o;
+  o.f = fd;
+  o.red = pot.red.as<double>();
+  o.status = reinterpret_cast<int *>(o.red + 12);
+  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s));
+
+  BopSystem sys;
+  sys.nat = b.nat;
+  const int *t = b.tiles.as<int>();
+  sys.tile_atom0 = t;
+  sys.tile_struct = t + b.ntiles + 1;
+  sys.seg = t + 2 * b.ntiles + 1;
+  sys.nseg = b.nstruct;
+  sys.red_seg = b.red_seg.as<double>();
+  sys.Acells = b.Acells.as<double>();
+  sys.Acells_ff = reinterpret_cast<const float2 *>(b.Acells_ff.p);
+  sys.ntiles = b.ntiles;
+  sys.apt = b.tiles_apt;
+  // the bond-order kernels take the element map from the potential
+  GB_CHECK(pot.el.ensure(sizeof(int) * std::max(b.nat, 1)));
+  GB_CUDA(cudaMemcpyAsync(pot.el.p, b.el.p, sizeof(int) * std::max(b.nat, 1),
+                          cudaMemcpyDeviceToDevice, s));
+  pot.el_for = nullptr;  // the potential's map no longer belongs to bound particles
+  GB_CHECK(bop_run(pot, sys, b.nl, o, false, false));
+  GB_CUDA(cudaEventRecord(pot.ev[2], s));
+  if (f_host) GB_CUDA(cudaMemcpyAsync(f, fd, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
+  GB_CHECK(b.hseg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1) + 64));
+  double *hs = b.hseg.as<double>();
+  GB_CUDA(cudaMemcpyAsync(hs, b.red_seg.p, sizeof(double) * 10 * b.nstruct,
+                          cudaMemcpyDeviceToHost, s));
+  GB_CHECK(pot.hred.ensure(sizeof(double) * 16));
+  double *hr = pot.hred.as<double>();
+  GB_CUDA(cudaMemcpyAsync(hr, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaEventRecord(pot.ev[3], s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  GB_CUDA(cudaGetLastError());
+  float ms[4] = {0, 0, 0, 0};
+  cudaEventElapsedTime(&ms[0], pot.ev[0], pot.ev[1]);
+  cudaEventElapsedTime(&ms[1], pot.ev[1], pot.ev[2]);
+  cudaEventElapsedTime(&ms[2], pot.ev[0], pot.ev[3]);
+  cudaEventElapsedTime(&ms[3], pot.kev[0], pot.kev[1]);
+  cudaGetLastError();
+  for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
+  const int st = reinterpret_cast<const int *>(hr + 12)[0];
+  pot.last_status = st;
+  pot.last_hot = reinterpret_cast<const int *>(hr + 12)[2];
+  pot.last_bonds = b.nl.nentries;
+  if (st & 2) {
+    set_error("Internal error: bond-order tile plan mismatch.");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  // epot set, wpot accumulated, per structure (as energy_and_forces)
+  const bool ed = is_device_ptr(epot), wd = is_device_ptr(wpot);
+  std::vector<double> e(b.nstruct), w(9 * (size_t)b.nstruct);
+  if (wd)
+    GB_CUDA(cudaMemcpy(w.data(), wpot, sizeof(double) * w.size(), cudaMemcpyDeviceToHost));
+  else
+    std::memcpy(w.data(), wpot, sizeof(double) * w.size());
+  for (int q = 0; q < b.nstruct; q++) {
+    e[q] = hs[10 * q];
+    for (int c = 0; c < 9; c++) w[9 * q + c] += hs[10 * q + 1 + c];
+  }
+  if (ed)
+    GB_CUDA(cudaMemcpy(epot, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice));
+  else
+    std::memcpy(epot, e.data(), sizeof(double) * e.size());
+  if (wd)
+    GB_CUDA(cudaMemcpy(wpot, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
+  else
+    std::memcpy(wpot, w.data(), sizeof(double) * w.size());
+  return 0;
+}
+
+}  // namespace gb
+
+// ===========================================================================
+// C-ABI.
+// ===========================================================================
+using namespace gb;
+
+struct gb_batch {
+  gb::Batch b;
+};
+
+extern "C" {
+
+int gb_batch_new(gb_batch_t **out) {
+  clear_error();
+  if (!out) return GB_ERROR_ARGUMENT;
+  *out = new gb_batch;
+  return 0;
+}
+
+void gb_batch_free(gb_batch_t *h) {
+  if (!h) return;
+  if (h->b.own_stream && h->b.stream) cudaStreamDestroy(h->b.stream);
+  delete h;
+}
+
+int gb_batch_set_stream(gb_batch_t *h, void *stream) {
+  if (!h) return GB_ERROR_ARGUMENT;
+  if (h->b.own_stream && h->b.stream) cudaStreamDestroy(h->b.stream);
+  h->b.stream = static_cast<cudaStream_t>(stream);
+  h->b.own_stream = false;
+  return 0;
+}
+
+int gb_batch_set_structures(gb_batch_t *h, int nstruct, const int *nat, const double *cells,
+                            const int *pbc, const int *Z) {
+  clear_error();
+  if (!h || nstruct < 0 || (nstruct > 0 && (!nat || !cells))) return GB_ERROR_ARGUMENT;
+  Batch &b = h->b;
+  std::vector<int> off(nstruct + 1, 0);
+  for (int q = 0; q < nstruct; q++) {
+    if (nat[q] < 0) {
+      set_error("batch: negative atom count");
+      return GB_ERROR_ARGUMENT;
+    }
+    off[q + 1] = off[q] + nat[q];
+  }
+  const int total = off[nstruct];
+  if (total > 0 && !Z) return GB_ERROR_ARGUMENT;
+  std::vector<double> A(9 * (size_t)nstruct), B(9 * (size_t)nstruct);
+  std::vector<int> pb(3 * (size_t)nstruct, 1);
+  for (int q = 0; q < nstruct; q++) {
+    double a[3][3], bi[3][3];
+    // cells: per structure 3 rows = lattice vectors (C layout), A[a][k] = cell[k][a]
+    for (int x = 0; x < 3; x++)
+      for (int k = 0; k < 3; k++) a[x][k] = cells[9 * (size_t)q + 3 * k + x];
+    if (cell_inverse(a, bi) != 0) {
+      set_error("Gauss elimination failed (singular cell) for structure " + std::to_string(q));
+      return GB_ERROR_ARGUMENT;
+    }
+    std::memcpy(&A[9 * (size_t)q], a, sizeof(a));
+    std::memcpy(&B[9 * (size_t)q], bi, sizeof(bi));
+    if (pbc)
+      for (int k = 0; k < 3; k++) pb[3 * (size_t)q + k] = pbc[3 * (size_t)q + k] != 0;
+  }
+  cudaStream_t s = batch_stream(b);
+  std::vector<int> sid(std::max(total, 1), 0);
+  for (int q = 0; q < nstruct; q++)
+    for (int i = off[q]; i < off[q + 1]; i++) sid[i] = q;
+  std::vector<float2> aff(9 * (size_t)std::max(nstruct, 1));
+  for (size_t k = 0; k < A.size(); k++) {
+    const float hi = (float)A[k];
+    aff[k] = make_float2(hi, (float)(A[k] - (double)hi));
+  }
+  GB_CHECK(b.sid.ensure(sizeof(int) * sid.size()));
+  GB_CHECK(b.Acells.ensure(sizeof(double) * std::max<size_t>(A.size(), 9)));
+  GB_CHECK(b.Acells_ff.ensure(sizeof(float2) * aff.size()));
+  GB_CHECK(b.r.ensure(sizeof(double) * 3 * std::max(total, 1)));
+  GB_CUDA(cudaMemcpyAsync(b.sid.p, sid.data(), sizeof(int) * sid.size(), cudaMemcpyHostToDevice,
+                          s));
+  if (!A.empty())
+    GB_CUDA(cudaMemcpyAsync(b.Acells.p, A.data(), sizeof(double) * A.size(),
+                            cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaMemcpyAsync(b.Acells_ff.p, aff.data(), sizeof(float2) * aff.size(),
+                          cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  b.nstruct = nstruct;
+  b.nat = total;
+  b.atom_off = off;
+  b.A = A;
+  b.B = B;
+  b.pbc = pb;
+  b.hZ.assign(Z ? Z : nullptr, Z ? Z + total : nullptr);
+  b.geom_rev++;
+  b.pos_rev++;
+  b.nl.valid = false;
+  b.ntiles = 0;
+  return 0;
+}
+
+int gb_batch_set_positions(gb_batch_t *h, const double *r) {
+  clear_error();
+  if (!h || (!r && h->b.nat > 0)) return GB_ERROR_ARGUMENT;
+  Batch &b = h->b;
+  if (b.nat > 0) {
+    cudaStream_t s = batch_stream(b);
+    GB_CUDA(cudaMemcpyAsync(b.r.p, r, sizeof(double) * 3 * b.nat, cudaMemcpyDefault, s));
+    if (!is_device_ptr(r)) GB_CUDA(cudaStreamSynchronize(s));
+  }
+  b.pos_rev++;
+  return 0;
+}
+
+int gb_batch_get_nat(const gb_batch_t *h) { return h ? h->b.nat : -1; }
+
+int gb_batch_energy_and_forces(gb_batch_t *h, gb_potential_t *pot, double *epot, double *f,
+                               double *wpot) {
+  clear_error();
+  if (!h || !pot) return GB_ERROR_ARGUMENT;
+  return batch_energy_and_forces(h->b, pot->pot, epot, f, wpot);
+}
+
+}  // extern "C"

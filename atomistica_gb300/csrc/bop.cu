@@ -70,7 +70,26 @@ struct BopArgs {
   double *wbond;    // 9 per bond (per-atom virial only)
   double *frbond;   // 3 per bond (f_per_bond only)
   double *tile_part;  // 10 per tile
+  // Batches of structures: tile t covers atoms [tile_atom0[t], tile_atom0[t+1])
+  // of structure tile_struct[t], whose cell is Acells[9 s ..] (FP64) /
+  // Acells_ff (float-float pairs); the mixed kernel then writes one partial
+  // row per tile.  nullptr for a single structure (uniform tiles of apt).
+  const int *tile_atom0 = nullptr;
+  const int *tile_struct = nullptr;
+  const double *Acells = nullptr;
+  const float2 *Acells_ff = nullptr;
+  int ntiles = 0;
 };
+
+__device__ __forceinline__ void tile_range(const BopArgs &a, int tile, int &a0, int &a1) {
+  if (a.tile_atom0) {
+    a0 = a.tile_atom0[tile];
+    a1 = a.tile_atom0[tile + 1];
+  } else {
+    a0 = tile * a.apt;
+    a1 = min(a0 + a.apt, a.nat);
+  }
+}
 
 // Shared-memory layout of one tile (nbt bonds, ntrip (ij, ik) slots).
 struct SmemLayout {
@@ -238,10 +257,14 @@ __global__ void __launch_bounds__(kBopThreads)
     bop_tile(const BopArgs a, const Pot pot, int max_nbt, int max_ntrip, int *status) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ double red_scratch[(kBopThreads / 32) * 9];
+  __shared__ double sA[3][3];  // this tile's cell
   static_assert(std::is_same<R, double>::value, "bop_tile is the FP64 form");
   const int tid = threadIdx.x;
-  const int a0 = blockIdx.x * a.apt;
-  const int a1 = min(a0 + a.apt, a.nat);
+  int a0, a1;
+  tile_range(a, blockIdx.x, a0, a1);
+  if (tid < 9)
+    sA[tid / 3][tid % 3] = a.Acells ? a.Acells[9 * a.tile_struct[blockIdx.x] + tid]
+                                    : a.A[tid / 3][tid % 3];
   const int na = a1 - a0;
   const int b0 = a.seed[a0];
   const int nbt = a.seed[a1] - b0;
@@ -300,9 +323,9 @@ __global__ void __launch_bounds__(kBopThreads)
         const double sx = s0, sy = s1, sz = s2;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          double as = __dmul_rn(a.A[c][0], sx);
-          as = __dadd_rn(as, __dmul_rn(a.A[c][1], sy));
-          as = __dadd_rn(as, __dmul_rn(a.A[c][2], sz));
+          double as = __dmul_rn(sA[c][0], sx);
+          as = __dadd_rn(as, __dmul_rn(sA[c][1], sy));
+          as = __dadd_rn(as, __dmul_rn(sA[c][2], sz));
           rij[c] = __dsub_rn(rij[c], as);
         }
       }
@@ -479,11 +502,12 @@ __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__r
 }
 
 // Tile plan: per tile bond count and sum of z^2.
-__global__ void bop_plan(int nat, int apt, const int *__restrict__ seed, int *__restrict__ out) {
+__global__ void bop_plan(int nat, int apt, int ntiles, const int *__restrict__ tile_atom0,
+                         const int *__restrict__ seed, int *__restrict__ out) {
   const int tile = blockIdx.x * blockDim.x + threadIdx.x;
-  const int a0 = tile * apt;
-  if (a0 >= nat) return;
-  const int a1 = min(a0 + apt, nat);
+  if (tile >= ntiles) return;
+  const int a0 = tile_atom0 ? tile_atom0[tile] : tile * apt;
+  const int a1 = tile_atom0 ? tile_atom0[tile + 1] : min(a0 + apt, nat);
   int ntrip = 0;
   for (int q = a0; q < a1; q++) {
     const int z = seed[q + 1] - seed[q];
@@ -616,6 +640,39 @@ int launch_gather(bool mixed, int nat, const int *seed, const int *rev, const do
 
 }  // namespace
 
+// Per-segment sums: block q adds rows [seg[q], seg[q+1]) in order.
+__global__ void reduce_segments_kernel(const double *__restrict__ part,
+                                       const int *__restrict__ seg, double *__restrict__ out) {
+  __shared__ double sh[2 * kRedCols];
+  const int r0 = seg[blockIdx.x], r1 = seg[blockIdx.x + 1];
+  double acc[kRedCols];
+#pragma unroll
+  for (int c = 0; c < kRedCols; c++) acc[c] = 0.0;
+  for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < kRedCols; c++) acc[c] += part[(size_t)t * kRedCols + c];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < kRedCols; c++) {
+    double x = acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[wid * kRedCols + c] = x;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < kRedCols)
+    out[(size_t)blockIdx.x * kRedCols + threadIdx.x] =
+        sh[threadIdx.x] + (blockDim.x > 32 ? sh[kRedCols + threadIdx.x] : 0.0);
+}
+
+int reduce_segments(const double *part, const int *seg, int nseg, double *out, cudaStream_t s) {
+  if (nseg <= 0) return 0;
+  reduce_segments_kernel<<<nseg, 64, 0, s>>>(part, seg, out);
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 size_t reduce_stage_bytes(int nrows) {
   return sizeof(double) * kRedCols * (size_t)((nrows + kRedRowsPerBlock - 1) / kRedRowsPerBlock);
 }
@@ -644,24 +701,29 @@ int reduce_partials(const double *part, int nrows, int nc, double *red, double *
 
 static const size_t kSmemBudget = 200 * 1024;
 
-int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
-                bool want_wat, bool want_pb) {
+int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
+            bool want_wat, bool want_pb) {
   cudaStream_t s = pot.stream;
-  const int nat = p.nat;
+  const int nat = sys.nat;
+  const bool batch = sys.tile_atom0 != nullptr;
   if (nat == 0) {
     GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
+    if (batch && sys.nseg > 0)
+      GB_CUDA(cudaMemsetAsync(sys.red_seg, 0, sizeof(double) * 10 * sys.nseg, s));
     return 0;
   }
-  GB_CHECK(neighbors_build_reverse(nl, p, s, false));  // checked after the plan read-back
+  GB_CHECK(neighbors_build_reverse(nl, nat, s, false));  // checked after the plan read-back
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
   // Atoms per tile: largest power of two <= kMaxApt whose worst tile fits.
   const int maxz = std::max(nl.maxz, 1);
-  int apt = kMaxApt;
+  int apt = batch ? sys.apt : kMaxApt;
   auto fits = [&](int aptc) {
     const size_t worst = bop_smem_bytes<double>(aptc * maxz, aptc * maxz * maxz);
     return worst <= kSmemBudget;
   };
-  if (pot.tile_request > 0) {
+  if (batch) {
+    // tiles were cut by the caller (bop_batch_apt)
+  } else if (pot.tile_request > 0) {
     apt = std::min(pot.tile_request, kMaxApt);
     while (apt > 1 && !fits(apt)) apt >>= 1;
   } else {
@@ -676,7 +738,7 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
               " neighbours within the cutoff, more than the bond-order kernel supports.");
     return GB_ERROR_CAPACITY;
   }
-  const int ntiles = (nat + apt - 1) / apt;
+  const int ntiles = batch ? sys.ntiles : (nat + apt - 1) / apt;
   const int64_t nb = std::max<int64_t>(nl.nentries, 1);
   GB_CHECK(pot.bond_G.ensure(sizeof(double) * 3 * nb));
   GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
@@ -686,7 +748,8 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   // Plan: exact max bonds / triplets per tile.
   int *plan = reinterpret_cast<int *>(pot.tile_part.as<double>() + 10 * (size_t)ntiles);
   GB_CUDA(cudaMemsetAsync(plan, 0, sizeof(int) * 4, s));
-  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, nl.seed.as<int>(), plan);
+  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, sys.tile_atom0,
+                                                nl.seed.as<int>(), plan);
   note_launch();
   GB_CHECK(pot.hred.ensure(64));
   int *hplan = pot.hred.as<int>();
@@ -704,7 +767,12 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   args.nbr = nl.nbr.as<int>();
   args.shift = nl.shift.as<int>();
   args.mask = o.mask;
-  std::memcpy(args.A, p.A, sizeof(args.A));
+  std::memcpy(args.A, sys.A, sizeof(args.A));
+  args.tile_atom0 = sys.tile_atom0;
+  args.tile_struct = sys.tile_struct;
+  args.Acells = sys.Acells;
+  args.Acells_ff = sys.Acells_ff;
+  args.ntiles = ntiles;
   args.G = pot.bond_G.as<double>();
   // per-bond energies only when per-atom or per-bond energies are requested
   args.ebond = (o.epot_per_at || o.epot_per_bond) ? pot.bond_e.as<double>() : nullptr;
@@ -738,10 +806,32 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
                          args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
-  GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(rows) + 64));
-  GB_CHECK(reduce_partials(args.tile_part, rows, 10, o.red, pot.red_stage.as<double>(), s));
+  if (batch) {
+    GB_CHECK(reduce_segments(args.tile_part, sys.seg, sys.nseg, sys.red_seg, s));
+    GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
+  } else {
+    GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(rows) + 64));
+    GB_CHECK(reduce_partials(args.tile_part, rows, 10, o.red, pot.red_stage.as<double>(), s));
+  }
   pot.tile_atoms = apt;
   return 0;
+}
+
+int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
+                bool want_wat, bool want_pb) {
+  BopSystem sys;
+  sys.nat = p.nat;
+  std::memcpy(sys.A, p.A, sizeof(sys.A));
+  return bop_run(pot, sys, nl, o, want_wat, want_pb);
+}
+
+int bop_batch_apt(int maxz) {
+  int apt = kMaxApt;
+  while (apt > 1 && bop_smem_bytes<double>(apt * std::max(maxz, 1),
+                                           apt * std::max(maxz, 1) * std::max(maxz, 1)) >
+                        kSmemBudget)
+    apt >>= 1;
+  return apt;
 }
 
 }  // namespace gb
@@ -977,7 +1067,7 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   }
   const int ntiles = (nat + apt - 1) / apt;
   int *plan = status + 4;
-  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, seed32, plan);
+  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, nullptr, seed32, plan);
   note_launch();
   int hp[2] = {0, 0};
   GB_CUDA(cudaMemcpyAsync(hp, plan, sizeof(hp), cudaMemcpyDeviceToHost, s));

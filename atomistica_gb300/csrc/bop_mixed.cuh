@@ -533,6 +533,7 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
   __shared__ ff red_scratch[(kMxThreads / 32) * 10];
   __shared__ ff s_exp[256], s_sin[257], s_cos[257];
   __shared__ int s_nhot;
+  __shared__ ff sAf[9];
   const int tid = threadIdx.x;
   for (int q = tid; q < 256; q += kMxThreads)
     s_exp[q] = ff_make(kFfExp2Tab[2 * q], kFfExp2Tab[2 * q + 1]);
@@ -546,12 +547,18 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
   float wacc[9];
 #pragma unroll
   for (int c = 0; c < 9; c++) wacc[c] = 0.0f;
-  const int ntiles = (a.nat + a.apt - 1) / a.apt;
+  const int ntiles = a.tile_atom0 ? a.ntiles : (a.nat + a.apt - 1) / a.apt;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     __syncthreads();  // the previous tile is done with shared memory
     if (tid == 0) s_nhot = 0;
-    const int a0 = tile * a.apt;
-    const int a1 = min(a0 + a.apt, a.nat);
+    if (tid < 9) {  // this tile's cell
+      const float2 v = a.Acells_ff ? a.Acells_ff[9 * a.tile_struct[tile] + tid]
+                                   : make_float2(mp.A[tid / 3][tid % 3].hi,
+                                                 mp.A[tid / 3][tid % 3].lo);
+      sAf[tid] = ff_make(v.x, v.y);
+    }
+    int a0, a1;
+    tile_range(a, tile, a0, a1);
     const int na = a1 - a0;
     const int b0 = a.seed[a0];
     const int nbt = a.seed[a1] - b0;
@@ -618,9 +625,9 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
           const float sx = (float)s0, sy = (float)s1, sz = (float)s2;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
-            ff as = ff_mulf(mp.A[c][0], sx);
-            as = ff_add(as, ff_mulf(mp.A[c][1], sy));
-            as = ff_add(as, ff_mulf(mp.A[c][2], sz));
+            ff as = ff_mulf(sAf[3 * c], sx);
+            as = ff_add(as, ff_mulf(sAf[3 * c + 1], sy));
+            as = ff_add(as, ff_mulf(sAf[3 * c + 2], sz));
             rij[c] = ff_sub(rij[c], as);
           }
         }
@@ -839,8 +846,15 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       Gout[1] = make_float2(G[1].hi, G[1].lo);
       Gout[2] = make_float2(G[2].hi, G[2].lo);
     }
+    if (a.tile_atom0) {  // batches: one partial row per tile (structure sums)
+      block_sum_tile(ff_norm(eacc), wacc, a.tile_part + 10 * (size_t)tile, red_scratch);
+      eacc = ff_make(0.0f, 0.0f);
+#pragma unroll
+      for (int c = 0; c < 9; c++) wacc[c] = 0.0f;
+    }
   }  // tiles
-  block_sum_tile(ff_norm(eacc), wacc, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
+  if (!a.tile_atom0)
+    block_sum_tile(ff_norm(eacc), wacc, a.tile_part + 10 * (size_t)blockIdx.x, red_scratch);
 }
 
 // Gather of the ff bond forces: F_a = sum_b (G[rev b] - G[b]) in ff.

@@ -945,9 +945,8 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   return 0;
 }
 
-int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream, bool sync) {
+int neighbors_build_reverse(Neighbors &nl, int nat, cudaStream_t stream, bool sync) {
   if (nl.rev_valid || nl.rev_pending) return sync ? neighbors_check_reverse(nl, stream) : 0;
-  const int nat = p.nat;
   GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(nl.nentries, 1)));
   int *status = nl.stats.as<int>();
   GB_CUDA(cudaMemsetAsync(status + 1, 0, sizeof(int), stream));

@@ -189,7 +189,7 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
 // Reverse-entry index of the list.  With sync = false the symmetry check is
 // deferred: call neighbors_check_reverse (stream = nullptr once the caller
 // has synchronised the stream itself) before rev is read.
-int neighbors_build_reverse(Neighbors &nl, const Particles &p, cudaStream_t stream,
+int neighbors_build_reverse(Neighbors &nl, int nat, cudaStream_t stream,
                             bool sync = true);
 int neighbors_check_reverse(Neighbors &nl, cudaStream_t stream);
 

@@ -100,6 +100,10 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
                 bool want_wat, bool want_per_bond);
 int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
                 bool want_wat);
+// Element count / atomic number of element q of the potential; its stream.
+int pot_nel(const Potential &pot);
+int pot_Z(const Potential &pot, int q);
+cudaStream_t pot_stream(Potential &pot);
 
 // Deterministic fixed-order sum of tile partials: red[c] = sum_t part[t*nc+c].
 // Deterministic sum of nrows rows of nc (= 10) doubles into red[0..nc); with a
@@ -108,6 +112,29 @@ constexpr int kRedRowsPerBlock = 256;
 size_t reduce_stage_bytes(int nrows);
 int reduce_partials(const double *part, int nrows, int nc, double *red, double *stage,
                     cudaStream_t s);
+// Per-segment sums of 10-column rows: out[q][.] = sum of rows [seg[q], seg[q+1]).
+int reduce_segments(const double *part, const int *seg, int nseg, double *out, cudaStream_t s);
+
+// The system a bond-order evaluation runs on: one structure (cell A), or a
+// batch of structures whose tiles (cut by the caller, at most apt atoms, never
+// across structures) carry their structure's cell and whose energy/virial sums
+// go per structure into red_seg (nseg x 10: energy, virial).
+struct BopSystem {
+  int nat = 0;
+  double A[3][3] = {{0}};
+  const int *tile_atom0 = nullptr;   // device, ntiles + 1
+  const int *tile_struct = nullptr;  // device, ntiles
+  const double *Acells = nullptr;    // device, 9 per structure
+  const float2 *Acells_ff = nullptr; // device, 9 float-float pairs per structure
+  int ntiles = 0, apt = 0;
+  const int *seg = nullptr;          // device, tile offsets of the structures (nseg + 1)
+  int nseg = 0;
+  double *red_seg = nullptr;         // device, nseg x 10
+};
+int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
+            bool want_wat, bool want_pb);
+// Atoms per tile for a list whose largest coordination is maxz.
+int bop_batch_apt(int maxz);
 
 }  // namespace gb
 

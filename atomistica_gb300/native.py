@@ -408,3 +408,79 @@ class TabulatedAlloyEAM(_Potential):
         c = np.zeros((8, n))
         self._L.gb_tabulated_alloy_eam_table(self._h, which, idx, x.ctypes.data, c.ctypes.data)
         return x, c
+
+
+class Batch:
+    """Many independent periodic structures evaluated together: one neighbour
+    build and one bond-order tile launch for all of them (no counterpart in
+    the reference, which evaluates one particles object per call).
+
+    ``structures``: objects with ``positions`` (n,3), ``cell`` (3,3, rows =
+    lattice vectors), ``pbc`` (3,) and ``numbers`` (n,) (ASE-like).
+    """
+
+    def __init__(self, structures=None):
+        self._L = load()
+        self._h = ctypes.c_void_p()
+        check(self._L.gb_batch_new(ctypes.byref(self._h)), "batch_new")
+        self.nat = []
+        if structures is not None:
+            self.set_structures(structures)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.gb_batch_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __len__(self):
+        return len(self.nat)
+
+    def set_stream(self, stream):
+        check(self._L.gb_batch_set_stream(self._h, stream), "batch_set_stream")
+
+    def set_structures(self, structures):
+        """Cells, pbc flags, atomic numbers and positions of all structures."""
+        nat = np.array([len(s.positions) for s in structures], dtype=np.int32)
+        cells = np.ascontiguousarray(np.array([np.asarray(s.cell, dtype=np.float64)
+                                               for s in structures]).reshape(-1, 3, 3))
+        pbc = np.ascontiguousarray(np.array([np.broadcast_to(np.asarray(s.pbc, dtype=bool), (3,))
+                                             for s in structures], dtype=np.int32))
+        Z = np.ascontiguousarray(np.concatenate([np.asarray(s.numbers, dtype=np.int32)
+                                                 for s in structures])
+                                 if len(structures) else np.zeros(0, np.int32))
+        check(self._L.gb_batch_set_structures(self._h, len(structures), nat.ctypes.data,
+                                              cells.ctypes.data, pbc.ctypes.data,
+                                              Z.ctypes.data), "batch_set_structures")
+        self.nat = [int(n) for n in nat]
+        self.offsets = np.concatenate([[0], np.cumsum(nat)]).astype(np.int64)
+        r = (np.concatenate([np.asarray(s.positions, dtype=np.float64) for s in structures])
+             if len(structures) else np.zeros((0, 3)))
+        self.set_positions(r)
+
+    def set_positions(self, r):
+        """Positions of all atoms, (total, 3): numpy array or CUDA tensor."""
+        ptr, keep = _ptr(r, np.float64)
+        self._r = keep
+        check(self._L.gb_batch_set_positions(self._h, ptr), "batch_set_positions")
+
+    def energy_and_forces(self, pot, forces=None):
+        """(epot (nstruct,), forces (total, 3), wpot (nstruct, 3, 3)); forces
+        (numpy or CUDA tensor) is accumulated into when given."""
+        total = int(self.offsets[-1]) if len(self.nat) else 0
+        if forces is None:
+            forces = np.zeros((total, 3))
+        dev = _is_torch(forces) and forces.is_cuda
+        if dev:
+            epot = torch.zeros(len(self.nat), dtype=torch.float64, device=forces.device)
+            wpot = torch.zeros((len(self.nat), 3, 3), dtype=torch.float64, device=forces.device)
+        else:
+            epot = np.zeros(len(self.nat))
+            wpot = np.zeros((len(self.nat), 3, 3))
+        fp, fkeep = _ptr(forces, np.float64)
+        ep, ekeep = _ptr(epot, np.float64)
+        wp, wkeep = _ptr(wpot, np.float64)
+        check(self._L.gb_batch_energy_and_forces(self._h, pot._h, ep, fp, wp),
+              "batch_energy_and_forces")
+        if fkeep is not forces and not dev:
+            forces[...] = fkeep
+        return epot, forces, wpot

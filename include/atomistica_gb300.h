@@ -61,6 +61,7 @@ extern "C" {
 typedef struct gb_particles gb_particles_t;
 typedef struct gb_neighbors gb_neighbors_t;
 typedef struct gb_potential gb_potential_t;
+typedef struct gb_batch gb_batch_t;
 
 /* Last error message of the calling thread ("" if none). */
 const char *gb_get_error(void);
@@ -239,6 +240,29 @@ int gb_bop_energy_and_forces_noalloc(gb_potential_t *pot, int nat, const double 
                                      const double *cell, const int *Z, const int64_t *seed,
                                      const int *j, const int *dc, double *epot, double *f,
                                      double *wpot, void *cuda_stream);
+
+/* ------------------------------------------------------------------------
+ * Batches of independent structures (no counterpart in the reference: it
+ * evaluates one particles object per call).  One neighbour build and one
+ * bond-order tile launch cover all structures; per structure the results
+ * equal a separate energy_and_forces call on that structure (same list, same
+ * kernels).  Tersoff and Kumagai, FP64 or mixed precision.
+ * ---------------------------------------------------------------------- */
+int gb_batch_new(gb_batch_t **batch);
+void gb_batch_free(gb_batch_t *batch);
+int gb_batch_set_stream(gb_batch_t *batch, void *cuda_stream);
+/* nstruct structures; nat[s] atoms each (atoms of structure s follow those of
+ * s-1); cells: nstruct x 3 x 3, rows = lattice vectors; pbc: nstruct x 3 (NULL:
+ * periodic in all directions); Z: atomic numbers of all atoms. */
+int gb_batch_set_structures(gb_batch_t *batch, int nstruct, const int *nat,
+                            const double *cells, const int *pbc, const int *Z);
+/* Positions of all atoms, (total atoms, 3); host or device memory. */
+int gb_batch_set_positions(gb_batch_t *batch, const double *r);
+int gb_batch_get_nat(const gb_batch_t *batch);
+/* epot[nstruct] set; f (total atoms, 3) and wpot[nstruct][3][3] (each in the
+ * layout of energy_and_forces' wpot) accumulated.  Host or device memory. */
+int gb_batch_energy_and_forces(gb_batch_t *batch, gb_potential_t *pot, double *epot, double *f,
+                               double *wpot);
 
 /* ------------------------------------------------------------------------
  * Diagnostics (no counterpart in the reference; used by the benchmark).

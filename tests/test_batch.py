@@ -1,0 +1,110 @@
+"""Batched evaluation (many structures, one neighbour build and one tile
+launch) against per-structure evaluations: the FP64 oracle, and the single-
+structure GPU path of the same library (identical forces, energies and
+virials to rounding of the tile sums)."""
+
+import numpy as np
+import pytest
+
+import oracle
+from atomistica_gb300 import structures as S
+
+from helpers import KUMAGAI, MIXED_F_TOL, TERSOFF, gpu_bop, rattled_diamond, triclinic_si
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_set(seed=0):
+    """Uneven structures: 8-atom triclinic cells (several images of each
+    atom within the cutoff), rattled diamond supercells, a non-periodic
+    cluster and a slab."""
+    out = [triclinic_si(8, seed=seed + 1), triclinic_si(24, seed=seed + 2),
+           rattled_diamond(size=(2, 2, 2), amp=0.3, seed=seed + 3),
+           triclinic_si(100, seed=seed + 4),
+           rattled_diamond(size=(1, 1, 1), amp=0.2, seed=seed + 5),
+           S.tersoff_si_4096(seed=seed + 6)]
+    slab = rattled_diamond(size=(2, 2, 3), amp=0.2, seed=seed + 7)
+    slab.pbc = np.array([True, True, False])
+    out.append(slab)
+    cluster = rattled_diamond(size=(2, 2, 2), amp=0.2, seed=seed + 8)
+    cluster.pbc = np.array([False, False, False])
+    out.append(cluster)
+    return out
+
+
+def _run_batch(structs, kind="tersoff", precision="fp64", params=None):
+    from atomistica_gb300 import native
+    b = native.Batch(structs)
+    cls = native.Tersoff if kind == "tersoff" else native.Kumagai
+    pot = cls(precision=precision, **(params or {}))
+    e, f, w = b.energy_and_forces(pot)
+    return b, e, f, w
+
+
+@pytest.mark.parametrize("kind", ["tersoff", "kumagai"])
+def test_batch_matches_oracle_fp64(gpu, kind):
+    structs = _mixed_set(10 if kind == "tersoff" else 20)
+    params = TERSOFF if kind == "tersoff" else KUMAGAI
+    b, e, f, w = _run_batch(structs, kind)
+    for q, s in enumerate(structs):
+        ref = oracle.bop(kind, params, s, per_at=False)
+        n = len(s)
+        fq = f[b.offsets[q]:b.offsets[q + 1]]
+        assert abs(e[q] - ref["epot"]) / n < 1e-10, (q, e[q], ref["epot"])
+        assert np.max(np.abs(fq - ref["f"])) < 1e-9, q
+        assert np.max(np.abs(w[q] - ref["wpot"])) < 1e-9 * max(n, 1), q
+
+
+def test_batch_equals_single_structure_path(gpu):
+    structs = _mixed_set(30)
+    b, e, f, w = _run_batch(structs)
+    for q, s in enumerate(structs):
+        one = gpu_bop("tersoff", s, per_at=False)
+        fq = f[b.offsets[q]:b.offsets[q + 1]]
+        assert np.array_equal(fq, one["f"]), q  # same list order, same per-bond sums
+        assert abs(e[q] - one["epot"]) <= 1e-12 * max(1.0, abs(one["epot"]))
+        assert np.max(np.abs(w[q] - one["wpot"])) <= 1e-12 * max(1.0, np.max(np.abs(w[q])))
+
+
+def test_batch_mixed_precision(gpu):
+    structs = S.si_batch(48, seed=41)
+    b, e, f, w = _run_batch(structs, precision="mixed")
+    for q, s in enumerate(structs):
+        ref = oracle.bop("tersoff", TERSOFF, s, per_at=False)
+        fq = f[b.offsets[q]:b.offsets[q + 1]]
+        assert np.max(np.abs(fq - ref["f"])) <= MIXED_F_TOL, q
+        assert abs(e[q] - ref["epot"]) / len(s) < 1e-6, q
+
+
+def test_batch_deterministic_and_accumulating(gpu):
+    structs = S.si_batch(32, seed=42)
+    from atomistica_gb300 import native
+    b = native.Batch(structs)
+    pot = native.Tersoff(precision="mixed")
+    e1, f1, w1 = b.energy_and_forces(pot)
+    e2, f2, w2 = b.energy_and_forces(pot)
+    assert np.array_equal(e1, e2) and np.array_equal(f1, f2) and np.array_equal(w1, w2)
+    # forces are accumulated into a caller array, energies set
+    f0 = np.ones_like(f1)
+    e3, f3, _ = b.energy_and_forces(pot, forces=f0)
+    assert np.array_equal(e3, e1)
+    assert np.array_equal(f3, f1 + 1.0)
+    # new positions rebuild the list
+    r = np.concatenate([s.positions for s in structs]) + 0.01
+    b.set_positions(r)
+    e4, f4, _ = b.energy_and_forces(pot)
+    assert not np.array_equal(f4, f1)
+
+
+def test_batch_c4_sample_fp64(gpu):
+    # a sample of the 2048-structure batch workload (N in [8, 512], strained
+    # triclinic cells, 2.0 A minimum separation)
+    structs = S.si_batch(64, seed=4)
+    b, e, f, w = _run_batch(structs)
+    worst = 0.0
+    for q, s in enumerate(structs):
+        ref = oracle.bop("tersoff", TERSOFF, s, per_at=False)
+        fq = f[b.offsets[q]:b.offsets[q + 1]]
+        worst = max(worst, float(np.max(np.abs(fq - ref["f"]))))
+        assert abs(e[q] - ref["epot"]) / len(s) < 1e-10, q
+    assert worst < 1e-9, worst
