@@ -239,12 +239,83 @@ def other_configs(dev, oracle):
         p.set_positions(d_pos)
         e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
         f = d_f.cpu().numpy()
+    out["si_batch_2048"] = batch_config(dev, oracle, nth)
     out["eam_cu_131072"] = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu,
                             "cpu_cores": nth,
                             "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
                                      "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                                      "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
     return out
+
+
+def batch_config(dev, oracle, nth):
+    """2048 triclinic Si structures, N ~ U{8..512}, in one batched evaluation
+    (FP64 and mixed) against the same structures evaluated one call each on
+    the GPU and by the oracle on all host cores."""
+    import numpy as np
+    import torch
+    from atomistica_gb300 import native, parameters, structures
+    t0 = time.perf_counter()
+    structs = structures.si_batch(2048, seed=4)
+    t_gen = time.perf_counter() - t0
+    nat = sum(len(q) for q in structs)
+    params = parameters.Tersoff_PRB_39_5566_Si_C
+    b = native.Batch(structs)
+    r = torch.tensor(np.concatenate([q.positions for q in structs]), dtype=torch.float64,
+                     device=dev)
+    f = torch.zeros((nat, 3), dtype=torch.float64, device=dev)
+    entry = {"nstruct": len(structs), "natoms": nat, "unit": UNIT,
+             "generation_s": t_gen, "sample": "all 2048 structures"}
+    refs = [oracle.bop_compute("tersoff", params, q, nthreads=nth) for q in structs]
+    for prec in ("fp64", "mixed"):
+        pot = native.Tersoff(precision=prec)
+        for _ in range(3):
+            f.zero_()
+            b.set_positions(r)
+            b.energy_and_forces(pot, forces=f)
+        torch.cuda.synchronize()
+        steps = 10
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            f.zero_()
+            b.set_positions(r)
+            e, _, w = b.energy_and_forces(pot, forces=f)
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / steps
+        fh = f.cpu().numpy()
+        eh = e.cpu().numpy()
+        off = b.offsets
+        df = max(float(np.max(np.abs(fh[off[q]:off[q + 1]] - refs[q]["f"])))
+                 for q in range(len(structs)))
+        de = max(abs(eh[q] - refs[q]["epot"]) / len(structs[q]) for q in range(len(structs)))
+        entry[prec] = {"value": nat / t, "ms_per_step": 1e3 * t, "max_abs_dF": df,
+                       "max_abs_dE_per_atom": de}
+    # the same structures one call each (particles + list + potential per structure)
+    pot = native.Tersoff(precision="fp64")
+    objs = []
+    for q in structs:
+        p = native.from_atoms(q)
+        nl = native.Neighbors(100)
+        pot.bind_to(p, nl)
+        objs.append((p, nl, torch.tensor(q.positions, dtype=torch.float64, device=dev),
+                     torch.zeros((len(q), 3), dtype=torch.float64, device=dev)))
+    for p, nl, rq, fq in objs:
+        pot.bind_to(p, nl)
+        pot.energy_and_forces(p, nl, forces=fq)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p, nl, rq, fq in objs:
+        pot.bind_to(p, nl)
+        p.set_positions(rq)
+        pot.energy_and_forces(p, nl, forces=fq)
+    torch.cuda.synchronize()
+    entry["fp64_one_call_per_structure"] = {"value": nat / (time.perf_counter() - t0)}
+    t0 = time.perf_counter()
+    for q in structs:
+        oracle.bop_compute("tersoff", params, q, nthreads=nth)
+    entry["cpu_oracle"] = nat / (time.perf_counter() - t0)
+    entry["cpu_cores"] = nth
+    return entry
 
 
 def run_reference(args):
