@@ -16,8 +16,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libatomistica_gb300.so")
-SOURCES = ["core.cu", "bop.cu", "eam.cu", "api.cu", "diag.cu", "batch.cu"]
-HEADERS = ["internal.h", "potential.h", "bop_math.h", "ff.h", "ff_tables.h", "bop_mixed.cuh"]
+SOURCES = ["core.cu", "bop.cu", "eam.cu", "api.cu", "diag.cu", "batch.cu",
+           "autodiff.cu"]
+HEADERS = ["internal.h", "potential.h", "bop_math.h", "ff.h", "ff_tables.h", "bop_mixed.cuh",
+           "batch.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code is compiled without FP contraction so that the cell inverse, the

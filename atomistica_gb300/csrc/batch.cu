@@ -20,33 +20,11 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "bop_math.h"
-#include "potential.h"
 
 namespace gb {
 
-struct Batch {
-  int nstruct = 0, nat = 0;
-  std::vector<int> atom_off;  // nstruct + 1
-  std::vector<double> A;      // 9 per structure: A[a][k], column k = lattice vector k
-  std::vector<double> B;      // inverses
-  std::vector<int> pbc;       // 3 per structure
-  std::vector<int> hZ;        // nat
-  uint64_t geom_rev = 0, pos_rev = 0;
-  DevBuf r, sid, bps, Acells, Acells_ff, tiles, red_seg, el;
-  HostBuf hseg;
-  // cached derived state
-  uint64_t built_geom = ~0ull, built_pos = ~0ull, el_geom = ~0ull;
-  const Potential *el_pot = nullptr;
-  double built_cutoff = -1.0;
-  int ncells = 0, tiles_apt = 0, ntiles = 0;
-  int64_t tiles_nentries = -1;
-  Neighbors nl;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-};
-
-namespace {
 
 cudaStream_t batch_stream(Batch &b) {
   if (!b.stream) {
@@ -156,8 +134,6 @@ int batch_tiles(Batch &b, int apt, cudaStream_t s) {
   b.tiles_nentries = b.nl.nentries;
   return 0;
 }
-
-}  // namespace
 
 int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, double *wpot) {
   if (!epot || !f || !wpot) {
@@ -292,10 +268,6 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
 // C-ABI.
 // ===========================================================================
 using namespace gb;
-
-struct gb_batch {
-  gb::Batch b;
-};
 
 extern "C" {
 

@@ -264,6 +264,19 @@ int gb_batch_get_nat(const gb_batch_t *batch);
 int gb_batch_energy_and_forces(gb_batch_t *batch, gb_potential_t *pot, double *epot, double *f,
                                double *wpot);
 
+/* Tangent evaluation for parameter fitting (no counterpart in the
+ * reference): single-element Tersoff (atoms of atomic number Z; others are
+ * skipped) with the 14 continuous parameters params = {A, B, lambda, mu, beta,
+ * n, c, d, h, R, S, xi, omega, mubo} and integer m.  Along the direction
+ * (dparams, dr) — dparams[14] (NULL: 0) and a position direction dr
+ * (total atoms, 3; NULL: 0) — returns epot[nstruct], f (total atoms, 3) and
+ * their directional derivatives depot, df (all set, not accumulated; host or
+ * device memory).  With dr = v and dparams = NULL, df = -H v (H the Hessian
+ * of the energy).  The neighbour list is built for the cutoff S. */
+int gb_batch_tersoff_tangent(gb_batch_t *batch, int Z, int m, const double *params,
+                             const double *dparams, const double *dr, double *epot,
+                             double *depot, double *f, double *df);
+
 /* ------------------------------------------------------------------------
  * Diagnostics (no counterpart in the reference; used by the benchmark).
  * ---------------------------------------------------------------------- */
