@@ -240,6 +240,7 @@ def other_configs(dev, oracle):
         e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
         f = d_f.cpu().numpy()
     out["si_batch_2048"] = batch_config(dev, oracle, nth)
+    out["si_fit_256"] = fitting_config(oracle, nth)
     out["eam_cu_131072"] = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu,
                             "cpu_cores": nth,
                             "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
@@ -316,6 +317,65 @@ def batch_config(dev, oracle, nth):
     entry["cpu_oracle"] = nat / (time.perf_counter() - t0)
     entry["cpu_cores"] = nth
     return entry
+
+
+def fitting_config(oracle, nth):
+    """Tersoff fitting loss over 256 diamond Si supercells (64-216 atoms):
+    one forward + backward (loss gradient w.r.t. the 14 parameters and the
+    positions: 1 evaluation + 14 parameter tangents + 1 Hessian-vector
+    product), its agreement with central differences, and one energy+forces
+    evaluation of the set by the oracle on the host cores."""
+    import numpy as np
+    import torch
+    from atomistica_gb300 import fitting, structures
+    structs = structures.si_fit_set(256, seed=5)
+    nat = sum(len(q) for q in structs)
+    theta, m = fitting.single_element_parameters()
+    rng = np.random.default_rng(5)
+    theta_t = theta * (1.0 + rng.uniform(-0.02, 0.02, size=14))
+    tb = fitting.TersoffBatch(structs, m=m)
+    r0 = np.concatenate([q.positions for q in structs])
+    tb.set_positions(r0)
+    et, _, ft, _ = tb.evaluate(theta_t)
+    E_t, F_t = torch.tensor(et), torch.tensor(ft)
+
+    def loss_grad():
+        th = torch.tensor(theta, requires_grad=True)
+        r = torch.tensor(r0, requires_grad=True)
+        E, F = fitting.EnergyForces.apply(th, r, tb)
+        loss = fitting.fitting_loss(E, F, tb.nat, E_t, F_t)
+        loss.backward()
+        return loss.item(), th.grad.numpy().copy()
+
+    loss_grad()
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        loss, g = loss_grad()
+        ts.append(time.perf_counter() - t0)
+    rel = []
+    with torch.no_grad():
+        for k in range(14):
+            h = 1e-6 * abs(theta[k]) if theta[k] != 0 else 1e-6
+            u = np.zeros(14)
+            u[k] = h
+            lv = []
+            for sgn in (1.0, -1.0):
+                E, F = fitting.EnergyForces.apply(torch.tensor(theta + sgn * u),
+                                                  torch.tensor(r0), tb)
+                lv.append(fitting.fitting_loss(E, F, tb.nat, E_t, F_t).item())
+            fd = (lv[0] - lv[1]) / (2 * h)
+            rel.append(abs(g[k] - fd) / max(abs(g[k]), abs(fd), 1e-300))
+    params = fitting.parameter_dict(theta, m)
+    t0 = time.perf_counter()
+    for q in structs:
+        oracle.bop("tersoff", params, q, per_at=False, nthreads=nth)
+    t_cpu = time.perf_counter() - t0
+    return {"nstruct": len(structs), "natoms": nat,
+            "forward_backward_s": statistics.median(ts), "loss": loss,
+            "grad_vs_central_differences_max_rel": max(rel),
+            "cpu_oracle_one_evaluation_s": t_cpu, "cpu_cores": nth,
+            "note": "central differences need 29 evaluations of the set"}
 
 
 def run_reference(args):
