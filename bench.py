@@ -74,10 +74,8 @@ def parse_args():
 
 
 def dist_info():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from atomistica_gb300.distributed import dist_info as _di
+    return _di()
 
 
 class ClockSampler:
@@ -490,12 +488,7 @@ def run_ours(args):
     sampler = ClockSampler(torch.cuda.current_device())
     msmx, partsmx, launches, clocks = timed(pots["mixed"], args.steps, sampler)
 
-    def tmax(x):
-        if ws > 1:
-            t = torch.tensor([x], dtype=torch.float64, device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return x
+    from atomistica_gb300.distributed import max_over_ranks as tmax
 
     t_mx = tmax(sum(msmx) / 1e3)
     t_64 = tmax(sum(ms64) / 1e3)
