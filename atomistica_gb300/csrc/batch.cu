@@ -135,6 +135,273 @@ int batch_tiles(Batch &b, int apt, cudaStream_t s) {
   return 0;
 }
 
+Batch::~Batch() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+}
+
+namespace {
+
+void drop_graph(Batch &b) {
+  if (b.graph_exec) cudaGraphExecDestroy(b.graph_exec);
+  if (b.graph) cudaGraphDestroy(b.graph);
+  b.graph_exec = nullptr;
+  b.graph = nullptr;
+  b.graph_kernels = 0;
+  b.graph_bufs.clear();
+}
+
+// Device buffers a captured evaluation writes or reads (their addresses are
+// baked into the graph).
+std::vector<const void *> graph_buffers(const Batch &b, const Potential &pot) {
+  const Neighbors &nl = b.nl;
+  return {b.r.p, b.sid.p, b.bps.p, b.Acells.p, b.Acells_ff.p, b.tiles.p, b.red_seg.p, b.el.p,
+          b.gf.p, b.hseg.p, nl.pos4.p, nl.posff.p, nl.atom_cell.p, nl.atom_wrap.p,
+          nl.cell_count.p, nl.cell_start.p, nl.cell_atoms.p, nl.counts.p, nl.spos.p, nl.swrap.p,
+          nl.seed.p, nl.nbr.p, nl.shift.p, nl.rev.p, nl.stage.p, nl.scan_tmp.p, nl.stats.p,
+          nl.hstats.p, pot.bond_G.p, pot.bond_e.p, pot.tile_part.p, pot.red.p, pot.hred.p};
+}
+
+BopSystem batch_system(const Batch &b) {
+  BopSystem sys;
+  sys.nat = b.nat;
+  const int *t = b.tiles.as<int>();
+  sys.tile_atom0 = t;
+  sys.tile_struct = t + b.ntiles + 1;
+  sys.seg = t + 2 * b.ntiles + 1;
+  sys.nseg = b.nstruct;
+  sys.red_seg = b.red_seg.as<double>();
+  sys.Acells = b.Acells.as<double>();
+  sys.Acells_ff = reinterpret_cast<const float2 *>(b.Acells_ff.p);
+  sys.ntiles = b.ntiles;
+  sys.apt = b.tiles_apt;
+  sys.el = b.el.as<int>();
+  return sys;
+}
+
+// Tile kernel, gather and per-structure sums into fdev (accumulated), then
+// the per-structure rows and the status words to pinned host memory.
+int batch_forces(Batch &b, Potential &pot, double *fdev, cudaStream_t s, BopSystem sys) {
+  GB_CHECK(pot.red.ensure(sizeof(double) * 16));
+  GB_CHECK(pot.hred.ensure(sizeof(double) * 16));
+  GB_CHECK(b.red_seg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1)));
+  GB_CHECK(b.hseg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1) + 64));
+  sys.red_seg = b.red_seg.as<double>();  // (allocated just now on the first call)
+  Outputs o;
+  o.f = fdev;
+  o.red = pot.red.as<double>();
+  o.status = reinterpret_cast<int *>(o.red + 12);
+  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s));
+  GB_CHECK(bop_run(pot, sys, b.nl, o, false, false));
+  GB_CUDA(cudaMemcpyAsync(b.hseg.p, b.red_seg.p, sizeof(double) * 10 * b.nstruct,
+                          cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaMemcpyAsync(pot.hred.p, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost, s));
+  return 0;
+}
+
+// epot set, wpot accumulated, per structure (as energy_and_forces).
+int batch_finish(Batch &b, Potential &pot, double *epot, double *wpot) {
+  const double *hs = b.hseg.as<double>();
+  const double *hr = pot.hred.as<double>();
+  const int st = reinterpret_cast<const int *>(hr + 12)[0];
+  pot.last_status = st;
+  pot.last_hot = reinterpret_cast<const int *>(hr + 12)[2];
+  pot.last_bonds = b.nl.nentries;
+  if (st & 2) {
+    set_error("Internal error: bond-order tile plan mismatch.");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  const bool ed = is_device_ptr(epot), wd = is_device_ptr(wpot);
+  std::vector<double> e(b.nstruct), w(9 * (size_t)b.nstruct);
+  if (wd)
+    GB_CUDA(cudaMemcpy(w.data(), wpot, sizeof(double) * w.size(), cudaMemcpyDeviceToHost));
+  else
+    std::memcpy(w.data(), wpot, sizeof(double) * w.size());
+  for (int q = 0; q < b.nstruct; q++) {
+    e[q] = hs[10 * q];
+    for (int c = 0; c < 9; c++) w[9 * q + c] += hs[10 * q + 1 + c];
+  }
+  if (ed)
+    GB_CUDA(cudaMemcpy(epot, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice));
+  else
+    std::memcpy(epot, e.data(), sizeof(double) * e.size());
+  if (wd)
+    GB_CUDA(cudaMemcpy(wpot, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
+  else
+    std::memcpy(wpot, w.data(), sizeof(double) * w.size());
+  return 0;
+}
+
+// Atoms per tile: the autotuned value when current, else the largest that
+// fits.  Tuning times the force part for apt, apt/2, apt/4 (>= 8) on scratch
+// forces and keeps the fastest.
+int batch_choose_apt(Batch &b, Potential &pot, cudaStream_t s) {
+  const int amax = bop_batch_apt(b.nl.maxz);
+  const bool current = b.tuned_apt > 0 && b.tuned_geom == b.geom_rev && b.tuned_pot == &pot &&
+                       b.tuned_prec == pot.precision && b.tuned_apt <= amax;
+  if (!b.autotune) return amax;
+  if (current) return b.tuned_apt;
+  GB_CHECK(b.gf.ensure(sizeof(double) * 3 * std::max(b.nat, 1)));
+  int best = amax, ncand = 0;
+  float best_ms = 0.0f;
+  for (int apt = amax; apt >= std::min(amax, 8); apt /= 2) {
+    GB_CHECK(batch_tiles(b, apt, s));
+    GB_CUDA(cudaMemsetAsync(b.gf.p, 0, sizeof(double) * 3 * b.nat, s));
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2; rep++) {  // the first run warms up
+      GB_CUDA(cudaEventRecord(pot.ev[1], s));
+      GB_CHECK(batch_forces(b, pot, b.gf.as<double>(), s, batch_system(b)));
+      GB_CUDA(cudaEventRecord(pot.ev[2], s));
+      GB_CUDA(cudaStreamSynchronize(s));
+      GB_CUDA(cudaEventElapsedTime(&ms, pot.ev[1], pot.ev[2]));
+    }
+    ncand++;
+    if (ncand == 1 || ms < best_ms) {
+      best_ms = ms;
+      best = apt;
+    }
+    if (apt < 16 || ncand == 3) break;
+  }
+  b.tuned_apt = best;
+  b.tuned_geom = b.geom_rev;
+  b.tuned_pot = &pot;
+  b.tuned_prec = pot.precision;
+  b.tune_candidates = ncand;
+  return best;
+}
+
+// Captures the whole evaluation (list build included) after an eager one
+// has sized everything; failures leave the eager path in use.
+void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
+  drop_graph(b);
+  const int cap = b.nl.stage_cap;
+  if (cap <= 0 || b.nat == 0) return;
+  const int64_t capacity = (int64_t)b.nat * cap;
+  // plan with head room for the next configurations (checked per tile)
+  const int apt = b.tiles_apt;
+  int max_nbt = std::min(apt * cap, pot.last_plan[0] + pot.last_plan[0] / 4 + 16);
+  int max_ntrip = std::min(apt * cap * cap, pot.last_plan[1] + pot.last_plan[1] / 2 + 64);
+  if (pot.last_plan[0] == 0) return;
+  const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  while (bop_tile_smem(mixed, max_nbt, max_ntrip) > bop_tile_smem_budget() &&
+         (max_nbt > pot.last_plan[0] || max_ntrip > pot.last_plan[1])) {
+    max_nbt = std::max(pot.last_plan[0], max_nbt - max_nbt / 8 - 1);
+    max_ntrip = std::max(pot.last_plan[1], max_ntrip - max_ntrip / 8 - 1);
+  }
+  Neighbors &nl = b.nl;
+  if (nl.nbr.ensure(sizeof(int) * capacity) || nl.shift.ensure(sizeof(int) * capacity) ||
+      nl.rev.ensure(sizeof(int) * capacity) || nl.stage.ensure(sizeof(int2) * capacity) ||
+      pot.bond_G.ensure(sizeof(double) * 3 * capacity) ||
+      pot.bond_e.ensure(sizeof(double) * capacity) ||
+      pot.tile_part.ensure(sizeof(double) * 10 * b.ntiles + 64) ||
+      b.gf.ensure(sizeof(double) * 3 * b.nat)) {
+    clear_error();
+    return;
+  }
+  BopSystem sys = batch_system(b);
+  sys.capture = true;
+  sys.nb_capacity = capacity;
+  sys.max_nbt = max_nbt;
+  sys.max_ntrip = max_ntrip;
+  // Capturing runs nothing: the list, reverse index and ff positions of the
+  // eager evaluation stay valid on the device; restore their flags after.
+  const bool rev_valid0 = nl.rev_valid, posff_valid0 = nl.posff_valid;
+  const int plan0[2] = {pot.last_plan[0], pot.last_plan[1]};
+  nl.rev_valid = false;
+  nl.rev_pending = false;
+  nl.posff_valid = nl.want_posff;
+  const uint64_t launches0 = gb_kernel_launches();
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  BinParams dummy{};
+  int rc = nl_build(nl, b.nat, b.r.as<double>(), dummy, b.bps.as<BinParams>(), b.sid.as<int>(),
+                    b.ncells, s, true);
+  if (rc == 0) rc = batch_forces(b, pot, b.gf.as<double>(), s, sys);
+  const cudaError_t ce = cudaStreamEndCapture(s, &g);
+  note_launch(-(int)(gb_kernel_launches() - launches0));  // captured, not run
+  nl.rev_valid = rev_valid0;
+  nl.rev_pending = false;
+  nl.posff_valid = posff_valid0;
+  pot.last_plan[0] = plan0[0];
+  pot.last_plan[1] = plan0[1];
+  if (rc != 0 || ce != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    clear_error();
+    b.graph_failed = true;
+    return;
+  }
+  cudaGraphExec_t x = nullptr;
+  if (cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    b.graph_failed = true;
+    return;
+  }
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+  int kernels = 0;
+  for (size_t k = 0; k < nn; k++) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+      kernels++;
+  }
+  b.graph = g;
+  b.graph_exec = x;
+  b.graph_kernels = kernels;
+  b.graph_geom = b.geom_rev;
+  b.graph_pot = &pot;
+  b.graph_prec = pot.precision;
+  b.graph_apt = apt;
+  b.graph_bufs = graph_buffers(b, pot);
+  (void)mixed;
+}
+
+bool graph_current(const Batch &b, const Potential &pot) {
+  return b.graph_exec && b.graph_geom == b.geom_rev && b.graph_pot == &pot &&
+         b.graph_prec == pot.precision && b.graph_apt == b.tiles_apt &&
+         b.graph_bufs == graph_buffers(b, pot);
+}
+
+// Replays the graph; true when its results are valid (no capacity, plan or
+// list problem), in which case the caller's outputs are written.
+int batch_replay(Batch &b, Potential &pot, double *epot, double *f, double *wpot,
+                 cudaStream_t s, bool &done) {
+  done = false;
+  const size_t nf = 3 * (size_t)b.nat;
+  GB_CUDA(cudaMemcpyAsync(b.gf.p, f, sizeof(double) * nf, cudaMemcpyDefault, s));
+  GB_CUDA(cudaGraphLaunch(b.graph_exec, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  note_launch(b.graph_kernels);
+  const int *hs = b.nl.hstats.as<int>();
+  const int *st = reinterpret_cast<const int *>(pot.hred.as<double>() + 12);
+  const bool ok = hs[0] <= b.nl.stage_cap && (hs[1] & (1 | 2)) == 0 && (hs[5] & 4) == 0 &&
+                  (st[0] & 2) == 0;
+  if (!ok) {
+    drop_graph(b);
+    b.nl.valid = false;
+    return 0;
+  }
+  b.nl.nentries = hs[4];
+  b.nl.maxz = hs[0];
+  b.nl.valid = true;
+  b.nl.rev_valid = true;
+  b.nl.rev_pending = false;
+  b.nl.posff_valid = b.nl.want_posff;
+  b.built_pos = b.pos_rev;
+  GB_CUDA(cudaMemcpy(f, b.gf.p, sizeof(double) * nf, cudaMemcpyDefault));
+  GB_CHECK(batch_finish(b, pot, epot, wpot));
+  done = true;
+  return 0;
+}
+
+}  // namespace
+
 int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, double *wpot) {
   if (!epot || !f || !wpot) {
     set_error("batch_energy_and_forces: epot, f and wpot are required");
@@ -144,6 +411,7 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
     set_error("batch_energy_and_forces: batches support the bond-order potentials");
     return GB_ERROR_ARGUMENT;
   }
+  b.info[0] = 0;
   if (b.nstruct == 0) return 0;
   if (b.nat > 0 && !b.r.p) {
     set_error("batch_energy_and_forces: positions not set");
@@ -164,6 +432,19 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
   }
   GB_CHECK(batch_binning(b, cutoff, s));
   if (mixed) b.nl.want_posff = true;
+
+  if (b.use_graph && graph_current(b, pot)) {
+    bool done = false;
+    GB_CHECK(batch_replay(b, pot, epot, f, wpot, s, done));
+    if (done) {
+      b.info[0] = 1;
+      b.info[1] = b.tiles_apt;
+      b.info[2] = b.graph_kernels;
+      return 0;
+    }
+  }
+
+  // Eager evaluation.
   if (!(b.nl.valid && b.built_pos == b.pos_rev && b.nl.posff_valid == b.nl.want_posff)) {
     b.nl.valid = false;
     b.nl.rev_valid = false;
@@ -176,9 +457,8 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
     b.built_pos = b.pos_rev;
   }
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
-  GB_CHECK(batch_tiles(b, bop_batch_apt(b.nl.maxz), s));
-
-  // Outputs: forces accumulated (host arrays staged), per-structure sums.
+  const int apt = batch_choose_apt(b, pot, s);
+  GB_CHECK(batch_tiles(b, apt, s));
   const size_t nf = 3 * (size_t)b.nat;
   double *fd = f;
   const bool f_host = b.nat > 0 && !is_device_ptr(f);
@@ -187,41 +467,9 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
     fd = pot.out_f.as<double>();
     GB_CUDA(cudaMemcpyAsync(fd, f, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
   }
-  GB_CHECK(pot.red.ensure(sizeof(double) * 16));
-  GB_CHECK(b.red_seg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1)));
-  Outputs o;
-  o.f = fd;
-  o.red = pot.red.as<double>();
-  o.status = reinterpret_cast<int *>(o.red + 12);
-  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s));
-
-  BopSystem sys;
-  sys.nat = b.nat;
-  const int *t = b.tiles.as<int>();
-  sys.tile_atom0 = t;
-  sys.tile_struct = t + b.ntiles + 1;
-  sys.seg = t + 2 * b.ntiles + 1;
-  sys.nseg = b.nstruct;
-  sys.red_seg = b.red_seg.as<double>();
-  sys.Acells = b.Acells.as<double>();
-  sys.Acells_ff = reinterpret_cast<const float2 *>(b.Acells_ff.p);
-  sys.ntiles = b.ntiles;
-  sys.apt = b.tiles_apt;
-  // the bond-order kernels take the element map from the potential
-  GB_CHECK(pot.el.ensure(sizeof(int) * std::max(b.nat, 1)));
-  GB_CUDA(cudaMemcpyAsync(pot.el.p, b.el.p, sizeof(int) * std::max(b.nat, 1),
-                          cudaMemcpyDeviceToDevice, s));
-  pot.el_for = nullptr;  // the potential's map no longer belongs to bound particles
-  GB_CHECK(bop_run(pot, sys, b.nl, o, false, false));
+  GB_CHECK(batch_forces(b, pot, fd, s, batch_system(b)));
   GB_CUDA(cudaEventRecord(pot.ev[2], s));
   if (f_host) GB_CUDA(cudaMemcpyAsync(f, fd, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
-  GB_CHECK(b.hseg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1) + 64));
-  double *hs = b.hseg.as<double>();
-  GB_CUDA(cudaMemcpyAsync(hs, b.red_seg.p, sizeof(double) * 10 * b.nstruct,
-                          cudaMemcpyDeviceToHost, s));
-  GB_CHECK(pot.hred.ensure(sizeof(double) * 16));
-  double *hr = pot.hred.as<double>();
-  GB_CUDA(cudaMemcpyAsync(hr, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaEventRecord(pot.ev[3], s));
   GB_CUDA(cudaStreamSynchronize(s));
   GB_CUDA(cudaGetLastError());
@@ -232,33 +480,11 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
   cudaEventElapsedTime(&ms[3], pot.kev[0], pot.kev[1]);
   cudaGetLastError();
   for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
-  const int st = reinterpret_cast<const int *>(hr + 12)[0];
-  pot.last_status = st;
-  pot.last_hot = reinterpret_cast<const int *>(hr + 12)[2];
-  pot.last_bonds = b.nl.nentries;
-  if (st & 2) {
-    set_error("Internal error: bond-order tile plan mismatch.");
-    return GB_ERROR_UNSPECIFIED;
-  }
-  // epot set, wpot accumulated, per structure (as energy_and_forces)
-  const bool ed = is_device_ptr(epot), wd = is_device_ptr(wpot);
-  std::vector<double> e(b.nstruct), w(9 * (size_t)b.nstruct);
-  if (wd)
-    GB_CUDA(cudaMemcpy(w.data(), wpot, sizeof(double) * w.size(), cudaMemcpyDeviceToHost));
-  else
-    std::memcpy(w.data(), wpot, sizeof(double) * w.size());
-  for (int q = 0; q < b.nstruct; q++) {
-    e[q] = hs[10 * q];
-    for (int c = 0; c < 9; c++) w[9 * q + c] += hs[10 * q + 1 + c];
-  }
-  if (ed)
-    GB_CUDA(cudaMemcpy(epot, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice));
-  else
-    std::memcpy(epot, e.data(), sizeof(double) * e.size());
-  if (wd)
-    GB_CUDA(cudaMemcpy(wpot, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
-  else
-    std::memcpy(wpot, w.data(), sizeof(double) * w.size());
+  GB_CHECK(batch_finish(b, pot, epot, wpot));
+  b.info[1] = b.tiles_apt;
+  b.info[3] = b.tune_candidates;
+  if (b.use_graph && !b.graph_failed && !graph_current(b, pot)) batch_capture(b, pot, s);
+  b.info[2] = b.graph_kernels;
   return 0;
 }
 
@@ -372,6 +598,23 @@ int gb_batch_set_positions(gb_batch_t *h, const double *r) {
 }
 
 int gb_batch_get_nat(const gb_batch_t *h) { return h ? h->b.nat : -1; }
+
+int gb_batch_set_options(gb_batch_t *h, int use_graph, int autotune) {
+  if (!h) return GB_ERROR_ARGUMENT;
+  Batch &b = h->b;
+  b.use_graph = use_graph != 0;
+  b.autotune = autotune != 0;
+  b.graph_failed = false;
+  if (!b.use_graph) drop_graph(b);
+  if (!b.autotune) b.tuned_apt = 0;
+  return 0;
+}
+
+int gb_batch_last_info(const gb_batch_t *h, int64_t *info) {
+  if (!h || !info) return GB_ERROR_ARGUMENT;
+  for (int k = 0; k < 4; k++) info[k] = h->b.info[k];
+  return 0;
+}
 
 int gb_batch_energy_and_forces(gb_batch_t *h, gb_potential_t *pot, double *epot, double *f,
                                double *wpot) {

@@ -28,6 +28,27 @@ struct Batch {
   Neighbors nl;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // Tile autotuning: the atoms per tile timed fastest for (geometry,
+  // potential, precision).
+  bool autotune = false;
+  int tuned_apt = 0;
+  uint64_t tuned_geom = ~0ull;
+  const Potential *tuned_pot = nullptr;
+  int tuned_prec = -1, tune_candidates = 0;
+  // CUDA graph of the whole evaluation (list build, tiles, gather, sums):
+  // replayed while geometry, potential, tiles and every buffer it uses are
+  // unchanged; any overflow seen after a replay falls back to the eager path.
+  bool use_graph = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_failed = false;
+  uint64_t graph_geom = ~0ull;
+  const Potential *graph_pot = nullptr;
+  int graph_prec = -1, graph_apt = 0, graph_kernels = 0;
+  std::vector<const void *> graph_bufs;
+  DevBuf gf;  // forces accumulated by the graph
+  int64_t info[4] = {0, 0, 0, 0};  // last call: replayed, atoms/tile, kernels in graph, tuned
+  ~Batch();
 };
 
 cudaStream_t batch_stream(Batch &b);

@@ -47,6 +47,8 @@ namespace gb {
 namespace {
 
 constexpr int kBopThreads = 128;
+// Largest dynamic shared memory a tile kernel is allowed to request (bytes).
+constexpr size_t kSmemBudgetAll = 208 * 1024;
 constexpr int kMaxApt = 64;
 
 // Bond meta word: owner local atom (bits 0-7), pair type (8-11), flags
@@ -486,6 +488,7 @@ __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__r
   const int s = seed[i], e = seed[i + 1];
   for (int b = s; b < e; b++) {
     const int rb = rev[b];
+    if (rb < 0) continue;  // (an incomplete list; reported by the reverse build)
 #pragma unroll
     for (int c = 0; c < 3; c++) F[c] += G[3 * (size_t)rb + c] - G[3 * (size_t)b + c];
     if (kEpa) E += ebond[b] + ebond[rb];
@@ -547,6 +550,23 @@ __global__ void reduce_rows_kernel(const double *__restrict__ part, int nrows, i
   }
 }
 
+// Dynamic shared memory above 48 KB needs an opt-in per kernel: raise it
+// once per kernel and device to the budget of the largest tile (so that no
+// attribute call happens while a stream is being captured into a graph).
+template <auto Kern>
+cudaError_t allow_smem(size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  if (smem > kSmemBudgetAll) return cudaErrorInvalidValue;
+  static int done_for = -1;  // one per kernel (template argument)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (done_for == dev) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudgetAll);
+  if (e == cudaSuccess) done_for = dev;
+  return e;
+}
+
 // Resident CTAs of a kernel on this device (for the persistent grid).
 template <class K>
 int resident_ctas(K kern, int threads, size_t smem) {
@@ -570,8 +590,7 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
   cudaError_t e = cudaSuccess;
   if (kMix) {
     auto kern = bop_tile_mx<Pot, kWat, kPB>;
-    if (smem > 48 * 1024)
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = allow_smem<bop_tile_mx<Pot, kWat, kPB>>(smem);
     if (e == cudaSuccess) {
       const int resident = resident_ctas(kern, kMxThreads, smem);
       const int grid = resident > 0 ? std::min(ntiles, resident) : ntiles;
@@ -582,8 +601,7 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
     }
   } else {
     auto kern = bop_tile<Pot, double, kWat, kPB>;
-    if (smem > 48 * 1024)
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = allow_smem<bop_tile<Pot, double, kWat, kPB>>(smem);
     if (e == cudaSuccess) {
       kern<<<ntiles, kBopThreads, smem, s>>>(args, pot, max_nbt, max_ntrip, status);
       note_launch();
@@ -739,7 +757,9 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
     return GB_ERROR_CAPACITY;
   }
   const int ntiles = batch ? sys.ntiles : (nat + apt - 1) / apt;
-  const int64_t nb = std::max<int64_t>(nl.nentries, 1);
+  // A captured evaluation sizes everything for the list capacity and uses
+  // the tile plan given by the caller (checked per tile by the kernel).
+  const int64_t nb = std::max<int64_t>(sys.capture ? sys.nb_capacity : nl.nentries, 1);
   GB_CHECK(pot.bond_G.ensure(sizeof(double) * 3 * nb));
   GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
   if (want_wat) GB_CHECK(pot.bond_w.ensure(sizeof(double) * 9 * nb));
@@ -751,18 +771,24 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, sys.tile_atom0,
                                                 nl.seed.as<int>(), plan);
   note_launch();
-  GB_CHECK(pot.hred.ensure(64));
-  int *hplan = pot.hred.as<int>();
-  GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
-  GB_CUDA(cudaStreamSynchronize(s));
-  GB_CHECK(neighbors_check_reverse(nl, nullptr));
-  const int max_nbt = hplan[0], max_ntrip = hplan[1];
+  int max_nbt = sys.max_nbt, max_ntrip = sys.max_ntrip;
+  if (!sys.capture) {
+    GB_CHECK(pot.hred.ensure(64));
+    int *hplan = pot.hred.as<int>();
+    GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    GB_CHECK(neighbors_check_reverse(nl, nullptr));
+    max_nbt = hplan[0];
+    max_ntrip = hplan[1];
+  }
+  pot.last_plan[0] = max_nbt;
+  pot.last_plan[1] = max_ntrip;
 
   BopArgs args;
   args.nat = nat;
   args.apt = apt;
   args.pos = nl.pos4.as<Pos4>();
-  args.el = pot.el.as<int>();
+  args.el = sys.el ? sys.el : pot.el.as<int>();
   args.seed = nl.seed.as<int>();
   args.nbr = nl.nbr.as<int>();
   args.shift = nl.shift.as<int>();
@@ -788,7 +814,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
     nl.posff_valid = true;
   }
   const float4 *posff = mixed ? nl.posff.as<float4>() : nullptr;
-  GB_CUDA(cudaEventRecord(pot.kev[0], s));
+  if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[0], s));
   if (pot.kind == kTersoff) {
     TersoffPot tp{make_tersoff_dev(pot.tp)};
     rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, max_nbt, max_ntrip,
@@ -803,7 +829,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
                                                    status, want_wat, want_pb, s, &rows);
   }
   GB_CHECK(rc);
-  GB_CUDA(cudaEventRecord(pot.kev[1], s));
+  if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
                          args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
   if (batch) {
@@ -824,6 +850,12 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   std::memcpy(sys.A, p.A, sizeof(sys.A));
   return bop_run(pot, sys, nl, o, want_wat, want_pb);
 }
+
+size_t bop_tile_smem(bool mixed, int nbt, int ntrip) {
+  return mixed ? bop_smem_bytes_mx(nbt, ntrip) : bop_smem_bytes<double>(nbt, ntrip);
+}
+
+size_t bop_tile_smem_budget() { return kSmemBudget; }
 
 int bop_batch_apt(int maxz) {
   int apt = kMaxApt;

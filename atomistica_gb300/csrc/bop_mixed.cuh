@@ -874,6 +874,7 @@ __global__ void bop_gather_mx(int nat, const int *__restrict__ seed, const int *
   const int s = seed[i], e = seed[i + 1];
   for (int b = s; b < e; b++) {
     const int rb = rev[b];
+    if (rb < 0) continue;  // (an incomplete list; reported by the reverse build)
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const float2 gr = G[3 * (size_t)rb + c], gb = G[3 * (size_t)b + c];

@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(128)
              const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
              const int *__restrict__ swrap, const int *__restrict__ cell_start,
              int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
-             int *__restrict__ shift, int2 *__restrict__ stage, int cap,
+             int *__restrict__ shift, int2 *__restrict__ stage, int cap, int clamp,
              int *__restrict__ status) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nat) return;
@@ -633,7 +633,10 @@ __global__ void __launch_bounds__(128)
     }
   }
   if (kMode != kPairsFill) {
-    counts[i] = cnt;
+    // clamp: the staged single pass without a host check (captured graphs)
+    // keeps at most cap entries per atom; status[0] still records the true
+    // maximum, which the caller compares with cap afterwards.
+    counts[i] = clamp ? min(cnt, cap) : cnt;
     atomicMax(&status[0], cnt);
   }
 }
@@ -777,8 +780,13 @@ int bin_params(const double A[3][3], const double B[3][3], const int pbc[3], dou
 // batch passes per-structure parameters bps (device) and the atoms'
 // structure ids sid; bp0 is then unused.
 int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
-             const BinParams *bps, const int *sid, int ncells, cudaStream_t stream) {
+             const BinParams *bps, const int *sid, int ncells, cudaStream_t stream,
+             bool capture) {
   const bool batch = bps != nullptr;
+  if (capture && nl.stage_cap <= 0) {
+    set_error("nl_build: a captured build needs the staged single pass (build once first)");
+    return GB_ERROR_ARGUMENT;
+  }
   GB_CHECK(nl.pos4.ensure(sizeof(Pos4) * std::max(nat, 1)));
   if (nl.want_posff) GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * std::max(nat, 1)));
   nl.posff_valid = nl.want_posff;
@@ -816,18 +824,18 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
   GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
   int *cell_atoms = nl.cell_atoms.as<int>();
   auto pairs = [&](auto mode_tag, int *counts, const int *seed, int *nbr, int *shift,
-                   int2 *stage, int cap) {
+                   int2 *stage, int cap, int clamp = 0) {
     constexpr int kMode = decltype(mode_tag)::value;
     if (batch)
       nl_pairs<kMode, true><<<(nat + 127) / 128, 128, 0, stream>>>(
           nat, bp0, bps, sid, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
           nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr, shift, stage, cap,
-          status);
+          clamp, status);
     else
       nl_pairs<kMode, false><<<(nat + 127) / 128, 128, 0, stream>>>(
           nat, bp0, nullptr, nullptr, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(),
           nl.spos.as<float4>(), nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr,
-          shift, stage, cap, status);
+          shift, stage, cap, clamp, status);
     note_launch();
   };
   if (nat > 0) {
@@ -853,15 +861,30 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
     if (nl.stage_cap > 0) {
       GB_CHECK(nl.stage.ensure(sizeof(int2) * (size_t)nat * nl.stage_cap));
       pairs(std::integral_constant<int, kPairsCountStage>(), nl.counts.as<int>(), nullptr,
-            nullptr, nullptr, nl.stage.as<int2>(), nl.stage_cap);
+            nullptr, nullptr, nl.stage.as<int2>(), nl.stage_cap, capture ? 1 : 0);
     } else {
       pairs(std::integral_constant<int, kPairsCount>(), nl.counts.as<int>(), nullptr, nullptr,
             nullptr, nullptr, 0);
     }
   }
   GB_CHECK(exclusive_scan_i32(nl.counts.as<int>(), nl.seed.as<int>(), nat, nl.scan_tmp, stream));
-  // Read back: maxz, flags, n_big, total entries.
   int *hs = nl.hstats.as<int>();
+  if (capture) {
+    // No host decisions: compact the staged entries (at most cap per atom, so
+    // at most nat * cap in all; the buffers were sized for that) and leave
+    // the status words in hstats for the caller to check after the replay.
+    if (nat > 0) {
+      nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
+                                                        nl.stage.as<int2>(), nl.nbr.as<int>(),
+                                                        nl.shift.as<int>());
+      note_launch();
+    }
+    GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
+    GB_CUDA(cudaMemcpyAsync(hs + 4, nl.seed.as<int>() + nat, sizeof(int), cudaMemcpyDeviceToHost,
+                            stream));
+    return 0;
+  }
+  // Read back: maxz, flags, n_big, total entries.
   GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
   GB_CUDA(cudaMemcpyAsync(hs + 4, nl.seed.as<int>() + nat, sizeof(int), cudaMemcpyDeviceToHost,
                           stream));
@@ -935,7 +958,7 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
   nl.dy = bp.dy;
   nl.dz = bp.dz;
   const int ncells = bp.n[0] * bp.n[1] * bp.n[2];
-  GB_CHECK(nl_build(nl, p.nat, p.r.as<double>(), bp, nullptr, nullptr, ncells, stream));
+  GB_CHECK(nl_build(nl, p.nat, p.r.as<double>(), bp, nullptr, nullptr, ncells, stream, false));
   nl.cutoff = cutoff;
   nl.valid = true;
   nl.built_for = &p;
@@ -957,7 +980,8 @@ int neighbors_build_reverse(Neighbors &nl, int nat, cudaStream_t stream, bool sy
     note_launch();
   }
   int *hs = nl.hstats.as<int>();
-  GB_CUDA(cudaMemcpyAsync(hs + 1, status + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  // (hstats[5]: the list build's own status words stay in hstats[0..4])
+  GB_CUDA(cudaMemcpyAsync(hs + 5, status + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
   nl.rev_pending = true;
   return sync ? neighbors_check_reverse(nl, stream) : 0;
 }
@@ -966,7 +990,7 @@ int neighbors_check_reverse(Neighbors &nl, cudaStream_t stream) {
   if (!nl.rev_pending) return 0;
   if (stream) GB_CUDA(cudaStreamSynchronize(stream));
   nl.rev_pending = false;
-  if (nl.hstats.as<int>()[1] & 4) {
+  if (nl.hstats.as<int>()[5] & 4) {
     set_error("Internal error: neighbour list is not symmetric.");
     return GB_ERROR_UNSPECIFIED;
   }

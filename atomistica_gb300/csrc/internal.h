@@ -184,8 +184,12 @@ int bin_params(const double A[3][3], const double B[3][3], const int pbc[3], dou
 int cell_inverse(const double A[3][3], double B[3][3]);
 // List build of nat atoms at r (device (nat,3)); a batch passes per-structure
 // parameters bps (device) and per-atom structure ids sid.
+// capture: no host synchronisation (for CUDA-graph capture); needs a
+// previous build (staged pass with capacity nl.stage_cap) and buffers sized
+// for nat * stage_cap entries; the status words land in nl.hstats.
 int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
-             const BinParams *bps, const int *sid, int ncells, cudaStream_t stream);
+             const BinParams *bps, const int *sid, int ncells, cudaStream_t stream,
+             bool capture = false);
 // Reverse-entry index of the list.  With sync = false the symmetry check is
 // deferred: call neighbors_check_reverse (stream = nullptr once the caller
 // has synchronised the stream itself) before rev is read.

@@ -90,6 +90,7 @@ struct Potential {
   int last_status = 0;
   int last_hot = 0;         // bonds recomputed on the accurate path (mixed form)
   int64_t last_bonds = 0;   // directed bonds of the last bond-order call
+  int last_plan[2] = {0, 0};  // largest bonds / (ij, ik) slots per tile of the last call
 };
 
 // Interaction range requested by bind_to for the given element pair set.
@@ -127,6 +128,12 @@ struct BopSystem {
   const double *Acells = nullptr;    // device, 9 per structure
   const float2 *Acells_ff = nullptr; // device, 9 float-float pairs per structure
   int ntiles = 0, apt = 0;
+  // Captured evaluation (CUDA graph): no host synchronisation; buffers sized
+  // for nb_capacity list entries; tile plan max_nbt / max_ntrip given.
+  bool capture = false;
+  int64_t nb_capacity = 0;
+  const int *el = nullptr;           // device element map (nullptr: the potential's)
+  int max_nbt = 0, max_ntrip = 0;
   const int *seg = nullptr;          // device, tile offsets of the structures (nseg + 1)
   int nseg = 0;
   double *red_seg = nullptr;         // device, nseg x 10
@@ -135,6 +142,10 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
             bool want_wat, bool want_pb);
 // Atoms per tile for a list whose largest coordination is maxz.
 int bop_batch_apt(int maxz);
+// Shared memory of a tile with nbt bonds and ntrip (ij, ik) slots, and the
+// largest a tile may use (bytes).
+size_t bop_tile_smem(bool mixed, int nbt, int ntrip);
+size_t bop_tile_smem_budget();
 
 }  // namespace gb
 

@@ -438,6 +438,19 @@ class Batch:
     def set_stream(self, stream):
         check(self._L.gb_batch_set_stream(self._h, stream), "batch_set_stream")
 
+    def set_options(self, graph=False, autotune=False):
+        """CUDA-graph replay of the whole evaluation; tile-size autotuning."""
+        check(self._L.gb_batch_set_options(self._h, int(bool(graph)), int(bool(autotune))),
+              "batch_set_options")
+
+    def last_info(self):
+        """{'replayed', 'atoms_per_tile', 'graph_kernels', 'tuned_candidates'}
+        of the last evaluation."""
+        v = (ctypes.c_int64 * 4)()
+        check(self._L.gb_batch_last_info(self._h, v), "batch_last_info")
+        return {"replayed": bool(v[0]), "atoms_per_tile": int(v[1]),
+                "graph_kernels": int(v[2]), "tuned_candidates": int(v[3])}
+
     def set_structures(self, structures):
         """Cells, pbc flags, atomic numbers and positions of all structures."""
         nat = np.array([len(s.positions) for s in structures], dtype=np.int32)

@@ -259,6 +259,17 @@ int gb_batch_set_structures(gb_batch_t *batch, int nstruct, const int *nat,
 /* Positions of all atoms, (total atoms, 3); host or device memory. */
 int gb_batch_set_positions(gb_batch_t *batch, const double *r);
 int gb_batch_get_nat(const gb_batch_t *batch);
+/* use_graph: after an evaluation, capture the whole evaluation (list build,
+ * tiles, gather, sums) in a CUDA graph and replay it while structures,
+ * potential and buffer sizes are unchanged (a replay whose list or tiles
+ * overflow the captured sizes is discarded and the evaluation redone
+ * eagerly).  autotune: time 64/32/16 atoms per tile on the first evaluation
+ * of a geometry and keep the fastest.  Both off by default. */
+int gb_batch_set_options(gb_batch_t *batch, int use_graph, int autotune);
+/* Last evaluation: info[0] 1 if it was a graph replay, info[1] atoms per
+ * tile, info[2] kernels in the captured graph (0: none), info[3] tile sizes
+ * timed by the autotuner. */
+int gb_batch_last_info(const gb_batch_t *batch, int64_t *info);
 /* epot[nstruct] set; f (total atoms, 3) and wpot[nstruct][3][3] (each in the
  * layout of energy_and_forces' wpot) accumulated.  Host or device memory. */
 int gb_batch_energy_and_forces(gb_batch_t *batch, gb_potential_t *pot, double *epot, double *f,

@@ -108,3 +108,57 @@ def test_batch_c4_sample_fp64(gpu):
         worst = max(worst, float(np.max(np.abs(fq - ref["f"]))))
         assert abs(e[q] - ref["epot"]) / len(s) < 1e-10, q
     assert worst < 1e-9, worst
+
+
+def test_batch_graph_replay_and_fallback(gpu):
+    from atomistica_gb300 import native
+    structs = S.si_batch(24, seed=43)
+    r0 = np.concatenate([s.positions for s in structs])
+    for prec in ("fp64", "mixed"):
+        pot = native.Tersoff(precision=prec)
+        eager = native.Batch(structs)
+        graph = native.Batch(structs)
+        graph.set_options(graph=True)
+        e0, f0, w0 = eager.energy_and_forces(pot)
+        e1, f1, w1 = graph.energy_and_forces(pot)    # eager, then captured
+        info = graph.last_info()
+        assert not info["replayed"] and info["graph_kernels"] > 0
+        e2, f2, w2 = graph.energy_and_forces(pot)    # replay
+        assert graph.last_info()["replayed"]
+        for e, f, w in ((e1, f1, w1), (e2, f2, w2)):
+            assert np.array_equal(f, f0) and np.array_equal(e, e0) and np.array_equal(w, w0)
+        # new positions: the replay rebuilds the list on the device
+        r1 = r0 + np.random.default_rng(3).uniform(-0.05, 0.05, r0.shape)
+        eager.set_positions(r1)
+        graph.set_positions(r1)
+        e0, f0, _ = eager.energy_and_forces(pot)
+        e3, f3, _ = graph.energy_and_forces(pot)
+        assert graph.last_info()["replayed"]
+        assert np.array_equal(f3, f0) and np.array_equal(e3, e0)
+        # a denser configuration overflows the captured list capacity: the
+        # replay is discarded and the evaluation redone eagerly
+        dense = r0.copy()
+        sl = slice(int(graph.offsets[0]), int(graph.offsets[1]))
+        c = dense[sl].mean(axis=0)
+        dense[sl] = c + 0.6 * (dense[sl] - c)
+        eager.set_positions(dense)
+        graph.set_positions(dense)
+        e0, f0, _ = eager.energy_and_forces(pot)
+        e4, f4, _ = graph.energy_and_forces(pot)
+        assert not graph.last_info()["replayed"]
+        assert np.array_equal(f4, f0) and np.array_equal(e4, e0)
+
+
+def test_batch_autotune(gpu):
+    from atomistica_gb300 import native
+    structs = S.si_batch(16, seed=44)
+    pot = native.Tersoff()
+    plain = native.Batch(structs)
+    tuned = native.Batch(structs)
+    tuned.set_options(autotune=True)
+    e0, f0, _ = plain.energy_and_forces(pot)
+    e1, f1, _ = tuned.energy_and_forces(pot)
+    info = tuned.last_info()
+    assert info["tuned_candidates"] >= 1 and info["atoms_per_tile"] in (8, 16, 32, 64)
+    assert np.array_equal(f1, f0)  # per-bond sums do not depend on the tiles
+    assert np.max(np.abs(e1 - e0)) <= 1e-12 * np.max(np.abs(e0))
