@@ -61,6 +61,7 @@ SIGNATURES = [
     ("gb_batch_set_positions", _I, [_P, _P]),
     ("gb_batch_get_nat", _I, [_P]),
     ("gb_batch_set_options", _I, [_P, _I, _I]),
+    ("gb_random_packing", _I, [_I, _P, ctypes.c_double, ctypes.c_uint64, ctypes.c_int64, _P]),
     ("gb_batch_last_info", _I, [_P, _P]),
     ("gb_batch_energy_and_forces", _I, [_P, _P, _P, _P, _P]),
     ("gb_batch_tersoff_tangent", _I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),

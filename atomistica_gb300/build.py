@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libatomistica_gb300.so")
 SOURCES = ["core.cu", "bop.cu", "eam.cu", "api.cu", "diag.cu", "batch.cu",
-           "autodiff.cu"]
+           "autodiff.cu", "workload.cu"]
 HEADERS = ["internal.h", "potential.h", "bop_math.h", "ff.h", "ff_tables.h", "bop_mixed.cuh",
            "batch.h"]
 

@@ -9,6 +9,7 @@ reference's tests (ase.lattice.cubic.Diamond / FaceCenteredCubic); atom order
 within the supercell does not affect any energy, force or virial.
 """
 
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -140,82 +141,19 @@ def tersoff_si_amorphous(natoms=1048576, seed=3, sigma=0.25, rho_gcc=2.33):
     return s
 
 
-def _random_packing(rng, nat, cell, dmin, max_tries=5000000, block=64):
-    """Uniform fractional positions with every pair (all periodic images)
-    separated by at least ``dmin``: random sequential addition.  Candidates
-    are drawn ``block`` at a time; each is tested against the accepted atoms
-    of its own and the 26 neighbouring bins of a periodic grid whose bins are
-    at least ``dmin`` high (all periodic images of the cell when the grid
-    would have fewer than 3 bins along an axis), then accepted in order."""
-    inv = np.linalg.inv(cell)
-    heights = 1.0 / np.linalg.norm(inv, axis=0)
-    nimg = np.ceil(dmin / heights).astype(int)
-    shifts = np.stack(np.meshgrid(*[np.arange(-k, k + 1) for k in nimg], indexing="ij"),
-                      axis=-1).reshape(-1, 3).astype(float)
-    img = shifts @ cell  # (nimg, 3)
-    dmin2 = dmin * dmin
-    if nat > 0:
-        # self-images must also be separated
-        d = img[np.any(shifts != 0, axis=1)]
-        if len(d) and np.min(np.einsum("ij,ij->i", d, d)) < dmin2:
-            raise RuntimeError("cell too small for dmin")
+def _random_packing(rng, nat, cell, dmin, max_tries=50000000):
+    """Uniform positions in ``cell`` with every pair (all periodic images)
+    separated by at least ``dmin``: random sequential addition in the
+    library's host code (gb_random_packing), seeded from ``rng``."""
+    from . import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from .build import build
+        build()
+    seed = int(rng.integers(0, 2 ** 63))
+    cell = np.ascontiguousarray(cell, dtype=np.float64)
     pos = np.empty((nat, 3))
-    frac = np.empty((nat, 3))
-    ng = np.floor(heights / dmin).astype(int)
-    use_grid = bool(np.all(ng >= 3))
-    if use_grid:
-        cap = 16
-        occ = np.full((ng[0], ng[1], ng[2], cap), -1, dtype=np.int64)
-        nocc = np.zeros((ng[0], ng[1], ng[2]), dtype=np.int64)
-        offs = np.stack(np.meshgrid([-1, 0, 1], [-1, 0, 1], [-1, 0, 1], indexing="ij"),
-                        axis=-1).reshape(-1, 3)
-    n = 0
-    tries = 0
-
-    def clear(c, others):
-        if len(others) == 0:
-            return True
-        d = others[:, None, :] - c[None, None, :] + img[None, :, :]
-        return np.min(np.einsum("ijk,ijk->ij", d, d)) >= dmin2
-
-    while n < nat:
-        tries += block
-        if tries > max_tries:
-            raise RuntimeError("random packing failed")
-        cf = rng.random((block, 3))
-        cand = cf @ cell
-        if n == 0:
-            ok = np.ones(block, dtype=bool)
-        elif use_grid:
-            gc = np.minimum((cf * ng).astype(np.int64), ng - 1)      # (K, 3)
-            nb = gc[:, None, :] + offs[None, :, :]                   # (K, 27, 3)
-            wrap = np.floor_divide(nb, ng)                           # periodic image of the bin
-            nb -= wrap * ng
-            idx = occ[nb[..., 0], nb[..., 1], nb[..., 2]]           # (K, 27, cap)
-            valid = idx >= 0
-            # frac of the occupant, shifted to the candidate's image
-            of = frac[np.where(valid, idx, 0)] + wrap[:, :, None, :]
-            d = (of - cf[:, None, None, :]) @ cell
-            d2 = np.einsum("kbcx,kbcx->kbc", d, d)
-            ok = np.all(np.where(valid, d2 >= dmin2, True), axis=(1, 2))
-        else:
-            d = pos[:n, None, None, :] - cand[None, :, None, :] + img[None, None, :, :]
-            ok = np.min(np.einsum("ijkl,ijkl->ijk", d, d), axis=(0, 2)) >= dmin2
-        n0 = n
-        for k in np.nonzero(ok)[0]:
-            if clear(cand[k], pos[n0:n]):
-                pos[n] = cand[k]
-                frac[n] = cf[k]
-                if use_grid:
-                    g = np.minimum((cf[k] * ng).astype(np.int64), ng - 1)
-                    c = nocc[g[0], g[1], g[2]]
-                    if c >= cap:
-                        raise RuntimeError("random packing: bin overflow")
-                    occ[g[0], g[1], g[2], c] = n
-                    nocc[g[0], g[1], g[2]] = c + 1
-                n += 1
-                if n == nat:
-                    break
+    _lib.check(_lib.load().gb_random_packing(int(nat), cell.ctypes.data, float(dmin), seed,
+                                   int(max_tries), pos.ctypes.data), "random_packing")
     return pos
 
 

@@ -259,14 +259,19 @@ def batch_config(dev, oracle, nth):
     t_gen = time.perf_counter() - t0
     nat = sum(len(q) for q in structs)
     params = parameters.Tersoff_PRB_39_5566_Si_C
-    b = native.Batch(structs)
     r = torch.tensor(np.concatenate([q.positions for q in structs]), dtype=torch.float64,
                      device=dev)
     f = torch.zeros((nat, 3), dtype=torch.float64, device=dev)
     entry = {"nstruct": len(structs), "natoms": nat, "unit": UNIT,
              "generation_s": t_gen, "sample": "all 2048 structures"}
     refs = [oracle.bop_compute("tersoff", params, q, nthreads=nth) for q in structs]
-    for prec in ("fp64", "mixed"):
+    # eager (list build and tile plan read back to the host each step) and
+    # CUDA-graph replay of the whole step with autotuned tiles
+    for name in ("fp64", "mixed", "fp64_graph", "mixed_graph"):
+        prec = name.split("_")[0]
+        graph = name.endswith("_graph")
+        b = native.Batch(structs)
+        b.set_options(graph=graph, autotune=graph)
         pot = native.Tersoff(precision=prec)
         for _ in range(3):
             f.zero_()
@@ -287,8 +292,10 @@ def batch_config(dev, oracle, nth):
         df = max(float(np.max(np.abs(fh[off[q]:off[q + 1]] - refs[q]["f"])))
                  for q in range(len(structs)))
         de = max(abs(eh[q] - refs[q]["epot"]) / len(structs[q]) for q in range(len(structs)))
-        entry[prec] = {"value": nat / t, "ms_per_step": 1e3 * t, "max_abs_dF": df,
-                       "max_abs_dE_per_atom": de}
+        info = b.last_info()
+        entry[name] = {"value": nat / t, "ms_per_step": 1e3 * t, "max_abs_dF": df,
+                       "max_abs_dE_per_atom": de, "atoms_per_tile": info["atoms_per_tile"],
+                       "replayed": info["replayed"], "graph_kernels": info["graph_kernels"]}
     # the same structures one call each (particles + list + potential per structure)
     pot = native.Tersoff(precision="fp64")
     objs = []

@@ -310,6 +310,13 @@ uint64_t gb_kernel_launches(void);
 /* FMA-chain microbenchmark on the current device: sustained FP64 (fp64=1)
  * or FP32 (fp64=0) throughput in TFLOP/s (2 flops per FMA). */
 int gb_bench_fma_peak(int fp64, double *tflops);
+/* Host-only generator of the random workload structures: nat uniform
+ * positions (pos: nat x 3, Cartesian) in the cell (rows = lattice vectors)
+ * with every pair, over all periodic images, at least dmin apart (random
+ * sequential addition, xoshiro256** stream of the given seed; at most
+ * max_tries candidates).  Same result on every host. */
+int gb_random_packing(int nat, const double *cell, double dmin, uint64_t seed,
+                      int64_t max_tries, double *pos);
 
 #ifdef __cplusplus
 }

@@ -90,3 +90,20 @@ def test_frontend_fails_loudly_without_gpu():
         pytest.skip("a GPU is present")
     with pytest.raises(_lib.AtomisticaError):
         native.from_atoms(S.diamond("Si", 5.431))
+
+
+def test_random_packing_generator():
+    # grid path (large cell) and all-images path (thin triclinic cell)
+    for nat, cell in ((200, np.diag([14.0, 15.0, 16.0])),
+                      (12, np.array([[5.0, 0.0, 0.0], [2.6, 4.9, 0.0], [1.0, 1.2, 6.0]]))):
+        a = S._random_packing(np.random.default_rng(5), nat, cell, 2.0)
+        b = S._random_packing(np.random.default_rng(5), nat, cell, 2.0)
+        assert np.array_equal(a, b)
+        fr = a @ np.linalg.inv(cell)
+        assert np.all((fr > -1e-12) & (fr < 1 + 1e-12))
+        shifts = np.array([[i, j, k] for i in (-1, 0, 1) for j in (-1, 0, 1)
+                           for k in (-1, 0, 1)], dtype=float) @ cell
+        d = a[:, None, None, :] - a[None, :, None, :] + shifts[None, None, :, :]
+        r2 = np.einsum("ijsk,ijsk->ijs", d, d)
+        r2[np.arange(nat), np.arange(nat), 13] = np.inf  # self, zero shift
+        assert np.sqrt(r2.min()) >= 2.0
