@@ -53,9 +53,7 @@ int batch_elements(Batch &b, Potential &pot, cudaStream_t s) {
 // Interaction range: the largest r2 over the element pairs present
 // (default_bind_to_func.f90:123-144).
 double batch_cutoff(const Batch &b, const Potential &pot) {
-  std::vector<int> zs(b.hZ.begin(), b.hZ.end());
-  std::sort(zs.begin(), zs.end());
-  zs.erase(std::unique(zs.begin(), zs.end()), zs.end());
+  const std::vector<int> &zs = b.zu;
   const int nel = pot_nel(pot);
   auto dbidx = [&](int Z) {
     for (int q = 0; q < nel; q++)
@@ -358,6 +356,8 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
   b.graph_pot = &pot;
   b.graph_prec = pot.precision;
   b.graph_apt = apt;
+  b.graph_cap = cap;
+  b.graph_ncells = b.ncells;
   b.graph_bufs = graph_buffers(b, pot);
   (void)mixed;
 }
@@ -365,6 +365,7 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
 bool graph_current(const Batch &b, const Potential &pot) {
   return b.graph_exec && b.graph_geom == b.geom_rev && b.graph_pot == &pot &&
          b.graph_prec == pot.precision && b.graph_apt == b.tiles_apt &&
+         b.graph_ncells == b.ncells &&
          b.graph_bufs == graph_buffers(b, pot);
 }
 
@@ -380,7 +381,7 @@ int batch_replay(Batch &b, Potential &pot, double *epot, double *f, double *wpot
   note_launch(b.graph_kernels);
   const int *hs = b.nl.hstats.as<int>();
   const int *st = reinterpret_cast<const int *>(pot.hred.as<double>() + 12);
-  const bool ok = hs[0] <= b.nl.stage_cap && (hs[1] & (1 | 2)) == 0 && (hs[5] & 4) == 0 &&
+  const bool ok = hs[0] <= b.graph_cap && (hs[1] & (1 | 2)) == 0 && (hs[5] & 4) == 0 &&
                   (st[0] & 2) == 0;
   if (!ok) {
     drop_graph(b);
@@ -577,6 +578,9 @@ int gb_batch_set_structures(gb_batch_t *h, int nstruct, const int *nat, const do
   b.B = B;
   b.pbc = pb;
   b.hZ.assign(Z ? Z : nullptr, Z ? Z + total : nullptr);
+  b.zu = b.hZ;
+  std::sort(b.zu.begin(), b.zu.end());
+  b.zu.erase(std::unique(b.zu.begin(), b.zu.end()), b.zu.end());
   b.geom_rev++;
   b.pos_rev++;
   b.nl.valid = false;

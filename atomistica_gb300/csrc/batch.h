@@ -15,6 +15,7 @@ struct Batch {
   std::vector<double> B;      // inverses
   std::vector<int> pbc;       // 3 per structure
   std::vector<int> hZ;        // nat
+  std::vector<int> zu;        // distinct atomic numbers of the batch (sorted)
   uint64_t geom_rev = 0, pos_rev = 0;
   DevBuf r, sid, bps, Acells, Acells_ff, tiles, red_seg, el;
   DevBuf tan_G, tan_part, tan_f, tan_dpos, tan_red;  // tangent evaluation scratch
@@ -45,6 +46,7 @@ struct Batch {
   uint64_t graph_geom = ~0ull;
   const Potential *graph_pot = nullptr;
   int graph_prec = -1, graph_apt = 0, graph_kernels = 0;
+  int graph_cap = 0, graph_ncells = 0;  // list capacity per atom, cells: baked into the graph
   std::vector<const void *> graph_bufs;
   DevBuf gf;  // forces accumulated by the graph
   int64_t info[4] = {0, 0, 0, 0};  // last call: replayed, atoms/tile, kernels in graph, tuned

@@ -3,12 +3,12 @@
 // :423-627 (kernel), with the natural cubic spline of
 // src/support/simple_spline.f90:127-195, 373-614).
 //
-//   eam_density  one warp per atom i (lanes strided over its list entries):
+//   eam_density  four lanes per atom i (strided over its list entries):
 //                rho_i = sum_j rho_{el j}(r_ij) (no extrapolation: an argument
 //                outside the table raises an error as in the serial reference),
 //                rho clamped at 0, F_i and F'_i with index-clamped
 //                extrapolation (:506-554).
-//   eam_pair     one warp per atom i: for each entry (i->j) the i-side term of
+//   eam_pair     four lanes per atom i: for each entry (i->j) the i-side term of
 //                the reference (:561-607) and the j-side term of the mirror
 //                entry (j->i) (same r, exactly negated pair vector), so that
 //                f_i = sum_j [df_ij - df_ji] is a gather: no atomics, no
@@ -17,6 +17,10 @@
 // Spline coefficients are built on the host in FP64 with the reference's
 // operation order and uploaded as 8 doubles per interval
 // {y, c1, c2, c3, d1, d2, d3, 0}: a value gather is one 32-byte sector.
+// rho and phi of a setfl file share one r grid, so a pair locates its
+// interval once for all of its splines; the interval coordinate is
+// (r - x0) * (1/dx) and r, 1/r come from one reciprocal square root (both
+// within an ulp or two of the reference's divisions and square root).
 
 #include <cuda_runtime.h>
 
@@ -201,6 +205,7 @@ int eam_upload(EamTables &t) {
     d.n = s.n;
     d.x0 = s.x0;
     d.dx = s.dx;
+    d.rdx = 1.0 / s.dx;
     d.cut = s.cut;
     return d;
   };
@@ -232,49 +237,6 @@ struct EamArgs {
   double *part;           // 10 per block
   int *status;
 };
-
-// simple_spline_f / _df without extrapolation (:373-528): 1-based interval
-// index i = floor((x-x0)/dx + 1), or n-1 at x == cut; out of range -> error.
-__device__ __forceinline__ bool spline_index(const SplineDev &s, double x, double &B, int &k) {
-  double xf;
-  int i;
-  if (x == s.cut) {
-    xf = s.n;
-    i = s.n - 1;
-  } else {
-    xf = (x - s.x0) / s.dx + 1;
-    const double fl = floor(xf);
-    i = (fl < -1e9) ? -1000000000 : (fl > 1e9 ? 1000000000 : (int)fl);
-  }
-  if (i < 1 || i >= s.n) return false;
-  B = xf - i;
-  k = i - 1;
-  return true;
-}
-
-__device__ __forceinline__ double spline_f(const SplineDev &s, double x, int *err) {
-  double B;
-  int k;
-  if (!spline_index(s, x, B, k)) {
-    *err = 1;
-    return 1.0;
-  }
-  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k);
-  const double2 a = __ldg(t), b = __ldg(t + 1);
-  return a.x + B * (a.y + B * (b.x + B * b.y));
-}
-
-__device__ __forceinline__ double spline_df(const SplineDev &s, double x, int *err) {
-  double B;
-  int k;
-  if (!spline_index(s, x, B, k)) {
-    *err = 1;
-    return 1.0;
-  }
-  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k + 4);
-  const double2 c = __ldg(t), d = __ldg(t + 1);
-  return c.x + B * (c.y + B * d.x);
-}
 
 // simple_spline_f_and_df with extrapolate=.true. (:536-614).
 __device__ __forceinline__ void spline_fdf_extrap(const SplineDev &s, double x, double &f,
@@ -327,141 +289,216 @@ __device__ __forceinline__ double warp_sum(double x) {
 }
 
 constexpr int kEamThreads = 256;
+// Lanes per atom: an atom's list entries are strided over a group of 4
+// consecutive lanes (about 11 entries per lane for the ~43 neighbours of fcc
+// at 5 A), 8 atoms per warp.
+constexpr int kEamLanes = 4;
+
+__device__ __forceinline__ double group_sum(double x) {
+#pragma unroll
+  for (int o = 1; o < kEamLanes; o <<= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Interval of r on the grid that rho and phi share in a setfl file (nr + 2
+// points from 0 with step dr): 0-based k and local coordinate B of
+// simple_spline (:373-434), with k clamped to the table for the
+// extrapolating phi; ok = false where the non-extrapolating rho is out of
+// range (an error in the reference).
+__device__ __forceinline__ void r_interval(const SplineDev &s, double r, double &B, int &k,
+                                           bool &ok) {
+  const double xf = (r - s.x0) * s.rdx + 1.0;
+  const double fl = floor(xf);
+  int i = (int)fmin(fmax(fl, -1.0e9), 1.0e9);
+  ok = i >= 1 && (i < s.n || r <= s.cut);
+  i = min(max(i, 1), s.n - 1);
+  B = xf - i;
+  k = i - 1;
+}
+
+__device__ __forceinline__ void interval_fdf(const SplineDev &s, int k, double B, double &f,
+                                             double &df) {
+  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k);
+  const double2 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2), d = __ldg(t + 3);
+  f = a.x + B * (a.y + B * (b.x + B * b.y));
+  df = c.x + B * (c.y + B * d.x);
+}
+
+__device__ __forceinline__ double interval_f(const SplineDev &s, int k, double B) {
+  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k);
+  const double2 a = __ldg(t), b = __ldg(t + 1);
+  return a.x + B * (a.y + B * (b.x + B * b.y));
+}
+
+__device__ __forceinline__ double interval_df(const SplineDev &s, int k, double B) {
+  const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k + 4);
+  const double2 c = __ldg(t), d = __ldg(t + 1);
+  return c.x + B * (c.y + B * d.x);
+}
 
 __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
-  const int warp = (blockIdx.x * kEamThreads + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= a.nat) return;
-  const int i = warp;
-  const int eli = a.el[i];
-  if (eli < 0 || (a.mask && a.mask[i] == 0)) {
-    if (lane == 0) {
-      a.Fi[i] = 0.0;
-      a.dFi[i] = 0.0;
-    }
-    return;
+  const int gt = blockIdx.x * kEamThreads + threadIdx.x;
+  const int i = gt / kEamLanes, sub = gt % kEamLanes;
+  int eli = -1;
+  bool on = false;
+  if (i < a.nat) {
+    eli = a.el[i];
+    on = eli >= 0 && !(a.mask && a.mask[i] == 0);
   }
-  const Pos4 pi = a.pos[i];
   double rho = 0.0;
-  int err = 0;
-  const int s = a.seed[i], e = a.seed[i + 1];
-  for (int b = s + lane; b < e; b += 32) {
-    const int j = a.nbr[b];
-    const int elj = a.el[j];
-    if (elj < 0) continue;
-    double d[3];
-    get_drj(a, pi, a.pos[j], a.shift[b], d);
-    const double r2 = norm2_ref(d);
-    if (r2 < a.cutoff_sq) rho += spline_f(a.rho[elj], sqrt(r2), &err);
+  bool bad = false;
+  if (on) {
+    const Pos4 pi = a.pos[i];
+    const int s = a.seed[i], e = a.seed[i + 1];
+    for (int b = s + sub; b < e; b += kEamLanes) {
+      const int j = a.nbr[b];
+      const int elj = a.el[j];
+      if (elj < 0) continue;
+      double d[3];
+      get_drj(a, pi, a.pos[j], a.shift[b], d);
+      const double r2 = norm2_ref(d);
+      if (r2 < a.cutoff_sq) {
+        double B;
+        int k;
+        bool ok;
+        r_interval(a.rho[elj], sqrt(r2), B, k, ok);
+        bad |= !ok;
+        rho += interval_f(a.rho[elj], k, B);
+      }
+    }
   }
-  rho = warp_sum(rho);
-  if (err) atomicOr(a.status, 1);
-  if (lane == 0) {
-    if (rho < 0.0) rho = 0.0;
-    double F, dF;
-    spline_fdf_extrap(a.F[eli], rho, F, dF);
+  rho = group_sum(rho);  // (every lane takes part in the shuffles)
+  if (bad) atomicOr(a.status, 1);
+  if (i < a.nat && sub == 0) {
+    double F = 0.0, dF = 0.0;
+    if (on) {
+      if (rho < 0.0) rho = 0.0;
+      spline_fdf_extrap(a.F[eli], rho, F, dF);
+    }
     a.Fi[i] = F;
     a.dFi[i] = dF;
   }
 }
 
+// Virial components kept once (the pair virial is symmetric):
+// xx, yy, zz, xy, xz, yz; Fortran (c2 + 3 c) order of the 9 on output.
+__device__ __forceinline__ int sym_index(int c2, int c) {
+  return c2 == c ? c : 2 + c2 + c;  // (0,1) -> 3, (0,2) -> 4, (1,2) -> 5
+}
+
 template <bool kEpa, bool kWat>
 __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
-  __shared__ double sred[kEamThreads / 32][10];
-  const int wib = threadIdx.x >> 5;
-  const int warp = (blockIdx.x * kEamThreads + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  double e_tot = 0.0;
-  double w_tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if (warp < a.nat) {
-    const int i = warp;
-    const int eli = a.el[i];
-    double F3[3] = {0.0, 0.0, 0.0};
-    double Wa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    double Ei = 0.0;
-    if (eli >= 0) {
-      const bool mi = !(a.mask && a.mask[i] == 0);
-      const double dFi = mi ? a.dFi[i] : 0.0;
-      const Pos4 pi = a.pos[i];
-      int err = 0;
-      const int s = a.seed[i], e = a.seed[i + 1];
-      for (int b = s + lane; b < e; b += 32) {
-        const int j = a.nbr[b];
-        const int elj = a.el[j];
-        if (elj < 0) continue;
-        double d[3];
-        get_drj(a, pi, a.pos[j], a.shift[b], d);
-        const double r2 = norm2_ref(d);
-        if (!(r2 < a.cutoff_sq)) continue;
-        const bool mj = !(a.mask && a.mask[j] == 0);
-        const double r = sqrt(r2);
-        const double rinv = 1.0 / r;
-        double phi, dphi;
-        spline_fdf_extrap(a.phi[eli * a.nel + elj], r, phi, dphi);
-        const double pair = (dphi - phi * rinv) * rinv;
-        if (mi) {
-          // i-side of entry (i->j), :577-607
-          const double fac = spline_df(a.rho[elj], r, &err);
-          const double sc = -(dFi * fac + pair) * rinv;
-          Ei += phi * rinv;
+  __shared__ double sred[kEamThreads / 32][7];
+  const int gt = blockIdx.x * kEamThreads + threadIdx.x;
+  const int i = gt / kEamLanes, sub = gt % kEamLanes;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double w6[6] = {0, 0, 0, 0, 0, 0};  // total virial of this lane's entries
+  double F3[3] = {0.0, 0.0, 0.0};
+  double Wa[6] = {0, 0, 0, 0, 0, 0};  // per-atom virial of atom i
+  double Ei = 0.0;
+  const int eli = i < a.nat ? a.el[i] : -1;
+  const bool mi = eli >= 0 && !(a.mask && a.mask[i] == 0);
+  if (eli >= 0) {
+    const double dFi = mi ? a.dFi[i] : 0.0;
+    const Pos4 pi = a.pos[i];
+    bool bad = false;
+    const int s = a.seed[i], e = a.seed[i + 1];
+    for (int b = s + sub; b < e; b += kEamLanes) {
+      const int j = a.nbr[b];
+      const int elj = a.el[j];
+      if (elj < 0) continue;
+      double d[3];
+      get_drj(a, pi, a.pos[j], a.shift[b], d);
+      const double r2 = norm2_ref(d);
+      if (!(r2 < a.cutoff_sq)) continue;
+      const bool mj = !(a.mask && a.mask[j] == 0);
+      const double rinv = rsqrt(r2);
+      const double r = r2 * rinv;
+      // rho and phi share the r grid: one interval for all three splines
+      const SplineDev &sp = a.phi[eli * a.nel + elj];
+      double B;
+      int k;
+      bool ok;
+      r_interval(sp, r, B, k, ok);
+      double phi, dphi;
+      interval_fdf(sp, k, B, phi, dphi);
+      const double pair = (dphi - phi * rinv) * rinv;
+      double fac_i = 0.0;
+      if (mi) {
+        // i-side of entry (i->j), :577-607: df = sc d, f_i += df,
+        // w += -d (x) df
+        bad |= !ok;
+        fac_i = interval_df(a.rho[elj], k, B);
+        const double sc = -(dFi * fac_i + pair) * rinv;
+        Ei += phi * rinv;
+        const double df[3] = {sc * d[0], sc * d[1], sc * d[2]};
+        F3[0] += df[0];
+        F3[1] += df[1];
+        F3[2] += df[2];
+        const double w[6] = {-d[0] * df[0], -d[1] * df[1], -d[2] * df[2],
+                             -d[0] * df[1], -d[0] * df[2], -d[1] * df[2]};
 #pragma unroll
-          for (int c = 0; c < 3; c++) {
-            const double df = sc * d[c];
-            F3[c] += df;
-#pragma unroll
-            for (int c2 = 0; c2 < 3; c2++) {
-              const double w = -d[c2] * df;  // (c2, c) Fortran
-              w_tot[c2 + 3 * c] += w;
-              if (kWat) Wa[c2 + 3 * c] += 0.5 * w;
-            }
-          }
-        }
-        if (mj) {
-          // j-side of the mirror entry (j->i): dr' = -d, acts on i with -df'.
-          const double fac = spline_df(a.rho[eli], r, &err);
-          const double sc = -(a.dFi[j] * fac + pair) * rinv;
-#pragma unroll
-          for (int c = 0; c < 3; c++) {
-            const double dfp = sc * (-d[c]);
-            F3[c] -= dfp;
-            if (kWat)
-#pragma unroll
-              for (int c2 = 0; c2 < 3; c2++) Wa[c2 + 3 * c] += 0.5 * (d[c2] * dfp);
-          }
+        for (int c = 0; c < 6; c++) {
+          w6[c] += w[c];
+          if (kWat) Wa[c] += 0.5 * w[c];
         }
       }
-      if (err) atomicOr(a.status, 1);
+      if (mj) {
+        // j-side of the mirror entry (j->i): dr' = -d, acts on i with -df'.
+        bad |= !ok;
+        const double fac_j = (mi && elj == eli) ? fac_i : interval_df(a.rho[eli], k, B);
+        const double sc = -(a.dFi[j] * fac_j + pair) * rinv;
+        const double dfp[3] = {-sc * d[0], -sc * d[1], -sc * d[2]};
+        F3[0] -= dfp[0];
+        F3[1] -= dfp[1];
+        F3[2] -= dfp[2];
+        if (kWat) {
+          Wa[0] += 0.5 * (d[0] * dfp[0]);
+          Wa[1] += 0.5 * (d[1] * dfp[1]);
+          Wa[2] += 0.5 * (d[2] * dfp[2]);
+          Wa[3] += 0.5 * (d[0] * dfp[1]);
+          Wa[4] += 0.5 * (d[0] * dfp[2]);
+          Wa[5] += 0.5 * (d[1] * dfp[2]);
+        }
+      }
+    }
+    if (bad) atomicOr(a.status, 1);
+  }
+  // group sums (every lane takes part in the shuffles)
 #pragma unroll
-      for (int c = 0; c < 3; c++) F3[c] = warp_sum(F3[c]);
-      Ei = warp_sum(Ei);
+  for (int c = 0; c < 3; c++) F3[c] = group_sum(F3[c]);
+  Ei = group_sum(Ei);
+  if (kWat)
+#pragma unroll
+    for (int c = 0; c < 6; c++) Wa[c] = group_sum(Wa[c]);
+  double e_tot = 0.0;
+  if (eli >= 0) {
+    if (mi) Ei += a.Fi[i];
+    if (sub == 0) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) a.f[3 * (size_t)i + c] += F3[c];
+      if (kEpa && mi) a.epa[i] += Ei;
       if (kWat)
 #pragma unroll
-        for (int c = 0; c < 9; c++) Wa[c] = warp_sum(Wa[c]);
-      if (mi) Ei += a.Fi[i];
-      if (lane == 0) {
-#pragma unroll
-        for (int c = 0; c < 3; c++) a.f[3 * (size_t)i + c] += F3[c];
-        if (kEpa && mi) a.epa[i] += Ei;
-        if (kWat)
-#pragma unroll
-          for (int c = 0; c < 9; c++) a.wpa[9 * (size_t)i + c] += Wa[c];
-      }
-      e_tot = (lane == 0 && mi) ? Ei : 0.0;
+        for (int q = 0; q < 9; q++) a.wpa[9 * (size_t)i + q] += Wa[sym_index(q % 3, q / 3)];
+      if (mi) e_tot = Ei;
     }
   }
-  // Block partials: energy (lane 0 of each warp holds it) and virial.
+  // Block partials: energy and virial.
 #pragma unroll
-  for (int c = 0; c < 9; c++) w_tot[c] = warp_sum(w_tot[c]);
+  for (int c = 0; c < 6; c++) w6[c] = warp_sum(w6[c]);
   e_tot = warp_sum(e_tot);
   if (lane == 0) {
     sred[wib][0] = e_tot;
 #pragma unroll
-    for (int c = 0; c < 9; c++) sred[wib][1 + c] = w_tot[c];
+    for (int c = 0; c < 6; c++) sred[wib][1 + c] = w6[c];
   }
   __syncthreads();
   if (threadIdx.x < 10) {
+    const int col = threadIdx.x == 0 ? 0 : 1 + sym_index((threadIdx.x - 1) % 3,
+                                                         (threadIdx.x - 1) / 3);
     double s = 0.0;
-    for (int w = 0; w < kEamThreads / 32; w++) s += sred[w][threadIdx.x];
+    for (int w = 0; w < kEamThreads / 32; w++) s += sred[w][col];
     a.part[10 * (size_t)blockIdx.x + threadIdx.x] = s;
   }
 }
@@ -503,7 +540,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   a.f = o.f;
   a.epa = o.epot_per_at;
   a.wpa = o.wpot_per_at;
-  const int blocks = (nat * 32 + kEamThreads - 1) / kEamThreads;
+  const int blocks = (int)(((int64_t)nat * kEamLanes + kEamThreads - 1) / kEamThreads);
   GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * blocks + 64));
   a.part = pot.tile_part.as<double>();
   a.status = o.status;

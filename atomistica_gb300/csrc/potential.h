@@ -29,6 +29,7 @@ struct SplineDev {
   const double *tab;  // 8*(n-1) doubles
   int n;
   double x0, dx, cut;
+  double rdx;  // 1 / dx
 };
 
 struct EamTables {
