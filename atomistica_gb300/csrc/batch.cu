@@ -275,16 +275,24 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
   const int cap = b.nl.stage_cap;
   if (cap <= 0 || b.nat == 0) return;
   const int64_t capacity = (int64_t)b.nat * cap;
-  // plan with head room for the next configurations (checked per tile)
+  // Tile plan with head room for the next configurations (checked per tile
+  // by the kernel): as much as fits without fewer resident CTAs per SM than
+  // the exact plan of this evaluation, at most +25 % bonds / +50 % slots.
   const int apt = b.tiles_apt;
-  int max_nbt = std::min(apt * cap, pot.last_plan[0] + pot.last_plan[0] / 4 + 16);
-  int max_ntrip = std::min(apt * cap * cap, pot.last_plan[1] + pot.last_plan[1] / 2 + 64);
-  if (pot.last_plan[0] == 0) return;
+  const int nbt0 = pot.last_plan[0], ntrip0 = pot.last_plan[1];
+  if (nbt0 == 0) return;
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
-  while (bop_tile_smem(mixed, max_nbt, max_ntrip) > bop_tile_smem_budget() &&
-         (max_nbt > pot.last_plan[0] || max_ntrip > pot.last_plan[1])) {
-    max_nbt = std::max(pot.last_plan[0], max_nbt - max_nbt / 8 - 1);
-    max_ntrip = std::max(pot.last_plan[1], max_ntrip - max_ntrip / 8 - 1);
+  const int occ0 = bop_tile_ctas_per_sm(pot, bop_tile_smem(mixed, nbt0, ntrip0));
+  int max_nbt = nbt0, max_ntrip = ntrip0;
+  for (int step = 16; step >= 1; step--) {  // head room step/16 of the maxima
+    const int nb = std::min(apt * cap, nbt0 + nbt0 * step / 64 + step);
+    const int nt = std::min(apt * cap * cap, ntrip0 + ntrip0 * step / 32 + 4 * step);
+    const size_t sm = bop_tile_smem(mixed, nb, nt);
+    if (sm <= bop_tile_smem_budget() && bop_tile_ctas_per_sm(pot, sm) >= occ0) {
+      max_nbt = nb;
+      max_ntrip = nt;
+      break;
+    }
   }
   Neighbors &nl = b.nl;
   if (nl.nbr.ensure(sizeof(int) * capacity) || nl.shift.ensure(sizeof(int) * capacity) ||

@@ -857,6 +857,26 @@ size_t bop_tile_smem(bool mixed, int nbt, int ntrip) {
 
 size_t bop_tile_smem_budget() { return kSmemBudget; }
 
+namespace {
+template <auto Kern>
+int ctas_per_sm(int threads, size_t smem) {
+  if (allow_smem<Kern>(smem) != cudaSuccess) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kern, threads, smem) != cudaSuccess)
+    return 0;
+  return per_sm;
+}
+}  // namespace
+
+int bop_tile_ctas_per_sm(const Potential &pot, size_t smem) {
+  const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  if (pot.kind == kTersoff)
+    return mixed ? ctas_per_sm<bop_tile_mx<TersoffPot, false, false>>(kMxThreads, smem)
+                 : ctas_per_sm<bop_tile<TersoffPot, double, false, false>>(kBopThreads, smem);
+  return mixed ? ctas_per_sm<bop_tile_mx<KumagaiPot, false, false>>(kMxThreads, smem)
+               : ctas_per_sm<bop_tile<KumagaiPot, double, false, false>>(kBopThreads, smem);
+}
+
 int bop_batch_apt(int maxz) {
   int apt = kMaxApt;
   while (apt > 1 && bop_smem_bytes<double>(apt * std::max(maxz, 1),

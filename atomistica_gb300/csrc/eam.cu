@@ -19,8 +19,9 @@
 // {y, c1, c2, c3, d1, d2, d3, 0}: a value gather is one 32-byte sector.
 // rho and phi of a setfl file share one r grid, so a pair locates its
 // interval once for all of its splines; the interval coordinate is
-// (r - x0) * (1/dx) and r, 1/r come from one reciprocal square root (both
-// within an ulp or two of the reference's divisions and square root).
+// r is the correctly rounded square root and the interval coordinate rounds
+// as the reference's division, so B is bitwise the reference's; 1/r comes
+// from a reciprocal square root refined by a Newton step (within an ulp).
 
 #include <cuda_runtime.h>
 
@@ -305,9 +306,16 @@ __device__ __forceinline__ double group_sum(double x) {
 // simple_spline (:373-434), with k clamped to the table for the
 // extrapolating phi; ok = false where the non-extrapolating rho is out of
 // range (an error in the reference).
+// The quotient (r - x0) / dx is formed as the product with 1/dx and one
+// residual correction (Markstein), which rounds as the division does: near
+// the end of a setfl table (the zero padding) the spline's slope changes by
+// ~1e5 eV/A^2, so B must round exactly as in the reference.
 __device__ __forceinline__ void r_interval(const SplineDev &s, double r, double &B, int &k,
                                            bool &ok) {
-  const double xf = (r - s.x0) * s.rdx + 1.0;
+  const double u = r - s.x0;
+  double q = u * s.rdx;
+  q = fma(fma(-q, s.dx, u), s.rdx, q);
+  const double xf = q + 1.0;
   const double fl = floor(xf);
   int i = (int)fmin(fmax(fl, -1.0e9), 1.0e9);
   ok = i >= 1 && (i < s.n || r <= s.cut);
@@ -334,6 +342,14 @@ __device__ __forceinline__ double interval_df(const SplineDev &s, int k, double 
   const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k + 4);
   const double2 c = __ldg(t), d = __ldg(t + 1);
   return c.x + B * (c.y + B * d.x);
+}
+
+// 1/sqrt(r2) to about an ulp: the hardware reciprocal square root refined by
+// one Newton step, y (1 + (1/2 - r2/2 y^2)).
+__device__ __forceinline__ double rsqrt_nr(double r2) {
+  const double y = rsqrt(r2);
+  const double e = fma(-0.5 * r2 * y, y, 0.5);
+  return fma(y, e, y);
 }
 
 __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
@@ -412,8 +428,8 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
       const double r2 = norm2_ref(d);
       if (!(r2 < a.cutoff_sq)) continue;
       const bool mj = !(a.mask && a.mask[j] == 0);
-      const double rinv = rsqrt(r2);
-      const double r = r2 * rinv;
+      const double r = sqrt(r2);  // rounded as the reference's (table coordinate)
+      const double rinv = rsqrt_nr(r2);
       // rho and phi share the r grid: one interval for all three splines
       const SplineDev &sp = a.phi[eli * a.nel + elj];
       double B;

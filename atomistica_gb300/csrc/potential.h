@@ -147,6 +147,8 @@ int bop_batch_apt(int maxz);
 // largest a tile may use (bytes).
 size_t bop_tile_smem(bool mixed, int nbt, int ntrip);
 size_t bop_tile_smem_budget();
+// Resident tile CTAs per SM of the evaluation pot would launch with smem.
+int bop_tile_ctas_per_sm(const Potential &pot, size_t smem);
 
 }  // namespace gb
 
