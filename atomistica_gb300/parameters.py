@@ -12,7 +12,7 @@ src/potentials/bop/tersoff/tersoff_params.f90:99-142 and
 src/potentials/bop/kumagai/kumagai_params.f90:97-132.
 """
 
-from math import sqrt
+from math import log, sqrt
 
 
 def pair_index(i, j, maxval):
@@ -64,6 +64,40 @@ Kumagai_CompMaterSci_39_457_Si = {
     "r2": [3.30],
 }
 
+# Screened variants (TersoffScr / KumagaiScr; Pastewka et al., PRB 87, 205410
+# (2013)): inner cutoff r1 < r2 without screening, outer (VA, VR) cutoff
+# or1 < or2 and bond-order cutoff bor1 < bor2 with the screening window
+# Cmin < C < Cmax (tersoff_params.f90:114-135, kumagai_params.f90:119-128
+# under SCREENING; src/python/atomistica/parameters.py:79-107, 409-420).
+# mubo is the inverse dimer length (lambda - mu) / ln(lambda A / (mu B)).
+Tersoff_PRB_39_5566_Si_C__Scr = dict(
+    Tersoff_PRB_39_5566_Si_C,
+    m=[3, 3, 3],
+    r1=[2.00, sqrt(2.00 * 2.50), 2.50],
+    r2=[2.00 * 1.2, sqrt(2.00 * 2.50) * 1.2, 2.50 * 1.2],
+    or1=[2.00, sqrt(2.00 * 3.00), 3.00],
+    or2=[2.00 * 2.0, sqrt(2.00 * 3.00) * 2.0, 3.00 * 2.0],
+    bor1=[2.00, sqrt(2.00 * 3.00), 3.00],
+    bor2=[2.00 * 2.0, sqrt(2.00 * 3.00) * 2.0, 3.00 * 2.0],
+    Cmin=[1.00, 1.00, 1.00],
+    Cmax=[3.00, 3.00, 3.00],
+)
+Tersoff_PRB_39_5566_Si_C__Scr["mubo"] = [
+    (Tersoff_PRB_39_5566_Si_C__Scr["lambda"][q] - Tersoff_PRB_39_5566_Si_C__Scr["mu"][q]) /
+    log(Tersoff_PRB_39_5566_Si_C__Scr["lambda"][q] * Tersoff_PRB_39_5566_Si_C__Scr["A"][q] /
+        (Tersoff_PRB_39_5566_Si_C__Scr["mu"][q] * Tersoff_PRB_39_5566_Si_C__Scr["B"][q]))
+    for q in range(3)]
+
+Kumagai_CompMaterSci_39_457_Si__Scr = dict(
+    Kumagai_CompMaterSci_39_457_Si,
+    r1=[2.50], r2=[2.50 * 1.2],
+    or1=[3.00], or2=[3.00 * 2.0],
+    bor1=[3.00], bor2=[3.00 * 2.0],
+    Cmin=[1.00], Cmax=[3.00],
+)
+
+SCREENING_KEYS = ("or1", "or2", "bor1", "bor2", "Cmin", "Cmax")
+
 # The 14 continuous Tersoff parameters of a single-element set, in the order
 # used by the parameter-gradient interface.
 TERSOFF_FIT_KEYS = ("A", "B", "lambda", "mu", "beta", "n", "c", "d", "h",
@@ -91,7 +125,8 @@ def tersoff_single_element(p, symbol):
     nel = len(els)
     ij = pair_index(e, e, nel)
     q = {"el": [symbol]}
-    for k in ("A", "B", "xi", "lambda", "mu", "omega", "mubo", "m", "r1", "r2"):
+    for k in ("A", "B", "xi", "lambda", "mu", "omega", "mubo", "m", "r1", "r2") + \
+            tuple(k for k in SCREENING_KEYS if k in p):
         q[k] = [p[k][ij]]
     for k in ("beta", "n", "c", "d", "h"):
         q[k] = [p[k][e]]

@@ -15,6 +15,10 @@
 //   * Tersoff functions   src/potentials/bop/tersoff/tersoff_func.f90:32-232
 //   * Kumagai functions   src/potentials/bop/kumagai/kumagai_func.f90:32-242
 //   * trig_off cutoff     src/support/cutoff.f90:152-196
+//   * screened BOP        bop_kernel.f90:682-995 (pass 1), 1171-1527 and
+//                         1531-1611 (pass 2 and the screening forces),
+//                         default_bind_to_func.f90:45-71, 94-121;
+//                         exp_cutoff src/support/cutoff.f90:232-293
 //   * cubic spline        src/support/simple_spline.f90:127-195, 373-651, 756-773
 //   * alloy EAM           src/potentials/eam/tabulated_alloy_eam.f90:147-259,
 //                         423-627
@@ -360,6 +364,40 @@ struct TrigOff {
   }
 };
 
+// exp_cutoff (the CUTOFF_T of the screened potentials), cutoff.f90:232-293:
+// f(x) = exp(-8 x^3) corrected so that f, f' and f'' vanish at x = 1.
+struct ExpCutoff {
+  double r1, r2, fac1, fac2, c, d, off;
+  void init(double a, double b) {
+    r1 = a;
+    r2 = b;
+    fac1 = 1.0 / (r2 - r1);
+    const double val1 = std::exp(-8.0);
+    const double dval1 = -24 * val1;
+    const double ddval1 = -48 * val1 - 24 * dval1;
+    c = (-3 * dval1 + ddval1) / 3;
+    d = (2 * dval1 - ddval1) / 4;
+    fac2 = 1.0 / (1 - val1 - c - d);
+    off = val1 + c + d;
+  }
+  void f(double r, double &val, double &dval) const {
+    if (r <= r1) {
+      val = 1.0;
+      dval = 0.0;
+    } else if (r >= r2) {
+      val = 0.0;
+      dval = 0.0;
+    } else {
+      const double x = fac1 * (r - r1);
+      const double x2 = x * x;
+      val = std::exp(-8 * x * x2);
+      dval = -24 * x2 * val;
+      dval = fac1 * fac2 * (dval + 3 * c * x2 + 4 * d * x * x2);
+      val = fac2 * (val + c * x * x2 + d * x2 * x2 - off);
+    }
+  }
+};
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -376,6 +414,13 @@ struct orc_tersoff_params {
   int m[6];
   double beta[3], n[3], c[3], d[3], h[3];
   double r1[6], r2[6];
+};
+
+// Extra parameters of the screened variants (tersoff_params.f90:81-90 under
+// SCREENING): outer (attractive/repulsive) and bond-order cutoffs, screening
+// window Cmin < C < Cmax; per pair.  The inner cutoff is r1/r2 of the base set.
+struct orc_scr_params {
+  double or1[6], or2[6], bor1[6], bor2[6], Cmin[6], Cmax[6];
 };
 
 struct orc_kumagai_params {
@@ -750,6 +795,459 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
       for (int c = 0; c < 3; c++) twpot[9 * tid + 3 * a + c] = wpot[a][c];
   }
   // Reductions (bop_kernel.f90:1613-1628, tls_reduce).
+  double esum = 0.0;
+  for (int t = 0; t < nt; t++) {
+    if (tpe[t].empty()) continue;
+    double s = 0.0;
+    for (int i = 0; i < nat; i++) s += tpe[t][i];
+    esum += 0.5 * s;
+    for (size_t q = 0; q < 3 * (size_t)nat; q++) o.f[q] += tf[t][q];
+    if (o.epot_per_at)
+      for (int i = 0; i < nat; i++) o.epot_per_at[i] += 0.5 * tpe[t][i];
+    if (want_wat)
+      for (size_t q = 0; q < 9 * (size_t)nat; q++) o.wpot_per_at[q] += twat[t][q];
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) o.wpot[3 * c + a] += twpot[9 * t + 3 * a + c];
+  }
+  *o.epot += esum;
+  return 0;
+}
+
+// BOP_KERNEL with SCREENING defined (TersoffScr, KumagaiScr; PYTHON build,
+// neither SIN_S nor PARTIAL_SCREENING).  Differences to the plain kernel:
+//   * pass 1 (bop_kernel.f90:682-995): a bond beyond the inner cutoff r1 is
+//     tested for screening by every neighbour k of i (in list order, stopping
+//     at the first full screen or once ln S drops below screening_threshold):
+//     C = (2 (x_ik + x_jk) - (x_ik - x_jk)^2 - 1) / (1 - (x_ik - x_jk)^2),
+//     x = r^2 / r_ij^2; C <= Cmin screens fully, Cmin < C < Cmax adds
+//     -((Cmax - C)/(C - Cmin))^2 to ln S and records k with dS/dr_ik,
+//     dS/dr_jk.  A screened bond beyond r2 is dropped; the others get
+//     fc_ar = (1 - fc_in) S fc_out + fc_in and fc_bo likewise (exp_cutoff);
+//   * pass 2: VA/VR up to or2 with fc_ar, zeta terms up to bor2 with fc_bo;
+//     the screening neighbours of bond ij take forces from the pair term
+//     (:1531-1560), and those of bond ik from d zeta_ij / d S_ik accumulated
+//     over ij (sfacbo, :1462-1471, applied in the loop :1571-1611).
+template <class Fn>
+int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double *r,
+                   const Box &box, const int *el, const NList &nl, const int *mask,
+                   const BopOut &o, int nthreads) {
+  const int nel = fn.nel();
+  const int npairs = nel * (nel + 1) / 2;
+  std::vector<ExpCutoff> cut_in(npairs), cut_out(npairs), cut_bo(npairs);
+  std::vector<double> cut_in_l(npairs), cut_in_h(npairs), cut_in_h2(npairs), cut_out_l(npairs),
+      cut_out_h(npairs), cut_bo_h(npairs), max_cut_sq(npairs), Cmin(npairs), Cmax(npairs),
+      dC(npairs), C_dr_cut(npairs);
+  for (int q = 0; q < npairs; q++) {
+    cut_in[q].init(fn.r1(q), fn.r2(q));
+    cut_in_l[q] = fn.r1(q);
+    cut_in_h[q] = fn.r2(q);
+    cut_in_h2[q] = fn.r2(q) * fn.r2(q);
+    cut_out[q].init(sp.or1[q], sp.or2[q]);
+    cut_out_l[q] = sp.or1[q];
+    cut_out_h[q] = sp.or2[q];
+    cut_bo[q].init(sp.bor1[q], sp.bor2[q]);
+    cut_bo_h[q] = sp.bor2[q];
+    const double mc = std::max(std::max(cut_in_h[q], cut_out_h[q]), cut_bo_h[q]);
+    max_cut_sq[q] = mc * mc;
+    Cmin[q] = sp.Cmin[q];
+    Cmax[q] = sp.Cmax[q];
+    dC[q] = Cmax[q] - Cmin[q];
+    C_dr_cut[q] = Cmax[q] > 2.0 ? Cmax[q] * Cmax[q] / (4 * (Cmax[q] - 1)) : 1.0;
+  }
+  const double screening_threshold = std::log(1e-6);
+  const double dot_threshold = (double)1e-10f;  // a default-real literal in tersoff_type.f90:86
+
+  struct ScrEntry {
+    int k, kn;
+    double arik, arjk, boik, bojk;
+  };
+  struct Bond {
+    int j, nbb, typ;
+    double len, nm[3], fcar, dfcar, fcbo, dfcbo;
+    int s0, s1;  // screening entries [s0, s1) of the atom's ScrEntry list
+  };
+  auto get_rik = [&](int i, int64_t kn, double rik[3]) {
+    const int k = nl.nbr[kn];
+    const int *dc = &nl.dc[3 * kn];
+    for (int a = 0; a < 3; a++) {
+      double as = box.A[a][0] * (double)dc[0];
+      as = as + box.A[a][1] * (double)dc[1];
+      as = as + box.A[a][2] * (double)dc[2];
+      rik[a] = (r[3 * k + a] - r[3 * i + a]) - as;
+    }
+  };
+  std::vector<std::vector<Bond>> bonds_of(nat);
+  std::vector<std::vector<ScrEntry>> scr_of(nat);
+  // Pass 1.
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+  for (int i = 0; i < nat; i++) {
+    const int eli = el[i];
+    if (eli < 0) continue;
+    std::vector<Bond> &bonds = bonds_of[i];
+    std::vector<ScrEntry> &scr = scr_of[i];
+    const int64_t jbeg = nl.seed[i], jend = nl.seed[i + 1];
+    for (int64_t jn = jbeg; jn < jend; jn++) {
+      const int j = nl.nbr[jn];
+      const int elj = el[j];
+      if (elj < 0) continue;
+      const int *dcj = &nl.dc[3 * jn];
+      double rij[3];
+      get_rik(i, jn, rij);
+      double rlij = rij[0] * rij[0];
+      rlij = rlij + rij[1] * rij[1];
+      rlij = rlij + rij[2] * rij[2];
+      const int el2ij = pair_index(eli, elj, nel);
+      Bond b;
+      b.j = j;
+      b.nbb = (int)jn;
+      b.typ = el2ij;
+      b.s0 = b.s1 = (int)scr.size();
+      if (rlij < cut_in_l[el2ij] * cut_in_l[el2ij]) {
+        // region (a): no screening
+        b.fcar = b.fcbo = 1.0;
+        b.dfcar = b.dfcbo = 0.0;
+      } else if (rlij < max_cut_sq[el2ij] && cut_out_l[el2ij] < cut_out_h[el2ij]) {
+        bool screened = false, need_derivative = false;
+        double sij = 0.0, dsijdrij = 0.0;
+        const int ineb = (int)scr.size();
+        for (int64_t kn = jbeg; !(screened || sij < screening_threshold) && kn < jend; kn++) {
+          const int k = nl.nbr[kn];
+          double rik[3];
+          get_rik(i, kn, rik);
+          double rr = rik[0] * rik[0];
+          rr = rr + rik[1] * rik[1];
+          rr = rr + rik[2] * rik[2];
+          if (!(rr < C_dr_cut[el2ij] * rlij)) continue;
+          const int *dck = &nl.dc[3 * kn];
+          if (!(k != j || dck[0] != dcj[0] || dck[1] != dcj[1] || dck[2] != dcj[2])) continue;
+          double dot_ij_ik = rij[0] * rik[0];
+          dot_ij_ik = dot_ij_ik + rij[1] * rik[1];
+          dot_ij_ik = dot_ij_ik + rij[2] * rik[2];
+          const double rlik = rr;
+          double rjk[3];
+          for (int a = 0; a < 3; a++) rjk[a] = -rij[a] + rik[a];
+          double dot_ij_jk = rij[0] * rjk[0];
+          dot_ij_jk = dot_ij_jk + rij[1] * rjk[1];
+          dot_ij_jk = dot_ij_jk + rij[2] * rjk[2];
+          double rljk = rjk[0] * rjk[0];
+          rljk = rljk + rjk[1] * rjk[1];
+          rljk = rljk + rjk[2] * rjk[2];
+          if (!(dot_ij_ik > dot_threshold && dot_ij_jk < -dot_threshold)) continue;
+          const double xik = rlik / rlij, xjk = rljk / rlij;
+          const double xm = xik - xjk, xp = xik + xjk;
+          double fac = 1.0 / (1 - xm * xm);
+          const double C = (2 * xp - xm * xm - 1) * fac;
+          if (C <= Cmin[el2ij]) {
+            screened = true;
+          } else if (C < Cmax[el2ij]) {
+            need_derivative = true;
+            const double Cmax_C = Cmax[el2ij] - C, C_Cmin = C - Cmin[el2ij];
+            const double t = Cmax_C / C_Cmin;
+            sij = sij - t * t;
+            const double dCdrik = 4 * xik * fac * (1 + (C - 1) * xm);
+            const double dCdrjk = 4 * xjk * fac * (1 - (C - 1) * xm);
+            const double dCdrij = -(dCdrik + dCdrjk);
+            fac = 2 * Cmax_C * dC[el2ij] / (C_Cmin * C_Cmin * C_Cmin);
+            dsijdrij = dsijdrij + fac * dCdrij;
+            ScrEntry e;
+            e.k = k;
+            e.kn = (int)kn;
+            e.arik = fac * dCdrik / rlik;
+            e.arjk = fac * dCdrjk / rljk;
+            e.boik = e.bojk = 0.0;
+            scr.push_back(e);
+          }
+        }
+        if ((screened || sij < screening_threshold) && rlij > cut_in_h2[el2ij]) {
+          scr.resize(ineb);  // fully screened: not a bond
+          continue;
+        }
+        const double rl = std::sqrt(rlij);
+        double fcin, dfcin;
+        if (screened) {
+          cut_in[el2ij].f(rl, fcin, dfcin);
+          b.fcar = b.fcbo = fcin;
+          b.dfcar = b.dfcbo = dfcin;
+          scr.resize(ineb);
+        } else if (need_derivative) {
+          sij = std::exp(sij);
+          double fcar, dfcar, fcbo, dfcbo;
+          cut_in[el2ij].f(rl, fcin, dfcin);
+          cut_out[el2ij].f(rl, fcar, dfcar);
+          cut_bo[el2ij].f(rl, fcbo, dfcbo);
+          b.fcar = (1.0 - fcin) * sij * fcar + fcin;
+          b.dfcar = (1.0 - fcin) * sij * (dfcar + fcar * dsijdrij / rl) - dfcin * sij * fcar + dfcin;
+          b.fcbo = (1.0 - fcin) * sij * fcbo + fcin;
+          b.dfcbo = (1.0 - fcin) * sij * (dfcbo + fcbo * dsijdrij / rl) - dfcin * sij * fcbo + dfcin;
+          for (size_t q = ineb; q < scr.size(); q++) {
+            ScrEntry &e = scr[q];
+            e.boik = e.arik * sij * fcbo * (1.0 - fcin);
+            e.bojk = e.arjk * sij * fcbo * (1.0 - fcin);
+            e.arik = e.arik * sij * fcar * (1.0 - fcin);
+            e.arjk = e.arjk * sij * fcar * (1.0 - fcin);
+          }
+        } else {
+          double fcar, dfcar, fcbo, dfcbo;
+          cut_out[el2ij].f(rl, fcar, dfcar);
+          cut_bo[el2ij].f(rl, fcbo, dfcbo);
+          if (rl < cut_in_h[el2ij]) {
+            cut_in[el2ij].f(rl, fcin, dfcin);
+            b.fcar = (1.0 - fcin) * fcar + fcin;
+            b.dfcar = (1.0 - fcin) * dfcar - dfcin * fcar + dfcin;
+            b.fcbo = (1.0 - fcin) * fcbo + fcin;
+            b.dfcbo = (1.0 - fcin) * dfcbo - dfcin * fcbo + dfcin;
+          } else {
+            b.fcar = fcar;
+            b.dfcar = dfcar;
+            b.fcbo = fcbo;
+            b.dfcbo = dfcbo;
+          }
+        }
+        b.s0 = ineb;
+        b.s1 = (int)scr.size();
+      } else if (rlij < cut_in_h2[el2ij]) {
+        double fcin, dfcin;
+        cut_in[el2ij].f(std::sqrt(rlij), fcin, dfcin);
+        b.fcar = b.fcbo = fcin;
+        b.dfcar = b.dfcbo = dfcin;
+      } else {
+        continue;
+      }
+      rlij = std::sqrt(rlij);
+      b.len = rlij;
+      for (int a = 0; a < 3; a++) b.nm[a] = rij[a] / rlij;
+      bonds.push_back(b);
+    }
+  }
+  int nebmax = 0;
+  for (int i = 0; i < nat; i++) nebmax = std::max(nebmax, (int)bonds_of[i].size());
+
+  // Pass 2 and the screening-force loop, thread-private accumulators (tls.f90).
+  int nt = nthreads;
+  std::vector<std::vector<double>> tpe(nt), tf(nt), twat(nt);
+  std::vector<double> twpot(9 * nt, 0.0);
+  std::vector<std::vector<double>> sfacbo_of(nat);
+  const bool want_wat = o.wpot_per_at != nullptr;
+  auto add_w = [&](std::vector<double> &wat, double wpot[3][3], int i, int j, int nbb,
+                   const double wij[3][3]) {
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) wpot[a][c] += wij[a][c];
+    if (o.wpot_per_bond)
+      for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++) o.wpot_per_bond[9 * (size_t)nbb + 3 * c + a] += wij[a][c];
+    if (want_wat)
+      for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++) {
+          wat[9 * (size_t)i + 3 * c + a] += wij[a][c] / 2;
+          wat[9 * (size_t)j + 3 * c + a] += wij[a][c] / 2;
+        }
+  };
+#pragma omp parallel num_threads(nthreads)
+  {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#else
+    const int tid = 0;
+#endif
+    std::vector<double> &pe = tpe[tid];
+    std::vector<double> &f = tf[tid];
+    std::vector<double> &wat = twat[tid];
+    pe.assign(nat, 0.0);
+    f.assign(3 * (size_t)nat, 0.0);
+    if (want_wat) wat.assign(9 * (size_t)nat, 0.0);
+    double wpot[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    std::vector<double> dbidk(3 * (size_t)std::max(nebmax, 1)), zfaci(std::max(nebmax, 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < nat; i++) {
+      const int eli = el[i];
+      if (eli < 0) continue;
+      double fi[3] = {0, 0, 0};
+      const std::vector<Bond> &bi = bonds_of[i];
+      const std::vector<ScrEntry> &scr = scr_of[i];
+      const int nb = (int)bi.size();
+      std::vector<double> &sfacbo = sfacbo_of[i];
+      sfacbo.assign(nb, 0.0);
+      for (int ij = 0; ij < nb; ij++) {
+        const Bond &B = bi[ij];
+        const int j = B.j;
+        int maskfac = 2;
+        if (mask) {
+          if (mask[i] == 0 && mask[j] == 0)
+            maskfac = 0;
+          else if (mask[i] == 0 || mask[j] == 0)
+            maskfac = 1;
+        }
+        const int el2ij = B.typ;
+        const double rlij = B.len;
+        if (!(maskfac > 0 && rlij < cut_out_h[el2ij])) continue;
+        double fj[3] = {0, 0, 0};
+        const double rlijr = 1.0 / rlij;
+        const double rnij[3] = {B.nm[0], B.nm[1], B.nm[2]};
+        const double rij[3] = {rlij * rnij[0], rlij * rnij[1], rlij * rnij[2]};
+        const double fcarij = B.fcar, dfcarijr = B.dfcar;
+        double VAij, dVAij, VRij, dVRij;
+        fn.VA(el2ij, rlij, VAij, dVAij);
+        fn.VR(el2ij, rlij, VRij, dVRij);
+        VAij = 0.5 * maskfac * VAij;
+        dVAij = 0.5 * maskfac * dVAij;
+        VRij = 0.5 * maskfac * VRij;
+        dVRij = 0.5 * maskfac * dVRij;
+        double wij[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double wijb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double zij = 0.0;
+        double dbidi[3] = {0, 0, 0}, dbidj[3] = {0, 0, 0};
+        for (int ik = 0; ik < nb; ik++) {
+          if (ik == ij) continue;
+          const Bond &K = bi[ik];
+          const int ikpot = K.typ;
+          const double rlik = K.len;
+          if (!(rlik < cut_bo_h[ikpot])) {
+            zfaci[ik] = 0.0;
+            dbidk[3 * ik] = dbidk[3 * ik + 1] = dbidk[3 * ik + 2] = 0.0;
+            continue;
+          }
+          const double *rnik = K.nm;
+          const double rik[3] = {rlik * rnik[0], rlik * rnik[1], rlik * rnik[2]};
+          const double fcik = K.fcbo, dfcikr = K.dfcbo;
+          double h_Dr, dh_dDr;
+          fn.h(ikpot, rlij - rlik, h_Dr, dh_dDr);
+          const double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
+          double g_costh, dg_dcosth;
+          fn.g(eli, ikpot, costh, g_costh, dg_dcosth);
+          double dkc[3];
+          for (int a = 0; a < 3; a++) dkc[a] = rnik[a] * rlik - rnij[a] * rlij;
+          const double disjk = std::sqrt(dkc[0] * dkc[0] + dkc[1] * dkc[1] + dkc[2] * dkc[2]);
+          for (int a = 0; a < 3; a++) dkc[a] = dkc[a] / disjk;
+          const double dcsdij = 1.0 / rlik - costh * rlijr;
+          const double dcsdik = rlijr - costh / rlik;
+          const double dcsdjk = -disjk * rlijr / rlik;
+          double dcsdi[3], dcsdj[3], dcsdk[3];
+          for (int a = 0; a < 3; a++) {
+            dcsdi[a] = -dcsdij * rnij[a] - dcsdik * rnik[a];
+            dcsdj[a] = dcsdij * rnij[a] - dcsdjk * dkc[a];
+            dcsdk[a] = dcsdik * rnik[a] + dcsdjk * dkc[a];
+          }
+          const double dzfac = fcik * dg_dcosth * h_Dr;
+          double dgdi[3], dgdj[3], dgdk[3];
+          for (int a = 0; a < 3; a++) {
+            dgdi[a] = dzfac * dcsdi[a];
+            dgdj[a] = dzfac * dcsdj[a];
+            dgdk[a] = dzfac * dcsdk[a];
+          }
+          zfaci[ik] = g_costh * h_Dr;
+          zij = zij + fcik * g_costh * h_Dr;
+          const double dzdrij = g_costh * fcik * dh_dDr;
+          const double dzdrik = g_costh * (dfcikr * h_Dr - fcik * dh_dDr);
+          double df[3];
+          for (int a = 0; a < 3; a++) {
+            dbidi[a] = dbidi[a] - dzdrij * rnij[a] - dzdrik * rnik[a] + dgdi[a];
+            df[a] = dzdrij * rnij[a] + dgdj[a];
+            dbidj[a] = dbidj[a] + df[a];
+            dbidk[3 * ik + a] = dzdrik * rnik[a] + dgdk[a];
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++)
+              wijb[a][c] = wijb[a][c] - rij[a] * df[c] - rik[a] * dbidk[3 * ik + c];
+        }
+        double bij, dbij_dzij;
+        fn.bo(eli, el2ij, zij, fcarij, VAij, bij, dbij_dzij);
+        double dffac = 0.5 * fcarij * (VRij + bij * VAij);
+        pe[i] = pe[i] + dffac;
+        pe[j] = pe[j] + dffac;
+        if (o.epot_per_bond) o.epot_per_bond[B.nbb] += dffac;
+        dffac = 0.5 * (dVRij * fcarij + bij * dVAij * fcarij + VRij * dfcarijr +
+                       bij * VAij * dfcarijr);
+        double df[3];
+        for (int a = 0; a < 3; a++) {
+          df[a] = dffac * rnij[a];
+          fi[a] = fi[a] + df[a];
+          fj[a] = fj[a] - df[a];
+        }
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++)
+            wij[a][c] = wij[a][c] + rij[a] * df[c] - dbij_dzij * wijb[a][c];
+        if (o.f_per_bond)
+          for (int a = 0; a < 3; a++) o.f_per_bond[3 * (size_t)B.nbb + a] += df[a];
+        for (int a = 0; a < 3; a++) fi[a] = fi[a] - dbij_dzij * dbidi[a];
+        for (int a = 0; a < 3; a++) fj[a] = fj[a] - dbij_dzij * dbidj[a];
+        for (int ik = 0; ik < nb; ik++) {
+          if (ik == ij) continue;  // k == j and kdc == jdc (:1459)
+          const int k = bi[ik].j;
+          for (int a = 0; a < 3; a++)
+            f[3 * (size_t)k + a] += -dbij_dzij * dbidk[3 * ik + a];
+          if (bi[ik].s0 < bi[ik].s1) sfacbo[ik] = sfacbo[ik] + zfaci[ik] * dbij_dzij;
+        }
+        // forces on the screening neighbours of bond ij from the pair term
+        const double dffac2 = 0.5 * (VRij + bij * VAij);
+        for (int q = B.s0; q < B.s1; q++) {
+          const ScrEntry &e = scr[q];
+          double rik[3], rjk[3];
+          get_rik(i, e.kn, rik);
+          for (int a = 0; a < 3; a++) rjk[a] = -rij[a] + rik[a];
+          for (int a = 0; a < 3; a++) {
+            const double d1 = dffac2 * e.arik * rik[a];
+            fi[a] = fi[a] + d1;
+            f[3 * (size_t)e.k + a] += -d1;
+            df[a] = d1;
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) wij[a][c] = wij[a][c] + rik[a] * df[c];
+          for (int a = 0; a < 3; a++) {
+            const double d2 = dffac2 * e.arjk * rjk[a];
+            fj[a] = fj[a] + d2;
+            f[3 * (size_t)e.k + a] += -d2;
+            df[a] = d2;
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) wij[a][c] = wij[a][c] + rjk[a] * df[c];
+        }
+        add_w(wat, wpot, i, j, B.nbb, wij);
+        for (int a = 0; a < 3; a++) f[3 * (size_t)j + a] += fj[a];
+      }
+      for (int a = 0; a < 3; a++) f[3 * (size_t)i + a] += fi[a];
+    }
+    // Screening forces through the bond-order cutoff (:1571-1611).
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < nat; i++) {
+      if (el[i] < 0) continue;
+      double fi[3] = {0, 0, 0};
+      const std::vector<Bond> &bi = bonds_of[i];
+      const std::vector<ScrEntry> &scr = scr_of[i];
+      for (int ij = 0; ij < (int)bi.size(); ij++) {
+        const Bond &B = bi[ij];
+        double fj[3] = {0, 0, 0};
+        double wij[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        const double rij[3] = {B.len * B.nm[0], B.len * B.nm[1], B.len * B.nm[2]};
+        const double sfac = sfacbo_of[i][ij];
+        for (int q = B.s0; q < B.s1; q++) {
+          const ScrEntry &e = scr[q];
+          const double boik = sfac * e.boik, bojk = sfac * e.bojk;
+          double rik[3], rjk[3], df[3];
+          get_rik(i, e.kn, rik);
+          for (int a = 0; a < 3; a++) rjk[a] = -rij[a] + rik[a];
+          for (int a = 0; a < 3; a++) {
+            df[a] = boik * rik[a];
+            fi[a] = fi[a] + df[a];
+            f[3 * (size_t)e.k + a] += -df[a];
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) wij[a][c] = wij[a][c] + rik[a] * df[c];
+          for (int a = 0; a < 3; a++) {
+            df[a] = bojk * rjk[a];
+            fj[a] = fj[a] + df[a];
+            f[3 * (size_t)e.k + a] += -df[a];
+          }
+          for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) wij[a][c] = wij[a][c] + rjk[a] * df[c];
+        }
+        add_w(wat, wpot, i, B.j, B.nbb, wij);
+        for (int a = 0; a < 3; a++) f[3 * (size_t)B.j + a] += fj[a];
+      }
+      for (int a = 0; a < 3; a++) f[3 * (size_t)i + a] += fi[a];
+    }
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) twpot[9 * tid + 3 * a + c] = wpot[a][c];
+  }
   double esum = 0.0;
   for (int t = 0; t < nt; t++) {
     if (tpe[t].empty()) continue;
@@ -1224,6 +1722,119 @@ int orc_kumagai_compute(const orc_kumagai_params *p, int nat, const double *r,
   BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
   return bop_kernel(KumagaiFn(*p), nat, r, box, el.data(), nl, mask, o,
                     resolve_threads(nthreads));
+}
+
+// Interaction range of the screened variants for the elements present
+// (default_bind_to_func.f90:117-144): sqrt(C_dr_cut(pair)) times the largest
+// of all pairs' max(r2, or2, bor2).
+static double scr_range(int nat, const std::vector<int> &el, int nel, const double *r2,
+                        const orc_scr_params &sp) {
+  const int npairs = nel * (nel + 1) / 2;
+  double mx = 0.0;
+  for (int q = 0; q < npairs; q++) {
+    const double m = std::max(std::max(r2[q], sp.or2[q]), sp.bor2[q]);
+    mx = std::max(mx, m * m);
+  }
+  std::vector<int> present(nel, 0);
+  for (int i = 0; i < nat; i++)
+    if (el[i] >= 0) present[el[i]] = 1;
+  double range = 0.0;
+  for (int a = 0; a < nel; a++)
+    for (int b = 0; b < nel; b++)
+      if (present[a] && present[b]) {
+        const int q = pair_index(a, b, nel);
+        const double cdr = sp.Cmax[q] > 2.0 ? sp.Cmax[q] * sp.Cmax[q] / (4 * (sp.Cmax[q] - 1))
+                                            : 1.0;
+        range = std::max(range, std::sqrt(cdr) * std::sqrt(mx));
+      }
+  return range;
+}
+
+double orc_tersoff_scr_cutoff(const orc_tersoff_params *p, const orc_scr_params *sp, int nat,
+                              const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return scr_range(nat, el, p->nel, p->r2, *sp);
+}
+
+double orc_kumagai_scr_cutoff(const orc_kumagai_params *p, const orc_scr_params *sp, int nat,
+                              const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return scr_range(nat, el, p->nel, p->r2, *sp);
+}
+
+int orc_tersoff_scr_kernel(const orc_tersoff_params *p, const orc_scr_params *sp, int nat,
+                           const double *r, const double *cell, const int *pbc, const int *Z,
+                           const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                           double *epot, double *f, double *wpot, double *epot_per_at,
+                           double *epot_per_bond, double *f_per_bond, double *wpot_per_at,
+                           double *wpot_per_bond, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  NList nl;
+  nl_from_arrays(nat, seed, nbr, dc, nl);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return bop_kernel_scr(TersoffFn(*p), *sp, nat, r, box, el.data(), nl, mask, o,
+                        resolve_threads(nthreads));
+}
+
+int orc_kumagai_scr_kernel(const orc_kumagai_params *p, const orc_scr_params *sp, int nat,
+                           const double *r, const double *cell, const int *pbc, const int *Z,
+                           const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                           double *epot, double *f, double *wpot, double *epot_per_at,
+                           double *epot_per_bond, double *f_per_bond, double *wpot_per_at,
+                           double *wpot_per_bond, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  NList nl;
+  nl_from_arrays(nat, seed, nbr, dc, nl);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return bop_kernel_scr(KumagaiFn(*p), *sp, nat, r, box, el.data(), nl, mask, o,
+                        resolve_threads(nthreads));
+}
+
+// Neighbour build + screened kernel (the CPU baseline's timed unit).
+int orc_tersoff_scr_compute(const orc_tersoff_params *p, const orc_scr_params *sp, int nat,
+                            const double *r, const double *cell, const int *pbc, const int *Z,
+                            const int *mask, double *epot, double *f, double *wpot,
+                            double *epot_per_at, double *wpot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  double cutoff = scr_range(nat, el, p->nel, p->r2, *sp);
+  NList nl;
+  if (cutoff > 0) build_neighbors(nat, r, box, cutoff, nl);
+  else nl.seed.assign(nat + 1, 0);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return bop_kernel_scr(TersoffFn(*p), *sp, nat, r, box, el.data(), nl, mask, o,
+                        resolve_threads(nthreads));
+}
+
+int orc_kumagai_scr_compute(const orc_kumagai_params *p, const orc_scr_params *sp, int nat,
+                            const double *r, const double *cell, const int *pbc, const int *Z,
+                            const int *mask, double *epot, double *f, double *wpot,
+                            double *epot_per_at, double *wpot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  double cutoff = scr_range(nat, el, p->nel, p->r2, *sp);
+  NList nl;
+  if (cutoff > 0) build_neighbors(nat, r, box, cutoff, nl);
+  else nl.seed.assign(nat + 1, 0);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return bop_kernel_scr(KumagaiFn(*p), *sp, nat, r, box, el.data(), nl, mask, o,
+                        resolve_threads(nthreads));
 }
 
 struct orc_eam {

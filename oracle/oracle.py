@@ -49,6 +49,31 @@ class KumagaiParams(ctypes.Structure):
         [(k, ctypes.c_double * 1) for k in ("c1", "c2", "c3", "c4", "c5", "h", "r1", "r2")]
 
 
+class ScrParams(ctypes.Structure):
+    """Screened variants: outer / bond-order cutoffs and the screening window
+    (tersoff_params.f90:81-90, kumagai_params.f90 under SCREENING)."""
+    _fields_ = [(k, ctypes.c_double * 6) for k in ("or1", "or2", "bor1", "bor2", "Cmin",
+                                                   "Cmax")]
+
+
+def scr_params(d):
+    p = ScrParams()
+    n = len(d["or1"])
+    for k in ("or1", "or2", "bor1", "bor2", "Cmin", "Cmax"):
+        arr = getattr(p, k)
+        for q in range(n):
+            arr[q] = float(d[k][q])
+    return p
+
+
+def _kind(kind):
+    """(base kind, screened?) of 'tersoff', 'kumagai', 'tersoff_scr', 'kumagai_scr'."""
+    base = kind[:-4] if kind.endswith("_scr") else kind
+    if base not in ("tersoff", "kumagai"):
+        raise ValueError("unknown bond-order potential %r" % kind)
+    return base, kind.endswith("_scr")
+
+
 def _Z(sym):
     from atomistica_gb300.parameters import atomic_numbers
     return atomic_numbers[sym]
@@ -115,6 +140,15 @@ def lib():
         for name in ("orc_tersoff_compute", "orc_kumagai_compute"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = cargs
+        for name in ("orc_tersoff_scr_cutoff", "orc_kumagai_scr_cutoff"):
+            getattr(L, name).restype = ctypes.c_double
+            getattr(L, name).argtypes = [_P, _P, ctypes.c_int, _P]
+        for name in ("orc_tersoff_scr_kernel", "orc_kumagai_scr_kernel"):
+            getattr(L, name).restype = ctypes.c_int
+            getattr(L, name).argtypes = [_P] + kargs
+        for name in ("orc_tersoff_scr_compute", "orc_kumagai_scr_compute"):
+            getattr(L, name).restype = ctypes.c_int
+            getattr(L, name).argtypes = [_P] + cargs
         L.orc_eam_load.restype = _P
         L.orc_eam_load.argtypes = [ctypes.c_char_p, _P]
         L.orc_eam_free.argtypes = [_P]
@@ -218,9 +252,11 @@ def bop(kind, params, s, nl=None, mask=None, per_at=True, per_bond=False, nthrea
     L = lib()
     r, cell, pbc, Z = _geom(s)
     nat = len(r)
-    p = tersoff_params(params) if kind == "tersoff" else kumagai_params(params)
+    base, scr = _kind(kind)
+    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    pre = (ctypes.byref(p), ctypes.byref(scr_params(params))) if scr else (ctypes.byref(p),)
     if nl is None:
-        cut = getattr(L, "orc_%s_cutoff" % kind)(ctypes.byref(p), nat, _ptr(Z))
+        cut = getattr(L, "orc_%s_cutoff" % kind)(*pre, nat, _ptr(Z))
         nl = neighbors(s, cut) if cut > 0 else NeighborList(
             np.zeros(nat + 1, np.int64), np.zeros(0, np.int32), np.zeros((0, 3), np.int32))
     out = _alloc_outputs(nat, len(nl.nbr), per_at, per_bond)
@@ -229,7 +265,7 @@ def bop(kind, params, s, nl=None, mask=None, per_at=True, per_bond=False, nthrea
     nbr = nl.nbr if len(nl.nbr) else np.zeros(1, np.int32)
     dc = np.ascontiguousarray(nl.dc) if len(nl.nbr) else np.zeros((1, 3), np.int32)
     rc = getattr(L, "orc_%s_kernel" % kind)(
-        ctypes.byref(p), nat, _ptr(r), _ptr(cell), _ptr(pbc), _ptr(Z), _ptr(nl.seed),
+        *pre, nat, _ptr(r), _ptr(cell), _ptr(pbc), _ptr(Z), _ptr(nl.seed),
         _ptr(nbr), _ptr(dc), _ptr(m), ctypes.byref(epot), _ptr(out["f"]),
         _ptr(out["wpot"]), _ptr(out.get("epot_per_at")), _ptr(out.get("epot_per_bond")),
         _ptr(out.get("f_per_bond")), _ptr(out.get("wpot_per_at")),
@@ -247,12 +283,14 @@ def bop_compute(kind, params, s, mask=None, per_at=False, nthreads=0):
     L = lib()
     r, cell, pbc, Z = _geom(s)
     nat = len(r)
-    p = tersoff_params(params) if kind == "tersoff" else kumagai_params(params)
+    base, scr = _kind(kind)
+    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    pre = (ctypes.byref(p), ctypes.byref(scr_params(params))) if scr else (ctypes.byref(p),)
     out = _alloc_outputs(nat, 0, per_at, False)
     epot = ctypes.c_double(0.0)
     m = None if mask is None else np.ascontiguousarray(np.asarray(mask).astype(np.int32))
     rc = getattr(L, "orc_%s_compute" % kind)(
-        ctypes.byref(p), nat, _ptr(r), _ptr(cell), _ptr(pbc), _ptr(Z), _ptr(m),
+        *pre, nat, _ptr(r), _ptr(cell), _ptr(pbc), _ptr(Z), _ptr(m),
         ctypes.byref(epot), _ptr(out["f"]), _ptr(out["wpot"]), _ptr(out.get("epot_per_at")),
         _ptr(out.get("wpot_per_at")), int(nthreads))
     if rc != 0:

@@ -13,6 +13,10 @@ oracle:
   * neighbour-list geometry and pbc counts (tests/test_neighbor_list.py);
   * EAM special cases (tests/test_eam_special_cases.py);
   * dimer continuity (tests/test_dimers.py:109-136).
+
+The screened variants (TersoffScr, KumagaiScr) are pinned by the same tests
+the reference runs for them: bulk properties, FD forces and virials, mask
+additivity and the Kumagai dimer.
 """
 
 import os
@@ -24,7 +28,14 @@ import oracle
 from atomistica_gb300 import io as gio
 from atomistica_gb300 import structures as S
 
+from atomistica_gb300 import parameters as P
+
 from helpers import KUMAGAI, TERSOFF, random_carbon, rattled_diamond
+
+TERSOFF_SCR = P.Tersoff_PRB_39_5566_Si_C__Scr
+KUMAGAI_SCR = P.Kumagai_CompMaterSci_39_457_Si__Scr
+PARAMS = {"tersoff": TERSOFF, "kumagai": KUMAGAI, "tersoff_scr": TERSOFF_SCR,
+          "kumagai_scr": KUMAGAI_SCR}
 
 GPA = 160.21766208  # eV/A^3 -> GPa
 JM2 = 16.02176634  # eV/A^2 -> J/m^2
@@ -130,10 +141,19 @@ def test_surface_energy_and_pbc_bit_equality():
     ("tersoff B3-SiC", "tersoff", lambda a: S.b3(("Si", "C"), a), 6.165, 4.321, 437, 118, 311),
     ("kumagai dia-Si", "kumagai", lambda a: S.diamond("Si", a), 4.630, 5.429, 166.4, 65.3,
      120.9),
+    # screened variants: the same targets (tests/test_bulk_properties.py:122-160)
+    ("tersoff_scr dia-Si", "tersoff_scr", lambda a: S.diamond("Si", a), 4.63, 5.432, 143, 75,
+     119),
+    ("tersoff_scr dia-C", "tersoff_scr", lambda a: S.diamond("C", a), 7.396 - 0.0250, 3.566,
+     1067, 104, 671),
+    ("tersoff_scr B3-SiC", "tersoff_scr", lambda a: S.b3(("Si", "C"), a), 6.165, 4.321, 437,
+     118, 311),
+    ("kumagai_scr dia-Si", "kumagai_scr", lambda a: S.diamond("Si", a), 4.630, 5.429, 166.4,
+     65.3, 120.9),
 ])
 def test_bulk_properties_bop(case):
     name, kind, builder, Ec, a0, C11, C12, C440 = case
-    params = TERSOFF if kind == "tersoff" else KUMAGAI
+    params = PARAMS[kind]
     a_min, e_min = lattice_minimum(kind, builder, params, 0.9 * a0, 1.1 * a0)
     assert within(-e_min, Ec), (name, e_min)
     assert within(a_min, a0), (name, a_min)
@@ -184,8 +204,11 @@ def fd_check(kind, s, params, dx=1e-6, natoms=None, mask=None):
     return err, np.max(np.abs(W - o["wpot"]))
 
 
+@pytest.mark.parametrize("scr", [False, True])
 @pytest.mark.parametrize("name", ["dia-Si", "dia-C", "B3-SiC", "a-C", "kumagai"])
-def test_fd_forces_virial_bop(name):
+def test_fd_forces_virial_bop(name, scr):
+    # tests/test_forces_and_virial.py:115-140 (Tersoff, TersoffScr, Kumagai,
+    # KumagaiScr on dia-C, a-C, dia-Si, B3-SiC)
     if name == "dia-Si":
         kind, s = "tersoff", rattled_diamond("Si", 5.431, (2, 2, 2), 0.5, 1)
     elif name == "dia-C":
@@ -198,8 +221,9 @@ def test_fd_forces_virial_bop(name):
         kind, s = "tersoff", random_carbon(64, seed=4)
     else:
         kind, s = "kumagai", rattled_diamond("Si", 5.429, (2, 2, 2), 0.4, 5)
-    params = TERSOFF if kind == "tersoff" else KUMAGAI
-    ferr, werr = fd_check(kind, s, params, natoms=12)
+    if scr:
+        kind += "_scr"
+    ferr, werr = fd_check(kind, s, PARAMS[kind], natoms=12)
     assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
 
 
@@ -238,12 +262,14 @@ def test_eam_special_cases(reference_tests_dir):
         assert err < 1e-6, (fac, err)
 
 
-def test_mask_additivity():
+@pytest.mark.parametrize("kind", ["tersoff", "tersoff_scr"])
+def test_mask_additivity(kind):
+    # tests/test_mask.py:68 (Tersoff, TersoffScr)
     s = random_carbon(96, seed=8)
     mask = np.random.default_rng(9).integers(0, 2, len(s)).astype(bool)
-    o = energy("tersoff", s, TERSOFF)
-    o1 = energy("tersoff", s, TERSOFF, mask=mask)
-    o2 = energy("tersoff", s, TERSOFF, mask=~mask)
+    o = energy(kind, s, PARAMS[kind])
+    o1 = energy(kind, s, PARAMS[kind], mask=mask)
+    o2 = energy(kind, s, PARAMS[kind], mask=~mask)
     assert abs(o["epot"] - o1["epot"] - o2["epot"]) < 1e-6
     assert np.max(np.abs(o["f"] - o1["f"] - o2["f"])) < 1e-6
     assert np.max(np.abs(o["wpot"] - o1["wpot"] - o2["wpot"])) < 1e-6
@@ -328,14 +354,16 @@ def test_floating_point_issue_coordination():
         assert np.all(np.bincount(nl.i[r < 3.0], minlength=8) == 4)
 
 
-def test_dimer_continuity_kumagai():
+@pytest.mark.parametrize("kind", ["kumagai", "kumagai_scr"])
+def test_dimer_continuity_kumagai(kind):
+    # tests/test_dimers.py:109-136 (Kumagai, KumagaiScr)
     vac = 4.0
     e, f = [], []
     for d in np.linspace(1.8, 6.2, 1000):
         s = S.Structure(np.array([[vac, vac, vac], [vac + d, vac, vac]]),
                         np.diag([2 * vac + d + 6.2, 2 * vac, 2 * vac]), np.array([False] * 3),
                         np.array([14, 14], dtype=np.int32))
-        o = energy("kumagai", s, KUMAGAI)
+        o = energy(kind, s, PARAMS[kind])
         e.append(o["epot"])
         f.append(o["f"][0, 0])
     assert np.max(np.abs(np.diff(e))) < 0.08
