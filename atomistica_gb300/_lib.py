@@ -40,6 +40,8 @@ SIGNATURES = [
     ("gb_neighbors_set_stream", _I, [_P, _P]),
     ("gb_tersoff_new", _I, [_P, _P]),
     ("gb_kumagai_new", _I, [_P, _P]),
+    ("gb_tersoff_scr_new", _I, [_P, _P, _P]),
+    ("gb_kumagai_scr_new", _I, [_P, _P, _P]),
     ("gb_tabulated_alloy_eam_new", _I, [_P, ctypes.c_char_p]),
     ("gb_potential_free", None, [_P]),
     ("gb_potential_set_precision", _I, [_P, _I]),
@@ -90,6 +92,11 @@ class KumagaiParams(ctypes.Structure):
         [(k, _D * 1) for k in ("A", "B", "lambda1", "lambda2", "eta", "delta", "alpha")] + \
         [("beta", _I * 1)] + \
         [(k, _D * 1) for k in ("c1", "c2", "c3", "c4", "c5", "h", "r1", "r2")]
+
+
+class ScreeningParams(ctypes.Structure):
+    """gb_screening_params_t"""
+    _fields_ = [(k, _D * 6) for k in ("or1", "or2", "bor1", "bor2", "Cmin", "Cmax")]
 
 
 _lib = None

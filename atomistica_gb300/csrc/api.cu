@@ -80,6 +80,60 @@ gb_kumagai_params_t default_kumagai() {
   return p;
 }
 
+// Tersoff_PRB_39_5566_SiC__Scr (tersoff_params.f90:99-138 under SCREENING):
+// m = 3, mubo = 1 / dimer length, inner cutoff r1 < r2 = 1.2 r1.
+gb_tersoff_params_t default_tersoff_scr() {
+  gb_tersoff_params_t p = default_tersoff();
+  const double mubo[3] = {0.69103023078057590, 0.56580821386164815, 0.43569872294774004};
+  const double r1[3] = {2.00, std::sqrt(2.00 * 2.50), 2.50};
+  for (int q = 0; q < 3; q++) {
+    p.mubo[q] = mubo[q];
+    p.m[q] = 3;
+    p.r1[q] = r1[q];
+    p.r2[q] = r1[q] * 1.2;
+  }
+  return p;
+}
+
+gb_screening_params_t default_screening_tersoff() {
+  gb_screening_params_t s{};
+  const double o1[3] = {2.00, std::sqrt(2.00 * 3.00), 3.00};
+  for (int q = 0; q < 3; q++) {
+    s.or1[q] = s.bor1[q] = o1[q];
+    s.or2[q] = s.bor2[q] = o1[q] * 2.0;
+    s.Cmin[q] = 1.0;
+    s.Cmax[q] = 3.0;
+  }
+  return s;
+}
+
+// Kumagai_CompMaterSci_39_457_Si__Scr (kumagai_params.f90:119-128).
+gb_kumagai_params_t default_kumagai_scr() {
+  gb_kumagai_params_t p = default_kumagai();
+  p.r1[0] = 2.50;
+  p.r2[0] = 2.50 * 1.2;
+  return p;
+}
+
+gb_screening_params_t default_screening_kumagai() {
+  gb_screening_params_t s{};
+  s.or1[0] = s.bor1[0] = 3.00;
+  s.or2[0] = s.bor2[0] = 3.00 * 2.0;
+  s.Cmin[0] = 1.0;
+  s.Cmax[0] = 3.0;
+  return s;
+}
+
+int check_screening(const gb_screening_params_t &s, int npairs) {
+  for (int q = 0; q < npairs; q++) {
+    if (!(s.or2[q] > s.or1[q]) || !(s.bor2[q] > s.bor1[q]) || !(s.Cmax[q] > s.Cmin[q])) {
+      set_error("screening: need or1 < or2, bor1 < bor2 and Cmin < Cmax for every pair");
+      return GB_ERROR_ARGUMENT;
+    }
+  }
+  return 0;
+}
+
 int check_tersoff(const gb_tersoff_params_t &p) {
   if (p.nel < 1 || p.nel > 3) {
     set_error("Tersoff: nel must be 1..3");
@@ -121,6 +175,20 @@ int check_kumagai(const gb_kumagai_params_t &p) {
 }
 
 }  // namespace
+
+double bop_pair_range(const Potential &pot, int t) {
+  const double *r2 = pot.kind == kTersoff ? pot.tp.r2 : pot.kp.r2;
+  if (!pot.screened) return r2[t];
+  const int np = pot_nel(pot) * (pot_nel(pot) + 1) / 2;
+  double mx = 0.0;
+  for (int q = 0; q < np; q++) {
+    const double m = std::max(std::max(r2[q], pot.scr.or2[q]), pot.scr.bor2[q]);
+    mx = std::max(mx, m * m);
+  }
+  const double cmax = pot.scr.Cmax[t];
+  const double cdr = cmax > 2.0 ? cmax * cmax / (4 * (cmax - 1)) : 1.0;
+  return std::sqrt(cdr) * std::sqrt(mx);
+}
 
 int pot_nel(const Potential &pot) {
   if (pot.kind == kTersoff) return pot.tp.nel;
@@ -327,6 +395,11 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
     set_error("Internal error: bond-order tile plan mismatch.");
     return GB_ERROR_UNSPECIFIED;
   }
+  if (st & 4) {
+    set_error("Internal neighbor list exhausted: an atom has more bonds after screening than "
+              "the screened kernel supports (32).");
+    return GB_ERROR_CAPACITY;
+  }
   // epot is set; wpot accumulated (gen_factory.py:283, potential.c:468-479).
   if (is_device_ptr(epot)) {
     GB_CUDA(cudaMemcpy(epot, hr, sizeof(double), cudaMemcpyHostToDevice));
@@ -368,7 +441,7 @@ int bind_to(Potential &pot, Particles &p, Neighbors &nl) {
         const int ii = dbidx(zi), jj = dbidx(zj);
         if (ii < 0 || jj < 0) continue;
         const int t = pair_index(ii, jj, nel);
-        const double c = pot.kind == kTersoff ? pot.tp.r2[t] : pot.kp.r2[t];
+        const double c = bop_pair_range(pot, t);
         if (c > nl.interaction_range) {
           nl.interaction_range = c;
           nl.valid = false;
@@ -403,6 +476,38 @@ int gb_kumagai_new(gb_potential_t **h, const gb_kumagai_params_t *params) {
   *h = new gb_potential;
   (*h)->pot.kind = kKumagai;
   (*h)->pot.kp = p;
+  return 0;
+}
+
+int gb_tersoff_scr_new(gb_potential_t **h, const gb_tersoff_params_t *params,
+                       const gb_screening_params_t *scr) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_tersoff_params_t p = params ? *params : default_tersoff_scr();
+  gb_screening_params_t sc = scr ? *scr : default_screening_tersoff();
+  GB_CHECK(check_tersoff(p));
+  GB_CHECK(check_screening(sc, p.nel * (p.nel + 1) / 2));
+  *h = new gb_potential;
+  (*h)->pot.kind = kTersoff;
+  (*h)->pot.tp = p;
+  (*h)->pot.screened = true;
+  (*h)->pot.scr = sc;
+  return 0;
+}
+
+int gb_kumagai_scr_new(gb_potential_t **h, const gb_kumagai_params_t *params,
+                       const gb_screening_params_t *scr) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_kumagai_params_t p = params ? *params : default_kumagai_scr();
+  gb_screening_params_t sc = scr ? *scr : default_screening_kumagai();
+  GB_CHECK(check_kumagai(p));
+  GB_CHECK(check_screening(sc, 1));
+  *h = new gb_potential;
+  (*h)->pot.kind = kKumagai;
+  (*h)->pot.kp = p;
+  (*h)->pot.screened = true;
+  (*h)->pot.scr = sc;
   return 0;
 }
 
@@ -442,6 +547,10 @@ int gb_potential_set_precision(gb_potential_t *h, int precision) {
     set_error("TabulatedAlloyEAM has only the FP64 form.");
     return GB_ERROR_ARGUMENT;
   }
+  if (h->pot.screened && precision != GB_PRECISION_FP64) {
+    set_error("The screened potentials have only the FP64 form.");
+    return GB_ERROR_ARGUMENT;
+  }
   h->pot.precision = precision;
   return 0;
 }
@@ -462,8 +571,7 @@ double gb_potential_get_cutoff(const gb_potential_t *h) {
   if (pot.kind == kEAM) return pot.eam->cutoff;
   double c = 0.0;
   const int np = pot_nel(pot) * (pot_nel(pot) + 1) / 2;
-  for (int q = 0; q < np; q++)
-    c = std::max(c, pot.kind == kTersoff ? pot.tp.r2[q] : pot.kp.r2[q]);
+  for (int q = 0; q < np; q++) c = std::max(c, bop_pair_range(pot, q));
   return c;
 }
 

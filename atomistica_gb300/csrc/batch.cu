@@ -66,7 +66,7 @@ double batch_cutoff(const Batch &b, const Potential &pot) {
       const int ii = dbidx(zi), jj = dbidx(zj);
       if (ii < 0 || jj < 0) continue;
       const int t = pair_index(ii, jj, nel);
-      cut = std::max(cut, pot.kind == kTersoff ? pot.tp.r2[t] : pot.kp.r2[t]);
+      cut = std::max(cut, bop_pair_range(pot, t));
     }
   return cut;
 }
@@ -416,8 +416,8 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
     set_error("batch_energy_and_forces: epot, f and wpot are required");
     return GB_ERROR_ARGUMENT;
   }
-  if (pot.kind == kEAM) {
-    set_error("batch_energy_and_forces: batches support the bond-order potentials");
+  if (pot.kind == kEAM || pot.screened) {
+    set_error("batch_energy_and_forces: batches support the non-screened bond-order potentials");
     return GB_ERROR_ARGUMENT;
   }
   b.info[0] = 0;

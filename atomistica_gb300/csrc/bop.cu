@@ -467,6 +467,7 @@ __global__ void __launch_bounds__(kBopThreads)
 }  // namespace gb
 
 #include "bop_mixed.cuh"
+#include "bop_scr.cuh"
 
 namespace gb {
 namespace {
@@ -719,8 +720,91 @@ int reduce_partials(const double *part, int nrows, int nc, double *red, double *
 
 static const size_t kSmemBudget = 200 * 1024;
 
+namespace {
+
+template <class Pot>
+int launch_scr(const BopArgs &args, const Pot &pot, const ScrDev &sd, int blocks, int *status,
+               bool wat, bool pb, cudaStream_t s) {
+  if (wat && pb)
+    bop_scr_atom<Pot, true, true><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
+  else if (wat)
+    bop_scr_atom<Pot, true, false><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
+  else if (pb)
+    bop_scr_atom<Pot, false, true><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
+  else
+    bop_scr_atom<Pot, false, false><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// Screened variants: one thread per atom over the whole list (bop_scr.cuh),
+// then the same gather and sums as the tile kernels.
+int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
+                bool want_wat, bool want_pb) {
+  cudaStream_t s = pot.stream;
+  const int nat = sys.nat;
+  if (sys.tile_atom0) {
+    set_error("batches support the non-screened bond-order potentials");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (pot.precision != GB_PRECISION_FP64) {
+    set_error("The screened potentials have only the FP64 form.");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (nat == 0) {
+    GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
+    return 0;
+  }
+  GB_CHECK(neighbors_build_reverse(nl, nat, s, true));
+  const int64_t nb = std::max<int64_t>(nl.nentries, 1);
+  GB_CHECK(pot.bond_G.ensure(sizeof(double) * 3 * nb));
+  GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
+  if (want_wat) GB_CHECK(pot.bond_w.ensure(sizeof(double) * 9 * nb));
+  if (want_pb) GB_CHECK(pot.bond_fr.ensure(sizeof(double) * 3 * nb));
+  const int blocks = (nat + kScrThreads - 1) / kScrThreads;
+  GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * blocks + 64));
+  BopArgs args;
+  args.nat = nat;
+  args.apt = 1;
+  args.pos = nl.pos4.as<Pos4>();
+  args.el = pot.el.as<int>();
+  args.seed = nl.seed.as<int>();
+  args.nbr = nl.nbr.as<int>();
+  args.shift = nl.shift.as<int>();
+  args.mask = o.mask;
+  std::memcpy(args.A, sys.A, sizeof(args.A));
+  args.G = pot.bond_G.as<double>();
+  args.ebond = (o.epot_per_at || o.epot_per_bond) ? pot.bond_e.as<double>() : nullptr;
+  args.wbond = want_wat ? pot.bond_w.as<double>() : nullptr;
+  args.frbond = want_pb ? pot.bond_fr.as<double>() : nullptr;
+  args.tile_part = pot.tile_part.as<double>();
+  GB_CUDA(cudaEventRecord(pot.kev[0], s));
+  if (pot.kind == kTersoff) {
+    const ScrDev sd = make_scr_dev(pot.tp.r1, pot.tp.r2, pot.tp.nel * (pot.tp.nel + 1) / 2,
+                                   pot.scr);
+    GB_CHECK(launch_scr(args, TersoffPot{make_tersoff_dev(pot.tp)}, sd, blocks, o.status,
+                        want_wat, want_pb, s));
+  } else {
+    const ScrDev sd = make_scr_dev(pot.kp.r1, pot.kp.r2, 1, pot.scr);
+    GB_CHECK(launch_scr(args, KumagaiPot{make_kumagai_dev(pot.kp)}, sd, blocks, o.status,
+                        want_wat, want_pb, s));
+  }
+  GB_CUDA(cudaEventRecord(pot.kev[1], s));
+  GB_CHECK(launch_gather(false, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
+                         args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
+  GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(blocks) + 64));
+  GB_CHECK(reduce_partials(args.tile_part, blocks, 10, o.red, pot.red_stage.as<double>(), s));
+  pot.tile_atoms = 1;
+  pot.last_plan[0] = pot.last_plan[1] = 0;
+  return 0;
+}
+
+}  // namespace
+
 int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
             bool want_wat, bool want_pb) {
+  if (pot.screened) return bop_run_scr(pot, sys, nl, o, want_wat, want_pb);
   cudaStream_t s = pot.stream;
   const int nat = sys.nat;
   const bool batch = sys.tile_atom0 != nullptr;
@@ -1036,8 +1120,9 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
     return GB_ERROR_ARGUMENT;
   }
   Potential &pot = h->pot;
-  if (pot.kind != kTersoff && pot.kind != kKumagai) {
-    set_error("noalloc: only the bond-order potentials (Tersoff, Kumagai) are supported");
+  if ((pot.kind != kTersoff && pot.kind != kKumagai) || pot.screened) {
+    set_error("noalloc: only the non-screened bond-order potentials (Tersoff, Kumagai) are "
+              "supported");
     return GB_ERROR_ARGUMENT;
   }
   if (nat < 0 || nat > kNoallocMaxAtoms) {

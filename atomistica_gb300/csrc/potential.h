@@ -65,6 +65,8 @@ struct Potential {
   int precision = GB_PRECISION_FP64;
   gb_tersoff_params_t tp{};
   gb_kumagai_params_t kp{};
+  bool screened = false;        // TersoffScr / KumagaiScr
+  gb_screening_params_t scr{};  // their outer / bond-order cutoffs, Cmin, Cmax
   std::unique_ptr<EamTables> eam;
 
   cudaStream_t stream = nullptr;
@@ -94,8 +96,10 @@ struct Potential {
   int last_plan[2] = {0, 0};  // largest bonds / (ij, ik) slots per tile of the last call
 };
 
-// Interaction range requested by bind_to for the given element pair set.
-double bop_pair_cutoff(const Potential &pot, int zi, int zj);
+// Interaction range requested by bind_to for element pair t (database
+// indices): r2, or for the screened variants sqrt(C_dr_cut(t)) times the
+// largest cutoff of all pairs (default_bind_to_func.f90:117-144).
+double bop_pair_range(const Potential &pot, int t);
 
 // Kernel launches (on pot.stream) for an up-to-date neighbour list.
 int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,

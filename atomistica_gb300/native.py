@@ -26,8 +26,9 @@ import numpy as np
 
 from . import _lib
 from ._lib import GB_PRECISION_FP64, GB_PRECISION_MIXED, check, load
-from .parameters import (Kumagai_CompMaterSci_39_457_Si, Tersoff_PRB_39_5566_Si_C,
-                         atomic_numbers)
+from .parameters import (SCREENING_KEYS, Kumagai_CompMaterSci_39_457_Si,
+                         Kumagai_CompMaterSci_39_457_Si__Scr, Tersoff_PRB_39_5566_Si_C,
+                         Tersoff_PRB_39_5566_Si_C__Scr, atomic_numbers)
 
 try:  # PyTorch is optional: only for device-resident inputs/outputs.
     import torch
@@ -198,10 +199,10 @@ def _fill(arr, vals, n):
         arr[q] = vals[q]
 
 
-def tersoff_params(params):
+def tersoff_params(params, base=Tersoff_PRB_39_5566_Si_C):
     """gb_tersoff_params_t from a parameter dict (parameters.py format);
-    keys not given keep the values of the default Si-C set."""
-    d = dict(Tersoff_PRB_39_5566_Si_C)
+    keys not given keep the values of ``base`` (the default Si-C set)."""
+    d = dict(base)
     d.update({k: v for k, v in params.items() if not k.startswith("__")})
     p = _lib.TersoffParams()
     els = d["el"]
@@ -223,8 +224,18 @@ def tersoff_params(params):
     return p
 
 
-def kumagai_params(params):
-    d = dict(Kumagai_CompMaterSci_39_457_Si)
+def screening_params(params, base):
+    """gb_screening_params_t (or1, or2, bor1, bor2, Cmin, Cmax per pair)."""
+    d = dict(base)
+    d.update({k: v for k, v in params.items() if k in SCREENING_KEYS})
+    p = _lib.ScreeningParams()
+    for k in SCREENING_KEYS:
+        _fill(getattr(p, k), [float(v) for v in d[k]], len(d[k]))
+    return p
+
+
+def kumagai_params(params, base=Kumagai_CompMaterSci_39_457_Si):
+    d = dict(base)
     d.update({k: v for k, v in params.items() if not k.startswith("__")})
     p = _lib.KumagaiParams()
     if len(d["el"]) != 1:
@@ -381,6 +392,34 @@ class Kumagai(_Potential):
             check(self._L.gb_kumagai_new(ctypes.byref(self._h), ctypes.byref(p)), "Kumagai")
         else:
             check(self._L.gb_kumagai_new(ctypes.byref(self._h), None), "Kumagai")
+        self.set_precision(precision)
+
+
+class TersoffScr(_Potential):
+    """Screened Tersoff potential (src/potentials/bop/tersoff/tersoff_scr.f90):
+    FP64 only; default parameters Tersoff_PRB_39_5566_Si_C__Scr."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        base = Tersoff_PRB_39_5566_Si_C__Scr
+        p = tersoff_params(params, base)
+        sp = screening_params(params, base)
+        check(self._L.gb_tersoff_scr_new(ctypes.byref(self._h), ctypes.byref(p),
+                                         ctypes.byref(sp)), "TersoffScr")
+        self.set_precision(precision)
+
+
+class KumagaiScr(_Potential):
+    """Screened Kumagai potential (src/potentials/bop/kumagai/kumagai_scr.f90):
+    FP64 only; default parameters Kumagai_CompMaterSci_39_457_Si__Scr."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        base = Kumagai_CompMaterSci_39_457_Si__Scr
+        p = kumagai_params(params, base)
+        sp = screening_params(params, base)
+        check(self._L.gb_kumagai_scr_new(ctypes.byref(self._h), ctypes.byref(p),
+                                         ctypes.byref(sp)), "KumagaiScr")
         self.set_precision(precision)
 
 

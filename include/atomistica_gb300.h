@@ -142,6 +142,15 @@ typedef struct gb_kumagai_params {
   double r1[1], r2[1];
 } gb_kumagai_params_t;
 
+/* Extra parameters of the screened variants TersoffScr / KumagaiScr
+ * (tersoff_params.f90:81-90 under SCREENING), per element pair: outer
+ * (attractive/repulsive) cutoff or1 < or2, bond-order cutoff bor1 < bor2 and
+ * the screening window Cmin < Cmax.  The inner cutoff is r1 < r2 of the base
+ * parameter set (exp_cutoff form, cutoff.f90:232-293). */
+typedef struct gb_screening_params {
+  double or1[6], or2[6], bor1[6], bor2[6], Cmin[6], Cmax[6];
+} gb_screening_params_t;
+
 /* python_tersoff_new + register (parameters set through a struct instead of
  * the ptrdict config tree, tersoff_registry.f90:22-115). params may be NULL
  * for the default Tersoff_PRB_39_5566_SiC set (tersoff_params.f90:99-138). */
@@ -149,6 +158,15 @@ int gb_tersoff_new(gb_potential_t **pot, const gb_tersoff_params_t *params);
 /* python_kumagai_new; NULL = Kumagai_CompMaterSci_39_457_Si
  * (kumagai_params.f90:97-132). */
 int gb_kumagai_new(gb_potential_t **pot, const gb_kumagai_params_t *params);
+/* python_tersoff_scr_new (tersoff_scr.f90): NULL params / scr = the
+ * Tersoff_PRB_39_5566_SiC__Scr set (m = 3, mubo = 1 / dimer length,
+ * tersoff_params.f90:99-138 under SCREENING).  FP64 only. */
+int gb_tersoff_scr_new(gb_potential_t **pot, const gb_tersoff_params_t *params,
+                       const gb_screening_params_t *scr);
+/* python_kumagai_scr_new (kumagai_scr.f90): NULL = the
+ * Kumagai_CompMaterSci_39_457_Si__Scr set.  FP64 only. */
+int gb_kumagai_scr_new(gb_potential_t **pot, const gb_kumagai_params_t *params,
+                       const gb_screening_params_t *scr);
 /* python_tabulated_alloy_eam_new + init(fn=...) (tabulated_alloy_eam.f90:147-259):
  * reads a DYNAMO setfl file. */
 int gb_tabulated_alloy_eam_new(gb_potential_t **pot, const char *fn);

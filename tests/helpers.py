@@ -8,6 +8,8 @@ from atomistica_gb300 import structures as S
 
 TERSOFF = P.Tersoff_PRB_39_5566_Si_C
 KUMAGAI = P.Kumagai_CompMaterSci_39_457_Si
+TERSOFF_SCR = P.Tersoff_PRB_39_5566_Si_C__Scr
+KUMAGAI_SCR = P.Kumagai_CompMaterSci_39_457_Si__Scr
 
 # Tolerances of the FP64 drop-in against the FP64 oracle (per atom energy,
 # force and virial components), and of the mixed form's forces.
@@ -22,7 +24,8 @@ def gpu_bop(kind, s, precision="fp64", params=None, mask=None, per_at=True, per_
     from atomistica_gb300 import native
     p = native.from_atoms(s)
     nl = native.Neighbors(100)
-    cls = native.Tersoff if kind == "tersoff" else native.Kumagai
+    cls = {"tersoff": native.Tersoff, "kumagai": native.Kumagai,
+           "tersoff_scr": native.TersoffScr, "kumagai_scr": native.KumagaiScr}[kind]
     pot = cls(precision=precision, **(params or {}))
     pot.bind_to(p, nl)
     out = None
