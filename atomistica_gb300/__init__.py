@@ -1,8 +1,9 @@
 """
 atomistica_gb300 — GB300-native (CUDA sm_103a) per-step force path of the
 Atomistica interatomic-potential library: cell-list neighbour build,
-Tersoff / Kumagai bond-order potentials (FP64 drop-in and FP32-mixed form) and
-tabulated alloy EAM, behind Atomistica's potential API.
+Tersoff / Kumagai bond-order potentials (FP64 drop-in and FP32-mixed form),
+their screened variants TersoffScr / KumagaiScr (FP64) and tabulated alloy
+EAM, behind Atomistica's potential API.
 
     from atomistica_gb300 import Tersoff          # ASE-style calculator
     from atomistica_gb300 import native           # _atomistica-style objects
@@ -12,7 +13,9 @@ include/atomistica_gb300.h); build it with atomistica_gb300.build.build().
 """
 
 from . import parameters, structures  # noqa: F401
-from .parameters import Kumagai_CompMaterSci_39_457_Si, Tersoff_PRB_39_5566_Si_C  # noqa: F401
+from .parameters import (Kumagai_CompMaterSci_39_457_Si,  # noqa: F401
+                         Kumagai_CompMaterSci_39_457_Si__Scr, Tersoff_PRB_39_5566_Si_C,
+                         Tersoff_PRB_39_5566_Si_C__Scr)
 
 __version__ = "0.1.0"
 
@@ -20,7 +23,8 @@ __version__ = "0.1.0"
 def __getattr__(name):
     # The calculator classes load the CUDA library lazily, so that parameter
     # sets and structure builders stay importable on machines without a GPU.
-    if name in ("Atomistica", "Tersoff", "Kumagai", "TabulatedAlloyEAM"):
+    if name in ("Atomistica", "Tersoff", "Kumagai", "TersoffScr", "KumagaiScr",
+                "TabulatedAlloyEAM"):
         from . import calculator
         return getattr(calculator, name)
     if name in ("native", "calculator", "io", "build"):

@@ -186,6 +186,16 @@ class Kumagai(Atomistica):
     potential_class = native.Kumagai
 
 
+class TersoffScr(Atomistica):
+    name = "TersoffScr"
+    potential_class = native.TersoffScr
+
+
+class KumagaiScr(Atomistica):
+    name = "KumagaiScr"
+    potential_class = native.KumagaiScr
+
+
 class TabulatedAlloyEAM(Atomistica):
     name = "TabulatedAlloyEAM"
     potential_class = native.TabulatedAlloyEAM

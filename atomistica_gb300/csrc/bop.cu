@@ -551,12 +551,12 @@ __global__ void reduce_rows_kernel(const double *__restrict__ part, int nrows, i
   }
 }
 
-// Dynamic shared memory above 48 KB needs an opt-in per kernel: raise it
-// once per kernel and device to the budget of the largest tile (so that no
+// Dynamic plus static shared memory above 48 KB needs an opt-in per kernel:
+// raise the dynamic limit once per kernel and device to the budget of the
+// largest tile (on the first launch, which is always an eager one, so that no
 // attribute call happens while a stream is being captured into a graph).
 template <auto Kern>
 cudaError_t allow_smem(size_t smem) {
-  if (smem <= 48 * 1024) return cudaSuccess;
   if (smem > kSmemBudgetAll) return cudaErrorInvalidValue;
   static int done_for = -1;  // one per kernel (template argument)
   int dev = 0;
@@ -722,20 +722,25 @@ static const size_t kSmemBudget = 200 * 1024;
 
 namespace {
 
-template <class Pot>
-int launch_scr(const BopArgs &args, const Pot &pot, const ScrDev &sd, int blocks, int *status,
-               bool wat, bool pb, cudaStream_t s) {
-  if (wat && pb)
-    bop_scr_atom<Pot, true, true><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
-  else if (wat)
-    bop_scr_atom<Pot, true, false><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
-  else if (pb)
-    bop_scr_atom<Pot, false, true><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
-  else
-    bop_scr_atom<Pot, false, false><<<blocks, kScrThreads, 0, s>>>(args, pot, sd, status);
+template <class Pot, bool kWat, bool kPB>
+int launch_scr1(const BopArgs &args, const Pot &pot, const ScrDev &sd, int blocks, int *status,
+                cudaStream_t s) {
+  const size_t smem = sizeof(ScrWarpMem) * kScrWarps;
+  const cudaError_t ae = allow_smem<bop_scr_atom<Pot, kWat, kPB>>(smem);
+  GB_CUDA(ae);
+  bop_scr_atom<Pot, kWat, kPB><<<blocks, kScrThreads, smem, s>>>(args, pot, sd, status);
   note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
+}
+
+template <class Pot>
+int launch_scr(const BopArgs &args, const Pot &pot, const ScrDev &sd, int blocks, int *status,
+               bool wat, bool pb, cudaStream_t s) {
+  if (wat && pb) return launch_scr1<Pot, true, true>(args, pot, sd, blocks, status, s);
+  if (wat) return launch_scr1<Pot, true, false>(args, pot, sd, blocks, status, s);
+  if (pb) return launch_scr1<Pot, false, true>(args, pot, sd, blocks, status, s);
+  return launch_scr1<Pot, false, false>(args, pot, sd, blocks, status, s);
 }
 
 // Screened variants: one thread per atom over the whole list (bop_scr.cuh),
@@ -762,7 +767,7 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
   GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
   if (want_wat) GB_CHECK(pot.bond_w.ensure(sizeof(double) * 9 * nb));
   if (want_pb) GB_CHECK(pot.bond_fr.ensure(sizeof(double) * 3 * nb));
-  const int blocks = (nat + kScrThreads - 1) / kScrThreads;
+  const int blocks = (nat + kScrWarps - 1) / kScrWarps;  // a warp per atom
   GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * blocks + 64));
   BopArgs args;
   args.nat = nat;

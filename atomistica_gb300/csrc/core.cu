@@ -696,6 +696,38 @@ __global__ void nl_reverse(int nat, const int *__restrict__ seed, const int *__r
   }
 }
 
+// The same for long lists (large cutoffs, e.g. the screened potentials): a
+// warp per atom i, its lanes over the entries of i.
+__global__ void nl_reverse_dense(int nat, const int *__restrict__ seed,
+                                 const int *__restrict__ nbr, const int *__restrict__ shift,
+                                 int *__restrict__ rev, int *__restrict__ status) {
+  const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= nat) return;
+  const int b1 = seed[i + 1];
+  for (int b = seed[i] + lane; b < b1; b += 32) {
+    const int j = nbr[b];
+    int s0, s1, s2;
+    unpack_shift(shift[b], s0, s1, s2);
+    const int want = pack_shift(-s0, -s1, -s2);
+    const int c0 = seed[j], c1 = seed[j + 1];
+    int found = -1;
+    for (int c = c0; c < c1 && found < 0; c += 4) {
+      int nj[4], sj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        nj[q] = c + q < c1 ? nbr[c + q] : -1;
+        sj[q] = c + q < c1 ? shift[c + q] : 0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (found < 0 && nj[q] == i && sj[q] == want) found = c + q;
+    }
+    if (found < 0) atomicOr(&status[1], 4);
+    rev[b] = found;
+  }
+}
+
 }  // namespace
 
 // Host-side binning_init (python_neighbors.f90:765-871) for one cell:
@@ -974,9 +1006,13 @@ int neighbors_build_reverse(Neighbors &nl, int nat, cudaStream_t stream, bool sy
   int *status = nl.stats.as<int>();
   GB_CUDA(cudaMemsetAsync(status + 1, 0, sizeof(int), stream));
   if (nat > 0) {
-    nl_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.seed.as<int>(), nl.nbr.as<int>(),
-                                                     nl.shift.as<int>(), nl.rev.as<int>(),
-                                                     status);
+    if (nl.nentries > 24 * (int64_t)nat)  // long lists: a warp per atom
+      nl_reverse_dense<<<(unsigned)(((int64_t)nat * 32 + 127) / 128), 128, 0, stream>>>(
+          nat, nl.seed.as<int>(), nl.nbr.as<int>(), nl.shift.as<int>(), nl.rev.as<int>(), status);
+    else
+      nl_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.seed.as<int>(), nl.nbr.as<int>(),
+                                                       nl.shift.as<int>(), nl.rev.as<int>(),
+                                                       status);
     note_launch();
   }
   int *hs = nl.hstats.as<int>();

@@ -106,6 +106,18 @@ def tersoff_si_4096(seed=1):
     return s
 
 
+def amorphous_carbon(nat=4096, density=3.0, seed=7, dmin=1.2):
+    """Random carbon packing at ``density`` g/cm^3 (cubic box, minimum
+    separation ``dmin`` over all images): a stand-in for amorphous carbon
+    such as the reference's aC.cfg."""
+    rng = np.random.default_rng(seed)
+    L = (nat * 12.011 / (density * 6.02214076e23) * 1e24) ** (1.0 / 3.0)
+    cell = np.eye(3) * L
+    pos = _random_packing(rng, nat, cell, dmin)
+    return Structure(pos, cell, np.array([True, True, True]), np.full(nat, 6, dtype=np.int32),
+                     {"workload": "amorphous_carbon", "seed": seed, "density_gcc": density})
+
+
 def eam_cu_131072(seed=2):
     """FCC Cu, a=3.615, 32^3 cells (131072 atoms), Gaussian sigma=0.05 A."""
     rng = np.random.default_rng(seed)

@@ -218,6 +218,7 @@ def other_configs(dev, oracle):
                        "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                        "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}
     out["tersoff_si_4096"] = entry
+    out["tersoff_scr"] = screened_config(dev, oracle, nth, cpu_time)
 
     s = structures.eam_cu_131072(seed=2)
     with tempfile.TemporaryDirectory() as td:
@@ -244,6 +245,41 @@ def other_configs(dev, oracle):
                             "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
                                      "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                                      "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
+    return out
+
+
+def screened_config(dev, oracle, nth, cpu_time):
+    """TersoffScr (FP64) on the 4096-atom Si crystal and on 4096 atoms of
+    random carbon at 3.0 g/cm^3 (partially screened bonds everywhere): GPU
+    atom-evals/s through the public API with device-resident inputs against
+    the oracle on all host cores."""
+    import numpy as np
+    import torch
+    from atomistica_gb300 import native, parameters, structures
+    params = parameters.Tersoff_PRB_39_5566_Si_C__Scr
+    out = {}
+    for name, s in (("si_4096", structures.tersoff_si_4096(seed=1)),
+                    ("aC_4096", structures.amorphous_carbon(4096, seed=7))):
+        ref = oracle.bop_compute("tersoff_scr", params, s, nthreads=nth)
+        t_cpu = cpu_time(lambda: oracle.bop_compute("tersoff_scr", params, s, nthreads=nth),
+                         runs=3)
+        p = native.from_atoms(s)
+        nl = native.Neighbors(100)
+        pot = native.TersoffScr()
+        pot.bind_to(p, nl)
+        d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+        d_f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+        ms = _gpu_step_ms(pot, p, nl, d_pos, d_f, steps=5)
+        d_f.zero_()
+        p.set_positions(d_pos)
+        e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
+        f = d_f.cpu().numpy()
+        out[name] = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu,
+                     "cpu_cores": nth, "neighbours_per_atom": pot.last_stats()[0] / len(s),
+                     "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
+                              "kernel_ms": pot.last_timing()[3],
+                              "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
+                              "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
     return out
 
 
