@@ -41,6 +41,8 @@ SIGNATURES = [
     ("gb_tersoff_new", _I, [_P, _P]),
     ("gb_kumagai_new", _I, [_P, _P]),
     ("gb_tersoff_scr_new", _I, [_P, _P, _P]),
+    ("gb_potential_energy_and_forces_ghost", _I,
+     [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("gb_kumagai_scr_new", _I, [_P, _P, _P]),
     ("gb_tabulated_alloy_eam_new", _I, [_P, ctypes.c_char_p]),
     ("gb_potential_free", None, [_P]),

@@ -452,6 +452,192 @@ int bind_to(Potential &pot, Particles &p, Neighbors &nl) {
   return update_element_map(pot, p);
 }
 
+__global__ void fill_i32(int *__restrict__ p, int64_t n, int v) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    p[k] = v;
+}
+
+__global__ void ghost_pos4(int nat, const double *__restrict__ r, Pos4 *__restrict__ p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  Pos4 q;
+  q.x = r[3 * (size_t)i];
+  q.y = r[3 * (size_t)i + 1];
+  q.z = r[3 * (size_t)i + 2];
+  q.w = 0.0;
+  p[i] = q;
+}
+
+// The LAMMPS contract (bop_kernel.f90:577-597 under LAMMPS,
+// pair_atomistica.cpp:386-545): nat = local + ghost atoms with explicit
+// positions, a full list (CSR, 0-based) over all of them without image
+// shifts; bonds are computed for the first natloc atoms only and forces are
+// returned for all nat atoms (the caller sums the ghost forces back onto
+// their owners).  epot and wpot are the sums over the local atoms' bonds.
+int energy_and_forces_ghost(Potential &pot, int nat, int natloc, const double *r, const int *Z,
+                            const int *seed, const int *nbr, double *epot, double *f,
+                            double *wpot, const int *mask, double *epa, double *wpa) {
+  if (!epot || !f || !wpot || nat < 0 || natloc < 0 || natloc > nat ||
+      (nat > 0 && (!r || !Z || !seed))) {
+    set_error("energy_and_forces_ghost: invalid arguments");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (pot.kind == kEAM) {
+    set_error("energy_and_forces_ghost: ghost-atom lists are supported for the bond-order "
+              "potentials");
+    return GB_ERROR_ARGUMENT;
+  }
+  cudaStream_t s = pot_stream(pot);
+  Neighbors &nl = pot.gnl;
+  // list: CSR offsets (host copy for the sizes), entries, zero shifts
+  std::vector<int> hseed(nat + 1, 0);
+  if (is_device_ptr(seed))
+    GB_CUDA(cudaMemcpy(hseed.data(), seed, sizeof(int) * (nat + 1), cudaMemcpyDeviceToHost));
+  else
+    std::memcpy(hseed.data(), seed, sizeof(int) * (nat + 1));
+  const int64_t n = hseed[nat];
+  int maxz = 0;
+  for (int i = 0; i < nat; i++) {
+    if (hseed[i + 1] < hseed[i] || hseed[0] != 0) {
+      set_error("energy_and_forces_ghost: seed must be non-decreasing CSR offsets from 0");
+      return GB_ERROR_ARGUMENT;
+    }
+    maxz = std::max(maxz, hseed[i + 1] - hseed[i]);
+  }
+  if (n > 0 && !nbr) {
+    set_error("energy_and_forces_ghost: neighbor array missing");
+    return GB_ERROR_ARGUMENT;
+  }
+  GB_CHECK(nl.seed.ensure(sizeof(int) * (nat + 1)));
+  GB_CHECK(nl.nbr.ensure(sizeof(int) * std::max<int64_t>(n, 1)));
+  GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(n, 1)));
+  // status words of the reverse-index build (allocated by nl_build otherwise)
+  GB_CHECK(nl.stats.ensure(sizeof(int) * 8));
+  GB_CHECK(nl.hstats.ensure(sizeof(int) * 8));
+  GB_CUDA(cudaMemsetAsync(nl.stats.p, 0, sizeof(int) * 8, s));
+  GB_CUDA(cudaMemcpyAsync(nl.seed.p, hseed.data(), sizeof(int) * (nat + 1),
+                          cudaMemcpyHostToDevice, s));
+  if (n > 0) {
+    GB_CUDA(cudaMemcpyAsync(nl.nbr.p, nbr, sizeof(int) * n, cudaMemcpyDefault, s));
+    const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
+    fill_i32<<<blocks, 256, 0, s>>>(nl.shift.as<int>(), n, pack_shift(0, 0, 0));  // no image shifts
+    note_launch();
+  }
+  // positions
+  GB_CHECK(nl.pos4.ensure(sizeof(Pos4) * std::max(nat, 1)));
+  if (nat > 0) {
+    const double *rd = r;
+    if (!is_device_ptr(r)) {
+      GB_CHECK(pot.g_r.ensure(sizeof(double) * 3 * (size_t)nat));
+      GB_CUDA(cudaMemcpyAsync(pot.g_r.p, r, sizeof(double) * 3 * (size_t)nat,
+                              cudaMemcpyHostToDevice, s));
+      rd = pot.g_r.as<double>();
+    }
+    ghost_pos4<<<(nat + 127) / 128, 128, 0, s>>>(nat, rd, nl.pos4.as<Pos4>());
+    note_launch();
+  }
+  nl.nentries = n;
+  nl.maxz = maxz;
+  nl.valid = true;
+  nl.rev_valid = false;
+  nl.rev_pending = false;
+  nl.posff_valid = false;
+  nl.built_for = nullptr;  // (not a particles-bound list)
+  // element map from Z
+  {
+    std::vector<int> hz(std::max(nat, 1), 0);
+    if (nat > 0) {
+      if (is_device_ptr(Z))
+        GB_CUDA(cudaMemcpy(hz.data(), Z, sizeof(int) * nat, cudaMemcpyDeviceToHost));
+      else
+        std::memcpy(hz.data(), Z, sizeof(int) * nat);
+    }
+    const int nel = pot_nel(pot);
+    std::vector<int> el(std::max(nat, 1), -1);
+    for (int i = 0; i < nat; i++)
+      for (int q = 0; q < nel; q++)
+        if (hz[i] == pot_Z(pot, q)) el[i] = q;
+    GB_CHECK(pot.el.ensure(sizeof(int) * el.size()));
+    GB_CUDA(cudaMemcpyAsync(pot.el.p, el.data(), sizeof(int) * el.size(), cudaMemcpyHostToDevice,
+                            s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    pot.el_for = nullptr;  // the map belongs to this call
+  }
+  Stage sf, sepa, swpa;
+  GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, s, sf));
+  GB_CHECK(stage_in(epa, nat, pot.out_epa, s, sepa));
+  GB_CHECK(stage_in(wpa, 9 * (size_t)nat, pot.out_wpa, s, swpa));
+  Outputs o;
+  o.f = sf.dev;
+  o.epot_per_at = sepa.dev;
+  o.wpot_per_at = swpa.dev;
+  if (mask) {
+    if (is_device_ptr(mask)) {
+      o.mask = mask;
+    } else {
+      GB_CHECK(pot.mask_d.ensure(sizeof(int) * std::max(nat, 1)));
+      if (nat)
+        GB_CUDA(cudaMemcpyAsync(pot.mask_d.p, mask, sizeof(int) * nat, cudaMemcpyHostToDevice, s));
+      o.mask = pot.mask_d.as<int>();
+    }
+  }
+  GB_CHECK(pot.red.ensure(sizeof(double) * 16));
+  o.red = pot.red.as<double>();
+  o.status = reinterpret_cast<int *>(o.red + 12);
+  GB_CUDA(cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s));
+  // the ghosts' own entries carry no bond terms: start every entry from zero
+  const int64_t nb = std::max<int64_t>(n, 1);
+  const bool want_wat = wpa != nullptr;
+  GB_CHECK(pot.bond_G.ensure(sizeof(double) * 3 * nb));
+  GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
+  GB_CUDA(cudaMemsetAsync(pot.bond_G.p, 0, sizeof(double) * 3 * nb, s));
+  GB_CUDA(cudaMemsetAsync(pot.bond_e.p, 0, sizeof(double) * nb, s));
+  if (want_wat) {
+    GB_CHECK(pot.bond_w.ensure(sizeof(double) * 9 * nb));
+    GB_CUDA(cudaMemsetAsync(pot.bond_w.p, 0, sizeof(double) * 9 * nb, s));
+  }
+  BopSystem sys;
+  sys.nat = natloc;
+  sys.nat_all = nat;
+  if (pot.precision == GB_PRECISION_MIXED) nl.want_posff = true;
+  GB_CHECK(bop_run(pot, sys, nl, o, want_wat, false));
+  GB_CHECK(stage_out(sf, s));
+  GB_CHECK(stage_out(sepa, s));
+  GB_CHECK(stage_out(swpa, s));
+  GB_CHECK(pot.hred.ensure(sizeof(double) * 16));
+  double *hr = pot.hred.as<double>();
+  GB_CUDA(cudaMemcpyAsync(hr, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  GB_CUDA(cudaGetLastError());
+  const int st = reinterpret_cast<const int *>(hr + 12)[0];
+  pot.last_status = st;
+  pot.last_bonds = n;
+  if (st & 2) {
+    set_error("Internal error: bond-order tile plan mismatch.");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  if (st & 4) {
+    set_error("Internal neighbor list exhausted: an atom has more bonds after screening than "
+              "the screened kernel supports (32).");
+    return GB_ERROR_CAPACITY;
+  }
+  if (is_device_ptr(epot)) {
+    GB_CUDA(cudaMemcpy(epot, hr, sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    *epot = hr[0];
+  }
+  if (is_device_ptr(wpot)) {
+    double w[9];
+    GB_CUDA(cudaMemcpy(w, wpot, sizeof(w), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < 9; q++) w[q] += hr[1 + q];
+    GB_CUDA(cudaMemcpy(wpot, w, sizeof(w), cudaMemcpyHostToDevice));
+  } else {
+    for (int q = 0; q < 9; q++) wpot[q] += hr[1 + q];
+  }
+  return 0;
+}
+
 }  // namespace
 }  // namespace gb
 
@@ -578,6 +764,19 @@ double gb_potential_get_cutoff(const gb_potential_t *h) {
 int gb_potential_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl, int *ierror) {
   clear_error();
   int rc = (h && p && nl) ? bind_to(h->pot, p->p, nl->nl) : GB_ERROR_ARGUMENT;
+  if (ierror) *ierror = rc;
+  return rc;
+}
+
+int gb_potential_energy_and_forces_ghost(gb_potential_t *h, int nat, int natloc,
+                                         const double *r, const int *Z, const int *seed,
+                                         const int *nbr, double *epot, double *f, double *wpot,
+                                         const int *mask, double *epot_per_at,
+                                         double *wpot_per_at, int *ierror) {
+  clear_error();
+  int rc = h ? energy_and_forces_ghost(h->pot, nat, natloc, r, Z, seed, nbr, epot, f, wpot, mask,
+                                       epot_per_at, wpot_per_at)
+             : GB_ERROR_ARGUMENT;
   if (ierror) *ierror = rc;
   return rc;
 }

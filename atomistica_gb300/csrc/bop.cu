@@ -749,6 +749,7 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
                 bool want_wat, bool want_pb) {
   cudaStream_t s = pot.stream;
   const int nat = sys.nat;
+  const int nat_all = sys.nat_all > 0 ? sys.nat_all : nat;
   if (sys.tile_atom0) {
     set_error("batches support the non-screened bond-order potentials");
     return GB_ERROR_ARGUMENT;
@@ -761,7 +762,7 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
     GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
     return 0;
   }
-  GB_CHECK(neighbors_build_reverse(nl, nat, s, true));
+  GB_CHECK(neighbors_build_reverse(nl, nat_all, s, true));
   const int64_t nb = std::max<int64_t>(nl.nentries, 1);
   GB_CHECK(pot.bond_G.ensure(sizeof(double) * 3 * nb));
   GB_CHECK(pot.bond_e.ensure(sizeof(double) * nb));
@@ -796,8 +797,9 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
                         want_wat, want_pb, s));
   }
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
-  GB_CHECK(launch_gather(false, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
-                         args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
+  GB_CHECK(launch_gather(false, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
+                         args.ebond, args.wbond, o.f, o.epot_per_at,
+                         want_wat ? o.wpot_per_at : nullptr, s));
   GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(blocks) + 64));
   GB_CHECK(reduce_partials(args.tile_part, blocks, 10, o.red, pot.red_stage.as<double>(), s));
   pot.tile_atoms = 1;
@@ -812,6 +814,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   if (pot.screened) return bop_run_scr(pot, sys, nl, o, want_wat, want_pb);
   cudaStream_t s = pot.stream;
   const int nat = sys.nat;
+  const int nat_all = sys.nat_all > 0 ? sys.nat_all : nat;
   const bool batch = sys.tile_atom0 != nullptr;
   if (nat == 0) {
     GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
@@ -819,7 +822,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
       GB_CUDA(cudaMemsetAsync(sys.red_seg, 0, sizeof(double) * 10 * sys.nseg, s));
     return 0;
   }
-  GB_CHECK(neighbors_build_reverse(nl, nat, s, false));  // checked after the plan read-back
+  GB_CHECK(neighbors_build_reverse(nl, nat_all, s, false));  // checked after the plan read-back
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
   // Atoms per tile: largest power of two <= kMaxApt whose worst tile fits.
   const int maxz = std::max(nl.maxz, 1);
@@ -897,8 +900,8 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   int *status = o.status;
   int rc, rows = ntiles;
   if (mixed && !nl.posff_valid) {
-    GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * (size_t)nat));
-    bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, args.pos, nl.posff.as<float4>());
+    GB_CHECK(nl.posff.ensure(sizeof(float4) * 2 * (size_t)nat_all));
+    bop_posff<<<(nat_all + 127) / 128, 128, 0, s>>>(nat_all, args.pos, nl.posff.as<float4>());
     note_launch();
     nl.posff_valid = true;
   }
@@ -919,8 +922,9 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   }
   GB_CHECK(rc);
   if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[1], s));
-  GB_CHECK(launch_gather(mixed, nat, nl.seed.as<int>(), nl.rev.as<int>(), args.G, args.ebond,
-                         args.wbond, o.f, o.epot_per_at, want_wat ? o.wpot_per_at : nullptr, s));
+  GB_CHECK(launch_gather(mixed, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
+                         args.ebond, args.wbond, o.f, o.epot_per_at,
+                         want_wat ? o.wpot_per_at : nullptr, s));
   if (batch) {
     GB_CHECK(reduce_segments(args.tile_part, sys.seg, sys.nseg, sys.red_seg, s));
     GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));

@@ -82,6 +82,10 @@ struct Potential {
   DevBuf atom_dF;
   DevBuf red_stage;  // first-stage sums of the tile partials
   DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
+  // Ghost-atom calls (a caller's list over local + ghost atoms, no image
+  // shifts): the list, positions and element map live here.
+  Neighbors gnl;
+  DevBuf g_r;
   HostBuf hred;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t kev[2] = {nullptr, nullptr};  // around the dominant force kernel
@@ -126,7 +130,8 @@ int reduce_segments(const double *part, const int *seg, int nseg, double *out, c
 // across structures) carry their structure's cell and whose energy/virial sums
 // go per structure into red_seg (nseg x 10: energy, virial).
 struct BopSystem {
-  int nat = 0;
+  int nat = 0;      // atoms whose bonds are computed (the tiles)
+  int nat_all = 0;  // atoms of the list, forces gathered for all (ghost atoms; 0: nat)
   double A[3][3] = {{0}};
   const int *tile_atom0 = nullptr;   // device, ntiles + 1
   const int *tile_struct = nullptr;  // device, ntiles

@@ -291,6 +291,10 @@ class _Potential:
         self._L.gb_potential_last_timing(self._h, t)
         return tuple(t)
 
+    def energy_and_forces_ghost(self, r, Z, seed, nbr, natloc, **kw):
+        """The LAMMPS contract: see gb_potential_energy_and_forces_ghost."""
+        return _ghost_call(self, r, Z, seed, nbr, natloc, **kw)
+
     def set_tile_atoms(self, atoms):
         """Atoms per bond-order tile (power of two <= 64; 0: automatic)."""
         check(self._L.gb_potential_set_tile_atoms(self._h, int(atoms)), "set_tile_atoms")
@@ -367,6 +371,37 @@ class _Potential:
             if flag is not None:
                 res.append(out.get(k) if flag else None)
         return tuple(res)
+
+
+def _ghost_call(pot, r, Z, seed, nbr, natloc, forces=None, mask=None, epot_per_at=False,
+                wpot_per_at=False):
+    """energy_and_forces on a caller's list over local + ghost atoms (the
+    LAMMPS contract): returns (epot, forces (nat,3), wpot, [epot_per_at],
+    [wpot_per_at]); bonds of the first natloc atoms, forces on all."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    nat = len(r)
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    seed = np.ascontiguousarray(seed, dtype=np.int32)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    f = np.zeros((nat, 3)) if forces is None else forces
+    epot = ctypes.c_double(0.0)
+    wpot = np.zeros((3, 3), order="F")  # (layouts as energy_and_forces)
+    epa = np.zeros(nat) if epot_per_at else None
+    wpa = np.zeros((nat, 3, 3)) if wpot_per_at else None
+    m = None if mask is None else np.ascontiguousarray(np.asarray(mask).astype(np.int32))
+    err = ctypes.c_int(0)
+    ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+    check(pot._L.gb_potential_energy_and_forces_ghost(
+        pot._h, nat, int(natloc), r.ctypes.data, Z.ctypes.data, seed.ctypes.data,
+        nbr.ctypes.data if len(nbr) else None, ctypes.byref(epot), f.ctypes.data,
+        wpot.ctypes.data, ptr(m), ptr(epa), ptr(wpa), ctypes.byref(err)),
+        "energy_and_forces_ghost")
+    out = [epot.value, f, np.ascontiguousarray(wpot)]
+    if epot_per_at:
+        out.append(epa)
+    if wpot_per_at:
+        out.append(wpa)
+    return tuple(out)
 
 
 class Tersoff(_Potential):

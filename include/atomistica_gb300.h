@@ -184,6 +184,20 @@ double gb_potential_get_cutoff(const gb_potential_t *pot);
 int gb_potential_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
                          int *ierror);
 
+/* The LAMMPS contract (pair_atomistica.cpp:386-545, bop_kernel.f90:577-597
+ * under LAMMPS) for the bond-order potentials: nat = local + ghost atoms with
+ * explicit positions r (nat,3) and atomic numbers Z (nat), a full symmetric
+ * neighbour list over all of them without image shifts as 0-based CSR
+ * (seed[nat+1], nbr[seed[nat]]), bonds computed for the first natloc atoms.
+ * f (nat,3), wpot and the optional epot_per_at (nat) / wpot_per_at (nat,3,3)
+ * are accumulated into for all nat atoms (the caller sums ghost
+ * contributions back onto their owners); epot is set to the local atoms'
+ * share.  Host or device pointers. */
+int gb_potential_energy_and_forces_ghost(gb_potential_t *pot, int nat, int natloc,
+                                         const double *r, const int *Z, const int *seed,
+                                         const int *nbr, double *epot, double *f, double *wpot,
+                                         const int *mask, double *epot_per_at,
+                                         double *wpot_per_at, int *ierror);
 /* python_<mod>_energy_and_forces (gen_factory.py:239-356 -> COMPUTE_FUNC,
  * default_compute_func.f90:25-100; tabulated_alloy_eam.f90:360-415).
  * q (charges) is accepted and ignored, as by these potentials. */

@@ -574,7 +574,11 @@ struct BopOut {
 // neighbour-list slot (the reference's nbb).
 template <class Fn>
 int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int *el,
-               const NList &nl, const int *mask, const BopOut &o, int nthreads) {
+               const NList &nl, const int *mask, const BopOut &o, int nthreads,
+               int natloc = -1) {
+  // natloc < nat: the LAMMPS build, bonds of the first natloc atoms only
+  // (bop_kernel.f90:562, 1075 loop i = 1, natloc)
+  if (natloc < 0) natloc = nat;
   const int nel = fn.nel();
   const int npairs = nel * (nel + 1) / 2;
   std::vector<TrigOff> cut_in(npairs);
@@ -594,7 +598,7 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
   std::vector<int64_t> neb_seed(nat + 1, 0);
   std::vector<std::vector<Bond>> bonds_of(nat);
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
-  for (int i = 0; i < nat; i++) {
+  for (int i = 0; i < natloc; i++) {
     const int eli = el[i];
     if (eli < 0) continue;
     for (int64_t jn = nl.seed[i]; jn < nl.seed[i + 1]; jn++) {
@@ -660,7 +664,7 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
     double wpot[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     std::vector<double> dbidk(3 * (size_t)std::max(nebmax, 1));
 #pragma omp for schedule(dynamic, 64)
-    for (int i = 0; i < nat; i++) {
+    for (int i = 0; i < natloc; i++) {
       const int eli = el[i];
       if (eli < 0) continue;
       double fi[3] = {0, 0, 0};
@@ -830,7 +834,8 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
 template <class Fn>
 int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double *r,
                    const Box &box, const int *el, const NList &nl, const int *mask,
-                   const BopOut &o, int nthreads) {
+                   const BopOut &o, int nthreads, int natloc = -1) {
+  if (natloc < 0) natloc = nat;
   const int nel = fn.nel();
   const int npairs = nel * (nel + 1) / 2;
   std::vector<ExpCutoff> cut_in(npairs), cut_out(npairs), cut_bo(npairs);
@@ -880,7 +885,7 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
   std::vector<std::vector<ScrEntry>> scr_of(nat);
   // Pass 1.
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
-  for (int i = 0; i < nat; i++) {
+  for (int i = 0; i < natloc; i++) {
     const int eli = el[i];
     if (eli < 0) continue;
     std::vector<Bond> &bonds = bonds_of[i];
@@ -1058,7 +1063,7 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
     double wpot[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     std::vector<double> dbidk(3 * (size_t)std::max(nebmax, 1)), zfaci(std::max(nebmax, 1));
 #pragma omp for schedule(dynamic, 64)
-    for (int i = 0; i < nat; i++) {
+    for (int i = 0; i < natloc; i++) {
       const int eli = el[i];
       if (eli < 0) continue;
       double fi[3] = {0, 0, 0};
@@ -1208,7 +1213,7 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
     }
     // Screening forces through the bond-order cutoff (:1571-1611).
 #pragma omp for schedule(dynamic, 64)
-    for (int i = 0; i < nat; i++) {
+    for (int i = 0; i < natloc; i++) {
       if (el[i] < 0) continue;
       double fi[3] = {0, 0, 0};
       const std::vector<Bond> &bi = bonds_of[i];
@@ -1835,6 +1840,38 @@ int orc_kumagai_scr_compute(const orc_kumagai_params *p, const orc_scr_params *s
   BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
   return bop_kernel_scr(KumagaiFn(*p), *sp, nat, r, box, el.data(), nl, mask, o,
                         resolve_threads(nthreads));
+}
+
+// The LAMMPS contract (bop_kernel.f90 under LAMMPS): nat = local + ghost
+// atoms with explicit positions, a shift-free list over all of them, bonds of
+// the first natloc atoms; kind 0 Tersoff, 1 Kumagai; sp != NULL: screened.
+int orc_bop_ghost(int kind, const void *params, const orc_scr_params *sp, int nat, int natloc,
+                  const double *r, const int *Z, const int64_t *seed, const int *nbr,
+                  const int *mask, double *epot, double *f, double *wpot, double *epot_per_at,
+                  double *wpot_per_at, int nthreads) {
+  const double eye[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  const int nopbc[3] = {0, 0, 0};
+  Box box;
+  if (make_box(eye, nopbc, box) != 0) return -1;
+  const int64_t n = seed[nat];
+  std::vector<int> dc(3 * (size_t)std::max<int64_t>(n, 1), 0);
+  NList nl;
+  nl_from_arrays(nat, seed, nbr, dc.data(), nl);
+  *epot = 0.0;
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  std::vector<int> el;
+  const int nt = resolve_threads(nthreads);
+  if (kind == 0) {
+    const orc_tersoff_params *p = static_cast<const orc_tersoff_params *>(params);
+    map_elements(nat, Z, p->nel, p->Z, el);
+    return sp ? bop_kernel_scr(TersoffFn(*p), *sp, nat, r, box, el.data(), nl, mask, o, nt,
+                               natloc)
+              : bop_kernel(TersoffFn(*p), nat, r, box, el.data(), nl, mask, o, nt, natloc);
+  }
+  const orc_kumagai_params *p = static_cast<const orc_kumagai_params *>(params);
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return sp ? bop_kernel_scr(KumagaiFn(*p), *sp, nat, r, box, el.data(), nl, mask, o, nt, natloc)
+            : bop_kernel(KumagaiFn(*p), nat, r, box, el.data(), nl, mask, o, nt, natloc);
 }
 
 struct orc_eam {

@@ -149,6 +149,9 @@ def lib():
         for name in ("orc_tersoff_scr_compute", "orc_kumagai_scr_compute"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = [_P] + cargs
+        L.orc_bop_ghost.restype = ctypes.c_int
+        L.orc_bop_ghost.argtypes = [ctypes.c_int, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P,
+                                    _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
         L.orc_eam_load.restype = _P
         L.orc_eam_load.argtypes = [ctypes.c_char_p, _P]
         L.orc_eam_free.argtypes = [_P]
@@ -241,8 +244,10 @@ def bop_cutoff(kind, params, s):
     """Interaction range requested by bind_to for the elements of s."""
     L = lib()
     _, _, _, Z = _geom(s)
-    p = tersoff_params(params) if kind == "tersoff" else kumagai_params(params)
-    return getattr(L, "orc_%s_cutoff" % kind)(ctypes.byref(p), len(Z), _ptr(Z))
+    base, scr = _kind(kind)
+    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    pre = (ctypes.byref(p), ctypes.byref(scr_params(params))) if scr else (ctypes.byref(p),)
+    return getattr(L, "orc_%s_cutoff" % kind)(*pre, len(Z), _ptr(Z))
 
 
 def bop(kind, params, s, nl=None, mask=None, per_at=True, per_bond=False, nthreads=0):
@@ -275,6 +280,34 @@ def bop(kind, params, s, nl=None, mask=None, per_at=True, per_bond=False, nthrea
     out["epot"] = epot.value
     out["wpot"] = np.ascontiguousarray(out["wpot"])
     out["nl"] = nl
+    return out
+
+
+def bop_ghost(kind, params, r, Z, seed, nbr, natloc, mask=None, nthreads=0):
+    """The LAMMPS contract: explicit local + ghost positions, a shift-free
+    CSR list over all atoms, bonds of the first natloc atoms; returns epot,
+    f, wpot, epot_per_at, wpot_per_at for all atoms."""
+    L = lib()
+    base, scr = _kind(kind)
+    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    sp = scr_params(params) if scr else None
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    nat = len(r)
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    seed = np.ascontiguousarray(seed, dtype=np.int64)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32) if len(nbr) else np.zeros(1, np.int32)
+    out = _alloc_outputs(nat, 0, True, False)
+    epot = ctypes.c_double(0.0)
+    m = None if mask is None else np.ascontiguousarray(np.asarray(mask).astype(np.int32))
+    rc = L.orc_bop_ghost(0 if base == "tersoff" else 1, ctypes.byref(p),
+                         ctypes.byref(sp) if sp is not None else None, nat, int(natloc),
+                         _ptr(r), _ptr(Z), _ptr(seed), _ptr(nbr), _ptr(m), ctypes.byref(epot),
+                         _ptr(out["f"]), _ptr(out["wpot"]), _ptr(out["epot_per_at"]),
+                         _ptr(out["wpot_per_at"]), int(nthreads))
+    if rc != 0:
+        raise RuntimeError("oracle ghost kernel failed: %d" % rc)
+    out["epot"] = epot.value
+    out["wpot"] = np.ascontiguousarray(out["wpot"])
     return out
 
 

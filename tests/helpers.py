@@ -117,3 +117,43 @@ def sorted_triples(seed, j, dc):
     i = np.repeat(np.arange(len(seed) - 1), np.diff(seed))
     t = np.column_stack([i, j, dc]).astype(np.int64)
     return t[np.lexsort(t.T[::-1])]
+
+
+def ghost_system(s, cutoff):
+    """(r_all, Z_all, owner, seed, nbr): local atoms first, then the images
+    within 2 cutoff of the (orthorhombic) box; CSR list within cutoff over
+    all atoms, brute force in chunks."""
+    L = np.diag(s.cell)
+    assert np.allclose(s.cell, np.diag(L))
+    w = 2.0 * cutoff
+    r = s.positions % L
+    rs, own = [r], [np.arange(len(r))]
+    m = int(np.ceil(w / L.min()))
+    for n in np.ndindex(2 * m + 1, 2 * m + 1, 2 * m + 1):
+        n = np.array(n) - m
+        if not n.any():
+            continue
+        img = r + n * L
+        keep = np.all((img > -w) & (img < L + w), axis=1)
+        rs.append(img[keep])
+        own.append(np.nonzero(keep)[0])
+    r_all = np.concatenate(rs)
+    owner = np.concatenate(own)
+    nat = len(r_all)
+    seed = np.zeros(nat + 1, dtype=np.int32)
+    nbrs = []
+    for a in range(0, nat, 512):
+        d = r_all[a:a + 512, None, :] - r_all[None, :, :]
+        d2 = np.einsum("ijk,ijk->ij", d, d)
+        for q in range(d2.shape[0]):
+            js = np.nonzero((d2[q] < cutoff * cutoff) & (np.arange(nat) != a + q))[0]
+            nbrs.append(js.astype(np.int32))
+            seed[a + q + 1] = seed[a + q] + len(js)
+    Z = np.asarray(s.numbers, dtype=np.int32)[owner]
+    return r_all, Z, owner, seed, np.concatenate(nbrs) if nbrs else np.zeros(0, np.int32)
+
+
+def fold(owner, x, n):
+    out = np.zeros((n,) + x.shape[1:])
+    np.add.at(out, owner, x)
+    return out

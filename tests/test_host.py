@@ -107,3 +107,25 @@ def test_random_packing_generator():
         r2 = np.einsum("ijsk,ijsk->ijs", d, d)
         r2[np.arange(nat), np.arange(nat), 13] = np.inf  # self, zero shift
         assert np.sqrt(r2.min()) >= 2.0
+
+
+@pytest.mark.parametrize("kind", ["tersoff", "kumagai", "tersoff_scr"])
+def test_oracle_ghost_contract(kind):
+    # bonds of the local atoms with explicit ghost images (the LAMMPS build)
+    # equal the periodic evaluation; the screened loops depend on the list
+    # order (early exit), so there the agreement is to 1e-6 eV
+    import oracle
+    from helpers import KUMAGAI, TERSOFF, TERSOFF_SCR, fold, ghost_system, rattled_diamond
+    params = {"tersoff": TERSOFF, "kumagai": KUMAGAI, "tersoff_scr": TERSOFF_SCR}[kind]
+    s = rattled_diamond("Si", 5.431, (2, 2, 2), 0.25, 51)
+    ref = oracle.bop(kind, params, s)
+    cut = oracle.bop_cutoff(kind, params, s)
+    r, Z, owner, seed, nbr = ghost_system(s, cut)
+    g = oracle.bop_ghost(kind, params, r, Z, seed, nbr, len(s))
+    n = len(s)
+    tol = 1e-6 if kind == "tersoff_scr" else 1e-10
+    assert abs(g["epot"] - ref["epot"]) < tol * n
+    assert np.max(np.abs(fold(owner, g["f"], n) - ref["f"])) < (1e-5 if kind == "tersoff_scr"
+                                                                 else 1e-9)
+    assert np.max(np.abs(fold(owner, g["epot_per_at"], n) - ref["epot_per_at"])) < \
+        (1e-5 if kind == "tersoff_scr" else 1e-9)
