@@ -68,6 +68,9 @@ SIGNATURES = [
     ("gb_random_packing", _I, [_I, _P, ctypes.c_double, ctypes.c_uint64, ctypes.c_int64, _P]),
     ("gb_batch_last_info", _I, [_P, _P]),
     ("gb_batch_energy_and_forces", _I, [_P, _P, _P, _P, _P]),
+    ("gb_batch_md_set_state", _I, [_P, _P, _P]),
+    ("gb_batch_md_run", _I, [_P, _P, ctypes.c_double, _I, _P, _P]),
+    ("gb_batch_md_get_state", _I, [_P, _P, _P, _P]),
     ("gb_batch_tersoff_tangent", _I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     ("gb_potential_last_timing", _I, [_P, _P]),
     ("gb_potential_last_stats", _I, [_P, _P]),

@@ -140,6 +140,44 @@ Batch::~Batch() {
 
 namespace {
 
+// Velocity Verlet (verlet.f90:100-235): v += 0.5 f / m dt; r += v dt
+// (step1) ... forces ... v += 0.5 f / m dt (step2).  Atoms with m <= 0 do
+// not move (the reference's group filter p%g(i) > 0).
+__global__ void md_kick_drift(int nat, double *__restrict__ r, double *__restrict__ v,
+                              const double *__restrict__ f, const double *__restrict__ m,
+                              double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const double mi = m[i];
+  if (!(mi > 0.0)) return;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const double vv = v[3 * (size_t)i + c] + 0.5 * f[3 * (size_t)i + c] / mi * dt;
+    v[3 * (size_t)i + c] = vv;
+    r[3 * (size_t)i + c] = r[3 * (size_t)i + c] + vv * dt;
+  }
+}
+
+// step2 with the new forces f, which also become the stored forces fout.
+// nls / pst (captured steps): the list build's and the force kernels' status
+// words; a step whose list or tile plan overflowed leaves v and fout as they
+// are (the host redoes the evaluation).
+__global__ void md_kick(int nat, double *__restrict__ v, const double *__restrict__ f,
+                        const double *__restrict__ m, double dt, double *__restrict__ fout,
+                        const int *__restrict__ nls, const int *__restrict__ pst, int cap) {
+  if (nls && !(nls[0] <= cap && (nls[1] & 3) == 0 && (nls[4] & 4) == 0 && (pst[0] & 2) == 0))
+    return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const double mi = m[i];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const double fc = f[3 * (size_t)i + c];
+    if (mi > 0.0) v[3 * (size_t)i + c] = v[3 * (size_t)i + c] + 0.5 * fc / mi * dt;
+    fout[3 * (size_t)i + c] = fc;
+  }
+}
+
 void drop_graph(Batch &b) {
   if (b.graph_exec) cudaGraphExecDestroy(b.graph_exec);
   if (b.graph) cudaGraphDestroy(b.graph);
@@ -154,7 +192,8 @@ void drop_graph(Batch &b) {
 std::vector<const void *> graph_buffers(const Batch &b, const Potential &pot) {
   const Neighbors &nl = b.nl;
   return {b.r.p, b.sid.p, b.bps.p, b.Acells.p, b.Acells_ff.p, b.tiles.p, b.red_seg.p, b.el.p,
-          b.gf.p, b.hseg.p, nl.pos4.p, nl.posff.p, nl.atom_cell.p, nl.atom_wrap.p,
+          b.gf.p, b.hseg.p, b.md_v.p, b.md_m.p, b.md_f.p, nl.pos4.p, nl.posff.p, nl.atom_cell.p,
+          nl.atom_wrap.p,
           nl.cell_count.p, nl.cell_start.p, nl.cell_atoms.p, nl.counts.p, nl.spos.p, nl.swrap.p,
           nl.seed.p, nl.nbr.p, nl.shift.p, nl.rev.p, nl.stage.p, nl.scan_tmp.p, nl.stats.p,
           nl.hstats.p, pot.bond_G.p, pot.bond_e.p, pot.tile_part.p, pot.red.p, pot.hred.p};
@@ -270,7 +309,9 @@ int batch_choose_apt(Batch &b, Potential &pot, cudaStream_t s) {
 
 // Captures the whole evaluation (list build included) after an eager one
 // has sized everything; failures leave the eager path in use.
-void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
+// kind 0: one evaluation into gf; kind 1: a whole velocity-Verlet step of
+// time step dt (step1, gf = 0, evaluation, checked step2 into md_v / md_f).
+void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, double dt = 0.0) {
   drop_graph(b);
   const int cap = b.nl.stage_cap;
   if (cap <= 0 || b.nat == 0) return;
@@ -323,9 +364,24 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
     return;
   }
   BinParams dummy{};
-  int rc = nl_build(nl, b.nat, b.r.as<double>(), dummy, b.bps.as<BinParams>(), b.sid.as<int>(),
-                    b.ncells, s, true);
+  const int T = 256, nbk = (b.nat + T - 1) / T;
+  int rc = 0;
+  if (kind == 1) {
+    md_kick_drift<<<nbk, T, 0, s>>>(b.nat, b.r.as<double>(), b.md_v.as<double>(),
+                                    b.md_f.as<double>(), b.md_m.as<double>(), dt);
+    note_launch();
+    if (cudaMemsetAsync(b.gf.p, 0, sizeof(double) * 3 * b.nat, s) != cudaSuccess) rc = -1;
+  }
+  if (rc == 0)
+    rc = nl_build(nl, b.nat, b.r.as<double>(), dummy, b.bps.as<BinParams>(), b.sid.as<int>(),
+                  b.ncells, s, true);
   if (rc == 0) rc = batch_forces(b, pot, b.gf.as<double>(), s, sys);
+  if (rc == 0 && kind == 1) {
+    md_kick<<<nbk, T, 0, s>>>(b.nat, b.md_v.as<double>(), b.gf.as<double>(), b.md_m.as<double>(),
+                              dt, b.md_f.as<double>(), nl.stats.as<int>(),
+                              reinterpret_cast<const int *>(pot.red.as<double>() + 12), cap);
+    note_launch();
+  }
   const cudaError_t ce = cudaStreamEndCapture(s, &g);
   note_launch(-(int)(gb_kernel_launches() - launches0));  // captured, not run
   nl.rev_valid = rev_valid0;
@@ -366,12 +422,15 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s) {
   b.graph_apt = apt;
   b.graph_cap = cap;
   b.graph_ncells = b.ncells;
+  b.graph_kind = kind;
+  b.graph_dt = dt;
   b.graph_bufs = graph_buffers(b, pot);
   (void)mixed;
 }
 
-bool graph_current(const Batch &b, const Potential &pot) {
-  return b.graph_exec && b.graph_geom == b.geom_rev && b.graph_pot == &pot &&
+bool graph_current(const Batch &b, const Potential &pot, int kind = 0, double dt = 0.0) {
+  return b.graph_exec && b.graph_kind == kind && (kind == 0 || b.graph_dt == dt) &&
+         b.graph_geom == b.geom_rev && b.graph_pot == &pot &&
          b.graph_prec == pot.precision && b.graph_apt == b.tiles_apt &&
          b.graph_ncells == b.ncells &&
          b.graph_bufs == graph_buffers(b, pot);
@@ -409,51 +468,37 @@ int batch_replay(Batch &b, Potential &pot, double *epot, double *f, double *wpot
   return 0;
 }
 
-}  // namespace
-
-int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, double *wpot) {
-  if (!epot || !f || !wpot) {
-    set_error("batch_energy_and_forces: epot, f and wpot are required");
-    return GB_ERROR_ARGUMENT;
-  }
+// Checks, stream order, elements, cutoff and binning of an evaluation.
+int batch_prepare(Batch &b, Potential &pot, cudaStream_t &s, double &cutoff) {
   if (pot.kind == kEAM || pot.screened) {
     set_error("batch_energy_and_forces: batches support the non-screened bond-order potentials");
     return GB_ERROR_ARGUMENT;
   }
-  b.info[0] = 0;
-  if (b.nstruct == 0) return 0;
   if (b.nat > 0 && !b.r.p) {
     set_error("batch_energy_and_forces: positions not set");
     return GB_ERROR_ARGUMENT;
   }
-  cudaStream_t s = pot_stream(pot);
+  s = pot_stream(pot);
   if (b.stream && b.stream != s) {
     GB_CUDA(cudaEventRecord(pot.ev[3], b.stream));
     GB_CUDA(cudaStreamWaitEvent(s, pot.ev[3], 0));
   }
   GB_CUDA(cudaEventRecord(pot.ev[0], s));
-  const bool mixed = pot.precision == GB_PRECISION_MIXED;
   GB_CHECK(batch_elements(b, pot, s));
-  const double cutoff = batch_cutoff(b, pot);
+  cutoff = batch_cutoff(b, pot);
   if (!(cutoff > 0.0)) {
     set_error("batch_energy_and_forces: no element of the batch is known to the potential");
     return GB_ERROR_ARGUMENT;
   }
   GB_CHECK(batch_binning(b, cutoff, s));
-  if (mixed) b.nl.want_posff = true;
+  if (pot.precision == GB_PRECISION_MIXED) b.nl.want_posff = true;
+  return 0;
+}
 
-  if (b.use_graph && graph_current(b, pot)) {
-    bool done = false;
-    GB_CHECK(batch_replay(b, pot, epot, f, wpot, s, done));
-    if (done) {
-      b.info[0] = 1;
-      b.info[1] = b.tiles_apt;
-      b.info[2] = b.graph_kernels;
-      return 0;
-    }
-  }
-
-  // Eager evaluation.
+// One evaluation without graphs: list (if the positions changed), tiles,
+// forces accumulated into f, energies set / virials accumulated.
+int batch_eager(Batch &b, Potential &pot, double *epot, double *f, double *wpot, cudaStream_t s,
+                double cutoff) {
   if (!(b.nl.valid && b.built_pos == b.pos_rev && b.nl.posff_valid == b.nl.want_posff)) {
     b.nl.valid = false;
     b.nl.rev_valid = false;
@@ -492,8 +537,139 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
   GB_CHECK(batch_finish(b, pot, epot, wpot));
   b.info[1] = b.tiles_apt;
   b.info[3] = b.tune_candidates;
+  return 0;
+}
+
+// Replays a captured velocity-Verlet step; ok = false when its list or tile
+// plan overflowed (positions and the first half kick are applied, the second
+// half kick is not: the caller redoes the evaluation).
+int batch_replay_md(Batch &b, Potential &pot, cudaStream_t s, bool &ok) {
+  GB_CUDA(cudaGraphLaunch(b.graph_exec, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  note_launch(b.graph_kernels);
+  b.pos_rev++;  // the step moved the atoms
+  const int *hs = b.nl.hstats.as<int>();
+  const int *st = reinterpret_cast<const int *>(pot.hred.as<double>() + 12);
+  ok = hs[0] <= b.graph_cap && (hs[1] & (1 | 2)) == 0 && (hs[5] & 4) == 0 && (st[0] & 2) == 0;
+  if (!ok) {
+    drop_graph(b);
+    b.nl.valid = false;
+    return 0;
+  }
+  b.nl.nentries = hs[4];
+  b.nl.maxz = hs[0];
+  b.nl.valid = true;
+  b.nl.rev_valid = true;
+  b.nl.rev_pending = false;
+  b.nl.posff_valid = b.nl.want_posff;
+  b.built_pos = b.pos_rev;
+  b.md_f_pos = b.pos_rev;
+  return 0;
+}
+
+}  // namespace
+
+int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, double *wpot) {
+  if (!epot || !f || !wpot) {
+    set_error("batch_energy_and_forces: epot, f and wpot are required");
+    return GB_ERROR_ARGUMENT;
+  }
+  b.info[0] = 0;
+  if (b.nstruct == 0) return 0;
+  cudaStream_t s;
+  double cutoff;
+  GB_CHECK(batch_prepare(b, pot, s, cutoff));
+  if (b.use_graph && graph_current(b, pot)) {
+    bool done = false;
+    GB_CHECK(batch_replay(b, pot, epot, f, wpot, s, done));
+    if (done) {
+      b.info[0] = 1;
+      b.info[1] = b.tiles_apt;
+      b.info[2] = b.graph_kernels;
+      return 0;
+    }
+  }
+  GB_CHECK(batch_eager(b, pot, epot, f, wpot, s, cutoff));
   if (b.use_graph && !b.graph_failed && !graph_current(b, pot)) batch_capture(b, pot, s);
   b.info[2] = b.graph_kernels;
+  return 0;
+}
+
+// nsteps velocity-Verlet steps of time step dt; epot / wpot (per structure,
+// optional) of the last step.  With graphs on, a step after the first eager
+// one is captured whole and replayed.
+int batch_md_run(Batch &b, Potential &pot, double dt, int nsteps, double *epot, double *wpot) {
+  if (nsteps < 0 || !(dt == dt)) {
+    set_error("md_run: nsteps >= 0 and a finite dt are required");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (b.nstruct == 0 || b.nat == 0) return 0;
+  if (!b.md_v.p || !b.md_m.p) {
+    set_error("md_run: velocities and masses not set (gb_batch_md_set_state)");
+    return GB_ERROR_ARGUMENT;
+  }
+  cudaStream_t s;
+  double cutoff;
+  GB_CHECK(batch_prepare(b, pot, s, cutoff));
+  const size_t nf = 3 * (size_t)b.nat;
+  GB_CHECK(b.gf.ensure(sizeof(double) * nf));
+  GB_CHECK(b.md_f.ensure(sizeof(double) * nf));
+  b.md_e.assign(b.nstruct, 0.0);
+  b.md_w.assign(9 * (size_t)b.nstruct, 0.0);
+  const int T = 256, nbk = (b.nat + T - 1) / T;
+  auto eval_into_md_f = [&](bool kick) -> int {
+    // forces at the current positions into gf, then (kick) step2 and md_f
+    GB_CUDA(cudaMemsetAsync(b.gf.p, 0, sizeof(double) * nf, s));
+    std::fill(b.md_w.begin(), b.md_w.end(), 0.0);
+    GB_CHECK(batch_eager(b, pot, b.md_e.data(), b.gf.as<double>(), b.md_w.data(), s, cutoff));
+    if (kick) {
+      md_kick<<<nbk, T, 0, s>>>(b.nat, b.md_v.as<double>(), b.gf.as<double>(),
+                                b.md_m.as<double>(), dt, b.md_f.as<double>(), nullptr, nullptr, 0);
+      note_launch();
+    } else {
+      GB_CUDA(cudaMemcpyAsync(b.md_f.p, b.gf.p, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+    }
+    GB_CUDA(cudaStreamSynchronize(s));
+    GB_CUDA(cudaGetLastError());
+    b.md_f_pos = b.pos_rev;
+    return 0;
+  };
+  if (b.md_f_pos != b.pos_rev) GB_CHECK(eval_into_md_f(false));  // forces at the start
+  b.info[0] = 0;
+  for (int step = 0; step < nsteps; step++) {
+    if (b.use_graph && graph_current(b, pot, 1, dt)) {
+      bool ok = false;
+      GB_CHECK(batch_replay_md(b, pot, s, ok));
+      if (ok) {
+        std::fill(b.md_w.begin(), b.md_w.end(), 0.0);
+        GB_CHECK(batch_finish(b, pot, b.md_e.data(), b.md_w.data()));
+        b.info[0] = 1;
+        continue;
+      }
+      GB_CHECK(eval_into_md_f(true));  // an overflowed replay: the evaluation again
+      continue;
+    }
+    md_kick_drift<<<nbk, T, 0, s>>>(b.nat, b.r.as<double>(), b.md_v.as<double>(),
+                                    b.md_f.as<double>(), b.md_m.as<double>(), dt);
+    note_launch();
+    b.pos_rev++;
+    GB_CHECK(eval_into_md_f(true));
+    if (b.use_graph && !b.graph_failed) batch_capture(b, pot, s, 1, dt);
+  }
+  b.info[2] = b.graph_kernels;
+  if (epot) {
+    if (is_device_ptr(epot))
+      GB_CUDA(cudaMemcpy(epot, b.md_e.data(), sizeof(double) * b.nstruct, cudaMemcpyHostToDevice));
+    else
+      std::memcpy(epot, b.md_e.data(), sizeof(double) * b.nstruct);
+  }
+  if (wpot) {
+    if (is_device_ptr(wpot))
+      GB_CUDA(cudaMemcpy(wpot, b.md_w.data(), sizeof(double) * b.md_w.size(),
+                         cudaMemcpyHostToDevice));
+    else
+      std::memcpy(wpot, b.md_w.data(), sizeof(double) * b.md_w.size());
+  }
   return 0;
 }
 
@@ -626,6 +802,51 @@ int gb_batch_last_info(const gb_batch_t *h, int64_t *info) {
   if (!h || !info) return GB_ERROR_ARGUMENT;
   for (int k = 0; k < 4; k++) info[k] = h->b.info[k];
   return 0;
+}
+
+int gb_batch_md_set_state(gb_batch_t *h, const double *v, const double *m) {
+  clear_error();
+  if (!h || (h->b.nat > 0 && (!v || !m))) return GB_ERROR_ARGUMENT;
+  Batch &b = h->b;
+  const size_t n = (size_t)std::max(b.nat, 1);
+  GB_CHECK(b.md_v.ensure(sizeof(double) * 3 * n));
+  GB_CHECK(b.md_m.ensure(sizeof(double) * n));
+  if (b.nat > 0) {
+    cudaStream_t s = batch_stream(b);
+    GB_CUDA(cudaMemcpyAsync(b.md_v.p, v, sizeof(double) * 3 * b.nat, cudaMemcpyDefault, s));
+    GB_CUDA(cudaMemcpyAsync(b.md_m.p, m, sizeof(double) * b.nat, cudaMemcpyDefault, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+  }
+  b.md_f_pos = ~0ull;  // forces are recomputed at the next md_run
+  return 0;
+}
+
+int gb_batch_md_get_state(gb_batch_t *h, double *r, double *v, double *f) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  Batch &b = h->b;
+  if (b.nat == 0) return 0;
+  const size_t nb = sizeof(double) * 3 * b.nat;
+  if (r) GB_CUDA(cudaMemcpy(r, b.r.p, nb, cudaMemcpyDefault));
+  if (v) {
+    if (!b.md_v.p) return GB_ERROR_ARGUMENT;
+    GB_CUDA(cudaMemcpy(v, b.md_v.p, nb, cudaMemcpyDefault));
+  }
+  if (f) {
+    if (!b.md_f.p || b.md_f_pos != b.pos_rev) {
+      set_error("md_get_state: no forces at the current positions (run md_run first)");
+      return GB_ERROR_ARGUMENT;
+    }
+    GB_CUDA(cudaMemcpy(f, b.md_f.p, nb, cudaMemcpyDefault));
+  }
+  return 0;
+}
+
+int gb_batch_md_run(gb_batch_t *h, gb_potential_t *pot, double dt, int nsteps, double *epot,
+                    double *wpot) {
+  clear_error();
+  if (!h || !pot) return GB_ERROR_ARGUMENT;
+  return batch_md_run(h->b, pot->pot, dt, nsteps, epot, wpot);
 }
 
 int gb_batch_energy_and_forces(gb_batch_t *h, gb_potential_t *pot, double *epot, double *f,

@@ -47,6 +47,13 @@ struct Batch {
   const Potential *graph_pot = nullptr;
   int graph_prec = -1, graph_apt = 0, graph_kernels = 0;
   int graph_cap = 0, graph_ncells = 0;  // list capacity per atom, cells: baked into the graph
+  int graph_kind = 0;       // 0: one evaluation; 1: a velocity-Verlet step around it
+  double graph_dt = 0.0;
+  // Velocity Verlet (verlet.f90:100-235): velocities, masses and the forces
+  // at the current positions (valid while md_f_pos == pos_rev).
+  DevBuf md_v, md_m, md_f;
+  uint64_t md_f_pos = ~0ull;
+  std::vector<double> md_e, md_w;  // per-structure energies / virials of the last step
   std::vector<const void *> graph_bufs;
   DevBuf gf;  // forces accumulated by the graph
   int64_t info[4] = {0, 0, 0, 0};  // last call: replayed, atoms/tile, kernels in graph, tuned

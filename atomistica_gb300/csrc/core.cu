@@ -833,7 +833,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
   GB_CHECK(nl.seed.ensure(sizeof(int) * (nat + 1)));
   GB_CHECK(nl.stats.ensure(sizeof(int) * 8 + sizeof(int) * (size_t)(ncells + 1)));
   GB_CHECK(nl.hstats.ensure(sizeof(int) * 8));
-  int *status = nl.stats.as<int>();  // [0] maxz [1] flags [2] n_big [3] max |coordinate|
+  // [0] maxz [1] flags [2] n_big [3] max |coordinate| [4] reverse-index flags
+  int *status = nl.stats.as<int>();
   int *big_cells = status + 8;
   GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 8, stream));
   GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
@@ -1003,7 +1004,9 @@ int neighbors_update(Neighbors &nl, Particles &p, cudaStream_t stream) {
 int neighbors_build_reverse(Neighbors &nl, int nat, cudaStream_t stream, bool sync) {
   if (nl.rev_valid || nl.rev_pending) return sync ? neighbors_check_reverse(nl, stream) : 0;
   GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(nl.nentries, 1)));
-  int *status = nl.stats.as<int>();
+  // The symmetry flag goes to stats[4] (the kernels set bit 4 of their
+  // status[1]), so that the list build's own words stats[0..3] stay intact.
+  int *status = nl.stats.as<int>() + 3;
   GB_CUDA(cudaMemsetAsync(status + 1, 0, sizeof(int), stream));
   if (nat > 0) {
     if (nl.nentries > 24 * (int64_t)nat)  // long lists: a warp per atom

@@ -550,6 +550,31 @@ class Batch:
         self._r = keep
         check(self._L.gb_batch_set_positions(self._h, ptr), "batch_set_positions")
 
+    def md_set_state(self, velocities, masses):
+        """Velocities (total, 3) and masses (total,) for md_run (m <= 0
+        freezes an atom)."""
+        v = np.ascontiguousarray(velocities, dtype=np.float64)
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        check(self._L.gb_batch_md_set_state(self._h, v.ctypes.data, m.ctypes.data),
+              "batch_md_set_state")
+
+    def md_run(self, pot, dt, nsteps):
+        """nsteps velocity-Verlet steps (verlet.f90); (epot (nstruct,),
+        wpot (nstruct, 3, 3)) of the last step."""
+        e = np.zeros(len(self.nat))
+        w = np.zeros((len(self.nat), 3, 3))
+        check(self._L.gb_batch_md_run(self._h, pot._h, float(dt), int(nsteps), e.ctypes.data,
+                                      w.ctypes.data), "batch_md_run")
+        return e, w
+
+    def md_get_state(self):
+        """(positions, velocities, forces at the positions), each (total, 3)."""
+        n = int(self.offsets[-1]) if len(self.nat) else 0
+        r, v, f = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+        check(self._L.gb_batch_md_get_state(self._h, r.ctypes.data, v.ctypes.data,
+                                            f.ctypes.data), "batch_md_get_state")
+        return r, v, f
+
     def energy_and_forces(self, pot, forces=None):
         """(epot (nstruct,), forces (total, 3), wpot (nstruct, 3, 3)); forces
         (numpy or CUDA tensor) is accumulated into when given."""

@@ -302,6 +302,19 @@ int gb_batch_set_options(gb_batch_t *batch, int use_graph, int autotune);
  * tile, info[2] kernels in the captured graph (0: none), info[3] tile sizes
  * timed by the autotuner. */
 int gb_batch_last_info(const gb_batch_t *batch, int64_t *info);
+/* Velocity Verlet on the batch (src/standalone/verlet.f90:100-235):
+ * md_set_state sets velocities v (total atoms, 3) and masses m (total atoms;
+ * m <= 0 freezes an atom, the reference's group filter); md_run advances
+ * nsteps steps of dt (v += f dt / 2m; r += v dt; forces; v += f dt / 2m, in
+ * the caller's consistent units), writing epot[nstruct] / wpot (optional) of
+ * the last step; with use_graph a whole step (both kicks, the drift, the list
+ * build and the forces) is replayed as one CUDA graph.  md_get_state reads
+ * positions, velocities and the forces at the current positions (any may be
+ * NULL).  Host or device memory. */
+int gb_batch_md_set_state(gb_batch_t *batch, const double *v, const double *m);
+int gb_batch_md_run(gb_batch_t *batch, gb_potential_t *pot, double dt, int nsteps, double *epot,
+                    double *wpot);
+int gb_batch_md_get_state(gb_batch_t *batch, double *r, double *v, double *f);
 /* epot[nstruct] set; f (total atoms, 3) and wpot[nstruct][3][3] (each in the
  * layout of energy_and_forces' wpot) accumulated.  Host or device memory. */
 int gb_batch_energy_and_forces(gb_batch_t *batch, gb_potential_t *pot, double *epot, double *f,
