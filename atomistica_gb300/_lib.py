@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(HERE, "libatomistica_gb300.so")
 
 GB_PRECISION_FP64 = 0
 GB_PRECISION_MIXED = 1
+GB_FORCES_SET = 1
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -51,6 +52,7 @@ SIGNATURES = [
     ("gb_potential_get_cutoff", _D, [_P]),
     ("gb_potential_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_potential_energy_and_forces", _I, [_P] * 13 + [_P]),
+    ("gb_potential_energy_and_forces_flags", _I, [_P] * 13 + [_I, _P]),
     ("gb_tersoff_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_tersoff_energy_and_forces", _I, [_P] * 13 + [_P]),
     ("gb_kumagai_bind_to", _I, [_P, _P, _P, _P]),

@@ -281,7 +281,8 @@ int add_into(double *dst, const double *src, size_t n, cudaStream_t s) {
 
 int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot, double *f,
                       double *wpot, const int *mask, double *epa, double *epb, double *fpb,
-                      double *wpa, double *wpb) {
+                      double *wpa, double *wpb, int flags = 0) {
+  const bool set_f = (flags & GB_FORCES_SET) != 0;  // f is written, not accumulated into
   if (!epot || !f || !wpot) {
     set_error("energy_and_forces: epot, f and wpot are required");
     return GB_ERROR_ARGUMENT;
@@ -306,7 +307,7 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   // while the neighbour list is built.
   Stage sf, sepa, swpa, sepb, sfpb, swpb;
   const bool f_host = nat > 0 && !is_device_ptr(f);
-  if (f_host) {
+  if (f_host && !set_f) {
     if (!pot.aux) {
       GB_CUDA(cudaStreamCreateWithFlags(&pot.aux, cudaStreamNonBlocking));
       GB_CUDA(cudaEventCreateWithFlags(&pot.aux_ev, cudaEventDisableTiming));
@@ -322,10 +323,25 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
 
   const size_t nb = (size_t)nl.nentries;
-  if (f_host)
+  if (set_f) {
+    // nothing to upload: the forces start from zero on the device
+    if (f_host) {
+      GB_CHECK(pot.out_f.ensure(sizeof(double) * 3 * std::max<size_t>(nat, 1)));
+      sf.caller = f;
+      sf.dev = pot.out_f.as<double>();
+      sf.n = 3 * (size_t)nat;
+      sf.host = true;
+    } else {
+      sf.caller = sf.dev = f;
+      sf.n = 3 * (size_t)nat;
+      sf.host = false;
+    }
+    if (nat) GB_CUDA(cudaMemsetAsync(sf.dev, 0, sizeof(double) * 3 * nat, s));
+  } else if (f_host) {
     GB_CUDA(cudaStreamWaitEvent(s, pot.aux_ev, 0));
-  else
+  } else {
     GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, s, sf));
+  }
   GB_CHECK(stage_in(epa, nat, pot.out_epa, s, sepa));
   GB_CHECK(stage_in(wpa, 9 * (size_t)nat, pot.out_wpa, s, swpa));
   GB_CHECK(stage_in(epb, nb, pot.out_epb, s, sepb));
@@ -777,6 +793,21 @@ int gb_potential_energy_and_forces_ghost(gb_potential_t *h, int nat, int natloc,
   int rc = h ? energy_and_forces_ghost(h->pot, nat, natloc, r, Z, seed, nbr, epot, f, wpot, mask,
                                        epot_per_at, wpot_per_at)
              : GB_ERROR_ARGUMENT;
+  if (ierror) *ierror = rc;
+  return rc;
+}
+
+int gb_potential_energy_and_forces_flags(gb_potential_t *h, gb_particles_t *p,
+                                         gb_neighbors_t *nl, const double *q, double *epot,
+                                         double *f, double *wpot, const int *mask, double *epa,
+                                         double *epb, double *fpb, double *wpa, double *wpb,
+                                         int flags, int *ierror) {
+  (void)q;
+  clear_error();
+  int rc = (h && p && nl)
+               ? energy_and_forces(h->pot, p->p, nl->nl, epot, f, wpot, mask, epa, epb, fpb, wpa,
+                                   wpb, flags)
+               : GB_ERROR_ARGUMENT;
   if (ierror) *ierror = rc;
   return rc;
 }

@@ -308,9 +308,10 @@ class _Potential:
 
     def energy_and_forces(self, particles, neighbors, forces=None, mask=None, charges=None,
                           epot_per_at=None, epot_per_bond=None, f_per_bond=None,
-                          wpot_per_at=None, wpot_per_bond=None):
+                          wpot_per_at=None, wpot_per_bond=None, accumulate=True):
         nat = len(particles)
         dev = _is_torch(forces) and forces.is_cuda
+        accumulate = accumulate and forces is not None  # a fresh array is just written
 
         def zeros(shape):
             if dev:
@@ -355,10 +356,12 @@ class _Potential:
         epot = ctypes.c_double(0.0)
         err = ctypes.c_int(0)
         g = lambda k: ptrs[k][0] if k in ptrs else None  # noqa: E731
-        rc = self._L.gb_potential_energy_and_forces(
+        # accumulate=False: the forces array is overwritten (no upload of it)
+        rc = self._L.gb_potential_energy_and_forces_flags(
             self._h, particles._h, neighbors._h, None, ctypes.byref(epot), fp,
             wpot.ctypes.data, mp, g("epot_per_at"), g("epot_per_bond"), g("f_per_bond"),
-            g("wpot_per_at"), g("wpot_per_bond"), ctypes.byref(err))
+            g("wpot_per_at"), g("wpot_per_bond"), 0 if accumulate else _lib.GB_FORCES_SET,
+            ctypes.byref(err))
         check(rc, "%s.energy_and_forces" % type(self).__name__)
         if fkeep is not forces and not _is_torch(forces):
             forces[...] = fkeep

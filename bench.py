@@ -14,8 +14,9 @@ reference's ASE path with a zero Verlet shell) + energy, forces and virial.
           (256 MB write, outside the timed events); the FP64 drop-in is
           timed the same way and reported beside it.
   e2e     the same metric through the public API with pinned HOST buffers:
-          per step the position upload, the force upload (accumulate
-          semantics) and the force/energy/virial download are timed.
+          per step the position upload and the force/energy/virial download
+          are timed (forces written, as the reference's call without a forces
+          argument returns a fresh array).
   roofline  the dominant kernel (bond-order tile kernel, mixed form):
           algorithmic FP32/FP64 flops per launch / kernel time against the
           FP32 and FP64 FMA peaks measured in this run.
@@ -219,6 +220,7 @@ def other_configs(dev, oracle):
                        "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}
     out["tersoff_si_4096"] = entry
     out["tersoff_scr"] = screened_config(dev, oracle, nth, cpu_time)
+    out["md_si_4096"] = md_config()
 
     s = structures.eam_cu_131072(seed=2)
     with tempfile.TemporaryDirectory() as td:
@@ -245,6 +247,33 @@ def other_configs(dev, oracle):
                             "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
                                      "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                                      "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
+    return out
+
+
+def md_config():
+    """Velocity-Verlet MD of the 4096-atom Si crystal (a batch of one,
+    Tersoff, dt = 1 fs): wall time per step of 200 steps, eager (list size and
+    tile plan read back every step) and replayed as one CUDA graph per step."""
+    import numpy as np
+    from atomistica_gb300 import native, structures
+    s = structures.tersoff_si_4096(seed=1)
+    rng = np.random.default_rng(9)
+    v = rng.normal(0.0, 0.02, (len(s), 3))
+    m = np.full(len(s), 28.0855)
+    out = {"natoms": len(s), "unit": "steps/s", "dt": 0.1, "mass_amu": 28.0855}
+    for prec in ("fp64", "mixed"):
+        pot = native.Tersoff(precision=prec)
+        for graph in (False, True):
+            b = native.Batch([s])
+            b.set_options(graph=graph)
+            b.md_set_state(v, m)
+            b.md_run(pot, 0.1, 5)  # warm-up (and the capture)
+            t0 = time.perf_counter()
+            b.md_run(pot, 0.1, 200)
+            t = (time.perf_counter() - t0) / 200
+            out["%s_%s" % (prec, "graph" if graph else "eager")] = {
+                "value": 1.0 / t, "ms_per_step": 1e3 * t,
+                "atom_steps_per_s": len(s) / t, "replayed": b.last_info()["replayed"]}
     return out
 
 
@@ -559,22 +588,22 @@ def run_ours(args):
     pot = pots["mixed"]
     for _ in range(2):
         p.set_positions(pos_np)
-        pot.energy_and_forces(p, nl, forces=f_np)
+        pot.energy_and_forces(p, nl, forces=f_np, accumulate=False)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        f_np[...] = 0.0
         p.set_positions(pos_np)
-        e2e_e, _, e2e_w = pot.energy_and_forces(p, nl, forces=f_np)
+        e2e_e, _, e2e_w = pot.energy_and_forces(p, nl, forces=f_np, accumulate=False)
     torch.cuda.synchronize()
     t_e2e = tmax(time.perf_counter() - t0)
     e2e = {"value": ws * nat * args.steps / t_e2e, "unit": UNIT,
-           "h2d_bytes_per_step": 2 * 24 * nat, "d2h_bytes_per_step": 24 * nat + 80,
-           "api": "native.Particles.set_positions + Tersoff.energy_and_forces (C-ABI "
-                  "gb_particles_set_positions / gb_potential_energy_and_forces), pinned "
-                  "host numpy buffers"}
+           "h2d_bytes_per_step": 24 * nat, "d2h_bytes_per_step": 24 * nat + 80,
+           "api": "native.Particles.set_positions + Tersoff.energy_and_forces(accumulate="
+                  "False) (C-ABI gb_particles_set_positions / "
+                  "gb_potential_energy_and_forces_flags(GB_FORCES_SET)), pinned host numpy "
+                  "buffers: positions up, forces written down"}
 
     # Roofline of the dominant kernel (mixed bond-order tile kernel):
     # T_roof = max(flops / FP32 peak, bytes / HBM peak), frac = T_roof / t.

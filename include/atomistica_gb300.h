@@ -58,6 +58,9 @@ extern "C" {
 #define GB_PRECISION_FP64 0  /* drop-in: FP64 throughout */
 #define GB_PRECISION_MIXED 1 /* FP32 bond arithmetic, FP64 accumulation */
 
+/* Flags of gb_potential_energy_and_forces_flags. */
+#define GB_FORCES_SET 1 /* f is set to the forces instead of accumulated into */
+
 typedef struct gb_particles gb_particles_t;
 typedef struct gb_neighbors gb_neighbors_t;
 typedef struct gb_potential gb_potential_t;
@@ -201,6 +204,15 @@ int gb_potential_energy_and_forces_ghost(gb_potential_t *pot, int nat, int natlo
 /* python_<mod>_energy_and_forces (gen_factory.py:239-356 -> COMPUTE_FUNC,
  * default_compute_func.f90:25-100; tabulated_alloy_eam.f90:360-415).
  * q (charges) is accepted and ignored, as by these potentials. */
+/* As gb_potential_energy_and_forces; flags = GB_FORCES_SET writes f (the
+ * reference's own Python call without a forces argument returns a fresh
+ * zeroed array, potential.c:468): no upload of the caller's f. */
+int gb_potential_energy_and_forces_flags(gb_potential_t *pot, gb_particles_t *p,
+                                         gb_neighbors_t *nl, const double *q, double *epot,
+                                         double *f, double *wpot, const int *mask,
+                                         double *epot_per_at, double *epot_per_bond,
+                                         double *f_per_bond, double *wpot_per_at,
+                                         double *wpot_per_bond, int flags, int *ierror);
 int gb_potential_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
                                    const double *q, double *epot, double *f, double *wpot,
                                    const int *mask, double *epot_per_at, double *epot_per_bond,

@@ -250,3 +250,19 @@ def test_mixed_precision_amorphous_workload(gpu, natoms):
     # size-independent properties: no net force (translation invariance)
     assert np.max(np.abs(gmx["f"].sum(axis=0))) < 1e-6 * natoms ** 0.5
     assert np.max(np.abs(g64["f"].sum(axis=0))) < 1e-9 * natoms ** 0.5
+
+
+def test_forces_set_instead_of_accumulated(gpu):
+    from atomistica_gb300 import native
+    s = rattled_diamond("Si", 5.431, (2, 2, 2), 0.2, 71)
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    pot = native.Tersoff()
+    pot.bind_to(p, nl)
+    e0, f0, w0 = pot.energy_and_forces(p, nl)
+    f1 = np.full((len(s), 3), 7.0)
+    e1, f1, w1 = pot.energy_and_forces(p, nl, forces=f1, accumulate=False)
+    assert np.array_equal(f1, f0) and e1 == e0 and np.array_equal(w1, w0)
+    f2 = np.full((len(s), 3), 7.0)
+    _, f2, _ = pot.energy_and_forces(p, nl, forces=f2)
+    assert np.max(np.abs(f2 - (f0 + 7.0))) < 1e-12
