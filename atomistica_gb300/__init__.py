@@ -24,7 +24,7 @@ def __getattr__(name):
     # The calculator classes load the CUDA library lazily, so that parameter
     # sets and structure builders stay importable on machines without a GPU.
     if name in ("Atomistica", "Tersoff", "Kumagai", "TersoffScr", "KumagaiScr",
-                "TabulatedAlloyEAM"):
+                "TabulatedEAM", "TabulatedAlloyEAM"):
         from . import calculator
         return getattr(calculator, name)
     if name in ("native", "calculator", "io", "build"):

@@ -42,6 +42,7 @@ SIGNATURES = [
     ("gb_tersoff_new", _I, [_P, _P]),
     ("gb_kumagai_new", _I, [_P, _P]),
     ("gb_tersoff_scr_new", _I, [_P, _P, _P]),
+    ("gb_tabulated_eam_new", _I, [_P, ctypes.c_char_p]),
     ("gb_potential_energy_and_forces_ghost", _I,
      [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("gb_kumagai_scr_new", _I, [_P, _P, _P]),

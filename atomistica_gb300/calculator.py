@@ -35,7 +35,7 @@ class Atomistica:
         if potentials is not None:
             self.pots = list(potentials)
         else:
-            if self.potential_class is native.TabulatedAlloyEAM:
+            if self.potential_class in (native.TabulatedAlloyEAM, native.TabulatedEAM):
                 self.pots = [self.potential_class(**kwargs)]
             else:
                 self.pots = [self.potential_class(precision=precision, **kwargs)]
@@ -194,6 +194,11 @@ class TersoffScr(Atomistica):
 class KumagaiScr(Atomistica):
     name = "KumagaiScr"
     potential_class = native.KumagaiScr
+
+
+class TabulatedEAM(Atomistica):
+    name = "TabulatedEAM"
+    potential_class = native.TabulatedEAM
 
 
 class TabulatedAlloyEAM(Atomistica):

@@ -221,9 +221,10 @@ int update_element_map(Potential &pot, const Particles &p) {
   if (pot.el_for == &p && pot.el_zrev == p.z_rev && pot.el.p) return 0;
   const int nel = pot_nel(pot);
   std::vector<int> el(std::max(p.nat, 1), -1);
+  const bool all = pot.kind == kEAM && pot.eam->funcfl;  // elements = "*"
   for (int i = 0; i < p.nat; i++)
     for (int q = 0; q < nel; q++)
-      if (p.hZ[i] == pot_Z(pot, q)) el[i] = q;
+      if (all || p.hZ[i] == pot_Z(pot, q)) el[i] = q;
   GB_CHECK(pot.el.ensure(sizeof(int) * el.size()));
   GB_CUDA(cudaMemcpyAsync(pot.el.p, el.data(), sizeof(int) * el.size(), cudaMemcpyHostToDevice,
                           pot_stream(pot)));
@@ -289,6 +290,10 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   }
   if (pot.kind == kEAM && (epb || fpb || wpb)) {
     set_error("Per-bond properties are not supported by TabulatedAlloyEAM.");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (pot.kind == kEAM && pot.eam->funcfl && mask) {
+    set_error("Masks are not supported by TabulatedEAM.");  // features: per_at
     return GB_ERROR_ARGUMENT;
   }
   if (pot.kind == kEAM && pot.precision != GB_PRECISION_FP64) {
@@ -710,6 +715,18 @@ int gb_kumagai_scr_new(gb_potential_t **h, const gb_kumagai_params_t *params,
   (*h)->pot.kp = p;
   (*h)->pot.screened = true;
   (*h)->pot.scr = sc;
+  return 0;
+}
+
+int gb_tabulated_eam_new(gb_potential_t **h, const char *fn) {
+  clear_error();
+  if (!h || !fn) return GB_ERROR_ARGUMENT;
+  std::unique_ptr<EamTables> t(new EamTables);
+  GB_CHECK(eam_read_funcfl(fn, *t));
+  GB_CHECK(eam_upload(*t));
+  *h = new gb_potential;
+  (*h)->pot.kind = kEAM;
+  (*h)->pot.eam = std::move(t);
   return 0;
 }
 

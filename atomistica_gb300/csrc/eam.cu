@@ -31,6 +31,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <type_traits>
 
 #include "potential.h"
 
@@ -170,6 +171,75 @@ int eam_read_setfl(const char *fn, EamTables &t) {
       t.phi[(size_t)i * t.nel + j] = s;
       t.phi[(size_t)j * t.nel + i] = s;
     }
+  return 0;
+}
+
+// funcfl reader (tabulated_eam.f90:147-200): comment; "Z mass a0 lattice";
+// "nF dF nr dr cutoff"; F(rho) [nF], Z(r) [nr], rho(r) [nr]; no padding; Z
+// scaled by sqrt(Hartree Bohr / 2) with the constants of Units.f90:74-76.
+int eam_read_funcfl(const char *fn, EamTables &t) {
+  std::ifstream in(fn);
+  if (!in) {
+    set_error(std::string("Could not open file '") + fn + "'.");
+    return GB_ERROR_FILE_NOT_FOUND;
+  }
+  std::string line;
+  if (!std::getline(in, line) || !std::getline(in, line)) {
+    set_error("funcfl: premature end of file in header");
+    return GB_ERROR_IO_EOF;
+  }
+  t.nel = 1;
+  t.Z.assign(1, 0);
+  {
+    std::istringstream ss(line);
+    ss >> t.Z[0];
+    if (!ss || t.Z[0] <= 0) {
+      set_error("funcfl: bad element line: " + line);
+      return GB_ERROR_IO;
+    }
+  }
+  int nF = 0, nr = 0;
+  double dF = 0, dr = 0;
+  if (!std::getline(in, line)) {
+    set_error("funcfl: premature end of file");
+    return GB_ERROR_IO_EOF;
+  }
+  {
+    std::istringstream ss(line);
+    ss >> nF >> dF >> nr >> dr >> t.cutoff;
+    if (!ss || nF < 2 || nr < 2 || !(dF > 0) || !(dr > 0)) {
+      set_error("funcfl: bad grid line: " + line);
+      return GB_ERROR_IO;
+    }
+  }
+  auto read_values = [&](int n, std::vector<double> &v) {
+    v.clear();
+    std::string tok;
+    while ((int)v.size() < n && (in >> tok)) v.push_back(std::strtod(tok.c_str(), nullptr));
+    return (int)v.size() == n;
+  };
+  std::vector<double> v;
+  t.F.assign(1, SplineHost());
+  t.rho.assign(1, SplineHost());
+  t.phi.assign(1, SplineHost());
+  if (!read_values(nF, v)) {
+    set_error("funcfl: premature end of file in F(rho)");
+    return GB_ERROR_IO_EOF;
+  }
+  t.F[0].init(nF, 0.0, dF, v.data());
+  if (!read_values(nr, v)) {
+    set_error("funcfl: premature end of file in Z(r)");
+    return GB_ERROR_IO_EOF;
+  }
+  t.phi[0].init(nr, 0.0, dr, v.data());
+  if (!read_values(nr, v)) {
+    set_error("funcfl: premature end of file in rho(r)");
+    return GB_ERROR_IO_EOF;
+  }
+  t.rho[0].init(nr, 0.0, dr, v.data());
+  const double hartree = 27.2113961, bohr = 0.529177249;
+  t.phi[0].scale_y(std::sqrt(0.5 * hartree * bohr));
+  t.funcfl = true;
   return 0;
 }
 
@@ -324,6 +394,19 @@ __device__ __forceinline__ void r_interval(const SplineDev &s, double r, double 
   k = i - 1;
 }
 
+// The reference's SPLINE_* macros (spline.inc; funcfl EAM):
+// xf = (x - x0) * (1/dx) + 1, i = int(xf); an index outside the table (an
+// out-of-bounds read in the reference) is clamped and reported.
+__device__ __forceinline__ void inline_interval(const SplineDev &s, double x, double &B, int &k,
+                                                bool &ok) {
+  const double xf = __dadd_rn(__dmul_rn(__dsub_rn(x, s.x0), s.rdx), 1.0);
+  int i = (int)fmin(fmax(xf, -1.0e9), 1.0e9);
+  ok = i >= 1 && i < s.n;
+  i = min(max(i, 1), s.n - 1);
+  B = xf - i;
+  k = i - 1;
+}
+
 __device__ __forceinline__ void interval_fdf(const SplineDev &s, int k, double B, double &f,
                                              double &df) {
   const double2 *t = reinterpret_cast<const double2 *>(s.tab + 8 * (size_t)k);
@@ -352,6 +435,7 @@ __device__ __forceinline__ double rsqrt_nr(double r2) {
   return fma(y, e, y);
 }
 
+template <bool kFuncfl>
 __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
   const int gt = blockIdx.x * kEamThreads + threadIdx.x;
   const int i = gt / kEamLanes, sub = gt % kEamLanes;
@@ -377,7 +461,10 @@ __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
         double B;
         int k;
         bool ok;
-        r_interval(a.rho[elj], sqrt(r2), B, k, ok);
+        if (kFuncfl)
+          inline_interval(a.rho[elj], sqrt(r2), B, k, ok);
+        else
+          r_interval(a.rho[elj], sqrt(r2), B, k, ok);
         bad |= !ok;
         rho += interval_f(a.rho[elj], k, B);
       }
@@ -389,7 +476,16 @@ __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
     double F = 0.0, dF = 0.0;
     if (on) {
       if (rho < 0.0) rho = 0.0;
-      spline_fdf_extrap(a.F[eli], rho, F, dF);
+      if (kFuncfl) {
+        double B;
+        int k;
+        bool ok;
+        inline_interval(a.F[eli], rho, B, k, ok);
+        if (!ok) atomicOr(a.status, 1);
+        interval_fdf(a.F[eli], k, B, F, dF);
+      } else {
+        spline_fdf_extrap(a.F[eli], rho, F, dF);
+      }
     }
     a.Fi[i] = F;
     a.dFi[i] = dF;
@@ -402,7 +498,7 @@ __device__ __forceinline__ int sym_index(int c2, int c) {
   return c2 == c ? c : 2 + c2 + c;  // (0,1) -> 3, (0,2) -> 4, (1,2) -> 5
 }
 
-template <bool kEpa, bool kWat>
+template <bool kEpa, bool kWat, bool kFuncfl>
 __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
   __shared__ double sred[kEamThreads / 32][7];
   const int gt = blockIdx.x * kEamThreads + threadIdx.x;
@@ -435,10 +531,21 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
       double B;
       int k;
       bool ok;
-      r_interval(sp, r, B, k, ok);
-      double phi, dphi;
-      interval_fdf(sp, k, B, phi, dphi);
-      const double pair = (dphi - phi * rinv) * rinv;
+      double phi, dphi, pair;
+      if (kFuncfl) {
+        // Z(r): pair energy Z^2 / r, its derivative 2 Z Z' / r - Z^2 / r^2
+        // (tabulated_eam.f90:301-304)
+        inline_interval(sp, r, B, k, ok);
+        double z, dz;
+        interval_fdf(sp, k, B, z, dz);
+        phi = z * z * rinv;
+        pair = 2 * z * dz * rinv - phi * rinv;
+      } else {
+        r_interval(sp, r, B, k, ok);
+        interval_fdf(sp, k, B, phi, dphi);
+        pair = (dphi - phi * rinv) * rinv;
+        phi = phi * rinv;
+      }
       double fac_i = 0.0;
       if (mi) {
         // i-side of entry (i->j), :577-607: df = sc d, f_i += df,
@@ -446,7 +553,7 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
         bad |= !ok;
         fac_i = interval_df(a.rho[elj], k, B);
         const double sc = -(dFi * fac_i + pair) * rinv;
-        Ei += phi * rinv;
+        Ei += phi;
         const double df[3] = {sc * d[0], sc * d[1], sc * d[2]};
         F3[0] += df[0];
         F3[1] += df[1];
@@ -560,25 +667,36 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * blocks + 64));
   a.part = pot.tile_part.as<double>();
   a.status = o.status;
-  eam_density<<<blocks, kEamThreads, 0, s>>>(a);
+  const bool ff = t.funcfl;
+  if (ff)
+    eam_density<true><<<blocks, kEamThreads, 0, s>>>(a);
+  else
+    eam_density<false><<<blocks, kEamThreads, 0, s>>>(a);
   note_launch();
   const bool epa = o.epot_per_at != nullptr;
+  // the funcfl kernel of the reference leaves wpot_per_at untouched
+  const bool wat = want_wat && !ff;
   GB_CUDA(cudaEventRecord(pot.kev[0], s));
-  if (epa && want_wat) {
-    eam_pair<true, true><<<blocks, kEamThreads, 0, s>>>(a);
+  auto pair = [&](auto epa_t, auto wat_t, auto ff_t) {
+    eam_pair<decltype(epa_t)::value, decltype(wat_t)::value, decltype(ff_t)::value>
+        <<<blocks, kEamThreads, 0, s>>>(a);
     note_launch();
-  }
-  else if (epa) {
-    eam_pair<true, false><<<blocks, kEamThreads, 0, s>>>(a);
-    note_launch();
-  }
-  else if (want_wat) {
-    eam_pair<false, true><<<blocks, kEamThreads, 0, s>>>(a);
-    note_launch();
-  }
-  else {
-    eam_pair<false, false><<<blocks, kEamThreads, 0, s>>>(a);
-    note_launch();
+  };
+  using T = std::true_type;
+  using F = std::false_type;
+  if (ff) {
+    if (epa)
+      pair(T{}, F{}, T{});
+    else
+      pair(F{}, F{}, T{});
+  } else if (epa && wat) {
+    pair(T{}, T{}, F{});
+  } else if (epa) {
+    pair(T{}, F{}, F{});
+  } else if (wat) {
+    pair(F{}, T{}, F{});
+  } else {
+    pair(F{}, F{}, F{});
   }
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CUDA(cudaGetLastError());

@@ -36,12 +36,18 @@ struct EamTables {
   int nel = 0;
   std::vector<int> Z;
   double cutoff = 0;
+  // Single-element funcfl file (TabulatedEAM, tabulated_eam.f90): phi[0]
+  // holds the scaled effective charge Z(r), the pair term is Z^2 / r, the
+  // splines are evaluated as the reference's SPLINE_* macros, every atom is
+  // of the file's element.
+  bool funcfl = false;
   std::vector<SplineHost> F, rho, phi;  // phi[i*nel+j]
   DevBuf dev;                           // all tables, packed
   std::vector<SplineDev> dF, drho, dphi;
 };
 
 int eam_read_setfl(const char *fn, EamTables &t);
+int eam_read_funcfl(const char *fn, EamTables &t);
 int eam_upload(EamTables &t);
 
 struct Outputs {

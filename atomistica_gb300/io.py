@@ -4,6 +4,8 @@ Small file readers/writers needed by the force path without ASE:
 * ``read_cfg``   — AtomEye extended .cfg (the reference's aC.cfg fixtures).
 * ``write_setfl`` / ``cu_analytic_setfl`` — DYNAMO setfl tables in the layout
   read by src/potentials/eam/tabulated_alloy_eam.f90:178-253.
+* ``write_funcfl`` / ``cu_analytic_funcfl`` — single-element DYNAMO funcfl
+  tables as read by src/potentials/eam/tabulated_eam.f90:147-200.
 """
 
 import numpy as np
@@ -119,6 +121,34 @@ def cu_analytic_setfl(fn, nr=10000, cutoff=5.0, nrho=10000, rho_max=40.0):
                           "generated by atomistica_gb300.io.cu_analytic_setfl"],
                 Z=[29], mass=[63.546], a0=[3.615], lattice=["fcc"])
     return fn
+
+
+def write_funcfl(fn, comment, Z, mass, a0, lattice, nrho, drho, nr, dr, cutoff, F, Zr, rho):
+    """DYNAMO funcfl file (single element; tabulated_eam.f90:147-200 format):
+    comment; Z mass a0 lattice; nrho drho nr dr cutoff; F(rho), Z(r), rho(r)."""
+    def block(a):
+        a = np.asarray(a, dtype=np.float64)
+        return "\n".join(" ".join("% .16e" % x for x in a[q:q + 5]) for q in range(0, len(a), 5))
+    with open(fn, "w") as f:
+        f.write(comment.strip() + "\n")
+        f.write("%d %.6f %.6f %s\n" % (Z, mass, a0, lattice))
+        f.write("%d %.16e %d %.16e %.16e\n" % (nrho, drho, nr, dr, cutoff))
+        f.write(block(F) + "\n" + block(Zr) + "\n" + block(rho) + "\n")
+    return fn
+
+
+def cu_analytic_funcfl(fn, nr=2000, cutoff=5.5, nrho=2000, rho_max=40.0):
+    """Analytic funcfl Cu: density exp(-3(r/2.556 - 1)), effective charge
+    Z(r) = 10 exp(-1.5 r) (screened Coulomb pair term Z^2/r in the reference's
+    units), embedding F(rho) = -1.2 sqrt(rho)."""
+    dr = cutoff / (nr - 1)
+    r = np.arange(nr) * dr
+    rho = np.exp(-3.0 * (r / 2.556 - 1.0))
+    Zr = 10.0 * np.exp(-1.5 * r)
+    drho = rho_max / (nrho - 1)
+    F = -1.2 * np.sqrt(np.arange(nrho) * drho)
+    return write_funcfl(fn, "Analytic Cu funcfl (atomistica_gb300.io.cu_analytic_funcfl)", 29,
+                        63.546, 3.615, "FCC", nrho, drho, nr, dr, cutoff, F, Zr, rho)
 
 
 def read_poscar(fn):

@@ -461,6 +461,21 @@ class KumagaiScr(_Potential):
         self.set_precision(precision)
 
 
+class TabulatedEAM(_Potential):
+    """Single-element tabulated EAM from a DYNAMO funcfl file
+    (src/potentials/eam/tabulated_eam.f90)."""
+
+    features = ("per_at",)
+
+    def __init__(self, fn, elements="*"):
+        super().__init__()
+        if elements not in ("*", None):
+            raise NotImplementedError("element filters other than '*' are not supported")
+        check(self._L.gb_tabulated_eam_new(ctypes.byref(self._h), str(fn).encode()),
+              "TabulatedEAM")
+        self._precision = "fp64"
+
+
 class TabulatedAlloyEAM(_Potential):
     """Tabulated alloy EAM from a DYNAMO setfl file
     (src/potentials/eam/tabulated_alloy_eam.f90)."""

@@ -173,6 +173,11 @@ int gb_kumagai_scr_new(gb_potential_t **pot, const gb_kumagai_params_t *params,
 /* python_tabulated_alloy_eam_new + init(fn=...) (tabulated_alloy_eam.f90:147-259):
  * reads a DYNAMO setfl file. */
 int gb_tabulated_alloy_eam_new(gb_potential_t **pot, const char *fn);
+/* python_tabulated_eam_new + init(fn=...) (tabulated_eam.f90:147-200): a
+ * single-element DYNAMO funcfl file; every atom is of its element
+ * (elements = "*"); no mask; wpot_per_at is left untouched, as by the
+ * reference kernel. */
+int gb_tabulated_eam_new(gb_potential_t **pot, const char *fn);
 /* python_<mod>_free */
 void gb_potential_free(gb_potential_t *pot);
 /* GB_PRECISION_FP64 (default) or GB_PRECISION_MIXED (BOP only). */

@@ -1379,6 +1379,188 @@ struct Spline {
   }
 };
 
+// The SPLINE_* macros of src/spline.inc (used by tabulated_eam.f90):
+// xf = (x - x0) * (1/dx) + 1, i = int(xf) (truncation), no range check.
+struct InlineSpline {
+  const Spline *s;
+  double rdx;
+  explicit InlineSpline(const Spline &q) : s(&q), rdx(1.0 / q.dx) {}
+  void at(double x, double &B, int &k, int *err) const {
+    const double xf = (x - s->x0) * rdx + 1.0;
+    int i = (int)xf;
+    if (i < 1 || i >= s->n) {  // out of the table: undefined in the reference
+      if (err) *err = -1;
+      i = std::min(std::max(i, 1), s->n - 1);
+    }
+    B = xf - i;
+    k = i - 1;
+  }
+  double f(double x, int *err) const {
+    double B;
+    int k;
+    at(x, B, k, err);
+    return s->y[k] + B * (s->c1[k] + B * (s->c2[k] + B * s->c3[k]));
+  }
+  double df(double x, int *err) const {
+    double B;
+    int k;
+    at(x, B, k, err);
+    return s->d1[k] + B * (s->d2[k] + B * s->d3[k]);
+  }
+};
+
+// Single-element funcfl EAM (tabulated_eam.f90:147-200): F(rho), the
+// effective charge Z(r) scaled by sqrt(Hartree Bohr / 2) (Units.f90:74-76),
+// rho(r); no padding.
+struct FuncflEAM {
+  int Z = 0;
+  double mass = 0, a0 = 0, cutoff = 0;
+  Spline F, Zr, rho;
+};
+
+int funcfl_read(const char *fn, FuncflEAM &e) {
+  std::ifstream in(fn);
+  if (!in) return -1;
+  std::string line;
+  if (!std::getline(in, line)) return -2;  // comment
+  if (!std::getline(in, line)) return -2;
+  {
+    std::istringstream ss(line);
+    ss >> e.Z >> e.mass >> e.a0;
+    if (!ss) return -3;
+  }
+  int nF, nr;
+  double dF, dr;
+  if (!std::getline(in, line)) return -2;
+  {
+    std::istringstream ss(line);
+    ss >> nF >> dF >> nr >> dr >> e.cutoff;
+    if (!ss) return -3;
+  }
+  auto read_values = [&](int n, std::vector<double> &v) {
+    v.clear();
+    std::string tok;
+    while ((int)v.size() < n && (in >> tok)) v.push_back(std::strtod(tok.c_str(), nullptr));
+    return (int)v.size() == n;
+  };
+  std::vector<double> v;
+  if (!read_values(nF, v)) return -4;
+  e.F.init(nF, 0.0, dF, v.data());
+  if (!read_values(nr, v)) return -4;
+  e.Zr.init(nr, 0.0, dr, v.data());
+  if (!read_values(nr, v)) return -4;
+  e.rho.init(nr, 0.0, dr, v.data());
+  const double hartree = 27.2113961, bohr = 0.529177249;
+  e.Zr.scale_y(std::sqrt(0.5 * hartree * bohr));
+  return 0;
+}
+
+// tabulated_eam_energy_and_forces_kernel (tabulated_eam.f90:230-330): every
+// atom is of the potential's element (elements = "*"); no mask, no per-atom
+// virial (the reference leaves wpot_per_at untouched).
+int funcfl_kernel(const FuncflEAM &e, int nat, const double *r, const Box &box, const NList &nl,
+                  double *epot, double *fout, double *wpot, double *epot_per_at, int nthreads) {
+  const double cutoff_sq = e.cutoff * e.cutoff;
+  const InlineSpline sF(e.F), sZ(e.Zr), srho(e.rho);
+  int nt = nthreads;
+  std::vector<std::vector<double>> tsca(nt), tvec(nt);
+  std::vector<double> tw(9 * nt, 0.0);
+  int err_all = 0;
+#pragma omp parallel num_threads(nthreads) reduction(| : err_all)
+  {
+#ifdef _OPENMP
+    const int tid = omp_get_thread_num();
+#else
+    const int tid = 0;
+#endif
+    auto &sca = tsca[tid];
+    auto &vec = tvec[tid];
+    sca.assign(nat, 0.0);
+    vec.assign(3 * (size_t)nat, 0.0);
+    double w[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    std::vector<int> neb;
+    std::vector<double> neb_dr, neb_abs;
+#pragma omp for schedule(dynamic, 64)
+    for (int i = 0; i < nat; i++) {
+      double rho = 0.0;
+      neb.clear();
+      neb_dr.clear();
+      neb_abs.clear();
+      int err = 0;
+      for (int64_t ni = nl.seed[i]; ni < nl.seed[i + 1]; ni++) {
+        const int j = nl.nbr[ni];
+        const int *dc = &nl.dc[3 * ni];
+        double dr[3];
+        for (int a = 0; a < 3; a++) {
+          double as = box.A[a][0] * (double)dc[0];
+          as = as + box.A[a][1] * (double)dc[1];
+          as = as + box.A[a][2] * (double)dc[2];
+          dr[a] = (r[3 * i + a] - r[3 * j + a]) + as;
+        }
+        double abs_dr = dr[0] * dr[0];
+        abs_dr = abs_dr + dr[1] * dr[1];
+        abs_dr = abs_dr + dr[2] * dr[2];
+        if (abs_dr < cutoff_sq) {
+          abs_dr = std::sqrt(abs_dr);
+          rho = rho + srho.f(abs_dr, &err);
+          neb.push_back(j);
+          neb_dr.insert(neb_dr.end(), dr, dr + 3);
+          neb_abs.push_back(abs_dr);
+        }
+      }
+      if (rho < 0.0) rho = 0.0;
+      double B;
+      int k;
+      sF.at(rho, B, k, &err);
+      const double Fi = e.F.y[k] + B * (e.F.c1[k] + B * (e.F.c2[k] + B * e.F.c3[k]));
+      const double dFi = e.F.d1[k] + B * (e.F.d2[k] + B * e.F.d3[k]);
+      if (err) err_all |= 1;
+      sca[i] = sca[i] + Fi;
+      double esum = 0.0, fori[3] = {0, 0, 0};
+      for (size_t q = 0; q < neb.size(); q++) {
+        const double rr = neb_abs[q];
+        int e2 = 0;
+        sZ.at(rr, B, k, &e2);
+        double phi = e.Zr.y[k] + B * (e.Zr.c1[k] + B * (e.Zr.c2[k] + B * e.Zr.c3[k]));
+        double dphi = e.Zr.d1[k] + B * (e.Zr.d2[k] + B * e.Zr.d3[k]);
+        dphi = 2 * phi * dphi / rr;
+        phi = phi * phi / rr;
+        dphi = dphi - phi / rr;
+        esum = esum + phi;
+        const double fac = srho.df(rr, &e2);
+        if (e2) err_all |= 1;
+        const double *dr = &neb_dr[3 * q];
+        const double sc = -((dFi * fac + dphi) / rr);
+        double df[3];
+        for (int a = 0; a < 3; a++) df[a] = sc * dr[a];
+        const int j = neb[q];
+        for (int a = 0; a < 3; a++) {
+          fori[a] = fori[a] + df[a];
+          vec[3 * (size_t)j + a] = vec[3 * (size_t)j + a] - df[a];
+        }
+        for (int a = 0; a < 3; a++)
+          for (int c = 0; c < 3; c++) w[a][c] = w[a][c] + (-dr[a] * df[c]);
+      }
+      sca[i] = sca[i] + esum;
+      for (int a = 0; a < 3; a++) vec[3 * (size_t)i + a] += fori[a];
+    }
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) tw[9 * tid + 3 * a + c] = w[a][c];
+  }
+  double esum = 0.0;
+  for (int t = 0; t < nt; t++) {
+    if (tsca[t].empty()) continue;
+    for (int i = 0; i < nat; i++) esum += tsca[t][i];
+    for (size_t q = 0; q < 3 * (size_t)nat; q++) fout[q] += tvec[t][q];
+    if (epot_per_at)
+      for (int i = 0; i < nat; i++) epot_per_at[i] += tsca[t][i];
+    for (int a = 0; a < 3; a++)
+      for (int c = 0; c < 3; c++) wpot[3 * c + a] += tw[9 * t + 3 * a + c];
+  }
+  *epot = esum;
+  return err_all ? -5 : 0;
+}
+
 struct EAM {
   int nel = 0;
   std::vector<int> Z;
@@ -1872,6 +2054,35 @@ int orc_bop_ghost(int kind, const void *params, const orc_scr_params *sp, int na
   map_elements(nat, Z, p->nel, p->Z, el);
   return sp ? bop_kernel_scr(KumagaiFn(*p), *sp, nat, r, box, el.data(), nl, mask, o, nt, natloc)
             : bop_kernel(KumagaiFn(*p), nat, r, box, el.data(), nl, mask, o, nt, natloc);
+}
+
+struct orc_funcfl {
+  FuncflEAM e;
+};
+
+orc_funcfl *orc_funcfl_load(const char *fn, int *err) {
+  orc_funcfl *h = new orc_funcfl;
+  const int rc = funcfl_read(fn, h->e);
+  if (err) *err = rc;
+  if (rc != 0) {
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+void orc_funcfl_free(orc_funcfl *h) { delete h; }
+double orc_funcfl_cutoff(const orc_funcfl *h) { return h->e.cutoff; }
+
+// Neighbour build with the file's cutoff + kernel.
+int orc_funcfl_compute(const orc_funcfl *h, int nat, const double *r, const double *cell,
+                       const int *pbc, double *epot, double *f, double *wpot,
+                       double *epot_per_at, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  NList nl;
+  build_neighbors(nat, r, box, h->e.cutoff, nl);
+  return funcfl_kernel(h->e, nat, r, box, nl, epot, f, wpot, epot_per_at,
+                       resolve_threads(nthreads));
 }
 
 struct orc_eam {

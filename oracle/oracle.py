@@ -152,6 +152,14 @@ def lib():
         L.orc_bop_ghost.restype = ctypes.c_int
         L.orc_bop_ghost.argtypes = [ctypes.c_int, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P,
                                     _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
+        L.orc_funcfl_load.restype = _P
+        L.orc_funcfl_load.argtypes = [ctypes.c_char_p, _P]
+        L.orc_funcfl_free.argtypes = [_P]
+        L.orc_funcfl_cutoff.restype = ctypes.c_double
+        L.orc_funcfl_cutoff.argtypes = [_P]
+        L.orc_funcfl_compute.restype = ctypes.c_int
+        L.orc_funcfl_compute.argtypes = [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P,
+                                         ctypes.c_int]
         L.orc_eam_load.restype = _P
         L.orc_eam_load.argtypes = [ctypes.c_char_p, _P]
         L.orc_eam_free.argtypes = [_P]
@@ -331,6 +339,38 @@ def bop_compute(kind, params, s, mask=None, per_at=False, nthreads=0):
     out["epot"] = epot.value
     out["wpot"] = np.ascontiguousarray(out["wpot"])
     return out
+
+
+class FuncflEAM:
+    """Single-element funcfl EAM oracle (TabulatedEAM, tabulated_eam.f90)."""
+
+    def __init__(self, fn):
+        L = lib()
+        err = ctypes.c_int(0)
+        self._h = L.orc_funcfl_load(os.fsencode(fn), ctypes.byref(err))
+        if not self._h:
+            raise RuntimeError("oracle: cannot read funcfl %s (%d)" % (fn, err.value))
+        self.cutoff = L.orc_funcfl_cutoff(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.orc_funcfl_free(self._h)
+            self._h = None
+
+    def compute(self, s, per_at=True, nthreads=0):
+        L = lib()
+        r, cell, pbc, Z = _geom(s)
+        nat = len(r)
+        out = _alloc_outputs(nat, 0, per_at, False)
+        epot = ctypes.c_double(0.0)
+        rc = L.orc_funcfl_compute(self._h, nat, _ptr(r), _ptr(cell), _ptr(pbc),
+                                  ctypes.byref(epot), _ptr(out["f"]), _ptr(out["wpot"]),
+                                  _ptr(out.get("epot_per_at")), int(nthreads))
+        if rc != 0:
+            raise RuntimeError("oracle funcfl kernel failed: %d" % rc)
+        out["epot"] = epot.value
+        out["wpot"] = np.ascontiguousarray(out["wpot"])
+        return out
 
 
 class EAM:

@@ -266,3 +266,28 @@ def test_forces_set_instead_of_accumulated(gpu):
     f2 = np.full((len(s), 3), 7.0)
     _, f2, _ = pot.energy_and_forces(p, nl, forces=f2)
     assert np.max(np.abs(f2 - (f0 + 7.0))) < 1e-12
+
+
+@pytest.mark.parametrize("size", [(3, 3, 3), (5, 5, 5)])
+def test_funcfl_eam_fp64(gpu, tmp_path, size):
+    # TabulatedEAM (single-element funcfl) against the oracle's restatement
+    from atomistica_gb300 import io as gio
+    from atomistica_gb300 import native
+    from atomistica_gb300 import structures as S
+    fn = gio.cu_analytic_funcfl(str(tmp_path / "cu.eam"))
+    s = S.fcc("Cu", 3.615, size)
+    s.positions += np.random.default_rng(8).normal(0, 0.08, s.positions.shape)
+    ref = oracle.FuncflEAM(fn).compute(s)
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    pot = native.TabulatedEAM(fn)
+    pot.bind_to(p, nl)
+    e, f, w, epa, wpa = pot.energy_and_forces(p, nl, epot_per_at=True, wpot_per_at=True)
+    n = len(s)
+    assert abs(e - ref["epot"]) / n < 1e-10
+    assert np.max(np.abs(f - ref["f"])) < 1e-9
+    assert np.max(np.abs(w - ref["wpot"])) < 1e-9 * n
+    assert np.max(np.abs(epa - ref["epot_per_at"])) < 1e-9
+    assert not np.any(wpa)  # the reference kernel leaves the per-atom virial alone
+    with pytest.raises(Exception):
+        pot.energy_and_forces(p, nl, mask=np.ones(n, dtype=bool))

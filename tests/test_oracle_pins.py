@@ -180,6 +180,36 @@ def test_bulk_properties_eam_au(reference_tests_dir):
     assert within(c11, 202) and within(c12, 170) and within(c44, 46), (c11, c12, c44)
 
 
+class _Funcfl:
+    """funcfl oracle behind the EAM interface of these helpers (no masks)."""
+
+    def __init__(self, fn):
+        self.e = oracle.FuncflEAM(fn)
+
+    def compute(self, s, mask=None, per_at=False):
+        assert mask is None
+        return self.e.compute(s, per_at=per_at)
+
+
+def test_bulk_properties_funcfl_au(reference_tests_dir):
+    # TabulatedEAM Au_u3.eam (tests/test_bulk_properties.py:133-136)
+    e = _Funcfl(os.path.join(reference_tests_dir, "Au_u3.eam"))
+    builder = lambda a: S.fcc("Au", a)  # noqa: E731
+    a_min, e_min = lattice_minimum("eam", builder, e, 3.9, 4.2)
+    assert within(-e_min, 3.93) and within(a_min, 4.08), (e_min, a_min)
+    c11, c12, c44 = cubic_elastic_constants("eam", builder(a_min), e)
+    assert within(c11, 183) and within(c12, 159) and within(c44, 45), (c11, c12, c44)
+    assert within((c11 + 2 * c12) / 3, 167)
+
+
+def test_fd_forces_virial_funcfl(tmp_path):
+    e = _Funcfl(gio.cu_analytic_funcfl(str(tmp_path / "cu.eam")))
+    s = S.fcc("Cu", 3.615, (3, 3, 3))
+    s.positions += np.random.default_rng(7).normal(0, 0.05, s.positions.shape)
+    ferr, werr = fd_check("eam", s, e, natoms=8)
+    assert ferr < 1e-6 and werr < 1e-5, (ferr, werr)
+
+
 def fd_check(kind, s, params, dx=1e-6, natoms=None, mask=None):
     o = energy(kind, s, params, mask=mask)
     err = 0.0
