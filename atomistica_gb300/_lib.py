@@ -46,6 +46,8 @@ SIGNATURES = [
     ("gb_potential_energy_and_forces_ghost", _I,
      [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("gb_kumagai_scr_new", _I, [_P, _P, _P]),
+    ("gb_brenner_new", _I, [_P, _P]),
+    ("gb_brenner_scr_new", _I, [_P, _P, _P]),
     ("gb_tabulated_alloy_eam_new", _I, [_P, ctypes.c_char_p]),
     ("gb_potential_free", None, [_P]),
     ("gb_potential_set_precision", _I, [_P, _I]),
@@ -58,6 +60,8 @@ SIGNATURES = [
     ("gb_tersoff_energy_and_forces", _I, [_P] * 13 + [_P]),
     ("gb_kumagai_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_kumagai_energy_and_forces", _I, [_P] * 13 + [_P]),
+    ("gb_brenner_bind_to", _I, [_P, _P, _P, _P]),
+    ("gb_brenner_energy_and_forces", _I, [_P] * 13 + [_P]),
     ("gb_tabulated_alloy_eam_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_tabulated_alloy_eam_energy_and_forces", _I, [_P] * 10 + [_P]),
     ("gb_tabulated_alloy_eam_table", _I, [_P, _I, _I, _P, _P]),
@@ -100,6 +104,13 @@ class KumagaiParams(ctypes.Structure):
         [(k, _D * 1) for k in ("A", "B", "lambda1", "lambda2", "eta", "delta", "alpha")] + \
         [("beta", _I * 1)] + \
         [(k, _D * 1) for k in ("c1", "c2", "c3", "c4", "c5", "h", "r1", "r2")]
+
+
+class BrennerParams(ctypes.Structure):
+    """gb_brenner_params_t"""
+    _fields_ = [("nel", _I), ("Z", _I * 3)] + \
+        [(k, _D * 6) for k in ("D0", "r0", "S", "beta", "gamma", "c", "d", "h", "mu", "n")] + \
+        [("m", _I * 6), ("r1", _D * 6), ("r2", _D * 6)]
 
 
 class ScreeningParams(ctypes.Structure):

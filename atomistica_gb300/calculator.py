@@ -196,6 +196,16 @@ class KumagaiScr(Atomistica):
     potential_class = native.KumagaiScr
 
 
+class Brenner(Atomistica):
+    name = "Brenner"
+    potential_class = native.Brenner
+
+
+class BrennerScr(Atomistica):
+    name = "BrennerScr"
+    potential_class = native.BrennerScr
+
+
 class TabulatedEAM(Atomistica):
     name = "TabulatedEAM"
     potential_class = native.TabulatedEAM

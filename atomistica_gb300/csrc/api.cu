@@ -124,6 +124,87 @@ gb_screening_params_t default_screening_kumagai() {
   return s;
 }
 
+// Erhart_PRB_71_035211_SiC (brenner_params.f90:67-117, non-screened values;
+// el = C, Si).
+gb_brenner_params_t default_brenner() {
+  gb_brenner_params_t p{};
+  p.nel = 2;
+  p.Z[0] = 6;
+  p.Z[1] = 14;
+  const double D0[3] = {6.00, 4.36, 3.24}, r0[3] = {1.4276, 1.79, 2.232},
+               S[3] = {2.167, 1.847, 1.842}, beta[3] = {2.0099, 1.6991, 1.4761},
+               gamma[3] = {0.11233, 0.011877, 0.114354}, c[3] = {181.910, 273987.0, 2.00494},
+               d[3] = {6.28433, 180.314, 0.81472}, h[3] = {0.5556, 0.68, 0.259},
+               r1[3] = {1.85, 2.20, 2.68}, r2[3] = {2.15, 2.60, 2.96};
+  for (int q = 0; q < 3; q++) {
+    p.D0[q] = D0[q];
+    p.r0[q] = r0[q];
+    p.S[q] = S[q];
+    p.beta[q] = beta[q];
+    p.gamma[q] = gamma[q];
+    p.c[q] = c[q];
+    p.d[q] = d[q];
+    p.h[q] = h[q];
+    p.mu[q] = 0.0;
+    p.n[q] = 1.0;
+    p.m[q] = 1;
+    p.r1[q] = r1[q];
+    p.r2[q] = r2[q];
+  }
+  return p;
+}
+
+// The same set under SCREENING (brenner_params.f90:92-104): mu = 1/1.4276,
+// 1/1.79, 1/1.842, m = 3, inner cutoff r1 < r2 = 1.2 r1; the outer and
+// bond-order cutoffs and the C window are those of the screened Tersoff set.
+gb_brenner_params_t default_brenner_scr() {
+  gb_brenner_params_t p = default_brenner();
+  const double mu[3] = {1.0 / 1.4276, 1.0 / 1.79, 1.0 / 1.842};
+  const double r1[3] = {2.00, std::sqrt(2.00 * 2.50), 2.50};
+  for (int q = 0; q < 3; q++) {
+    p.mu[q] = mu[q];
+    p.m[q] = 3;
+    p.r1[q] = r1[q];
+    p.r2[q] = r1[q] * 1.2;
+  }
+  return p;
+}
+
+// The checks of the reference's bind_to (brenner_module.f90:200-210) and
+// the ones the kernels need.
+int check_brenner(const gb_brenner_params_t &p) {
+  if (p.nel < 1 || p.nel > 3) {
+    set_error("Brenner: nel must be 1..3 (BRENNER_MAX_EL = 3)");
+    return GB_ERROR_ARGUMENT;
+  }
+  const int np = p.nel * (p.nel + 1) / 2;
+  for (int q = 0; q < np; q++) {
+    if (!(p.r2[q] > p.r1[q]) || !(p.r1[q] >= 0)) {
+      set_error("Brenner: need 0 <= r1 < r2 for every pair");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (p.d[q] == 0.0) {
+      set_error("Brenner: d = 0! This leads to problems computing c**2/d**2. Please specify "
+                "d != 0.");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (!(p.S[q] > 1.0)) {
+      set_error("Brenner: S <= 1! This leads to problems computing (S-1)**(-1). Please "
+                "specify S > 1.");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (!(p.n[q] != 0.0)) {
+      set_error("Brenner: n must be nonzero");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (p.mu[q] != 0.0 && p.m[q] < 1) {
+      set_error("Brenner: m must be >= 1 when mu != 0");
+      return GB_ERROR_ARGUMENT;
+    }
+  }
+  return 0;
+}
+
 int check_screening(const gb_screening_params_t &s, int npairs) {
   for (int q = 0; q < npairs; q++) {
     if (!(s.or2[q] > s.or1[q]) || !(s.bor2[q] > s.bor1[q]) || !(s.Cmax[q] > s.Cmin[q])) {
@@ -176,12 +257,20 @@ int check_kumagai(const gb_kumagai_params_t &p) {
 
 }  // namespace
 
+const double *bop_r1(const Potential &pot) {
+  return pot.kind == kTersoff ? pot.tp.r1 : pot.kind == kBrenner ? pot.bp.r1 : pot.kp.r1;
+}
+const double *bop_r2(const Potential &pot) {
+  return pot.kind == kTersoff ? pot.tp.r2 : pot.kind == kBrenner ? pot.bp.r2 : pot.kp.r2;
+}
+
 double bop_pair_range(const Potential &pot, int t) {
-  const double *r2 = pot.kind == kTersoff ? pot.tp.r2 : pot.kp.r2;
+  const double *r2 = bop_r2(pot);
   if (!pot.screened) return r2[t];
   const int np = pot_nel(pot) * (pot_nel(pot) + 1) / 2;
   double mx = 0.0;
   for (int q = 0; q < np; q++) {
+    if (pot.kind == kBrenner && q != t) continue;  // BrennerScr: the pair's own cutoffs
     const double m = std::max(std::max(r2[q], pot.scr.or2[q]), pot.scr.bor2[q]);
     mx = std::max(mx, m * m);
   }
@@ -193,11 +282,13 @@ double bop_pair_range(const Potential &pot, int t) {
 int pot_nel(const Potential &pot) {
   if (pot.kind == kTersoff) return pot.tp.nel;
   if (pot.kind == kKumagai) return 1;
+  if (pot.kind == kBrenner) return pot.bp.nel;
   return pot.eam->nel;
 }
 int pot_Z(const Potential &pot, int q) {
   if (pot.kind == kTersoff) return pot.tp.Z[q];
   if (pot.kind == kKumagai) return pot.kp.Z[q];
+  if (pot.kind == kBrenner) return pot.bp.Z[q];
   return pot.eam->Z[q];
 }
 
@@ -718,6 +809,33 @@ int gb_kumagai_scr_new(gb_potential_t **h, const gb_kumagai_params_t *params,
   return 0;
 }
 
+int gb_brenner_new(gb_potential_t **h, const gb_brenner_params_t *params) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_brenner_params_t p = params ? *params : default_brenner();
+  GB_CHECK(check_brenner(p));
+  *h = new gb_potential;
+  (*h)->pot.kind = kBrenner;
+  (*h)->pot.bp = p;
+  return 0;
+}
+
+int gb_brenner_scr_new(gb_potential_t **h, const gb_brenner_params_t *params,
+                       const gb_screening_params_t *scr) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_brenner_params_t p = params ? *params : default_brenner_scr();
+  gb_screening_params_t sc = scr ? *scr : default_screening_tersoff();
+  GB_CHECK(check_brenner(p));
+  GB_CHECK(check_screening(sc, p.nel * (p.nel + 1) / 2));
+  *h = new gb_potential;
+  (*h)->pot.kind = kBrenner;
+  (*h)->pot.bp = p;
+  (*h)->pot.screened = true;
+  (*h)->pot.scr = sc;
+  return 0;
+}
+
 int gb_tabulated_eam_new(gb_potential_t **h, const char *fn) {
   clear_error();
   if (!h || !fn) return GB_ERROR_ARGUMENT;
@@ -857,6 +975,16 @@ int gb_kumagai_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
   return gb_potential_bind_to(h, p, nl, ierror);
 }
 int gb_kumagai_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                 const double *q, double *epot, double *f, double *wpot,
+                                 const int *mask, double *epa, double *epb, double *fpb,
+                                 double *wpa, double *wpb, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
+                                        ierror);
+}
+int gb_brenner_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl, int *ierror) {
+  return gb_potential_bind_to(h, p, nl, ierror);
+}
+int gb_brenner_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
                                  const double *q, double *epot, double *f, double *wpot,
                                  const int *mask, double *epa, double *epb, double *fpb,
                                  double *wpa, double *wpb, int *ierror) {

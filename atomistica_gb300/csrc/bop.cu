@@ -617,6 +617,23 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
   return 0;
 }
 
+// Calls f with the device functor of the potential's bond-order form and
+// returns its result.
+template <class F>
+int with_bop(const Potential &pot, F &&f) {
+  switch (pot.kind) {
+    case kTersoff:
+      return f(TersoffPot{make_tersoff_dev(pot.tp)});
+    case kKumagai:
+      return f(KumagaiPot{make_kumagai_dev(pot.kp)});
+    case kBrenner:
+      return f(BrennerPot{make_brenner_dev(pot.bp)});
+    default:
+      set_error("not a bond-order potential");
+      return GB_ERROR_ARGUMENT;
+  }
+}
+
 // R = double: FP64 drop-in; R = float: mixed form (posff: ff positions).
 template <class Pot, class R>
 int dispatch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int ntiles,
@@ -786,15 +803,12 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
   args.frbond = want_pb ? pot.bond_fr.as<double>() : nullptr;
   args.tile_part = pot.tile_part.as<double>();
   GB_CUDA(cudaEventRecord(pot.kev[0], s));
-  if (pot.kind == kTersoff) {
-    const ScrDev sd = make_scr_dev(pot.tp.r1, pot.tp.r2, pot.tp.nel * (pot.tp.nel + 1) / 2,
-                                   pot.scr);
-    GB_CHECK(launch_scr(args, TersoffPot{make_tersoff_dev(pot.tp)}, sd, blocks, o.status,
-                        want_wat, want_pb, s));
-  } else {
-    const ScrDev sd = make_scr_dev(pot.kp.r1, pot.kp.r2, 1, pot.scr);
-    GB_CHECK(launch_scr(args, KumagaiPot{make_kumagai_dev(pot.kp)}, sd, blocks, o.status,
-                        want_wat, want_pb, s));
+  {
+    const ScrDev sd = make_scr_dev(bop_r1(pot), bop_r2(pot),
+                                   pot_nel(pot) * (pot_nel(pot) + 1) / 2, pot.scr);
+    GB_CHECK(with_bop(pot, [&](const auto &P) {
+      return launch_scr(args, P, sd, blocks, o.status, want_wat, want_pb, s);
+    }));
   }
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(false, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
@@ -907,19 +921,13 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   }
   const float4 *posff = mixed ? nl.posff.as<float4>() : nullptr;
   if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[0], s));
-  if (pot.kind == kTersoff) {
-    TersoffPot tp{make_tersoff_dev(pot.tp)};
-    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, max_nbt, max_ntrip,
-                                                  status, want_wat, want_pb, s, &rows)
-               : dispatch_tile<TersoffPot, double>(args, tp, posff, ntiles, max_nbt, max_ntrip,
-                                                   status, want_wat, want_pb, s, &rows);
-  } else {
-    KumagaiPot kp{make_kumagai_dev(pot.kp)};
-    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, posff, ntiles, max_nbt, max_ntrip,
-                                                  status, want_wat, want_pb, s, &rows)
-               : dispatch_tile<KumagaiPot, double>(args, kp, posff, ntiles, max_nbt, max_ntrip,
-                                                   status, want_wat, want_pb, s, &rows);
-  }
+  rc = with_bop(pot, [&](const auto &P) {
+    using PotT = std::decay_t<decltype(P)>;
+    return mixed ? dispatch_tile<PotT, float>(args, P, posff, ntiles, max_nbt, max_ntrip, status,
+                                              want_wat, want_pb, s, &rows)
+                 : dispatch_tile<PotT, double>(args, P, posff, ntiles, max_nbt, max_ntrip, status,
+                                               want_wat, want_pb, s, &rows);
+  });
   GB_CHECK(rc);
   if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
@@ -963,11 +971,12 @@ int ctas_per_sm(int threads, size_t smem) {
 
 int bop_tile_ctas_per_sm(const Potential &pot, size_t smem) {
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
-  if (pot.kind == kTersoff)
-    return mixed ? ctas_per_sm<bop_tile_mx<TersoffPot, false, false>>(kMxThreads, smem)
-                 : ctas_per_sm<bop_tile<TersoffPot, double, false, false>>(kBopThreads, smem);
-  return mixed ? ctas_per_sm<bop_tile_mx<KumagaiPot, false, false>>(kMxThreads, smem)
-               : ctas_per_sm<bop_tile<KumagaiPot, double, false, false>>(kBopThreads, smem);
+  const int n = with_bop(pot, [&](const auto &P) {
+    using PotT = std::decay_t<decltype(P)>;
+    return mixed ? ctas_per_sm<bop_tile_mx<PotT, false, false>>(kMxThreads, smem)
+                 : ctas_per_sm<bop_tile<PotT, double, false, false>>(kBopThreads, smem);
+  });
+  return std::max(n, 0);
 }
 
 int bop_batch_apt(int maxz) {
@@ -988,7 +997,7 @@ int bop_batch_apt(int maxz) {
 // has already reserved the device memory for its own pool (so cudaMalloc
 // fails or would fragment that pool), and MD loops that must not allocate —
 // or implicitly synchronise the device — inside a time step.  For them
-// gb_bop_energy_and_forces_noalloc evaluates Tersoff or Kumagai on a
+// gb_bop_energy_and_forces_noalloc evaluates Tersoff, Kumagai or Brenner on a
 // neighbour list the caller supplies, using only the file-scope scratch array
 // below for every intermediate buffer.  The array is sized for at most
 // kNoallocMaxAtoms atoms and kNoallocMaxEntries list entries; every GPU that
@@ -1129,9 +1138,9 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
     return GB_ERROR_ARGUMENT;
   }
   Potential &pot = h->pot;
-  if ((pot.kind != kTersoff && pot.kind != kKumagai) || pot.screened) {
-    set_error("noalloc: only the non-screened bond-order potentials (Tersoff, Kumagai) are "
-              "supported");
+  if ((pot.kind != kTersoff && pot.kind != kKumagai && pot.kind != kBrenner) || pot.screened) {
+    set_error("noalloc: only the non-screened bond-order potentials (Tersoff, Kumagai, "
+              "Brenner) are supported");
     return GB_ERROR_ARGUMENT;
   }
   if (nat < 0 || nat > kNoallocMaxAtoms) {
@@ -1174,9 +1183,9 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   double *G = reinterpret_cast<double *>(base + kNaG);
   double *ebond = reinterpret_cast<double *>(base + kNaE);
   double *part = reinterpret_cast<double *>(base + kNaPart);
-  const int nel = pot.kind == kTersoff ? pot.tp.nel : 1;
-  const int *pz = pot.kind == kTersoff ? pot.tp.Z : pot.kp.Z;
-  const int z0 = pz[0], z1 = nel > 1 ? pz[1] : -1, z2 = nel > 2 ? pz[2] : -1;
+  const int nel = pot_nel(pot);
+  const int z0 = pot_Z(pot, 0), z1 = nel > 1 ? pot_Z(pot, 1) : -1,
+            z2 = nel > 2 ? pot_Z(pot, 2) : -1;
   noalloc_prepare<<<(nat + 1 + 127) / 128, 128, 0, s>>>(nat, r, Z, nel, z0, z1, z2, seed, pos, el,
                                                        seed32, status);
   note_launch();
@@ -1241,20 +1250,14 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
     bop_posff<<<(nat + 127) / 128, 128, 0, s>>>(nat, pos, posff);
     note_launch();
   }
-  int rc, rows = ntiles;
-  if (pot.kind == kTersoff) {
-    TersoffPot tp{make_tersoff_dev(pot.tp)};
-    rc = mixed ? dispatch_tile<TersoffPot, float>(args, tp, posff, ntiles, hp[0], hp[1],
-                                                  status + 2, false, false, s, &rows)
-               : dispatch_tile<TersoffPot, double>(args, tp, posff, ntiles, hp[0], hp[1],
-                                                   status + 2, false, false, s, &rows);
-  } else {
-    KumagaiPot kp{make_kumagai_dev(pot.kp)};
-    rc = mixed ? dispatch_tile<KumagaiPot, float>(args, kp, posff, ntiles, hp[0], hp[1],
-                                                  status + 2, false, false, s, &rows)
-               : dispatch_tile<KumagaiPot, double>(args, kp, posff, ntiles, hp[0], hp[1],
-                                                   status + 2, false, false, s, &rows);
-  }
+  int rows = ntiles;
+  const int rc = with_bop(pot, [&](const auto &P) {
+    using PotT = std::decay_t<decltype(P)>;
+    return mixed ? dispatch_tile<PotT, float>(args, P, posff, ntiles, hp[0], hp[1], status + 2,
+                                              false, false, s, &rows)
+                 : dispatch_tile<PotT, double>(args, P, posff, ntiles, hp[0], hp[1], status + 2,
+                                               false, false, s, &rows);
+  });
   GB_CHECK(rc);
   GB_CHECK(launch_gather(mixed, nat, seed32, rev, G, ebond, nullptr, f, nullptr, nullptr, s));
   GB_CHECK(reduce_partials(part, rows, 10, red, nullptr, s));

@@ -4,6 +4,8 @@
 //
 //   Tersoff   src/potentials/bop/tersoff/tersoff_func.f90:32-232
 //   Kumagai   src/potentials/bop/kumagai/kumagai_func.f90:32-242
+//   Brenner   src/potentials/bop/brenner/brenner_func.f90:32-225, derived
+//             constants brenner_module.f90:196-214
 //   trig_off  src/support/cutoff.f90:152-196
 //   pair idx  src/macros.inc:123
 //
@@ -11,7 +13,8 @@
 // arithmetic):
 //   * Tersoff g = omega*(1 + c^2/d^2 - c^2/(d^2+(h-cos)^2)) is evaluated as
 //     omega*(1 + c^2 (h-cos)^2 / (d^2 (d^2+(h-cos)^2))): for Si, c^2/d^2 ~ 4e7
-//     and the reference form cancels three digits.
+//     and the reference form cancels three digits.  The Brenner g (h + cos,
+//     constants of the (i,k) pair) is the same function of hc = -h - cos.
 //   * bo powers use exp(n log z): z^(n-1) = z^n / z, arg^(e-1) = arg^e / arg.
 #pragma once
 
@@ -74,6 +77,48 @@ struct KumagaiDev {
   double c1[1], c2[1], c3[1], c4[1], c5[1], h[1];
   double r1[1], r2[1], r1sq[1], r2sq[1], fac[1];
 };
+
+// Brenner form: every constant per symmetric pair; VR = VR_f e^{-expR (r-r0)},
+// VA = -VA_f e^{-expA (r-r0)}, g from (gamma, c, d, -h) of the (i,k) pair,
+// b = (1 + zeta^n)^bo_exp of the (i,j) pair, h(dr) as Tersoff with (mu, m).
+struct BrennerDev {
+  int nel;
+  double r0[6], VR_f[6], VA_f[6], expR[6], expA[6];
+  double gamma[6], c2[6], d2[6], c2d2inv[6], hneg[6];
+  double n[6], bo_exp[6], bo_fac[6];
+  double mu[6];
+  int m[6];
+  double r1[6], r2[6], r1sq[6], r2sq[6], fac[6];
+};
+
+inline BrennerDev make_brenner_dev(const gb_brenner_params_t &p) {
+  BrennerDev d{};
+  d.nel = p.nel;
+  const int np = p.nel * (p.nel + 1) / 2;
+  for (int q = 0; q < np; q++) {
+    d.r0[q] = p.r0[q];
+    d.expR[q] = p.beta[q] * std::sqrt(2 * p.S[q]);
+    d.expA[q] = p.beta[q] * std::sqrt(2 / p.S[q]);
+    d.VR_f[q] = p.D0[q] / (p.S[q] - 1);
+    d.VA_f[q] = p.S[q] * p.D0[q] / (p.S[q] - 1);
+    d.gamma[q] = p.gamma[q];
+    d.c2[q] = p.c[q] * p.c[q];
+    d.d2[q] = p.d[q] * p.d[q];
+    d.c2d2inv[q] = d.c2[q] / d.d2[q];
+    d.hneg[q] = -p.h[q];
+    d.n[q] = p.n[q];
+    d.bo_exp[q] = -0.5 / p.n[q];
+    d.bo_fac[q] = 0.5 * d.bo_exp[q] * p.n[q];
+    d.mu[q] = p.mu[q];
+    d.m[q] = p.m[q];
+    d.r1[q] = p.r1[q];
+    d.r2[q] = p.r2[q];
+    d.r1sq[q] = p.r1[q] * p.r1[q];
+    d.r2sq[q] = p.r2[q] * p.r2[q];
+    d.fac[q] = M_PI / (p.r2[q] - p.r1[q]);
+  }
+  return d;
+}
 
 inline TersoffDev make_tersoff_dev(const gb_tersoff_params_t &p) {
   TersoffDev d{};
@@ -155,6 +200,8 @@ GB_HD void trig_off(double r, double r1, double r2, double fac, double &val, dou
 }
 
 struct TersoffPot {
+  // g and b constants per centre element (false) or per element pair (true)
+  static constexpr bool kPairTerms = false;
   TersoffDev p;
   GB_HD int nel() const { return p.nel; }
   GB_HD double r1(int t) const { return p.r1[t]; }
@@ -195,7 +242,8 @@ struct TersoffPot {
     val = om * (R(1) + (R)p.c2d2inv[eli] * hc * hc * inv);
     dval = R(-2) * om * (R)p.c2[eli] * hc * inv * inv;
   }
-  GB_HD double hpar(int eli) const { return p.h[eli]; }
+  // h - cos theta is the argument of g_hc (centre element; the pair is unused)
+  GB_HD double hpar(int eli, int /*ikpot*/) const { return p.h[eli]; }
   // h(r_ij - r_ik) (tersoff_func.f90:168-211), pair (i,k).
   template <class R>
   GB_HD void h(int ikpot, R dr, R &val, R &dval) const {
@@ -254,8 +302,9 @@ struct TersoffPot {
 };
 
 struct KumagaiPot {
+  static constexpr bool kPairTerms = false;
   KumagaiDev p;
-  GB_HD double hpar(int eli) const { return p.h[eli]; }
+  GB_HD double hpar(int eli, int /*ikpot*/) const { return p.h[eli]; }
   // g as a function of hc = h - cos theta.
   template <class R>
   GB_HD void g_hc(int eli, int /*ikpot*/, R hcos, R &val, R &dval) const {
@@ -344,6 +393,84 @@ struct KumagaiPot {
       const R ad = gexp<R>(delta * glog<R>(arg));
       b = ad;
       dfb = R(0.5) * fc * VA * eta * (ze / z) * delta * (ad / arg);
+    } else {
+      b = R(1);
+      dfb = R(0);
+    }
+  }
+};
+
+struct BrennerPot {
+  static constexpr bool kPairTerms = true;
+  BrennerDev p;
+  GB_HD int nel() const { return p.nel; }
+  GB_HD double r1(int t) const { return p.r1[t]; }
+  GB_HD double r2(int t) const { return p.r2[t]; }
+  GB_HD double r1sq(int t) const { return p.r1sq[t]; }
+  GB_HD double r2sq(int t) const { return p.r2sq[t]; }
+  GB_HD double fac(int t) const { return p.fac[t]; }
+  // VA, VR (brenner_func.f90:32-78)
+  GB_HD void VA(int t, double r, double &v, double &dv) const {
+    const double ex = exp(-p.expA[t] * (r - p.r0[t]));
+    v = -p.VA_f[t] * ex;
+    dv = p.VA_f[t] * p.expA[t] * ex;
+  }
+  GB_HD void VR(int t, double r, double &v, double &dv) const {
+    const double ex = exp(-p.expR[t] * (r - p.r0[t]));
+    v = p.VR_f[t] * ex;
+    dv = -p.VR_f[t] * p.expR[t] * ex;
+  }
+  // g as a function of hc = -h - cos theta of the (i,k) pair
+  template <class R>
+  GB_HD void g_hc(int /*eli*/, int ikpot, R hc, R &val, R &dval) const {
+    const R ga = (R)p.gamma[ikpot];
+    const R inv = R(1) / ((R)p.d2[ikpot] + hc * hc);
+    val = ga * (R(1) + (R)p.c2d2inv[ikpot] * hc * hc * inv);
+    dval = R(-2) * ga * (R)p.c2[ikpot] * hc * inv * inv;
+  }
+  // g(cos theta) (brenner_func.f90:86-103)
+  template <class R>
+  GB_HD void g(int eli, int ikpot, R cs, R &val, R &dval) const {
+    g_hc<R>(eli, ikpot, (R)p.hneg[ikpot] - cs, val, dval);
+  }
+  GB_HD double hpar(int /*eli*/, int ikpot) const { return p.hneg[ikpot]; }
+  // h (brenner_func.f90:178-214), pair (i,k)
+  template <class R>
+  GB_HD void h(int ikpot, R dr, R &val, R &dval) const {
+    const double mu = p.mu[ikpot];
+    if (mu == 0.0) {
+      val = R(1);
+      dval = R(0);
+      return;
+    }
+    const int m = p.m[ikpot];
+    const R mu2 = R(2) * (R)mu;
+    if (m == 1) {
+      val = gexp<R>(mu2 * dr);
+      dval = mu2 * val;
+    } else {
+      const R arg = mu2 * dr;
+      R pw = R(1);
+      for (int q = 0; q < m - 1; q++) pw *= arg;
+      val = gexp<R>(pw * arg);
+      dval = mu2 * R(m) * pw * val;
+    }
+  }
+  // bo (brenner_func.f90:122-170) of the (i,j) pair: b = (1 + zeta^n)^(-1/(2n)),
+  // dfb = -1/4 fc VA zeta^(n-1) (1 + zeta^n)^(-1/(2n)-1); n = 1 without the
+  // zeta > 0 test.
+  template <class R>
+  GB_HD void bo(int /*eli*/, int t, R z, R fc, R VA, R &b, R &dfb) const {
+    const R e = (R)p.bo_exp[t];
+    if (p.n[t] == 1.0) {
+      const R arg = R(1) + z;
+      b = gexp<R>(e * glog<R>(arg));
+      dfb = (R)p.bo_fac[t] * fc * VA * (b / arg);
+    } else if (z > R(0)) {
+      const R zn = gexp<R>((R)p.n[t] * glog<R>(z));
+      const R arg = R(1) + zn;
+      b = gexp<R>(e * glog<R>(arg));
+      dfb = (R)p.bo_fac[t] * fc * VA * (zn / z) * (b / arg);
     } else {
       b = R(1);
       dfb = R(0);

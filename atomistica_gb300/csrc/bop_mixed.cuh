@@ -46,12 +46,26 @@ struct MxElem {
   ff c1, kc2, c3, c4, c5;          // Kumagai g
   float sens;                      // |d ln b / d ln x| prefactor (|e n|, |delta eta|)
 };
+// el[] holds the g and bond-order constants per centre element (Tersoff,
+// Kumagai) or per element pair (Brenner: g of the (i,k) pair, b of the (i,j)
+// pair; the kernels index it through el_g / el_b).
 struct MxParams {
-  int kind;  // 0 Tersoff, 1 Kumagai
+  int kind;  // 0 Tersoff and Brenner, 1 Kumagai
   MxPair pr[6];
-  MxElem el[3];
+  MxElem el[6];
   ff A[3][3];
 };
+
+// Index into MxParams::el of the g constants (centre element eli, pair ikpot)
+// and of the bond-order constants (pair t); kPP: per-pair constants.
+template <bool kPP>
+__host__ __device__ __forceinline__ int el_g(int eli, int ikpot) {
+  return kPP ? ikpot : eli;
+}
+template <bool kPP>
+__host__ __device__ __forceinline__ int el_b(int eli, int t) {
+  return kPP ? t : eli;
+}
 
 inline ff ffh(double d) { return ff_from_double(d); }
 
@@ -91,6 +105,41 @@ inline MxParams make_mx(const TersoffDev &d, const double A[3][3]) {
     e.d2 = ffh(d.d2[q]);
     e.c2d2 = ffh(d.c2d2inv[q]);
     e.sens = (float)std::fabs(d.e[q] * d.n[q]);
+  }
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 3; k++) m.A[a][k] = ffh(A[a][k]);
+  return m;
+}
+
+// Brenner: VA = -Bc e^{-cA r} with Bc = VA_f e^{expA r0} (and VR alike), the
+// Tersoff g with gamma for omega and -h for h, the Tersoff b with beta = xi = 1
+// and the pair's n; all constants per pair.
+inline MxParams make_mx(const BrennerDev &d, const double A[3][3]) {
+  MxParams m{};
+  m.kind = 0;
+  const int np = d.nel * (d.nel + 1) / 2;
+  for (int q = 0; q < np; q++) {
+    MxPair &pq = m.pr[q];
+    pq.cA = ffh(d.expA[q]);
+    pq.cR = ffh(d.expR[q]);
+    pq.Ac = ffh(d.VR_f[q] * std::exp(d.expR[q] * d.r0[q]));
+    pq.Bc = ffh(d.VA_f[q] * std::exp(d.expA[q] * d.r0[q]));
+    pq.xi = ffh(1.0);
+    mx_cutoffs(pq, d.r1[q], d.r2[q], d.fac[q]);
+    pq.hae = ffh(1.0);
+    pq.had = ffh(1.0);
+    pq.hs = ffh(2.0 * d.mu[q]);
+    pq.hm = d.mu[q] == 0.0 ? 0 : d.m[q];
+    pq.om = ffh(d.gamma[q]);
+    MxElem &e = m.el[q];
+    e.n = ffh(d.n[q]);
+    e.lbetan = ffh(0.0);
+    e.e = ffh(d.bo_exp[q]);
+    e.h = ffh(d.hneg[q]);
+    e.c2 = ffh(d.c2[q]);
+    e.d2 = ffh(d.d2[q]);
+    e.c2d2 = ffh(d.c2d2inv[q]);
+    e.sens = (float)std::fabs(d.bo_exp[q] * d.n[q]);
   }
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) m.A[a][k] = ffh(A[a][k]);
@@ -188,6 +237,7 @@ __device__ inline MxLayout carve_mx(unsigned char *sm, int nbt, int ntrip) {
 }
 
 // ---- Three-body functions on the MxParams copies of the parameters. ----
+// Their element argument is the index into MxParams::el (el_g / el_b).
 // g as a function of hc = h - cos theta, and d g / d cos theta
 // (tersoff_func.f90:86-114 in the stable form g = omega (1 + c^2 hc^2 /
 // (d^2 (d^2 + hc^2))); kumagai_func.f90:86-131).
@@ -325,14 +375,14 @@ __device__ __forceinline__ void bo_hot(const MxParams &mp, int eli, int t, ff P0
 // Three-body k loop of bond lb in FP32 (h - cos theta from an ff dot
 // product, bop_kernel.f90:1171-1343).  Also returns sum_k |d zeta/d r_k| for
 // the error estimate.
-template <bool kWat>
+template <bool kWat, bool kPP>
 __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, int lb, int s,
                                          int z, int eli, ff *trow, float &zeta, float dbj[3],
                                          float wk[9], float &sumdk) {
   const int nbt = L.nbt, ntrip = L.ntrip;
   const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
   const float rlij = L.r[lb].hi, rinvj = L.rinv[lb].hi;
-  const ff h = mp.el[eli].h;
+  const ff h0 = mp.el[eli].h;
   for (int q = 0; q < z; q++) {
     const int lk = s + q;
     if (lk == lb) continue;
@@ -360,12 +410,13 @@ __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, 
     clo = fmaf(rnik[2].hi, rnij[2].lo, clo);
     clo = fmaf(rnik[2].lo, rnij[2].hi, clo);
     const float cs = s2.hi + clo;
+    const ff h = kPP ? mp.el[ikpot].h : h0;
     const ff dh0 = two_sum(h.hi, -s2.hi);
     const float hcf = dh0.hi + ((dh0.lo + h.lo) - clo);
     float hv, dh;
     h_f(mp.pr[ikpot], rlij - rlik, hv, dh);
     float gv, dg;
-    g_f(mp, eli, ikpot, hcf, gv, dg);
+    g_f(mp, el_g<kPP>(eli, ikpot), ikpot, hcf, gv, dg);
     const float dzfac = fcik * dg * hv;
     zeta += fcik * gv * hv;
     const float dzdrij = gv * fcik * dh;
@@ -390,14 +441,14 @@ __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, 
 // The same k loop in ff arithmetic for the hot bonds, over the slots
 // q = q0, q0 + dq, ... of bond lb's row (the partial sums of zeta, d zeta /
 // d r_j and the virial term are added up across the lanes afterwards).
-template <bool kWat>
+template <bool kWat, bool kPP>
 __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, int lb, int s,
                                          int z, int eli, ff *trow, const ff *etab, int q0,
                                          int dq, ff &zeta, ff dbj[3], ff wk[9]) {
   const int nbt = L.nbt, ntrip = L.ntrip;
   const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
   const ff rlij = L.r[lb], rinvj = L.rinv[lb];
-  const ff h = mp.el[eli].h;
+  const ff h0 = mp.el[eli].h;
   for (int q = q0; q < z; q += dq) {
     const int lk = s + q;
     if (lk == lb) continue;
@@ -417,7 +468,8 @@ __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, 
     cs = ff_add(cs, ff_mul(rnik[1], rnij[1]));
     cs = ff_add(cs, ff_mul(rnik[2], rnij[2]));
     ff gv, dg;
-    g_ff(mp, eli, ikpot, ff_sub(h, cs), etab, gv, dg);
+    g_ff(mp, el_g<kPP>(eli, ikpot), ikpot, ff_sub(kPP ? mp.el[ikpot].h : h0, cs), etab, gv,
+         dg);
     const ff fh = ff_mul(fcik, hv);
     const ff dzfac = ff_mul(fh, dg);
     zeta = ff_add(zeta, ff_mul(fh, gv));
@@ -714,18 +766,19 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       if (kWat)
 #pragma unroll
         for (int c = 0; c < 9; c++) wk[c] = 0.0f;
-      kloop_mx<kWat>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
+      kloop_mx<kWat, Pot::kPairTerms>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
       // A zeta below 1e-30 would overflow the FP32 range inside ln/exp: such a
       // bond (and any non-finite estimate) takes the accurate path.
       const bool tiny = zeta > 0.0f && zeta < 1.0e-30f;
       ff bij, P, x0;
       float L0;
-      bo_f(mp, eli, t, tiny ? 1.0f : zeta, L.fc[lb], VA, s_exp, bij, P, x0, L0);
+      const int eb = el_b<Pot::kPairTerms>(eli, t);
+      bo_f(mp, eb, t, tiny ? 1.0f : zeta, L.fc[lb], VA, s_exp, bij, P, x0, L0);
       // Error estimate (eV/A) of this bond's forces on the FP32 path: the FP32
       // zeta through d b / d ln zeta, the FP32 log1p/expm1 of b, and the FP32
       // three-body derivatives multiplied by P.
       const float fva = fabsf(dVA.hi) * L.fc[lb].hi;
-      const float est = fva * (2.4e-7f * bsens_f(mp, eli, zeta) +
+      const float est = fva * (2.4e-7f * bsens_f(mp, eb, zeta) +
                                1.5e-7f * fabsf(bij.hi - mp.pr[t].xi.hi)) +
                         3.0e-7f * fabsf(P.hi) *
                             (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
@@ -769,8 +822,8 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
           lb = L.hot[hq];
           const int ai = L.meta[lb] & 0xff;
           const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-          kloop_ff<kWat>(mp, L, lb, s, z, L.el[ai], L.t + L.toff[ai] + p * z, s_exp, gl,
-                         kHotLanes, zeta, dbj, wk);
+          kloop_ff<kWat, Pot::kPairTerms>(mp, L, lb, s, z, L.el[ai], L.t + L.toff[ai] + p * z,
+                                          s_exp, gl, kHotLanes, zeta, dbj, wk);
         }
 #pragma unroll
         for (int o = 1; o < kHotLanes; o <<= 1) {
@@ -794,8 +847,8 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
           ff bij, P;
           const ff zl = L.G[2 * nbt + lb];  // (FP32-pass zeta, L0)
           if (zl.hi > 0.0f && zeta.hi > 1.0e-30f) {
-            bo_hot(mp, eli, t, L.G[lb], L.G[nbt + lb], zl.hi, zl.lo, (zeta.hi - zl.hi) + zeta.lo,
-                   s_exp, bij, P);
+            bo_hot(mp, el_b<Pot::kPairTerms>(eli, t), t, L.G[lb], L.G[nbt + lb], zl.hi, zl.lo,
+                   (zeta.hi - zl.hi) + zeta.lo, s_exp, bij, P);
           } else {
             // FP64 bond order for a vanishing zeta (outside the FP32 range of ln/exp)
             double b64, P64;

@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(kScrThreads)
           pot.template h<double>(ikpot, rlij - rlik, h_Dr, dh_dDr);
           const double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
           double g_costh, dg_dcosth;
-          pot.template g_hc<double>(eli, ikpot, pot.hpar(eli) - costh, g_costh, dg_dcosth);
+          pot.template g_hc<double>(eli, ikpot, pot.hpar(eli, ikpot) - costh, g_costh, dg_dcosth);
           double dkc[3];
 #pragma unroll
           for (int c = 0; c < 3; c++) dkc[c] = rnik[c] * rlik - rnij[c] * rlij;
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(kScrThreads)
             pot.template h<double>(ikpot, rlij - rlik, h_Dr, dh_dDr);
             const double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
             double g_costh, dg_dcosth;
-            pot.template g_hc<double>(eli, ikpot, pot.hpar(eli) - costh, g_costh, dg_dcosth);
+            pot.template g_hc<double>(eli, ikpot, pot.hpar(eli, ikpot) - costh, g_costh, dg_dcosth);
             double dkc[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) dkc[c] = rnik[c] * rlik - rnij[c] * rlij;

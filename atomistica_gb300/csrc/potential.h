@@ -11,7 +11,7 @@
 
 namespace gb {
 
-enum PotKind { kTersoff = 0, kKumagai = 1, kEAM = 2 };
+enum PotKind { kTersoff = 0, kKumagai = 1, kEAM = 2, kBrenner = 3 };
 
 // Uniform natural cubic spline tables (simple_spline.f90:127-195) built on the
 // host.  Device layout: 8 doubles per interval k = {y_k, c1_k, c2_k, c3_k,
@@ -71,7 +71,8 @@ struct Potential {
   int precision = GB_PRECISION_FP64;
   gb_tersoff_params_t tp{};
   gb_kumagai_params_t kp{};
-  bool screened = false;        // TersoffScr / KumagaiScr
+  gb_brenner_params_t bp{};
+  bool screened = false;        // TersoffScr / KumagaiScr / BrennerScr
   gb_screening_params_t scr{};  // their outer / bond-order cutoffs, Cmin, Cmax
   std::unique_ptr<EamTables> eam;
 
@@ -108,7 +109,8 @@ struct Potential {
 
 // Interaction range requested by bind_to for element pair t (database
 // indices): r2, or for the screened variants sqrt(C_dr_cut(t)) times the
-// largest cutoff of all pairs (default_bind_to_func.f90:117-144).
+// largest cutoff of all pairs (default_bind_to_func.f90:117-144; BrennerScr:
+// of pair t itself, brenner_module.f90:229-243).
 double bop_pair_range(const Potential &pot, int t);
 
 // Kernel launches (on pot.stream) for an up-to-date neighbour list.
@@ -119,6 +121,9 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 // Element count / atomic number of element q of the potential; its stream.
 int pot_nel(const Potential &pot);
 int pot_Z(const Potential &pot, int q);
+// Inner cutoffs r1, r2 per pair of a bond-order potential.
+const double *bop_r1(const Potential &pot);
+const double *bop_r2(const Potential &pot);
 cudaStream_t pot_stream(Potential &pot);
 
 // Deterministic fixed-order sum of tile partials: red[c] = sum_t part[t*nc+c].

@@ -26,7 +26,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import GB_PRECISION_FP64, GB_PRECISION_MIXED, check, load
-from .parameters import (SCREENING_KEYS, Kumagai_CompMaterSci_39_457_Si,
+from .parameters import (BRENNER_KEYS, SCREENING_KEYS, Erhart_PRB_71_035211_SiC,
+                         Kumagai_CompMaterSci_39_457_Si,
                          Kumagai_CompMaterSci_39_457_Si__Scr, Tersoff_PRB_39_5566_Si_C,
                          Tersoff_PRB_39_5566_Si_C__Scr, atomic_numbers)
 
@@ -231,6 +232,42 @@ def screening_params(params, base):
     p = _lib.ScreeningParams()
     for k in SCREENING_KEYS:
         _fill(getattr(p, k), [float(v) for v in d[k]], len(d[k]))
+    return p
+
+
+# The compiled-in default of BrennerScr (brenner_params.f90:92-104 under
+# SCREENING), the base that keyword arguments override; it differs from the
+# front-end's Erhart_PRB_71_035211_SiC__Scr dictionary in the C-Si cutoffs.
+_BRENNER_SCR_DEFAULT = dict(
+    Erhart_PRB_71_035211_SiC,
+    mu=[1.0 / 1.4276, 1.0 / 1.79, 1.0 / 1.842], m=[3, 3, 3],
+    r1=[2.00, (2.00 * 2.50) ** 0.5, 2.50],
+    r2=[2.00 * 1.2, (2.00 * 2.50) ** 0.5 * 1.2, 2.50 * 1.2],
+    or1=[2.00, (2.00 * 3.00) ** 0.5, 3.00], or2=[2.00 * 2.0, (2.00 * 3.00) ** 0.5 * 2.0, 6.0],
+    bor1=[2.00, (2.00 * 3.00) ** 0.5, 3.00], bor2=[2.00 * 2.0, (2.00 * 3.00) ** 0.5 * 2.0, 6.0],
+    Cmin=[1.0, 1.0, 1.0], Cmax=[3.0, 3.0, 3.0])
+
+
+def brenner_params(params, base=Erhart_PRB_71_035211_SiC):
+    """gb_brenner_params_t from a parameter dict (every array per element
+    pair); keys not given keep the values of ``base``."""
+    d = dict(base)
+    d.update({k: v for k, v in params.items() if not k.startswith("__")})
+    p = _lib.BrennerParams()
+    els = d["el"]
+    p.nel = len(els)
+    if not 1 <= p.nel <= 3:
+        raise ValueError("Brenner supports 1..3 elements")
+    for q, s in enumerate(els):
+        p.Z[q] = atomic_numbers[s]
+    npair = p.nel * (p.nel + 1) // 2
+    for k in BRENNER_KEYS:
+        if len(d[k]) < npair:
+            raise ValueError("Brenner: %s needs %d entries (one per element pair)" % (k, npair))
+        if k == "m":
+            _fill(p.m, [int(v) for v in d[k]], npair)
+        else:
+            _fill(getattr(p, k), [float(v) for v in d[k]], npair)
     return p
 
 
@@ -458,6 +495,37 @@ class KumagaiScr(_Potential):
         sp = screening_params(params, base)
         check(self._L.gb_kumagai_scr_new(ctypes.byref(self._h), ctypes.byref(p),
                                          ctypes.byref(sp)), "KumagaiScr")
+        self.set_precision(precision)
+
+
+class Brenner(_Potential):
+    """Brenner-form (Albe-Erhart) bond-order potential
+    (src/potentials/bop/brenner/); default Erhart_PRB_71_035211_SiC."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        if params:
+            p = brenner_params(params)
+            check(self._L.gb_brenner_new(ctypes.byref(self._h), ctypes.byref(p)), "Brenner")
+        else:
+            check(self._L.gb_brenner_new(ctypes.byref(self._h), None), "Brenner")
+        self.set_precision(precision)
+
+
+class BrennerScr(_Potential):
+    """Screened Brenner potential (src/potentials/bop/brenner/brenner_scr.f90):
+    FP64 only; default parameters the compiled-in screened Erhart-Albe Si-C
+    set (pass **Erhart_PRB_71_035211_SiC__Scr for the front-end's table)."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        if params:
+            p = brenner_params(params, _BRENNER_SCR_DEFAULT)
+            sp = screening_params(params, _BRENNER_SCR_DEFAULT)
+            check(self._L.gb_brenner_scr_new(ctypes.byref(self._h), ctypes.byref(p),
+                                             ctypes.byref(sp)), "BrennerScr")
+        else:
+            check(self._L.gb_brenner_scr_new(ctypes.byref(self._h), None, None), "BrennerScr")
         self.set_precision(precision)
 
 

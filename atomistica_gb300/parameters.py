@@ -8,8 +8,10 @@ m, lambda1, lambda2, alpha, r1, r2) use the symmetric pair index of
 src/macros.inc:123 (``pair_index`` below, 0-based).
 
 The numerical values are those of the original publications as tabulated in
-src/potentials/bop/tersoff/tersoff_params.f90:99-142 and
-src/potentials/bop/kumagai/kumagai_params.f90:97-132.
+src/potentials/bop/tersoff/tersoff_params.f90:99-142,
+src/potentials/bop/kumagai/kumagai_params.f90:97-132 and
+src/potentials/bop/brenner/brenner_params.f90:67-200 (Brenner-form sets,
+whose arrays are all per element pair).
 """
 
 from math import log, sqrt
@@ -97,6 +99,122 @@ Kumagai_CompMaterSci_39_457_Si__Scr = dict(
 )
 
 SCREENING_KEYS = ("or1", "or2", "bor1", "bor2", "Cmin", "Cmax")
+
+# Brenner-form (Albe-Erhart) bond-order sets for the *Brenner* potential
+# (src/potentials/bop/brenner/brenner_params.f90:67-200,
+# src/python/atomistica/parameters.py:174-276, 346-380).  Every array is per
+# symmetric element pair: VR = D0/(S-1) exp(-beta sqrt(2S) (r-r0)),
+# VA = -S D0/(S-1) exp(-beta sqrt(2/S) (r-r0)),
+# g = gamma (1 + c^2/d^2 - c^2/(d^2 + (h + cos)^2)) of the (i,k) pair,
+# b = (1 + zeta^n)^(-1/(2n)), h(dr) = exp((2 mu dr)^m).
+BRENNER_KEYS = ("D0", "r0", "S", "beta", "gamma", "c", "d", "h", "mu", "n", "m", "r1", "r2")
+
+Erhart_PRB_71_035211_SiC = {
+    "__ref__": "Erhart P., Albe K., Phys. Rev. B 71, 035211 (2005)",
+    "el": ["C", "Si"],
+    "D0": [6.00, 4.36, 3.24],
+    "r0": [1.4276, 1.79, 2.232],
+    "S": [2.167, 1.847, 1.842],
+    "beta": [2.0099, 1.6991, 1.4761],
+    "gamma": [0.11233, 0.011877, 0.114354],
+    "c": [181.910, 273987.0, 2.00494],
+    "d": [6.28433, 180.314, 0.81472],
+    "h": [0.5556, 0.68, 0.259],
+    "mu": [0.0, 0.0, 0.0],
+    "n": [1.0, 1.0, 1.0],
+    "m": [1, 1, 1],
+    "r1": [1.85, 2.20, 2.68],
+    "r2": [2.15, 2.60, 2.96],
+}
+
+# Screened form of the same set (BrennerScr), as the reference's Python
+# front-end tabulates it (parameters.py:196-218).
+Erhart_PRB_71_035211_SiC__Scr = dict(
+    Erhart_PRB_71_035211_SiC,
+    mu=[1.0 / 1.4276, 1.0 / 1.79, 1.0 / 1.842],
+    m=[3, 3, 3],
+    r1=[2.00, 2.40, 2.50],
+    r2=[2.00 * 1.2, 2.40 * 1.2, 2.50 * 1.2],
+    or1=[2.00, 2.40, 3.00],
+    or2=[2.00 * 2.0, 2.40 * 2.0, 3.00 * 2.0],
+    bor1=[2.00, 2.40, 3.00],
+    bor2=[2.00 * 2.0, 2.40 * 2.0, 3.00 * 2.0],
+    Cmin=[1.00, 1.00, 1.00],
+    Cmax=[3.00, 3.00, 3.00],
+)
+
+Albe_PRB_65_195124_PtC = {
+    "__ref__": "Albe K., Nordlund K., Averback R. S., Phys. Rev. B 65, 195124 (2002)",
+    "el": ["Pt", "C"],
+    "D0": [3.683, 5.3, 6.0],
+    "r0": [2.384, 1.84, 1.39],
+    "S": [2.24297, 1.1965, 1.22],
+    "beta": [1.64249, 1.836, 2.1],
+    "gamma": [8.542e-4, 9.7e-3, 2.0813e-4],
+    "c": [34.0, 1.23, 330.0],
+    "d": [1.1, 0.36, 3.5],
+    "h": [1.0, 1.0, 1.0],
+    "mu": [1.335, 0.0, 0.0],
+    "n": [1.0, 1.0, 1.0],
+    "m": [1, 1, 1],
+    "r1": [2.9, 2.5, 1.7],
+    "r2": [3.3, 2.8, 2.0],
+}
+
+Henriksson_PRB_79_114107_FeC = {
+    "__ref__": "Henriksson K.O.E., Nordlund K., Phys. Rev. B 79, 144107 (2009)",
+    "el": ["Fe", "C"],
+    "D0": [1.5, 4.82645134, 6.0],
+    "r0": [2.29, 1.47736510, 1.39],
+    "S": [2.0693109, 1.43134755, 1.22],
+    "beta": [1.4, 1.63208170, 2.1],
+    "gamma": [0.0115751, 0.00205862, 0.00020813],
+    "c": [1.2898716, 8.95583221, 330.0],
+    "d": [0.3413219, 0.72062047, 3.5],
+    "h": [-0.26, 0.87099874, 1.0],
+    "mu": [0.0, 0.0, 0.0],
+    "n": [1.0, 1.0, 1.0],
+    "m": [1, 1, 1],
+    "r1": [2.95, 2.3, 1.70],
+    "r2": [3.35, 2.7, 2.00],
+}
+
+Kioseoglou_PSSb_245_1118_AlN = {
+    "__ref__": "Kioseoglou J., Komninou Ph., Karakostas Th., Phys. Stat. Sol. (b) 245, 1118 "
+               "(2008)",
+    "el": ["N", "Al"],
+    "D0": [9.9100, 3.3407, 1.5000],
+    "r0": [1.1100, 1.8616, 2.4660],
+    "S": [1.4922, 1.7269, 2.7876],
+    "beta": [2.05945, 1.7219, 1.0949],
+    "gamma": [0.76612, 1.1e-6, 0.3168],
+    "c": [0.178493, 100390, 0.0748],
+    "d": [0.20172, 16.2170, 19.5691],
+    "h": [0.045238, 0.5980, 0.6593],
+    "mu": [0.0, 0.0, 0.0],
+    "n": [1.0, 0.7200, 6.0865],
+    "m": [1, 1, 1],
+    "r1": [2.00, 2.19, 3.40],
+    "r2": [2.40, 2.49, 3.60],
+}
+
+# Brenner's carbon potentials I and II without the correction tables
+# (Brenner, Phys. Rev. B 42, 9458 (1990); parameters.py:346-380).
+Brenner_PRB_42_9458_C_I = {
+    "__ref__": "Brenner D., Phys. Rev. B 42, 9458 (1990) [potential I]",
+    "el": ["C"],
+    "D0": [6.325], "r0": [1.315], "S": [1.29], "beta": [1.5], "gamma": [0.011304],
+    "c": [19.0], "d": [2.5], "h": [1.0], "mu": [0.0], "n": [1.0 / (2 * 0.80469)], "m": [1],
+    "r1": [1.70], "r2": [2.00],
+}
+
+Brenner_PRB_42_9458_C_II = {
+    "__ref__": "Brenner D., Phys. Rev. B 42, 9458 (1990) [potential II]",
+    "el": ["C"],
+    "D0": [6.0], "r0": [1.39], "S": [1.22], "beta": [2.1], "gamma": [0.00020813],
+    "c": [330.0], "d": [3.5], "h": [1.0], "mu": [0.0], "n": [1.0 / (2 * 0.5)], "m": [1],
+    "r1": [1.70], "r2": [2.00],
+}
 
 # The 14 continuous Tersoff parameters of a single-element set, in the order
 # used by the parameter-gradient interface.

@@ -78,6 +78,33 @@ def fcc(symbol="Cu", a=3.615, size=(1, 1, 1)):
     return _lattice(_FCC, symbol, a, size)
 
 
+def bcc(symbol="Fe", a=2.87, size=(1, 1, 1)):
+    """Body-centred cubic supercell, 2 atoms per conventional cell."""
+    return _lattice(np.array([[0, 0, 0], [.5, .5, .5]]), symbol, a, size)
+
+
+def sc(symbol="Fe", a=2.4, size=(1, 1, 1)):
+    """Simple cubic supercell, 1 atom per cell."""
+    return _lattice(np.array([[0, 0, 0]]), symbol, a, size)
+
+
+def b1(symbols=("Fe", "C"), a=3.9, size=(1, 1, 1)):
+    """Rock-salt (B1) supercell: first symbol on the fcc sites, second on the
+    fcc sites shifted by a/2 along x."""
+    basis = np.concatenate([_FCC, (_FCC + np.array([.5, 0, 0])) % 1.0])
+    s = _lattice(basis, symbols[0], a, size)
+    s.numbers[np.arange(len(s)) % len(basis) >= 4] = atomic_numbers[symbols[1]]
+    return s
+
+
+def b2(symbols=("W", "C"), a=2.7, size=(1, 1, 1)):
+    """CsCl (B2) supercell: first symbol at the cube corners, second at the
+    centre."""
+    s = bcc(symbols[0], a, size)
+    s.numbers[np.arange(len(s)) % 2 == 1] = atomic_numbers[symbols[1]]
+    return s
+
+
 def b3(symbols=("Si", "C"), a=4.3596, size=(1, 1, 1)):
     """Zinc-blende (B3) supercell: first symbol on the fcc sites."""
     s = diamond(symbols[0], a, size)

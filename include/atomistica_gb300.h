@@ -145,6 +145,19 @@ typedef struct gb_kumagai_params {
   double r1[1], r2[1];
 } gb_kumagai_params_t;
 
+/* Brenner (Albe-Erhart form) parameter set: layout of BOP_DB_TYPE
+ * (src/potentials/bop/brenner/brenner_params.f90:27-65), every array per
+ * symmetric element pair (0-based, src/macros.inc:123): dimer energy D0,
+ * dimer length r0, Pauling slope S, stiffness beta, angular gamma, c, d, h,
+ * bond-order exponents mu, n, m and the cutoff r1 < r2. */
+typedef struct gb_brenner_params {
+  int nel;
+  int Z[3];
+  double D0[6], r0[6], S[6], beta[6], gamma[6], c[6], d[6], h[6], mu[6], n[6];
+  int m[6];
+  double r1[6], r2[6];
+} gb_brenner_params_t;
+
 /* Extra parameters of the screened variants TersoffScr / KumagaiScr
  * (tersoff_params.f90:81-90 under SCREENING), per element pair: outer
  * (attractive/repulsive) cutoff or1 < or2, bond-order cutoff bor1 < bor2 and
@@ -169,6 +182,14 @@ int gb_tersoff_scr_new(gb_potential_t **pot, const gb_tersoff_params_t *params,
 /* python_kumagai_scr_new (kumagai_scr.f90): NULL = the
  * Kumagai_CompMaterSci_39_457_Si__Scr set.  FP64 only. */
 int gb_kumagai_scr_new(gb_potential_t **pot, const gb_kumagai_params_t *params,
+                       const gb_screening_params_t *scr);
+/* python_brenner_new (brenner.f90, brenner_module.f90:26-246): NULL params =
+ * the Erhart_PRB_71_035211_SiC set (brenner_params.f90:67-117).  Rejects
+ * d = 0 and S <= 1 as the reference's bind_to does. */
+int gb_brenner_new(gb_potential_t **pot, const gb_brenner_params_t *params);
+/* python_brenner_scr_new (brenner_scr.f90): NULL params / scr = the
+ * Erhart_PRB_71_035211_SiC__Scr set.  FP64 only. */
+int gb_brenner_scr_new(gb_potential_t **pot, const gb_brenner_params_t *params,
                        const gb_screening_params_t *scr);
 /* python_tabulated_alloy_eam_new + init(fn=...) (tabulated_alloy_eam.f90:147-259):
  * reads a DYNAMO setfl file. */
@@ -239,6 +260,13 @@ int gb_kumagai_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neig
                                  const int *mask, double *epot_per_at, double *epot_per_bond,
                                  double *f_per_bond, double *wpot_per_at,
                                  double *wpot_per_bond, int *ierror);
+int gb_brenner_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                       int *ierror);
+int gb_brenner_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                                 const double *q, double *epot, double *f, double *wpot,
+                                 const int *mask, double *epot_per_at, double *epot_per_bond,
+                                 double *f_per_bond, double *wpot_per_at,
+                                 double *wpot_per_bond, int *ierror);
 int gb_tabulated_alloy_eam_bind_to(gb_potential_t *pot, gb_particles_t *p,
                                    gb_neighbors_t *nl, int *ierror);
 int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *pot, gb_particles_t *p,
@@ -261,8 +289,8 @@ int gb_tabulated_alloy_eam_table(const gb_potential_t *pot, int which, int idx, 
  * reference.  It is meant for callers that cannot call cudaMalloc: codes
  * embedded in a host framework that has already reserved the device memory
  * for its own pool, and MD loops that must not allocate (nor implicitly
- * synchronise the device) during a time step.  It evaluates a Tersoff or
- * Kumagai potential (FP64 or mixed, as set on `pot`) on a neighbour list the
+ * synchronise the device) during a time step.  It evaluates a Tersoff,
+ * Kumagai or Brenner potential (FP64 or mixed, as set on `pot`) on a neighbour list the
  * caller supplies and allocates nothing: all intermediate buffers live in one
  * static device array of about 12.5 MB that every GPU loading this library
  * holds until the process exits.
@@ -295,7 +323,7 @@ int gb_bop_energy_and_forces_noalloc(gb_potential_t *pot, int nat, const double 
  * evaluates one particles object per call).  One neighbour build and one
  * bond-order tile launch cover all structures; per structure the results
  * equal a separate energy_and_forces call on that structure (same list, same
- * kernels).  Tersoff and Kumagai, FP64 or mixed precision.
+ * kernels).  Tersoff, Kumagai and Brenner, FP64 or mixed precision.
  * ---------------------------------------------------------------------- */
 int gb_batch_new(gb_batch_t **batch);
 void gb_batch_free(gb_batch_t *batch);

@@ -14,6 +14,9 @@
 //                         src/potentials/bop/default_compute_func.f90:54-95
 //   * Tersoff functions   src/potentials/bop/tersoff/tersoff_func.f90:32-232
 //   * Kumagai functions   src/potentials/bop/kumagai/kumagai_func.f90:32-242
+//   * Brenner functions   src/potentials/bop/brenner/brenner_func.f90:32-225,
+//                         brenner_module.f90:119-243 (derived constants,
+//                         interaction range)
 //   * trig_off cutoff     src/support/cutoff.f90:152-196
 //   * screened BOP        bop_kernel.f90:682-995 (pass 1), 1171-1527 and
 //                         1531-1611 (pass 2 and the screening forces),
@@ -433,6 +436,16 @@ struct orc_kumagai_params {
   double r1[1], r2[1];
 };
 
+// Brenner-form parameter set (brenner_params.f90:27-65): every array per
+// symmetric element pair.
+struct orc_brenner_params {
+  int nel;
+  int Z[3];
+  double D0[6], r0[6], S[6], beta[6], gamma[6], c[6], d[6], h[6], mu[6], n[6];
+  int m[6];
+  double r1[6], r2[6];
+};
+
 }  // extern "C"
 
 namespace {
@@ -559,6 +572,89 @@ struct KumagaiFn {
       } else {
         val = std::exp(alpha * std::pow(dr, beta));
         dval = beta * alpha * std::pow(dr, beta - 1) * val;
+      }
+    }
+  }
+};
+
+// Brenner functional form, brenner_func.f90:32-225, with the derived
+// constants of BIND_TO_FUNC (brenner_module.f90:196-214): bo_exp = -1/(2n),
+// bo_fac = bo_exp n / 2, expR = beta sqrt(2 S), expA = beta sqrt(2 / S),
+// VR_f = D0 / (S - 1), VA_f = S D0 / (S - 1), c_d = c^2 / d^2.
+struct BrennerFn {
+  const orc_brenner_params &p;
+  double bo_exp[6], bo_fac[6], bo_exp1[6], expR[6], expA[6], c_sq[6], d_sq[6], c_d[6],
+      VR_f[6], VA_f[6];
+  explicit BrennerFn(const orc_brenner_params &q) : p(q) {
+    const int np = p.nel * (p.nel + 1) / 2;
+    for (int i = 0; i < np; i++) {
+      bo_exp[i] = -0.5 / p.n[i];
+      bo_fac[i] = 0.5 * bo_exp[i] * p.n[i];
+      bo_exp1[i] = bo_exp[i] - 1.0;
+      expR[i] = p.beta[i] * std::sqrt(2 * p.S[i]);
+      expA[i] = p.beta[i] * std::sqrt(2 / p.S[i]);
+      c_sq[i] = p.c[i] * p.c[i];
+      d_sq[i] = p.d[i] * p.d[i];
+      c_d[i] = c_sq[i] / d_sq[i];
+      VR_f[i] = p.D0[i] / (p.S[i] - 1);
+      VA_f[i] = p.S[i] * p.D0[i] / (p.S[i] - 1);
+    }
+  }
+  int nel() const { return p.nel; }
+  double r1(int ij) const { return p.r1[ij]; }
+  double r2(int ij) const { return p.r2[ij]; }
+  void VA(int ij, double dr, double &val, double &dval) const {
+    const double e = std::exp(-expA[ij] * (dr - p.r0[ij]));
+    val = -VA_f[ij] * e;
+    dval = VA_f[ij] * expA[ij] * e;
+  }
+  void VR(int ij, double dr, double &val, double &dval) const {
+    const double e = std::exp(-expR[ij] * (dr - p.r0[ij]));
+    val = VR_f[ij] * e;
+    dval = -VR_f[ij] * expR[ij] * e;
+  }
+  // angular term of the (i,k) pair; the sign convention is h + cos theta
+  void g(int /*ktypi*/, int ikpot, double costh, double &val, double &dval) const {
+    const double hc = p.h[ikpot] + costh;
+    const double h = d_sq[ikpot] + hc * hc;
+    val = p.gamma[ikpot] * (1 + c_d[ikpot] - c_sq[ikpot] / h);
+    dval = 2 * p.gamma[ikpot] * c_sq[ikpot] * hc / (h * h);
+  }
+  // bond order of the (i,j) pair; n = 1 takes the branch without the
+  // zeta > 0 test (brenner_func.f90:146-150)
+  void bo(int /*ktypi*/, int ijpot, double zij, double fcij, double faij, double &bij,
+          double &dfbij) const {
+    if (p.n[ijpot] == 1.0) {
+      const double arg = 1.0 + zij;
+      bij = std::pow(arg, bo_exp[ijpot]);
+      dfbij = bo_fac[ijpot] * fcij * faij * std::pow(arg, bo_exp1[ijpot]);
+    } else if (zij > 0.0) {
+      const double arg = 1.0 + std::pow(zij, p.n[ijpot]);
+      bij = std::pow(arg, bo_exp[ijpot]);
+      dfbij = bo_fac[ijpot] * fcij * faij * std::pow(zij, p.n[ijpot] - 1.0) *
+              std::pow(arg, bo_exp1[ijpot]);
+    } else {
+      bij = 1.0;
+      dfbij = 0.0;
+    }
+  }
+  void h(int ikpot, double dr, double &val, double &dval) const {
+    const double mu = p.mu[ikpot];
+    if (mu == 0.0) {
+      val = 1.0;
+      dval = 0.0;
+    } else {
+      const int m = p.m[ikpot];
+      if (m == 1) {
+        val = std::exp(2 * mu * dr);
+        dval = 2 * mu * val;
+      } else if (m == 3) {
+        const double arg = 2 * mu * dr;
+        val = std::exp(arg * arg * arg);
+        dval = 6 * mu * arg * arg * val;
+      } else {
+        val = std::exp(std::pow(2 * mu * dr, m));
+        dval = 2 * mu * m * std::pow(2 * mu * dr, m - 1) * val;
       }
     }
   }
@@ -2024,9 +2120,106 @@ int orc_kumagai_scr_compute(const orc_kumagai_params *p, const orc_scr_params *s
                         resolve_threads(nthreads));
 }
 
+// Brenner entry points.  The screened interaction range differs from the
+// default bind_to: sqrt(C_dr_cut) times max(r2, or2, bor2) of the same pair
+// (brenner_module.f90:191-243), not of all pairs.
+static double brenner_scr_range(int nat, const std::vector<int> &el, const orc_brenner_params &p,
+                                const orc_scr_params &sp) {
+  const int nel = p.nel;
+  std::vector<int> present(nel, 0);
+  for (int i = 0; i < nat; i++)
+    if (el[i] >= 0) present[el[i]] = 1;
+  double range = 0.0;
+  for (int a = 0; a < nel; a++)
+    for (int b = 0; b < nel; b++)
+      if (present[a] && present[b]) {
+        const int q = pair_index(a, b, nel);
+        const double cdr = sp.Cmax[q] > 2.0 ? sp.Cmax[q] * sp.Cmax[q] / (4 * (sp.Cmax[q] - 1))
+                                            : 1.0;
+        const double mc = std::max(std::max(p.r2[q], sp.or2[q]), sp.bor2[q]);
+        range = std::max(range, std::sqrt(cdr) * std::sqrt(mc * mc));
+      }
+  return range;
+}
+
+double orc_brenner_cutoff(const orc_brenner_params *p, int nat, const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return bop_range(nat, el, p->nel, p->r2);
+}
+
+double orc_brenner_scr_cutoff(const orc_brenner_params *p, const orc_scr_params *sp, int nat,
+                              const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  return brenner_scr_range(nat, el, *p, *sp);
+}
+
+// sp == NULL: Brenner; else BrennerScr.  nl_seed == NULL: the list is built
+// here (compute); else it is the caller's (kernel).
+static int brenner_run(const orc_brenner_params *p, const orc_scr_params *sp, int nat,
+                       const double *r, const double *cell, const int *pbc, const int *Z,
+                       const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                       const BopOut &o, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  NList nl;
+  if (seed) {
+    nl_from_arrays(nat, seed, nbr, dc, nl);
+  } else {
+    const double cutoff =
+        sp ? brenner_scr_range(nat, el, *p, *sp) : bop_range(nat, el, p->nel, p->r2);
+    if (cutoff > 0) build_neighbors(nat, r, box, cutoff, nl);
+    else nl.seed.assign(nat + 1, 0);
+  }
+  *o.epot = 0.0;
+  const BrennerFn fn(*p);
+  const int nt = resolve_threads(nthreads);
+  return sp ? bop_kernel_scr(fn, *sp, nat, r, box, el.data(), nl, mask, o, nt)
+            : bop_kernel(fn, nat, r, box, el.data(), nl, mask, o, nt);
+}
+
+int orc_brenner_kernel(const orc_brenner_params *p, int nat, const double *r, const double *cell,
+                       const int *pbc, const int *Z, const int64_t *seed, const int *nbr,
+                       const int *dc, const int *mask, double *epot, double *f, double *wpot,
+                       double *epot_per_at, double *epot_per_bond, double *f_per_bond,
+                       double *wpot_per_at, double *wpot_per_bond, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return brenner_run(p, nullptr, nat, r, cell, pbc, Z, seed, nbr, dc, mask, o, nthreads);
+}
+
+int orc_brenner_scr_kernel(const orc_brenner_params *p, const orc_scr_params *sp, int nat,
+                           const double *r, const double *cell, const int *pbc, const int *Z,
+                           const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                           double *epot, double *f, double *wpot, double *epot_per_at,
+                           double *epot_per_bond, double *f_per_bond, double *wpot_per_at,
+                           double *wpot_per_bond, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return brenner_run(p, sp, nat, r, cell, pbc, Z, seed, nbr, dc, mask, o, nthreads);
+}
+
+int orc_brenner_compute(const orc_brenner_params *p, int nat, const double *r, const double *cell,
+                        const int *pbc, const int *Z, const int *mask, double *epot, double *f,
+                        double *wpot, double *epot_per_at, double *wpot_per_at, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return brenner_run(p, nullptr, nat, r, cell, pbc, Z, nullptr, nullptr, nullptr, mask, o,
+                     nthreads);
+}
+
+int orc_brenner_scr_compute(const orc_brenner_params *p, const orc_scr_params *sp, int nat,
+                            const double *r, const double *cell, const int *pbc, const int *Z,
+                            const int *mask, double *epot, double *f, double *wpot,
+                            double *epot_per_at, double *wpot_per_at, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return brenner_run(p, sp, nat, r, cell, pbc, Z, nullptr, nullptr, nullptr, mask, o, nthreads);
+}
+
 // The LAMMPS contract (bop_kernel.f90 under LAMMPS): nat = local + ghost
 // atoms with explicit positions, a shift-free list over all of them, bonds of
-// the first natloc atoms; kind 0 Tersoff, 1 Kumagai; sp != NULL: screened.
+// the first natloc atoms; kind 0 Tersoff, 1 Kumagai, 2 Brenner; sp != NULL:
+// screened.
 int orc_bop_ghost(int kind, const void *params, const orc_scr_params *sp, int nat, int natloc,
                   const double *r, const int *Z, const int64_t *seed, const int *nbr,
                   const int *mask, double *epot, double *f, double *wpot, double *epot_per_at,
@@ -2049,6 +2242,13 @@ int orc_bop_ghost(int kind, const void *params, const orc_scr_params *sp, int na
     return sp ? bop_kernel_scr(TersoffFn(*p), *sp, nat, r, box, el.data(), nl, mask, o, nt,
                                natloc)
               : bop_kernel(TersoffFn(*p), nat, r, box, el.data(), nl, mask, o, nt, natloc);
+  }
+  if (kind == 2) {
+    const orc_brenner_params *p = static_cast<const orc_brenner_params *>(params);
+    map_elements(nat, Z, p->nel, p->Z, el);
+    const BrennerFn fn(*p);
+    return sp ? bop_kernel_scr(fn, *sp, nat, r, box, el.data(), nl, mask, o, nt, natloc)
+              : bop_kernel(fn, nat, r, box, el.data(), nl, mask, o, nt, natloc);
   }
   const orc_kumagai_params *p = static_cast<const orc_kumagai_params *>(params);
   map_elements(nat, Z, p->nel, p->Z, el);

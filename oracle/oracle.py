@@ -4,7 +4,7 @@ TEST INFRASTRUCTURE ONLY — ctypes wrapper around the C++ FP64 oracle
 never by the atomistica_gb300 package.
 
 The oracle restates Atomistica's neighbour build (python_neighbors.f90),
-the Tersoff/Kumagai BOP kernel (bop_kernel.f90 + *_func.f90) and the tabulated
+the Tersoff/Kumagai/Brenner BOP kernel (bop_kernel.f90 + *_func.f90) and the tabulated
 alloy EAM (tabulated_alloy_eam.f90 + simple_spline.f90); see oracle.cpp for
 line citations.  Output layouts follow src/python/c/potential.c:446-611:
 f (nat,3), wpot (3,3) with wpot[a,c] = W(a,c), wpot_per_at (nat,3,3) with
@@ -49,6 +49,13 @@ class KumagaiParams(ctypes.Structure):
         [(k, ctypes.c_double * 1) for k in ("c1", "c2", "c3", "c4", "c5", "h", "r1", "r2")]
 
 
+class BrennerParams(ctypes.Structure):
+    _fields_ = [("nel", ctypes.c_int), ("Z", ctypes.c_int * 3)] + \
+        [(k, ctypes.c_double * 6) for k in ("D0", "r0", "S", "beta", "gamma", "c", "d", "h",
+                                            "mu", "n")] + \
+        [("m", ctypes.c_int * 6), ("r1", ctypes.c_double * 6), ("r2", ctypes.c_double * 6)]
+
+
 class ScrParams(ctypes.Structure):
     """Screened variants: outer / bond-order cutoffs and the screening window
     (tersoff_params.f90:81-90, kumagai_params.f90 under SCREENING)."""
@@ -67,11 +74,20 @@ def scr_params(d):
 
 
 def _kind(kind):
-    """(base kind, screened?) of 'tersoff', 'kumagai', 'tersoff_scr', 'kumagai_scr'."""
+    """(base kind, screened?) of 'tersoff', 'kumagai', 'brenner' and their
+    '_scr' forms."""
     base = kind[:-4] if kind.endswith("_scr") else kind
-    if base not in ("tersoff", "kumagai"):
+    if base not in ("tersoff", "kumagai", "brenner"):
         raise ValueError("unknown bond-order potential %r" % kind)
     return base, kind.endswith("_scr")
+
+
+_KIND_ID = {"tersoff": 0, "kumagai": 1, "brenner": 2}
+
+
+def _params(base, d):
+    return {"tersoff": tersoff_params, "kumagai": kumagai_params,
+            "brenner": brenner_params}[base](d)
 
 
 def _Z(sym):
@@ -113,6 +129,22 @@ def kumagai_params(d):
     return p
 
 
+def brenner_params(d):
+    p = BrennerParams()
+    els = d["el"]
+    p.nel = len(els)
+    for q, s in enumerate(els):
+        p.Z[q] = _Z(s)
+    npair = p.nel * (p.nel + 1) // 2
+    for k in ("D0", "r0", "S", "beta", "gamma", "c", "d", "h", "mu", "n", "r1", "r2"):
+        arr = getattr(p, k)
+        for q in range(npair):
+            arr[q] = float(d[k][q])
+    for q in range(npair):
+        p.m[q] = int(d["m"][q])
+    return p
+
+
 _P = ctypes.c_void_p
 
 
@@ -128,25 +160,28 @@ def lib():
         L.orc_neighbors_copy.argtypes = [_P, _P, _P, _P]
         L.orc_neighbors_free.argtypes = [_P]
         L.orc_cell_inverse.argtypes = [_P, _P]
-        for name in ("orc_tersoff_cutoff", "orc_kumagai_cutoff"):
+        for name in ("orc_tersoff_cutoff", "orc_kumagai_cutoff", "orc_brenner_cutoff"):
             getattr(L, name).restype = ctypes.c_double
             getattr(L, name).argtypes = [_P, ctypes.c_int, _P]
         kargs = [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                  _P, _P, ctypes.c_int]
-        for name in ("orc_tersoff_kernel", "orc_kumagai_kernel"):
+        for name in ("orc_tersoff_kernel", "orc_kumagai_kernel", "orc_brenner_kernel"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = kargs
         cargs = [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
-        for name in ("orc_tersoff_compute", "orc_kumagai_compute"):
+        for name in ("orc_tersoff_compute", "orc_kumagai_compute", "orc_brenner_compute"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = cargs
-        for name in ("orc_tersoff_scr_cutoff", "orc_kumagai_scr_cutoff"):
+        for name in ("orc_tersoff_scr_cutoff", "orc_kumagai_scr_cutoff",
+                     "orc_brenner_scr_cutoff"):
             getattr(L, name).restype = ctypes.c_double
             getattr(L, name).argtypes = [_P, _P, ctypes.c_int, _P]
-        for name in ("orc_tersoff_scr_kernel", "orc_kumagai_scr_kernel"):
+        for name in ("orc_tersoff_scr_kernel", "orc_kumagai_scr_kernel",
+                     "orc_brenner_scr_kernel"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = [_P] + kargs
-        for name in ("orc_tersoff_scr_compute", "orc_kumagai_scr_compute"):
+        for name in ("orc_tersoff_scr_compute", "orc_kumagai_scr_compute",
+                     "orc_brenner_scr_compute"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = [_P] + cargs
         L.orc_bop_ghost.restype = ctypes.c_int
@@ -253,7 +288,7 @@ def bop_cutoff(kind, params, s):
     L = lib()
     _, _, _, Z = _geom(s)
     base, scr = _kind(kind)
-    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    p = _params(base, params)
     pre = (ctypes.byref(p), ctypes.byref(scr_params(params))) if scr else (ctypes.byref(p),)
     return getattr(L, "orc_%s_cutoff" % kind)(*pre, len(Z), _ptr(Z))
 
@@ -266,7 +301,7 @@ def bop(kind, params, s, nl=None, mask=None, per_at=True, per_bond=False, nthrea
     r, cell, pbc, Z = _geom(s)
     nat = len(r)
     base, scr = _kind(kind)
-    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    p = _params(base, params)
     pre = (ctypes.byref(p), ctypes.byref(scr_params(params))) if scr else (ctypes.byref(p),)
     if nl is None:
         cut = getattr(L, "orc_%s_cutoff" % kind)(*pre, nat, _ptr(Z))
@@ -297,7 +332,7 @@ def bop_ghost(kind, params, r, Z, seed, nbr, natloc, mask=None, nthreads=0):
     f, wpot, epot_per_at, wpot_per_at for all atoms."""
     L = lib()
     base, scr = _kind(kind)
-    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    p = _params(base, params)
     sp = scr_params(params) if scr else None
     r = np.ascontiguousarray(r, dtype=np.float64)
     nat = len(r)
@@ -307,7 +342,7 @@ def bop_ghost(kind, params, r, Z, seed, nbr, natloc, mask=None, nthreads=0):
     out = _alloc_outputs(nat, 0, True, False)
     epot = ctypes.c_double(0.0)
     m = None if mask is None else np.ascontiguousarray(np.asarray(mask).astype(np.int32))
-    rc = L.orc_bop_ghost(0 if base == "tersoff" else 1, ctypes.byref(p),
+    rc = L.orc_bop_ghost(_KIND_ID[base], ctypes.byref(p),
                          ctypes.byref(sp) if sp is not None else None, nat, int(natloc),
                          _ptr(r), _ptr(Z), _ptr(seed), _ptr(nbr), _ptr(m), ctypes.byref(epot),
                          _ptr(out["f"]), _ptr(out["wpot"]), _ptr(out["epot_per_at"]),
@@ -325,7 +360,7 @@ def bop_compute(kind, params, s, mask=None, per_at=False, nthreads=0):
     r, cell, pbc, Z = _geom(s)
     nat = len(r)
     base, scr = _kind(kind)
-    p = tersoff_params(params) if base == "tersoff" else kumagai_params(params)
+    p = _params(base, params)
     pre = (ctypes.byref(p), ctypes.byref(scr_params(params))) if scr else (ctypes.byref(p),)
     out = _alloc_outputs(nat, 0, per_at, False)
     epot = ctypes.c_double(0.0)

@@ -25,7 +25,8 @@ def gpu_bop(kind, s, precision="fp64", params=None, mask=None, per_at=True, per_
     p = native.from_atoms(s)
     nl = native.Neighbors(100)
     cls = {"tersoff": native.Tersoff, "kumagai": native.Kumagai,
-           "tersoff_scr": native.TersoffScr, "kumagai_scr": native.KumagaiScr}[kind]
+           "tersoff_scr": native.TersoffScr, "kumagai_scr": native.KumagaiScr,
+           "brenner": native.Brenner, "brenner_scr": native.BrennerScr}[kind]
     pot = cls(precision=precision, **(params or {}))
     pot.bind_to(p, nl)
     out = None

@@ -60,17 +60,20 @@ def test_struct_layout_matches_c(tmp_path):
 #include <stddef.h>
 #include "atomistica_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu\\n", sizeof(gb_tersoff_params_t),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gb_tersoff_params_t),
          offsetof(gb_tersoff_params_t, m), offsetof(gb_tersoff_params_t, r2),
-         sizeof(gb_kumagai_params_t), offsetof(gb_kumagai_params_t, beta));
+         sizeof(gb_kumagai_params_t), offsetof(gb_kumagai_params_t, beta),
+         sizeof(gb_brenner_params_t), offsetof(gb_brenner_params_t, m),
+         offsetof(gb_brenner_params_t, r2));
   return 0;
 }
 """)
     exe = tmp_path / "layout"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)])
     vals = [int(x) for x in subprocess.check_output([str(exe)]).split()]
-    T, K = _lib.TersoffParams, _lib.KumagaiParams
-    assert vals == [ctypes.sizeof(T), T.m.offset, T.r2.offset, ctypes.sizeof(K), K.beta.offset]
+    T, K, B = _lib.TersoffParams, _lib.KumagaiParams, _lib.BrennerParams
+    assert vals == [ctypes.sizeof(T), T.m.offset, T.r2.offset, ctypes.sizeof(K), K.beta.offset,
+                    ctypes.sizeof(B), B.m.offset, B.r2.offset]
 
 
 def test_library_reports_missing_gpu_cleanly(lib):

@@ -67,6 +67,39 @@ def test_parameter_conversion():
     assert isinstance(p, _lib.TersoffParams)
 
 
+def test_brenner_parameters_and_checks():
+    # brenner_module.f90:200-210: d = 0 and S <= 1 are rejected at set-up
+    from atomistica_gb300 import _lib, native
+    p = native.brenner_params(P.Erhart_PRB_71_035211_SiC)
+    assert p.nel == 2 and list(p.Z)[:2] == [6, 14] and p.c[1] == 273987.0 and p.m[2] == 1
+    with pytest.raises(ValueError):
+        native.brenner_params(dict(P.Erhart_PRB_71_035211_SiC, D0=[6.0]))
+    native.Brenner(**P.Erhart_PRB_71_035211_SiC)
+    native.BrennerScr(**P.Erhart_PRB_71_035211_SiC__Scr)
+    for bad in (dict(S=[2.167, 1.0, 1.842]), dict(d=[6.28433, 0.0, 0.81472]),
+                dict(r2=[1.0, 2.6, 2.96])):
+        with pytest.raises(_lib.AtomisticaError):
+            native.Brenner(**dict(P.Erhart_PRB_71_035211_SiC, **bad))
+
+
+@pytest.mark.parametrize("kind", ["brenner", "brenner_scr"])
+def test_brenner_interaction_range(kind):
+    # Brenner requests r2 of each present pair; BrennerScr sqrt(C_dr_cut)
+    # max(r2, or2, bor2) of the pair itself (brenner_module.f90:229-243)
+    import oracle
+    prm = P.Erhart_PRB_71_035211_SiC__Scr if kind == "brenner_scr" else \
+        P.Erhart_PRB_71_035211_SiC
+    si = S.diamond("Si", 5.43)
+    c = S.diamond("C", 3.57)
+    if kind == "brenner":
+        assert oracle.bop_cutoff(kind, prm, si) == 2.96
+        assert oracle.bop_cutoff(kind, prm, c) == 2.15
+    else:
+        x = np.sqrt(9.0 / 8.0)
+        assert abs(oracle.bop_cutoff(kind, prm, si) - x * 6.0) < 1e-12
+        assert abs(oracle.bop_cutoff(kind, prm, c) - x * 4.0) < 1e-12
+
+
 def test_pair_index_matches_reference_table():
     # src/macros.inc:110-123 table for maxval=4 (1-based): row i, col j>=i
     expect = {(1, 1): 1, (1, 2): 2, (1, 3): 3, (1, 4): 4, (2, 2): 5, (2, 3): 6, (2, 4): 7,

@@ -16,7 +16,10 @@ oracle:
 
 The screened variants (TersoffScr, KumagaiScr) are pinned by the same tests
 the reference runs for them: bulk properties, FD forces and virials, mask
-additivity and the Kumagai dimer.
+additivity and the Kumagai dimer.  The Brenner form (Erhart-Albe Si-C and
+BrennerScr, Brenner's carbon potential II, Henriksson Fe-C with masks,
+Kioseoglou Al-N with n != 1) likewise: tests/test_bulk_properties.py:67-94 and
+tests/test_forces_and_virial.py:91-114.
 """
 
 import os
@@ -34,8 +37,10 @@ from helpers import KUMAGAI, TERSOFF, random_carbon, rattled_diamond
 
 TERSOFF_SCR = P.Tersoff_PRB_39_5566_Si_C__Scr
 KUMAGAI_SCR = P.Kumagai_CompMaterSci_39_457_Si__Scr
+BRENNER = P.Erhart_PRB_71_035211_SiC
+BRENNER_SCR = P.Erhart_PRB_71_035211_SiC__Scr
 PARAMS = {"tersoff": TERSOFF, "kumagai": KUMAGAI, "tersoff_scr": TERSOFF_SCR,
-          "kumagai_scr": KUMAGAI_SCR}
+          "kumagai_scr": KUMAGAI_SCR, "brenner": BRENNER, "brenner_scr": BRENNER_SCR}
 
 GPA = 160.21766208  # eV/A^3 -> GPa
 JM2 = 16.02176634  # eV/A^2 -> J/m^2
@@ -163,6 +168,40 @@ def test_bulk_properties_bop(case):
     assert within(c44, C440), (name, c44)
 
 
+@pytest.mark.parametrize("case", [
+    # tests/test_bulk_properties.py:67-94: name, kind, params, builder, Ec, a0, C11, C12,
+    # unrelaxed C44 (C440), relaxed C44 (C44r), B = (C11 + 2 C12)/3
+    ("erhart dia-C", "brenner", BRENNER, lambda a: S.diamond("C", a), 7.3731, 3.566, 1082, 127,
+     None, 673, 445),
+    ("erhart dia-Si", "brenner", BRENNER, lambda a: S.diamond("Si", a), 4.63, 5.429, 167, 65,
+     105, None, 99),
+    ("erhart B3-SiC", "brenner", BRENNER, lambda a: S.b3(("Si", "C"), a), 6.340, 4.359, 382,
+     145, 305, None, 224),
+    ("erhart_scr dia-C", "brenner_scr", BRENNER_SCR, lambda a: S.diamond("C", a), 7.3731, 3.566,
+     1082, 127, None, 673, 445),
+    ("erhart_scr dia-Si", "brenner_scr", BRENNER_SCR, lambda a: S.diamond("Si", a), 4.63, 5.429,
+     167, 65, 105, None, 99),
+    ("erhart_scr B3-SiC", "brenner_scr", BRENNER_SCR, lambda a: S.b3(("Si", "C"), a), 6.340,
+     4.359, 382, 145, 305, None, 224),
+    ("brenner II dia-C", "brenner", P.Brenner_PRB_42_9458_C_II, lambda a: S.diamond("C", a),
+     7.376 - 0.0524, 3.558, 621, 415, None, 383, 484),
+])
+def test_bulk_properties_brenner(case):
+    name, kind, params, builder, Ec, a0, C11, C12, C440, C44r, B = case
+    a_min, e_min = lattice_minimum(kind, builder, params, 0.9 * a0, 1.1 * a0)
+    assert within(-e_min, Ec), (name, e_min)
+    assert within(a_min, a0), (name, a_min)
+    c11, c12, c44 = cubic_elastic_constants(kind, builder(a_min), params)
+    assert within(c11, C11), (name, c11)
+    assert within(c12, C12), (name, c12)
+    assert within((c11 + 2 * c12) / 3, B), (name, c11, c12)
+    if C440 is not None:
+        assert within(c44, C440), (name, c44)
+    if C44r is not None:
+        _, _, c44r = cubic_elastic_constants(kind, builder(a_min), params, eps=1e-3, relax=True)
+        assert within(c44r, C44r), (name, c44r)
+
+
 def test_relaxed_c44_tersoff_si():
     a_min, _ = lattice_minimum("tersoff", lambda a: S.diamond("Si", a), TERSOFF, 5.3, 5.6)
     s = S.diamond("Si", a_min)
@@ -257,6 +296,53 @@ def test_fd_forces_virial_bop(name, scr):
     assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
 
 
+@pytest.mark.parametrize("scr", [False, True])
+@pytest.mark.parametrize("name", ["dia-C", "dia-Si", "B3-SiC", "a-C"])
+def test_fd_forces_virial_brenner(name, scr):
+    # tests/test_forces_and_virial.py:91-102 (Brenner, BrennerScr with
+    # Erhart_PRB_71_035211_SiC on dia-C, a-C, dia-Si, B3-SiC)
+    if name == "dia-C":
+        s = rattled_diamond("C", 3.566, (2, 2, 2), 0.3, 21)
+    elif name == "dia-Si":
+        s = rattled_diamond("Si", 5.429, (2, 2, 2), 0.5, 22)
+    elif name == "B3-SiC":
+        s = S.b3(("Si", "C"), 4.3596, (2, 2, 2))
+        s.positions += np.random.default_rng(23).uniform(-0.4, 0.4, s.positions.shape)
+    else:
+        s = random_carbon(64, seed=24)
+    kind = "brenner_scr" if scr else "brenner"
+    # dx = 1e-5: the reference form of g, 1 + c^2/d^2 - c^2/(d^2 + (h + cos)^2),
+    # cancels ~6 digits for the Si-C pair (c^2/d^2 = 2.3e6), so the energy
+    # carries ~1e-11 eV of rounding noise that a 1e-6 step turns into 3e-5 eV/A
+    ferr, werr = fd_check(kind, s, PARAMS[kind], dx=1e-5, natoms=12)
+    assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
+
+
+@pytest.mark.parametrize("name", ["dia-C", "a-C", "bcc-Fe", "fcc-Fe", "sc-Fe", "B1-Fe-C"])
+def test_fd_forces_virial_brenner_fec_masked(name):
+    # tests/test_forces_and_virial.py:103-114 (Henriksson_PRB_79_114107_FeC,
+    # mask=True, rattled)
+    rng = np.random.default_rng(25)
+    s = {"dia-C": lambda: S.diamond("C", 3.566, (2, 2, 2)),
+         "a-C": lambda: random_carbon(64, seed=26),
+         "bcc-Fe": lambda: S.bcc("Fe", 2.87, (3, 3, 3)),
+         "fcc-Fe": lambda: S.fcc("Fe", 3.6, (2, 2, 2)),
+         "sc-Fe": lambda: S.sc("Fe", 2.4, (3, 3, 3)),
+         "B1-Fe-C": lambda: S.b1(("Fe", "C"), 3.9, (2, 2, 2))}[name]()
+    s.positions += rng.uniform(-0.1, 0.1, s.positions.shape)
+    mask = rng.integers(0, 2, len(s)).astype(bool)
+    ferr, werr = fd_check("brenner", s, P.Henriksson_PRB_79_114107_FeC, natoms=8, mask=mask)
+    assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
+
+
+def test_fd_forces_virial_brenner_aln_fractional_n():
+    # Kioseoglou Al-N: n = 0.72 and 6.0865 (the zeta^n branch of bo)
+    s = S.b3(("Al", "N"), 4.38, (2, 2, 2))
+    s.positions += np.random.default_rng(27).uniform(-0.3, 0.3, s.positions.shape)
+    ferr, werr = fd_check("brenner", s, P.Kioseoglou_PSSb_245_1118_AlN, natoms=12)
+    assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
+
+
 def test_fd_forces_virial_eam(tmp_path):
     fn = gio.cu_analytic_setfl(str(tmp_path / "cu.setfl"), nr=3000, nrho=3000)
     e = oracle.EAM(fn)
@@ -292,9 +378,9 @@ def test_eam_special_cases(reference_tests_dir):
         assert err < 1e-6, (fac, err)
 
 
-@pytest.mark.parametrize("kind", ["tersoff", "tersoff_scr"])
+@pytest.mark.parametrize("kind", ["tersoff", "tersoff_scr", "brenner", "brenner_scr"])
 def test_mask_additivity(kind):
-    # tests/test_mask.py:68 (Tersoff, TersoffScr)
+    # tests/test_mask.py:68 (Tersoff, TersoffScr; Brenner, BrennerScr)
     s = random_carbon(96, seed=8)
     mask = np.random.default_rng(9).integers(0, 2, len(s)).astype(bool)
     o = energy(kind, s, PARAMS[kind])
