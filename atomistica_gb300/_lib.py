@@ -48,6 +48,8 @@ SIGNATURES = [
     ("gb_kumagai_scr_new", _I, [_P, _P, _P]),
     ("gb_brenner_new", _I, [_P, _P]),
     ("gb_brenner_scr_new", _I, [_P, _P, _P]),
+    ("gb_juslin_new", _I, [_P, _P]),
+    ("gb_juslin_scr_new", _I, [_P, _P, _P]),
     ("gb_tabulated_alloy_eam_new", _I, [_P, ctypes.c_char_p]),
     ("gb_potential_free", None, [_P]),
     ("gb_potential_set_precision", _I, [_P, _I]),
@@ -62,6 +64,8 @@ SIGNATURES = [
     ("gb_kumagai_energy_and_forces", _I, [_P] * 13 + [_P]),
     ("gb_brenner_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_brenner_energy_and_forces", _I, [_P] * 13 + [_P]),
+    ("gb_juslin_bind_to", _I, [_P, _P, _P, _P]),
+    ("gb_juslin_energy_and_forces", _I, [_P] * 13 + [_P]),
     ("gb_tabulated_alloy_eam_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_tabulated_alloy_eam_energy_and_forces", _I, [_P] * 10 + [_P]),
     ("gb_tabulated_alloy_eam_table", _I, [_P, _I, _I, _P, _P]),
@@ -113,9 +117,17 @@ class BrennerParams(ctypes.Structure):
         [("m", _I * 6), ("r1", _D * 6), ("r2", _D * 6)]
 
 
+class JuslinParams(ctypes.Structure):
+    """gb_juslin_params_t"""
+    _fields_ = [("nel", _I), ("Z", _I * 3)] + \
+        [(k, _D * 9) for k in ("D0", "r0", "S", "beta", "gamma", "c", "d", "h", "n")] + \
+        [("alpha", _D * 27), ("omega", _D * 27), ("m", _I * 27), ("r1", _D * 9),
+         ("r2", _D * 9)]
+
+
 class ScreeningParams(ctypes.Structure):
     """gb_screening_params_t"""
-    _fields_ = [(k, _D * 6) for k in ("or1", "or2", "bor1", "bor2", "Cmin", "Cmax")]
+    _fields_ = [(k, _D * 9) for k in ("or1", "or2", "bor1", "bor2", "Cmin", "Cmax")]
 
 
 _lib = None

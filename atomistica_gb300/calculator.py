@@ -206,6 +206,16 @@ class BrennerScr(Atomistica):
     potential_class = native.BrennerScr
 
 
+class Juslin(Atomistica):
+    name = "Juslin"
+    potential_class = native.Juslin
+
+
+class JuslinScr(Atomistica):
+    name = "JuslinScr"
+    potential_class = native.JuslinScr
+
+
 class TabulatedEAM(Atomistica):
     name = "TabulatedEAM"
     potential_class = native.TabulatedEAM

@@ -205,6 +205,139 @@ int check_brenner(const gb_brenner_params_t &p) {
   return 0;
 }
 
+// Juslin_J_Appl_Phys_98_123520_WCH (juslin_params.f90:75-108; el = W, C, H;
+// ordered pairs, r0 = -1 marks the pairs (C,W) and (H,W) that take their
+// mirror's constants).  screened: the SCREENING values of r1, r2.
+gb_juslin_params_t default_juslin(bool screened) {
+  gb_juslin_params_t p{};
+  p.nel = 3;
+  p.Z[0] = 74;
+  p.Z[1] = 6;
+  p.Z[2] = 1;
+  const double D0[9] = {5.41861, 6.64, 2.748, 0.0, 6.0, 3.6422, 0.0, 3.642, 4.7509};
+  const double r0[9] = {2.34095, 1.90547, 1.727, -1.0, 1.39, 1.1199, -1.0, 1.1199, 0.74144};
+  const double S[9] = {1.92708, 2.96149, 1.2489, 0.0, 1.22, 1.69077, 0.0, 1.69077, 2.3432};
+  const double beta[9] = {1.38528, 1.80370, 1.52328, 0.0, 2.1, 1.9583, 0.0, 1.9583, 1.9436};
+  const double gamma[9] = {0.00188227, 0.072855, 0.0054, 0.0, 0.00020813,
+                           0.00020813, 0.0,      12.33,  12.33};
+  const double c[9] = {2.14969, 1.10304, 1.788, 0.0, 330.0, 330.0, 0.0, 0.0, 0.0};
+  const double d[9] = {0.17126, 0.33018, 0.8255, 0.0, 3.5, 3.5, 0.0, 1.0, 1.0};
+  const double h[9] = {-0.27780, 0.75107, 0.38912, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0};
+  const double r1[9] = {3.20, 2.60, screened ? 2.68 : 1.95, 0.0, 1.70, 1.30, 0.0, 1.30, 1.10};
+  const double r2[9] = {3.80, 3.00, screened ? 2.96 : 2.35, 0.0, 2.00, 1.80, 0.0, 1.80, 1.70};
+  for (int q = 0; q < 9; q++) {
+    p.D0[q] = D0[q];
+    p.r0[q] = r0[q];
+    p.S[q] = S[q];
+    p.beta[q] = beta[q];
+    p.gamma[q] = gamma[q];
+    p.c[q] = c[q];
+    p.d[q] = d[q];
+    p.h[q] = h[q];
+    p.n[q] = 1.0;
+    p.r1[q] = r1[q];
+    p.r2[q] = r2[q];
+  }
+  // alpha = 0.45876 for (W,W,W), (W,C,W), (W,H,W); alpha = 4 for (C,C,H),
+  // (C,H,C), (C,H,H), (H,C,C), (H,C,H), (H,H,C), (H,H,H); omega of (C,H,C),
+  // (C,H,H), (H,C,C), (H,C,H) as tabulated; every other triplet alpha = 0,
+  // omega = 1; m = 1 throughout.
+  const int a1[3] = {0, 3, 6}, a4[7] = {14, 16, 17, 22, 23, 25, 26};
+  for (int q = 0; q < 27; q++) {
+    p.alpha[q] = 0.0;
+    p.omega[q] = 1.0;
+    p.m[q] = 1;
+  }
+  for (int q : a1) p.alpha[q] = 0.45876;
+  for (int q : a4) p.alpha[q] = 4.0;
+  p.omega[16] = 2.94586;
+  p.omega[17] = 4.54415;
+  p.omega[22] = 0.33946;
+  p.omega[23] = 0.22006;
+  return p;
+}
+
+gb_screening_params_t default_screening_juslin() {
+  gb_screening_params_t s{};
+  const gb_juslin_params_t p = default_juslin(true);
+  for (int q = 0; q < 9; q++) {
+    s.or1[q] = s.bor1[q] = p.r1[q];
+    s.or2[q] = s.bor2[q] = p.r2[q];
+    s.Cmin[q] = q == 3 || q == 6 ? 0.0 : 1.0;
+    s.Cmax[q] = q == 3 || q == 6 ? 0.0 : 3.0;
+  }
+  return s;
+}
+
+// The mirror fill of the reference's bind_to (juslin_module.f90:273-300): an
+// ordered pair (i, j) with r0 < 0 takes every constant of (j, i), screening
+// cutoffs included.  (The reference indexes this loop with the maximal
+// element count 3; for nel = 3, the only published sets, that is the
+// kernel's index.)
+void fill_juslin(gb_juslin_params_t &p, gb_screening_params_t *sc) {
+  const int nel = p.nel;
+  for (int i = 0; i < nel; i++)
+    for (int j = 0; j < nel; j++) {
+      const int a = j + i * nel, b = i + j * nel;
+      if (!(p.r0[a] < 0.0)) continue;
+      p.D0[a] = p.D0[b];
+      p.r0[a] = p.r0[b];
+      p.S[a] = p.S[b];
+      p.beta[a] = p.beta[b];
+      p.gamma[a] = p.gamma[b];
+      p.c[a] = p.c[b];
+      p.d[a] = p.d[b];
+      p.h[a] = p.h[b];
+      p.n[a] = p.n[b];
+      p.r1[a] = p.r1[b];
+      p.r2[a] = p.r2[b];
+      if (sc) {
+        sc->or1[a] = sc->or1[b];
+        sc->or2[a] = sc->or2[b];
+        sc->bor1[a] = sc->bor1[b];
+        sc->bor2[a] = sc->bor2[b];
+        sc->Cmin[a] = sc->Cmin[b];
+        sc->Cmax[a] = sc->Cmax[b];
+      }
+    }
+}
+
+// The checks of the reference's bind_to (juslin_module.f90:331-343) and the
+// ones the kernels need.
+int check_juslin(const gb_juslin_params_t &p) {
+  if (p.nel < 1 || p.nel > 3) {
+    set_error("Juslin: nel must be 1..3 (JUSLIN_MAX_EL = 3)");
+    return GB_ERROR_ARGUMENT;
+  }
+  const int np = p.nel * p.nel;
+  for (int q = 0; q < np; q++) {
+    if (!(p.r2[q] > p.r1[q]) || !(p.r1[q] >= 0)) {
+      set_error("Juslin: need 0 <= r1 < r2 for every pair");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (p.d[q] == 0.0) {
+      set_error("Juslin: d = 0! This leads to problems computing c**2/d**2. Please specify "
+                "d != 0.");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (!(p.S[q] > 1.0)) {
+      set_error("Juslin: S <= 1! This leads to problems computing (S-1)**(-1). Please "
+                "specify S > 1.");
+      return GB_ERROR_ARGUMENT;
+    }
+    if (!(p.n[q] != 0.0)) {
+      set_error("Juslin: n must be nonzero");
+      return GB_ERROR_ARGUMENT;
+    }
+  }
+  for (int q = 0; q < np * p.nel; q++)
+    if (p.alpha[q] != 0.0 && p.m[q] < 1) {
+      set_error("Juslin: m must be >= 1 where alpha != 0");
+      return GB_ERROR_ARGUMENT;
+    }
+  return 0;
+}
+
 int check_screening(const gb_screening_params_t &s, int npairs) {
   for (int q = 0; q < npairs; q++) {
     if (!(s.or2[q] > s.or1[q]) || !(s.bor2[q] > s.bor1[q]) || !(s.Cmax[q] > s.Cmin[q])) {
@@ -258,16 +391,18 @@ int check_kumagai(const gb_kumagai_params_t &p) {
 }  // namespace
 
 const double *bop_r1(const Potential &pot) {
+  if (pot.kind == kJuslin) return pot.jp.r1;
   return pot.kind == kTersoff ? pot.tp.r1 : pot.kind == kBrenner ? pot.bp.r1 : pot.kp.r1;
 }
 const double *bop_r2(const Potential &pot) {
+  if (pot.kind == kJuslin) return pot.jp.r2;
   return pot.kind == kTersoff ? pot.tp.r2 : pot.kind == kBrenner ? pot.bp.r2 : pot.kp.r2;
 }
 
 double bop_pair_range(const Potential &pot, int t) {
   const double *r2 = bop_r2(pot);
   if (!pot.screened) return r2[t];
-  const int np = pot_nel(pot) * (pot_nel(pot) + 1) / 2;
+  const int np = pot_npairs(pot);
   double mx = 0.0;
   for (int q = 0; q < np; q++) {
     if (pot.kind == kBrenner && q != t) continue;  // BrennerScr: the pair's own cutoffs
@@ -275,7 +410,9 @@ double bop_pair_range(const Potential &pot, int t) {
     mx = std::max(mx, m * m);
   }
   const double cmax = pot.scr.Cmax[t];
-  const double cdr = cmax > 2.0 ? cmax * cmax / (4 * (cmax - 1)) : 1.0;
+  // JuslinScr: no Cmax > 2 guard (juslin_module.f90:305-307)
+  const double cdr =
+      (cmax > 2.0 || pot.kind == kJuslin) ? cmax * cmax / (4 * (cmax - 1)) : 1.0;
   return std::sqrt(cdr) * std::sqrt(mx);
 }
 
@@ -283,13 +420,22 @@ int pot_nel(const Potential &pot) {
   if (pot.kind == kTersoff) return pot.tp.nel;
   if (pot.kind == kKumagai) return 1;
   if (pot.kind == kBrenner) return pot.bp.nel;
+  if (pot.kind == kJuslin) return pot.jp.nel;
   return pot.eam->nel;
 }
 int pot_Z(const Potential &pot, int q) {
   if (pot.kind == kTersoff) return pot.tp.Z[q];
   if (pot.kind == kKumagai) return pot.kp.Z[q];
   if (pot.kind == kBrenner) return pot.bp.Z[q];
+  if (pot.kind == kJuslin) return pot.jp.Z[q];
   return pot.eam->Z[q];
+}
+int pot_npairs(const Potential &pot) {
+  const int nel = pot_nel(pot);
+  return pot.kind == kJuslin ? nel * nel : nel * (nel + 1) / 2;
+}
+int pot_pair(const Potential &pot, int a, int b) {
+  return pot.kind == kJuslin ? b + a * pot_nel(pot) : pair_index(a, b, pot_nel(pot));
 }
 
 cudaStream_t pot_stream(Potential &pot) {
@@ -552,7 +698,7 @@ int bind_to(Potential &pot, Particles &p, Neighbors &nl) {
       for (int zj : zs) {
         const int ii = dbidx(zi), jj = dbidx(zj);
         if (ii < 0 || jj < 0) continue;
-        const int t = pair_index(ii, jj, nel);
+        const int t = pot_pair(pot, ii, jj);
         const double c = bop_pair_range(pot, t);
         if (c > nl.interaction_range) {
           nl.interaction_range = c;
@@ -836,6 +982,42 @@ int gb_brenner_scr_new(gb_potential_t **h, const gb_brenner_params_t *params,
   return 0;
 }
 
+int gb_juslin_new(gb_potential_t **h, const gb_juslin_params_t *params) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_juslin_params_t p = params ? *params : default_juslin(false);
+  if (p.nel < 1 || p.nel > 3) return check_juslin(p);
+  fill_juslin(p, nullptr);
+  GB_CHECK(check_juslin(p));
+  *h = new gb_potential;
+  (*h)->pot.kind = kJuslin;
+  (*h)->pot.jp = p;
+  return 0;
+}
+
+int gb_juslin_scr_new(gb_potential_t **h, const gb_juslin_params_t *params,
+                      const gb_screening_params_t *scr) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  gb_juslin_params_t p = params ? *params : default_juslin(true);
+  gb_screening_params_t sc = scr ? *scr : default_screening_juslin();
+  if (p.nel < 1 || p.nel > 3) return check_juslin(p);
+  fill_juslin(p, &sc);
+  GB_CHECK(check_juslin(p));
+  GB_CHECK(check_screening(sc, p.nel * p.nel));
+  for (int q = 0; q < p.nel * p.nel; q++)
+    if (!(sc.Cmax[q] > 1.0)) {
+      set_error("JuslinScr: Cmax must be > 1 (C_dr_cut = Cmax^2 / (4 (Cmax - 1)))");
+      return GB_ERROR_ARGUMENT;
+    }
+  *h = new gb_potential;
+  (*h)->pot.kind = kJuslin;
+  (*h)->pot.jp = p;
+  (*h)->pot.screened = true;
+  (*h)->pot.scr = sc;
+  return 0;
+}
+
 int gb_tabulated_eam_new(gb_potential_t **h, const char *fn) {
   clear_error();
   if (!h || !fn) return GB_ERROR_ARGUMENT;
@@ -907,7 +1089,7 @@ double gb_potential_get_cutoff(const gb_potential_t *h) {
   const Potential &pot = h->pot;
   if (pot.kind == kEAM) return pot.eam->cutoff;
   double c = 0.0;
-  const int np = pot_nel(pot) * (pot_nel(pot) + 1) / 2;
+  const int np = pot_npairs(pot);
   for (int q = 0; q < np; q++) c = std::max(c, bop_pair_range(pot, q));
   return c;
 }
@@ -988,6 +1170,16 @@ int gb_brenner_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighb
                                  const double *q, double *epot, double *f, double *wpot,
                                  const int *mask, double *epa, double *epb, double *fpb,
                                  double *wpa, double *wpb, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
+                                        ierror);
+}
+int gb_juslin_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl, int *ierror) {
+  return gb_potential_bind_to(h, p, nl, ierror);
+}
+int gb_juslin_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                const double *q, double *epot, double *f, double *wpot,
+                                const int *mask, double *epa, double *epb, double *fpb,
+                                double *wpa, double *wpb, int *ierror) {
   return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
                                         ierror);
 }

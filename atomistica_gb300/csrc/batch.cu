@@ -65,7 +65,7 @@ double batch_cutoff(const Batch &b, const Potential &pot) {
     for (int zj : zs) {
       const int ii = dbidx(zi), jj = dbidx(zj);
       if (ii < 0 || jj < 0) continue;
-      const int t = pair_index(ii, jj, nel);
+      const int t = pot_pair(pot, ii, jj);
       cut = std::max(cut, bop_pair_range(pot, t));
     }
   return cut;

@@ -167,6 +167,7 @@ __device__ __forceinline__ void kloop64(const Pot &pot, const SmemLayout &L, int
   const int nbt = L.nbt, ntrip = L.ntrip;
   const double rnij[3] = {L.rn64[lb], L.rn64[nbt + lb], L.rn64[2 * nbt + lb]};
   const double rlij = L.r64[lb], rinvj = L.rinv64[lb];
+  const int ijpot = (L.meta[lb] >> 8) & 0xf;
   for (int q = 0; q < z; q++) {
     const int lk = s + q;
     if (lk == lb) continue;
@@ -181,7 +182,7 @@ __device__ __forceinline__ void kloop64(const Pot &pot, const SmemLayout &L, int
     const double rnik[3] = {L.rn64[lk], L.rn64[nbt + lk], L.rn64[2 * nbt + lk]};
     const double rlik = L.r64[lk], rinvk = L.rinv64[lk], fcik = L.fc64[lk], dfcik = L.dfc64[lk];
     double hv, dh;
-    pot.template h<double>(ikpot, rlij - rlik, hv, dh);
+    pot.template h<double>(eli, ijpot, ikpot, rlij - rlik, hv, dh);
     const double cs = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
     double gv, dg;
     pot.template g<double>(eli, ikpot, cs, gv, dg);
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(kBopThreads)
       double r2 = __dmul_rn(rij[0], rij[0]);
       r2 = __dadd_rn(r2, __dmul_rn(rij[1], rij[1]));
       r2 = __dadd_rn(r2, __dmul_rn(rij[2], rij[2]));
-      const int t = pair_index(eli, elj, nel);
+      const int t = pot.pair(eli, elj);
       meta |= t << 8;
       bool in_short = false;
       if (r2 < pot.r1sq(t)) {
@@ -595,7 +596,7 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
     if (e == cudaSuccess) {
       const int resident = resident_ctas(kern, kMxThreads, smem);
       const int grid = resident > 0 ? std::min(ntiles, resident) : ntiles;
-      const MxParams mp = make_mx(pot.p, args.A);
+      const MxParams mp = make_mx(pot, args.A);
       kern<<<grid, kMxThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
       note_launch();
       *rows = grid;
@@ -628,6 +629,8 @@ int with_bop(const Potential &pot, F &&f) {
       return f(KumagaiPot{make_kumagai_dev(pot.kp)});
     case kBrenner:
       return f(BrennerPot{make_brenner_dev(pot.bp)});
+    case kJuslin:
+      return f(JuslinPot(make_juslin_dev(pot.jp)));
     default:
       set_error("not a bond-order potential");
       return GB_ERROR_ARGUMENT;
@@ -804,8 +807,8 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
   args.tile_part = pot.tile_part.as<double>();
   GB_CUDA(cudaEventRecord(pot.kev[0], s));
   {
-    const ScrDev sd = make_scr_dev(bop_r1(pot), bop_r2(pot),
-                                   pot_nel(pot) * (pot_nel(pot) + 1) / 2, pot.scr);
+    const ScrDev sd =
+        make_scr_dev(bop_r1(pot), bop_r2(pot), pot_npairs(pot), pot.scr, pot.kind != kJuslin);
     GB_CHECK(with_bop(pot, [&](const auto &P) {
       return launch_scr(args, P, sd, blocks, o.status, want_wat, want_pb, s);
     }));

@@ -81,14 +81,15 @@ struct KumagaiDev {
 // Brenner form: every constant per symmetric pair; VR = VR_f e^{-expR (r-r0)},
 // VA = -VA_f e^{-expA (r-r0)}, g from (gamma, c, d, -h) of the (i,k) pair,
 // b = (1 + zeta^n)^bo_exp of the (i,j) pair, h(dr) as Tersoff with (mu, m).
+// Arrays of 9: Juslin (below) keeps its constants per ordered pair.
 struct BrennerDev {
   int nel;
-  double r0[6], VR_f[6], VA_f[6], expR[6], expA[6];
-  double gamma[6], c2[6], d2[6], c2d2inv[6], hneg[6];
-  double n[6], bo_exp[6], bo_fac[6];
-  double mu[6];
-  int m[6];
-  double r1[6], r2[6], r1sq[6], r2sq[6], fac[6];
+  double r0[9], VR_f[9], VA_f[9], expR[9], expA[9];
+  double gamma[9], c2[9], d2[9], c2d2inv[9], hneg[9];
+  double n[9], bo_exp[9], bo_fac[9];
+  double mu[9];
+  int m[9];
+  double r1[9], r2[9], r1sq[9], r2sq[9], fac[9];
 };
 
 inline BrennerDev make_brenner_dev(const gb_brenner_params_t &p) {
@@ -116,6 +117,47 @@ inline BrennerDev make_brenner_dev(const gb_brenner_params_t &p) {
     d.r1sq[q] = p.r1[q] * p.r1[q];
     d.r2sq[q] = p.r2[q] * p.r2[q];
     d.fac[q] = M_PI / (p.r2[q] - p.r1[q]);
+  }
+  return d;
+}
+
+// Juslin form (juslin_func.f90, juslin_module.f90:322-377): the Brenner
+// functions with every pair constant per ORDERED element pair (t = j + i nel,
+// src/macros.inc:139) and h(dr) = omega e^{(alpha dr)^m} with (alpha, omega,
+// m) per element triplet (k + nel (j + nel i), src/macros.inc:146).
+struct JuslinDev : BrennerDev {
+  double alpha[27], omega[27];
+  int m3[27];
+};
+
+inline JuslinDev make_juslin_dev(const gb_juslin_params_t &p) {
+  JuslinDev d{};
+  d.nel = p.nel;
+  const int np = p.nel * p.nel;
+  for (int q = 0; q < np; q++) {
+    d.r0[q] = p.r0[q];
+    d.expR[q] = p.beta[q] * std::sqrt(2 * p.S[q]);
+    d.expA[q] = p.beta[q] * std::sqrt(2 / p.S[q]);
+    d.VR_f[q] = p.D0[q] / (p.S[q] - 1);
+    d.VA_f[q] = p.S[q] * p.D0[q] / (p.S[q] - 1);
+    d.gamma[q] = p.gamma[q];
+    d.c2[q] = p.c[q] * p.c[q];
+    d.d2[q] = p.d[q] * p.d[q];
+    d.c2d2inv[q] = d.c2[q] / d.d2[q];
+    d.hneg[q] = -p.h[q];
+    d.n[q] = p.n[q];
+    d.bo_exp[q] = -0.5 / p.n[q];
+    d.bo_fac[q] = 0.5 * d.bo_exp[q] * p.n[q];
+    d.r1[q] = p.r1[q];
+    d.r2[q] = p.r2[q];
+    d.r1sq[q] = p.r1[q] * p.r1[q];
+    d.r2sq[q] = p.r2[q] * p.r2[q];
+    d.fac[q] = M_PI / (p.r2[q] - p.r1[q]);
+  }
+  for (int q = 0; q < np * p.nel; q++) {
+    d.alpha[q] = p.alpha[q];
+    d.omega[q] = p.omega[q];
+    d.m3[q] = p.m[q];
   }
   return d;
 }
@@ -200,10 +242,12 @@ GB_HD void trig_off(double r, double r1, double r2, double fac, double &val, dou
 }
 
 struct TersoffPot {
+  static constexpr bool kTripletH = false;  // h constants per element triplet
   // g and b constants per centre element (false) or per element pair (true)
   static constexpr bool kPairTerms = false;
   TersoffDev p;
   GB_HD int nel() const { return p.nel; }
+  GB_HD int pair(int i, int j) const { return pair_index(i, j, p.nel); }
   GB_HD double r1(int t) const { return p.r1[t]; }
   GB_HD double r2(int t) const { return p.r2[t]; }
   GB_HD double r1sq(int t) const { return p.r1sq[t]; }
@@ -246,7 +290,7 @@ struct TersoffPot {
   GB_HD double hpar(int eli, int /*ikpot*/) const { return p.h[eli]; }
   // h(r_ij - r_ik) (tersoff_func.f90:168-211), pair (i,k).
   template <class R>
-  GB_HD void h(int ikpot, R dr, R &val, R &dval) const {
+  GB_HD void h(int /*eli*/, int /*ijpot*/, int ikpot, R dr, R &val, R &dval) const {
     const double mu = p.mubo[ikpot];
     if (mu == 0.0) {
       val = R(1);
@@ -302,6 +346,7 @@ struct TersoffPot {
 };
 
 struct KumagaiPot {
+  static constexpr bool kTripletH = false;  // h constants per element triplet
   static constexpr bool kPairTerms = false;
   KumagaiDev p;
   GB_HD double hpar(int eli, int /*ikpot*/) const { return p.h[eli]; }
@@ -319,6 +364,7 @@ struct KumagaiPot {
     val = c1 + hcos * v;
   }
   GB_HD int nel() const { return 1; }
+  GB_HD int pair(int /*i*/, int /*j*/) const { return 0; }
   GB_HD double r1(int t) const { return p.r1[t]; }
   GB_HD double r2(int t) const { return p.r2[t]; }
   GB_HD double r1sq(int t) const { return p.r1sq[t]; }
@@ -351,7 +397,7 @@ struct KumagaiPot {
   // h (kumagai_func.f90:179-221); the beta == 3 branch omits alpha in the
   // exponent exactly as the reference does (:211-213).
   template <class R>
-  GB_HD void h(int ikpot, R dr, R &val, R &dval) const {
+  GB_HD void h(int /*eli*/, int /*ijpot*/, int ikpot, R dr, R &val, R &dval) const {
     const R alpha = (R)p.alpha[ikpot];
     if (p.alpha[ikpot] == 0.0) {
       val = R(1);
@@ -401,9 +447,11 @@ struct KumagaiPot {
 };
 
 struct BrennerPot {
+  static constexpr bool kTripletH = false;  // h constants per element triplet
   static constexpr bool kPairTerms = true;
   BrennerDev p;
   GB_HD int nel() const { return p.nel; }
+  GB_HD int pair(int i, int j) const { return pair_index(i, j, p.nel); }
   GB_HD double r1(int t) const { return p.r1[t]; }
   GB_HD double r2(int t) const { return p.r2[t]; }
   GB_HD double r1sq(int t) const { return p.r1sq[t]; }
@@ -436,7 +484,7 @@ struct BrennerPot {
   GB_HD double hpar(int /*eli*/, int ikpot) const { return p.hneg[ikpot]; }
   // h (brenner_func.f90:178-214), pair (i,k)
   template <class R>
-  GB_HD void h(int ikpot, R dr, R &val, R &dval) const {
+  GB_HD void h(int /*eli*/, int /*ijpot*/, int ikpot, R dr, R &val, R &dval) const {
     const double mu = p.mu[ikpot];
     if (mu == 0.0) {
       val = R(1);
@@ -474,6 +522,43 @@ struct BrennerPot {
     } else {
       b = R(1);
       dfb = R(0);
+    }
+  }
+};
+
+// Juslin: Brenner's VA, VR, g and b on ordered pairs; h per triplet
+// (juslin_func.f90:257-294).  For pairs t = j + i nel the triplet (i, j, k)
+// of bonds ij (t) and ik (ikpot) is ikpot + nel (t - i).
+struct JuslinPot : BrennerPot {
+  static constexpr bool kTripletH = true;
+  double alpha[27], omega[27];
+  int m3[27];
+  explicit JuslinPot(const JuslinDev &d) : BrennerPot{d} {
+    for (int q = 0; q < 27; q++) {
+      alpha[q] = d.alpha[q];
+      omega[q] = d.omega[q];
+      m3[q] = d.m3[q];
+    }
+  }
+  GB_HD int pair(int i, int j) const { return j + i * p.nel; }
+  template <class R>
+  GB_HD void h(int eli, int ijpot, int ikpot, R dr, R &val, R &dval) const {
+    const int q = ikpot + p.nel * (ijpot - eli);
+    const R al = (R)alpha[q], om = (R)omega[q];
+    const int m = m3[q];
+    if (m == 1) {
+      val = om * gexp<R>(al * dr);
+      dval = al * val;
+    } else if (m == 3) {
+      const R arg = al * dr;
+      val = om * gexp<R>(arg * arg * arg);
+      dval = R(3) * al * arg * arg * val;
+    } else {
+      const R arg = al * dr;
+      R pw = R(1);
+      for (int k = 0; k < m - 1; k++) pw *= arg;
+      val = om * gexp<R>(pw * arg);
+      dval = R(m) * pw * al * val;
     }
   }
 };

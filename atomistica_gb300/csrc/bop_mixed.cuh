@@ -49,10 +49,17 @@ struct MxElem {
 // el[] holds the g and bond-order constants per centre element (Tersoff,
 // Kumagai) or per element pair (Brenner: g of the (i,k) pair, b of the (i,j)
 // pair; the kernels index it through el_g / el_b).
+// Juslin's h(dr) = om e^{(hs dr)^hm} per element triplet (hm = 0: h = om).
+struct MxTrip {
+  ff hs, om;
+  int hm;
+};
 struct MxParams {
-  int kind;  // 0 Tersoff and Brenner, 1 Kumagai
-  MxPair pr[6];
-  MxElem el[6];
+  int kind;  // 0 Tersoff, Brenner and Juslin, 1 Kumagai
+  int nel;
+  MxPair pr[9];
+  MxElem el[9];
+  MxTrip tr[27];  // Juslin only
   ff A[3][3];
 };
 
@@ -114,10 +121,11 @@ inline MxParams make_mx(const TersoffDev &d, const double A[3][3]) {
 // Brenner: VA = -Bc e^{-cA r} with Bc = VA_f e^{expA r0} (and VR alike), the
 // Tersoff g with gamma for omega and -h for h, the Tersoff b with beta = xi = 1
 // and the pair's n; all constants per pair.
-inline MxParams make_mx(const BrennerDev &d, const double A[3][3]) {
+inline MxParams make_mx(const BrennerDev &d, const double A[3][3], int np = -1) {
   MxParams m{};
   m.kind = 0;
-  const int np = d.nel * (d.nel + 1) / 2;
+  m.nel = d.nel;
+  if (np < 0) np = d.nel * (d.nel + 1) / 2;
   for (int q = 0; q < np; q++) {
     MxPair &pq = m.pr[q];
     pq.cA = ffh(d.expA[q]);
@@ -176,6 +184,21 @@ inline MxParams make_mx(const KumagaiDev &d, const double A[3][3]) {
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) m.A[a][k] = ffh(A[a][k]);
   return m;
+}
+
+// Juslin: Brenner's constants on the nel^2 ordered pairs and h per triplet.
+inline MxParams make_mx(const JuslinPot &P, const double A[3][3]) {
+  MxParams m = make_mx(P.p, A, P.p.nel * P.p.nel);
+  for (int q = 0; q < P.p.nel * P.p.nel * P.p.nel; q++) {
+    m.tr[q].hs = ffh(P.alpha[q]);
+    m.tr[q].om = ffh(P.omega[q]);
+    m.tr[q].hm = P.alpha[q] == 0.0 ? 0 : P.m3[q];
+  }
+  return m;
+}
+template <class Pot>
+inline MxParams make_mx(const Pot &P, const double A[3][3]) {
+  return make_mx(P.p, A);
 }
 
 
@@ -281,6 +304,34 @@ __device__ __forceinline__ void g_ff(const MxParams &mp, int eli, int ikpot, ff 
   }
 }
 
+// Juslin's h (juslin_func.f90:257-294) of triplet q.
+__device__ __forceinline__ void h3_f(const MxTrip &q, float dr, float &val, float &dval) {
+  if (q.hm == 0) {
+    val = q.om.hi;
+    dval = 0.0f;
+    return;
+  }
+  const float x = q.hs.hi * dr;
+  float pw = 1.0f;
+  for (int k = 1; k < q.hm; k++) pw *= x;
+  val = q.om.hi * expf(pw * x);
+  dval = (float)q.hm * q.hs.hi * pw * val;
+}
+
+__device__ __forceinline__ void h3_ff(const MxTrip &q, ff dr, const ff *etab, ff &val,
+                                      ff &dval) {
+  if (q.hm == 0) {
+    val = q.om;
+    dval = ff_make(0.0f, 0.0f);
+    return;
+  }
+  const ff x = ff_mul(q.hs, dr);
+  ff pw = ff_make(1.0f, 0.0f);
+  for (int k = 1; k < q.hm; k++) pw = ff_mul(pw, x);
+  val = ff_mul(q.om, ff_exp(ff_mul(pw, x), etab));
+  dval = ff_mul(ff_mulf(q.hs, (float)q.hm), ff_mul(pw, val));
+}
+
 // h(dr), dr = r_ij - r_ik (tersoff_func.f90:168-211, kumagai_func.f90:179-221).
 __device__ __forceinline__ void h_f(const MxPair &q, float dr, float &val, float &dval) {
   if (q.hm == 0) {
@@ -375,11 +426,13 @@ __device__ __forceinline__ void bo_hot(const MxParams &mp, int eli, int t, ff P0
 // Three-body k loop of bond lb in FP32 (h - cos theta from an ff dot
 // product, bop_kernel.f90:1171-1343).  Also returns sum_k |d zeta/d r_k| for
 // the error estimate.
-template <bool kWat, bool kPP>
+template <bool kWat, bool kPP, bool kTri>
 __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, int lb, int s,
                                          int z, int eli, ff *trow, float &zeta, float dbj[3],
                                          float wk[9], float &sumdk) {
   const int nbt = L.nbt, ntrip = L.ntrip;
+  // kTri: triplet (i, j, k) = ikpot + nel (ijpot - eli) of the ordered pairs
+  const int tri0 = kTri ? mp.nel * (((L.meta[lb] >> 8) & 0xf) - eli) : 0;
   const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
   const float rlij = L.r[lb].hi, rinvj = L.rinv[lb].hi;
   const ff h0 = mp.el[eli].h;
@@ -414,7 +467,10 @@ __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, 
     const ff dh0 = two_sum(h.hi, -s2.hi);
     const float hcf = dh0.hi + ((dh0.lo + h.lo) - clo);
     float hv, dh;
-    h_f(mp.pr[ikpot], rlij - rlik, hv, dh);
+    if (kTri)
+      h3_f(mp.tr[tri0 + ikpot], rlij - rlik, hv, dh);
+    else
+      h_f(mp.pr[ikpot], rlij - rlik, hv, dh);
     float gv, dg;
     g_f(mp, el_g<kPP>(eli, ikpot), ikpot, hcf, gv, dg);
     const float dzfac = fcik * dg * hv;
@@ -441,11 +497,12 @@ __device__ __forceinline__ void kloop_mx(const MxParams &mp, const MxLayout &L, 
 // The same k loop in ff arithmetic for the hot bonds, over the slots
 // q = q0, q0 + dq, ... of bond lb's row (the partial sums of zeta, d zeta /
 // d r_j and the virial term are added up across the lanes afterwards).
-template <bool kWat, bool kPP>
+template <bool kWat, bool kPP, bool kTri>
 __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, int lb, int s,
                                          int z, int eli, ff *trow, const ff *etab, int q0,
                                          int dq, ff &zeta, ff dbj[3], ff wk[9]) {
   const int nbt = L.nbt, ntrip = L.ntrip;
+  const int tri0 = kTri ? mp.nel * (((L.meta[lb] >> 8) & 0xf) - eli) : 0;
   const ff rnij[3] = {L.rn[lb], L.rn[nbt + lb], L.rn[2 * nbt + lb]};
   const ff rlij = L.r[lb], rinvj = L.rinv[lb];
   const ff h0 = mp.el[eli].h;
@@ -463,7 +520,10 @@ __device__ __forceinline__ void kloop_ff(const MxParams &mp, const MxLayout &L, 
     const ff rnik[3] = {L.rn[lk], L.rn[nbt + lk], L.rn[2 * nbt + lk]};
     const ff rlik = L.r[lk], rinvk = L.rinv[lk], fcik = L.fc[lk], dfcik = L.dfc[lk];
     ff hv, dh;
-    h_ff(mp.pr[ikpot], ff_sub(rlij, rlik), etab, hv, dh);
+    if (kTri)
+      h3_ff(mp.tr[tri0 + ikpot], ff_sub(rlij, rlik), etab, hv, dh);
+    else
+      h_ff(mp.pr[ikpot], ff_sub(rlij, rlik), etab, hv, dh);
     ff cs = ff_mul(rnik[0], rnij[0]);
     cs = ff_add(cs, ff_mul(rnik[1], rnij[1]));
     cs = ff_add(cs, ff_mul(rnik[2], rnij[2]));
@@ -686,7 +746,7 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
         ff r2 = ff_mul(rij[0], rij[0]);
         r2 = ff_add(r2, ff_mul(rij[1], rij[1]));
         r2 = ff_add(r2, ff_mul(rij[2], rij[2]));
-        const int t = pair_index(eli, elj, nel);
+        const int t = pot.pair(eli, elj);
         meta |= t << 8;
         const float r2f = r2.hi + r2.lo;
         const MxPair &pp = mp.pr[t];
@@ -766,7 +826,8 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       if (kWat)
 #pragma unroll
         for (int c = 0; c < 9; c++) wk[c] = 0.0f;
-      kloop_mx<kWat, Pot::kPairTerms>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk, sumdk);
+      kloop_mx<kWat, Pot::kPairTerms, Pot::kTripletH>(mp, L, lb, s, z, eli, trow, zeta, dbj, wk,
+                                                       sumdk);
       // A zeta below 1e-30 would overflow the FP32 range inside ln/exp: such a
       // bond (and any non-finite estimate) takes the accurate path.
       const bool tiny = zeta > 0.0f && zeta < 1.0e-30f;
@@ -822,8 +883,9 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
           lb = L.hot[hq];
           const int ai = L.meta[lb] & 0xff;
           const int s = L.aseed[ai], z = L.aseed[ai + 1] - s, p = lb - s;
-          kloop_ff<kWat, Pot::kPairTerms>(mp, L, lb, s, z, L.el[ai], L.t + L.toff[ai] + p * z,
-                                          s_exp, gl, kHotLanes, zeta, dbj, wk);
+          kloop_ff<kWat, Pot::kPairTerms, Pot::kTripletH>(mp, L, lb, s, z, L.el[ai],
+                                                           L.t + L.toff[ai] + p * z, s_exp, gl,
+                                                           kHotLanes, zeta, dbj, wk);
         }
 #pragma unroll
         for (int o = 1; o < kHotLanes; o <<= 1) {

@@ -76,12 +76,15 @@ struct ScrPair {
   double in_l2, in_h, in_h2, out_l, out_h, bo_h, max_cut_sq, Cmin, Cmax, dC, C_dr_cut;
 };
 struct ScrDev {
-  ScrPair pr[6];
+  ScrPair pr[9];
   double thr_s, thr_dot;  // ln 1e-6; 1e-10 as a default-real literal
 };
 
+// guard: C_dr_cut = 1 for Cmax <= 2 (default_bind_to_func.f90:62-68,
+// brenner_module.f90:198-204); the Juslin module takes Cmax^2 / (4 (Cmax - 1))
+// for every pair (juslin_module.f90:305-307).
 inline ScrDev make_scr_dev(const double *r1, const double *r2, int npairs,
-                           const gb_screening_params_t &s) {
+                           const gb_screening_params_t &s, bool guard = true) {
   ScrDev d{};
   for (int q = 0; q < npairs; q++) {
     ScrPair &p = d.pr[q];
@@ -99,7 +102,8 @@ inline ScrDev make_scr_dev(const double *r1, const double *r2, int npairs,
     p.Cmin = s.Cmin[q];
     p.Cmax = s.Cmax[q];
     p.dC = s.Cmax[q] - s.Cmin[q];
-    p.C_dr_cut = s.Cmax[q] > 2.0 ? s.Cmax[q] * s.Cmax[q] / (4 * (s.Cmax[q] - 1)) : 1.0;
+    p.C_dr_cut = (s.Cmax[q] > 2.0 || !guard) ? s.Cmax[q] * s.Cmax[q] / (4 * (s.Cmax[q] - 1))
+                                             : 1.0;
   }
   d.thr_s = std::log(1e-6);
   d.thr_dot = (double)1e-10f;
@@ -339,7 +343,7 @@ __global__ void __launch_bounds__(kScrThreads)
         const int j = scr_get(a, pi, W, cached, s, jn, rij, rlij, shj);
         const int elj = a.el[j];
         if (elj >= 0) {
-          const int t = pair_index(eli, elj, nel);
+          const int t = pot.pair(eli, elj);
           const ScrPair &P = sd.pr[t];
           bd.jn = jn;
           bd.typ = t;
@@ -485,7 +489,7 @@ __global__ void __launch_bounds__(kScrThreads)
           const double rik[3] = {rlik * rnik[0], rlik * rnik[1], rlik * rnik[2]};
           const double fcik = Bk.fcbo, dfcikr = Bk.dfcbo;
           double h_Dr, dh_dDr;
-          pot.template h<double>(ikpot, rlij - rlik, h_Dr, dh_dDr);
+          pot.template h<double>(eli, t, ikpot, rlij - rlik, h_Dr, dh_dDr);
           const double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
           double g_costh, dg_dcosth;
           pot.template g_hc<double>(eli, ikpot, pot.hpar(eli, ikpot) - costh, g_costh, dg_dcosth);
@@ -566,7 +570,7 @@ __global__ void __launch_bounds__(kScrThreads)
             const double rlij = Bj.len, rlijr = 1.0 / rlij;
             const double rnij[3] = {Bj.nm[0], Bj.nm[1], Bj.nm[2]};
             double h_Dr, dh_dDr;
-            pot.template h<double>(ikpot, rlij - rlik, h_Dr, dh_dDr);
+            pot.template h<double>(eli, Bj.typ, ikpot, rlij - rlik, h_Dr, dh_dDr);
             const double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
             double g_costh, dg_dcosth;
             pot.template g_hc<double>(eli, ikpot, pot.hpar(eli, ikpot) - costh, g_costh, dg_dcosth);

@@ -11,7 +11,7 @@
 
 namespace gb {
 
-enum PotKind { kTersoff = 0, kKumagai = 1, kEAM = 2, kBrenner = 3 };
+enum PotKind { kTersoff = 0, kKumagai = 1, kEAM = 2, kBrenner = 3, kJuslin = 4 };
 
 // Uniform natural cubic spline tables (simple_spline.f90:127-195) built on the
 // host.  Device layout: 8 doubles per interval k = {y_k, c1_k, c2_k, c3_k,
@@ -72,7 +72,8 @@ struct Potential {
   gb_tersoff_params_t tp{};
   gb_kumagai_params_t kp{};
   gb_brenner_params_t bp{};
-  bool screened = false;        // TersoffScr / KumagaiScr / BrennerScr
+  gb_juslin_params_t jp{};      // ordered-pair entries filled as juslin_module.f90:273-300
+  bool screened = false;        // TersoffScr / KumagaiScr / BrennerScr / JuslinScr
   gb_screening_params_t scr{};  // their outer / bond-order cutoffs, Cmin, Cmax
   std::unique_ptr<EamTables> eam;
 
@@ -120,6 +121,10 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
                 bool want_wat);
 // Element count / atomic number of element q of the potential; its stream.
 int pot_nel(const Potential &pot);
+// Number of element-pair entries (nel (nel + 1) / 2 symmetric pairs; Juslin:
+// nel^2 ordered pairs) and the entry of the database elements (a, b).
+int pot_npairs(const Potential &pot);
+int pot_pair(const Potential &pot, int a, int b);
 int pot_Z(const Potential &pot, int q);
 // Inner cutoffs r1, r2 per pair of a bond-order potential.
 const double *bop_r1(const Potential &pot);

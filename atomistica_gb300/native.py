@@ -26,7 +26,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import GB_PRECISION_FP64, GB_PRECISION_MIXED, check, load
-from .parameters import (BRENNER_KEYS, SCREENING_KEYS, Erhart_PRB_71_035211_SiC,
+from .parameters import (BRENNER_KEYS, JUSLIN_KEYS, SCREENING_KEYS, Erhart_PRB_71_035211_SiC,
+                         Juslin_JAP_98_123520_WCH,
                          Kumagai_CompMaterSci_39_457_Si,
                          Kumagai_CompMaterSci_39_457_Si__Scr, Tersoff_PRB_39_5566_Si_C,
                          Tersoff_PRB_39_5566_Si_C__Scr, atomic_numbers)
@@ -268,6 +269,34 @@ def brenner_params(params, base=Erhart_PRB_71_035211_SiC):
             _fill(p.m, [int(v) for v in d[k]], npair)
         else:
             _fill(getattr(p, k), [float(v) for v in d[k]], npair)
+    return p
+
+
+def juslin_params(params, base=Juslin_JAP_98_123520_WCH):
+    """gb_juslin_params_t from a parameter dict (pair arrays per ordered
+    element pair, alpha / omega / m per element triplet); keys not given keep
+    the values of ``base``.  m defaults to 1 for every triplet."""
+    d = dict(base)
+    d.update({k: v for k, v in params.items() if not k.startswith("__")})
+    p = _lib.JuslinParams()
+    els = d["el"]
+    p.nel = len(els)
+    if not 1 <= p.nel <= 3:
+        raise ValueError("Juslin supports 1..3 elements")
+    for q, s in enumerate(els):
+        p.Z[q] = atomic_numbers[s]
+    npair, ntrip = p.nel * p.nel, p.nel ** 3
+    for k in JUSLIN_KEYS:
+        if len(d[k]) < npair:
+            raise ValueError("Juslin: %s needs %d entries (one per ordered element pair)"
+                             % (k, npair))
+        _fill(getattr(p, k), [float(v) for v in d[k]], npair)
+    ms = d.get("m", [1] * ntrip)
+    for k, vals in (("alpha", d["alpha"]), ("omega", d["omega"]), ("m", ms)):
+        if len(vals) < ntrip:
+            raise ValueError("Juslin: %s needs %d entries (one per element triplet)"
+                             % (k, ntrip))
+        _fill(getattr(p, k), [int(v) if k == "m" else float(v) for v in vals], ntrip)
     return p
 
 
@@ -526,6 +555,52 @@ class BrennerScr(_Potential):
                                              ctypes.byref(sp)), "BrennerScr")
         else:
             check(self._L.gb_brenner_scr_new(ctypes.byref(self._h), None, None), "BrennerScr")
+        self.set_precision(precision)
+
+
+class Juslin(_Potential):
+    """Juslin-form bond-order potential (src/potentials/bop/juslin/): Brenner's
+    functions on ordered element pairs with a three-body h per element
+    triplet.  Default: the compiled-in W-C-H set (juslin_params.f90:75-108,
+    W-H cutoff 1.95-2.35 A); the front-end's Juslin_JAP_98_123520_WCH
+    dictionary has 2.68-2.96 A there."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        if params:
+            p = juslin_params(params)
+            check(self._L.gb_juslin_new(ctypes.byref(self._h), ctypes.byref(p)), "Juslin")
+        else:
+            check(self._L.gb_juslin_new(ctypes.byref(self._h), None), "Juslin")
+        self.set_precision(precision)
+
+
+# The compiled-in default of JuslinScr (juslin_params.f90:95-103 under
+# SCREENING): the screened r1, r2 for the outer and bond-order cutoffs too,
+# Cmin = 1, Cmax = 3.  The front-end's Juslin_JAP_98_123520_WCH__Scr table
+# differs in Cmin and Cmax.
+_JUSLIN_SCR_DEFAULT = dict(
+    Juslin_JAP_98_123520_WCH,
+    or1=list(Juslin_JAP_98_123520_WCH["r1"]), or2=list(Juslin_JAP_98_123520_WCH["r2"]),
+    bor1=list(Juslin_JAP_98_123520_WCH["r1"]), bor2=list(Juslin_JAP_98_123520_WCH["r2"]),
+    Cmin=[1.0, 1.0, 1.0, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0],
+    Cmax=[3.0, 3.0, 3.0, 0.0, 3.0, 3.0, 0.0, 3.0, 3.0])
+
+
+class JuslinScr(_Potential):
+    """Screened Juslin potential (src/potentials/bop/juslin/juslin_scr.f90):
+    FP64 only; default parameters the compiled-in screened W-C-H set (pass
+    **Juslin_JAP_98_123520_WCH__Scr for the front-end's table)."""
+
+    def __init__(self, precision="fp64", **params):
+        super().__init__()
+        if params:
+            p = juslin_params(params, _JUSLIN_SCR_DEFAULT)
+            sp = screening_params(params, _JUSLIN_SCR_DEFAULT)
+            check(self._L.gb_juslin_scr_new(ctypes.byref(self._h), ctypes.byref(p),
+                                            ctypes.byref(sp)), "JuslinScr")
+        else:
+            check(self._L.gb_juslin_scr_new(ctypes.byref(self._h), None, None), "JuslinScr")
         self.set_precision(precision)
 
 

@@ -11,7 +11,9 @@ The numerical values are those of the original publications as tabulated in
 src/potentials/bop/tersoff/tersoff_params.f90:99-142,
 src/potentials/bop/kumagai/kumagai_params.f90:97-132 and
 src/potentials/bop/brenner/brenner_params.f90:67-200 (Brenner-form sets,
-whose arrays are all per element pair).
+whose arrays are all per element pair) and
+src/potentials/bop/juslin/juslin_params.f90:75-145 (Juslin-form sets, arrays
+per ordered element pair and per element triplet).
 """
 
 from math import log, sqrt
@@ -215,6 +217,82 @@ Brenner_PRB_42_9458_C_II = {
     "c": [330.0], "d": [3.5], "h": [1.0], "mu": [0.0], "n": [1.0 / (2 * 0.5)], "m": [1],
     "r1": [1.70], "r2": [2.00],
 }
+
+# Juslin-form sets (src/potentials/bop/juslin/): the Brenner functions with
+# every pair array per ORDERED element pair, entry j + i*nel (src/macros.inc:139;
+# an entry with r0 < 0 takes the constants of its mirror pair), and h(dr) =
+# omega exp((alpha dr)^m) with alpha, omega, m per element triplet, entry
+# k + nel*(j + nel*i) (src/macros.inc:146).  m defaults to 1.
+JUSLIN_KEYS = ("D0", "r0", "S", "beta", "gamma", "c", "d", "h", "n", "r1", "r2")
+JUSLIN_TRIPLET_KEYS = ("alpha", "omega", "m")
+
+_JUSLIN_ALPHA_H = [0.0] * 14 + [4.0, 0.0, 4.0, 4.0, 0.0, 0.0, 0.0, 0.0, 4.0, 4.0, 0.0, 4.0, 4.0]
+_JUSLIN_OMEGA = [1.0] * 16 + [2.94586, 4.54415, 1.0, 1.0, 1.0, 1.0, 0.33946, 0.22006,
+                              1.0, 1.0, 1.0]
+
+# Juslin et al., J. Appl. Phys. 98, 123520 (2005); W-C-H
+# (juslin_params.f90:75-108, parameters.py:278-295).
+Juslin_JAP_98_123520_WCH = {
+    "__ref__": "Juslin N., Erhart P., Traskelin P., Nord J., Henriksson K.O.E, Nordlund K., "
+               "Salonen E., Albe K., J. Appl. Phys. 98, 123520 (2005)",
+    "el": ["W", "C", "H"],
+    "D0": [5.41861, 6.64, 2.748, 0.0, 6.0, 3.6422, 0.0, 3.642, 4.7509],
+    "r0": [2.34095, 1.90547, 1.727, -1.0, 1.39, 1.1199, -1.0, 1.1199, 0.74144],
+    "S": [1.92708, 2.96149, 1.2489, 0.0, 1.22, 1.69077, 0.0, 1.69077, 2.3432],
+    "beta": [1.38528, 1.80370, 1.52328, 0.0, 2.1, 1.9583, 0.0, 1.9583, 1.9436],
+    "gamma": [0.00188227, 0.072855, 0.0054, 0.0, 0.00020813, 0.00020813, 0.0, 12.33, 12.33],
+    "c": [2.14969, 1.10304, 1.788, 0.0, 330.0, 330.0, 0.0, 0.0, 0.0],
+    "d": [0.17126, 0.33018, 0.8255, 0.0, 3.5, 3.5, 0.0, 1.0, 1.0],
+    "h": [-0.27780, 0.75107, 0.38912, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0],
+    "n": [1.0, 1.0, 1.0, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0],
+    "alpha": [0.45876, 0.0, 0.0, 0.45876, 0.0, 0.0, 0.45876] + _JUSLIN_ALPHA_H[7:],
+    "omega": list(_JUSLIN_OMEGA),
+    "r1": [3.20, 2.60, 2.68, 0.0, 1.70, 1.30, 0.0, 1.30, 1.10],
+    "r2": [3.80, 3.00, 2.96, 0.0, 2.00, 1.80, 0.0, 1.80, 1.70],
+}
+
+# The screened set of the Python front-end (parameters.py:297-309): the outer
+# and bond-order cutoffs equal the inner ones, and Cmin / Cmax are set to the
+# r1 / r2 values as the reference tabulates them.
+Juslin_JAP_98_123520_WCH__Scr = dict(
+    Juslin_JAP_98_123520_WCH,
+    or1=list(Juslin_JAP_98_123520_WCH["r1"]), or2=list(Juslin_JAP_98_123520_WCH["r2"]),
+    bor1=list(Juslin_JAP_98_123520_WCH["r1"]), bor2=list(Juslin_JAP_98_123520_WCH["r2"]),
+    Cmin=list(Juslin_JAP_98_123520_WCH["r1"]), Cmax=list(Juslin_JAP_98_123520_WCH["r2"]),
+    m=[1] * 27,
+)
+
+# Kuopanportti et al., Comp. Mat. Sci. 111, 525 (2016); Fe-C-H
+# (parameters.py:313-327).
+Kuopanportti_CMS_111_525_FeCH = {
+    "__ref__": "Kuopanportti P., Hayward, N., Fu C., Kuronen A., Nordlund K., "
+               "Comp. Mat. Sci. 111, 525 (2016)",
+    "el": ["Fe", "C", "H"],
+    "D0": [1.5, 4.82645134, 1.630, 0.0, 6.0, 3.6422, 0.0, 3.642, 4.7509],
+    "r0": [2.29, 1.47736510, 1.589, -1.0, 1.39, 1.1199, -1.0, 1.1199, 0.74144],
+    "S": [2.0693, 1.43134755, 4.000, 0.0, 1.22, 1.69077, 0.0, 1.69077, 2.3432],
+    "beta": [1.4, 1.63208170, 1.875, 0.0, 2.1, 1.9583, 0.0, 1.9583, 1.9436],
+    "gamma": [0.01158, 0.00205862, 0.01332, 0.0, 0.00020813, 0.00020813, 0.0, 12.33, 12.33],
+    "c": [1.2899, 8.95583221, 424.5, 0.0, 330.0, 330.0, 0.0, 0.0, 0.0],
+    "d": [0.3413, 0.72062047, 7.282, 0.0, 3.5, 3.5, 0.0, 1.0, 1.0],
+    "h": [-0.26, 0.87099874, -0.1091, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0],
+    "n": [1.0, 1.0, 1.0, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0],
+    "alpha": list(_JUSLIN_ALPHA_H),
+    "omega": list(_JUSLIN_OMEGA),
+    "r1": [2.95, 2.30, 2.2974, 0.0, 1.70, 1.30, 0.0, 1.30, 1.10],
+    "r2": [3.35, 2.70, 2.6966, 0.0, 2.00, 1.80, 0.0, 1.80, 1.70],
+}
+
+# parameters.py:330-342
+Kuopanportti_CMS_111_525_FeCH__Scr = dict(
+    Kuopanportti_CMS_111_525_FeCH,
+    or1=list(Kuopanportti_CMS_111_525_FeCH["r1"]), or2=list(Kuopanportti_CMS_111_525_FeCH["r2"]),
+    bor1=list(Kuopanportti_CMS_111_525_FeCH["r1"]),
+    bor2=list(Kuopanportti_CMS_111_525_FeCH["r2"]),
+    Cmin=[1.0, 1.0, 1.0, 0.0, 1.0, 1.0, 0.0, 1.0, 1.0],
+    Cmax=[3.0, 3.0, 3.0, 0.0, 3.0, 3.0, 0.0, 3.0, 3.0],
+    m=[1] * 27,
+)
 
 # The 14 continuous Tersoff parameters of a single-element set, in the order
 # used by the parameter-gradient interface.

@@ -158,13 +158,31 @@ typedef struct gb_brenner_params {
   double r1[6], r2[6];
 } gb_brenner_params_t;
 
-/* Extra parameters of the screened variants TersoffScr / KumagaiScr
- * (tersoff_params.f90:81-90 under SCREENING), per element pair: outer
- * (attractive/repulsive) cutoff or1 < or2, bond-order cutoff bor1 < bor2 and
- * the screening window Cmin < Cmax.  The inner cutoff is r1 < r2 of the base
- * parameter set (exp_cutoff form, cutoff.f90:232-293). */
+/* Juslin parameter set: layout of BOP_DB_TYPE
+ * (src/potentials/bop/juslin/juslin_params.f90:31-70).  Pair arrays are per
+ * ORDERED element pair, entry j + i*nel (0-based, src/macros.inc:139); an
+ * entry with r0 < 0 takes the constants of its mirror pair (j, i) as the
+ * reference's bind_to does (juslin_module.f90:273-300).  The h(dr) constants
+ * alpha, omega, m are per element triplet (i, j, k), entry k + nel*(j + nel*i)
+ * (src/macros.inc:146): h = omega exp((alpha dr)^m). */
+typedef struct gb_juslin_params {
+  int nel;
+  int Z[3];
+  double D0[9], r0[9], S[9], beta[9], gamma[9], c[9], d[9], h[9], n[9];
+  double alpha[27], omega[27];
+  int m[27];
+  double r1[9], r2[9];
+} gb_juslin_params_t;
+
+/* Extra parameters of the screened variants TersoffScr / KumagaiScr /
+ * BrennerScr / JuslinScr (tersoff_params.f90:81-90 under SCREENING), per
+ * element pair entry (the first nel(nel+1)/2 symmetric entries; JuslinScr:
+ * nel^2 ordered entries): outer (attractive/repulsive) cutoff or1 < or2,
+ * bond-order cutoff bor1 < bor2 and the screening window Cmin < Cmax.  The
+ * inner cutoff is r1 < r2 of the base parameter set (exp_cutoff form,
+ * cutoff.f90:232-293). */
 typedef struct gb_screening_params {
-  double or1[6], or2[6], bor1[6], bor2[6], Cmin[6], Cmax[6];
+  double or1[9], or2[9], bor1[9], bor2[9], Cmin[9], Cmax[9];
 } gb_screening_params_t;
 
 /* python_tersoff_new + register (parameters set through a struct instead of
@@ -191,6 +209,16 @@ int gb_brenner_new(gb_potential_t **pot, const gb_brenner_params_t *params);
  * Erhart_PRB_71_035211_SiC__Scr set.  FP64 only. */
 int gb_brenner_scr_new(gb_potential_t **pot, const gb_brenner_params_t *params,
                        const gb_screening_params_t *scr);
+/* python_juslin_new (juslin.f90, juslin_module.f90:27-406): NULL params =
+ * the Juslin_J_Appl_Phys_98_123520_WCH set (juslin_params.f90:75-108).
+ * Rejects d = 0 and S <= 1 as the reference's bind_to does. */
+int gb_juslin_new(gb_potential_t **pot, const gb_juslin_params_t *params);
+/* python_juslin_scr_new (juslin_scr.f90): NULL params / scr = the compiled-in
+ * screened W-C-H set (juslin_params.f90:95-103 under SCREENING: Cmin = 1,
+ * Cmax = 3).  C_dr_cut = Cmax^2 / (4 (Cmax - 1)) for every pair
+ * (juslin_module.f90:305-307).  FP64 only. */
+int gb_juslin_scr_new(gb_potential_t **pot, const gb_juslin_params_t *params,
+                      const gb_screening_params_t *scr);
 /* python_tabulated_alloy_eam_new + init(fn=...) (tabulated_alloy_eam.f90:147-259):
  * reads a DYNAMO setfl file. */
 int gb_tabulated_alloy_eam_new(gb_potential_t **pot, const char *fn);
@@ -267,6 +295,13 @@ int gb_brenner_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neig
                                  const int *mask, double *epot_per_at, double *epot_per_bond,
                                  double *f_per_bond, double *wpot_per_at,
                                  double *wpot_per_bond, int *ierror);
+int gb_juslin_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                      int *ierror);
+int gb_juslin_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                                const double *q, double *epot, double *f, double *wpot,
+                                const int *mask, double *epot_per_at, double *epot_per_bond,
+                                double *f_per_bond, double *wpot_per_at,
+                                double *wpot_per_bond, int *ierror);
 int gb_tabulated_alloy_eam_bind_to(gb_potential_t *pot, gb_particles_t *p,
                                    gb_neighbors_t *nl, int *ierror);
 int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *pot, gb_particles_t *p,

@@ -423,7 +423,7 @@ struct orc_tersoff_params {
 // SCREENING): outer (attractive/repulsive) and bond-order cutoffs, screening
 // window Cmin < C < Cmax; per pair.  The inner cutoff is r1/r2 of the base set.
 struct orc_scr_params {
-  double or1[6], or2[6], bor1[6], bor2[6], Cmin[6], Cmax[6];
+  double or1[9], or2[9], bor1[9], bor2[9], Cmin[9], Cmax[9];
 };
 
 struct orc_kumagai_params {
@@ -446,6 +446,18 @@ struct orc_brenner_params {
   double r1[6], r2[6];
 };
 
+// Juslin parameter set (juslin_params.f90:31-70): pair arrays per ordered
+// element pair j + i nel (macros.inc:139), h constants per element triplet
+// k + nel (j + nel i) (macros.inc:146).
+struct orc_juslin_params {
+  int nel;
+  int Z[3];
+  double D0[9], r0[9], S[9], beta[9], gamma[9], c[9], d[9], h[9], n[9];
+  double alpha[27], omega[27];
+  int m[27];
+  double r1[9], r2[9];
+};
+
 }  // extern "C"
 
 namespace {
@@ -455,6 +467,9 @@ struct TersoffFn {
   const orc_tersoff_params &p;
   explicit TersoffFn(const orc_tersoff_params &q) : p(q) {}
   int nel() const { return p.nel; }
+  int npairs() const { return p.nel * (p.nel + 1) / 2; }
+  int pair(int i, int j) const { return pair_index(i, j, p.nel); }
+  bool cdr_guard() const { return true; }
   double r1(int ij) const { return p.r1[ij]; }
   double r2(int ij) const { return p.r2[ij]; }
   void VA(int ij, double dr, double &val, double &dval) const {
@@ -490,7 +505,8 @@ struct TersoffFn {
       dfbij = 0.0;
     }
   }
-  void h(int ikpot, double dr, double &val, double &dval) const {
+  void h(int /*eli*/, int /*elj*/, int /*elk*/, int ikpot, double dr, double &val,
+         double &dval) const {
     double mu = p.mubo[ikpot];
     if (mu == 0.0) {
       val = 1.0;
@@ -517,6 +533,9 @@ struct KumagaiFn {
   const orc_kumagai_params &p;
   explicit KumagaiFn(const orc_kumagai_params &q) : p(q) {}
   int nel() const { return p.nel; }
+  int npairs() const { return 1; }
+  int pair(int /*i*/, int /*j*/) const { return 0; }
+  bool cdr_guard() const { return true; }
   double r1(int ij) const { return p.r1[ij]; }
   double r2(int ij) const { return p.r2[ij]; }
   void VA(int ij, double dr, double &val, double &dval) const {
@@ -555,7 +574,8 @@ struct KumagaiFn {
       dfbij = 0.0;
     }
   }
-  void h(int ikpot, double dr, double &val, double &dval) const {
+  void h(int /*eli*/, int /*elj*/, int /*elk*/, int ikpot, double dr, double &val,
+         double &dval) const {
     double alpha = p.alpha[ikpot];
     if (alpha == 0.0) {
       val = 1.0;
@@ -601,6 +621,9 @@ struct BrennerFn {
     }
   }
   int nel() const { return p.nel; }
+  int npairs() const { return p.nel * (p.nel + 1) / 2; }
+  int pair(int i, int j) const { return pair_index(i, j, p.nel); }
+  bool cdr_guard() const { return true; }
   double r1(int ij) const { return p.r1[ij]; }
   double r2(int ij) const { return p.r2[ij]; }
   void VA(int ij, double dr, double &val, double &dval) const {
@@ -638,7 +661,8 @@ struct BrennerFn {
       dfbij = 0.0;
     }
   }
-  void h(int ikpot, double dr, double &val, double &dval) const {
+  void h(int /*eli*/, int /*elj*/, int /*elk*/, int ikpot, double dr, double &val,
+         double &dval) const {
     const double mu = p.mu[ikpot];
     if (mu == 0.0) {
       val = 1.0;
@@ -660,6 +684,106 @@ struct BrennerFn {
   }
 };
 
+// Juslin functional form, juslin_func.f90:25-313, with the derived constants
+// of BIND_TO_FUNC (juslin_module.f90:322-377).  The caller's set is first
+// completed by the mirror fill of juslin_module.f90:273-300 (an ordered pair
+// with r0 < 0 takes the constants of its mirror).  VA, VR, g and bo are
+// Brenner's; h is omega e^{(alpha dr)^m} of the triplet (i, j, k).
+struct JuslinFn {
+  orc_juslin_params p;
+  double bo_exp[9], bo_fac[9], bo_exp1[9], expR[9], expA[9], c_sq[9], d_sq[9], c_d[9], VR_f[9],
+      VA_f[9];
+  explicit JuslinFn(const orc_juslin_params &q) : p(q) {
+    const int nel = p.nel;
+    for (int i = 0; i < nel; i++)
+      for (int j = 0; j < nel; j++) {
+        const int a = j + i * nel, b = i + j * nel;
+        if (p.r0[a] < 0.0) {
+          p.D0[a] = p.D0[b];
+          p.r0[a] = p.r0[b];
+          p.S[a] = p.S[b];
+          p.beta[a] = p.beta[b];
+          p.gamma[a] = p.gamma[b];
+          p.c[a] = p.c[b];
+          p.d[a] = p.d[b];
+          p.h[a] = p.h[b];
+          p.n[a] = p.n[b];
+          p.r1[a] = p.r1[b];
+          p.r2[a] = p.r2[b];
+        }
+      }
+    for (int i = 0; i < nel * nel; i++) {
+      bo_exp[i] = -0.5 / p.n[i];
+      bo_fac[i] = 0.5 * bo_exp[i] * p.n[i];
+      bo_exp1[i] = bo_exp[i] - 1.0;
+      expR[i] = p.beta[i] * std::sqrt(2 * p.S[i]);
+      expA[i] = p.beta[i] * std::sqrt(2 / p.S[i]);
+      c_sq[i] = p.c[i] * p.c[i];
+      d_sq[i] = p.d[i] * p.d[i];
+      c_d[i] = c_sq[i] / d_sq[i];
+      VR_f[i] = p.D0[i] / (p.S[i] - 1);
+      VA_f[i] = p.S[i] * p.D0[i] / (p.S[i] - 1);
+    }
+  }
+  int nel() const { return p.nel; }
+  int npairs() const { return p.nel * p.nel; }
+  int pair(int i, int j) const { return j + i * p.nel; }
+  bool cdr_guard() const { return false; }
+  double r1(int ij) const { return p.r1[ij]; }
+  double r2(int ij) const { return p.r2[ij]; }
+  void VA(int ij, double dr, double &val, double &dval) const {
+    const double e = std::exp(-expA[ij] * (dr - p.r0[ij]));
+    val = -VA_f[ij] * e;
+    dval = VA_f[ij] * expA[ij] * e;
+  }
+  void VR(int ij, double dr, double &val, double &dval) const {
+    const double e = std::exp(-expR[ij] * (dr - p.r0[ij]));
+    val = VR_f[ij] * e;
+    dval = -VR_f[ij] * expR[ij] * e;
+  }
+  void g(int /*ktypi*/, int ikpot, double costh, double &val, double &dval) const {
+    const double hc = p.h[ikpot] + costh;
+    const double h = d_sq[ikpot] + hc * hc;
+    val = p.gamma[ikpot] * (1 + c_d[ikpot] - c_sq[ikpot] / h);
+    dval = 2.0 * p.gamma[ikpot] * c_sq[ikpot] * hc / (h * h);
+  }
+  void bo(int /*ktypi*/, int ijpot, double zij, double fcij, double faij, double &bij,
+          double &dfbij) const {
+    if (p.n[ijpot] == 1.0) {
+      const double arg = 1.0 + zij;
+      bij = std::pow(arg, bo_exp[ijpot]);
+      dfbij = bo_fac[ijpot] * fcij * faij * std::pow(arg, bo_exp1[ijpot]);
+    } else if (zij > 0.0) {
+      const double arg = 1.0 + std::pow(zij, p.n[ijpot]);
+      bij = std::pow(arg, bo_exp[ijpot]);
+      dfbij = bo_fac[ijpot] * fcij * faij * std::pow(zij, p.n[ijpot] - 1.0) *
+              std::pow(arg, bo_exp1[ijpot]);
+    } else {
+      bij = 1.0;
+      dfbij = 0.0;
+    }
+  }
+  // juslin_func.f90:257-294; TRIPLET_INDEX_NS(ktypi, ktypj, ktypk)
+  void h(int eli, int elj, int elk, int /*ikpot*/, double dr, double &val,
+         double &dval) const {
+    const int t = elk + p.nel * (elj + p.nel * eli);
+    const double alpha = p.alpha[t], omega = p.omega[t];
+    const int m = p.m[t];
+    if (m == 1) {
+      val = omega * std::exp(alpha * dr);
+      dval = alpha * val;
+    } else if (m == 3) {
+      const double arg = alpha * dr;
+      val = omega * std::exp(arg * arg * arg);
+      dval = 3 * alpha * arg * arg * val;
+    } else {
+      const double arg = alpha * dr;
+      val = omega * std::exp(std::pow(arg, m));
+      dval = m * std::pow(arg, m - 1) * alpha * val;
+    }
+  }
+};
+
 struct BopOut {
   double *epot, *f, *wpot, *epot_per_at, *epot_per_bond, *f_per_bond, *wpot_per_at,
       *wpot_per_bond;
@@ -676,7 +800,8 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
   // (bop_kernel.f90:562, 1075 loop i = 1, natloc)
   if (natloc < 0) natloc = nat;
   const int nel = fn.nel();
-  const int npairs = nel * (nel + 1) / 2;
+  (void)nel;
+  const int npairs = fn.npairs();
   std::vector<TrigOff> cut_in(npairs);
   std::vector<double> cut_in_l(npairs), cut_in_h(npairs), cut_in_h2(npairs);
   for (int i = 0; i < npairs; i++) {
@@ -712,7 +837,7 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
       double rlij = rij[0] * rij[0];
       rlij = rlij + rij[1] * rij[1];
       rlij = rlij + rij[2] * rij[2];
-      const int el2ij = pair_index(eli, elj, nel);
+      const int el2ij = fn.pair(eli, elj);
       Bond b;
       b.j = j;
       b.nbb = (int)jn;
@@ -810,7 +935,7 @@ int bop_kernel(const Fn &fn, int nat, const double *r, const Box &box, const int
           double rik[3] = {rlik * rnik[0], rlik * rnik[1], rlik * rnik[2]};
           const double fcik = K.fc, dfcikr = K.dfc;
           double h_Dr, dh_dDr;
-          fn.h(ikpot, rlij - rlik, h_Dr, dh_dDr);
+          fn.h(eli, el[j], el[K.j], ikpot, rlij - rlik, h_Dr, dh_dDr);
           double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
           double g_costh, dg_dcosth;
           fn.g(eli, ikpot, costh, g_costh, dg_dcosth);
@@ -933,7 +1058,8 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
                    const BopOut &o, int nthreads, int natloc = -1) {
   if (natloc < 0) natloc = nat;
   const int nel = fn.nel();
-  const int npairs = nel * (nel + 1) / 2;
+  (void)nel;
+  const int npairs = fn.npairs();
   std::vector<ExpCutoff> cut_in(npairs), cut_out(npairs), cut_bo(npairs);
   std::vector<double> cut_in_l(npairs), cut_in_h(npairs), cut_in_h2(npairs), cut_out_l(npairs),
       cut_out_h(npairs), cut_bo_h(npairs), max_cut_sq(npairs), Cmin(npairs), Cmax(npairs),
@@ -953,7 +1079,10 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
     Cmin[q] = sp.Cmin[q];
     Cmax[q] = sp.Cmax[q];
     dC[q] = Cmax[q] - Cmin[q];
-    C_dr_cut[q] = Cmax[q] > 2.0 ? Cmax[q] * Cmax[q] / (4 * (Cmax[q] - 1)) : 1.0;
+    // default_bind_to_func.f90:62-68; Juslin without the guard
+    // (juslin_module.f90:305-307)
+    C_dr_cut[q] =
+        (Cmax[q] > 2.0 || !fn.cdr_guard()) ? Cmax[q] * Cmax[q] / (4 * (Cmax[q] - 1)) : 1.0;
   }
   const double screening_threshold = std::log(1e-6);
   const double dot_threshold = (double)1e-10f;  // a default-real literal in tersoff_type.f90:86
@@ -997,7 +1126,7 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
       double rlij = rij[0] * rij[0];
       rlij = rlij + rij[1] * rij[1];
       rlij = rlij + rij[2] * rij[2];
-      const int el2ij = pair_index(eli, elj, nel);
+      const int el2ij = fn.pair(eli, elj);
       Bond b;
       b.j = j;
       b.nbb = (int)jn;
@@ -1211,7 +1340,7 @@ int bop_kernel_scr(const Fn &fn, const orc_scr_params &sp, int nat, const double
           const double rik[3] = {rlik * rnik[0], rlik * rnik[1], rlik * rnik[2]};
           const double fcik = K.fcbo, dfcikr = K.dfcbo;
           double h_Dr, dh_dDr;
-          fn.h(ikpot, rlij - rlik, h_Dr, dh_dDr);
+          fn.h(eli, el[j], el[K.j], ikpot, rlij - rlik, h_Dr, dh_dDr);
           const double costh = rnik[0] * rnij[0] + rnik[1] * rnij[1] + rnik[2] * rnij[2];
           double g_costh, dg_dcosth;
           fn.g(eli, ikpot, costh, g_costh, dg_dcosth);
@@ -2216,9 +2345,139 @@ int orc_brenner_scr_compute(const orc_brenner_params *p, const orc_scr_params *s
   return brenner_run(p, sp, nat, r, cell, pbc, Z, nullptr, nullptr, nullptr, mask, o, nthreads);
 }
 
+// Juslin entry points.  The screening parameters take the mirror fill of
+// juslin_module.f90:273-300 as well; the screened range is sqrt(C_dr_cut) of
+// the pair times the largest max(r2, or2, bor2) of all pairs
+// (juslin_module.f90:381-404), C_dr_cut without the Cmax > 2 guard.
+static orc_scr_params juslin_fill_scr(const orc_juslin_params &p, const orc_scr_params &sp) {
+  orc_scr_params q = sp;
+  const int nel = p.nel;
+  for (int i = 0; i < nel; i++)
+    for (int j = 0; j < nel; j++) {
+      const int a = j + i * nel, b = i + j * nel;
+      if (p.r0[a] < 0.0) {
+        q.or1[a] = q.or1[b];
+        q.or2[a] = q.or2[b];
+        q.bor1[a] = q.bor1[b];
+        q.bor2[a] = q.bor2[b];
+        q.Cmin[a] = q.Cmin[b];
+        q.Cmax[a] = q.Cmax[b];
+      }
+    }
+  return q;
+}
+
+static double juslin_range(int nat, const std::vector<int> &el, const JuslinFn &fn,
+                           const orc_scr_params *sp) {
+  const int nel = fn.nel();
+  (void)nel;
+  std::vector<int> present(nel, 0);
+  for (int i = 0; i < nat; i++)
+    if (el[i] >= 0) present[el[i]] = 1;
+  double mx = 0.0;
+  if (sp)
+    for (int q = 0; q < nel * nel; q++) {
+      const double m = std::max(std::max(fn.p.r2[q], sp->or2[q]), sp->bor2[q]);
+      mx = std::max(mx, m * m);
+    }
+  double range = 0.0;
+  for (int a = 0; a < nel; a++)
+    for (int b = 0; b < nel; b++)
+      if (present[a] && present[b]) {
+        const int q = fn.pair(a, b);
+        if (!sp) {
+          range = std::max(range, fn.p.r2[q]);
+        } else {
+          const double cdr = sp->Cmax[q] * sp->Cmax[q] / (4 * (sp->Cmax[q] - 1));
+          range = std::max(range, std::sqrt(cdr) * std::sqrt(mx));
+        }
+      }
+  return range;
+}
+
+static double juslin_cutoff(const orc_juslin_params *p, const orc_scr_params *sp, int nat,
+                            const int *Z) {
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  const JuslinFn fn(*p);
+  if (!sp) return juslin_range(nat, el, fn, nullptr);
+  const orc_scr_params q = juslin_fill_scr(*p, *sp);
+  return juslin_range(nat, el, fn, &q);
+}
+
+// sp == NULL: Juslin; else JuslinScr.  seed == NULL: the list is built here.
+static int juslin_run(const orc_juslin_params *p, const orc_scr_params *sp, int nat,
+                      const double *r, const double *cell, const int *pbc, const int *Z,
+                      const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                      const BopOut &o, int nthreads) {
+  Box box;
+  if (make_box(cell, pbc, box) != 0) return -1;
+  std::vector<int> el;
+  map_elements(nat, Z, p->nel, p->Z, el);
+  const JuslinFn fn(*p);
+  orc_scr_params q{};
+  if (sp) q = juslin_fill_scr(*p, *sp);
+  NList nl;
+  if (seed) {
+    nl_from_arrays(nat, seed, nbr, dc, nl);
+  } else {
+    const double cutoff = juslin_range(nat, el, fn, sp ? &q : nullptr);
+    if (cutoff > 0) build_neighbors(nat, r, box, cutoff, nl);
+    else nl.seed.assign(nat + 1, 0);
+  }
+  *o.epot = 0.0;
+  const int nt = resolve_threads(nthreads);
+  return sp ? bop_kernel_scr(fn, q, nat, r, box, el.data(), nl, mask, o, nt)
+            : bop_kernel(fn, nat, r, box, el.data(), nl, mask, o, nt);
+}
+
+double orc_juslin_cutoff(const orc_juslin_params *p, int nat, const int *Z) {
+  return juslin_cutoff(p, nullptr, nat, Z);
+}
+
+double orc_juslin_scr_cutoff(const orc_juslin_params *p, const orc_scr_params *sp, int nat,
+                             const int *Z) {
+  return juslin_cutoff(p, sp, nat, Z);
+}
+
+int orc_juslin_kernel(const orc_juslin_params *p, int nat, const double *r, const double *cell,
+                      const int *pbc, const int *Z, const int64_t *seed, const int *nbr,
+                      const int *dc, const int *mask, double *epot, double *f, double *wpot,
+                      double *epot_per_at, double *epot_per_bond, double *f_per_bond,
+                      double *wpot_per_at, double *wpot_per_bond, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return juslin_run(p, nullptr, nat, r, cell, pbc, Z, seed, nbr, dc, mask, o, nthreads);
+}
+
+int orc_juslin_scr_kernel(const orc_juslin_params *p, const orc_scr_params *sp, int nat,
+                          const double *r, const double *cell, const int *pbc, const int *Z,
+                          const int64_t *seed, const int *nbr, const int *dc, const int *mask,
+                          double *epot, double *f, double *wpot, double *epot_per_at,
+                          double *epot_per_bond, double *f_per_bond, double *wpot_per_at,
+                          double *wpot_per_bond, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, epot_per_bond, f_per_bond, wpot_per_at, wpot_per_bond};
+  return juslin_run(p, sp, nat, r, cell, pbc, Z, seed, nbr, dc, mask, o, nthreads);
+}
+
+int orc_juslin_compute(const orc_juslin_params *p, int nat, const double *r, const double *cell,
+                       const int *pbc, const int *Z, const int *mask, double *epot, double *f,
+                       double *wpot, double *epot_per_at, double *wpot_per_at, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return juslin_run(p, nullptr, nat, r, cell, pbc, Z, nullptr, nullptr, nullptr, mask, o,
+                    nthreads);
+}
+
+int orc_juslin_scr_compute(const orc_juslin_params *p, const orc_scr_params *sp, int nat,
+                           const double *r, const double *cell, const int *pbc, const int *Z,
+                           const int *mask, double *epot, double *f, double *wpot,
+                           double *epot_per_at, double *wpot_per_at, int nthreads) {
+  BopOut o{epot, f, wpot, epot_per_at, nullptr, nullptr, wpot_per_at, nullptr};
+  return juslin_run(p, sp, nat, r, cell, pbc, Z, nullptr, nullptr, nullptr, mask, o, nthreads);
+}
+
 // The LAMMPS contract (bop_kernel.f90 under LAMMPS): nat = local + ghost
 // atoms with explicit positions, a shift-free list over all of them, bonds of
-// the first natloc atoms; kind 0 Tersoff, 1 Kumagai, 2 Brenner; sp != NULL:
+// the first natloc atoms; kind 0 Tersoff, 1 Kumagai, 2 Brenner, 3 Juslin; sp != NULL:
 // screened.
 int orc_bop_ghost(int kind, const void *params, const orc_scr_params *sp, int nat, int natloc,
                   const double *r, const int *Z, const int64_t *seed, const int *nbr,
@@ -2242,6 +2501,14 @@ int orc_bop_ghost(int kind, const void *params, const orc_scr_params *sp, int na
     return sp ? bop_kernel_scr(TersoffFn(*p), *sp, nat, r, box, el.data(), nl, mask, o, nt,
                                natloc)
               : bop_kernel(TersoffFn(*p), nat, r, box, el.data(), nl, mask, o, nt, natloc);
+  }
+  if (kind == 3) {
+    const orc_juslin_params *p = static_cast<const orc_juslin_params *>(params);
+    map_elements(nat, Z, p->nel, p->Z, el);
+    const JuslinFn fn(*p);
+    if (!sp) return bop_kernel(fn, nat, r, box, el.data(), nl, mask, o, nt, natloc);
+    const orc_scr_params q = juslin_fill_scr(*p, *sp);
+    return bop_kernel_scr(fn, q, nat, r, box, el.data(), nl, mask, o, nt, natloc);
   }
   if (kind == 2) {
     const orc_brenner_params *p = static_cast<const orc_brenner_params *>(params);

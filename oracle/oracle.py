@@ -56,10 +56,19 @@ class BrennerParams(ctypes.Structure):
         [("m", ctypes.c_int * 6), ("r1", ctypes.c_double * 6), ("r2", ctypes.c_double * 6)]
 
 
+class JuslinParams(ctypes.Structure):
+    _fields_ = [("nel", ctypes.c_int), ("Z", ctypes.c_int * 3)] + \
+        [(k, ctypes.c_double * 9) for k in ("D0", "r0", "S", "beta", "gamma", "c", "d", "h",
+                                            "n")] + \
+        [("alpha", ctypes.c_double * 27), ("omega", ctypes.c_double * 27),
+         ("m", ctypes.c_int * 27), ("r1", ctypes.c_double * 9), ("r2", ctypes.c_double * 9)]
+
+
 class ScrParams(ctypes.Structure):
     """Screened variants: outer / bond-order cutoffs and the screening window
-    (tersoff_params.f90:81-90, kumagai_params.f90 under SCREENING)."""
-    _fields_ = [(k, ctypes.c_double * 6) for k in ("or1", "or2", "bor1", "bor2", "Cmin",
+    (tersoff_params.f90:81-90, kumagai_params.f90 under SCREENING), one entry
+    per element pair (nine for Juslin's ordered pairs)."""
+    _fields_ = [(k, ctypes.c_double * 9) for k in ("or1", "or2", "bor1", "bor2", "Cmin",
                                                    "Cmax")]
 
 
@@ -74,20 +83,20 @@ def scr_params(d):
 
 
 def _kind(kind):
-    """(base kind, screened?) of 'tersoff', 'kumagai', 'brenner' and their
-    '_scr' forms."""
+    """(base kind, screened?) of 'tersoff', 'kumagai', 'brenner', 'juslin'
+    and their '_scr' forms."""
     base = kind[:-4] if kind.endswith("_scr") else kind
-    if base not in ("tersoff", "kumagai", "brenner"):
+    if base not in ("tersoff", "kumagai", "brenner", "juslin"):
         raise ValueError("unknown bond-order potential %r" % kind)
     return base, kind.endswith("_scr")
 
 
-_KIND_ID = {"tersoff": 0, "kumagai": 1, "brenner": 2}
+_KIND_ID = {"tersoff": 0, "kumagai": 1, "brenner": 2, "juslin": 3}
 
 
 def _params(base, d):
     return {"tersoff": tersoff_params, "kumagai": kumagai_params,
-            "brenner": brenner_params}[base](d)
+            "brenner": brenner_params, "juslin": juslin_params}[base](d)
 
 
 def _Z(sym):
@@ -145,6 +154,28 @@ def brenner_params(d):
     return p
 
 
+def juslin_params(d):
+    """Juslin set: pair arrays of nel^2 ordered pairs, alpha / omega / m of
+    nel^3 triplets (m defaults to 1, as the reference's Python sets leave it
+    to the compiled-in table)."""
+    p = JuslinParams()
+    els = d["el"]
+    p.nel = len(els)
+    for q, s in enumerate(els):
+        p.Z[q] = _Z(s)
+    npair = p.nel * p.nel
+    for k in ("D0", "r0", "S", "beta", "gamma", "c", "d", "h", "n", "r1", "r2"):
+        arr = getattr(p, k)
+        for q in range(npair):
+            arr[q] = float(d[k][q])
+    ms = d.get("m", [1] * npair * p.nel)
+    for q in range(npair * p.nel):
+        p.alpha[q] = float(d["alpha"][q])
+        p.omega[q] = float(d["omega"][q])
+        p.m[q] = int(ms[q])
+    return p
+
+
 _P = ctypes.c_void_p
 
 
@@ -160,28 +191,31 @@ def lib():
         L.orc_neighbors_copy.argtypes = [_P, _P, _P, _P]
         L.orc_neighbors_free.argtypes = [_P]
         L.orc_cell_inverse.argtypes = [_P, _P]
-        for name in ("orc_tersoff_cutoff", "orc_kumagai_cutoff", "orc_brenner_cutoff"):
+        for name in ("orc_tersoff_cutoff", "orc_kumagai_cutoff", "orc_brenner_cutoff",
+                     "orc_juslin_cutoff"):
             getattr(L, name).restype = ctypes.c_double
             getattr(L, name).argtypes = [_P, ctypes.c_int, _P]
         kargs = [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                  _P, _P, ctypes.c_int]
-        for name in ("orc_tersoff_kernel", "orc_kumagai_kernel", "orc_brenner_kernel"):
+        for name in ("orc_tersoff_kernel", "orc_kumagai_kernel", "orc_brenner_kernel",
+                     "orc_juslin_kernel"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = kargs
         cargs = [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
-        for name in ("orc_tersoff_compute", "orc_kumagai_compute", "orc_brenner_compute"):
+        for name in ("orc_tersoff_compute", "orc_kumagai_compute", "orc_brenner_compute",
+                     "orc_juslin_compute"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = cargs
         for name in ("orc_tersoff_scr_cutoff", "orc_kumagai_scr_cutoff",
-                     "orc_brenner_scr_cutoff"):
+                     "orc_brenner_scr_cutoff", "orc_juslin_scr_cutoff"):
             getattr(L, name).restype = ctypes.c_double
             getattr(L, name).argtypes = [_P, _P, ctypes.c_int, _P]
         for name in ("orc_tersoff_scr_kernel", "orc_kumagai_scr_kernel",
-                     "orc_brenner_scr_kernel"):
+                     "orc_brenner_scr_kernel", "orc_juslin_scr_kernel"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = [_P] + kargs
         for name in ("orc_tersoff_scr_compute", "orc_kumagai_scr_compute",
-                     "orc_brenner_scr_compute"):
+                     "orc_brenner_scr_compute", "orc_juslin_scr_compute"):
             getattr(L, name).restype = ctypes.c_int
             getattr(L, name).argtypes = [_P] + cargs
         L.orc_bop_ghost.restype = ctypes.c_int

@@ -26,7 +26,8 @@ def gpu_bop(kind, s, precision="fp64", params=None, mask=None, per_at=True, per_
     nl = native.Neighbors(100)
     cls = {"tersoff": native.Tersoff, "kumagai": native.Kumagai,
            "tersoff_scr": native.TersoffScr, "kumagai_scr": native.KumagaiScr,
-           "brenner": native.Brenner, "brenner_scr": native.BrennerScr}[kind]
+           "brenner": native.Brenner, "brenner_scr": native.BrennerScr,
+           "juslin": native.Juslin, "juslin_scr": native.JuslinScr}[kind]
     pot = cls(precision=precision, **(params or {}))
     pot.bind_to(p, nl)
     out = None
@@ -101,6 +102,16 @@ def random_carbon(nat=128, density=3.0, seed=0, dmin=1.2):
     pos = S._random_packing(rng, nat, cell, dmin)
     return S.Structure(pos, cell, np.array([True, True, True]),
                        np.full(nat, 6, dtype=np.int32))
+
+
+def random_wch(nat=96, seed=0, frac=(0.4, 0.35, 0.25), density=3.0, dmin=1.1):
+    """Random W-C-H packing (a carbon-density random packing whose species are
+    drawn W / C / H with the given fractions): every ordered pair and every
+    triplet type of the Juslin sets occurs."""
+    s = random_carbon(nat, density=density, seed=seed, dmin=dmin)
+    rng = np.random.default_rng(seed + 1000)
+    s.numbers = rng.choice([74, 6, 1], size=nat, p=list(frac)).astype(np.int32)
+    return s
 
 
 def triclinic_si(nat=24, seed=0, strain=0.08, dmin=2.0):

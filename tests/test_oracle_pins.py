@@ -33,14 +33,17 @@ from atomistica_gb300 import structures as S
 
 from atomistica_gb300 import parameters as P
 
-from helpers import KUMAGAI, TERSOFF, random_carbon, rattled_diamond
+from helpers import KUMAGAI, TERSOFF, random_carbon, random_wch, rattled_diamond
 
 TERSOFF_SCR = P.Tersoff_PRB_39_5566_Si_C__Scr
 KUMAGAI_SCR = P.Kumagai_CompMaterSci_39_457_Si__Scr
 BRENNER = P.Erhart_PRB_71_035211_SiC
 BRENNER_SCR = P.Erhart_PRB_71_035211_SiC__Scr
+JUSLIN = P.Juslin_JAP_98_123520_WCH
+JUSLIN_SCR = P.Juslin_JAP_98_123520_WCH__Scr
 PARAMS = {"tersoff": TERSOFF, "kumagai": KUMAGAI, "tersoff_scr": TERSOFF_SCR,
-          "kumagai_scr": KUMAGAI_SCR, "brenner": BRENNER, "brenner_scr": BRENNER_SCR}
+          "kumagai_scr": KUMAGAI_SCR, "brenner": BRENNER, "brenner_scr": BRENNER_SCR,
+          "juslin": JUSLIN, "juslin_scr": JUSLIN_SCR}
 
 GPA = 160.21766208  # eV/A^3 -> GPa
 JM2 = 16.02176634  # eV/A^2 -> J/m^2
@@ -202,6 +205,35 @@ def test_bulk_properties_brenner(case):
         assert within(c44r, C44r), (name, c44r)
 
 
+@pytest.mark.parametrize("case", [
+    # tests/test_bulk_properties.py:95-117 (Juslin, Juslin_JAP_98_123520_WCH):
+    # name, builder, Ec, a0, C11, C12, C44 (bcc: no internal relaxation), B.
+    # The reference's sc-W cell is 2x2x2 simple-cubic cells, so its a0 is
+    # twice the lattice constant of the one-atom cell built here.
+    ("bcc-W", lambda a: S.bcc("W", a), 8.89, 3.165, 542, 191, 162, 308),
+    ("fcc-W", lambda a: S.fcc("W", a), 8.89 - 0.346, 4.005, None, None, None, None),
+    ("sc-W", lambda a: S.sc("W", a), 8.89 - 1.614, 2.671, None, None, None, None),
+    ("dia-C", lambda a: S.diamond("C", a), 7.376 - 0.0524, 3.558, 621, 415, None, 484),
+    ("B1-W-C", lambda a: S.b1(("W", "C"), a), (16.68 - 0.98) / 2, 4.380, None, None, None, 433),
+    ("B2-W-C", lambda a: S.b2(("W", "C"), a), (16.68 - 2.32) / 2, 2.704, None, None, None, 411),
+    ("B3-W-C", lambda a: S.b3(("W", "C"), a), (16.68 - 2.12) / 2, 4.679, None, None, None, 511),
+])
+def test_bulk_properties_juslin(case):
+    name, builder, Ec, a0, C11, C12, C44, B = case
+    a_min, e_min = lattice_minimum("juslin", builder, JUSLIN, 0.9 * a0, 1.1 * a0)
+    assert within(-e_min, Ec), (name, e_min)
+    assert within(a_min, a0), (name, a_min)
+    if C11 is None and B is None:
+        return
+    c11, c12, c44 = cubic_elastic_constants("juslin", builder(a_min), JUSLIN)
+    if C11 is not None:
+        assert within(c11, C11), (name, c11)
+        assert within(c12, C12), (name, c12)
+    if C44 is not None:
+        assert within(c44, C44), (name, c44)
+    assert within((c11 + 2 * c12) / 3, B), (name, c11, c12)
+
+
 def test_relaxed_c44_tersoff_si():
     a_min, _ = lattice_minimum("tersoff", lambda a: S.diamond("Si", a), TERSOFF, 5.3, 5.6)
     s = S.diamond("Si", a_min)
@@ -318,6 +350,33 @@ def test_fd_forces_virial_brenner(name, scr):
     assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
 
 
+@pytest.mark.parametrize("params", ["WCH", "FeCH"])
+@pytest.mark.parametrize("scr", [False, True])
+@pytest.mark.parametrize("name", ["bcc-W", "B1-W-C", "W-C-H"])
+def test_fd_forces_virial_juslin(name, scr, params):
+    # Juslin / JuslinScr (W-C-H and Kuopanportti Fe-C-H sets): rattled W and
+    # WC crystals and a random W-C-H packing in which every triplet type of
+    # h = omega exp(alpha dr) occurs, with and without masks
+    rng = np.random.default_rng(91)
+    metal = "W" if params == "WCH" else "Fe"
+    if name == "bcc-W":
+        s = S.bcc(metal, 3.165 if metal == "W" else 2.87, (3, 3, 3))
+        s.positions += rng.uniform(-0.15, 0.15, s.positions.shape)
+    elif name == "B1-W-C":
+        s = S.b1((metal, "C"), 4.38, (2, 2, 2))
+        s.positions += rng.uniform(-0.15, 0.15, s.positions.shape)
+    else:
+        s = random_wch(64, seed=92)
+        s.numbers[s.numbers == 74] = 74 if metal == "W" else 26
+    base = {"WCH": (JUSLIN, JUSLIN_SCR),
+            "FeCH": (P.Kuopanportti_CMS_111_525_FeCH,
+                     P.Kuopanportti_CMS_111_525_FeCH__Scr)}[params]
+    kind = "juslin_scr" if scr else "juslin"
+    mask = rng.integers(0, 2, len(s)).astype(bool) if name == "W-C-H" else None
+    ferr, werr = fd_check(kind, s, base[1] if scr else base[0], natoms=10, mask=mask)
+    assert ferr < 1e-5 and werr < 1e-4, (ferr, werr)
+
+
 @pytest.mark.parametrize("name", ["dia-C", "a-C", "bcc-Fe", "fcc-Fe", "sc-Fe", "B1-Fe-C"])
 def test_fd_forces_virial_brenner_fec_masked(name):
     # tests/test_forces_and_virial.py:103-114 (Henriksson_PRB_79_114107_FeC,
@@ -378,10 +437,12 @@ def test_eam_special_cases(reference_tests_dir):
         assert err < 1e-6, (fac, err)
 
 
-@pytest.mark.parametrize("kind", ["tersoff", "tersoff_scr", "brenner", "brenner_scr"])
+@pytest.mark.parametrize("kind", ["tersoff", "tersoff_scr", "brenner", "brenner_scr", "juslin",
+                                  "juslin_scr"])
 def test_mask_additivity(kind):
-    # tests/test_mask.py:68 (Tersoff, TersoffScr; Brenner, BrennerScr)
-    s = random_carbon(96, seed=8)
+    # tests/test_mask.py:68 (Tersoff, TersoffScr; Brenner, BrennerScr; the
+    # same property for Juslin, JuslinScr on a W-C-H packing)
+    s = random_wch(96, seed=8) if kind.startswith("juslin") else random_carbon(96, seed=8)
     mask = np.random.default_rng(9).integers(0, 2, len(s)).astype(bool)
     o = energy(kind, s, PARAMS[kind])
     o1 = energy(kind, s, PARAMS[kind], mask=mask)
