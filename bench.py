@@ -79,6 +79,78 @@ def dist_info():
     return _di()
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event reasons sampled through NVML (read-only
+    queries, libnvidia-ml via ctypes) about every millisecond by a thread, so
+    that even a timed region of a few tens of milliseconds gets many samples.
+    The device is matched to the CUDA device by UUID."""
+
+    # nvmlClocksEventReasons bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, cuda_index):
+        import ctypes
+        import torch
+        self.ct = ctypes
+        self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        uuid = str(getattr(torch.cuda.get_device_properties(cuda_index), "uuid", ""))
+        ok = False
+        if uuid:
+            u = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+            ok = self.nv.nvmlDeviceGetHandleByUUID(u.encode(), ctypes.byref(self.h)) == 0
+        if not ok:
+            idx = os.environ.get("CUDA_VISIBLE_DEVICES", str(cuda_index)).split(",")[cuda_index]
+            if self.nv.nvmlDeviceGetHandleByIndex_v2(int(idx), ctypes.byref(self.h)) != 0:
+                raise RuntimeError("no NVML handle for the CUDA device")
+        fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn or self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        self.sm_max = float(mx.value) if self.nv.nvmlDeviceGetMaxClockInfo(
+            self.h, 1, ctypes.byref(mx)) == 0 else None
+        self.samples, self.reason_bits = [], 0
+        self.thread, self.running = None, False
+
+    def _loop(self):
+        ct = self.ct
+        clk, rs = ct.c_uint(), ct.c_ulonglong()
+        while self.running:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0:  # NVML_CLOCK_SM
+                self.samples.append(float(clk.value))
+            if self.reasons_fn(self.h, ct.byref(rs)) == 0:
+                self.reason_bits |= rs.value
+            time.sleep(0.001)
+
+    def start(self):
+        import threading
+        self._swi = sys.getswitchinterval()
+        sys.setswitchinterval(0.0005)
+        self.running = True
+        self.thread = threading.Thread(target=self._loop, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        self.running = False
+        self.thread.join()
+        sys.setswitchinterval(self._swi)
+        reasons = sorted(n for b, n in self.REASONS.items() if self.reason_bits & b)
+        sm = self.samples
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.sm_max,
+                "sm_mhz_min": min(sm) if sm else None, "reasons": reasons, "samples": len(sm),
+                "source": "NVML, ~1 ms sampling thread during the timed region"}
+
+
+def clock_sampler(cuda_index):
+    """NVML sampler, else the nvidia-smi one."""
+    try:
+        return NvmlClockSampler(cuda_index)
+    except Exception:
+        return ClockSampler(cuda_index)
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle-reason sampling during the timed region."""
 
@@ -557,7 +629,7 @@ def run_ours(args):
     torch.cuda.synchronize()
 
     ms64, parts64, _, _ = timed(pots["fp64"], args.steps)
-    sampler = ClockSampler(torch.cuda.current_device())
+    sampler = clock_sampler(torch.cuda.current_device())
     msmx, partsmx, launches, clocks = timed(pots["mixed"], args.steps, sampler)
 
     from atomistica_gb300.distributed import max_over_ranks as tmax
