@@ -165,6 +165,33 @@ __global__ void scan_add(int *__restrict__ out, int n, const int *__restrict__ t
   }
 }
 
+// Second pass of the two-pass scan (tiles <= kScanFlatTiles): the block
+// adds the sum of the tile sums before it (integer sums: exact in any order)
+// and the last block writes the total out[n].
+constexpr int kScanFlatTiles = 2048;
+__global__ void scan_add_prefix(int *__restrict__ out, int n, const int *__restrict__ tile_sums,
+                                int tiles) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  int s = 0;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += kScanThreads) s += tile_sums[t];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) warp_tot[wid] = s;
+  __syncthreads();
+  int add = 0;
+#pragma unroll
+  for (int w = 0; w < kScanThreads / 32; w++) add += warp_tot[w];
+  if (add != 0) {
+    const int idx = blockIdx.x * kScanTile + threadIdx.x;
+    for (int q = 0; q < kScanPerThread; q++) {
+      const int k = idx + q * kScanThreads;
+      if (k < n) out[k] += add;
+    }
+  }
+  if (blockIdx.x == tiles - 1 && threadIdx.x == 0) out[n] = add + tile_sums[tiles - 1];
+}
+
 __global__ void scan_total(const int *__restrict__ in, int *__restrict__ out, int n) {
   // out[n] = out[n-1] + in[n-1]
   if (n == 0)
@@ -203,9 +230,18 @@ size_t scan_tmp_ints(int n) {
 
 int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t stream) {
   GB_CHECK(tmp.ensure(scan_tmp_ints(n) * sizeof(int)));
-  scan_rec(in, out, n, tmp.as<int>(), stream);
-  scan_total<<<1, 1, 0, stream>>>(in, out, n);
-  note_launch();
+  const int tiles = (n + kScanTile - 1) / kScanTile;
+  if (n > 0 && tiles <= kScanFlatTiles) {
+    // two launches: tile scans, then the tile offsets and the total
+    scan_tiles<<<tiles, kScanThreads, 0, stream>>>(in, out, n, tmp.as<int>());
+    note_launch();
+    scan_add_prefix<<<tiles, kScanThreads, 0, stream>>>(out, n, tmp.as<int>(), tiles);
+    note_launch();
+  } else {
+    scan_rec(in, out, n, tmp.as<int>(), stream);
+    scan_total<<<1, 1, 0, stream>>>(in, out, n);
+    note_launch();
+  }
   GB_CUDA(cudaGetLastError());
   return 0;
 }
