@@ -180,6 +180,17 @@ def tersoff_si_amorphous(natoms=1048576, seed=3, sigma=0.25, rho_gcc=2.33):
     return s
 
 
+def random_wch(nat=96, seed=0, frac=(0.4, 0.35, 0.25), density=3.0, dmin=1.1):
+    """Random W-C-H packing: a random packing at the carbon number density of
+    ``density`` g/cm^3 whose species are drawn W / C / H with the given
+    fractions, so that every ordered pair and element triplet of the Juslin
+    sets occurs."""
+    s = amorphous_carbon(nat, density=density, seed=seed, dmin=dmin)
+    rng = np.random.default_rng(seed + 1000)
+    s.numbers = rng.choice([74, 6, 1], size=nat, p=list(frac)).astype(np.int32)
+    return s
+
+
 def _random_packing(rng, nat, cell, dmin, max_tries=50000000):
     """Uniform positions in ``cell`` with every pair (all periodic images)
     separated by at least ``dmin``: random sequential addition in the

@@ -293,6 +293,7 @@ def other_configs(dev, oracle):
     out["tersoff_si_4096"] = entry
     out["tersoff_scr"] = screened_config(dev, oracle, nth, cpu_time)
     out["md_si_4096"] = md_config()
+    out["bop_forms"] = bop_forms_config(dev, oracle, nth, cpu_time)
 
     s = structures.eam_cu_131072(seed=2)
     with tempfile.TemporaryDirectory() as td:
@@ -319,6 +320,77 @@ def other_configs(dev, oracle):
                             "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
                                      "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                                      "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
+    return out
+
+
+def bop_forms_config(dev, oracle, nth, cpu_time):
+    """The other members of the bond-order template and the funcfl EAM, each
+    against the oracle on all host cores (device-resident inputs, public API):
+    Brenner / BrennerScr (Erhart-Albe Si-C) on a rattled B3-SiC crystal of
+    32,768 atoms, Juslin (W-C-H) on a random W-C-H packing of 8,192 atoms,
+    Juslin / JuslinScr on a rattled bcc W crystal of 8,192 sites with C and H
+    substituted, and TabulatedEAM (analytic funcfl Cu) on a 32,000-atom fcc
+    block."""
+    import numpy as np
+    import torch
+    from atomistica_gb300 import io as gio, native, parameters, structures
+
+    def measure(pot, s, ref):
+        p = native.from_atoms(s)
+        nl = native.Neighbors(100)
+        pot.bind_to(p, nl)
+        d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+        d_f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+        ms = _gpu_step_ms(pot, p, nl, d_pos, d_f, steps=10)
+        d_f.zero_()
+        p.set_positions(d_pos)
+        e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
+        f = d_f.cpu().numpy()
+        return {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
+                "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
+                "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}
+
+    out = {}
+    sic = structures.b3(("Si", "C"), 4.3596, (16, 16, 16))
+    sic.positions += np.random.default_rng(11).uniform(-0.1, 0.1, sic.positions.shape)
+    wch = structures.random_wch(8192, seed=12)
+    # bcc W with 10 % C and 5 % H on its sites (screened form: its kernel keeps
+    # at most 32 bonds per atom after screening, which the dense random
+    # packing exceeds under the front-end's weakly screening table)
+    wcl = structures.bcc("W", 3.165, (16, 16, 16))
+    rng = np.random.default_rng(14)
+    u = rng.random(len(wcl))
+    wcl.numbers[u < 0.15] = 6
+    wcl.numbers[u < 0.05] = 1
+    wcl.positions += rng.uniform(-0.1, 0.1, wcl.positions.shape)
+    for name, s, kind, cls, params in (
+            ("brenner_sic_32768", sic, "brenner", native.Brenner,
+             parameters.Erhart_PRB_71_035211_SiC),
+            ("brenner_scr_sic_32768", sic, "brenner_scr", native.BrennerScr,
+             parameters.Erhart_PRB_71_035211_SiC__Scr),
+            ("juslin_wch_8192", wch, "juslin", native.Juslin,
+             parameters.Juslin_JAP_98_123520_WCH),
+            ("juslin_wch_bcc_8192", wcl, "juslin", native.Juslin,
+             parameters.Juslin_JAP_98_123520_WCH),
+            ("juslin_scr_wch_bcc_8192", wcl, "juslin_scr", native.JuslinScr,
+             parameters.Juslin_JAP_98_123520_WCH__Scr)):
+        ref = oracle.bop_compute(kind, params, s, nthreads=nth)
+        t_cpu = cpu_time(lambda: oracle.bop_compute(kind, params, s, nthreads=nth), runs=3)
+        entry = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu,
+                 "cpu_cores": nth}
+        for prec in ("fp64",) if kind.endswith("_scr") else ("fp64", "mixed"):
+            entry[prec] = measure(cls(precision=prec, **params), s, ref)
+        out[name] = entry
+    cu = structures.fcc("Cu", 3.615, (20, 20, 20))
+    cu.positions += np.random.default_rng(13).normal(0.0, 0.05, cu.positions.shape)
+    with tempfile.TemporaryDirectory() as td:
+        fn = gio.cu_analytic_funcfl(os.path.join(td, "cu.eam"))
+        fo = oracle.FuncflEAM(fn)
+        ref = fo.compute(cu, nthreads=nth)
+        t_cpu = cpu_time(lambda: fo.compute(cu, nthreads=nth), runs=3)
+        out["funcfl_cu_32000"] = {"natoms": len(cu), "unit": UNIT, "cpu_oracle": len(cu) / t_cpu,
+                                  "cpu_cores": nth,
+                                  "fp64": measure(native.TabulatedEAM(fn), cu, ref)}
     return out
 
 

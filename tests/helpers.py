@@ -105,13 +105,7 @@ def random_carbon(nat=128, density=3.0, seed=0, dmin=1.2):
 
 
 def random_wch(nat=96, seed=0, frac=(0.4, 0.35, 0.25), density=3.0, dmin=1.1):
-    """Random W-C-H packing (a carbon-density random packing whose species are
-    drawn W / C / H with the given fractions): every ordered pair and every
-    triplet type of the Juslin sets occurs."""
-    s = random_carbon(nat, density=density, seed=seed, dmin=dmin)
-    rng = np.random.default_rng(seed + 1000)
-    s.numbers = rng.choice([74, 6, 1], size=nat, p=list(frac)).astype(np.int32)
-    return s
+    return S.random_wch(nat, seed=seed, frac=frac, density=density, dmin=dmin)
 
 
 def triclinic_si(nat=24, seed=0, strain=0.08, dmin=2.0):
