@@ -998,13 +998,15 @@ int bop_batch_apt(int maxz) {
 //
 // Some callers cannot call cudaMalloc: codes embedded in a host framework that
 // has already reserved the device memory for its own pool (so cudaMalloc
-// fails or would fragment that pool), and MD loops that must not allocate —
-// or implicitly synchronise the device — inside a time step.  For them
+// fails or would fragment that pool), and MD loops that must not allocate
+// inside a time step.  For them
 // gb_bop_energy_and_forces_noalloc evaluates Tersoff, Kumagai or Brenner on a
 // neighbour list the caller supplies, using only the file-scope scratch array
 // below for every intermediate buffer.  The array is sized for at most
 // kNoallocMaxAtoms atoms and kNoallocMaxEntries list entries; every GPU that
-// loads this library holds it (about 13 MB) until the process exits.
+// loads this library holds it (kNoallocBytes = 12,976,896 bytes, about 13 MB)
+// until the process exits.  The call waits for its stream to read the list
+// size, the list checks and the tile plan back, so it blocks the host.
 // ===========================================================================
 
 namespace gb {
@@ -1027,6 +1029,7 @@ constexpr size_t kNaE = na_align(kNaG + 24 * (size_t)kNoallocMaxEntries);    // 
 constexpr size_t kNaPart = na_align(kNaE + 8 * (size_t)kNoallocMaxEntries);  // 10 doubles/tile
 constexpr size_t kNaPosff = na_align(kNaPart + 80 * (size_t)kNoallocMaxAtoms);  // 2 float4/atom
 constexpr size_t kNoallocBytes = na_align(kNaPosff + 32 * (size_t)kNoallocMaxAtoms);
+static_assert(kNoallocBytes == 12976896, "scratch size quoted in the header");
 
 }  // namespace
 }  // namespace gb
@@ -1061,21 +1064,27 @@ int noalloc_scratch(unsigned char **out) {
 }
 
 // Per atom: padded position, element index (Z -> parameter-set index), int32
-// offsets, max neighbour count.  status[0] = max z, status[1] = flags.
-__global__ void noalloc_prepare(int nat, const double *__restrict__ r, const int *__restrict__ Z,
-                                int nel, int z0, int z1, int z2, const int64_t *__restrict__ seed,
-                                Pos4 *__restrict__ pos, int *__restrict__ el,
-                                int *__restrict__ seed32, int *__restrict__ status) {
+// offsets, max neighbour count.  status[0] = max z, status[1] = flags.  The
+// offsets are validated here, before any kernel walks the list: seed[0] = 0,
+// non-decreasing, every offset within [0, n] (n = seed[nat], already checked
+// against the scratch capacity on the host).
+__global__ void noalloc_prepare(int nat, int64_t n, const double *__restrict__ r,
+                                const int *__restrict__ Z, int nel, int z0, int z1, int z2,
+                                const int64_t *__restrict__ seed, Pos4 *__restrict__ pos,
+                                int *__restrict__ el, int *__restrict__ seed32,
+                                int *__restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i > nat) return;
-  seed32[i] = (int)seed[i];
+  const int64_t si = seed[i];
+  if (si < 0 || si > n || (i == 0 && si != 0)) atomicOr(&status[1], 16);
+  seed32[i] = (int)(si < 0 ? 0 : si > n ? n : si);
   if (i == nat) return;
   pos[i] = Pos4{r[3 * i], r[3 * i + 1], r[3 * i + 2], 0.0};
   const int z = Z[i];
   el[i] = (nel > 0 && z == z0) ? 0 : (nel > 1 && z == z1) ? 1 : (nel > 2 && z == z2) ? 2 : -1;
-  const int64_t cnt = seed[i + 1] - seed[i];
+  const int64_t cnt = seed[i + 1] - si;
   if (cnt < 0) atomicOr(&status[1], 1);
-  atomicMax(&status[0], (int)(cnt > 0 ? cnt : 0));
+  atomicMax(&status[0], (int)(cnt < 0 ? 0 : cnt > n ? n : cnt));
 }
 
 // Per entry: packed image shift; neighbour index range check.
@@ -1189,27 +1198,34 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   const int nel = pot_nel(pot);
   const int z0 = pot_Z(pot, 0), z1 = nel > 1 ? pot_Z(pot, 1) : -1,
             z2 = nel > 2 ? pot_Z(pot, 2) : -1;
-  noalloc_prepare<<<(nat + 1 + 127) / 128, 128, 0, s>>>(nat, r, Z, nel, z0, z1, z2, seed, pos, el,
-                                                       seed32, status);
+  // Status words: [0] max z, [1] list flags, [4..5] tile plan, [8..15] the
+  // tile kernel's own status (separate slots: the mixed kernel counts its
+  // hot bonds in its status[2]).
+  int *plan = status + 4;
+  int *kstatus = status + 8;
+  noalloc_prepare<<<(nat + 1 + 127) / 128, 128, 0, s>>>(nat, n64, r, Z, nel, z0, z1, z2, seed,
+                                                       pos, el, seed32, status);
   note_launch();
   if (n > 0) {
     noalloc_pack<<<(n + 255) / 256, 256, 0, s>>>(nat, n, j, dc, shift, status);
     note_launch();
   }
-  noalloc_reverse<<<(nat + 127) / 128, 128, 0, s>>>(nat, seed32, j, shift, rev, status);
-  note_launch();
   GB_CUDA(cudaGetLastError());
+  // The offsets and neighbour indices are checked before any kernel walks
+  // the list (noalloc_reverse and the tile kernel index through both).
   int hs[2] = {0, 0};
   GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(hs), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
-  if (hs[1]) {
+  auto list_error = [](int flags) {
     set_error(std::string("noalloc: invalid neighbour list (") +
-              ((hs[1] & 1) ? "decreasing offsets " : "") +
-              ((hs[1] & 2) ? "image shift beyond +-511 " : "") +
-              ((hs[1] & 4) ? "neighbour index out of range " : "") +
-              ((hs[1] & 8) ? "list not symmetric" : "") + ")");
+              ((flags & 16) ? "offsets not within [0, seed[nat]] or seed[0] != 0 " : "") +
+              ((flags & 1) ? "decreasing offsets " : "") +
+              ((flags & 2) ? "image shift beyond +-511 " : "") +
+              ((flags & 4) ? "neighbour index out of range " : "") +
+              ((flags & 8) ? "list not symmetric" : "") + ")");
     return GB_ERROR_ARGUMENT;
-  }
+  };
+  if (hs[1]) return list_error(hs[1]);
   // Tile size as in bop_compute.
   const int maxz = std::max(hs[0], 1);
   int apt = kMaxApt;
@@ -1224,12 +1240,15 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
     return GB_ERROR_CAPACITY;
   }
   const int ntiles = (nat + apt - 1) / apt;
-  int *plan = status + 4;
+  noalloc_reverse<<<(nat + 127) / 128, 128, 0, s>>>(nat, seed32, j, shift, rev, status);
+  note_launch();
   bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, nullptr, seed32, plan);
   note_launch();
-  int hp[2] = {0, 0};
-  GB_CUDA(cudaMemcpyAsync(hp, plan, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaGetLastError());
+  int hp[6] = {0, 0, 0, 0, 0, 0};
+  GB_CUDA(cudaMemcpyAsync(hp, status, sizeof(hp), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
+  if (hp[1]) return list_error(hp[1]);
 
   BopArgs args;
   args.nat = nat;
@@ -1256,9 +1275,9 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   int rows = ntiles;
   const int rc = with_bop(pot, [&](const auto &P) {
     using PotT = std::decay_t<decltype(P)>;
-    return mixed ? dispatch_tile<PotT, float>(args, P, posff, ntiles, hp[0], hp[1], status + 2,
+    return mixed ? dispatch_tile<PotT, float>(args, P, posff, ntiles, hp[4], hp[5], kstatus,
                                               false, false, s, &rows)
-                 : dispatch_tile<PotT, double>(args, P, posff, ntiles, hp[0], hp[1], status + 2,
+                 : dispatch_tile<PotT, double>(args, P, posff, ntiles, hp[4], hp[5], kstatus,
                                                false, false, s, &rows);
   });
   GB_CHECK(rc);
@@ -1268,7 +1287,7 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   note_launch();
   GB_CUDA(cudaGetLastError());
   int hst = 0;
-  GB_CUDA(cudaMemcpyAsync(&hst, status + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaMemcpyAsync(&hst, kstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
   if (hst) {
     set_error("noalloc: internal error (tile plan mismatch)");

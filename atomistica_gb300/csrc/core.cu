@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -561,6 +562,9 @@ __global__ void __launch_bounds__(128)
              int *__restrict__ shift, int2 *__restrict__ stage, int cap, int clamp,
              int *__restrict__ status) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // lanes with an atom (blockDim.x is a multiple of 32): they sum their
+  // counts into the 64-bit list total at the end
+  const unsigned active = __ballot_sync(0xffffffffu, t < nat);
   if (t >= nat) return;
   const float4 pi = spos[t];
   const int i = __float_as_int(pi.w);
@@ -674,6 +678,13 @@ __global__ void __launch_bounds__(128)
     // maximum, which the caller compares with cap afterwards.
     counts[i] = clamp ? min(cnt, cap) : cnt;
     atomicMax(&status[0], cnt);
+    // 64-bit total of the entries (status[6..7]): the CSR offsets are int32,
+    // and a total beyond 2^31 - 1 must be refused before the scan's wrapped
+    // result is used.  A count of 2^26 or more per atom is refused outright.
+    if (cnt >= (1 << 26)) atomicOr(&status[1], 8);
+    const unsigned wsum = __reduce_add_sync(active, (unsigned)min(cnt, (1 << 26) - 1));
+    if ((threadIdx.x & 31) == __ffs(active) - 1)
+      atomicAdd(reinterpret_cast<unsigned long long *>(status + 6), (unsigned long long)wsum);
   }
 }
 
@@ -953,10 +964,11 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
                             stream));
     return 0;
   }
-  // Read back: maxz, flags, n_big, total entries.
+  // Read back: maxz, flags, n_big, total entries (int32 scan and 64-bit sum).
   GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
   GB_CUDA(cudaMemcpyAsync(hs + 4, nl.seed.as<int>() + nat, sizeof(int), cudaMemcpyDeviceToHost,
                           stream));
+  GB_CUDA(cudaMemcpyAsync(hs + 6, status + 6, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
   GB_CUDA(cudaStreamSynchronize(stream));
   GB_CUDA(cudaGetLastError());
   if (hs[1] & 1) {
@@ -967,11 +979,14 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
     set_error("Particle or image shift outside the supported range (|shift| <= 511 cells).");
     return GB_ERROR_DOMAIN;
   }
-  const int64_t total = hs[4];
-  if (total < 0) {
-    set_error("Neighbor list overflow (more than 2^31 entries).");
+  unsigned long long total64 = 0;
+  std::memcpy(&total64, hs + 6, sizeof(total64));
+  if ((hs[1] & 8) || total64 > (unsigned long long)INT_MAX) {
+    set_error("Neighbor list overflow (" + std::to_string(total64) +
+              " entries, more than the 2^31 - 1 of the int32 offsets).");
     return GB_ERROR_CAPACITY;
   }
+  const int64_t total = hs[4];
   GB_CHECK(nl.nbr.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
   GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
   const int maxz = hs[0];

@@ -8,8 +8,12 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-# Location of the reference checkout (fixture files read by CPU-only pins).
-REFERENCE = os.environ.get("ATOMISTICA_REFERENCE", "/root/reference")
+# Location of a checkout of the reference (its fixture files are read by a few
+# CPU-only pins): the environment variable ATOMISTICA_REFERENCE, else a
+# directory named "reference" beside this repository; tests that need it are
+# skipped when neither exists.
+REFERENCE = os.environ.get("ATOMISTICA_REFERENCE",
+                           os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def pytest_configure(config):
