@@ -67,7 +67,10 @@ SIGNATURES = [
     ("gb_juslin_bind_to", _I, [_P, _P, _P, _P]),
     ("gb_juslin_energy_and_forces", _I, [_P] * 13 + [_P]),
     ("gb_tabulated_alloy_eam_bind_to", _I, [_P, _P, _P, _P]),
-    ("gb_tabulated_alloy_eam_energy_and_forces", _I, [_P] * 10 + [_P]),
+    ("gb_tabulated_alloy_eam_energy_and_forces", _I, [_P] * 14),
+    ("gb_tabulated_eam_bind_to", _I, [_P, _P, _P, _P]),
+    ("gb_tabulated_eam_energy_and_forces", _I, [_P] * 14),
+    ("gb_potential_set_elements", _I, [_P, ctypes.c_char_p]),
     ("gb_tabulated_alloy_eam_table", _I, [_P, _I, _I, _P, _P]),
     ("gb_batch_new", _I, [_P]),
     ("gb_batch_free", None, [_P]),
@@ -83,6 +86,7 @@ SIGNATURES = [
     ("gb_batch_md_run", _I, [_P, _P, ctypes.c_double, _I, _P, _P]),
     ("gb_batch_md_get_state", _I, [_P, _P, _P, _P]),
     ("gb_batch_tersoff_tangent", _I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+    ("gb_batch_tersoff_adjoint", _I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     ("gb_potential_last_timing", _I, [_P, _P]),
     ("gb_potential_last_stats", _I, [_P, _P]),
     ("gb_potential_set_tile_atoms", _I, [_P, _I]),

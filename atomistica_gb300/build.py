@@ -19,6 +19,7 @@ LIB = os.path.join(HERE, "libatomistica_gb300.so")
 SOURCES = ["core.cu", "bop.cu", "eam.cu", "api.cu", "diag.cu", "batch.cu",
            "autodiff.cu", "workload.cu"]
 HEADERS = ["internal.h", "potential.h", "bop_math.h", "ff.h", "ff_tables.h", "bop_mixed.cuh",
+           "elements.h",
            "bop_scr.cuh",
            "batch.h"]
 

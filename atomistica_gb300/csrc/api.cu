@@ -11,6 +11,7 @@
 #include <string>
 
 #include "bop_math.h"
+#include "elements.h"
 #include "potential.h"
 
 using namespace gb;
@@ -458,10 +459,16 @@ int update_element_map(Potential &pot, const Particles &p) {
   if (pot.el_for == &p && pot.el_zrev == p.z_rev && pot.el.p) return 0;
   const int nel = pot_nel(pot);
   std::vector<int> el(std::max(p.nat, 1), -1);
-  const bool all = pot.kind == kEAM && pot.eam->funcfl;  // elements = "*"
-  for (int i = 0; i < p.nat; i++)
+  const bool all = pot.kind == kEAM && pot.eam->funcfl;  // one table for every element
+  const std::vector<int> &flt = pot.el_filter;
+  for (int i = 0; i < p.nat; i++) {
+    // the element filter (IS_EL2(els, eli), tabulated_alloy_eam.f90:316-335):
+    // atoms of other elements are skipped as i and as j, like atoms of
+    // elements without parameters
+    if (!flt.empty() && std::find(flt.begin(), flt.end(), p.hZ[i]) == flt.end()) continue;
     for (int q = 0; q < nel; q++)
       if (all || p.hZ[i] == pot_Z(pot, q)) el[i] = q;
+  }
   GB_CHECK(pot.el.ensure(sizeof(int) * el.size()));
   GB_CUDA(cudaMemcpyAsync(pot.el.p, el.data(), sizeof(int) * el.size(), cudaMemcpyHostToDevice,
                           pot_stream(pot)));
@@ -525,13 +532,19 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
     set_error("energy_and_forces: epot, f and wpot are required");
     return GB_ERROR_ARGUMENT;
   }
-  if (pot.kind == kEAM && (epb || fpb || wpb)) {
-    set_error("Per-bond properties are not supported by TabulatedAlloyEAM.");
-    return GB_ERROR_ARGUMENT;
-  }
-  if (pot.kind == kEAM && pot.eam->funcfl && mask) {
-    set_error("Masks are not supported by TabulatedEAM.");  // features: per_at
-    return GB_ERROR_ARGUMENT;
+  // Optional arguments outside the class's features are refused as by the
+  // generated shims (gen_factory.py:302-351): TabulatedAlloyEAM has
+  // mask,per_at (tabulated_alloy_eam.f90:24), TabulatedEAM per_at
+  // (tabulated_eam.f90:24).
+  if (pot.kind == kEAM) {
+    const char *cls = pot.eam->funcfl ? "TabulatedEAM" : "TabulatedAlloyEAM";
+    const char *bad = epb ? "epot_per_bond" : fpb ? "f_per_bond" : wpb ? "wpot_per_bond"
+                      : (pot.eam->funcfl && mask) ? "mask" : nullptr;
+    if (bad) {
+      set_error(std::string("*") + bad + "* argument present but not supported by potential " +
+                cls + ".");
+      return GB_ERROR_ARGUMENT;
+    }
   }
   if (pot.kind == kEAM && pot.precision != GB_PRECISION_FP64) {
     set_error("TabulatedAlloyEAM has only the FP64 form.");
@@ -1190,9 +1203,61 @@ int gb_tabulated_alloy_eam_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neig
 int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *h, gb_particles_t *p,
                                              gb_neighbors_t *nl, const double *q, double *epot,
                                              double *f, double *wpot, const int *mask,
-                                             double *epa, double *wpa, int *ierror) {
-  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, nullptr, nullptr,
-                                        wpa, nullptr, ierror);
+                                             double *epa, double *epb, double *fpb,
+                                             double *wpa, double *wpb, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
+                                        ierror);
+}
+int gb_tabulated_eam_bind_to(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                             int *ierror) {
+  return gb_potential_bind_to(h, p, nl, ierror);
+}
+int gb_tabulated_eam_energy_and_forces(gb_potential_t *h, gb_particles_t *p, gb_neighbors_t *nl,
+                                       const double *q, double *epot, double *f, double *wpot,
+                                       const int *mask, double *epa, double *epb, double *fpb,
+                                       double *wpa, double *wpb, int *ierror) {
+  return gb_potential_energy_and_forces(h, p, nl, q, epot, f, wpot, mask, epa, epb, fpb, wpa, wpb,
+                                        ierror);
+}
+
+int gb_potential_set_elements(gb_potential_t *h, const char *elements) {
+  clear_error();
+  if (!h || !elements) {
+    set_error("set_elements: missing argument");
+    return GB_ERROR_ARGUMENT;
+  }
+  Potential &pot = h->pot;
+  if (pot.kind != kEAM) {
+    set_error("set_elements: only the EAM potentials have an element filter");
+    return GB_ERROR_ARGUMENT;
+  }
+  // filter_from_string (src/core/filter.f90:55-120): "*" = all elements,
+  // else comma-separated symbols (or atomic numbers), each read into two
+  // characters; an unknown symbol is an error.
+  std::vector<int> flt;
+  const std::string str(elements);
+  std::string trimmed = str;
+  trimmed.erase(trimmed.find_last_not_of(' ') + 1);
+  if (trimmed != "*") {
+    size_t start = 0;
+    while (true) {
+      const size_t comma = str.find(',', start);
+      const std::string tok = str.substr(start, comma == std::string::npos ? std::string::npos
+                                                                            : comma - start);
+      const std::string sym = tok.substr(0, 2);
+      const int Z = element_Z(sym);
+      if (Z <= 0) {
+        set_error("Unknown element '" + sym + "'.");
+        return GB_ERROR_ARGUMENT;
+      }
+      flt.push_back(Z);
+      if (comma == std::string::npos) break;
+      start = comma + 1;
+    }
+  }
+  pot.el_filter = flt;
+  pot.el_for = nullptr;  // rebuild the element map on the next call
+  return 0;
 }
 
 int gb_tabulated_alloy_eam_table(const gb_potential_t *h, int which, int idx, double *x0dx,

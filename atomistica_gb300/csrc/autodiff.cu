@@ -89,19 +89,35 @@ struct TangentArgs {
 };
 
 __host__ __device__ inline size_t talign(size_t x) { return (x + 15) & ~size_t(15); }
+// Per-bond Dual slots: rn (3), r, 1/r, fc, dfc/dr, P, E, G (3), and for the
+// adjoint dfc/dR, dfc/dS.
+constexpr int kTBondSlots = 14;
 __host__ __device__ inline size_t tangent_smem(int nbt, int ntrip) {
   size_t o = talign(sizeof(int) * (2 * kTMaxApt + 2 + (size_t)nbt));
-  o += talign(sizeof(Dual) * (size_t)nbt * 12);
+  o += talign(sizeof(Dual) * (size_t)nbt * kTBondSlots);
   o += talign(sizeof(Dual) * (size_t)ntrip * 3);
   return o + 64;
 }
 
+// Parameter order of the gradients (and of the parameter vector).
+enum TParam { tA, tB, tLam, tMu, tBeta, tN, tC, tD, tH, tR, tS, tXi, tOm, tMubo, kTParams };
+// Columns of a tile row: E (value, derivative), dE/dtheta (14 values, 14
+// derivatives along the position direction), 2 spare.
+constexpr int kTRow = 32;
+
+// kAdj = false: the tangent evaluation (E, F and their derivatives along a
+// direction in parameters and positions).  kAdj = true: in addition the
+// reverse-mode gradient dE/dtheta of the 14 parameters, written by hand
+// below, with every quantity still a Dual along the position direction v:
+// one pass gives dE/dtheta and D_v(dE/dtheta) = d(v . dE/dr)/dtheta, the
+// parameter gradient of the force-matching term, next to D_v F = -H v.
+template <bool kAdj>
 __global__ void __launch_bounds__(kTThreads)
     tangent_tile(const TangentArgs a, const TersoffTangent p, int max_nbt, int max_ntrip,
                  int *status) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ double sA[9];
-  __shared__ double red[2 * (kTThreads / 32)];
+  __shared__ double red[(kAdj ? kTRow : 2) * (kTThreads / 32)];
   const int tid = threadIdx.x, tile = blockIdx.x;
   const int a0 = a.tile_atom0[tile], a1 = a.tile_atom0[tile + 1];
   if (tid < 9) sA[tid] = a.Acells[9 * a.tile_struct[tile] + tid];
@@ -131,8 +147,9 @@ __global__ void __launch_bounds__(kTThreads)
   size_t o = talign(sizeof(int) * (2 * kTMaxApt + 2 + (size_t)nbt));
   Dual *D = reinterpret_cast<Dual *>(sm + o);
   Dual *rn = D, *rl = D + 3 * nbt, *rinv = D + 4 * nbt, *fc = D + 5 * nbt, *dfc = D + 6 * nbt,
-       *P = D + 7 * nbt, *E = D + 8 * nbt, *Gs = D + 9 * nbt;
-  o += talign(sizeof(Dual) * (size_t)nbt * 12);
+       *P = D + 7 * nbt, *E = D + 8 * nbt, *Gs = D + 9 * nbt, *dfcR = D + 12 * nbt,
+       *dfcS = D + 13 * nbt;
+  o += talign(sizeof(Dual) * (size_t)nbt * kTBondSlots);
   Dual *T = reinterpret_cast<Dual *>(sm + o);
   for (int q = tid; q < na; q += kTThreads)
     for (int lb = aseed[q]; lb < aseed[q + 1]; lb++) meta[lb] = q;
@@ -143,7 +160,7 @@ __global__ void __launch_bounds__(kTThreads)
     const int ai = meta[lb];
     const int i = a0 + ai, b = b0 + lb, j = a.nbr[b];
     int mt = ai;
-    Dual f = mk(0.0), df = mk(0.0), r = mk(1.0), ri = mk(1.0);
+    Dual f = mk(0.0), df = mk(0.0), r = mk(1.0), ri = mk(1.0), fR = mk(0.0), fS = mk(0.0);
     Dual n3[3] = {mk(0.0), mk(0.0), mk(0.0)};
     if (a.el[i] >= 0 && a.el[j] >= 0) {
       const Pos4 pi = a.pos[i], pj = a.pos[j];
@@ -167,9 +184,16 @@ __global__ void __launch_bounds__(kTThreads)
           f = mk(1.0);
         } else {
           Dual sx, cx;
-          dsincos(p.fac * (r - p.r1), sx, cx);
+          const Dual x = p.fac * (r - p.r1);
+          dsincos(x, sx, cx);
           f = 0.5 * (1.0 + cx);
           df = -0.5 * (p.fac * sx);
+          if (kAdj) {
+            // x = pi (r - R) / (S - R): dx/dR = (x - pi) / (S - R), dx/dS = -x / (S - R)
+            const Dual w = p.r2 - p.r1;
+            fR = -0.5 * (sx * ((x - mk(M_PI)) / w));
+            fS = 0.5 * (sx * (x / w));
+          }
         }
         mt |= kTFlagShort | kTFlagK | kTFlagIJ;
       }
@@ -181,10 +205,18 @@ __global__ void __launch_bounds__(kTThreads)
     rinv[lb] = ri;
     fc[lb] = f;
     dfc[lb] = df;
+    if (kAdj) {
+      dfcR[lb] = fR;
+      dfcS[lb] = fS;
+    }
   }
   __syncthreads();
 
-  // Phase 2: per bond ij, zeta and its derivatives, b, P, energy, j-role G.
+  // Phase 2: per bond ij, zeta and its derivatives, b, P, energy, j-role G;
+  // with kAdj also the bond's share of dE/dtheta.
+  Dual gth[kAdj ? kTParams : 1];
+#pragma unroll
+  for (int q = 0; q < (kAdj ? kTParams : 1); q++) gth[q] = mk(0.0);
   for (int lb = tid; lb < nbt; lb += kTThreads) {
     const int mt = meta[lb];
     if (!(mt & kTFlagIJ)) {
@@ -203,6 +235,9 @@ __global__ void __launch_bounds__(kTThreads)
     const Dual VR = p.A * eR, dVR = -(p.A * p.lam * eR);
     const Dual nij[3] = {rn[lb], rn[nbt + lb], rn[2 * nbt + lb]};
     Dual zeta = mk(0.0), dbj[3] = {mk(0.0), mk(0.0), mk(0.0)};
+    // kAdj: d zeta / d (c, d, h, omega, mubo, R, S)
+    Dual zc = mk(0.0), zd = mk(0.0), zh = mk(0.0), zom = mk(0.0), zmu = mk(0.0),
+         zR = mk(0.0), zS = mk(0.0);
     for (int q = 0; q < z; q++) {
       const int lk = s + q;
       if (lk == lb) continue;
@@ -213,13 +248,16 @@ __global__ void __launch_bounds__(kTThreads)
         continue;
       }
       const Dual nik[3] = {rn[lk], rn[nbt + lk], rn[2 * nbt + lk]};
-      Dual hv = mk(1.0), dh = mk(0.0);
+      Dual hv = mk(1.0), dh = mk(0.0), dhmu = mk(0.0);
       if (!p.h_one) {
-        const Dual x = 2.0 * (p.mubo * (r - rl[lk]));
+        const Dual drr = r - rl[lk];
+        const Dual x = 2.0 * (p.mubo * drr);
         Dual pw = mk(1.0);
         for (int k = 1; k < p.m; k++) pw = pw * x;
         hv = dexp(pw * x);
         dh = 2.0 * (p.mubo * ((double)p.m * (pw * hv)));
+        // h = exp((2 mubo dr)^m): dh/dmubo = 2 m dr (2 mubo dr)^(m-1) h
+        if (kAdj) dhmu = 2.0 * (drr * ((double)p.m * (pw * hv)));
       }
       const Dual cs = nik[0] * nij[0] + nik[1] * nij[1] + nik[2] * nij[2];
       // g = omega (1 + c^2 hc^2 / (d^2 (d^2 + hc^2))), hc = h - cos theta
@@ -228,6 +266,20 @@ __global__ void __launch_bounds__(kTThreads)
       const Dual gv = p.om * (1.0 + (p.c2 * hc * hc) / (p.d2 * den));
       const Dual dg = -2.0 * ((p.om * p.c2 * hc) / (den * den));
       const Dual fk = fc[lk];
+      if (kAdj) {
+        // g = omega G0, G0 = 1 + c^2 hc^2 / (d^2 den), den = d^2 + hc^2
+        const Dual fh = fk * hv;
+        const Dual G0 = 1.0 + (p.c2 * hc * hc) / (p.d2 * den);
+        const Dual dd2 = p.d2 * den;
+        zom = zom + fh * G0;
+        zc = zc + fh * (2.0 * (p.om * p.c * hc * hc) / dd2);
+        zd = zd - fh * (2.0 * (p.om * p.c2 * hc * hc * p.d * (2.0 * p.d2 + hc * hc)) /
+                        (dd2 * dd2));
+        zh = zh + fh * (2.0 * (p.om * p.c2 * hc) / (den * den));
+        zmu = zmu + fk * gv * dhmu;
+        zR = zR + dfcR[lk] * gv * hv;
+        zS = zS + dfcS[lk] * gv * hv;
+      }
       zeta = zeta + fk * gv * hv;
       const Dual dzfac = fk * dg * hv;
       const Dual dzdrij = gv * fk * dh;
@@ -242,15 +294,41 @@ __global__ void __launch_bounds__(kTThreads)
     }
     // b = xi (1 + beta^n zeta^n)^e, e = -1/(2n); P = dE/dzeta
     Dual bij = mk(1.0), Pij = mk(0.0);
+    Dual bxi = mk(0.0), bbeta = mk(0.0), bn = mk(0.0);  // d b / d (xi, beta, n)
     if (zeta.v > 0.0) {
-      const Dual x = dexp(p.n * (dlog(p.beta) + dlog(zeta)));
+      const Dual lbz = dlog(p.beta) + dlog(zeta);
+      const Dual x = dexp(p.n * lbz);
       const Dual l1x = dlog(1.0 + x);
       const Dual ae = dexp(p.e * l1x);
       bij = p.xi * ae;
       Pij = -0.25 * (fc[lb] * VA * p.xi * (x / zeta) * (ae / (1.0 + x)));
+      if (kAdj) {
+        // ln b = ln xi - ln(1 + x) / (2 n), x = (beta zeta)^n
+        bxi = ae;
+        bbeta = -0.5 * (bij * x / (p.beta * (1.0 + x)));
+        bn = bij * (l1x / (2.0 * (p.n * p.n)) - (x * lbz) / (2.0 * (p.n * (1.0 + x))));
+      }
     }
     const Dual f = fc[lb], dfv = dfc[lb];
     E[lb] = 0.5 * (f * (VR + bij * VA));
+    if (kAdj) {
+      // e = f (VR + b VA) / 2 with VR = A e^{-lambda r}, VA = -B e^{-mu r}
+      const Dual hf = 0.5 * f, v = VR + bij * VA, hfVA = hf * VA;
+      gth[tA] = gth[tA] + hf * eR;
+      gth[tLam] = gth[tLam] - hf * (r * VR);
+      gth[tB] = gth[tB] - hf * (bij * eA);
+      gth[tMu] = gth[tMu] - hf * (bij * (r * VA));
+      gth[tXi] = gth[tXi] + hfVA * bxi;
+      gth[tBeta] = gth[tBeta] + hfVA * bbeta;
+      gth[tN] = gth[tN] + hfVA * bn;
+      gth[tR] = gth[tR] + 0.5 * (dfcR[lb] * v) + Pij * zR;
+      gth[tS] = gth[tS] + 0.5 * (dfcS[lb] * v) + Pij * zS;
+      gth[tC] = gth[tC] + Pij * zc;
+      gth[tD] = gth[tD] + Pij * zd;
+      gth[tH] = gth[tH] + Pij * zh;
+      gth[tOm] = gth[tOm] + Pij * zom;
+      gth[tMubo] = gth[tMubo] + Pij * zmu;
+    }
     const Dual dff = 0.5 * (dVR * f + bij * dVA * f + VR * dfv + bij * VA * dfv);
     P[lb] = Pij;
 #pragma unroll
@@ -282,23 +360,43 @@ __global__ void __launch_bounds__(kTThreads)
     Go[1] = G[1];
     Go[2] = G[2];
   }
-  // tile energy (fixed tree)
+  // tile sums (fixed trees): energy, and with kAdj dE/dtheta
+  constexpr int kCols = kAdj ? kTRow : 2;
+  double col[kCols];
+  col[0] = ev;
+  col[1] = ed;
+  if (kAdj) {
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    ev += __shfl_down_sync(0xffffffffu, ev, off);
-    ed += __shfl_down_sync(0xffffffffu, ed, off);
+    for (int q = 0; q < kTParams; q++) {
+      col[2 + q] = gth[q].v;
+      col[2 + kTParams + q] = gth[q].d;
+    }
+#pragma unroll
+    for (int q = 2 + 2 * kTParams; q < kCols; q++) col[q] = 0.0;
   }
-  if ((tid & 31) == 0) {
-    red[2 * (tid >> 5)] = ev;
-    red[2 * (tid >> 5) + 1] = ed;
+#pragma unroll
+  for (int q = 0; q < kCols; q++) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) col[q] += __shfl_down_sync(0xffffffffu, col[q], off);
+    if ((tid & 31) == 0) red[kCols * (tid >> 5) + q] = col[q];
   }
   __syncthreads();
-  if (tid < 10) {
+  const int rowlen = kAdj ? kTRow : 10;
+  if (tid < rowlen) {
     double v = 0.0;
-    if (tid < 2)
-      for (int w = 0; w < kTThreads / 32; w++) v += red[2 * w + tid];
-    a.tile_part[10 * (size_t)tile + tid] = v;
+    if (tid < kCols)
+      for (int w = 0; w < kTThreads / 32; w++) v += red[kCols * w + tid];
+    a.tile_part[rowlen * (size_t)tile + tid] = v;
   }
+}
+
+// Per-structure sums of the kTRow-column tile rows, rows in order.
+__global__ void adjoint_segments(const double *__restrict__ part, const int *__restrict__ seg,
+                                 double *__restrict__ out) {
+  const int q = blockIdx.x, c = threadIdx.x;
+  double v = 0.0;
+  for (int t = seg[q]; t < seg[q + 1]; t++) v += part[kTRow * (size_t)t + c];
+  out[kTRow * (size_t)q + c] = v;
 }
 
 // F_a = sum_b (G[rev b] - G[b]) (value and derivative).
@@ -353,11 +451,19 @@ TersoffTangent make_tangent(const double *q, const double *dq, int m) {
 
 }  // namespace
 
-int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const double *dparams,
-                          const double *dr, double *epot, double *depot, double *f, double *df,
-                          cudaStream_t s) {
-  if (!params || !epot || !depot || !f || !df) {
+// One tile pass over the batch.  adj = false: tangent along (dparams, dr);
+// outputs epot/depot (nstruct), f/df (nat,3).  adj = true: dparams must be
+// NULL; additionally dEdp / dvdEdp (nstruct,14): dE_s/dtheta and its
+// derivative along dr.  Output pointers may be host or device memory.
+int batch_tersoff_eval(Batch &b, int Z, int m, const double *params, const double *dparams,
+                       const double *dr, bool adj, double *epot, double *depot, double *f,
+                       double *df, double *dEdp, double *dvdEdp, cudaStream_t s) {
+  if (!params || !epot || !f || (!adj && (!depot || !df))) {
     set_error("tersoff_tangent: params, epot, depot, f and df are required");
+    return GB_ERROR_ARGUMENT;
+  }
+  if (adj && (dparams || !dEdp)) {
+    set_error("tersoff_adjoint: dE/dparams is required; no parameter direction");
     return GB_ERROR_ARGUMENT;
   }
   if (b.nstruct == 0) return 0;
@@ -401,12 +507,13 @@ int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const do
   }
   GB_CHECK(batch_tiles(b, apt, s));
   const int ntiles = b.ntiles;
+  const int rowlen = adj ? kTRow : 10;
   const int64_t nb = std::max<int64_t>(b.nl.nentries, 1);
   DevBuf &G = b.tan_G, &part = b.tan_part, &fo = b.tan_f, &dp = b.tan_dpos, &red = b.tan_red;
   GB_CHECK(G.ensure(sizeof(Dual) * 3 * nb));
-  GB_CHECK(part.ensure(sizeof(double) * 10 * std::max(ntiles, 1) + 64));
+  GB_CHECK(part.ensure(sizeof(double) * rowlen * std::max(ntiles, 1) + 64));
   GB_CHECK(fo.ensure(sizeof(double) * 6 * std::max(b.nat, 1)));
-  GB_CHECK(red.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1) + 64));
+  GB_CHECK(red.ensure(sizeof(double) * rowlen * std::max(b.nstruct, 1) + 64));
   const double *dpos = nullptr;
   if (dr) {
     if (is_device_ptr(dr)) {
@@ -417,7 +524,7 @@ int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const do
       dpos = dp.as<double>();
     }
   }
-  int *status = reinterpret_cast<int *>(part.as<double>() + 10 * (size_t)std::max(ntiles, 1));
+  int *status = reinterpret_cast<int *>(part.as<double>() + rowlen * (size_t)std::max(ntiles, 1));
   GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 4, s));
   TangentArgs a;
   a.nat = b.nat;
@@ -435,12 +542,20 @@ int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const do
   a.tile_part = part.as<double>();
   const int max_nbt = apt * maxz, max_ntrip = apt * maxz * maxz;
   const size_t smem = tangent_smem(max_nbt, max_ntrip);
-  if (smem > 48 * 1024)
-    GB_CUDA(cudaFuncSetAttribute(tangent_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-  const TersoffTangent p = make_tangent(params, dparams, m);
+  TersoffTangent p = make_tangent(params, dparams, m);
+  if (adj) p.h_one = false;  // mubo is differentiated even at 0
   if (ntiles > 0) {
-    tangent_tile<<<ntiles, kTThreads, smem, s>>>(a, p, max_nbt, max_ntrip, status);
+    if (adj) {
+      if (smem > 48 * 1024)
+        GB_CUDA(cudaFuncSetAttribute(tangent_tile<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      tangent_tile<true><<<ntiles, kTThreads, smem, s>>>(a, p, max_nbt, max_ntrip, status);
+    } else {
+      if (smem > 48 * 1024)
+        GB_CUDA(cudaFuncSetAttribute(tangent_tile<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      tangent_tile<false><<<ntiles, kTThreads, smem, s>>>(a, p, max_nbt, max_ntrip, status);
+    }
     note_launch();
   }
   double *fv = fo.as<double>(), *fd = fv + 3 * (size_t)b.nat;
@@ -449,14 +564,21 @@ int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const do
                                                        b.nl.rev.as<int>(), a.G, fv, fd);
     note_launch();
   }
-  GB_CHECK(reduce_segments(part.as<double>(), t + 2 * ntiles + 1, b.nstruct, red.as<double>(), s));
-  std::vector<double> hred(10 * (size_t)b.nstruct);
+  if (adj) {
+    adjoint_segments<<<b.nstruct, kTRow, 0, s>>>(part.as<double>(), t + 2 * ntiles + 1,
+                                                  red.as<double>());
+    note_launch();
+  } else {
+    GB_CHECK(reduce_segments(part.as<double>(), t + 2 * ntiles + 1, b.nstruct, red.as<double>(),
+                             s));
+  }
+  std::vector<double> hred(rowlen * (size_t)b.nstruct);
   int hst[4];
   GB_CUDA(cudaMemcpyAsync(hred.data(), red.p, sizeof(double) * hred.size(),
                           cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaMemcpyAsync(hst, status, sizeof(hst), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaMemcpyAsync(f, fv, sizeof(double) * 3 * b.nat, cudaMemcpyDefault, s));
-  GB_CUDA(cudaMemcpyAsync(df, fd, sizeof(double) * 3 * b.nat, cudaMemcpyDefault, s));
+  if (df) GB_CUDA(cudaMemcpyAsync(df, fd, sizeof(double) * 3 * b.nat, cudaMemcpyDefault, s));
   GB_CUDA(cudaStreamSynchronize(s));
   GB_CUDA(cudaGetLastError());
   if (hst[0] & 2) {
@@ -465,12 +587,30 @@ int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const do
   }
   std::vector<double> e(b.nstruct), de(b.nstruct);
   for (int q = 0; q < b.nstruct; q++) {
-    e[q] = hred[10 * q];
-    de[q] = hred[10 * q + 1];
+    e[q] = hred[rowlen * q];
+    de[q] = hred[rowlen * q + 1];
   }
   GB_CUDA(cudaMemcpy(epot, e.data(), sizeof(double) * e.size(), cudaMemcpyDefault));
-  GB_CUDA(cudaMemcpy(depot, de.data(), sizeof(double) * de.size(), cudaMemcpyDefault));
+  if (depot) GB_CUDA(cudaMemcpy(depot, de.data(), sizeof(double) * de.size(), cudaMemcpyDefault));
+  if (adj) {
+    std::vector<double> gv((size_t)kTParams * b.nstruct), gd((size_t)kTParams * b.nstruct);
+    for (int q = 0; q < b.nstruct; q++)
+      for (int k = 0; k < kTParams; k++) {
+        gv[(size_t)kTParams * q + k] = hred[rowlen * q + 2 + k];
+        gd[(size_t)kTParams * q + k] = hred[rowlen * q + 2 + kTParams + k];
+      }
+    GB_CUDA(cudaMemcpy(dEdp, gv.data(), sizeof(double) * gv.size(), cudaMemcpyDefault));
+    if (dvdEdp)
+      GB_CUDA(cudaMemcpy(dvdEdp, gd.data(), sizeof(double) * gd.size(), cudaMemcpyDefault));
+  }
   return 0;
+}
+
+int batch_tersoff_tangent(Batch &b, int Z, int m, const double *params, const double *dparams,
+                          const double *dr, double *epot, double *depot, double *f, double *df,
+                          cudaStream_t s) {
+  return batch_tersoff_eval(b, Z, m, params, dparams, dr, false, epot, depot, f, df, nullptr,
+                            nullptr, s);
 }
 
 }  // namespace gb
@@ -483,4 +623,13 @@ extern "C" int gb_batch_tersoff_tangent(gb_batch_t *h, int Z, int m, const doubl
   clear_error();
   if (!h) return GB_ERROR_ARGUMENT;
   return batch_tersoff_tangent(h->b, Z, m, params, dparams, dr, epot, depot, f, df, nullptr);
+}
+
+extern "C" int gb_batch_tersoff_adjoint(gb_batch_t *h, int Z, int m, const double *params,
+                                        const double *v, double *epot, double *f, double *hv,
+                                        double *dE_dparams, double *dv_dE_dparams) {
+  clear_error();
+  if (!h) return GB_ERROR_ARGUMENT;
+  return batch_tersoff_eval(h->b, Z, m, params, nullptr, v, true, epot, nullptr, f, hv,
+                            dE_dparams, dv_dE_dparams, nullptr);
 }

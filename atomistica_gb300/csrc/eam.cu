@@ -33,6 +33,7 @@
 #include <string>
 #include <type_traits>
 
+#include "elements.h"
 #include "potential.h"
 
 namespace gb {
@@ -99,10 +100,17 @@ int eam_read_setfl(const char *fn, EamTables &t) {
     return GB_ERROR_IO_EOF;
   }
   {
+    // "nel el_1 ... el_nel" (:196-198); at most MAX_EAM_ELS = 10 (:60)
     std::istringstream ss(line);
     ss >> t.nel;
     if (!ss || t.nel <= 0 || t.nel > 10) {
-      set_error("setfl: bad element count line: " + line);
+      set_error("setfl: bad element count line (1 to 10 elements): " + line);
+      return GB_ERROR_IO;
+    }
+    t.names.assign(t.nel, std::string());
+    for (int e = 0; e < t.nel; e++) ss >> t.names[e];
+    if (!ss) {
+      set_error("setfl: element count line lists fewer names than elements: " + line);
       return GB_ERROR_IO;
     }
   }
@@ -142,6 +150,14 @@ int eam_read_setfl(const char *fn, EamTables &t) {
     ss >> t.Z[e];
     if (!ss || t.Z[e] <= 0) {
       set_error("setfl: bad element line: " + line);
+      return GB_ERROR_IO;
+    }
+    // the atomic number must name the element of the header (:206-213)
+    const char *name = element_name(t.Z[e]);
+    if (!name || t.names[e] != name) {
+      set_error("Atomic number " + std::to_string(t.Z[e]) + " is element " +
+                (name ? name : "?") + " and does not match element name " + t.names[e] +
+                " found in data file.");
       return GB_ERROR_IO;
     }
     if (!read_values(nF, v)) {
@@ -292,7 +308,7 @@ int eam_upload(EamTables &t) {
 
 namespace {
 
-constexpr int kMaxEamEl = 4;
+constexpr int kMaxEamEl = 10;  // MAX_EAM_ELS (tabulated_alloy_eam.f90:60)
 
 struct EamArgs {
   int nat;
@@ -638,7 +654,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
     return 0;
   }
   if (t.nel > kMaxEamEl) {
-    set_error("TabulatedAlloyEAM: more than 4 elements in the setfl file are not supported.");
+    set_error("TabulatedAlloyEAM: more than 10 elements in the setfl file.");
     return GB_ERROR_ARGUMENT;
   }
   EamArgs a;

@@ -35,6 +35,7 @@ struct SplineDev {
 struct EamTables {
   int nel = 0;
   std::vector<int> Z;
+  std::vector<std::string> names;  // element names of the setfl header
   double cutoff = 0;
   // Single-element funcfl file (TabulatedEAM, tabulated_eam.f90): phi[0]
   // holds the scaled effective charge Z(r), the pair term is Z^2 / r, the
@@ -79,6 +80,11 @@ struct Potential {
 
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+
+  // Element filter of the EAM potentials (the `elements` property,
+  // tabulated_alloy_eam.f90:72, tabulated_eam.f90): atomic numbers the
+  // potential acts on; empty = "*" (all).
+  std::vector<int> el_filter;
 
   // Element map for the bound particles.
   DevBuf el;

@@ -8,10 +8,14 @@ the 14 continuous single-element Tersoff parameters
 
 (tersoff_params.f90 / tersoff_func.f90 naming: R = r1, S = r2, xi = chi) and
 of the positions.  ``EnergyForces`` is a ``torch.autograd.Function``: its
-forward pass is one batched evaluation, its backward pass contracts the
-incoming gradients with the tangent evaluations of the library
-(gb_batch_tersoff_tangent): one pass per parameter and one Hessian-vector
-product for the positions (dF/dr^T g = -H g).
+forward pass is one batched evaluation, its backward pass one adjoint pass of
+the library (gb_batch_tersoff_adjoint): the hand-written reverse-mode
+gradient dE_s/dtheta evaluated in dual numbers along v = dL/dF, which gives
+in the same pass the parameter gradient of the force term,
+d(v . dE/dr)/dtheta, and the Hessian-vector product -H v for the positions
+(bond-order intermediates recomputed, nothing stored per triplet).  The
+forward-mode tangents (gb_batch_tersoff_tangent, one pass per parameter)
+remain available as ``TersoffBatch.evaluate`` and check the adjoint.
 
 No counterpart in the reference (which has no gradients with respect to
 parameters); ``fitting_loss`` is the loss of the fitting workload:
@@ -86,6 +90,23 @@ class TersoffBatch:
             e.ctypes.data, de.ctypes.data, f.ctypes.data, df.ctypes.data), "tersoff_tangent")
         return e, de, f, df
 
+    def adjoint(self, theta, v=None):
+        """One adjoint pass: (E[nstruct], F (total,3), Hv (total,3),
+        dE/dtheta (nstruct,14), dv_dE/dtheta (nstruct,14)) with Hv the
+        derivative of F along v (= -H v) and dv_dE/dtheta the derivative of
+        dE_s/dtheta along v (= d(v . dE_s/dr)/dtheta); v = 0 if None."""
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        ns, nat = len(self.nat), int(self.offsets[-1])
+        e = np.zeros(ns)
+        f, hv = np.zeros((nat, 3)), np.zeros((nat, 3))
+        g, gd = np.zeros((ns, 14)), np.zeros((ns, 14))
+        check(self._L.gb_batch_tersoff_adjoint(
+            self.batch._h, self.Z, self.m, theta.ctypes.data,
+            None if vv is None else vv.ctypes.data, e.ctypes.data, f.ctypes.data,
+            hv.ctypes.data, g.ctypes.data, gd.ctypes.data), "tersoff_adjoint")
+        return e, f, hv, g, gd
+
 
 if torch is not None:
     class EnergyForces(torch.autograd.Function):
@@ -112,19 +133,18 @@ if torch is not None:
             ge = np.zeros(len(tb.nat)) if gE is None else gE.detach().cpu().numpy()
             gf = np.zeros_like(ctx.f) if gF is None else gF.detach().cpu().numpy()
             g_theta = g_pos = None
-            if ctx.needs_input_grad[0]:
-                g = np.zeros(len(PARAM_NAMES))
-                for k in range(len(PARAM_NAMES)):
-                    u = np.zeros(len(PARAM_NAMES))
-                    u[k] = 1.0
-                    _, de, _, df = tb.evaluate(th, dtheta=u)
-                    g[k] = float(np.dot(ge, de) + np.sum(gf * df))
-                g_theta = torch.as_tensor(g, dtype=theta.dtype, device=theta.device)
-            if ctx.needs_input_grad[1]:
-                # dE_s/dr_i = -F_i (i in s); (dF/dr)^T gF = -H gF = dF along gF
-                _, _, f, hv = tb.evaluate(th, dr=gf)
-                gp = -ge[tb.sid][:, None] * f + hv
-                g_pos = torch.as_tensor(gp, dtype=positions.dtype, device=positions.device)
+            if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
+                # one adjoint pass along v = gF:
+                #   dL/dtheta = sum_s gE_s dE_s/dtheta + sum_i gF_i . dF_i/dtheta
+                #             = sum_s gE_s dE_s/dtheta - D_v (dE/dtheta)   (F = -dE/dr)
+                #   dL/dr_i   = -gE_s(i) F_i + (dF/dr)^T gF,  (dF/dr)^T gF = -H gF = D_v F
+                _, f, hv, dedp, dvdedp = tb.adjoint(th, gf)
+                if ctx.needs_input_grad[0]:
+                    g = ge @ dedp - dvdedp.sum(axis=0)
+                    g_theta = torch.as_tensor(g, dtype=theta.dtype, device=theta.device)
+                if ctx.needs_input_grad[1]:
+                    gp = -ge[tb.sid][:, None] * f + hv
+                    g_pos = torch.as_tensor(gp, dtype=positions.dtype, device=positions.device)
             return g_theta, g_pos, None
 
 

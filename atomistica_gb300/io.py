@@ -123,6 +123,42 @@ def cu_analytic_setfl(fn, nr=10000, cutoff=5.0, nrho=10000, rho_max=40.0):
     return fn
 
 
+def analytic_alloy_setfl(fn, elements, nr=2000, cutoff=5.0, nrho=2000, rho_max=60.0, seed=0):
+    """Analytic alloy EAM tables for any number of elements, with seeded
+    per-element parameters: density f_e(r) = a_e exp(-b_e (r/r_e - 1)),
+    embedding F_e(rho) = -c_e sqrt(rho) + g_e rho, and Morse pair terms
+    phi_ij(r) = D (exp(-2 alpha (r - r0)) - 2 exp(-alpha (r - r0))) with
+    D = sqrt(D_i D_j) and the means of alpha and r0 (stored as r*phi per
+    setfl).  Test tables of a plausible shape, not a fitted alloy."""
+    rng = np.random.default_rng(seed)
+    nel = len(elements)
+    dr = cutoff / (nr - 1)
+    r = np.arange(nr) * dr
+    drho = rho_max / (nrho - 1)
+    rhov = np.arange(nrho) * drho
+    a = rng.uniform(0.7, 1.3, nel)
+    b = rng.uniform(2.5, 3.5, nel)
+    re = rng.uniform(2.45, 2.75, nel)
+    c = rng.uniform(0.9, 1.5, nel)
+    g = rng.uniform(0.0, 0.02, nel)
+    D = rng.uniform(0.25, 0.45, nel)
+    al = rng.uniform(1.2, 1.6, nel)
+    r0 = rng.uniform(2.45, 2.75, nel)
+    F = [-c[e] * np.sqrt(rhov) + g[e] * rhov for e in range(nel)]
+    frho = [a[e] * np.exp(-b[e] * (r / re[e] - 1.0)) for e in range(nel)]
+    rphi = {}
+    for i in range(nel):
+        for j in range(i + 1):
+            Dij, aij, rij = np.sqrt(D[i] * D[j]), 0.5 * (al[i] + al[j]), 0.5 * (r0[i] + r0[j])
+            rphi[(i, j)] = r * Dij * (np.exp(-2 * aij * (r - rij)) - 2 * np.exp(-aij * (r - rij)))
+    write_setfl(fn, list(elements), nrho, drho, nr, dr, cutoff, F, frho, rphi,
+                comments=["Analytic %d-element alloy EAM test tables (seed %d)" % (nel, seed),
+                          "nr=%d cutoff=%g nrho=%d rho_max=%g" % (nr, cutoff, nrho, rho_max),
+                          "generated by atomistica_gb300.io.analytic_alloy_setfl"],
+                Z=[atomic_numbers[x] for x in elements])
+    return fn
+
+
 def write_funcfl(fn, comment, Z, mass, a0, lattice, nrho, drho, nr, dr, cutoff, F, Zr, rho):
     """DYNAMO funcfl file (single element; tabulated_eam.f90:147-200 format):
     comment; Z mass a0 lattice; nrho drho nr dr cutoff; F(rho), Z(r), rho(r)."""

@@ -612,11 +612,16 @@ class TabulatedEAM(_Potential):
 
     def __init__(self, fn, elements="*"):
         super().__init__()
-        if elements not in ("*", None):
-            raise NotImplementedError("element filters other than '*' are not supported")
         check(self._L.gb_tabulated_eam_new(ctypes.byref(self._h), str(fn).encode()),
               "TabulatedEAM")
         self._precision = "fp64"
+        self.set_elements(elements)
+
+    def set_elements(self, elements="*"):
+        """Element filter (filter_from_string): "*" or comma-separated
+        symbols; atoms of other elements are skipped."""
+        check(self._L.gb_potential_set_elements(self._h, str(elements or "*").encode()),
+              "elements")
 
 
 class TabulatedAlloyEAM(_Potential):
@@ -627,11 +632,17 @@ class TabulatedAlloyEAM(_Potential):
 
     def __init__(self, fn, elements="*"):
         super().__init__()
-        if elements not in ("*", None):
-            raise NotImplementedError("element filters other than '*' are not supported")
         check(self._L.gb_tabulated_alloy_eam_new(ctypes.byref(self._h),
                                                  str(fn).encode()), "TabulatedAlloyEAM")
         self._precision = "fp64"
+        self.set_elements(elements)
+
+    def set_elements(self, elements="*"):
+        """Element filter (tabulated_alloy_eam.f90:72, filter_from_string):
+        "*" or comma-separated symbols; atoms of other elements are skipped
+        as centre and as neighbour."""
+        check(self._L.gb_potential_set_elements(self._h, str(elements or "*").encode()),
+              "elements")
 
     def table(self, which, idx):
         """((x0, dx, cut), coefficients (8, n)) of a spline table:

@@ -220,7 +220,8 @@ int gb_juslin_new(gb_potential_t **pot, const gb_juslin_params_t *params);
 int gb_juslin_scr_new(gb_potential_t **pot, const gb_juslin_params_t *params,
                       const gb_screening_params_t *scr);
 /* python_tabulated_alloy_eam_new + init(fn=...) (tabulated_alloy_eam.f90:147-259):
- * reads a DYNAMO setfl file. */
+ * reads a DYNAMO setfl file of 1 to 10 elements (MAX_EAM_ELS, :60); each
+ * element's atomic number must match its name in the header (:206-213). */
 int gb_tabulated_alloy_eam_new(gb_potential_t **pot, const char *fn);
 /* python_tabulated_eam_new + init(fn=...) (tabulated_eam.f90:147-200): a
  * single-element DYNAMO funcfl file; every atom is of its element
@@ -302,13 +303,36 @@ int gb_juslin_energy_and_forces(gb_potential_t *pot, gb_particles_t *p, gb_neigh
                                 const int *mask, double *epot_per_at, double *epot_per_bond,
                                 double *f_per_bond, double *wpot_per_at,
                                 double *wpot_per_bond, int *ierror);
+/* The EAM classes keep the uniform 14-argument shim type of
+ * python_<mod>_energy_and_forces (factory.template.h:48-50), so they fit
+ * the same function table; arguments outside a class's features (per-bond
+ * outputs; for TabulatedEAM also mask) are refused with GB_ERROR_ARGUMENT
+ * and the shim's message (gen_factory.py:302-351). */
 int gb_tabulated_alloy_eam_bind_to(gb_potential_t *pot, gb_particles_t *p,
                                    gb_neighbors_t *nl, int *ierror);
 int gb_tabulated_alloy_eam_energy_and_forces(gb_potential_t *pot, gb_particles_t *p,
                                              gb_neighbors_t *nl, const double *q, double *epot,
                                              double *f, double *wpot, const int *mask,
-                                             double *epot_per_at, double *wpot_per_at,
-                                             int *ierror);
+                                             double *epot_per_at, double *epot_per_bond,
+                                             double *f_per_bond, double *wpot_per_at,
+                                             double *wpot_per_bond, int *ierror);
+int gb_tabulated_eam_bind_to(gb_potential_t *pot, gb_particles_t *p, gb_neighbors_t *nl,
+                             int *ierror);
+int gb_tabulated_eam_energy_and_forces(gb_potential_t *pot, gb_particles_t *p,
+                                       gb_neighbors_t *nl, const double *q, double *epot,
+                                       double *f, double *wpot, const int *mask,
+                                       double *epot_per_at, double *epot_per_bond,
+                                       double *f_per_bond, double *wpot_per_at,
+                                       double *wpot_per_bond, int *ierror);
+
+/* The `elements` property of TabulatedAlloyEAM / TabulatedEAM
+ * (tabulated_alloy_eam.f90:72, filter_from_string in src/core/filter.f90:
+ * 55-120): "*" (default) = every element; otherwise comma-separated element
+ * symbols or atomic numbers, each read into two characters.  Atoms of other
+ * elements are skipped as centre and as neighbour (:316-335).  An unknown
+ * symbol returns GB_ERROR_ARGUMENT ("Unknown element 'X'.").  Takes effect
+ * on the next evaluation. */
+int gb_potential_set_elements(gb_potential_t *pot, const char *elements);
 
 /* Spline table export of an EAM potential (for parity checks of the host
  * setfl reader and spline builder against simple_spline_init,
@@ -323,12 +347,13 @@ int gb_tabulated_alloy_eam_table(const gb_potential_t *pot, int which, int idx, 
  * Allocation-free evaluation.  This entry point has no counterpart in the
  * reference.  It is meant for callers that cannot call cudaMalloc: codes
  * embedded in a host framework that has already reserved the device memory
- * for its own pool, and MD loops that must not allocate (nor implicitly
- * synchronise the device) during a time step.  It evaluates a Tersoff,
- * Kumagai or Brenner potential (FP64 or mixed, as set on `pot`) on a neighbour list the
- * caller supplies and allocates nothing: all intermediate buffers live in one
- * static device array of about 12.5 MB that every GPU loading this library
- * holds until the process exits.
+ * for its own pool (so a cudaMalloc would fail or fragment that pool), and MD
+ * loops that must not allocate during a time step.  It evaluates a Tersoff,
+ * Kumagai or Brenner potential (non-screened; FP64 or mixed, as set on `pot`)
+ * on a neighbour list the caller supplies and allocates nothing: all
+ * intermediate buffers live in one static device array of 12,976,896 bytes
+ * (about 13 MB) that every GPU loading this library holds until the process
+ * exits.
  *
  *   limits: nat <= 16384 atoms and at most 262144 list entries; larger
  *           inputs are rejected with GB_ERROR_CAPACITY and a message.
@@ -338,8 +363,14 @@ int gb_tabulated_alloy_eam_table(const gb_potential_t *pot, int which, int idx, 
  *           Fortran order), both accumulated into, as in
  *           gb_potential_energy_and_forces.
  *   host memory: cell (3x3, rows = lattice vectors).
- *   stream: the CUDA stream all work is issued on (NULL = default stream);
- *           the call returns after that stream has finished its work.
+ *   stream: the CUDA stream all work is issued on (NULL = default stream).
+ *           The call blocks the host: it waits for the stream several times
+ *           (to read the list size, the list checks and the tile plan) and
+ *           returns after the stream has finished its work.
+ *   checks: seed[0] = 0, non-decreasing offsets up to seed[nat], neighbour
+ *           indices in [0, nat), image shifts within +-511 and a symmetric
+ *           list are verified before any kernel walks the list; a violation
+ *           returns GB_ERROR_ARGUMENT with a message.
  *   set-up: the first call on a device looks up the device address of the
  *           static array (cudaGetSymbolAddress); make that first call before
  *           any stream capture.
@@ -412,6 +443,21 @@ int gb_batch_energy_and_forces(gb_batch_t *batch, gb_potential_t *pot, double *e
 int gb_batch_tersoff_tangent(gb_batch_t *batch, int Z, int m, const double *params,
                              const double *dparams, const double *dr, double *epot,
                              double *depot, double *f, double *df);
+/* The reverse-mode (adjoint) counterpart for loss gradients, in one pass: the
+ * hand-written gradient of each structure's energy with respect to the 14
+ * parameters, dE_dparams (nstruct,14), evaluated in dual numbers along a
+ * position direction v (total atoms,3; NULL: 0), which also gives
+ * dv_dE_dparams (nstruct,14) = v . d(dE_s/dparams)/dr = d(v . dE_s/dr)/dparams
+ * (the parameter gradient of a force-matching term with v = dL/dF, up to
+ * sign) and hv (total atoms,3) = derivative of the forces along v = -H v,
+ * recomputed from bond-order intermediates without per-triplet storage.
+ * epot (nstruct) and f (total atoms,3) are the values.  mubo is
+ * differentiated also at 0 (h = exp((2 mubo dr)^m)).  hv and dv_dE_dparams
+ * may be NULL.  Host or device output pointers; all set, not accumulated.
+ * No counterpart in the reference. */
+int gb_batch_tersoff_adjoint(gb_batch_t *batch, int Z, int m, const double *params,
+                             const double *v, double *epot, double *f, double *hv,
+                             double *dE_dparams, double *dv_dE_dparams);
 
 /* ------------------------------------------------------------------------
  * Diagnostics (no counterpart in the reference; used by the benchmark).

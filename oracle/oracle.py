@@ -468,9 +468,15 @@ class EAM:
         L.orc_eam_table(self._h, which, idx, _ptr(x), _ptr(c))
         return x, c
 
-    def compute(self, s, nl=None, mask=None, per_at=True, nthreads=0):
+    def compute(self, s, nl=None, mask=None, per_at=True, nthreads=0, elements=None):
+        """elements: None / "*" or a list of atomic numbers (the element
+        filter, tabulated_alloy_eam.f90:316-335: atoms of other elements are
+        skipped as i and as j, exactly as atoms of elements the file has no
+        parameters for, so they are given Z = 0 here)."""
         L = lib()
         r, cell, pbc, Z = _geom(s)
+        if elements not in (None, "*"):
+            Z = np.ascontiguousarray(np.where(np.isin(Z, list(elements)), Z, 0).astype(np.int32))
         nat = len(r)
         if nl is None:
             nl = neighbors(s, self.cutoff)

@@ -124,3 +124,44 @@ def test_autograd_loss_gradients(gpu):
               loss_of(th.detach(), r.detach() - eps * v)).item() / (2 * eps)
         ana = float(np.sum(g_r * v.numpy()))
         assert abs(ana - fd) <= 1e-6 * max(abs(ana), abs(fd)) + 1e-12
+
+
+def test_adjoint_matches_tangents(gpu):
+    # the reverse-mode pass against the forward-mode tangents (one per
+    # parameter), value part and derivative along v, at 1e-10 relative
+    fitting, structs, tb, theta, m = _setup(5, seed=55)
+    r0 = np.concatenate([s.positions for s in structs])
+    tb.set_positions(r0)
+    v = np.random.default_rng(9).normal(size=r0.shape)
+    e, f, hv, g, gd = tb.adjoint(theta, v)
+    e0, _, f0, hv0 = tb.evaluate(theta, dr=v)
+    assert np.max(np.abs(e - e0)) <= 1e-12 * np.max(np.abs(e0))
+    assert np.max(np.abs(f - f0)) <= 1e-12 * np.max(np.abs(f0))
+    assert np.max(np.abs(hv - hv0)) <= 1e-12 * np.max(np.abs(hv0))
+    for k, name in enumerate(fitting.PARAM_NAMES):
+        u = np.zeros(14)
+        u[k] = 1.0
+        _, de, _, df = tb.evaluate(theta, dtheta=u)
+        # D_v(dE_s/dtheta_k) = -sum_{i in s} v_i . dF_i/dtheta_k
+        dv = np.array([-np.sum(v[tb.offsets[q]:tb.offsets[q + 1]] *
+                               df[tb.offsets[q]:tb.offsets[q + 1]])
+                       for q in range(len(structs))])
+        assert np.max(np.abs(g[:, k] - de)) <= 1e-10 * max(np.max(np.abs(de)), 1e-300), \
+            (name, g[:, k], de)
+        assert np.max(np.abs(gd[:, k] - dv)) <= 1e-10 * max(np.max(np.abs(dv)), 1e-300), \
+            (name, gd[:, k], dv)
+
+
+def test_adjoint_matches_central_differences(gpu):
+    # dE/dtheta of the adjoint against central differences of the energies
+    fitting, structs, tb, theta, m = _setup(4, seed=56)
+    _, _, _, g, _ = tb.adjoint(theta)
+    for k, name in enumerate(fitting.PARAM_NAMES):
+        u = np.zeros(14)
+        u[k] = 1.0
+        h = _step(theta, k)
+        ep, _, _, _ = tb.evaluate(theta + h * u)
+        em, _, _, _ = tb.evaluate(theta - h * u)
+        fd = (ep - em) / (2 * h)
+        assert np.max(np.abs(g[:, k] - fd)) <= 1e-6 * max(np.max(np.abs(g[:, k])), 1e-300), \
+            (name, g[:, k], fd)
