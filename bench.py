@@ -56,8 +56,17 @@ FLOPS_TRIPLET = 165.0
 BYTES_ATOM = 40.0
 BYTES_BOND = 32.0
 # DRAM bytes (read + write) of one launch of the mixed tile kernel at this
-# workload, from ncu (profiles/bop_tile_mx_tersoff_si_1048576.md).
+# workload, from the ncu capture summarised in
+# profiles/bop_tile_mx_tersoff_si_1048576.md (a past capture of the kernel
+# named there, not a measurement of this run).
 TRAFFIC_MX = 75.56e6 + 48.86e6
+# Alloy EAM flop model per list entry, counted from the reference's kernel
+# (tabulated_alloy_eam.f90:423-627): the density pass (displacement 21,
+# dot 5, sqrt, rho spline 11) and the force pass (phi spline f and df 14,
+# 1/r, energy 2, rho' 8, force 10, f adds 6, virial 18), the latter being
+# the algorithmic work of the pair kernel eam_pair.
+EAM_FLOPS_DENSITY = 38.0
+EAM_FLOPS_PAIR = 59.0
 
 
 def parse_args():
@@ -69,6 +78,9 @@ def parse_args():
     ap.add_argument("--natoms", type=int, default=1048576)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-runs", type=int, default=3)
+    ap.add_argument("--config", default=None, choices=["eam_cu_131072"],
+                    help="measure one of the other workloads alone and print its entry "
+                         "(a short command for profiling it)")
     ap.add_argument("--skip-oracle", action="store_true",
                     help="skip the FP64 oracle error check and CPU baseline")
     return ap.parse_args()
@@ -295,6 +307,20 @@ def other_configs(dev, oracle):
     out["md_si_4096"] = md_config()
     out["bop_forms"] = bop_forms_config(dev, oracle, nth, cpu_time)
 
+    out["eam_cu_131072"] = eam_config(dev, oracle, nth, cpu_time)
+    out["si_batch_2048"] = batch_config(dev, oracle, nth)
+    out["si_fit_256"] = fitting_config(oracle, nth)
+    return out
+
+
+def eam_config(dev, oracle, nth, cpu_time):
+    """The 131,072-atom alloy-EAM Cu block (FP64; analytic tables on 10,000
+    points): atom-evals/s per step including the list build, the oracle on
+    all host cores, the deviations, and the pair kernel against the FP64
+    FMA peak."""
+    import numpy as np
+    import torch
+    from atomistica_gb300 import io as gio, native, structures
     s = structures.eam_cu_131072(seed=2)
     with tempfile.TemporaryDirectory() as td:
         fn = os.path.join(td, "cu.setfl")
@@ -313,14 +339,27 @@ def other_configs(dev, oracle):
         p.set_positions(d_pos)
         e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
         f = d_f.cpu().numpy()
-    out["si_batch_2048"] = batch_config(dev, oracle, nth)
-    out["si_fit_256"] = fitting_config(oracle, nth)
-    out["eam_cu_131072"] = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu,
-                            "cpu_cores": nth,
-                            "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
-                                     "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
-                                     "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}}
-    return out
+        # the pair kernel alone (CUDA events on the potential's stream)
+        pair_ms = []
+        for _ in range(10):
+            p.set_positions(d_pos)
+            pot.energy_and_forces(p, nl, forces=d_f)
+            pair_ms.append(pot.last_timing()[3])
+        pair_ms = statistics.median(pair_ms)
+        n_entries = int(nl.get_list(p)[0][-1])
+    from atomistica_gb300 import _lib
+    fp64_peak = _peak(_lib.load(), True)
+    eam_roof = {"bound": "fp64", "kernel": "eam_pair (force pass)", "kernel_ms": pair_ms,
+                "list_entries": n_entries, "flops_per_entry": EAM_FLOPS_PAIR,
+                "achieved": EAM_FLOPS_PAIR * n_entries / (pair_ms * 1e-3) * 1e-12,
+                "peak": fp64_peak, "unit": "TFLOP/s",
+                "peak_source": "FP64 FMA-chain microbenchmark in this run"}
+    eam_roof["frac"] = eam_roof["achieved"] / fp64_peak
+    return {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu, "cpu_cores": nth,
+            "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
+                     "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
+                     "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)},
+            "roofline": eam_roof}
 
 
 def bop_forms_config(dev, oracle, nth, cpu_time):
@@ -761,7 +800,7 @@ def run_ours(args):
                 "achieved": fm["flops"] / t_k / 1e12, "peak": p32, "unit": "TFLOP/s",
                 "frac": max(t_flop, t_byte) / t_k,
                 "traffic": TRAFFIC_MX if nat == 1048576 else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                "traffic_source": "past ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, one launch) "
                                   "(profiles/bop_tile_mx_tersoff_si_1048576.md)",
                 "kernel": "bop_tile_mx<Tersoff> (mixed form)",
                 "kernel_ms": kern_mx,
@@ -851,10 +890,32 @@ def _peak(L, fp64):
     return _peaks[fp64]
 
 
+def run_config(args):
+    """One of the other workloads alone (its JSON entry on one line)."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from atomistica_gb300 import build as gbuild
+    gbuild.build()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker and the CPU baseline
+    nth = oracle.max_threads()
+
+    def cpu_time(fn, runs=1):
+        t0 = time.perf_counter()
+        fn()
+        return time.perf_counter() - t0
+
+    entry = eam_config(dev, oracle, nth, cpu_time)
+    print(json.dumps({"config": args.config, **entry}))
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config:
+        run_config(args)
     else:
         run_ours(args)
 
