@@ -5,6 +5,8 @@ double references (CPU only)."""
 import os
 import subprocess
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -20,3 +22,21 @@ def test_ff_kernel_math(tmp_path):
     assert e_log < 2e-12      # absolute
     assert e_sin < 1e-11 and e_cos < 1e-11
     assert e_sqrt < 1e-13 and e_rsqrt < 1e-13 and e_rcp < 1e-13 and e_mul < 1e-13
+
+
+def test_ff_tables_header_is_generated():
+    # csrc/ff_tables.h is exactly the output of its generator
+    # (csrc/gen_ff_tables.py: 60-digit arithmetic, integer rounding to FP32)
+    import io
+    import sys
+    pytest.importorskip("mpmath")
+    here = os.path.join(ROOT, "atomistica_gb300", "csrc")
+    sys.path.insert(0, here)
+    try:
+        import gen_ff_tables
+    finally:
+        sys.path.remove(here)
+    buf = io.StringIO()
+    gen_ff_tables.main(buf)
+    with open(os.path.join(here, "ff_tables.h")) as fh:
+        assert fh.read() == buf.getvalue()
