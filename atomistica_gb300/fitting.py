@@ -148,6 +148,36 @@ if torch is not None:
             return g_theta, g_pos, None
 
 
+def sharded_loss_and_gradient(theta, shard, nat, e_target, f_target, w_force=0.1):
+    """The fitting loss and its gradients when the structures are sharded
+    over ranks (one process per GPU, each holding a contiguous slice of the
+    structures, distributed.shard_range) — no counterpart in the reference.
+
+    shard: this rank's structures, with ``evaluate(theta)`` -> (E, dE, F, dF)
+    and ``adjoint(theta, v)`` -> (E, F, Hv, dE/dtheta, D_v dE/dtheta) as
+    TersoffBatch; nat, e_target, f_target: this rank's atom counts and
+    targets.  Collectives (distributed.allreduce_sum; none without a process
+    group): one sum over ranks of (sum_s (dE_s/N_s)^2, sum_i |dF_i|^2,
+    structures, atoms), which fixes the global means, and one sum of the 14
+    parameter-gradient partials.  Returns (loss, dL/dtheta — the same on
+    every rank —, dL/dpositions of this rank's atoms)."""
+    from . import distributed as D
+    theta = np.asarray(theta, dtype=np.float64)
+    nat = np.asarray(nat, dtype=np.float64)
+    e, _, f, _ = shard.evaluate(theta)
+    de = (e - np.asarray(e_target)) / nat
+    df = f - np.asarray(f_target)
+    tot = D.allreduce_sum([np.sum(de * de), np.sum(df * df), len(de), df.shape[0]])
+    loss = tot[0] / tot[2] + w_force * tot[1] / tot[3]
+    gE = 2.0 * de / nat / tot[2]          # dL/dE_s
+    gF = 2.0 * w_force * df / tot[3]      # dL/dF_i
+    _, f, hv, dedp, dvdedp = shard.adjoint(theta, gF)
+    g = D.allreduce_sum(gE @ dedp - dvdedp.sum(axis=0))
+    sid = np.repeat(np.arange(len(nat)), nat.astype(np.int64))
+    g_pos = -gE[sid][:, None] * f + hv
+    return float(loss), g, g_pos
+
+
 def fitting_loss(E, F, nat, E_target, F_target, w_force=0.1):
     """mean_s (E_s/N_s - E_t/N_s)^2 + w_force mean_i |F_i - F_t,i|^2 (torch)."""
     n = torch.as_tensor(np.asarray(nat, dtype=np.float64), device=E.device)

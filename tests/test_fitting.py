@@ -165,3 +165,25 @@ def test_adjoint_matches_central_differences(gpu):
         fd = (ep - em) / (2 * h)
         assert np.max(np.abs(g[:, k] - fd)) <= 1e-6 * max(np.max(np.abs(g[:, k])), 1e-300), \
             (name, g[:, k], fd)
+
+
+def test_sharded_path_equals_autograd(gpu):
+    # fitting.sharded_loss_and_gradient (the multi-rank path; world size 1
+    # here) on the GPU batch equals the torch.autograd path
+    torch = pytest.importorskip("torch")
+    fitting, structs, tb, theta, m = _setup(4, seed=57)
+    rng = np.random.default_rng(10)
+    theta_t = theta * (1.0 + rng.uniform(-0.02, 0.02, size=14))
+    r0 = np.concatenate([s.positions for s in structs])
+    tb.set_positions(r0)
+    et, _, ft, _ = tb.evaluate(theta_t)
+    tb.set_positions(r0)
+    loss, g, gp = fitting.sharded_loss_and_gradient(theta, tb, tb.nat, et, ft)
+    th = torch.tensor(theta, requires_grad=True)
+    r = torch.tensor(r0, requires_grad=True)
+    E, F = fitting.EnergyForces.apply(th, r, tb)
+    L = fitting.fitting_loss(E, F, tb.nat, torch.tensor(et), torch.tensor(ft))
+    L.backward()
+    assert abs(loss - L.item()) <= 1e-13 * abs(L.item())
+    assert np.max(np.abs(g - th.grad.numpy())) <= 1e-12 * np.max(np.abs(g))
+    assert np.max(np.abs(gp - r.grad.numpy())) <= 1e-12 * np.max(np.abs(gp))
