@@ -102,8 +102,8 @@ int batch_binning(Batch &b, double cutoff, cudaStream_t s) {
 // Tiles of at most apt atoms inside each structure; per-structure tile
 // offsets for the energy/virial sums.
 int batch_tiles(Batch &b, int apt, cudaStream_t s) {
-  if (b.tiles_apt == apt && b.tiles_nentries == b.nl.nentries && b.ntiles > 0 &&
-      b.built_geom == b.geom_rev)
+  if (b.tiles_budget == 0 && b.tiles_apt == apt && b.tiles_nentries == b.nl.nentries &&
+      b.ntiles > 0 && b.built_geom == b.geom_rev)
     return 0;
   std::vector<int> atom0, strct, seg(b.nstruct + 1, 0);
   for (int q = 0; q < b.nstruct; q++) {
@@ -128,6 +128,75 @@ int batch_tiles(Batch &b, int apt, cudaStream_t s) {
                           cudaMemcpyHostToDevice, s));
   GB_CUDA(cudaStreamSynchronize(s));
   b.tiles_apt = apt;
+  b.tiles_budget = 0;
+  b.graph_geom = ~0ull;  // a captured graph holds the previous tiles: capture again
+  b.tile_max_atoms = apt;
+  b.ntiles = nt;
+  b.tiles_nentries = b.nl.nentries;
+  return 0;
+}
+
+// Tiles of the bond-order kernels, balanced by work: inside each structure,
+// consecutive atoms join a tile while it keeps at most kMaxTileAtoms atoms,
+// `budget` bonds and 6 budget (ij, ik) slots (a first atom always joins), so
+// a tile's work matches the CTA's threads whatever the coordination (tiles
+// of a fixed atom count leave threads idle where it is low and overflow
+// shared memory where it is high).  The counts come from the list built
+// last; the tiles are kept while the geometry is unchanged: any tiling is
+// correct (every evaluation plans its exact per-tile maxima), only the
+// balance depends on the counts.
+int batch_tiles_work(Batch &b, int budget, cudaStream_t s, bool recut) {
+  constexpr int kMaxTileAtoms = 64;
+  if (!recut && b.tiles_budget == budget && b.tiles_geom == b.geom_rev && b.ntiles > 0) return 0;
+  std::vector<int> seed(b.nat + 1, 0);
+  if (b.nat > 0)
+    GB_CUDA(cudaMemcpyAsync(seed.data(), b.nl.seed.p, sizeof(int) * (b.nat + 1),
+                            cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  const int64_t tmax = 6 * (int64_t)budget;
+  std::vector<int> atom0, strct, seg(b.nstruct + 1, 0);
+  int most = 1;
+  for (int q = 0; q < b.nstruct; q++) {
+    seg[q] = (int)strct.size();
+    int na = 0;
+    int64_t nb = 0, nt = 0;
+    for (int a = b.atom_off[q]; a < b.atom_off[q + 1]; a++) {
+      const int64_t z = seed[a + 1] - seed[a];
+      if (na > 0 && (na == kMaxTileAtoms || nb + z > budget || nt + z * z > tmax)) {
+        most = std::max(most, na);
+        na = 0;
+      }
+      if (na == 0) {
+        atom0.push_back(a);
+        strct.push_back(q);
+        nb = nt = 0;
+      }
+      na++;
+      nb += z;
+      nt += z * z;
+    }
+    if (na > 0) most = std::max(most, na);
+  }
+  seg[b.nstruct] = (int)strct.size();
+  const int nt = (int)strct.size();
+  atom0.push_back(b.nat);
+  // layout: tile_atom0 [nt + 1] | tile_struct [nt] | seg [nstruct + 1]
+  const size_t n = atom0.size() + strct.size() + seg.size();
+  GB_CHECK(b.tiles.ensure(sizeof(int) * n));
+  int *d = b.tiles.as<int>();
+  GB_CUDA(cudaMemcpyAsync(d, atom0.data(), sizeof(int) * atom0.size(), cudaMemcpyHostToDevice, s));
+  if (nt)
+    GB_CUDA(cudaMemcpyAsync(d + atom0.size(), strct.data(), sizeof(int) * strct.size(),
+                            cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaMemcpyAsync(d + atom0.size() + strct.size(), seg.data(), sizeof(int) * seg.size(),
+                          cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  b.tiles_apt = budget;
+  b.tiles_budget = budget;
+  b.tile_max_atoms = most;
+  b.tiles_geom = b.geom_rev;
+  b.tiles_pos = b.built_pos;
+  b.graph_geom = ~0ull;  // a captured graph holds the previous tiles: capture again
   b.ntiles = nt;
   b.tiles_nentries = b.nl.nentries;
   return 0;
@@ -269,20 +338,21 @@ int batch_finish(Batch &b, Potential &pot, double *epot, double *wpot) {
   return 0;
 }
 
-// Atoms per tile: the autotuned value when current, else the largest that
-// fits.  Tuning times the force part for apt, apt/2, apt/4 (>= 8) on scratch
-// forces and keeps the fastest.
-int batch_choose_apt(Batch &b, Potential &pot, cudaStream_t s) {
-  const int amax = bop_batch_apt(b.nl.maxz);
+// Bond budget per tile: the autotuned value when current, else one bond per
+// thread of the mixed kernel (two per thread of the FP64 one).  Tuning times
+// the force part for budgets 256, 192 and 128 on scratch forces and keeps
+// the fastest.
+int batch_choose_budget(Batch &b, Potential &pot, cudaStream_t s) {
+  constexpr int kBudgets[3] = {256, 192, 128};
   const bool current = b.tuned_apt > 0 && b.tuned_geom == b.geom_rev && b.tuned_pot == &pot &&
-                       b.tuned_prec == pot.precision && b.tuned_apt <= amax;
-  if (!b.autotune) return amax;
+                       b.tuned_prec == pot.precision;
+  if (!b.autotune) return kBudgets[0];
   if (current) return b.tuned_apt;
   GB_CHECK(b.gf.ensure(sizeof(double) * 3 * std::max(b.nat, 1)));
-  int best = amax, ncand = 0;
+  int best = kBudgets[0], ncand = 0;
   float best_ms = 0.0f;
-  for (int apt = amax; apt >= std::min(amax, 8); apt /= 2) {
-    GB_CHECK(batch_tiles(b, apt, s));
+  for (int budget : kBudgets) {
+    GB_CHECK(batch_tiles_work(b, budget, s));
     GB_CUDA(cudaMemsetAsync(b.gf.p, 0, sizeof(double) * 3 * b.nat, s));
     float ms = 0.0f;
     for (int rep = 0; rep < 2; rep++) {  // the first run warms up
@@ -295,9 +365,8 @@ int batch_choose_apt(Batch &b, Potential &pot, cudaStream_t s) {
     ncand++;
     if (ncand == 1 || ms < best_ms) {
       best_ms = ms;
-      best = apt;
+      best = budget;
     }
-    if (apt < 16 || ncand == 3) break;
   }
   b.tuned_apt = best;
   b.tuned_geom = b.geom_rev;
@@ -319,7 +388,7 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, doubl
   // Tile plan with head room for the next configurations (checked per tile
   // by the kernel): as much as fits without fewer resident CTAs per SM than
   // the exact plan of this evaluation, at most +25 % bonds / +50 % slots.
-  const int apt = b.tiles_apt;
+  const int apt = b.tile_max_atoms;  // most atoms in one tile
   const int nbt0 = pot.last_plan[0], ntrip0 = pot.last_plan[1];
   if (nbt0 == 0) return;
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
@@ -419,7 +488,7 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, doubl
   b.graph_geom = b.geom_rev;
   b.graph_pot = &pot;
   b.graph_prec = pot.precision;
-  b.graph_apt = apt;
+  b.graph_apt = b.tiles_apt;
   b.graph_cap = cap;
   b.graph_ncells = b.ncells;
   b.graph_kind = kind;
@@ -511,8 +580,8 @@ int batch_eager(Batch &b, Potential &pot, double *epot, double *f, double *wpot,
     b.built_pos = b.pos_rev;
   }
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
-  const int apt = batch_choose_apt(b, pot, s);
-  GB_CHECK(batch_tiles(b, apt, s));
+  const int budget = batch_choose_budget(b, pot, s);
+  GB_CHECK(batch_tiles_work(b, budget, s));
   const size_t nf = 3 * (size_t)b.nat;
   double *fd = f;
   const bool f_host = b.nat > 0 && !is_device_ptr(f);
@@ -521,7 +590,15 @@ int batch_eager(Batch &b, Potential &pot, double *epot, double *f, double *wpot,
     fd = pot.out_f.as<double>();
     GB_CUDA(cudaMemcpyAsync(fd, f, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
   }
-  GB_CHECK(batch_forces(b, pot, fd, s, batch_system(b)));
+  int rc = batch_forces(b, pot, fd, s, batch_system(b));
+  if (rc == GB_ERROR_CAPACITY && b.tiles_pos != b.built_pos) {
+    // tiles cut for other positions (e.g. before a compression) no longer
+    // fit: cut them again from this list (the failed call changed no output)
+    clear_error();
+    GB_CHECK(batch_tiles_work(b, budget, s, true));
+    rc = batch_forces(b, pot, fd, s, batch_system(b));
+  }
+  GB_CHECK(rc);
   GB_CUDA(cudaEventRecord(pot.ev[2], s));
   if (f_host) GB_CUDA(cudaMemcpyAsync(f, fd, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaEventRecord(pot.ev[3], s));

@@ -26,10 +26,16 @@ struct Batch {
   double built_cutoff = -1.0;
   int ncells = 0, tiles_apt = 0, ntiles = 0;
   int64_t tiles_nentries = -1;
+  // Tiles of the bond-order kernels (batch_tiles_work): cut inside each
+  // structure by a bond budget from the per-atom counts of the list built
+  // when they were cut; kept while the geometry is unchanged.
+  int tiles_budget = 0;      // bonds per tile; 0: the tiles are of fixed atom count
+  int tile_max_atoms = 0;    // most atoms in one tile
+  uint64_t tiles_geom = ~0ull, tiles_pos = ~0ull;  // geometry / positions they were cut for
   Neighbors nl;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  // Tile autotuning: the atoms per tile timed fastest for (geometry,
+  // Tile autotuning: the bond budget per tile timed fastest for (geometry,
   // potential, precision).
   bool autotune = false;
   int tuned_apt = 0;
@@ -56,7 +62,7 @@ struct Batch {
   std::vector<double> md_e, md_w;  // per-structure energies / virials of the last step
   std::vector<const void *> graph_bufs;
   DevBuf gf;  // forces accumulated by the graph
-  int64_t info[4] = {0, 0, 0, 0};  // last call: replayed, atoms/tile, kernels in graph, tuned
+  int64_t info[4] = {0, 0, 0, 0};  // last call: replayed, bonds/tile, kernels in graph, tuned
   ~Batch();
 };
 
@@ -66,6 +72,7 @@ cudaStream_t batch_stream(Batch &b);
 int batch_elements(Batch &b, Potential &pot, cudaStream_t s);
 int batch_binning(Batch &b, double cutoff, cudaStream_t s);
 int batch_tiles(Batch &b, int apt, cudaStream_t s);
+int batch_tiles_work(Batch &b, int budget, cudaStream_t s, bool recut = false);
 double batch_cutoff(const Batch &b, const Potential &pot);
 
 }  // namespace gb

@@ -849,7 +849,8 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
     return worst <= kSmemBudget;
   };
   if (batch) {
-    // tiles were cut by the caller (bop_batch_apt)
+    // tiles were cut by the caller (at most kMaxApt atoms each); their exact
+    // plan is checked against shared memory below
   } else if (pot.tile_request > 0) {
     apt = std::min(pot.tile_request, kMaxApt);
     while (apt > 1 && !fits(apt)) apt >>= 1;
@@ -860,7 +861,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
                           2 * kBopThreads)
       apt >>= 1;
   }
-  if (!fits(apt)) {
+  if (!batch && !fits(apt)) {
     set_error("Internal neighbor list exhausted: an atom has " + std::to_string(maxz) +
               " neighbours within the cutoff, more than the bond-order kernel supports.");
     return GB_ERROR_CAPACITY;
@@ -889,6 +890,11 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
     GB_CHECK(neighbors_check_reverse(nl, nullptr));
     max_nbt = hplan[0];
     max_ntrip = hplan[1];
+    if (batch && bop_tile_smem(mixed, max_nbt, max_ntrip) > kSmemBudget) {
+      set_error("Internal neighbor list exhausted: a tile of " + std::to_string(max_nbt) +
+                " bonds does not fit the bond-order kernel's shared memory.");
+      return GB_ERROR_CAPACITY;
+    }
   }
   pot.last_plan[0] = max_nbt;
   pot.last_plan[1] = max_ntrip;
@@ -982,14 +988,6 @@ int bop_tile_ctas_per_sm(const Potential &pot, size_t smem) {
   return std::max(n, 0);
 }
 
-int bop_batch_apt(int maxz) {
-  int apt = kMaxApt;
-  while (apt > 1 && bop_smem_bytes<double>(apt * std::max(maxz, 1),
-                                           apt * std::max(maxz, 1) * std::max(maxz, 1)) >
-                        kSmemBudget)
-    apt >>= 1;
-  return apt;
-}
 
 }  // namespace gb
 

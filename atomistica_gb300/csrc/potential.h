@@ -173,7 +173,6 @@ struct BopSystem {
 int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
             bool want_wat, bool want_pb);
 // Atoms per tile for a list whose largest coordination is maxz.
-int bop_batch_apt(int maxz);
 // Shared memory of a tile with nbt bonds and ntrip (ij, ik) slots, and the
 // largest a tile may use (bytes).
 size_t bop_tile_smem(bool mixed, int nbt, int ntrip);

@@ -690,11 +690,11 @@ class Batch:
               "batch_set_options")
 
     def last_info(self):
-        """{'replayed', 'atoms_per_tile', 'graph_kernels', 'tuned_candidates'}
-        of the last evaluation."""
+        """{'replayed', 'tile_bonds' (the bond budget of the tiles),
+        'graph_kernels', 'tuned_candidates'} of the last evaluation."""
         v = (ctypes.c_int64 * 4)()
         check(self._L.gb_batch_last_info(self._h, v), "batch_last_info")
-        return {"replayed": bool(v[0]), "atoms_per_tile": int(v[1]),
+        return {"replayed": bool(v[0]), "tile_bonds": int(v[1]),
                 "graph_kernels": int(v[2]), "tuned_candidates": int(v[3])}
 
     def set_structures(self, structures):

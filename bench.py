@@ -78,7 +78,8 @@ def parse_args():
     ap.add_argument("--natoms", type=int, default=1048576)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--cpu-runs", type=int, default=3)
-    ap.add_argument("--config", default=None, choices=["eam_cu_131072"],
+    ap.add_argument("--config", default=None,
+                    choices=["eam_cu_131072", "si_batch_2048", "si_fit_256"],
                     help="measure one of the other workloads alone and print its entry "
                          "(a short command for profiling it)")
     ap.add_argument("--skip-oracle", action="store_true",
@@ -542,7 +543,7 @@ def batch_config(dev, oracle, nth):
         de = max(abs(eh[q] - refs[q]["epot"]) / len(structs[q]) for q in range(len(structs)))
         info = b.last_info()
         entry[name] = {"value": nat / t, "ms_per_step": 1e3 * t, "max_abs_dF": df,
-                       "max_abs_dE_per_atom": de, "atoms_per_tile": info["atoms_per_tile"],
+                       "max_abs_dE_per_atom": de, "tile_bonds": info["tile_bonds"],
                        "replayed": info["replayed"], "graph_kernels": info["graph_kernels"]}
     # the same structures one call each (particles + list + potential per structure)
     pot = native.Tersoff(precision="fp64")
@@ -575,9 +576,10 @@ def batch_config(dev, oracle, nth):
 def fitting_config(oracle, nth):
     """Tersoff fitting loss over 256 diamond Si supercells (64-216 atoms):
     one forward + backward (loss gradient w.r.t. the 14 parameters and the
-    positions: 1 evaluation + 14 parameter tangents + 1 Hessian-vector
-    product), its agreement with central differences, and one energy+forces
-    evaluation of the set by the oracle on the host cores."""
+    positions: 1 evaluation + 1 adjoint pass, which gives the parameter
+    gradient and the Hessian-vector product together), its agreement with
+    central differences, and one energy+forces evaluation of the set by the
+    oracle on the host cores."""
     import numpy as np
     import torch
     from atomistica_gb300 import fitting, structures
@@ -906,7 +908,12 @@ def run_config(args):
         fn()
         return time.perf_counter() - t0
 
-    entry = eam_config(dev, oracle, nth, cpu_time)
+    if args.config == "eam_cu_131072":
+        entry = eam_config(dev, oracle, nth, cpu_time)
+    elif args.config == "si_batch_2048":
+        entry = batch_config(dev, oracle, nth)
+    else:
+        entry = fitting_config(oracle, nth)
     print(json.dumps({"config": args.config, **entry}))
 
 
