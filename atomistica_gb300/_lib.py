@@ -45,6 +45,8 @@ SIGNATURES = [
     ("gb_tabulated_eam_new", _I, [_P, ctypes.c_char_p]),
     ("gb_potential_energy_and_forces_ghost", _I,
      [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("gb_potential_energy_and_forces_lammps", _I,
+     [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("gb_kumagai_scr_new", _I, [_P, _P, _P]),
     ("gb_brenner_new", _I, [_P, _P]),
     ("gb_brenner_scr_new", _I, [_P, _P, _P]),

@@ -574,6 +574,14 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   }
   nl.stream = s;
   if (pot.precision == GB_PRECISION_MIXED) nl.want_posff = true;
+  if (pot.kind != kEAM && !pot.screened) {
+    // the bond-order kernels need the reverse index, and the list build can
+    // plan their tiles (the size of the previous evaluation's tiles)
+    nl.want_rev = true;
+    nl.plan_apt = pot.tile_atoms;
+  } else {
+    nl.plan_apt = 0;
+  }
   GB_CHECK(neighbors_update(nl, p, s));
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
 
@@ -647,6 +655,7 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CUDA(cudaEventRecord(pot.ev[3], s));
   GB_CUDA(cudaStreamSynchronize(s));
   GB_CUDA(cudaGetLastError());
+  GB_CHECK(neighbors_check_reverse(nl, nullptr));  // (when the tile plan came with the list)
   float ms[4] = {0, 0, 0, 0};
   cudaEventElapsedTime(&ms[0], pot.ev[0], pot.ev[1]);
   cudaEventElapsedTime(&ms[1], pot.ev[1], pot.ev[2]);
@@ -746,9 +755,28 @@ __global__ void ghost_pos4(int nat, const double *__restrict__ r, Pos4 *__restri
 // shifts; bonds are computed for the first natloc atoms only and forces are
 // returned for all nat atoms (the caller sums the ghost forces back onto
 // their owners).  epot and wpot are the sums over the local atoms' bonds.
+// LAMMPS's per-atom virial layout, vatom (nat,6) = Fortran (6,nat), from the
+// (3,3,nat) per-atom virial w (element (a,c,i) at a + 3c + 9i): the
+// reference's LAMMPS build accumulates -w11, -w22, -w33, -w21, -w31, -w32
+// (SUM_VIRIAL under LAMMPS, macros.inc:202; bop_kernel.f90:1514-1517).
+__global__ void per_at_virial_to_voigt(int nat, const double *__restrict__ w,
+                                       double *__restrict__ v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const double *a = w + 9 * (size_t)i;
+  double *o = v + 6 * (size_t)i;
+  o[0] -= a[0];
+  o[1] -= a[4];
+  o[2] -= a[8];
+  o[3] -= a[1];
+  o[4] -= a[2];
+  o[5] -= a[5];
+}
+
 int energy_and_forces_ghost(Potential &pot, int nat, int natloc, const double *r, const int *Z,
                             const int *seed, const int *nbr, double *epot, double *f,
-                            double *wpot, const int *mask, double *epa, double *wpa) {
+                            double *wpot, const int *mask, double *epa, double *wpa,
+                            bool voigt) {
   if (!epot || !f || !wpot || nat < 0 || natloc < 0 || natloc > nat ||
       (nat > 0 && (!r || !Z || !seed))) {
     set_error("energy_and_forces_ghost: invalid arguments");
@@ -813,6 +841,7 @@ int energy_and_forces_ghost(Potential &pot, int nat, int natloc, const double *r
   nl.valid = true;
   nl.rev_valid = false;
   nl.rev_pending = false;
+  nl.plan_ready = false;
   nl.posff_valid = false;
   nl.built_for = nullptr;  // (not a particles-bound list)
   // element map from Z
@@ -838,11 +867,17 @@ int energy_and_forces_ghost(Potential &pot, int nat, int natloc, const double *r
   Stage sf, sepa, swpa;
   GB_CHECK(stage_in(f, 3 * (size_t)nat, pot.out_f, s, sf));
   GB_CHECK(stage_in(epa, nat, pot.out_epa, s, sepa));
-  GB_CHECK(stage_in(wpa, 9 * (size_t)nat, pot.out_wpa, s, swpa));
+  GB_CHECK(stage_in(wpa, (voigt ? 6 : 9) * (size_t)nat, pot.out_wpa, s, swpa));
   Outputs o;
   o.f = sf.dev;
   o.epot_per_at = sepa.dev;
   o.wpot_per_at = swpa.dev;
+  if (voigt && wpa) {
+    // the (3,3,nat) per-atom virial goes to a zeroed scratch, converted below
+    GB_CHECK(pot.g_wpa9.ensure(sizeof(double) * 9 * (size_t)std::max(nat, 1)));
+    GB_CUDA(cudaMemsetAsync(pot.g_wpa9.p, 0, sizeof(double) * 9 * (size_t)std::max(nat, 1), s));
+    o.wpot_per_at = pot.g_wpa9.as<double>();
+  }
   if (mask) {
     if (is_device_ptr(mask)) {
       o.mask = mask;
@@ -873,6 +908,10 @@ int energy_and_forces_ghost(Potential &pot, int nat, int natloc, const double *r
   sys.nat_all = nat;
   if (pot.precision == GB_PRECISION_MIXED) nl.want_posff = true;
   GB_CHECK(bop_run(pot, sys, nl, o, want_wat, false));
+  if (voigt && wpa && nat > 0) {
+    per_at_virial_to_voigt<<<(nat + 255) / 256, 256, 0, s>>>(nat, o.wpot_per_at, swpa.dev);
+    note_launch();
+  }
   GB_CHECK(stage_out(sf, s));
   GB_CHECK(stage_out(sepa, s));
   GB_CHECK(stage_out(swpa, s));
@@ -1121,7 +1160,20 @@ int gb_potential_energy_and_forces_ghost(gb_potential_t *h, int nat, int natloc,
                                          double *wpot_per_at, int *ierror) {
   clear_error();
   int rc = h ? energy_and_forces_ghost(h->pot, nat, natloc, r, Z, seed, nbr, epot, f, wpot, mask,
-                                       epot_per_at, wpot_per_at)
+                                       epot_per_at, wpot_per_at, false)
+             : GB_ERROR_ARGUMENT;
+  if (ierror) *ierror = rc;
+  return rc;
+}
+
+int gb_potential_energy_and_forces_lammps(gb_potential_t *h, int nat, int natloc,
+                                          const double *r, const int *Z, const int *seed,
+                                          const int *nbr, double *epot, double *f, double *wpot,
+                                          const int *mask, double *epot_per_at, double *vatom,
+                                          int *ierror) {
+  clear_error();
+  int rc = h ? energy_and_forces_ghost(h->pot, nat, natloc, r, Z, seed, nbr, epot, f, wpot, mask,
+                                       epot_per_at, vatom, true)
              : GB_ERROR_ARGUMENT;
   if (ierror) *ierror = rc;
   return rc;

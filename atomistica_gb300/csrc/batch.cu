@@ -162,7 +162,8 @@ int batch_tiles_work(Batch &b, int budget, cudaStream_t s, bool recut) {
     int64_t nb = 0, nt = 0;
     for (int a = b.atom_off[q]; a < b.atom_off[q + 1]; a++) {
       const int64_t z = seed[a + 1] - seed[a];
-      if (na > 0 && (na == kMaxTileAtoms || nb + z > budget || nt + z * z > tmax)) {
+      if (na > 0 && (na == kMaxTileAtoms || nb + z > budget ||
+                     nt + trip_slots((int)z) > tmax)) {
         most = std::max(most, na);
         na = 0;
       }
@@ -173,7 +174,7 @@ int batch_tiles_work(Batch &b, int budget, cudaStream_t s, bool recut) {
       }
       na++;
       nb += z;
-      nt += z * z;
+      nt += trip_slots((int)z);
     }
     if (na > 0) most = std::max(most, na);
   }
@@ -396,7 +397,7 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, doubl
   int max_nbt = nbt0, max_ntrip = ntrip0;
   for (int step = 16; step >= 1; step--) {  // head room step/16 of the maxima
     const int nb = std::min(apt * cap, nbt0 + nbt0 * step / 64 + step);
-    const int nt = std::min(apt * cap * cap, ntrip0 + ntrip0 * step / 32 + 4 * step);
+    const int nt = std::min(apt * trip_slots(cap), ntrip0 + ntrip0 * step / 32 + 4 * step);
     const size_t sm = bop_tile_smem(mixed, nb, nt);
     if (sm <= bop_tile_smem_budget() && bop_tile_ctas_per_sm(pot, sm) >= occ0) {
       max_nbt = nb;

@@ -81,6 +81,9 @@ struct BopArgs {
   const double *Acells = nullptr;
   const float2 *Acells_ff = nullptr;
   int ntiles = 0;
+  // Batches, mixed kernel: a counter (zero at launch) from which the
+  // persistent CTAs take their tiles in turn; nullptr = the static schedule.
+  int *tile_queue = nullptr;
 };
 
 __device__ __forceinline__ void tile_range(const BopArgs &a, int tile, int &a0, int &a1) {
@@ -250,15 +253,21 @@ __device__ __forceinline__ void finalize_bond(const BopArgs &a, const SmemLayout
 // the 2.33 g/cm^3, sigma = 0.25 A amorphous Si workload (1,048,576 atoms)
 // the largest force error against FP64 is 1.6e-6 eV/A with 2e-6 (2.3 % of
 // the bonds recomputed), 2.3e-6 with 4e-6 (0.6 %), 3.2e-6 with 6e-6
-// (0.23 %) and 3.5e-6 with 8e-6 (0.09 %); on the 2048 random packings
-// 3.9e-6 (2e-6) and 4.2e-6 (6e-6, 8e-6).  Each tile that has a hot bond runs
-// the dependent float-float chain while its other warps wait, so fewer hot
-// bonds mean fewer tiles paying for it: 8e-6 keeps the largest error below
-// half the 1e-5 eV/A bound.
+// (0.23 %), 3.5e-6 with 8e-6 (0.09 %), 4.8e-6 with 1.2e-5 (0.02 %), 5.2e-6
+// with 1.6e-5 and 6.8e-6 with 3.2e-5 (no bond recomputed); on the 2048
+// random packings 3.9e-6 (2e-6) and 4.2e-6 (6e-6 to 3.2e-5).  Each tile that
+// has a hot bond runs the dependent float-float chain while its other warps
+// wait, so fewer hot bonds mean fewer tiles paying for it: 1.2e-5 keeps the
+// largest error below half the 1e-5 eV/A bound.
 #ifndef GB_MX_HOT_THRESHOLD
-#define GB_MX_HOT_THRESHOLD 8.0e-6f
+#define GB_MX_HOT_THRESHOLD 1.2e-5f
 #endif
 constexpr float kHotThreshold = GB_MX_HOT_THRESHOLD;
+// 1: the mixed kernel takes a batch's tiles from a counter (dynamic
+// schedule); 0: the static round-robin schedule for batches too.
+#ifndef GB_MX_TILE_QUEUE
+#define GB_MX_TILE_QUEUE 1
+#endif
 
 template <class Pot, class R, bool kWat, bool kPB>
 __global__ void __launch_bounds__(kBopThreads)
@@ -291,7 +300,7 @@ __global__ void __launch_bounds__(kBopThreads)
       for (int q = 0; q < na; q++) {
         toff[q] = s;
         const int z = aseed[q + 1] - aseed[q];
-        s += z * z;
+        s += trip_slots(z);
       }
       toff[na] = s;
     }
@@ -511,7 +520,7 @@ __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__r
     for (int c = 0; c < 9; c++) wpa[9 * (size_t)i + c] += 0.5 * W[c];
 }
 
-// Tile plan: per tile bond count and sum of z^2.
+// Tile plan: per tile bond count and (ij, ik) slots.
 __global__ void bop_plan(int nat, int apt, int ntiles, const int *__restrict__ tile_atom0,
                          const int *__restrict__ seed, int *__restrict__ out) {
   const int tile = blockIdx.x * blockDim.x + threadIdx.x;
@@ -521,7 +530,7 @@ __global__ void bop_plan(int nat, int apt, int ntiles, const int *__restrict__ t
   int ntrip = 0;
   for (int q = a0; q < a1; q++) {
     const int z = seed[q + 1] - seed[q];
-    ntrip += z * z;
+    ntrip += trip_slots(z);
   }
   atomicMax(&out[0], seed[a1] - seed[a0]);
   atomicMax(&out[1], ntrip);
@@ -850,7 +859,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   const int maxz = std::max(nl.maxz, 1);
   int apt = batch ? sys.apt : kMaxApt;
   auto fits = [&](int aptc) {
-    const size_t worst = bop_smem_bytes<double>(aptc * maxz, aptc * maxz * maxz);
+    const size_t worst = bop_smem_bytes<double>(aptc * maxz, aptc * trip_slots(maxz));
     return worst <= kSmemBudget;
   };
   if (batch) {
@@ -880,14 +889,22 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   if (want_wat) GB_CHECK(pot.bond_w.ensure(sizeof(double) * 9 * nb));
   if (want_pb) GB_CHECK(pot.bond_fr.ensure(sizeof(double) * 3 * nb));
   GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * ntiles + 64));
-  // Plan: exact max bonds / triplets per tile.
+  // Plan: exact max bonds / triplets per tile.  A single structure's list
+  // build may have planned these tiles already (read back with the list's
+  // sizes); the reverse index is then checked by the caller after its
+  // final synchronisation.
   int *plan = reinterpret_cast<int *>(pot.tile_part.as<double>() + 10 * (size_t)ntiles);
   GB_CUDA(cudaMemsetAsync(plan, 0, sizeof(int) * 4, s));
-  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, sys.tile_atom0,
-                                                nl.seed.as<int>(), plan);
-  note_launch();
   int max_nbt = sys.max_nbt, max_ntrip = sys.max_ntrip;
-  if (!sys.capture) {
+  const bool preplanned = !batch && !sys.capture && nat_all == nat && nl.plan_ready &&
+                          nl.plan_done_apt == apt;
+  if (preplanned) {
+    max_nbt = nl.hplan[0];
+    max_ntrip = nl.hplan[1];
+  } else {
+    GB_CHECK(bop_plan_launch(nat, apt, ntiles, sys.tile_atom0, nl.seed.as<int>(), plan, s));
+  }
+  if (!sys.capture && !preplanned) {
     GB_CHECK(pot.hred.ensure(64));
     int *hplan = pot.hred.as<int>();
     GB_CUDA(cudaMemcpyAsync(hplan, plan, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
@@ -925,6 +942,10 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   args.wbond = want_wat ? pot.bond_w.as<double>() : nullptr;
   args.frbond = want_pb ? pot.bond_fr.as<double>() : nullptr;
   args.tile_part = pot.tile_part.as<double>();
+  // Batch tiles carry their own partial rows, so the order in which CTAs
+  // take them does not change any sum: they are handed out by a counter
+  // (plan[2], zeroed with the plan above).
+  if (batch && mixed && GB_MX_TILE_QUEUE) args.tile_queue = plan + 2;
   int *status = o.status;
   int rc, rows = ntiles;
   if (mixed && !nl.posff_valid) {
@@ -964,6 +985,15 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   sys.nat = p.nat;
   std::memcpy(sys.A, p.A, sizeof(sys.A));
   return bop_run(pot, sys, nl, o, want_wat, want_pb);
+}
+
+int bop_plan_launch(int nat, int apt, int ntiles, const int *tile_atom0, const int *seed,
+                    int *out, cudaStream_t s) {
+  if (ntiles <= 0) return 0;
+  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, tile_atom0, seed, out);
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
 }
 
 size_t bop_tile_smem(bool mixed, int nbt, int ntrip) {
@@ -1233,7 +1263,7 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   const int maxz = std::max(hs[0], 1);
   int apt = kMaxApt;
   auto fits = [&](int aptc) {
-    return bop_smem_bytes<double>(aptc * maxz, aptc * maxz * maxz) <= kSmemBudget;
+    return bop_smem_bytes<double>(aptc * maxz, aptc * trip_slots(maxz)) <= kSmemBudget;
   };
   while (apt > 1 && !fits(apt)) apt >>= 1;
   while (apt > 1 && (int64_t)apt * std::max(1, n / nat) > 2 * kBopThreads) apt >>= 1;

@@ -637,6 +637,13 @@ __device__ inline void block_sum_tile(ff e, const float (&w)[9], double *out, ff
   }
 }
 
+// The tile index that thread 0 took from the queue at the start of the
+// current tile (the barrier orders its write before every thread's read).
+__device__ __forceinline__ int next_queued_tile(const int &s_next) {
+  __syncthreads();
+  return s_next;
+}
+
 template <class Pot, bool kWat, bool kPB>
 __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
     bop_tile_mx(const BopArgs a, const Pot pot, const MxParams mp, const float4 *__restrict__ posff,
@@ -644,7 +651,7 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ ff red_scratch[(kMxThreads / 32) * 10];
   __shared__ ff s_exp[256], s_sin[257], s_cos[257];
-  __shared__ int s_nhot;
+  __shared__ int s_nhot, s_next;
   __shared__ ff sAf[9];
   const int tid = threadIdx.x;
   for (int q = tid; q < 256; q += kMxThreads)
@@ -653,16 +660,27 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
     s_sin[q] = ff_make(kFfSinTab[2 * q], kFfSinTab[2 * q + 1]);
     s_cos[q] = ff_make(kFfCosTab[2 * q], kFfCosTab[2 * q + 1]);
   }
-  // Persistent CTAs: tiles blockIdx.x, blockIdx.x + gridDim.x, ... (a static
-  // schedule, so the per-CTA energy and virial sums are reproducible).
+  // Persistent CTAs.  A single structure: tiles blockIdx.x, blockIdx.x +
+  // gridDim.x, ... (a static schedule, so the per-CTA energy and virial sums
+  // are reproducible).  A batch (one partial row per tile): the next tile
+  // from the counter a.tile_queue, taken at the start of the current one.
   ff eacc = ff_make(0.0f, 0.0f);
   float wacc[9];
 #pragma unroll
   for (int c = 0; c < 9; c++) wacc[c] = 0.0f;
   const int ntiles = a.tile_atom0 ? a.ntiles : (a.nat + a.apt - 1) / a.apt;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    __syncthreads();  // the previous tile is done with shared memory
-    if (tid == 0) s_nhot = 0;
+  int *const queue = a.tile_atom0 ? a.tile_queue : nullptr;
+  if (queue) {
+    if (tid == 0) s_next = atomicAdd(queue, 1);
+    __syncthreads();
+  }
+  for (int tile = queue ? s_next : blockIdx.x; tile < ntiles;
+       tile = queue ? next_queued_tile(s_next) : tile + gridDim.x) {
+    __syncthreads();  // the previous tile is done with shared memory (and s_next)
+    if (tid == 0) {
+      s_nhot = 0;
+      if (queue) s_next = atomicAdd(queue, 1);
+    }
     if (tid < 9) {  // this tile's cell
       const float2 v = a.Acells_ff ? a.Acells_ff[9 * a.tile_struct[tile] + tid]
                                    : make_float2(mp.A[tid / 3][tid % 3].hi,
@@ -683,12 +701,12 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
       for (int q = tid; q < na; q += kMxThreads) el[q] = a.el[a0 + q];
       __syncthreads();
       if (tid < 32) {
-        // triplet-slot offsets: exclusive scan of z^2 over the tile's atoms
+        // triplet-slot offsets: exclusive scan of trip_slots(z) over the tile's atoms
         // (na <= 64: two atoms per lane)
         const int q0 = 2 * tid, q1 = 2 * tid + 1;
         const int z0 = q0 < na ? aseed[q0 + 1] - aseed[q0] : 0;
         const int z1 = q1 < na ? aseed[q1 + 1] - aseed[q1] : 0;
-        const int own = z0 * z0 + z1 * z1;
+        const int own = trip_slots(z0) + trip_slots(z1);
         int inc = own;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -697,7 +715,7 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
         }
         const int ex = inc - own;
         if (q0 < na) toff[q0] = ex;
-        if (q1 < na) toff[q1] = ex + z0 * z0;
+        if (q1 < na) toff[q1] = ex + trip_slots(z0);
         if (tid == 31) toff[na] = inc;
       }
       __syncthreads();

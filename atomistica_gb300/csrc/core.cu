@@ -711,6 +711,63 @@ __global__ void nl_compact(int nat, int cap, const int *__restrict__ seed,
   }
 }
 
+// nl_compact and the reverse index in one pass: entry k of atom i, staged as
+// (j, s) at stage[i cap + k], goes to nbr / shift at seed[i] + k, and its
+// reverse (j -> i, -s) is looked up among j's staged entries instead of in the
+// compacted arrays: rev = seed[j] + its position.  Four entries of i at a
+// time, so that their loads (seed[j], then the first 32-byte sector of j's
+// staged row: its first four entries; cap is a multiple of 4) overlap.
+__global__ void nl_compact_reverse(int nat, int cap, const int *__restrict__ seed,
+                                   const int2 *__restrict__ stage, int *__restrict__ nbr,
+                                   int *__restrict__ shift, int *__restrict__ rev,
+                                   int *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const int s = seed[i], n = seed[i + 1] - s;
+  const int2 *src = stage + (size_t)i * cap;
+  for (int k0 = 0; k0 < n; k0 += 4) {
+    int2 v[4];
+    int want[4], cj[4], nj[4], found[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) v[q] = k0 + q < n ? src[k0 + q] : make_int2(i, 0);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (k0 + q < n) {
+        nbr[s + k0 + q] = v[q].x;
+        shift[s + k0 + q] = v[q].y;
+      }
+      int s0, s1, s2;
+      unpack_shift(v[q].y, s0, s1, s2);
+      want[q] = pack_shift(-s0, -s1, -s2);
+      cj[q] = seed[v[q].x];
+      nj[q] = k0 + q < n ? seed[v[q].x + 1] - cj[q] : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      found[q] = -1;
+      if (nj[q] > 0) {
+        const int4 *row = reinterpret_cast<const int4 *>(stage + (size_t)v[q].x * cap);
+        const int4 e01 = row[0], e23 = row[1];
+        const int ex[4] = {e01.x, e01.z, e23.x, e23.z}, ey[4] = {e01.y, e01.w, e23.y, e23.w};
+#pragma unroll
+        for (int c = 3; c >= 0; c--)
+          if (c < nj[q] && ex[c] == i && ey[c] == want[q]) found[q] = c;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (k0 + q >= n) continue;
+      const int2 *row = stage + (size_t)v[q].x * cap;
+      for (int c = 4; c < nj[q] && found[q] < 0; c++) {
+        const int2 e = row[c];
+        if (e.x == i && e.y == want[q]) found[q] = c;
+      }
+      if (found[q] < 0) atomicOr(&status[1], 4);
+      rev[s + k0 + q] = found[q] < 0 ? -1 : cj[q] + found[q];
+    }
+  }
+}
+
 // rev[b] = entry (j -> i, -s) of the entry b = (i -> j, s).
 // One thread per atom i: each entry b = (i -> j, s) searches atom j's entries
 // for (j -> i, -s), four candidates per step.
@@ -878,12 +935,14 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
   GB_CHECK(nl.spos.ensure(sizeof(float4) * std::max(nat, 1)));
   GB_CHECK(nl.swrap.ensure(sizeof(int) * std::max(nat, 1)));
   GB_CHECK(nl.seed.ensure(sizeof(int) * (nat + 1)));
-  GB_CHECK(nl.stats.ensure(sizeof(int) * 8 + sizeof(int) * (size_t)(ncells + 1)));
-  GB_CHECK(nl.hstats.ensure(sizeof(int) * 8));
+  GB_CHECK(nl.stats.ensure(sizeof(int) * 16 + sizeof(int) * (size_t)(ncells + 1)));
+  GB_CHECK(nl.hstats.ensure(sizeof(int) * 16));
   // [0] maxz [1] flags [2] n_big [3] max |coordinate| [4] reverse-index flags
+  // [6..7] 64-bit entry total [8..9] tile plan (most bonds, most slots)
   int *status = nl.stats.as<int>();
-  int *big_cells = status + 8;
-  GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 8, stream));
+  int *big_cells = status + 16;
+  GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 16, stream));
+  nl.plan_ready = false;
   GB_CUDA(cudaMemsetAsync(nl.cell_count.p, 0, sizeof(int) * (ncells + 1), stream));
   const int T = 256;
   const int nb = (nat + T - 1) / T;
@@ -964,13 +1023,26 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
                             stream));
     return 0;
   }
-  // Read back: maxz, flags, n_big, total entries (int32 scan and 64-bit sum).
+  // The bond-order tile plan of this list, for the tiles the potential asked
+  // for, goes back with the list's sizes (one host synchronisation for both).
+  const int plan_apt = batch ? 0 : nl.plan_apt;
+  if (plan_apt > 0 && nat > 0)
+    GB_CHECK(bop_plan_launch(nat, plan_apt, (nat + plan_apt - 1) / plan_apt, nullptr,
+                             nl.seed.as<int>(), status + 8, stream));
+  // Read back: maxz, flags, n_big, total entries (int32 scan and 64-bit sum),
+  // the tile plan.
   GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
   GB_CUDA(cudaMemcpyAsync(hs + 4, nl.seed.as<int>() + nat, sizeof(int), cudaMemcpyDeviceToHost,
                           stream));
-  GB_CUDA(cudaMemcpyAsync(hs + 6, status + 6, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
+  GB_CUDA(cudaMemcpyAsync(hs + 6, status + 6, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
   GB_CUDA(cudaStreamSynchronize(stream));
   GB_CUDA(cudaGetLastError());
+  if (plan_apt > 0 && nat > 0) {
+    nl.hplan[0] = hs[8];
+    nl.hplan[1] = hs[9];
+    nl.plan_done_apt = plan_apt;
+    nl.plan_ready = true;
+  }
   if (hs[1] & 1) {
     set_error("Non-finite particle position.");
     return GB_ERROR_DOMAIN;
@@ -991,7 +1063,18 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
   GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
   const int maxz = hs[0];
   if (nat > 0) {
-    if (nl.stage_cap > 0 && maxz <= nl.stage_cap) {
+    if (nl.stage_cap > 0 && maxz <= nl.stage_cap && nl.want_rev && !batch &&
+        total <= 24 * (int64_t)nat) {
+      // compaction and reverse index together (the symmetry flag is read
+      // by the caller's next synchronisation, as after neighbors_build_reverse)
+      GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
+      nl_compact_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, nl.stage_cap, nl.seed.as<int>(), nl.stage.as<int2>(), nl.nbr.as<int>(),
+          nl.shift.as<int>(), nl.rev.as<int>(), status + 3);
+      note_launch();
+      GB_CUDA(cudaMemcpyAsync(hs + 5, status + 4, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      nl.rev_pending = true;
+    } else if (nl.stage_cap > 0 && maxz <= nl.stage_cap) {
       nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
                                                         nl.stage.as<int2>(), nl.nbr.as<int>(),
                                                         nl.shift.as<int>());

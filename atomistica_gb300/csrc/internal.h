@@ -98,6 +98,18 @@ __host__ __device__ inline void unpack_shift(int32_t p, int &s0, int &s1, int &s
   s2 = (int)((u >> 20) & 1023u) - 512;
 }
 constexpr int kMaxShift = 511;
+
+// (ij, ik) slots of an atom with z bonds in the bond-order tile kernels: its
+// z x z block, one slot longer for even z > 0, so that consecutive atoms'
+// blocks start an odd number of slots apart and the rows that a warp's
+// lanes write and read at one time (several atoms at once) fall into
+// different shared-memory banks.
+#ifndef GB_TRIP_PAD
+#define GB_TRIP_PAD 1
+#endif
+__host__ __device__ __forceinline__ int trip_slots(int z) {
+  return z * z + ((GB_TRIP_PAD && z > 0 && !(z & 1)) ? 1 : 0);
+}
 // Largest staging buffer of the single-pass neighbour build (bytes).
 constexpr size_t kStageMaxBytes = size_t(2) << 30;
 
@@ -168,10 +180,24 @@ struct Neighbors {
   HostBuf hstats;
   bool rev_valid = false;
   bool rev_pending = false;  // reverse index built, symmetry flag not yet read
+  // Set by a bond-order potential before a single-structure build: the
+  // staged compaction also writes the reverse index, and the tile plan for
+  // tiles of plan_apt atoms is computed before the build's one read-back.
+  bool want_rev = false;
+  int plan_apt = 0;
+  bool plan_ready = false;  // hplan holds the plan of this list for plan_done_apt
+  int plan_done_apt = 0;
+  int hplan[2] = {0, 0};    // most bonds and (ij, ik) slots in one tile
   int64_t nentries = 0;
   int maxz = 0;
   cudaStream_t stream = nullptr;
 };
+
+// Tile plan of the bond-order kernels (launch only): out[0] = most bonds and
+// out[1] = most (ij, ik) slots of the tiles of apt consecutive atoms (or of
+// the caller's tiles, tile_atom0 != nullptr); out[0..1] must start at zero.
+int bop_plan_launch(int nat, int apt, int ntiles, const int *tile_atom0, const int *seed,
+                    int *out, cudaStream_t s);
 
 // Builds/refreshes the list for p if positions or cell changed
 // (neighbors_update, :430-456).

@@ -100,6 +100,7 @@ struct Potential {
   // shifts): the list, positions and element map live here.
   Neighbors gnl;
   DevBuf g_r;
+  DevBuf g_wpa9;  // (3,3,nat) per-atom virial before the LAMMPS Voigt conversion
   HostBuf hred;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t kev[2] = {nullptr, nullptr};  // around the dominant force kernel

@@ -443,10 +443,13 @@ class _Potential:
 
 
 def _ghost_call(pot, r, Z, seed, nbr, natloc, forces=None, mask=None, epot_per_at=False,
-                wpot_per_at=False):
+                wpot_per_at=False, vatom=None):
     """energy_and_forces on a caller's list over local + ghost atoms (the
     LAMMPS contract): returns (epot, forces (nat,3), wpot, [epot_per_at],
-    [wpot_per_at]); bonds of the first natloc atoms, forces on all."""
+    [wpot_per_at]); bonds of the first natloc atoms, forces on all.  With
+    ``vatom`` (a (nat,6) float64 array) the per-atom virial is accumulated
+    into it in LAMMPS's layout and sign instead
+    (gb_potential_energy_and_forces_lammps)."""
     r = np.ascontiguousarray(r, dtype=np.float64)
     nat = len(r)
     Z = np.ascontiguousarray(Z, dtype=np.int32)
@@ -460,11 +463,19 @@ def _ghost_call(pot, r, Z, seed, nbr, natloc, forces=None, mask=None, epot_per_a
     m = None if mask is None else np.ascontiguousarray(np.asarray(mask).astype(np.int32))
     err = ctypes.c_int(0)
     ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
-    check(pot._L.gb_potential_energy_and_forces_ghost(
-        pot._h, nat, int(natloc), r.ctypes.data, Z.ctypes.data, seed.ctypes.data,
-        nbr.ctypes.data if len(nbr) else None, ctypes.byref(epot), f.ctypes.data,
-        wpot.ctypes.data, ptr(m), ptr(epa), ptr(wpa), ctypes.byref(err)),
-        "energy_and_forces_ghost")
+    if vatom is not None:
+        if vatom.shape != (nat, 6) or vatom.dtype != np.float64 or \
+                not vatom.flags["C_CONTIGUOUS"]:
+            raise ValueError("vatom must be a C-contiguous (nat, 6) float64 array")
+        if wpot_per_at:
+            raise ValueError("vatom and wpot_per_at exclude each other")
+        fn, wpa, name = (pot._L.gb_potential_energy_and_forces_lammps, vatom,
+                         "energy_and_forces_lammps")
+    else:
+        fn, name = pot._L.gb_potential_energy_and_forces_ghost, "energy_and_forces_ghost"
+    check(fn(pot._h, nat, int(natloc), r.ctypes.data, Z.ctypes.data, seed.ctypes.data,
+             nbr.ctypes.data if len(nbr) else None, ctypes.byref(epot), f.ctypes.data,
+             wpot.ctypes.data, ptr(m), ptr(epa), ptr(wpa), ctypes.byref(err)), name)
     out = [epot.value, f, np.ascontiguousarray(wpot)]
     if epot_per_at:
         out.append(epa)

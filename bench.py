@@ -84,6 +84,9 @@ def parse_args():
                          "(a short command for profiling it)")
     ap.add_argument("--skip-oracle", action="store_true",
                     help="skip the FP64 oracle error check and CPU baseline")
+    ap.add_argument("--forms", default="fp64,mixed,fp64_graph,mixed_graph",
+                    help="--config si_batch_2048: the forms to time (comma list); with "
+                         "--skip-oracle only those run (a short command for a launch list)")
     return ap.parse_args()
 
 
@@ -225,11 +228,11 @@ def flop_model(z):
             "bytes": BYTES_ATOM * len(z) + BYTES_BOND * nb}
 
 
-def cpu_baseline(structure, params, runs):
+def cpu_baseline(structure, params, runs, nthreads=None):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # CPU baseline leg: the reference algorithm on the host cores
     oracle.build()
-    nthreads = oracle.max_threads()
+    nthreads = nthreads or oracle.max_threads()
     oracle.bop_compute("tersoff", params, structure, nthreads=nthreads)
     ts = []
     for _ in range(runs):
@@ -239,8 +242,8 @@ def cpu_baseline(structure, params, runs):
     t = statistics.median(ts)
     return {"value": len(structure) / t, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": "full %d-atom workload incl. neighbour build, median of %d calls "
-                      "(C++ FP64 restatement of the reference algorithm, OpenMP)"
-                      % (len(structure), runs),
+                      "(C++ FP64 restatement of the reference algorithm, OpenMP, %d "
+                      "thread%s)" % (len(structure), runs, nthreads, "" if nthreads == 1 else "s"),
             "seconds_per_call": t}
 
 
@@ -496,7 +499,8 @@ def screened_config(dev, oracle, nth, cpu_time):
     return out
 
 
-def batch_config(dev, oracle, nth):
+def batch_config(dev, oracle, nth, forms=("fp64", "mixed", "fp64_graph", "mixed_graph"),
+                 check=True):
     """2048 triclinic Si structures, N ~ U{8..512}, in one batched evaluation
     (FP64 and mixed) against the same structures evaluated one call each on
     the GPU and by the oracle on all host cores."""
@@ -513,10 +517,11 @@ def batch_config(dev, oracle, nth):
     f = torch.zeros((nat, 3), dtype=torch.float64, device=dev)
     entry = {"nstruct": len(structs), "natoms": nat, "unit": UNIT,
              "generation_s": t_gen, "sample": "all 2048 structures"}
-    refs = [oracle.bop_compute("tersoff", params, q, nthreads=nth) for q in structs]
+    refs = [oracle.bop_compute("tersoff", params, q, nthreads=nth) for q in structs] \
+        if check else None
     # eager (list build and tile plan read back to the host each step) and
     # CUDA-graph replay of the whole step with autotuned tiles
-    for name in ("fp64", "mixed", "fp64_graph", "mixed_graph"):
+    for name in forms:
         prec = name.split("_")[0]
         graph = name.endswith("_graph")
         b = native.Batch(structs)
@@ -535,16 +540,20 @@ def batch_config(dev, oracle, nth):
             e, _, w = b.energy_and_forces(pot, forces=f)
         torch.cuda.synchronize()
         t = (time.perf_counter() - t0) / steps
-        fh = f.cpu().numpy()
-        eh = e.cpu().numpy()
-        off = b.offsets
-        df = max(float(np.max(np.abs(fh[off[q]:off[q + 1]] - refs[q]["f"])))
-                 for q in range(len(structs)))
-        de = max(abs(eh[q] - refs[q]["epot"]) / len(structs[q]) for q in range(len(structs)))
         info = b.last_info()
-        entry[name] = {"value": nat / t, "ms_per_step": 1e3 * t, "max_abs_dF": df,
-                       "max_abs_dE_per_atom": de, "tile_bonds": info["tile_bonds"],
+        entry[name] = {"value": nat / t, "ms_per_step": 1e3 * t, "tile_bonds": info["tile_bonds"],
                        "replayed": info["replayed"], "graph_kernels": info["graph_kernels"]}
+        if check:
+            fh = f.cpu().numpy()
+            eh = e.cpu().numpy()
+            off = b.offsets
+            entry[name]["max_abs_dF"] = max(
+                float(np.max(np.abs(fh[off[q]:off[q + 1]] - refs[q]["f"])))
+                for q in range(len(structs)))
+            entry[name]["max_abs_dE_per_atom"] = max(
+                abs(eh[q] - refs[q]["epot"]) / len(structs[q]) for q in range(len(structs)))
+    if not check:
+        return entry
     # the same structures one call each (particles + list + potential per structure)
     pot = native.Tersoff(precision="fp64")
     objs = []
@@ -765,30 +774,39 @@ def run_ours(args):
     seed_np, _, _ = nl.get_list(p)
     fm = flop_model(np.diff(seed_np))
 
-    # e2e through the public API with pinned host buffers.
+    # e2e through the public API: pinned host buffers, and the plain
+    # (pageable) numpy arrays an ASE-style caller passes.
+    pot = pots["mixed"]
+
+    def e2e_rate(pos_np, f_np):
+        for _ in range(2):
+            p.set_positions(pos_np)
+            pot.energy_and_forces(p, nl, forces=f_np, accumulate=False)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            p.set_positions(pos_np)
+            pot.energy_and_forces(p, nl, forces=f_np, accumulate=False)
+        torch.cuda.synchronize()
+        t = tmax(time.perf_counter() - t0)
+        return ws * nat * args.steps / t, 1e3 * t / args.steps
+
     pos_h = torch.empty((nat, 3), dtype=torch.float64).pin_memory()
     pos_h.copy_(torch.from_numpy(s.positions))
     f_h = torch.zeros((nat, 3), dtype=torch.float64).pin_memory()
-    pos_np, f_np = pos_h.numpy(), f_h.numpy()
-    pot = pots["mixed"]
-    for _ in range(2):
-        p.set_positions(pos_np)
-        pot.energy_and_forces(p, nl, forces=f_np, accumulate=False)
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        p.set_positions(pos_np)
-        e2e_e, _, e2e_w = pot.energy_and_forces(p, nl, forces=f_np, accumulate=False)
-    torch.cuda.synchronize()
-    t_e2e = tmax(time.perf_counter() - t0)
-    e2e = {"value": ws * nat * args.steps / t_e2e, "unit": UNIT,
+    e2e_value, e2e_ms = e2e_rate(pos_h.numpy(), f_h.numpy())
+    pg_value, pg_ms = e2e_rate(np.array(s.positions, dtype=np.float64, order="C"),
+                               np.zeros((nat, 3)))
+    e2e = {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms,
            "h2d_bytes_per_step": 24 * nat, "d2h_bytes_per_step": 24 * nat + 80,
            "api": "native.Particles.set_positions + Tersoff.energy_and_forces(accumulate="
                   "False) (C-ABI gb_particles_set_positions / "
                   "gb_potential_energy_and_forces_flags(GB_FORCES_SET)), pinned host numpy "
-                  "buffers: positions up, forces written down"}
+                  "buffers: positions up, forces written down",
+           "pageable": {"value": pg_value, "unit": UNIT, "ms_per_step": pg_ms,
+                        "buffers": "plain numpy arrays (pageable host memory), same calls"}}
 
     # Roofline of the dominant kernel (mixed bond-order tile kernel):
     # T_roof = max(flops / FP32 peak, bytes / HBM peak), frac = T_roof / t.
@@ -861,6 +879,7 @@ def run_ours(args):
                 "abs_dE_per_atom": abs(e - ref["epot"]) / nat,
                 "max_abs_dW": float(np.max(np.abs(w - ref["wpot"])))}
         line["cpu_baseline"] = cpu_baseline(s, params, args.cpu_runs)
+        line["cpu_baseline_1thread"] = cpu_baseline(s, params, 1, nthreads=1)
         line["other_configs"] = other_configs(dev, oracle)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -911,7 +930,8 @@ def run_config(args):
     if args.config == "eam_cu_131072":
         entry = eam_config(dev, oracle, nth, cpu_time)
     elif args.config == "si_batch_2048":
-        entry = batch_config(dev, oracle, nth)
+        entry = batch_config(dev, oracle, nth, tuple(args.forms.split(",")),
+                             check=not args.skip_oracle)
     else:
         entry = fitting_config(oracle, nth)
     print(json.dumps({"config": args.config, **entry}))

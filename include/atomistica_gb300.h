@@ -256,6 +256,17 @@ int gb_potential_energy_and_forces_ghost(gb_potential_t *pot, int nat, int natlo
                                          const int *nbr, double *epot, double *f, double *wpot,
                                          const int *mask, double *epot_per_at,
                                          double *wpot_per_at, int *ierror);
+/* lammps_<mod>_energy_and_forces (src/lammps/gen_factory.py:175-226): as
+ * gb_potential_energy_and_forces_ghost, with the per-atom virial in the
+ * layout the reference's LAMMPS build writes: vatom (nat,6) (= Fortran
+ * (6,nat)), accumulated into with the LAMMPS sign, vatom[6i + k] -= w_k(i)
+ * for k = xx, yy, zz, yx, zx, zy of atom i's virial (SUM_VIRIAL under
+ * LAMMPS, macros.inc:202). */
+int gb_potential_energy_and_forces_lammps(gb_potential_t *pot, int nat, int natloc,
+                                          const double *r, const int *Z, const int *seed,
+                                          const int *nbr, double *epot, double *f, double *wpot,
+                                          const int *mask, double *epot_per_at, double *vatom,
+                                          int *ierror);
 /* python_<mod>_energy_and_forces (gen_factory.py:239-356 -> COMPUTE_FUNC,
  * default_compute_func.f90:25-100; tabulated_alloy_eam.f90:360-415).
  * q (charges) is accepted and ignored, as by these potentials. */
