@@ -99,6 +99,34 @@ int batch_binning(Batch &b, double cutoff, cudaStream_t s) {
   return 0;
 }
 
+// Uploads a tiling: tile_atom0 [nt + 1] | tile_struct [nt] | seg [nstruct + 1]
+// | piece0 [np + 1] | seg_piece [nstruct + 1], where the pieces cut each
+// structure's rows [seg[q], seg[q + 1]) into runs of at most 32 rows for the
+// two-step per-structure sums.
+int upload_tiles(Batch &b, const std::vector<int> &atom0, const std::vector<int> &strct,
+                 const std::vector<int> &seg, cudaStream_t s) {
+  const int nt = (int)strct.size();
+  std::vector<int> piece0, seg_piece(b.nstruct + 1, 0);
+  for (int q = 0; q < b.nstruct; q++) {
+    seg_piece[q] = (int)piece0.size();
+    for (int r = seg[q]; r < seg[q + 1]; r += 32) piece0.push_back(r);
+  }
+  seg_piece[b.nstruct] = (int)piece0.size();
+  const int np = (int)piece0.size();
+  piece0.push_back(nt);
+  std::vector<int> all;
+  all.reserve(atom0.size() + strct.size() + seg.size() + piece0.size() + seg_piece.size());
+  const std::vector<int> *parts[] = {&atom0, &strct, &seg, &piece0, &seg_piece};
+  for (const std::vector<int> *v : parts) all.insert(all.end(), v->begin(), v->end());
+  GB_CHECK(b.tiles.ensure(sizeof(int) * all.size()));
+  GB_CUDA(cudaMemcpyAsync(b.tiles.p, all.data(), sizeof(int) * all.size(),
+                          cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  b.ntiles = nt;
+  b.npiece = np;
+  return 0;
+}
+
 // Tiles of at most apt atoms inside each structure; per-structure tile
 // offsets for the energy/virial sums.
 int batch_tiles(Batch &b, int apt, cudaStream_t s) {
@@ -114,24 +142,12 @@ int batch_tiles(Batch &b, int apt, cudaStream_t s) {
     }
   }
   seg[b.nstruct] = (int)strct.size();
-  const int nt = (int)strct.size();
   atom0.push_back(b.nat);
-  // layout: tile_atom0 [nt + 1] | tile_struct [nt] | seg [nstruct + 1]
-  const size_t n = atom0.size() + strct.size() + seg.size();
-  GB_CHECK(b.tiles.ensure(sizeof(int) * n));
-  int *d = b.tiles.as<int>();
-  GB_CUDA(cudaMemcpyAsync(d, atom0.data(), sizeof(int) * atom0.size(), cudaMemcpyHostToDevice, s));
-  if (nt)
-    GB_CUDA(cudaMemcpyAsync(d + atom0.size(), strct.data(), sizeof(int) * strct.size(),
-                            cudaMemcpyHostToDevice, s));
-  GB_CUDA(cudaMemcpyAsync(d + atom0.size() + strct.size(), seg.data(), sizeof(int) * seg.size(),
-                          cudaMemcpyHostToDevice, s));
-  GB_CUDA(cudaStreamSynchronize(s));
+  GB_CHECK(upload_tiles(b, atom0, strct, seg, s));
   b.tiles_apt = apt;
   b.tiles_budget = 0;
   b.graph_geom = ~0ull;  // a captured graph holds the previous tiles: capture again
   b.tile_max_atoms = apt;
-  b.ntiles = nt;
   b.tiles_nentries = b.nl.nentries;
   return 0;
 }
@@ -179,26 +195,14 @@ int batch_tiles_work(Batch &b, int budget, cudaStream_t s, bool recut) {
     if (na > 0) most = std::max(most, na);
   }
   seg[b.nstruct] = (int)strct.size();
-  const int nt = (int)strct.size();
   atom0.push_back(b.nat);
-  // layout: tile_atom0 [nt + 1] | tile_struct [nt] | seg [nstruct + 1]
-  const size_t n = atom0.size() + strct.size() + seg.size();
-  GB_CHECK(b.tiles.ensure(sizeof(int) * n));
-  int *d = b.tiles.as<int>();
-  GB_CUDA(cudaMemcpyAsync(d, atom0.data(), sizeof(int) * atom0.size(), cudaMemcpyHostToDevice, s));
-  if (nt)
-    GB_CUDA(cudaMemcpyAsync(d + atom0.size(), strct.data(), sizeof(int) * strct.size(),
-                            cudaMemcpyHostToDevice, s));
-  GB_CUDA(cudaMemcpyAsync(d + atom0.size() + strct.size(), seg.data(), sizeof(int) * seg.size(),
-                          cudaMemcpyHostToDevice, s));
-  GB_CUDA(cudaStreamSynchronize(s));
+  GB_CHECK(upload_tiles(b, atom0, strct, seg, s));
   b.tiles_apt = budget;
   b.tiles_budget = budget;
   b.tile_max_atoms = most;
   b.tiles_geom = b.geom_rev;
   b.tiles_pos = b.built_pos;
   b.graph_geom = ~0ull;  // a captured graph holds the previous tiles: capture again
-  b.ntiles = nt;
   b.tiles_nentries = b.nl.nentries;
   return 0;
 }
@@ -278,6 +282,10 @@ BopSystem batch_system(const Batch &b) {
   sys.seg = t + 2 * b.ntiles + 1;
   sys.nseg = b.nstruct;
   sys.red_seg = b.red_seg.as<double>();
+  sys.piece0 = t + 2 * b.ntiles + 1 + b.nstruct + 1;
+  sys.seg_piece = sys.piece0 + b.npiece + 1;
+  sys.npiece = b.npiece;
+  sys.piece_sum = b.red_piece.as<double>();
   sys.Acells = b.Acells.as<double>();
   sys.Acells_ff = reinterpret_cast<const float2 *>(b.Acells_ff.p);
   sys.ntiles = b.ntiles;
@@ -292,8 +300,10 @@ int batch_forces(Batch &b, Potential &pot, double *fdev, cudaStream_t s, BopSyst
   GB_CHECK(pot.red.ensure(sizeof(double) * 16));
   GB_CHECK(pot.hred.ensure(sizeof(double) * 16));
   GB_CHECK(b.red_seg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1)));
+  GB_CHECK(b.red_piece.ensure(sizeof(double) * 10 * std::max(b.npiece, 1)));
   GB_CHECK(b.hseg.ensure(sizeof(double) * 10 * std::max(b.nstruct, 1) + 64));
   sys.red_seg = b.red_seg.as<double>();  // (allocated just now on the first call)
+  sys.piece_sum = b.red_piece.as<double>();
   Outputs o;
   o.f = fdev;
   o.red = pot.red.as<double>();
@@ -562,6 +572,7 @@ int batch_prepare(Batch &b, Potential &pot, cudaStream_t &s, double &cutoff) {
   }
   GB_CHECK(batch_binning(b, cutoff, s));
   if (pot.precision == GB_PRECISION_MIXED) b.nl.want_posff = true;
+  b.nl.want_rev = true;  // the compaction also builds the reverse index
   return 0;
 }
 

@@ -17,14 +17,14 @@ struct Batch {
   std::vector<int> hZ;        // nat
   std::vector<int> zu;        // distinct atomic numbers of the batch (sorted)
   uint64_t geom_rev = 0, pos_rev = 0;
-  DevBuf r, sid, bps, Acells, Acells_ff, tiles, red_seg, el;
+  DevBuf r, sid, bps, Acells, Acells_ff, tiles, red_seg, red_piece, el;
   DevBuf tan_G, tan_part, tan_f, tan_dpos, tan_red;  // tangent evaluation scratch
   HostBuf hseg;
   // cached derived state
   uint64_t built_geom = ~0ull, built_pos = ~0ull, el_geom = ~0ull;
   const Potential *el_pot = nullptr;
   double built_cutoff = -1.0;
-  int ncells = 0, tiles_apt = 0, ntiles = 0;
+  int ncells = 0, tiles_apt = 0, ntiles = 0, npiece = 0;
   int64_t tiles_nentries = -1;
   // Tiles of the bond-order kernels (batch_tiles_work): cut inside each
   // structure by a bond budget from the per-atom counts of the list built

@@ -718,6 +718,55 @@ __global__ void reduce_segments_kernel(const double *__restrict__ part,
         sh[threadIdx.x] + (blockDim.x > 32 ? sh[kRedCols + threadIdx.x] : 0.0);
 }
 
+// Per-structure sums in two steps, so that a structure with many tiles is
+// summed by many warps: the sum of each piece (a run of at most 32 of one
+// structure's tile rows), then per structure the sum of its pieces.  Each
+// warp takes three pieces (or structures), a lane per (piece, column), and
+// adds the rows in order: one FP64 add per row and column.
+constexpr int kPerWarp = 32 / kRedCols;
+static_assert(kPerWarp >= 1, "one column per lane");
+
+__global__ void reduce_pieces_kernel(const double *__restrict__ part,
+                                     const int *__restrict__ piece0, int npiece,
+                                     double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kPerWarp + lane / kRedCols;
+  const int c = lane % kRedCols;
+  if (lane >= kPerWarp * kRedCols || p >= npiece) return;
+  double v = 0.0;
+  for (int r = piece0[p]; r < piece0[p + 1]; r++) v += part[(size_t)r * kRedCols + c];
+  out[(size_t)p * kRedCols + c] = v;
+}
+
+__global__ void reduce_seg_pieces_kernel(const double *__restrict__ psum,
+                                         const int *__restrict__ seg_piece, int nseg,
+                                         double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int q = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kPerWarp + lane / kRedCols;
+  const int c = lane % kRedCols;
+  if (lane >= kPerWarp * kRedCols || q >= nseg) return;
+  double v = 0.0;
+  for (int p = seg_piece[q]; p < seg_piece[q + 1]; p++) v += psum[(size_t)p * kRedCols + c];
+  out[(size_t)q * kRedCols + c] = v;
+}
+
+int reduce_seg_pieces(const double *part, const int *piece0, int npiece, const int *seg_piece,
+                      int nseg, double *psum, double *out, cudaStream_t s) {
+  if (nseg <= 0) return 0;
+  if (npiece > 0) {
+    const int64_t warps = (npiece + kPerWarp - 1) / kPerWarp;
+    reduce_pieces_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(part, piece0,
+                                                                            npiece, psum);
+    note_launch();
+  }
+  const int64_t warps = (nseg + kPerWarp - 1) / kPerWarp;
+  reduce_seg_pieces_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+      psum, seg_piece, nseg, out);
+  note_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 int reduce_segments(const double *part, const int *seg, int nseg, double *out, cudaStream_t s) {
   if (nseg <= 0) return 0;
   reduce_segments_kernel<<<nseg, 64, 0, s>>>(part, seg, out);
@@ -969,7 +1018,11 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
                          args.ebond, args.wbond, o.f, o.epot_per_at,
                          want_wat ? o.wpot_per_at : nullptr, s));
   if (batch) {
-    GB_CHECK(reduce_segments(args.tile_part, sys.seg, sys.nseg, sys.red_seg, s));
+    if (sys.piece0)
+      GB_CHECK(reduce_seg_pieces(args.tile_part, sys.piece0, sys.npiece, sys.seg_piece, sys.nseg,
+                                 sys.piece_sum, sys.red_seg, s));
+    else
+      GB_CHECK(reduce_segments(args.tile_part, sys.seg, sys.nseg, sys.red_seg, s));
     GB_CUDA(cudaMemsetAsync(o.red, 0, sizeof(double) * 10, s));
   } else {
     GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(rows) + 64));

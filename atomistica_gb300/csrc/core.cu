@@ -8,8 +8,9 @@
 //   K1c nl_scatter        atoms into their cell slots (atomic slot claim).
 //   K1d nl_sort_cells     per-cell sort by atom id, so that every cell lists its
 //                         atoms in increasing id as the reference's linked
-//                         list does (binning_update, :904-959).
-//   K1e nl_gather_sorted  float positions (+ id, wrap) in cell-sorted order.
+//                         list does (binning_update, :904-959), written as
+//                         float positions (+ id, wrap) in cell-sorted order
+//                         (nl_sort_big_cells: the same for crowded cells).
 //   K2  nl_pairs<count>   per atom (cell-sorted thread order): stencil loop in
 //                         the reference order; each candidate is decided by an
 //                         FP32 test with a rigorous error bound, and only the
@@ -18,7 +19,9 @@
 //                         contraction, reference order, :708-711), so the
 //                         decision always equals the reference's -> counts.
 //   K2b exclusive scan    CSR offsets.
-//   K2c nl_pairs<fill>    same loop, writes j and the packed image shift.
+//   K2c nl_pairs<fill>    same loop, writes j and the packed image shift
+//                         (steady state: one pass that also stages the
+//                         entries, then nl_compact / nl_compact_reverse).
 // The resulting per-atom entry order equals the reference's (stencil offset
 // x-major/z-minor, then atom id), so pair sets and per-bond indices match.
 
@@ -317,6 +320,17 @@ __device__ __forceinline__ int floor_div(int a, int n) {
 // FP32 and FP64 roundings) of the FP64 value, so floor(s_f -/+ e) agreeing
 // decides the cell; otherwise (an atom within ~1e-5 cells of a boundary) the
 // FP64 evaluation does.
+// (a call, not inlined: kept out of line so that the rare FP64 evaluation is
+// not executed under predicates for every atom)
+__device__ __noinline__ int raw_cell_fp64(const double *rec_row, double x, double y, double z) {
+  double sd = __dmul_rn(rec_row[0], x);
+  sd = __dadd_rn(sd, __dmul_rn(rec_row[1], y));
+  sd = __dadd_rn(sd, __dmul_rn(rec_row[2], z));
+  double f = floor(sd);
+  f = fmin(fmax(f, -1.0e9), 1.0e9);
+  return (int)f;
+}
+
 __device__ __forceinline__ void raw_cell(const BinParams &bp, double x, double y, double z,
                                          float xf, float yf, float zf, int c[3]) {
 #pragma unroll
@@ -326,16 +340,10 @@ __device__ __forceinline__ void raw_cell(const BinParams &bp, double x, double y
     const float sf = __fadd_rn(__fadd_rn(p0, p1), p2);
     const float e = 4.8e-7f * (fabsf(p0) + fabsf(p1) + fabsf(p2)) + 1.0e-37f;
     const float fl = floorf(sf - e);
-    if (fl == floorf(sf + e) && fabsf(fl) < 1.0e9f) {
+    if (fl == floorf(sf + e) && fabsf(fl) < 1.0e9f)
       c[k] = (int)fl;
-    } else {
-      double sd = __dmul_rn(bp.rec[k][0], x);
-      sd = __dadd_rn(sd, __dmul_rn(bp.rec[k][1], y));
-      sd = __dadd_rn(sd, __dmul_rn(bp.rec[k][2], z));
-      double f = floor(sd);
-      f = fmin(fmax(f, -1.0e9), 1.0e9);
-      c[k] = (int)f;
-    }
+    else
+      c[k] = raw_cell_fp64(bp.rec[k], x, y, z);
   }
 }
 
@@ -435,14 +443,29 @@ __global__ void nl_scatter(int nat, const int *__restrict__ atom_cell,
 // rank-by-count pass (one block per cell) for the rare crowded cell.
 constexpr int kSmallCell = 48;
 
+// The sorted slot t of atom i: float copy of its position with the atom id
+// in .w and its wrap counts, so that the candidate loop reads one 16-byte
+// record per candidate.
+__device__ __forceinline__ void put_sorted(int t, int i, const Pos4 *__restrict__ pos4,
+                                           const int *__restrict__ atom_wrap,
+                                           float4 *__restrict__ spos, int *__restrict__ swrap) {
+  const Pos4 p = pos4[i];
+  spos[t] = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(i));
+  swrap[t] = atom_wrap[i];
+}
+
+// Per cell (a thread each): the cell's atoms sorted by id (insertion sort),
+// written to their sorted slots; crowded cells are left to nl_sort_big_cells.
 __global__ void nl_sort_cells(int ncells, const int *__restrict__ cell_start,
-                              int *__restrict__ cell_atoms, int *__restrict__ big_cells,
-                              int *__restrict__ n_big) {
+                              const int *__restrict__ cell_atoms, int *__restrict__ big_cells,
+                              int *__restrict__ n_big, const Pos4 *__restrict__ pos4,
+                              const int *__restrict__ atom_wrap, float4 *__restrict__ spos,
+                              int *__restrict__ swrap) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   const int s = cell_start[c], e = cell_start[c + 1];
   const int m = e - s;
-  if (m <= 1) return;
+  if (m == 0) return;
   if (m > kSmallCell) {
     big_cells[atomicAdd(n_big, 1)] = c;
     return;
@@ -458,45 +481,31 @@ __global__ void nl_sort_cells(int ncells, const int *__restrict__ cell_start,
     }
     v[p + 1] = key;
   }
-  for (int q = 0; q < m; q++) cell_atoms[s + q] = v[q];
+  for (int q = 0; q < m; q++) put_sorted(s + q, v[q], pos4, atom_wrap, spos, swrap);
 }
 
+// Crowded cells (rare), a block each: rank by count into tmp, then the
+// sorted slots from tmp (one block per cell, so a barrier orders the two).
 __global__ void nl_sort_big_cells(const int *__restrict__ big_cells, const int *__restrict__ n_big,
-                                  const int *__restrict__ cell_start, const int *__restrict__ src,
-                                  int *__restrict__ dst) {
-  for (int bc = blockIdx.x; bc < *n_big; bc += gridDim.x) {
+                                  const int *__restrict__ cell_start,
+                                  const int *__restrict__ cell_atoms, int *__restrict__ tmp,
+                                  const Pos4 *__restrict__ pos4,
+                                  const int *__restrict__ atom_wrap, float4 *__restrict__ spos,
+                                  int *__restrict__ swrap) {
+  const int nbig = *n_big;
+  for (int bc = blockIdx.x; bc < nbig; bc += gridDim.x) {
     const int c = big_cells[bc];
     const int s = cell_start[c], e = cell_start[c + 1];
     for (int q = s + threadIdx.x; q < e; q += blockDim.x) {
-      const int me = src[q];
+      const int me = cell_atoms[q];
       int rank = 0;
-      for (int t = s; t < e; t++) rank += src[t] < me;
-      dst[s + rank] = me;
+      for (int t = s; t < e; t++) rank += cell_atoms[t] < me;
+      tmp[s + rank] = me;
     }
+    __syncthreads();
+    for (int q = s + threadIdx.x; q < e; q += blockDim.x)
+      put_sorted(q, tmp[q], pos4, atom_wrap, spos, swrap);
   }
-}
-
-__global__ void nl_copy_big_cells(const int *__restrict__ big_cells, const int *__restrict__ n_big,
-                                  const int *__restrict__ cell_start, const int *__restrict__ src,
-                                  int *__restrict__ dst) {
-  for (int bc = blockIdx.x; bc < *n_big; bc += gridDim.x) {
-    const int c = big_cells[bc];
-    for (int q = cell_start[c] + threadIdx.x; q < cell_start[c + 1]; q += blockDim.x)
-      dst[q] = src[q];
-  }
-}
-
-// Per sorted slot: float copy of the position with the atom id in .w and the
-// atom's wrap counts, so that the candidate loop reads one 16-byte record.
-__global__ void nl_gather_sorted(int nat, const int *__restrict__ cell_atoms,
-                                 const Pos4 *__restrict__ pos4, const int *__restrict__ atom_wrap,
-                                 float4 *__restrict__ spos, int *__restrict__ swrap) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nat) return;
-  const int i = cell_atoms[t];
-  const Pos4 p = pos4[i];
-  spos[t] = make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(i));
-  swrap[t] = atom_wrap[i];
 }
 
 // Exact reference test |r_i - r_j + A s|^2 < cutoff^2: FP64, no FMA
@@ -981,19 +990,13 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
     nl_scatter<<<nb, T, 0, stream>>>(nat, nl.atom_cell.as<int>(), nl.cell_start.as<int>(),
                                      nl.cell_count.as<int>(), cell_atoms);
     note_launch();
-    nl_sort_cells<<<(ncells + T - 1) / T, T, 0, stream>>>(ncells, nl.cell_start.as<int>(),
-                                                         cell_atoms, big_cells, &status[2]);
+    nl_sort_cells<<<(ncells + T - 1) / T, T, 0, stream>>>(
+        ncells, nl.cell_start.as<int>(), cell_atoms, big_cells, &status[2], nl.pos4.as<Pos4>(),
+        nl.atom_wrap.as<int>(), nl.spos.as<float4>(), nl.swrap.as<int>());
     note_launch();
-    // Crowded cells (rare): rank-by-count into the second half, copy back.
     nl_sort_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
-        big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms, cell_atoms + nat);
-    note_launch();
-    nl_copy_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
-        big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms + nat, cell_atoms);
-    note_launch();
-    nl_gather_sorted<<<nb, T, 0, stream>>>(nat, cell_atoms, nl.pos4.as<Pos4>(),
-                                           nl.atom_wrap.as<int>(), nl.spos.as<float4>(),
-                                           nl.swrap.as<int>());
+        big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms, cell_atoms + nat,
+        nl.pos4.as<Pos4>(), nl.atom_wrap.as<int>(), nl.spos.as<float4>(), nl.swrap.as<int>());
     note_launch();
     // Single pass (count + staged entries) once a previous build has sized
     // the per-atom capacity; count-only pass otherwise.
@@ -1012,7 +1015,15 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
     // No host decisions: compact the staged entries (at most cap per atom, so
     // at most nat * cap in all; the buffers were sized for that) and leave
     // the status words in hstats for the caller to check after the replay.
-    if (nat > 0) {
+    if (nat > 0 && nl.want_rev && nl.stage_cap <= 32) {
+      // (rev sized for nat * cap entries by the caller, like nbr and shift)
+      nl_compact_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(
+          nat, nl.stage_cap, nl.seed.as<int>(), nl.stage.as<int2>(), nl.nbr.as<int>(),
+          nl.shift.as<int>(), nl.rev.as<int>(), status + 3);
+      note_launch();
+      GB_CUDA(cudaMemcpyAsync(hs + 5, status + 4, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      nl.rev_pending = true;
+    } else if (nat > 0) {
       nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
                                                         nl.stage.as<int2>(), nl.nbr.as<int>(),
                                                         nl.shift.as<int>());
@@ -1063,7 +1074,7 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
   GB_CHECK(nl.shift.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
   const int maxz = hs[0];
   if (nat > 0) {
-    if (nl.stage_cap > 0 && maxz <= nl.stage_cap && nl.want_rev && !batch &&
+    if (nl.stage_cap > 0 && maxz <= nl.stage_cap && nl.want_rev &&
         total <= 24 * (int64_t)nat) {
       // compaction and reverse index together (the symmetry flag is read
       // by the caller's next synchronisation, as after neighbors_build_reverse)

@@ -147,6 +147,8 @@ int reduce_partials(const double *part, int nrows, int nc, double *red, double *
                     cudaStream_t s);
 // Per-segment sums of 10-column rows: out[q][.] = sum of rows [seg[q], seg[q+1]).
 int reduce_segments(const double *part, const int *seg, int nseg, double *out, cudaStream_t s);
+int reduce_seg_pieces(const double *part, const int *piece0, int npiece, const int *seg_piece,
+                      int nseg, double *psum, double *out, cudaStream_t s);
 
 // The system a bond-order evaluation runs on: one structure (cell A), or a
 // batch of structures whose tiles (cut by the caller, at most apt atoms, never
@@ -170,6 +172,14 @@ struct BopSystem {
   const int *seg = nullptr;          // device, tile offsets of the structures (nseg + 1)
   int nseg = 0;
   double *red_seg = nullptr;         // device, nseg x 10
+  // Pieces of the structures' tile rows (at most 32 rows each): piece p is
+  // rows [piece0[p], piece0[p + 1]), structure q has pieces
+  // [seg_piece[q], seg_piece[q + 1]); piece_sum (npiece x 10) is scratch.
+  // nullptr: the structures' rows are summed by one block each.
+  const int *piece0 = nullptr;
+  const int *seg_piece = nullptr;
+  int npiece = 0;
+  double *piece_sum = nullptr;
 };
 int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
             bool want_wat, bool want_pb);
