@@ -92,6 +92,7 @@ SIGNATURES = [
     ("gb_potential_last_timing", _I, [_P, _P]),
     ("gb_potential_last_stats", _I, [_P, _P]),
     ("gb_potential_set_tile_atoms", _I, [_P, _I]),
+    ("gb_potential_set_graph", _I, [_P, _I]),
     ("gb_bop_energy_and_forces_noalloc", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                               _P]),
     ("gb_kernel_launches", ctypes.c_uint64, []),

@@ -524,6 +524,257 @@ int add_into(double *dst, const double *src, size_t n, cudaStream_t s) {
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// CUDA graph of a whole single-structure evaluation (gb_potential_set_graph).
+// After an eager evaluation has sized every buffer, the next evaluation of
+// the same particles, list, cell and force buffer captures the list build
+// (single staged pass, no host decision), the tile kernel with a plan that
+// has head room, the gather, the sums and the copies of the status words and
+// results to pinned memory; later evaluations replay it.  A replay whose
+// list or tile plan overflowed leaves the forces as they were (the gather
+// checks the status words on the device) and is redone eagerly.
+// ---------------------------------------------------------------------------
+void drop_single_graph(Potential &pot) {
+  if (pot.graph_exec) cudaGraphExecDestroy(pot.graph_exec);
+  if (pot.graph) cudaGraphDestroy(pot.graph);
+  pot.graph_exec = nullptr;
+  pot.graph = nullptr;
+  pot.graph_kernels = 0;
+  pot.graph_bufs.clear();
+}
+
+// Device (and pinned) buffers whose addresses a captured evaluation holds.
+std::vector<const void *> single_graph_buffers(const Potential &pot, const Particles &p,
+                                               const Neighbors &nl) {
+  return {p.r.p,          pot.el.p,       nl.pos4.p,      nl.posff.p,    nl.atom_cell.p,
+          nl.atom_wrap.p, nl.cell_count.p, nl.cell_start.p, nl.cell_atoms.p, nl.counts.p,
+          nl.spos.p,      nl.swrap.p,     nl.seed.p,      nl.nbr.p,      nl.shift.p,
+          nl.rev.p,       nl.stage.p,     nl.scan_tmp.p,  nl.stats.p,    nl.hstats.p,
+          pot.bond_G.p,   pot.bond_e.p,   pot.tile_part.p, pot.red.p,    pot.hred.p,
+          pot.red_stage.p, pot.out_f.p};
+}
+
+bool single_graph_current(const Potential &pot, const Particles &p, const Neighbors &nl,
+                          const double *fd, bool set_f, cudaStream_t s) {
+  return pot.graph_exec && pot.graph_p == &p && pot.graph_nl == &nl && pot.graph_nat == p.nat &&
+         pot.graph_cell_rev == p.cell_rev && pot.graph_fd == fd && pot.graph_set_f == set_f &&
+         pot.graph_prec == pot.precision && pot.graph_stream == s &&
+         pot.graph_tile_request == pot.tile_request &&
+         pot.graph_cutoff == nl.interaction_range && pot.el_for == &p &&
+         pot.graph_bufs == single_graph_buffers(pot, p, nl);
+}
+
+// Captures the evaluation into pot.graph (nothing runs).  fd: the device
+// force array the graph accumulates into (zeroed first when set_f).
+void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, bool set_f,
+                    cudaStream_t s) {
+  drop_single_graph(pot);
+  const int nat = p.nat;
+  const int cap = nl.stage_cap;
+  const int nbt0 = pot.last_plan[0], ntrip0 = pot.last_plan[1];
+  if (cap <= 0 || nat <= 0 || !nl.valid || nl.built_for != &p || nbt0 <= 0 || !nl.want_rev)
+    return;
+  const int64_t capacity = (int64_t)nat * cap;
+  if (capacity > (int64_t)INT_MAX / 3) return;
+  const bool mixed = pot.precision == GB_PRECISION_MIXED;
+  const int apt = pot.tile_atoms;
+  const int ntiles = (nat + apt - 1) / apt;
+  // Tile plan with head room for the next configurations (checked per tile
+  // by the kernel): as much as fits without fewer resident CTAs per SM than
+  // the exact plan of this evaluation, at most +25 % bonds / +50 % slots.
+  const int occ0 = bop_tile_ctas_per_sm(pot, bop_tile_smem(mixed, nbt0, ntrip0));
+  int max_nbt = nbt0, max_ntrip = ntrip0;
+  for (int step = 16; step >= 1; step--) {
+    const int nb = std::min(apt * cap, nbt0 + nbt0 * step / 64 + step);
+    const int nt = std::min(apt * trip_slots(cap), ntrip0 + ntrip0 * step / 32 + 4 * step);
+    const size_t sm = bop_tile_smem(mixed, nb, nt);
+    if (sm <= bop_tile_smem_budget() && bop_tile_ctas_per_sm(pot, sm) >= occ0) {
+      max_nbt = nb;
+      max_ntrip = nt;
+      break;
+    }
+  }
+  // every buffer at its captured size now: nothing may be allocated inside
+  if (nl.nbr.ensure(sizeof(int) * capacity) || nl.shift.ensure(sizeof(int) * capacity) ||
+      nl.rev.ensure(sizeof(int) * capacity) || nl.stage.ensure(sizeof(int2) * capacity) ||
+      pot.bond_G.ensure(sizeof(double) * 3 * capacity) ||
+      pot.bond_e.ensure(sizeof(double) * capacity) ||
+      pot.tile_part.ensure(sizeof(double) * 10 * (size_t)ntiles + 64) ||
+      pot.red_stage.ensure(reduce_stage_bytes(ntiles) + 64) || pot.red.ensure(sizeof(double) * 16) ||
+      pot.hred.ensure(sizeof(double) * 16)) {
+    clear_error();
+    return;
+  }
+  BinParams bp;
+  if (bin_params(p.A, p.B, p.pbc, nl.interaction_range, 0, bp)) {
+    clear_error();
+    return;
+  }
+  const int ncells = bp.n[0] * bp.n[1] * bp.n[2];
+  Outputs o;
+  o.f = fd;
+  o.red = pot.red.as<double>();
+  o.status = reinterpret_cast<int *>(o.red + 12);
+  BopSystem sys;
+  sys.nat = nat;
+  std::memcpy(sys.A, p.A, sizeof(sys.A));
+  sys.capture = true;
+  sys.nb_capacity = capacity;
+  sys.max_nbt = max_nbt;
+  sys.max_ntrip = max_ntrip;
+  sys.check.nl = nl.stats.as<int>();
+  sys.check.tile = o.status;
+  sys.check.cap = cap;
+  // capturing runs nothing: the eager evaluation's list state stays valid
+  const bool rev_valid0 = nl.rev_valid, posff_valid0 = nl.posff_valid;
+  const bool plan_ready0 = nl.plan_ready;
+  const int plan0[2] = {pot.last_plan[0], pot.last_plan[1]};
+  const int tile_atoms0 = pot.tile_atoms;
+  nl.rev_valid = false;
+  nl.rev_pending = false;
+  const uint64_t launches0 = gb_kernel_launches();
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    pot.graph_failed = true;
+    return;
+  }
+  int rc = 0;
+  if (set_f && cudaMemsetAsync(fd, 0, sizeof(double) * 3 * (size_t)nat, s) != cudaSuccess)
+    rc = -1;
+  if (rc == 0 && cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s) != cudaSuccess) rc = -1;
+  if (rc == 0) rc = nl_build(nl, nat, p.r.as<double>(), bp, nullptr, nullptr, ncells, s, true);
+  if (rc == 0) rc = bop_run(pot, sys, nl, o, false, false);
+  if (rc == 0 && cudaMemcpyAsync(pot.hred.p, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost,
+                                 s) != cudaSuccess)
+    rc = -1;
+  const cudaError_t ce = cudaStreamEndCapture(s, &g);
+  note_launch(-(int)(gb_kernel_launches() - launches0));  // captured, not run
+  nl.rev_valid = rev_valid0;
+  nl.rev_pending = false;
+  nl.posff_valid = posff_valid0;
+  nl.plan_ready = plan_ready0;
+  pot.last_plan[0] = plan0[0];
+  pot.last_plan[1] = plan0[1];
+  pot.tile_atoms = tile_atoms0;
+  cudaGraphExec_t x = nullptr;
+  if (rc != 0 || ce != cudaSuccess || !g || cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    clear_error();
+    pot.graph_failed = true;
+    return;
+  }
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+  int kernels = 0;
+  for (size_t k = 0; k < nn; k++) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+      kernels++;
+  }
+  pot.graph = g;
+  pot.graph_exec = x;
+  pot.graph_kernels = kernels;
+  pot.graph_cap = cap;
+  pot.graph_p = &p;
+  pot.graph_nl = &nl;
+  pot.graph_nat = nat;
+  pot.graph_cell_rev = p.cell_rev;
+  pot.graph_cutoff = nl.interaction_range;
+  pot.graph_fd = fd;
+  pot.graph_set_f = set_f;
+  pot.graph_prec = pot.precision;
+  pot.graph_stream = s;
+  pot.graph_tile_request = pot.tile_request;
+  pot.graph_bufs = single_graph_buffers(pot, p, nl);
+}
+
+// Energy (set) and virial (accumulated) from the pinned result row hr, after
+// the checks of the force kernels' status word.
+int finish_results(Potential &pot, const double *hr, double *epot, double *wpot) {
+  const int st = reinterpret_cast<const int *>(hr + 12)[0];
+  pot.last_status = st;
+  pot.last_hot = reinterpret_cast<const int *>(hr + 12)[2];
+  if (st & 1) {
+    set_error("Spline argument outside of the defined interval (EAM density table).");
+    return GB_ERROR_DOMAIN;
+  }
+  if (st & 2) {
+    set_error("Internal error: bond-order tile plan mismatch.");
+    return GB_ERROR_UNSPECIFIED;
+  }
+  if (st & 4) {
+    set_error("Internal neighbor list exhausted: an atom has more bonds after screening than "
+              "the screened kernel supports (32).");
+    return GB_ERROR_CAPACITY;
+  }
+  // epot is set; wpot accumulated (gen_factory.py:283, potential.c:468-479).
+  if (is_device_ptr(epot)) {
+    GB_CUDA(cudaMemcpy(epot, hr, sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    *epot = hr[0];
+  }
+  if (is_device_ptr(wpot)) {
+    double w[9];
+    GB_CUDA(cudaMemcpy(w, wpot, sizeof(w), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < 9; q++) w[q] += hr[1 + q];
+    GB_CUDA(cudaMemcpy(wpot, w, sizeof(w), cudaMemcpyHostToDevice));
+  } else {
+    for (int q = 0; q < 9; q++) wpot[q] += hr[1 + q];
+  }
+  return 0;
+}
+
+// Replays the captured evaluation; done = false when its list or tile plan
+// overflowed (the forces are then as before the call, or zero with set_f).
+int single_replay(Potential &pot, Particles &p, Neighbors &nl, double *f, double *fd,
+                  bool f_host, bool set_f, double *epot, double *wpot, cudaStream_t s,
+                  bool &done) {
+  done = false;
+  const size_t nf = 3 * (size_t)p.nat;
+  GB_CUDA(cudaEventRecord(pot.ev[0], s));
+  if (f_host && !set_f)
+    GB_CUDA(cudaMemcpyAsync(fd, f, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
+  GB_CUDA(cudaGraphLaunch(pot.graph_exec, s));
+  if (f_host) GB_CUDA(cudaMemcpyAsync(f, fd, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaEventRecord(pot.ev[3], s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  note_launch(pot.graph_kernels);
+  const int *hs = nl.hstats.as<int>();
+  const double *hr = pot.hred.as<double>();
+  const int *st = reinterpret_cast<const int *>(hr + 12);
+  if (!(hs[0] <= pot.graph_cap && (hs[1] & (1 | 2 | 8)) == 0 && (hs[5] & 4) == 0 &&
+        (st[0] & 2) == 0)) {
+    drop_single_graph(pot);
+    nl.valid = false;
+    return 0;
+  }
+  nl.nentries = hs[4];
+  nl.maxz = hs[0];
+  nl.valid = true;
+  nl.built_for = &p;
+  nl.built_pos_rev = p.pos_rev;
+  nl.built_cell_rev = p.cell_rev;
+  nl.built_nat = p.nat;
+  nl.cutoff = nl.interaction_range;
+  nl.rev_valid = true;
+  nl.rev_pending = false;
+  nl.posff_valid = nl.want_posff;
+  nl.plan_ready = false;
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, pot.ev[0], pot.ev[3]);
+  cudaGetLastError();
+  pot.timing[0] = pot.timing[1] = pot.timing[3] = 0.0;
+  pot.timing[2] = ms;
+  pot.last_bonds = nl.nentries;
+  GB_CHECK(finish_results(pot, hr, epot, wpot));
+  done = true;
+  return 0;
+}
+
 int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot, double *f,
                       double *wpot, const int *mask, double *epa, double *epb, double *fpb,
                       double *wpa, double *wpb, int flags = 0) {
@@ -558,6 +809,25 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CUDA(cudaEventRecord(pot.ev[0], s));
   GB_CHECK(update_element_map(pot, p));
   const int nat = p.nat;
+  // CUDA-graph replay of a whole evaluation (outputs: energy, forces, virial)
+  pot.last_replayed = false;
+  const bool graph_ok = pot.use_graph && !pot.graph_failed && pot.kind != kEAM &&
+                        !pot.screened && nat > 0 && !mask && !epa && !wpa && !epb && !fpb &&
+                        !wpb;
+  double *gfd = nullptr;
+  if (graph_ok) {
+    const bool fh = !is_device_ptr(f);
+    if (fh) GB_CHECK(pot.out_f.ensure(sizeof(double) * 3 * std::max<size_t>(nat, 1)));
+    gfd = fh ? pot.out_f.as<double>() : f;
+    if (single_graph_current(pot, p, nl, gfd, set_f, s)) {
+      bool done = false;
+      GB_CHECK(single_replay(pot, p, nl, f, gfd, fh, set_f, epot, wpot, s, done));
+      if (done) {
+        pot.last_replayed = true;
+        return 0;
+      }
+    }
+  }
   // Host forces (accumulated into): their upload runs on a second stream
   // while the neighbour list is built.
   Stage sf, sepa, swpa, sepb, sfpb, swpb;
@@ -663,37 +933,10 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   if (nat > 0) cudaEventElapsedTime(&ms[3], pot.kev[0], pot.kev[1]);
   cudaGetLastError();
   for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
-  const int st = reinterpret_cast<const int *>(hr + 12)[0];
-  pot.last_status = st;
-  pot.last_hot = reinterpret_cast<const int *>(hr + 12)[2];
   pot.last_bonds = pot.kind == kEAM ? 0 : nl.nentries;
-  if (st & 1) {
-    set_error("Spline argument outside of the defined interval (EAM density table).");
-    return GB_ERROR_DOMAIN;
-  }
-  if (st & 2) {
-    set_error("Internal error: bond-order tile plan mismatch.");
-    return GB_ERROR_UNSPECIFIED;
-  }
-  if (st & 4) {
-    set_error("Internal neighbor list exhausted: an atom has more bonds after screening than "
-              "the screened kernel supports (32).");
-    return GB_ERROR_CAPACITY;
-  }
-  // epot is set; wpot accumulated (gen_factory.py:283, potential.c:468-479).
-  if (is_device_ptr(epot)) {
-    GB_CUDA(cudaMemcpy(epot, hr, sizeof(double), cudaMemcpyHostToDevice));
-  } else {
-    *epot = hr[0];
-  }
-  if (is_device_ptr(wpot)) {
-    double w[9];
-    GB_CUDA(cudaMemcpy(w, wpot, sizeof(w), cudaMemcpyDeviceToHost));
-    for (int q = 0; q < 9; q++) w[q] += hr[1 + q];
-    GB_CUDA(cudaMemcpy(wpot, w, sizeof(w), cudaMemcpyHostToDevice));
-  } else {
-    for (int q = 0; q < 9; q++) wpot[q] += hr[1 + q];
-  }
+  GB_CHECK(finish_results(pot, hr, epot, wpot));
+  if (graph_ok && !single_graph_current(pot, p, nl, gfd, set_f, s))
+    single_capture(pot, p, nl, gfd, set_f, s);
   return 0;
 }
 
@@ -1097,6 +1340,7 @@ int gb_tabulated_alloy_eam_new(gb_potential_t **h, const char *fn) {
 void gb_potential_free(gb_potential_t *h) {
   if (!h) return;
   Potential &pot = h->pot;
+  drop_single_graph(pot);
   for (int q = 0; q < 4; q++)
     if (pot.ev[q]) cudaEventDestroy(pot.ev[q]);
   for (int q = 0; q < 2; q++)
@@ -1343,6 +1587,14 @@ int gb_potential_last_timing(const gb_potential_t *h, double *ms) {
   return 0;
 }
 
+int gb_potential_set_graph(gb_potential_t *h, int on) {
+  if (!h) return GB_ERROR_ARGUMENT;
+  h->pot.use_graph = on != 0;
+  h->pot.graph_failed = false;
+  if (!on) drop_single_graph(h->pot);
+  return 0;
+}
+
 int gb_potential_set_tile_atoms(gb_potential_t *h, int atoms) {
   if (!h || atoms < 0) return GB_ERROR_ARGUMENT;
   h->pot.tile_request = atoms;
@@ -1354,7 +1606,7 @@ int gb_potential_last_stats(const gb_potential_t *h, int64_t *stats) {
   stats[0] = h->pot.last_bonds;
   stats[1] = h->pot.last_hot;
   stats[2] = h->pot.tile_atoms;
-  stats[3] = 0;
+  stats[3] = h->pot.last_replayed ? 1 : 0;
   return 0;
 }
 

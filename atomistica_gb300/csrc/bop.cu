@@ -492,9 +492,9 @@ template <bool kEpa, bool kWat>
 __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__restrict__ rev,
                            const double *__restrict__ G, const double *__restrict__ ebond,
                            const double *__restrict__ wbond, double *__restrict__ f,
-                           double *__restrict__ epa, double *__restrict__ wpa) {
+                           double *__restrict__ epa, double *__restrict__ wpa, ReplayCheck chk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nat) return;
+  if (i >= nat || replay_invalid(chk)) return;
   double F[3] = {0.0, 0.0, 0.0};
   double E = 0.0;
   double W[9];
@@ -670,21 +670,23 @@ int dispatch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int 
 }
 
 // Per-atom gather of the bond forces (FP64 G, or ff G for the mixed form).
+// chk: a captured evaluation's gather leaves the outputs as they are when
+// the replayed list or tile plan overflowed (ReplayCheck, internal.h).
 int launch_gather(bool mixed, int nat, const int *seed, const int *rev, const double *G,
                   const double *ebond, const double *wbond, double *f, double *epa, double *wpa,
-                  cudaStream_t s) {
+                  cudaStream_t s, ReplayCheck chk = ReplayCheck{}) {
   const int T = 128, nb = (nat + T - 1) / T;
   const float2 *Gf = reinterpret_cast<const float2 *>(G);
   if (mixed) {
-    if (epa && wpa) bop_gather_mx<true, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
-    else if (epa) bop_gather_mx<true, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
-    else if (wpa) bop_gather_mx<false, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
-    else bop_gather_mx<false, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa);
+    if (epa && wpa) bop_gather_mx<true, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
+    else if (epa) bop_gather_mx<true, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
+    else if (wpa) bop_gather_mx<false, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
+    else bop_gather_mx<false, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
   } else {
-    if (epa && wpa) bop_gather<true, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
-    else if (epa) bop_gather<true, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
-    else if (wpa) bop_gather<false, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
-    else bop_gather<false, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa);
+    if (epa && wpa) bop_gather<true, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
+    else if (epa) bop_gather<true, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
+    else if (wpa) bop_gather<false, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
+    else bop_gather<false, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
   }
   note_launch();
   GB_CUDA(cudaGetLastError());
@@ -1016,7 +1018,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                          args.ebond, args.wbond, o.f, o.epot_per_at,
-                         want_wat ? o.wpot_per_at : nullptr, s));
+                         want_wat ? o.wpot_per_at : nullptr, s, sys.check));
   if (batch) {
     if (sys.piece0)
       GB_CHECK(reduce_seg_pieces(args.tile_part, sys.piece0, sys.npiece, sys.seg_piece, sys.nseg,

@@ -995,9 +995,10 @@ template <bool kEpa, bool kWat>
 __global__ void bop_gather_mx(int nat, const int *__restrict__ seed, const int *__restrict__ rev,
                               const float2 *__restrict__ G, const double *__restrict__ ebond,
                               const double *__restrict__ wbond, double *__restrict__ f,
-                              double *__restrict__ epa, double *__restrict__ wpa) {
+                              double *__restrict__ epa, double *__restrict__ wpa,
+                              ReplayCheck chk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nat) return;
+  if (i >= nat || replay_invalid(chk)) return;
   ff F[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
   double E = 0.0;
   double W[9];

@@ -99,6 +99,21 @@ __host__ __device__ inline void unpack_shift(int32_t p, int &s0, int &s1, int &s
 }
 constexpr int kMaxShift = 511;
 
+// Validity of a replayed (CUDA-graph) evaluation, read on the device by the
+// kernels that write the caller's outputs: nl = the list build's status words
+// (nl[0] largest coordination, nl[1] flags, nl[4] reverse-index flags), tile
+// = the force kernels' status word, cap = the captured per-atom capacity.
+// nl == nullptr: no check.
+struct ReplayCheck {
+  const int *nl = nullptr;
+  const int *tile = nullptr;
+  int cap = 0;
+};
+__device__ __forceinline__ bool replay_invalid(const ReplayCheck &c) {
+  return c.nl && !(c.nl[0] <= c.cap && (c.nl[1] & (1 | 2 | 8)) == 0 && (c.nl[4] & 4) == 0 &&
+                   (c.tile[0] & 2) == 0);
+}
+
 // (ij, ik) slots of an atom with z bonds in the bond-order tile kernels: its
 // z x z block, one slot longer for even z > 0, so that consecutive atoms'
 // blocks start an odd number of slots apart and the rows that a warp's

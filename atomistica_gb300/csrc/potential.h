@@ -113,6 +113,24 @@ struct Potential {
   int last_hot = 0;         // bonds recomputed on the accurate path (mixed form)
   int64_t last_bonds = 0;   // directed bonds of the last bond-order call
   int last_plan[2] = {0, 0};  // largest bonds / (ij, ik) slots per tile of the last call
+
+  // CUDA graph of a whole single-structure evaluation (gb_potential_set_graph):
+  // list build, tile kernel, gather, sums and the status / result copies,
+  // captured after an eager evaluation and replayed while the particles,
+  // list, cell, force buffer and every device buffer are unchanged.
+  bool use_graph = false;
+  bool graph_failed = false;  // capture not possible: stay eager
+  bool last_replayed = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_kernels = 0, graph_cap = 0, graph_nat = 0, graph_prec = 0, graph_tile_request = 0;
+  bool graph_set_f = false;
+  const void *graph_p = nullptr, *graph_nl = nullptr;
+  uint64_t graph_cell_rev = 0;
+  double graph_cutoff = 0.0;
+  double *graph_fd = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  std::vector<const void *> graph_bufs;
 };
 
 // Interaction range requested by bind_to for element pair t (database
@@ -180,6 +198,8 @@ struct BopSystem {
   const int *seg_piece = nullptr;
   int npiece = 0;
   double *piece_sum = nullptr;
+  // A captured evaluation's gathers check the replay's validity.
+  ReplayCheck check;
 };
 int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &o,
             bool want_wat, bool want_pb);

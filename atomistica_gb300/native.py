@@ -365,12 +365,24 @@ class _Potential:
         """Atoms per bond-order tile (power of two <= 64; 0: automatic)."""
         check(self._L.gb_potential_set_tile_atoms(self._h, int(atoms)), "set_tile_atoms")
 
+    def set_graph(self, on=True):
+        """CUDA-graph replay of whole evaluations (gb_potential_set_graph):
+        after an eager call, calls with only energy, forces and virial on
+        the same particles, list, cell and force array replay one graph."""
+        check(self._L.gb_potential_set_graph(self._h, 1 if on else 0), "set_graph")
+
     def last_stats(self):
         """(directed bonds, bonds recomputed on the accurate path of the mixed
         form, atoms per tile) of the last call."""
         v = (ctypes.c_int64 * 4)()
         self._L.gb_potential_last_stats(self._h, v)
         return tuple(v[:3])
+
+    def last_replayed(self):
+        """True when the last call was a CUDA-graph replay."""
+        v = (ctypes.c_int64 * 4)()
+        self._L.gb_potential_last_stats(self._h, v)
+        return bool(v[3])
 
     def energy_and_forces(self, particles, neighbors, forces=None, mask=None, charges=None,
                           epot_per_at=None, epot_per_bond=None, f_per_bond=None,

@@ -295,17 +295,23 @@ def other_configs(dev, oracle):
     d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
     d_f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
     entry = {"natoms": len(s), "unit": UNIT, "cpu_oracle": len(s) / t_cpu, "cpu_cores": nth}
-    for prec in ("fp64", "mixed"):
-        pot = native.Tersoff(precision=prec)
-        pot.bind_to(p, nl)
-        ms = _gpu_step_ms(pot, p, nl, d_pos, d_f)
+    for name in ("fp64", "mixed", "fp64_graph", "mixed_graph"):
+        # (*_graph: CUDA-graph replay of whole evaluations, own particles/list)
+        pq, nq = (native.from_atoms(s), native.Neighbors(100)) if "graph" in name else (p, nl)
+        pot = native.Tersoff(precision=name.split("_")[0])
+        pot.bind_to(pq, nq)
+        if "graph" in name:
+            pot.set_graph(True)
+        ms = _gpu_step_ms(pot, pq, nq, d_pos, d_f)
         d_f.zero_()
-        p.set_positions(d_pos)
-        e, _, w = pot.energy_and_forces(p, nl, forces=d_f)
+        pq.set_positions(d_pos)
+        e, _, w = pot.energy_and_forces(pq, nq, forces=d_f)
         f = d_f.cpu().numpy()
-        entry[prec] = {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
+        entry[name] = {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
                        "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                        "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}
+        if "graph" in name:
+            entry[name]["replayed"] = pot.last_replayed()
     out["tersoff_si_4096"] = entry
     out["tersoff_scr"] = screened_config(dev, oracle, nth, cpu_time)
     out["md_si_4096"] = md_config()
@@ -708,16 +714,27 @@ def run_ours(args):
         pot.set_stream(stream.cuda_stream)
         pot.bind_to(p, nl)
         pots[prec] = pot
+    # the mixed form with CUDA-graph replay of whole evaluations
+    # (gb_potential_set_graph), on its own particles and list
+    pg = native.from_atoms(s)
+    pg.set_stream(stream.cuda_stream)
+    nlg = native.Neighbors(100)
+    pots["mixed_graph"] = native.Tersoff(precision="mixed")
+    pots["mixed_graph"].set_stream(stream.cuda_stream)
+    pots["mixed_graph"].bind_to(pg, nlg)
+    pots["mixed_graph"].set_graph(True)
+    where = {"mixed": (p, nl), "fp64": (p, nl), "mixed_graph": (pg, nlg)}
 
     d_pos = torch.tensor(s.positions, dtype=torch.float64, device=dev)
     d_f = torch.zeros((nat, 3), dtype=torch.float64, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
 
     def step(pot):
+        pp, nn = next(where[k] for k, v in pots.items() if v is pot)
         with torch.cuda.stream(stream):
             d_f.zero_()
-        p.set_positions(d_pos)   # marks positions changed -> full neighbour rebuild
-        return pot.energy_and_forces(p, nl, forces=d_f)
+        pp.set_positions(d_pos)   # marks positions changed -> full neighbour rebuild
+        return pot.energy_and_forces(pp, nn, forces=d_f)
 
     def timed(pot, k, sampler=None):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -729,6 +746,7 @@ def run_ours(args):
         n0 = L.gb_kernel_launches()
         if sampler:
             sampler.start()
+        replayed = 0
         for q in range(k):
             with torch.cuda.stream(stream):
                 flush.zero_()
@@ -737,6 +755,8 @@ def run_ours(args):
             with torch.cuda.stream(stream):
                 ev[q][1].record(stream)
             parts.append(pot.last_timing())
+            replayed += pot.last_replayed()
+        timed.replayed = replayed
         torch.cuda.synchronize()
         clocks = sampler.stop() if sampler else None
         launches = L.gb_kernel_launches() - n0
@@ -745,20 +765,24 @@ def run_ours(args):
         ms = [a.elapsed_time(b) for a, b in ev]
         return ms, parts, launches, clocks
 
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "mixed", "mixed_graph"):
         for _ in range(max(args.warmup, 3)):
             step(pots[prec])
     torch.cuda.synchronize()
 
     ms64, parts64, _, _ = timed(pots["fp64"], args.steps)
+    msmx, partsmx, launches_mx, _ = timed(pots["mixed"], args.steps)
     sampler = clock_sampler(torch.cuda.current_device())
-    msmx, partsmx, launches, clocks = timed(pots["mixed"], args.steps, sampler)
+    msg, _, launches, clocks = timed(pots["mixed_graph"], args.steps, sampler)
+    replayed_g = timed.replayed
 
     from atomistica_gb300.distributed import max_over_ranks as tmax
 
     t_mx = tmax(sum(msmx) / 1e3)
     t_64 = tmax(sum(ms64) / 1e3)
-    value = ws * nat * args.steps / t_mx
+    t_g = tmax(sum(msg) / 1e3)
+    value = ws * nat * args.steps / t_g
+    value_mx = ws * nat * args.steps / t_mx
     value64 = ws * nat * args.steps / t_64
     nl_mx = statistics.mean(q[0] for q in partsmx)
     kern_mx = statistics.mean(q[3] for q in partsmx)
@@ -767,9 +791,12 @@ def run_ours(args):
 
     # Accuracy of both forms at the workload against each other and the oracle.
     res = {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "mixed", "mixed_graph"):
         e, f, w = step(pots[prec])
         res[prec] = (e, f.cpu().numpy().copy(), np.array(w))
+    graph_equal = (res["mixed_graph"][0] == res["mixed"][0]
+                   and np.array_equal(res["mixed_graph"][1], res["mixed"][1])
+                   and np.array_equal(res["mixed_graph"][2], res["mixed"][2]))
     hot = pots["mixed"].last_stats()
     seed_np, _, _ = nl.get_list(p)
     fm = flop_model(np.diff(seed_np))
@@ -796,17 +823,27 @@ def run_ours(args):
     pos_h = torch.empty((nat, 3), dtype=torch.float64).pin_memory()
     pos_h.copy_(torch.from_numpy(s.positions))
     f_h = torch.zeros((nat, 3), dtype=torch.float64).pin_memory()
+    pot, (p, nl) = pots["mixed"], where["mixed"]
+    e2e_mx_value, e2e_mx_ms = e2e_rate(pos_h.numpy(), f_h.numpy())
+    pot, (p, nl) = pots["mixed_graph"], where["mixed_graph"]
     e2e_value, e2e_ms = e2e_rate(pos_h.numpy(), f_h.numpy())
+    e2e_replayed = pot.last_replayed()
     pg_value, pg_ms = e2e_rate(np.array(s.positions, dtype=np.float64, order="C"),
                                np.zeros((nat, 3)))
+    pot, (p, nl) = pots["mixed"], where["mixed"]
     e2e = {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms,
            "h2d_bytes_per_step": 24 * nat, "d2h_bytes_per_step": 24 * nat + 80,
            "api": "native.Particles.set_positions + Tersoff.energy_and_forces(accumulate="
                   "False) (C-ABI gb_particles_set_positions / "
-                  "gb_potential_energy_and_forces_flags(GB_FORCES_SET)), pinned host numpy "
-                  "buffers: positions up, forces written down",
+                  "gb_potential_energy_and_forces_flags(GB_FORCES_SET)) on a potential with "
+                  "set_graph(True) (gb_potential_set_graph: each step one CUDA-graph replay "
+                  "of the whole evaluation, full neighbour rebuild included), pinned host "
+                  "numpy buffers: positions up, forces written down",
+           "replayed": bool(e2e_replayed),
            "pageable": {"value": pg_value, "unit": UNIT, "ms_per_step": pg_ms,
-                        "buffers": "plain numpy arrays (pageable host memory), same calls"}}
+                        "buffers": "plain numpy arrays (pageable host memory), same calls"},
+           "eager": {"value": e2e_mx_value, "unit": UNIT, "ms_per_step": e2e_mx_ms,
+                     "api": "the same calls without the graph option (pinned buffers)"}}
 
     # Roofline of the dominant kernel (mixed bond-order tile kernel):
     # T_roof = max(flops / FP32 peak, bytes / HBM peak), frac = T_roof / t.
@@ -839,7 +876,7 @@ def run_ours(args):
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_mx / args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_g / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32 three-body terms + float-float (2 x fp32) geometry, pair terms, "
                  "bond order, accumulation; fp64 tile sums",
@@ -850,14 +887,22 @@ def run_ours(args):
                    else "single GPU", "l2": "flushed between steps (256 MB write outside the "
                                             "timed events)",
                    "step": "set_positions (D2D) + energy_and_forces incl. full neighbour "
-                           "rebuild"},
+                           "rebuild, replayed as one CUDA graph (Tersoff.set_graph(True), "
+                           "gb_potential_set_graph; results equal the eager path's bit for "
+                           "bit, checked below)"},
         "fp64_dropin": {"value": value64, "unit": UNIT, "ms_per_step": 1e3 * t_64 / args.steps,
                         "neighbour_ms": nl_64, "kernel_ms": kern_64},
-        "mixed_over_fp64": value / value64,
+        "mixed_over_fp64": value_mx / value64,
+        "replayed_steps": int(replayed_g),
+        "graph_equals_eager": bool(graph_equal),
+        "eager": {"value": value_mx, "unit": UNIT, "ms_per_step": 1e3 * t_mx / args.steps,
+                  "gpu_launches": int(launches_mx), "neighbour_ms": nl_mx, "kernel_ms": kern_mx,
+                  "value_without_neighbour_build":
+                      ws * nat / ((1e3 * t_mx / args.steps - nl_mx) * 1e-3),
+                  "api": "the same calls without the graph option (host synchronisations: "
+                         "list sizes, final results)"},
         "mixed_accurate_path": {"bonds": hot[0], "recomputed": hot[1],
                                 "fraction": hot[1] / max(hot[0], 1), "atoms_per_tile": hot[2]},
-        "value_without_neighbour_build": ws * nat / ((1e3 * t_mx / args.steps - nl_mx) * 1e-3),
-        "neighbour_ms": nl_mx,
         "e2e": e2e,
         "roofline": roofline,
         "gpu_launches": int(launches),

@@ -481,8 +481,22 @@ int gb_potential_last_timing(const gb_potential_t *pot, double *ms);
 /* Work counts of the last energy_and_forces call: stats[0] directed bonds
  * (bond-order potentials), stats[1] bonds of the mixed form whose estimated
  * FP32 error sent them through the float-float recomputation, stats[2] atoms
- * per bond-order tile, stats[3] reserved (0).  stats must hold 4 int64_t. */
+ * per bond-order tile, stats[3] 1 when the call was a CUDA-graph replay
+ * (gb_potential_set_graph), else 0.  stats must hold 4 int64_t. */
 int gb_potential_last_stats(const gb_potential_t *pot, int64_t *stats);
+/* CUDA-graph replay of whole evaluations (on != 0; off by default) for the
+ * non-screened bond-order potentials: an evaluation with only epot, f and
+ * wpot requested (no mask, no per-atom or per-bond outputs) that follows an
+ * eager one on the same particles, neighbour list, cell and force array is
+ * captured — neighbour build (single staged pass, no host decision), tile
+ * kernel, gather, sums, the copies of status words and results — and the
+ * next such evaluations replay it with one host synchronisation.  The
+ * captured list has a per-atom capacity (1.25 x the largest coordination of
+ * the eager build + 4) and the captured tile plan head room; a replay that
+ * exceeded either leaves the forces untouched (set to zero with
+ * GB_FORCES_SET) and is redone eagerly, then captured again.  Results equal
+ * the eager path's bit for bit. */
+int gb_potential_set_graph(gb_potential_t *pot, int on);
 /* Atoms per bond-order tile (a power of two <= 64, reduced until the worst
  * tile fits in shared memory); 0 restores the automatic choice.  A tuning
  * knob: results do not depend on it beyond FP rounding of the tile sums. */
