@@ -263,6 +263,13 @@ __device__ __forceinline__ void finalize_bond(const BopArgs &a, const SmemLayout
 #define GB_MX_HOT_THRESHOLD 1.2e-5f
 #endif
 constexpr float kHotThreshold = GB_MX_HOT_THRESHOLD;
+// Juslin's W-C-H random packings (3 g/cm^3, 1.1 A minimum separation; H-H
+// contacts with forces of hundreds of eV/A) reach 7.5e-6 eV/A with 8e-6 and
+// 9.7e-6 with 1.2e-5: their threshold stays at 2e-6.
+#ifndef GB_MX_HOT_THRESHOLD_JUSLIN
+#define GB_MX_HOT_THRESHOLD_JUSLIN 2.0e-6f
+#endif
+constexpr float kHotThresholdJuslin = GB_MX_HOT_THRESHOLD_JUSLIN;
 // 1: the mixed kernel takes a batch's tiles from a counter (dynamic
 // schedule); 0: the static round-robin schedule for batches too.
 #ifndef GB_MX_TILE_QUEUE
@@ -610,7 +617,8 @@ int launch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int nt
     if (e == cudaSuccess) {
       const int resident = resident_ctas(kern, kMxThreads, smem);
       const int grid = resident > 0 ? std::min(ntiles, resident) : ntiles;
-      const MxParams mp = make_mx(pot, args.A);
+      MxParams mp = make_mx(pot, args.A);
+      mp.hot = std::is_same<Pot, JuslinPot>::value ? kHotThresholdJuslin : kHotThreshold;
       kern<<<grid, kMxThreads, smem, s>>>(args, pot, mp, posff, max_nbt, max_ntrip, status);
       note_launch();
       *rows = grid;

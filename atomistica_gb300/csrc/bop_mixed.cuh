@@ -9,7 +9,7 @@
 //            product; VA, VR, the bond order b and P = dE/dzeta in ff (ff exp,
 //            ln zeta by a Newton step); the energy, radial force and G partial
 //            in ff.  A bond whose estimated FP32 error (from |P| sum_k
-//            |dzeta/dr_k| and |dVA| d ln b/d ln zeta) exceeds kHotThreshold is
+//            |dzeta/dr_k| and |dVA| d ln b/d ln zeta) exceeds MxParams::hot is
 //            recomputed in FP64 (phase 2b);
 //   phase 3  G_ik -= P_ij dzeta_ij/dr_k and the virial in ff.
 // The only FP64 arithmetic left is the hot-bond recomputation, the conversion
@@ -57,6 +57,7 @@ struct MxTrip {
 struct MxParams {
   int kind;  // 0 Tersoff, Brenner and Juslin, 1 Kumagai
   int nel;
+  float hot;  // estimated force error (eV/A) above which a bond is recomputed
   MxPair pr[9];
   MxElem el[9];
   MxTrip tr[27];  // Juslin only
@@ -861,7 +862,7 @@ __global__ void __launch_bounds__(kMxThreads, GB_MX_MIN_BLOCKS)
                                1.5e-7f * fabsf(bij.hi - mp.pr[t].xi.hi)) +
                         3.0e-7f * fabsf(P.hi) *
                             (sumdk + fabsf(dbj[0]) + fabsf(dbj[1]) + fabsf(dbj[2]));
-      if (tiny || !(est <= kHotThreshold)) {
+      if (tiny || !(est <= mp.hot)) {
         L.hot[atomicAdd(&s_nhot, 1)] = lb;
         // kept for the accurate pass (which overwrites these slots)
         L.P[lb] = VA;

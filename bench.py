@@ -58,8 +58,8 @@ BYTES_BOND = 32.0
 # DRAM bytes (read + write) of one launch of the mixed tile kernel at this
 # workload, from the ncu capture summarised in
 # profiles/bop_tile_mx_tersoff_si_1048576.md (a past capture of the kernel
-# named there, hot-bond threshold 8e-6 eV/A; not a measurement of this run).
-TRAFFIC_MX = 75.56e6 + 50.34e6
+# named there, hot-bond threshold 1.2e-5 eV/A; not a measurement of this run).
+TRAFFIC_MX = 75.59e6 + 49.54e6
 # Alloy EAM flop model per list entry, counted from the reference's kernel
 # (tabulated_alloy_eam.f90:423-627): the density pass (displacement 21,
 # dot 5, sqrt, rho spline 11) and the force pass (phi spline f and df 14,
