@@ -561,36 +561,95 @@ __device__ __forceinline__ bool wrap_cell(const BinParams &bp, int k, int &c, in
   return true;
 }
 
-template <int kMode, bool kBatch>
-__global__ void __launch_bounds__(128)
-    nl_pairs(int nat, BinParams bp0, const BinParams *__restrict__ bps,
-             const int *__restrict__ sid, const Pos4 *__restrict__ pos4,
-             const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
-             const int *__restrict__ swrap, const int *__restrict__ cell_start,
-             int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
-             int *__restrict__ shift, int2 *__restrict__ stage, int cap, int clamp,
-             int *__restrict__ status) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  // lanes with an atom (blockDim.x is a multiple of 32): they sum their
-  // counts into the 64-bit list total at the end
-  const unsigned active = __ballot_sync(0xffffffffu, t < nat);
-  if (t >= nat) return;
-  const float4 pi = spos[t];
-  const int i = __float_as_int(pi.w);
-  const BinParams &bp = kBatch ? bps[sid[i]] : bp0;
-  int ci = atom_cell[i] - bp.cell_base;
-  const int cz0 = ci % bp.n[2];
-  ci /= bp.n[2];
-  const int cy0 = ci % bp.n[1];
-  const int cx0 = ci / bp.n[1];
-  int q0, q1, q2;
-  unpack_shift(swrap[t], q0, q1, q2);
+// One candidate: atom j at sorted slot jq for atom i (position pi), seen
+// through the run's image shift s = (sx, sy, sz) (s1zero: s = 0; o = A s in
+// FP32, Erun the run's error term) plus j's own wrap.  Returns the reference's
+// decision; j, the packed shift and whether the shift is outside the packed
+// range are returned for an accepted pair.
+__device__ __forceinline__ bool pair_test(const BinParams &bp, const float4 &pi, int i, int jq,
+                                          const float4 *__restrict__ spos,
+                                          const int *__restrict__ swrap,
+                                          const Pos4 *__restrict__ pos4, int sx, int sy, int sz,
+                                          bool s1zero, float ox, float oy, float oz, float Erun,
+                                          float Ebase, float eA, int packed1, bool &have_ri,
+                                          Pos4 &ri, int &j, int &packed, bool &range_bad) {
   const float u = 5.9604645e-8f;
-  const float X = __int_as_float(status[3]);
-  const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
-  const float eA = 8.0f * u * bp.Amax;
   const int kZeroWrap = pack_shift(0, 0, 0);
-  int cur = kMode == kPairsFill ? seed[i] : 0;
+  const float4 pj = spos[jq];
+  j = __float_as_int(pj.w);
+  const int wj = swrap[jq];
+  int s2x = sx, s2y = sy, s2z = sz;
+  bool zero_shift = s1zero;
+  float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+  float E = Erun;
+  if (wj == kZeroWrap) {
+    dx += ox;
+    dy += oy;
+    dz += oz;
+  } else {
+    int w0, w1, w2;
+    unpack_shift(wj, w0, w1, w2);
+    s2x += w0;
+    s2y += w1;
+    s2z += w2;
+    zero_shift = (s2x | s2y | s2z) == 0;
+    const float fx = (float)s2x, fy = (float)s2y, fz = (float)s2z;
+    dx += bp.Af[0][0] * fx + bp.Af[0][1] * fy + bp.Af[0][2] * fz;
+    dy += bp.Af[1][0] * fx + bp.Af[1][1] * fy + bp.Af[1][2] * fz;
+    dz += bp.Af[2][0] * fx + bp.Af[2][1] * fy + bp.Af[2][2] * fz;
+    E = Ebase + eA * (fabsf(fx) + fabsf(fy) + fabsf(fz));
+  }
+  if (j == i && zero_shift) return false;
+  const float d2f = dx * dx + dy * dy + dz * dz;
+  const float B = 2.0f * E * (1.735f * (d2f + 1.0f) + 9.0f * E) + 12.0f * u * d2f;
+  bool accept;
+  if (d2f + B < bp.cutoff_sq_lo) {
+    accept = true;
+  } else if (d2f - B > bp.cutoff_sq_hi) {
+    accept = false;
+  } else {
+    if (!have_ri) {
+      ri = pos4[i];
+      have_ri = true;
+    }
+    accept = exact_pair_test(bp, ri, pos4[j], s2x, s2y, s2z);
+  }
+  if (accept) {
+    packed = wj == kZeroWrap ? packed1 : pack_shift(s2x, s2y, s2z);
+    range_bad = s2x > kMaxShift || s2x < -kMaxShift || s2y > kMaxShift || s2y < -kMaxShift ||
+                s2z > kMaxShift || s2z < -kMaxShift;
+  }
+  return accept;
+}
+
+// An accepted entry number pos of atom i, as kMode stores it.
+template <int kMode>
+__device__ __forceinline__ void pair_store(int i, int pos, int j, int packed, bool range_bad,
+                                           int seed_i, int *__restrict__ nbr,
+                                           int *__restrict__ shift, int2 *__restrict__ stage,
+                                           int cap, int *__restrict__ status) {
+  if (kMode == kPairsFill) {
+    nbr[seed_i + pos] = j;
+    shift[seed_i + pos] = packed;
+  } else {
+    if (kMode == kPairsCountStage && pos < cap)
+      stage[(size_t)i * cap + pos] = make_int2(j, packed);
+    if (range_bad) atomicOr(&status[1], 2);
+  }
+}
+
+// The whole stencil of atom i (sorted slot t, cell (cx0, cy0, cz0), wrap q)
+// walked on one thread in the reference's order; returns its entry count.
+template <int kMode>
+__device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const float4 &pi, int cx0,
+                                          int cy0, int cz0, int q0, int q1, int q2, float Ebase,
+                                          float eA, const Pos4 *__restrict__ pos4,
+                                          const float4 *__restrict__ spos,
+                                          const int *__restrict__ swrap,
+                                          const int *__restrict__ cell_start, int seed_i,
+                                          int *__restrict__ nbr, int *__restrict__ shift,
+                                          int2 *__restrict__ stage, int cap,
+                                          int *__restrict__ status) {
   int cnt = 0;
   bool have_ri = false;
   Pos4 ri;
@@ -623,64 +682,53 @@ __global__ void __launch_bounds__(128)
         }
         const int packed1 = pack_shift(sx, sy, sz);
         for (int jq = js; jq < je; jq++) {
-          const float4 pj = spos[jq];
-          const int j = __float_as_int(pj.w);
-          const int wj = swrap[jq];
-          int s2x = sx, s2y = sy, s2z = sz;
-          bool zero_shift = s1zero;
-          float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-          float E = Erun;
-          if (wj == kZeroWrap) {
-            dx += ox;
-            dy += oy;
-            dz += oz;
-          } else {
-            int w0, w1, w2;
-            unpack_shift(wj, w0, w1, w2);
-            s2x += w0;
-            s2y += w1;
-            s2z += w2;
-            zero_shift = (s2x | s2y | s2z) == 0;
-            const float fx = (float)s2x, fy = (float)s2y, fz = (float)s2z;
-            dx += bp.Af[0][0] * fx + bp.Af[0][1] * fy + bp.Af[0][2] * fz;
-            dy += bp.Af[1][0] * fx + bp.Af[1][1] * fy + bp.Af[1][2] * fz;
-            dz += bp.Af[2][0] * fx + bp.Af[2][1] * fy + bp.Af[2][2] * fz;
-            E = Ebase + eA * (fabsf(fx) + fabsf(fy) + fabsf(fz));
-          }
-          if (j == i && zero_shift) continue;
-          const float d2f = dx * dx + dy * dy + dz * dz;
-          const float B = 2.0f * E * (1.735f * (d2f + 1.0f) + 9.0f * E) + 12.0f * u * d2f;
-          bool accept;
-          if (d2f + B < bp.cutoff_sq_lo) {
-            accept = true;
-          } else if (d2f - B > bp.cutoff_sq_hi) {
-            accept = false;
-          } else {
-            if (!have_ri) {
-              ri = pos4[i];
-              have_ri = true;
-            }
-            accept = exact_pair_test(bp, ri, pos4[j], s2x, s2y, s2z);
-          }
-          if (accept) {
-            const int packed = wj == kZeroWrap ? packed1 : pack_shift(s2x, s2y, s2z);
-            if (kMode == kPairsFill) {
-              nbr[cur] = j;
-              shift[cur] = packed;
-              cur++;
-            } else {
-              if (kMode == kPairsCountStage && cnt < cap)
-                stage[(size_t)i * cap + cnt] = make_int2(j, packed);
-              cnt++;
-              if (s2x > kMaxShift || s2x < -kMaxShift || s2y > kMaxShift ||
-                  s2y < -kMaxShift || s2z > kMaxShift || s2z < -kMaxShift)
-                atomicOr(&status[1], 2);
-            }
+          int j, packed;
+          bool range_bad;
+          if (pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz, Erun,
+                        Ebase, eA, packed1, have_ri, ri, j, packed, range_bad)) {
+            pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
+                              status);
+            cnt++;
           }
         }
       }
     }
   }
+  return cnt;
+}
+
+template <int kMode, bool kBatch>
+__global__ void __launch_bounds__(128)
+    nl_pairs(int nat, BinParams bp0, const BinParams *__restrict__ bps,
+             const int *__restrict__ sid, const Pos4 *__restrict__ pos4,
+             const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
+             const int *__restrict__ swrap, const int *__restrict__ cell_start,
+             int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
+             int *__restrict__ shift, int2 *__restrict__ stage, int cap, int clamp,
+             int *__restrict__ status) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // lanes with an atom (blockDim.x is a multiple of 32): they sum their
+  // counts into the 64-bit list total at the end
+  const unsigned active = __ballot_sync(0xffffffffu, t < nat);
+  if (t >= nat) return;
+  const float4 pi = spos[t];
+  const int i = __float_as_int(pi.w);
+  const BinParams &bp = kBatch ? bps[sid[i]] : bp0;
+  int ci = atom_cell[i] - bp.cell_base;
+  const int cz0 = ci % bp.n[2];
+  ci /= bp.n[2];
+  const int cy0 = ci % bp.n[1];
+  const int cx0 = ci / bp.n[1];
+  int q0, q1, q2;
+  unpack_shift(swrap[t], q0, q1, q2);
+  const float u = 5.9604645e-8f;
+  const float X = __int_as_float(status[3]);
+  const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
+  const float eA = 8.0f * u * bp.Amax;
+  const int cnt =
+      pairs_walk<kMode>(bp, i, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4, spos, swrap,
+                        cell_start, kMode == kPairsFill ? seed[i] : 0, nbr, shift, stage, cap,
+                        status);
   if (kMode != kPairsFill) {
     // clamp: the staged single pass without a host check (captured graphs)
     // keeps at most cap entries per atom; status[0] still records the true
