@@ -571,37 +571,44 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
   drop_single_graph(pot);
   const int nat = p.nat;
   const int cap = nl.stage_cap;
+  const bool bop = pot.kind != kEAM;
   const int nbt0 = pot.last_plan[0], ntrip0 = pot.last_plan[1];
-  if (cap <= 0 || nat <= 0 || !nl.valid || nl.built_for != &p || nbt0 <= 0 || !nl.want_rev)
-    return;
+  if (cap <= 0 || nat <= 0 || !nl.valid || nl.built_for != &p || (bop && nbt0 <= 0)) return;
   const int64_t capacity = (int64_t)nat * cap;
   if (capacity > (int64_t)INT_MAX / 3) return;
   const bool mixed = pot.precision == GB_PRECISION_MIXED;
-  const int apt = pot.tile_atoms;
-  const int ntiles = (nat + apt - 1) / apt;
-  // Tile plan with head room for the next configurations (checked per tile
-  // by the kernel): as much as fits without fewer resident CTAs per SM than
-  // the exact plan of this evaluation, at most +25 % bonds / +50 % slots.
-  const int occ0 = bop_tile_ctas_per_sm(pot, bop_tile_smem(mixed, nbt0, ntrip0));
   int max_nbt = nbt0, max_ntrip = ntrip0;
-  for (int step = 16; step >= 1; step--) {
-    const int nb = std::min(apt * cap, nbt0 + nbt0 * step / 64 + step);
-    const int nt = std::min(apt * trip_slots(cap), ntrip0 + ntrip0 * step / 32 + 4 * step);
-    const size_t sm = bop_tile_smem(mixed, nb, nt);
-    if (sm <= bop_tile_smem_budget() && bop_tile_ctas_per_sm(pot, sm) >= occ0) {
-      max_nbt = nb;
-      max_ntrip = nt;
-      break;
+  if (bop) {
+    const int apt = pot.tile_atoms;
+    const int ntiles = (nat + apt - 1) / apt;
+    // Tile plan with head room for the next configurations (checked per tile
+    // by the kernel): as much as fits without fewer resident CTAs per SM than
+    // the exact plan of this evaluation, at most +25 % bonds / +50 % slots.
+    const int occ0 = bop_tile_ctas_per_sm(pot, bop_tile_smem(mixed, nbt0, ntrip0));
+    for (int step = 16; step >= 1; step--) {
+      const int nb = std::min(apt * cap, nbt0 + nbt0 * step / 64 + step);
+      const int nt = std::min(apt * trip_slots(cap), ntrip0 + ntrip0 * step / 32 + 4 * step);
+      const size_t sm = bop_tile_smem(mixed, nb, nt);
+      if (sm <= bop_tile_smem_budget() && bop_tile_ctas_per_sm(pot, sm) >= occ0) {
+        max_nbt = nb;
+        max_ntrip = nt;
+        break;
+      }
+    }
+    if (pot.bond_G.ensure(sizeof(double) * 3 * capacity) ||
+        pot.bond_e.ensure(sizeof(double) * capacity) ||
+        pot.tile_part.ensure(sizeof(double) * 10 * (size_t)ntiles + 64) ||
+        pot.red_stage.ensure(reduce_stage_bytes(ntiles) + 64)) {
+      clear_error();
+      return;
     }
   }
   // every buffer at its captured size now: nothing may be allocated inside
+  // (the EAM kernels' per-atom and per-block buffers depend on nat only and
+  // were sized by the eager call)
   if (nl.nbr.ensure(sizeof(int) * capacity) || nl.shift.ensure(sizeof(int) * capacity) ||
       nl.rev.ensure(sizeof(int) * capacity) || nl.stage.ensure(sizeof(int2) * capacity) ||
-      pot.bond_G.ensure(sizeof(double) * 3 * capacity) ||
-      pot.bond_e.ensure(sizeof(double) * capacity) ||
-      pot.tile_part.ensure(sizeof(double) * 10 * (size_t)ntiles + 64) ||
-      pot.red_stage.ensure(reduce_stage_bytes(ntiles) + 64) || pot.red.ensure(sizeof(double) * 16) ||
-      pot.hred.ensure(sizeof(double) * 16)) {
+      pot.red.ensure(sizeof(double) * 16) || pot.hred.ensure(sizeof(double) * 16)) {
     clear_error();
     return;
   }
@@ -644,7 +651,9 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
     rc = -1;
   if (rc == 0 && cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s) != cudaSuccess) rc = -1;
   if (rc == 0) rc = nl_build(nl, nat, p.r.as<double>(), bp, nullptr, nullptr, ncells, s, true);
-  if (rc == 0) rc = bop_run(pot, sys, nl, o, false, false);
+  if (rc == 0)
+    rc = bop ? bop_run(pot, sys, nl, o, false, false)
+             : eam_compute(pot, p, nl, o, false, sys.check, true);
   if (rc == 0 && cudaMemcpyAsync(pot.hred.p, o.red, sizeof(double) * 14, cudaMemcpyDeviceToHost,
                                  s) != cudaSuccess)
     rc = -1;
@@ -760,7 +769,7 @@ int single_replay(Potential &pot, Particles &p, Neighbors &nl, double *f, double
   nl.built_cell_rev = p.cell_rev;
   nl.built_nat = p.nat;
   nl.cutoff = nl.interaction_range;
-  nl.rev_valid = true;
+  nl.rev_valid = pot.kind != kEAM;  // (the bond-order evaluation builds the reverse index)
   nl.rev_pending = false;
   nl.posff_valid = nl.want_posff;
   nl.plan_ready = false;
@@ -811,9 +820,8 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   const int nat = p.nat;
   // CUDA-graph replay of a whole evaluation (outputs: energy, forces, virial)
   pot.last_replayed = false;
-  const bool graph_ok = pot.use_graph && !pot.graph_failed && pot.kind != kEAM &&
-                        !pot.screened && nat > 0 && !mask && !epa && !wpa && !epb && !fpb &&
-                        !wpb;
+  const bool graph_ok = pot.use_graph && !pot.graph_failed && !pot.screened && nat > 0 &&
+                        !mask && !epa && !wpa && !epb && !fpb && !wpb;
   double *gfd = nullptr;
   if (graph_ok) {
     const bool fh = !is_device_ptr(f);

@@ -323,6 +323,7 @@ struct EamArgs {
   double *f, *epa, *wpa;  // outputs (device, accumulated)
   double *part;           // 10 per block
   int *status;
+  ReplayCheck chk;        // a replayed evaluation writes no forces when invalid
 };
 
 // simple_spline_f_and_df with extrapolate=.true. (:536-614).
@@ -613,7 +614,7 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
   double e_tot = 0.0;
   if (eli >= 0) {
     if (mi) Ei += a.Fi[i];
-    if (sub == 0) {
+    if (sub == 0 && !replay_invalid(a.chk)) {
 #pragma unroll
       for (int c = 0; c < 3; c++) a.f[3 * (size_t)i + c] += F3[c];
       if (kEpa && mi) a.epa[i] += Ei;
@@ -645,7 +646,7 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
 }  // namespace
 
 int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
-                bool want_wat) {
+                bool want_wat, ReplayCheck chk, bool capture) {
   cudaStream_t s = pot.stream;
   const int nat = p.nat;
   EamTables &t = *pot.eam;
@@ -683,6 +684,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   GB_CHECK(pot.tile_part.ensure(sizeof(double) * 10 * blocks + 64));
   a.part = pot.tile_part.as<double>();
   a.status = o.status;
+  a.chk = chk;
   const bool ff = t.funcfl;
   if (ff)
     eam_density<true><<<blocks, kEamThreads, 0, s>>>(a);
@@ -692,7 +694,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   const bool epa = o.epot_per_at != nullptr;
   // the funcfl kernel of the reference leaves wpot_per_at untouched
   const bool wat = want_wat && !ff;
-  GB_CUDA(cudaEventRecord(pot.kev[0], s));
+  if (!capture) GB_CUDA(cudaEventRecord(pot.kev[0], s));
   auto pair = [&](auto epa_t, auto wat_t, auto ff_t) {
     eam_pair<decltype(epa_t)::value, decltype(wat_t)::value, decltype(ff_t)::value>
         <<<blocks, kEamThreads, 0, s>>>(a);
@@ -714,7 +716,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   } else {
     pair(F{}, F{}, F{});
   }
-  GB_CUDA(cudaEventRecord(pot.kev[1], s));
+  if (!capture) GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CUDA(cudaGetLastError());
   GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(blocks) + 64));
   GB_CHECK(reduce_partials(a.part, blocks, 10, o.red, pot.red_stage.as<double>(), s));

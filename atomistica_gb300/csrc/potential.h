@@ -142,8 +142,9 @@ double bop_pair_range(const Potential &pot, int t);
 // Kernel launches (on pot.stream) for an up-to-date neighbour list.
 int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
                 bool want_wat, bool want_per_bond);
+// (chk, capture: a captured evaluation, see ReplayCheck; no event records)
 int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
-                bool want_wat);
+                bool want_wat, ReplayCheck chk = ReplayCheck{}, bool capture = false);
 // Element count / atomic number of element q of the potential; its stream.
 int pot_nel(const Potential &pot);
 // Number of element-pair entries (nel (nel + 1) / 2 symmetric pairs; Juslin:

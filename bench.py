@@ -357,6 +357,19 @@ def eam_config(dev, oracle, nth, cpu_time):
             pair_ms.append(pot.last_timing()[3])
         pair_ms = statistics.median(pair_ms)
         n_entries = int(nl.get_list(p)[0][-1])
+        # the same step replayed as a CUDA graph (own particles and list)
+        pg = native.from_atoms(s)
+        nlg = native.Neighbors(100)
+        potg = native.TabulatedAlloyEAM(fn)
+        potg.bind_to(pg, nlg)
+        potg.set_graph(True)
+        ms_g = _gpu_step_ms(potg, pg, nlg, d_pos, d_f)
+        d_f.zero_()
+        pg.set_positions(d_pos)
+        e_g, _, _ = potg.energy_and_forces(pg, nlg, forces=d_f)
+        graph = {"value": len(s) / (ms_g * 1e-3), "ms_per_step": ms_g,
+                 "replayed": potg.last_replayed(),
+                 "equals_eager": bool(e_g == e and np.array_equal(d_f.cpu().numpy(), f))}
     from atomistica_gb300 import _lib
     fp64_peak = _peak(_lib.load(), True)
     eam_roof = {"bound": "fp64", "kernel": "eam_pair (force pass)", "kernel_ms": pair_ms,
@@ -369,6 +382,7 @@ def eam_config(dev, oracle, nth, cpu_time):
             "fp64": {"value": len(s) / (ms * 1e-3), "ms_per_step": ms,
                      "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                      "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)},
+            "fp64_graph": graph,
             "roofline": eam_roof}
 
 

@@ -485,7 +485,8 @@ int gb_potential_last_timing(const gb_potential_t *pot, double *ms);
  * (gb_potential_set_graph), else 0.  stats must hold 4 int64_t. */
 int gb_potential_last_stats(const gb_potential_t *pot, int64_t *stats);
 /* CUDA-graph replay of whole evaluations (on != 0; off by default) for the
- * non-screened bond-order potentials: an evaluation with only epot, f and
+ * non-screened bond-order potentials and the EAM classes: an evaluation with
+ * only epot, f and
  * wpot requested (no mask, no per-atom or per-bond outputs) that follows an
  * eager one on the same particles, neighbour list, cell and force array is
  * captured — neighbour build (single staged pass, no host decision), tile

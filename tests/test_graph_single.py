@@ -148,3 +148,33 @@ def test_nonfinite_position_after_replays(gpu):
     p.set_positions(r)
     with pytest.raises(AtomisticaError, match="Non-finite particle position"):
         pot.energy_and_forces(p, nl)
+
+
+def test_eam_replay_equals_eager(gpu, tmp_path):
+    import torch
+    from atomistica_gb300 import io as gio
+    from atomistica_gb300 import native
+    fn = gio.analytic_alloy_setfl(str(tmp_path / "a.setfl"), ["Cu", "Ag"], seed=3)
+    s = S.fcc("Cu", 3.7, (5, 5, 5))
+    rng = np.random.default_rng(20)
+    s.numbers = np.array(rng.choice([29, 47], len(s)), dtype=np.int32)
+    dev = torch.device("cuda", 0)
+    r0 = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+    f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+    runs = []
+    for graph in (False, True):
+        p = native.from_atoms(s)
+        nl = native.Neighbors(100)
+        pot = native.TabulatedAlloyEAM(fn)
+        pot.bind_to(p, nl)
+        if graph:
+            pot.set_graph(True)
+        runs.append((p, nl, pot))
+    replays = 0
+    for step in range(4):
+        r = r0 + torch.tensor(rng.normal(0, 0.05, (len(s), 3)), device=dev)
+        e0, f0, w0 = _eval(*runs[0], r, f)
+        e1, f1, w1 = _eval(*runs[1], r, f)
+        replays += runs[1][2].last_replayed()
+        assert e1 == e0 and np.array_equal(f1, f0) and np.array_equal(w1, w0), step
+    assert replays >= 2
