@@ -527,20 +527,22 @@ __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__r
     for (int c = 0; c < 9; c++) wpa[9 * (size_t)i + c] += 0.5 * W[c];
 }
 
-// Tile plan: per tile bond count and (ij, ik) slots.
+// Tile plan: per tile bond count and (ij, ik) slots; a warp per tile, its
+// lanes over the tile's atoms (at most 64), one atomic per warp.
 __global__ void bop_plan(int nat, int apt, int ntiles, const int *__restrict__ tile_atom0,
                          const int *__restrict__ seed, int *__restrict__ out) {
-  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tile >= ntiles) return;
+  const int tile = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (tile >= ntiles) return;  // (whole warps)
   const int a0 = tile_atom0 ? tile_atom0[tile] : tile * apt;
   const int a1 = tile_atom0 ? tile_atom0[tile + 1] : min(a0 + apt, nat);
   int ntrip = 0;
-  for (int q = a0; q < a1; q++) {
-    const int z = seed[q + 1] - seed[q];
-    ntrip += trip_slots(z);
+  for (int q = a0 + lane; q < a1; q += 32) ntrip += trip_slots(seed[q + 1] - seed[q]);
+  ntrip = __reduce_add_sync(0xffffffffu, ntrip);
+  if (lane == 0) {
+    atomicMax(&out[0], seed[a1] - seed[a0]);
+    atomicMax(&out[1], ntrip);
   }
-  atomicMax(&out[0], seed[a1] - seed[a0]);
-  atomicMax(&out[1], ntrip);
 }
 
 // Deterministic sum of rows of kRedCols doubles: block q sums rows
@@ -1053,7 +1055,8 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 int bop_plan_launch(int nat, int apt, int ntiles, const int *tile_atom0, const int *seed,
                     int *out, cudaStream_t s) {
   if (ntiles <= 0) return 0;
-  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, tile_atom0, seed, out);
+  bop_plan<<<(unsigned)(((int64_t)ntiles * 32 + 127) / 128), 128, 0, s>>>(nat, apt, ntiles,
+                                                                          tile_atom0, seed, out);
   note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -1338,9 +1341,7 @@ extern "C" int gb_bop_energy_and_forces_noalloc(gb_potential_t *h, int nat, cons
   const int ntiles = (nat + apt - 1) / apt;
   noalloc_reverse<<<(nat + 127) / 128, 128, 0, s>>>(nat, seed32, j, shift, rev, status);
   note_launch();
-  bop_plan<<<(ntiles + 127) / 128, 128, 0, s>>>(nat, apt, ntiles, nullptr, seed32, plan);
-  note_launch();
-  GB_CUDA(cudaGetLastError());
+  GB_CHECK(bop_plan_launch(nat, apt, ntiles, nullptr, seed32, plan, s));
   int hp[6] = {0, 0, 0, 0, 0, 0};
   GB_CUDA(cudaMemcpyAsync(hp, status, sizeof(hp), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));

@@ -232,10 +232,55 @@ size_t scan_tmp_ints(int n) {
 
 }  // namespace
 
+// Small inputs (n <= 16384): one block of 1024 threads, 16 consecutive
+// elements each, and the total out[n]: one launch.
+constexpr int kScanSmallThreads = 1024, kScanSmallPer = 16;
+__global__ void __launch_bounds__(kScanSmallThreads)
+    scan_small(const int *__restrict__ in, int *__restrict__ out, int n) {
+  __shared__ int warp_tot[kScanSmallThreads / 32];
+  const int base = threadIdx.x * kScanSmallPer;
+  int v[kScanSmallPer];
+  int s = 0;
+#pragma unroll
+  for (int q = 0; q < kScanSmallPer; q++) {
+    v[q] = base + q < n ? in[base + q] : 0;
+    s += v[q];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  int run = incl - s + (wid > 0 ? warp_tot[wid - 1] : 0);
+#pragma unroll
+  for (int q = 0; q < kScanSmallPer; q++) {
+    if (base + q < n) out[base + q] = run;
+    run += v[q];
+  }
+  if (threadIdx.x == kScanSmallThreads - 1) out[n] = run;
+}
+
 int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t stream) {
   GB_CHECK(tmp.ensure(scan_tmp_ints(n) * sizeof(int)));
   const int tiles = (n + kScanTile - 1) / kScanTile;
-  if (n > 0 && tiles <= kScanFlatTiles) {
+  if (n > 0 && n <= kScanSmallThreads * kScanSmallPer) {
+    scan_small<<<1, kScanSmallThreads, 0, stream>>>(in, out, n);
+    note_launch();
+  } else if (n > 0 && tiles <= kScanFlatTiles) {
     // two launches: tile scans, then the tile offsets and the total
     scan_tiles<<<tiles, kScanThreads, 0, stream>>>(in, out, n, tmp.as<int>());
     note_launch();
@@ -745,6 +790,177 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Small structures (too few atoms to fill the GPU with one thread per atom):
+// the candidates of an atom are dealt to a group of kPairLanes lanes, so that
+// its walk does not run serially on one thread.  The group's lanes lay out
+// the atom's stencil rows (row k on lane k mod 8; per row at most two runs of
+// consecutive cells, as the row splits where it crosses the periodic
+// boundary in z) with their image shifts in a shared table, take a prefix
+// over the runs in stencil order and deal the candidates c = 0, 1, ... to the
+// lanes in turn (lane g takes c = g, g + 8, ...); the group's ballot places
+// the accepted entries in exactly the order of the one-thread walk.  An atom
+// with more than 16 rows or more than two runs in a row is walked by the
+// group's first lane.
+constexpr int kPairLanes = 8;
+constexpr int kPairRows = 16;
+constexpr int kPairSlots = 2 * kPairRows;
+constexpr int kPairGroupMaxAtoms = 32768;
+
+template <int kMode>
+__global__ void __launch_bounds__(128)
+    nl_pairs_grp(int nat, BinParams bp, const Pos4 *__restrict__ pos4,
+                 const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
+                 const int *__restrict__ swrap, const int *__restrict__ cell_start,
+                 int *__restrict__ counts, const int *__restrict__ seed, int *__restrict__ nbr,
+                 int *__restrict__ shift, int2 *__restrict__ stage, int cap, int clamp,
+                 int *__restrict__ status) {
+  constexpr int G = kPairLanes;
+  __shared__ int s_js[128 / G][kPairSlots], s_sh[128 / G][kPairSlots];
+  __shared__ int s_pre[128 / G][kPairSlots + 1];
+  const int lane = threadIdx.x & 31, g = threadIdx.x & (G - 1), grp = threadIdx.x / G;
+  const unsigned gmask = 0xFFu << (lane & 24);
+  const int t = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G);
+  int cnt = 0, i = -1;
+  if (t < nat) {  // (uniform over the group)
+    const float4 pi = spos[t];
+    i = __float_as_int(pi.w);
+    int ci = atom_cell[i];
+    const int cz0 = ci % bp.n[2];
+    ci /= bp.n[2];
+    const int cy0 = ci % bp.n[1];
+    const int cx0 = ci / bp.n[1];
+    int q0, q1, q2;
+    unpack_shift(swrap[t], q0, q1, q2);
+    const float u = 5.9604645e-8f;
+    const float X = __int_as_float(status[3]);
+    const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
+    const float eA = 8.0f * u * bp.Amax;
+    const int seed_i = kMode == kPairsFill ? seed[i] : 0;
+    const int ny = 2 * bp.dy + 1, nrows = (2 * bp.dx + 1) * ny;
+    bool over = nrows > kPairRows;
+    int js[2][2], len[2][2], sh[2][2];
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+#pragma unroll
+      for (int p = 0; p < 2; p++) {
+        js[m][p] = 0;
+        len[m][p] = 0;
+        sh[m][p] = 0;
+      }
+      const int k = g + G * m;
+      if (over || k >= nrows) continue;
+      int cx = cx0 + k / ny - bp.dx, sx = -q0;
+      int cy = cy0 + k % ny - bp.dy, sy = -q1;
+      if (!wrap_cell(bp, 0, cx, sx) || !wrap_cell(bp, 1, cy, sy)) continue;
+      const int row = cell_linear(bp, cx, cy, 0);
+      int z = -bp.dz, np = 0;
+      while (z <= bp.dz) {
+        int cz = cz0 + z, sz = -q2;
+        if (!wrap_cell(bp, 2, cz, sz)) {
+          z++;
+          continue;
+        }
+        const int run = min(bp.dz - z + 1, bp.n[2] - cz);
+        if (np < 2) {
+          js[m][np] = cell_start[row + cz];
+          len[m][np] = cell_start[row + cz + run] - js[m][np];
+          sh[m][np] = pack_shift(sx, sy, sz);
+        }
+        np++;
+        z += run;
+      }
+      if (np > 2) over = true;
+    }
+    over = __any_sync(gmask, over);
+    if (!over) {
+      // slots 2k + p (row k, run p) in stencil order: exclusive prefix
+      int base = 0;
+#pragma unroll
+      for (int m = 0; m < 2; m++) {
+        const int rl = len[m][0] + len[m][1];
+        int inc = rl;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+          const int v = __shfl_up_sync(gmask, inc, o, G);
+          if (g >= o) inc += v;
+        }
+        const int k = g + G * m;
+        if (k < nrows) {
+          const int p0 = base + inc - rl;
+#pragma unroll
+          for (int p = 0; p < 2; p++) {
+            s_js[grp][2 * k + p] = js[m][p];
+            s_sh[grp][2 * k + p] = sh[m][p];
+          }
+          s_pre[grp][2 * k] = p0;
+          s_pre[grp][2 * k + 1] = p0 + len[m][0];
+        }
+        base += __shfl_sync(gmask, inc, G - 1, G);
+      }
+      if (g == 0) s_pre[grp][2 * nrows] = base;
+      __syncwarp(gmask);
+      const int total = base;
+      bool have_ri = false;
+      Pos4 ri;
+      int r = 0, rs = -1, sx = 0, sy = 0, sz = 0, packed1 = 0;
+      bool s1zero = true;
+      float ox = 0.0f, oy = 0.0f, oz = 0.0f, Erun = Ebase;
+      for (int c0 = 0; c0 < total; c0 += G) {
+        const int c = c0 + g;
+        bool accept = false, range_bad = false;
+        int j = 0, packed = 0;
+        if (c < total) {
+          while (s_pre[grp][r + 1] <= c) r++;
+          if (r != rs) {  // the run's image offset, as pairs_walk forms it
+            rs = r;
+            packed1 = s_sh[grp][r];
+            unpack_shift(packed1, sx, sy, sz);
+            s1zero = (sx | sy | sz) == 0;
+            ox = oy = oz = 0.0f;
+            Erun = Ebase;
+            if (!s1zero) {
+              const float fx = (float)sx, fy = (float)sy, fz = (float)sz;
+              ox = bp.Af[0][0] * fx + bp.Af[0][1] * fy + bp.Af[0][2] * fz;
+              oy = bp.Af[1][0] * fx + bp.Af[1][1] * fy + bp.Af[1][2] * fz;
+              oz = bp.Af[2][0] * fx + bp.Af[2][1] * fy + bp.Af[2][2] * fz;
+              Erun += eA * (fabsf(fx) + fabsf(fy) + fabsf(fz));
+            }
+          }
+          const int jq = s_js[grp][r] + (c - s_pre[grp][r]);
+          accept = pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz,
+                             Erun, Ebase, eA, packed1, have_ri, ri, j, packed, range_bad);
+        }
+        const unsigned mine = (__ballot_sync(gmask, accept) >> (lane & 24)) & 0xFFu;
+        if (accept)
+          pair_store<kMode>(i, cnt + __popc(mine & ((1u << g) - 1u)), j, packed, range_bad,
+                            seed_i, nbr, shift, stage, cap, status);
+        cnt += __popc(mine);
+      }
+    } else if (g == 0) {
+      cnt = pairs_walk<kMode>(bp, i, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4, spos, swrap,
+                              cell_start, seed_i, nbr, shift, stage, cap, status);
+    }
+    cnt = __shfl_sync(gmask, cnt, 0, G);
+  }
+  if (kMode != kPairsFill) {
+    // as nl_pairs: counts (clamped for a captured build), the largest count,
+    // the refusal of 2^26 or more per atom and the 64-bit total; one atomic
+    // per warp for the last two
+    const bool lead = g == 0 && i >= 0;
+    if (lead) {
+      counts[i] = clamp ? min(cnt, cap) : cnt;
+      if (cnt >= (1 << 26)) atomicOr(&status[1], 8);
+    }
+    const unsigned mx = __reduce_max_sync(0xffffffffu, lead ? (unsigned)cnt : 0u);
+    const unsigned wsum =
+        __reduce_add_sync(0xffffffffu, lead ? (unsigned)min(cnt, (1 << 26) - 1) : 0u);
+    if (lane == 0) {
+      atomicMax(&status[0], (int)min(mx, (unsigned)INT_MAX));
+      atomicAdd(reinterpret_cast<unsigned long long *>(status + 6), (unsigned long long)wsum);
+    }
+  }
+}
+
 // CSR from the staged entries (every atom has at most cap of them).
 __global__ void nl_compact(int nat, int cap, const int *__restrict__ seed,
                            const int2 *__restrict__ stage, int *__restrict__ nbr,
@@ -1027,6 +1243,12 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
           nat, bp0, bps, sid, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
           nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr, shift, stage, cap,
           clamp, status);
+    else if (nat <= kPairGroupMaxAtoms)
+      nl_pairs_grp<kMode><<<(unsigned)(((int64_t)nat * kPairLanes + 127) / 128), 128, 0,
+                            stream>>>(nat, bp0, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(),
+                                      nl.spos.as<float4>(), nl.swrap.as<int>(),
+                                      nl.cell_start.as<int>(), counts, seed, nbr, shift, stage,
+                                      cap, clamp, status);
     else
       nl_pairs<kMode, false><<<(nat + 127) / 128, 128, 0, stream>>>(
           nat, bp0, nullptr, nullptr, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(),
@@ -1042,7 +1264,7 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
         ncells, nl.cell_start.as<int>(), cell_atoms, big_cells, &status[2], nl.pos4.as<Pos4>(),
         nl.atom_wrap.as<int>(), nl.spos.as<float4>(), nl.swrap.as<int>());
     note_launch();
-    nl_sort_big_cells<<<std::min(ncells, 1024), 256, 0, stream>>>(
+    nl_sort_big_cells<<<std::min(ncells, 128), 256, 0, stream>>>(
         big_cells, &status[2], nl.cell_start.as<int>(), cell_atoms, cell_atoms + nat,
         nl.pos4.as<Pos4>(), nl.atom_wrap.as<int>(), nl.spos.as<float4>(), nl.swrap.as<int>());
     note_launch();
