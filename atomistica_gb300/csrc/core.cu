@@ -804,7 +804,10 @@ __global__ void __launch_bounds__(128)
 constexpr int kPairLanes = 8;
 constexpr int kPairRows = 16;
 constexpr int kPairSlots = 2 * kPairRows;
-constexpr int kPairGroupMaxAtoms = 32768;
+#ifndef GB_PAIR_GROUP_MAX_ATOMS
+#define GB_PAIR_GROUP_MAX_ATOMS 32768
+#endif
+constexpr int kPairGroupMaxAtoms = GB_PAIR_GROUP_MAX_ATOMS;
 
 template <int kMode>
 __global__ void __launch_bounds__(128)

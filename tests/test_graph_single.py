@@ -178,3 +178,28 @@ def test_eam_replay_equals_eager(gpu, tmp_path):
         replays += runs[1][2].last_replayed()
         assert e1 == e0 and np.array_equal(f1, f0) and np.array_equal(w1, w0), step
     assert replays >= 2
+
+
+def test_cell_change_recaptures(gpu):
+    # a new cell (strain) changes the binning baked into the graph: that call
+    # runs eagerly and captures again; the results equal the eager path's
+    import torch
+    s = rattled_diamond("Si", 5.431, (3, 3, 3), 0.1, 21)
+    dev = torch.device("cuda", 0)
+    r0 = torch.tensor(s.positions, dtype=torch.float64, device=dev)
+    f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+    eager = _setup(s, "Tersoff", "mixed", False)
+    graph = _setup(s, "Tersoff", "mixed", True)
+    for _ in range(2):
+        _eval(*graph, r0, f)
+    assert graph[2].last_replayed()
+    strain = np.diag([1.01, 0.99, 1.02])
+    cell = s.cell @ strain
+    r1 = torch.tensor(s.positions @ strain, dtype=torch.float64, device=dev)
+    for p, _, _ in (eager, graph):
+        p.set_cell(cell, True)
+    for call in range(3):
+        e0, f0, w0 = _eval(*eager, r1, f)
+        e1, f1, w1 = _eval(*graph, r1, f)
+        assert graph[2].last_replayed() == (call > 0)
+        assert e1 == e0 and np.array_equal(f1, f0) and np.array_equal(w1, w0), call
