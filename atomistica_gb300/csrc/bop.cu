@@ -527,21 +527,36 @@ __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__r
     for (int c = 0; c < 9; c++) wpa[9 * (size_t)i + c] += 0.5 * W[c];
 }
 
-// Tile plan: per tile bond count and (ij, ik) slots; a warp per tile, its
-// lanes over the tile's atoms (at most 64), one atomic per warp.
-__global__ void bop_plan(int nat, int apt, int ntiles, const int *__restrict__ tile_atom0,
-                         const int *__restrict__ seed, int *__restrict__ out) {
-  const int tile = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (tile >= ntiles) return;  // (whole warps)
-  const int a0 = tile_atom0 ? tile_atom0[tile] : tile * apt;
-  const int a1 = tile_atom0 ? tile_atom0[tile + 1] : min(a0 + apt, nat);
-  int ntrip = 0;
-  for (int q = a0 + lane; q < a1; q += 32) ntrip += trip_slots(seed[q + 1] - seed[q]);
-  ntrip = __reduce_add_sync(0xffffffffu, ntrip);
+// Tile plan: the largest bond count and (ij, ik) slot count of the tiles.
+// Each warp walks tiles w, w + (warps in the grid), ..., its lanes over a
+// tile's atoms (at most 64), keeps its maxima, and the block adds them to the
+// result with one atomic per value (same-address atomics from every tile
+// would serialise).
+constexpr int kPlanThreads = 256;
+__global__ void __launch_bounds__(kPlanThreads)
+    bop_plan(int nat, int apt, int ntiles, const int *__restrict__ tile_atom0,
+             const int *__restrict__ seed, int *__restrict__ out) {
+  __shared__ int smax[2][kPlanThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (int)(gridDim.x * (kPlanThreads / 32));
+  int mb = 0, mt = 0;
+  for (int tile = (int)blockIdx.x * (kPlanThreads / 32) + wid; tile < ntiles; tile += nw) {
+    const int a0 = tile_atom0 ? tile_atom0[tile] : tile * apt;
+    const int a1 = tile_atom0 ? tile_atom0[tile + 1] : min(a0 + apt, nat);
+    int ntrip = 0;
+    for (int q = a0 + lane; q < a1; q += 32) ntrip += trip_slots(seed[q + 1] - seed[q]);
+    mt = max(mt, (int)__reduce_add_sync(0xffffffffu, ntrip));
+    mb = max(mb, seed[a1] - seed[a0]);
+  }
   if (lane == 0) {
-    atomicMax(&out[0], seed[a1] - seed[a0]);
-    atomicMax(&out[1], ntrip);
+    smax[0][wid] = mb;
+    smax[1][wid] = mt;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    int m = 0;
+    for (int w = 0; w < kPlanThreads / 32; w++) m = max(m, smax[threadIdx.x][w]);
+    atomicMax(&out[threadIdx.x], m);
   }
 }
 
@@ -1055,8 +1070,8 @@ int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
 int bop_plan_launch(int nat, int apt, int ntiles, const int *tile_atom0, const int *seed,
                     int *out, cudaStream_t s) {
   if (ntiles <= 0) return 0;
-  bop_plan<<<(unsigned)(((int64_t)ntiles * 32 + 127) / 128), 128, 0, s>>>(nat, apt, ntiles,
-                                                                          tile_atom0, seed, out);
+  const int blocks = std::min((ntiles + kPlanThreads / 32 - 1) / (kPlanThreads / 32), 152 * 4);
+  bop_plan<<<blocks, kPlanThreads, 0, s>>>(nat, apt, ntiles, tile_atom0, seed, out);
   note_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
