@@ -770,10 +770,40 @@ __global__ void __launch_bounds__(128)
   const float X = __int_as_float(status[3]);
   const float Ebase = u * (4.0f * X + 4.0f * bp.cutoff_f + 4.0f);
   const float eA = 8.0f * u * bp.Amax;
-  const int cnt =
-      pairs_walk<kMode>(bp, i, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4, spos, swrap,
-                        cell_start, kMode == kPairsFill ? seed[i] : 0, nbr, shift, stage, cap,
-                        status);
+  const int seed_i = kMode == kPairsFill ? seed[i] : 0;
+  // Inside the cell grid (no row of the stencil needs a periodic wrap, the
+  // atom is not wrapped): every row is one run of 2 dz + 1 cells with a zero
+  // image shift, so a whole warp of such atoms takes a lean walk (the same
+  // rows, runs, candidates and decisions as pairs_walk; a wrapped j still
+  // brings its own shift through pair_test).
+  const bool deep = !kBatch && (q0 | q1 | q2) == 0 && cx0 >= bp.dx &&
+                    cx0 < bp.n[0] - bp.dx && cy0 >= bp.dy && cy0 < bp.n[1] - bp.dy &&
+                    cz0 >= bp.dz && cz0 < bp.n[2] - bp.dz;
+  int cnt = 0;
+  if (__all_sync(active, deep)) {
+    const int kZeroWrap = pack_shift(0, 0, 0);
+    bool have_ri = false;
+    Pos4 ri;
+    for (int x = -bp.dx; x <= bp.dx; x++) {
+      for (int y = -bp.dy; y <= bp.dy; y++) {
+        const int row = cell_linear(bp, cx0 + x, cy0 + y, 0);
+        const int js = cell_start[row + cz0 - bp.dz], je = cell_start[row + cz0 + bp.dz + 1];
+        for (int jq = js; jq < je; jq++) {
+          int j, packed;
+          bool range_bad;
+          if (pair_test(bp, pi, i, jq, spos, swrap, pos4, 0, 0, 0, true, 0.0f, 0.0f, 0.0f, Ebase,
+                        Ebase, eA, kZeroWrap, have_ri, ri, j, packed, range_bad)) {
+            pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
+                              status);
+            cnt++;
+          }
+        }
+      }
+    }
+  } else {
+    cnt = pairs_walk<kMode>(bp, i, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4, spos, swrap,
+                            cell_start, seed_i, nbr, shift, stage, cap, status);
+  }
   if (kMode != kPairsFill) {
     // clamp: the staged single pass without a host check (captured graphs)
     // keeps at most cap entries per atom; status[0] still records the true
