@@ -832,6 +832,7 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
       GB_CHECK(single_replay(pot, p, nl, f, gfd, fh, set_f, epot, wpot, s, done));
       if (done) {
         pot.last_replayed = true;
+        pot.graph_unused = 0;
         return 0;
       }
     }
@@ -943,8 +944,17 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
   pot.last_bonds = pot.kind == kEAM ? 0 : nl.nentries;
   GB_CHECK(finish_results(pot, hr, epot, wpot));
-  if (graph_ok && !single_graph_current(pot, p, nl, gfd, set_f, s))
-    single_capture(pot, p, nl, gfd, set_f, s);
+  if (graph_ok && !single_graph_current(pot, p, nl, gfd, set_f, s)) {
+    // a caller whose calls never match the previous capture (e.g. a new
+    // force array every call) would pay a capture per call: after three
+    // captures in a row that were never replayed, stay eager
+    if (pot.graph_exec && ++pot.graph_unused >= 3) {
+      drop_single_graph(pot);
+      pot.graph_failed = true;
+    } else {
+      single_capture(pot, p, nl, gfd, set_f, s);
+    }
+  }
   return 0;
 }
 
@@ -1599,6 +1609,7 @@ int gb_potential_set_graph(gb_potential_t *h, int on) {
   if (!h) return GB_ERROR_ARGUMENT;
   h->pot.use_graph = on != 0;
   h->pot.graph_failed = false;
+  h->pot.graph_unused = 0;
   if (!on) drop_single_graph(h->pot);
   return 0;
 }

@@ -119,7 +119,8 @@ struct Potential {
   // captured after an eager evaluation and replayed while the particles,
   // list, cell, force buffer and every device buffer are unchanged.
   bool use_graph = false;
-  bool graph_failed = false;  // capture not possible: stay eager
+  bool graph_failed = false;  // capture not possible (or not useful): stay eager
+  int graph_unused = 0;       // captures in a row that were never replayed
   bool last_replayed = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;

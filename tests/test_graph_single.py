@@ -203,3 +203,20 @@ def test_cell_change_recaptures(gpu):
         e1, f1, w1 = _eval(*graph, r1, f)
         assert graph[2].last_replayed() == (call > 0)
         assert e1 == e0 and np.array_equal(f1, f0) and np.array_equal(w1, w0), call
+
+
+def test_new_force_array_every_call_stays_eager(gpu):
+    # a new device force array every call never matches the captured one:
+    # after a few captures the potential stops capturing; results stay exact
+    import torch
+    s = rattled_diamond("Si", 5.431, (3, 3, 3), 0.1, 22)
+    dev = torch.device("cuda", 0)
+    p, nl, pot = _setup(s, "Tersoff", "mixed", True)
+    pe, nle, pote = _setup(s, "Tersoff", "mixed", False)
+    fe = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+    e0, _, _ = pote.energy_and_forces(pe, nle, forces=fe)
+    for _ in range(6):
+        f = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+        e, _, _ = pot.energy_and_forces(p, nl, forces=f)
+        assert not pot.last_replayed()
+        assert e == e0 and torch.equal(f, fe)
