@@ -605,10 +605,19 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
   }
   // every buffer at its captured size now: nothing may be allocated inside
   // (the EAM kernels' per-atom and per-block buffers depend on nat only and
-  // were sized by the eager call)
-  if (nl.nbr.ensure(sizeof(int) * capacity) || nl.shift.ensure(sizeof(int) * capacity) ||
-      nl.rev.ensure(sizeof(int) * capacity) || nl.stage.ensure(sizeof(int2) * capacity) ||
-      pot.red.ensure(sizeof(double) * 16) || pot.hred.ensure(sizeof(double) * 16)) {
+  // were sized by the eager call).  A list array that grows here loses the
+  // eager call's list: the list is then marked for a rebuild.
+  const void *list0[3] = {nl.nbr.p, nl.shift.p, nl.rev.p};
+  const int grow = nl.nbr.ensure(sizeof(int) * capacity) ||
+                   nl.shift.ensure(sizeof(int) * capacity) ||
+                   nl.rev.ensure(sizeof(int) * capacity) ||
+                   nl.stage.ensure(sizeof(int2) * capacity) ||
+                   pot.red.ensure(sizeof(double) * 16) || pot.hred.ensure(sizeof(double) * 16);
+  if (nl.nbr.p != list0[0] || nl.shift.p != list0[1] || nl.rev.p != list0[2]) {
+    nl.valid = false;
+    nl.rev_valid = false;
+  }
+  if (grow) {
     clear_error();
     return;
   }
@@ -634,7 +643,7 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
   sys.check.cap = cap;
   // capturing runs nothing: the eager evaluation's list state stays valid
   const bool rev_valid0 = nl.rev_valid, posff_valid0 = nl.posff_valid;
-  const bool plan_ready0 = nl.plan_ready;
+  const bool plan_ready0 = nl.plan_ready, valid0 = nl.valid;
   const int plan0[2] = {pot.last_plan[0], pot.last_plan[1]};
   const int tile_atoms0 = pot.tile_atoms;
   nl.rev_valid = false;
@@ -663,6 +672,7 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
   nl.rev_pending = false;
   nl.posff_valid = posff_valid0;
   nl.plan_ready = plan_ready0;
+  nl.valid = valid0;
   pot.last_plan[0] = plan0[0];
   pot.last_plan[1] = plan0[1];
   pot.tile_atoms = tile_atoms0;

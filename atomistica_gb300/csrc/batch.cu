@@ -416,8 +416,16 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, doubl
     }
   }
   Neighbors &nl = b.nl;
-  if (nl.nbr.ensure(sizeof(int) * capacity) || nl.shift.ensure(sizeof(int) * capacity) ||
-      nl.rev.ensure(sizeof(int) * capacity) || nl.stage.ensure(sizeof(int2) * capacity) ||
+  // a list array that grows here loses the eager call's list: rebuild it next
+  const void *list0[3] = {nl.nbr.p, nl.shift.p, nl.rev.p};
+  const bool grew = nl.nbr.ensure(sizeof(int) * capacity) ||
+                    nl.shift.ensure(sizeof(int) * capacity) ||
+                    nl.rev.ensure(sizeof(int) * capacity);
+  if (nl.nbr.p != list0[0] || nl.shift.p != list0[1] || nl.rev.p != list0[2]) {
+    nl.valid = false;
+    nl.rev_valid = false;
+  }
+  if (grew || nl.stage.ensure(sizeof(int2) * capacity) ||
       pot.bond_G.ensure(sizeof(double) * 3 * capacity) ||
       pot.bond_e.ensure(sizeof(double) * capacity) ||
       pot.tile_part.ensure(sizeof(double) * 10 * b.ntiles + 64) ||

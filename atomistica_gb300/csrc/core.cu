@@ -616,8 +616,9 @@ __device__ __forceinline__ bool pair_test(const BinParams &bp, const float4 &pi,
                                           const int *__restrict__ swrap,
                                           const Pos4 *__restrict__ pos4, int sx, int sy, int sz,
                                           bool s1zero, float ox, float oy, float oz, float Erun,
-                                          float Ebase, float eA, int packed1, bool &have_ri,
-                                          Pos4 &ri, int &j, int &packed, bool &range_bad) {
+                                          float Ebase, float eA, int packed1, float clo,
+                                          float chi, bool &have_ri, Pos4 &ri, int &j,
+                                          int &packed, bool &range_bad) {
   const float u = 5.9604645e-8f;
   const int kZeroWrap = pack_shift(0, 0, 0);
   const float4 pj = spos[jq];
@@ -648,9 +649,9 @@ __device__ __forceinline__ bool pair_test(const BinParams &bp, const float4 &pi,
   const float d2f = dx * dx + dy * dy + dz * dz;
   const float B = 2.0f * E * (1.735f * (d2f + 1.0f) + 9.0f * E) + 12.0f * u * d2f;
   bool accept;
-  if (d2f + B < bp.cutoff_sq_lo) {
+  if (d2f + B < clo) {
     accept = true;
-  } else if (d2f - B > bp.cutoff_sq_hi) {
+  } else if (d2f - B > chi) {
     accept = false;
   } else {
     if (!have_ri) {
@@ -698,6 +699,7 @@ __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const floa
   int cnt = 0;
   bool have_ri = false;
   Pos4 ri;
+  const float clo = bp.cutoff_sq_lo, chi = bp.cutoff_sq_hi;  // (once per atom)
   for (int x = -bp.dx; x <= bp.dx; x++) {
     int cx = cx0 + x, sx = -q0;
     if (!wrap_cell(bp, 0, cx, sx)) continue;
@@ -730,7 +732,7 @@ __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const floa
           int j, packed;
           bool range_bad;
           if (pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz, Erun,
-                        Ebase, eA, packed1, have_ri, ri, j, packed, range_bad)) {
+                        Ebase, eA, packed1, clo, chi, have_ri, ri, j, packed, range_bad)) {
             pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
                               status);
             cnt++;
@@ -782,6 +784,7 @@ __global__ void __launch_bounds__(128)
   int cnt = 0;
   if (__all_sync(active, deep)) {
     const int kZeroWrap = pack_shift(0, 0, 0);
+    const float clo = bp.cutoff_sq_lo, chi = bp.cutoff_sq_hi;
     bool have_ri = false;
     Pos4 ri;
     for (int x = -bp.dx; x <= bp.dx; x++) {
@@ -792,7 +795,7 @@ __global__ void __launch_bounds__(128)
           int j, packed;
           bool range_bad;
           if (pair_test(bp, pi, i, jq, spos, swrap, pos4, 0, 0, 0, true, 0.0f, 0.0f, 0.0f, Ebase,
-                        Ebase, eA, kZeroWrap, have_ri, ri, j, packed, range_bad)) {
+                        Ebase, eA, kZeroWrap, clo, chi, have_ri, ri, j, packed, range_bad)) {
             pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
                               status);
             cnt++;
@@ -935,6 +938,7 @@ __global__ void __launch_bounds__(128)
       const int total = base;
       bool have_ri = false;
       Pos4 ri;
+      const float clo = bp.cutoff_sq_lo, chi = bp.cutoff_sq_hi;
       int r = 0, rs = -1, sx = 0, sy = 0, sz = 0, packed1 = 0;
       bool s1zero = true;
       float ox = 0.0f, oy = 0.0f, oz = 0.0f, Erun = Ebase;
@@ -961,7 +965,7 @@ __global__ void __launch_bounds__(128)
           }
           const int jq = s_js[grp][r] + (c - s_pre[grp][r]);
           accept = pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz,
-                             Erun, Ebase, eA, packed1, have_ri, ri, j, packed, range_bad);
+                             Erun, Ebase, eA, packed1, clo, chi, have_ri, ri, j, packed, range_bad);
         }
         const unsigned mine = (__ballot_sync(gmask, accept) >> (lane & 24)) & 0xFFu;
         if (accept)

@@ -162,3 +162,17 @@ def test_batch_autotune(gpu):
     assert info["tuned_candidates"] >= 1 and info["tile_bonds"] in (128, 192, 256)
     assert np.array_equal(f1, f0)  # per-bond sums do not depend on the tiles
     assert np.max(np.abs(e1 - e0)) <= 1e-12 * np.max(np.abs(e0))
+
+
+def test_batch_eager_after_capture_same_positions(gpu):
+    # the capture sizes the list arrays for its capacity; an eager call on
+    # unchanged positions afterwards must not use a list lost by that
+    from atomistica_gb300 import native
+    structs = S.si_batch(24, seed=45)
+    pot = native.Tersoff(precision="mixed")
+    b = native.Batch(structs)
+    b.set_options(graph=True)
+    e1, f1, w1 = b.energy_and_forces(pot)   # eager, then captured
+    b.set_options(graph=False)
+    e2, f2, w2 = b.energy_and_forces(pot)   # eager on the same positions
+    assert np.array_equal(f2, f1) and np.array_equal(e2, e1) and np.array_equal(w2, w1)
