@@ -564,8 +564,9 @@ bool single_graph_current(const Potential &pot, const Particles &p, const Neighb
          pot.graph_bufs == single_graph_buffers(pot, p, nl);
 }
 
-// Captures the evaluation into pot.graph (nothing runs).  fd: the device
-// force array the graph accumulates into (zeroed first when set_f).
+// Captures the evaluation into pot.graph (nothing runs).  fd: the force
+// array (device, or mapped page-locked host memory) the graph accumulates
+// into, or writes for every atom when set_f.
 void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, bool set_f,
                     cudaStream_t s) {
   drop_single_graph(pot);
@@ -629,6 +630,7 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
   const int ncells = bp.n[0] * bp.n[1] * bp.n[2];
   Outputs o;
   o.f = fd;
+  o.f_set = set_f;  // (every atom's force written: no zeroing first)
   o.red = pot.red.as<double>();
   o.status = reinterpret_cast<int *>(o.red + 12);
   BopSystem sys;
@@ -656,9 +658,7 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
     return;
   }
   int rc = 0;
-  if (set_f && cudaMemsetAsync(fd, 0, sizeof(double) * 3 * (size_t)nat, s) != cudaSuccess)
-    rc = -1;
-  if (rc == 0 && cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s) != cudaSuccess) rc = -1;
+  if (cudaMemsetAsync(o.status, 0, sizeof(int) * 4, s) != cudaSuccess) rc = -1;
   if (rc == 0) rc = nl_build(nl, nat, p.r.as<double>(), bp, nullptr, nullptr, ncells, s, true);
   if (rc == 0)
     rc = bop ? bop_run(pot, sys, nl, o, false, false)
@@ -748,17 +748,18 @@ int finish_results(Potential &pot, const double *hr, double *epot, double *wpot)
 }
 
 // Replays the captured evaluation; done = false when its list or tile plan
-// overflowed (the forces are then as before the call, or zero with set_f).
+// overflowed (the forces are then as before the call; with set_f they are
+// written by the eager call that follows).
 int single_replay(Potential &pot, Particles &p, Neighbors &nl, double *f, double *fd,
-                  bool f_host, bool set_f, double *epot, double *wpot, cudaStream_t s,
+                  bool staged, bool set_f, double *epot, double *wpot, cudaStream_t s,
                   bool &done) {
   done = false;
   const size_t nf = 3 * (size_t)p.nat;
   GB_CUDA(cudaEventRecord(pot.ev[0], s));
-  if (f_host && !set_f)
+  if (staged && !set_f)
     GB_CUDA(cudaMemcpyAsync(fd, f, sizeof(double) * nf, cudaMemcpyHostToDevice, s));
   GB_CUDA(cudaGraphLaunch(pot.graph_exec, s));
-  if (f_host) GB_CUDA(cudaMemcpyAsync(f, fd, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
+  if (staged) GB_CUDA(cudaMemcpyAsync(f, fd, sizeof(double) * nf, cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaEventRecord(pot.ev[3], s));
   GB_CUDA(cudaStreamSynchronize(s));
   note_launch(pot.graph_kernels);
@@ -834,12 +835,19 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
                         !mask && !epa && !wpa && !epb && !fpb && !wpb;
   double *gfd = nullptr;
   if (graph_ok) {
+    // the forces go to the caller's device array, to page-locked host memory
+    // directly when they are written (not accumulated), or through the
+    // staging buffer out_f (copied in and out around the replay)
     const bool fh = !is_device_ptr(f);
-    if (fh) GB_CHECK(pot.out_f.ensure(sizeof(double) * 3 * std::max<size_t>(nat, 1)));
-    gfd = fh ? pot.out_f.as<double>() : f;
+    gfd = !fh ? f : (set_f && pot.kind != kEAM ? mapped_host_ptr(f) : nullptr);
+    if (!gfd) {
+      GB_CHECK(pot.out_f.ensure(sizeof(double) * 3 * std::max<size_t>(nat, 1)));
+      gfd = pot.out_f.as<double>();
+    }
+    const bool staged = gfd == pot.out_f.as<double>();
     if (single_graph_current(pot, p, nl, gfd, set_f, s)) {
       bool done = false;
-      GB_CHECK(single_replay(pot, p, nl, f, gfd, fh, set_f, epot, wpot, s, done));
+      GB_CHECK(single_replay(pot, p, nl, f, gfd, staged, set_f, epot, wpot, s, done));
       if (done) {
         pot.last_replayed = true;
         pot.graph_unused = 0;
@@ -863,6 +871,13 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   }
   nl.stream = s;
   if (pot.precision == GB_PRECISION_MIXED) nl.want_posff = true;
+  // Forces that are written (not accumulated) go straight to their array:
+  // a device array, or page-locked host memory, which the gather writes over
+  // the host link while it computes (no staging copy).
+  // (the EAM pair kernel writes an atom's three values from one lane, which
+  // suits device memory only)
+  double *f_direct = nullptr;
+  if (set_f && nat > 0) f_direct = !f_host ? f : pot.kind != kEAM ? mapped_host_ptr(f) : nullptr;
   if (pot.kind != kEAM && !pot.screened) {
     // the bond-order kernels need the reverse index, and the list build can
     // plan their tiles (the size of the previous evaluation's tiles)
@@ -875,7 +890,12 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CUDA(cudaEventRecord(pot.ev[1], s));
 
   const size_t nb = (size_t)nl.nentries;
-  if (set_f) {
+  if (f_direct) {
+    // written by the force kernels in store mode (every atom)
+    sf.caller = sf.dev = f_direct;
+    sf.n = 3 * (size_t)nat;
+    sf.host = false;
+  } else if (set_f) {
     // nothing to upload: the forces start from zero on the device
     if (f_host) {
       GB_CHECK(pot.out_f.ensure(sizeof(double) * 3 * std::max<size_t>(nat, 1)));
@@ -901,6 +921,7 @@ int energy_and_forces(Potential &pot, Particles &p, Neighbors &nl, double *epot,
   GB_CHECK(stage_in(wpb, 9 * nb, pot.out_wpb, s, swpb));
   Outputs o;
   o.f = sf.dev;
+  o.f_set = f_direct != nullptr;
   o.epot_per_at = sepa.dev;
   o.wpot_per_at = swpa.dev;
   o.epot_per_bond = sepb.dev;

@@ -488,6 +488,7 @@ __global__ void __launch_bounds__(kBopThreads)
 }  // namespace
 }  // namespace gb
 
+constexpr int kGatherThreads = 128;  // threads per block of the per-atom gathers
 #include "bop_mixed.cuh"
 #include "bop_scr.cuh"
 
@@ -499,16 +500,17 @@ template <bool kEpa, bool kWat>
 __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__restrict__ rev,
                            const double *__restrict__ G, const double *__restrict__ ebond,
                            const double *__restrict__ wbond, double *__restrict__ f,
-                           double *__restrict__ epa, double *__restrict__ wpa, ReplayCheck chk) {
+                           double *__restrict__ epa, double *__restrict__ wpa, ReplayCheck chk,
+                           int fset) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nat || replay_invalid(chk)) return;
+  if (replay_invalid(chk)) return;  // (uniform over the grid)
   double F[3] = {0.0, 0.0, 0.0};
   double E = 0.0;
   double W[9];
   if (kWat)
 #pragma unroll
     for (int c = 0; c < 9; c++) W[c] = 0.0;
-  const int s = seed[i], e = seed[i + 1];
+  const int s = i < nat ? seed[i] : 0, e = i < nat ? seed[i + 1] : 0;
   for (int b = s; b < e; b++) {
     const int rb = rev[b];
     if (rb < 0) continue;  // (an incomplete list; reported by the reverse build)
@@ -519,8 +521,8 @@ __global__ void bop_gather(int nat, const int *__restrict__ seed, const int *__r
 #pragma unroll
       for (int c = 0; c < 9; c++) W[c] += wbond[9 * (size_t)b + c] + wbond[9 * (size_t)rb + c];
   }
-#pragma unroll
-  for (int c = 0; c < 3; c++) f[3 * (size_t)i + c] += F[c];
+  store_block_forces<kGatherThreads>(f, nat, F, fset);
+  if (i >= nat) return;
   if (kEpa) epa[i] += 0.5 * E;
   if (kWat)
 #pragma unroll
@@ -699,19 +701,20 @@ int dispatch_tile(const BopArgs &args, const Pot &pot, const float4 *posff, int 
 // the replayed list or tile plan overflowed (ReplayCheck, internal.h).
 int launch_gather(bool mixed, int nat, const int *seed, const int *rev, const double *G,
                   const double *ebond, const double *wbond, double *f, double *epa, double *wpa,
-                  cudaStream_t s, ReplayCheck chk = ReplayCheck{}) {
-  const int T = 128, nb = (nat + T - 1) / T;
+                  cudaStream_t s, ReplayCheck chk = ReplayCheck{}, bool fset = false) {
+  const int T = kGatherThreads, nb = (nat + T - 1) / T;
   const float2 *Gf = reinterpret_cast<const float2 *>(G);
+  const int fs = fset ? 1 : 0;
   if (mixed) {
-    if (epa && wpa) bop_gather_mx<true, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
-    else if (epa) bop_gather_mx<true, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
-    else if (wpa) bop_gather_mx<false, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
-    else bop_gather_mx<false, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk);
+    if (epa && wpa) bop_gather_mx<true, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk, fs);
+    else if (epa) bop_gather_mx<true, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk, fs);
+    else if (wpa) bop_gather_mx<false, true><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk, fs);
+    else bop_gather_mx<false, false><<<nb, T, 0, s>>>(nat, seed, rev, Gf, ebond, wbond, f, epa, wpa, chk, fs);
   } else {
-    if (epa && wpa) bop_gather<true, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
-    else if (epa) bop_gather<true, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
-    else if (wpa) bop_gather<false, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
-    else bop_gather<false, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk);
+    if (epa && wpa) bop_gather<true, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk, fs);
+    else if (epa) bop_gather<true, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk, fs);
+    else if (wpa) bop_gather<false, true><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk, fs);
+    else bop_gather<false, false><<<nb, T, 0, s>>>(nat, seed, rev, G, ebond, wbond, f, epa, wpa, chk, fs);
   }
   note_launch();
   GB_CUDA(cudaGetLastError());
@@ -906,7 +909,7 @@ int bop_run_scr(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outpu
   GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(false, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                          args.ebond, args.wbond, o.f, o.epot_per_at,
-                         want_wat ? o.wpot_per_at : nullptr, s));
+                         want_wat ? o.wpot_per_at : nullptr, s, ReplayCheck{}, o.f_set));
   GB_CHECK(pot.red_stage.ensure(reduce_stage_bytes(blocks) + 64));
   GB_CHECK(reduce_partials(args.tile_part, blocks, 10, o.red, pot.red_stage.as<double>(), s));
   pot.tile_atoms = 1;
@@ -1043,7 +1046,7 @@ int bop_run(Potential &pot, const BopSystem &sys, Neighbors &nl, const Outputs &
   if (!sys.capture) GB_CUDA(cudaEventRecord(pot.kev[1], s));
   GB_CHECK(launch_gather(mixed, nat_all, nl.seed.as<int>(), nl.rev.as<int>(), args.G,
                          args.ebond, args.wbond, o.f, o.epot_per_at,
-                         want_wat ? o.wpot_per_at : nullptr, s, sys.check));
+                         want_wat ? o.wpot_per_at : nullptr, s, sys.check, o.f_set));
   if (batch) {
     if (sys.piece0)
       GB_CHECK(reduce_seg_pieces(args.tile_part, sys.piece0, sys.npiece, sys.seg_piece, sys.nseg,

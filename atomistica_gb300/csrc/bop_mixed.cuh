@@ -997,16 +997,16 @@ __global__ void bop_gather_mx(int nat, const int *__restrict__ seed, const int *
                               const float2 *__restrict__ G, const double *__restrict__ ebond,
                               const double *__restrict__ wbond, double *__restrict__ f,
                               double *__restrict__ epa, double *__restrict__ wpa,
-                              ReplayCheck chk) {
+                              ReplayCheck chk, int fset) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nat || replay_invalid(chk)) return;
+  if (replay_invalid(chk)) return;  // (uniform over the grid)
   ff F[3] = {ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f), ff_make(0.0f, 0.0f)};
   double E = 0.0;
   double W[9];
   if (kWat)
 #pragma unroll
     for (int c = 0; c < 9; c++) W[c] = 0.0;
-  const int s = seed[i], e = seed[i + 1];
+  const int s = i < nat ? seed[i] : 0, e = i < nat ? seed[i + 1] : 0;
   for (int b = s; b < e; b++) {
     const int rb = rev[b];
     if (rb < 0) continue;  // (an incomplete list; reported by the reverse build)
@@ -1020,8 +1020,9 @@ __global__ void bop_gather_mx(int nat, const int *__restrict__ seed, const int *
 #pragma unroll
       for (int c = 0; c < 9; c++) W[c] += wbond[9 * (size_t)b + c] + wbond[9 * (size_t)rb + c];
   }
-#pragma unroll
-  for (int c = 0; c < 3; c++) f[3 * (size_t)i + c] += ff_to_double(F[c]);
+  const double Fd[3] = {ff_to_double(F[0]), ff_to_double(F[1]), ff_to_double(F[2])};
+  store_block_forces<kGatherThreads>(f, nat, Fd, fset);
+  if (i >= nat) return;
   if (kEpa) epa[i] += 0.5 * E;
   if (kWat)
 #pragma unroll

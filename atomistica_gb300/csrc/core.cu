@@ -102,6 +102,16 @@ bool is_device_ptr(const void *ptr) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+double *mapped_host_ptr(void *ptr) {
+  if (!ptr) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? static_cast<double *>(a.devicePointer) : nullptr;
+}
+
 Cell make_cell(const Particles &p) {
   Cell c;
   std::memcpy(c.A, p.A, sizeof(c.A));

@@ -324,6 +324,7 @@ struct EamArgs {
   double *part;           // 10 per block
   int *status;
   ReplayCheck chk;        // a replayed evaluation writes no forces when invalid
+  int fset;               // f is written for every atom (1) or accumulated into (0)
 };
 
 // simple_spline_f_and_df with extrapolate=.true. (:536-614).
@@ -612,11 +613,19 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
 #pragma unroll
     for (int c = 0; c < 6; c++) Wa[c] = group_sum(Wa[c]);
   double e_tot = 0.0;
+  if (a.fset && eli < 0 && i < a.nat && sub == 0 && !replay_invalid(a.chk))
+#pragma unroll
+    for (int c = 0; c < 3; c++) a.f[3 * (size_t)i + c] = 0.0;  // (skipped atom, written)
   if (eli >= 0) {
     if (mi) Ei += a.Fi[i];
     if (sub == 0 && !replay_invalid(a.chk)) {
 #pragma unroll
-      for (int c = 0; c < 3; c++) a.f[3 * (size_t)i + c] += F3[c];
+      for (int c = 0; c < 3; c++) {
+        if (a.fset)
+          a.f[3 * (size_t)i + c] = F3[c];
+        else
+          a.f[3 * (size_t)i + c] += F3[c];
+      }
       if (kEpa && mi) a.epa[i] += Ei;
       if (kWat)
 #pragma unroll
@@ -685,6 +694,7 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   a.part = pot.tile_part.as<double>();
   a.status = o.status;
   a.chk = chk;
+  a.fset = o.f_set ? 1 : 0;
   const bool ff = t.funcfl;
   if (ff)
     eam_density<true><<<blocks, kEamThreads, 0, s>>>(a);

@@ -68,6 +68,10 @@ void note_launch(int n = 1);
 
 // Does the pointer refer to device (or managed) memory?
 bool is_device_ptr(const void *ptr);
+// The device address of page-locked host memory that kernels may access
+// directly (mapped, as every page-locked allocation is under unified
+// addressing), or nullptr for other memory.
+double *mapped_host_ptr(void *ptr);
 
 // ---------------------------------------------------------------------------
 // Particles (python_particles.f90:85-140, set_cell :286-346).
@@ -112,6 +116,31 @@ struct ReplayCheck {
 __device__ __forceinline__ bool replay_invalid(const ReplayCheck &c) {
   return c.nl && !(c.nl[0] <= c.cap && (c.nl[1] & (1 | 2 | 8)) == 0 && (c.nl[4] & 4) == 0 &&
                    (c.tile[0] & 2) == 0);
+}
+
+// A block's per-atom forces (3 doubles per atom; atom blockIdx.x * kThreads +
+// threadIdx.x) written out through shared memory, so that consecutive
+// threads store consecutive doubles: coalesced lines in device memory, and
+// whole lines over the host link when f is page-locked host memory.  fset:
+// written, else accumulated into.  Every thread of the block takes part.
+template <int kThreads>
+__device__ __forceinline__ void store_block_forces(double *__restrict__ f, int nat,
+                                                   const double F[3], int fset) {
+  __shared__ double sf[3 * kThreads];
+  const int t = threadIdx.x;
+  const int a0 = blockIdx.x * kThreads;
+  sf[3 * t] = F[0];
+  sf[3 * t + 1] = F[1];
+  sf[3 * t + 2] = F[2];
+  __syncthreads();
+  const int n = 3 * (nat - a0 < kThreads ? nat - a0 : kThreads);
+  for (int k = t; k < n; k += kThreads) {
+    const size_t q = 3 * (size_t)a0 + k;
+    if (fset)
+      f[q] = sf[k];
+    else
+      f[q] += sf[k];
+  }
 }
 
 // (ij, ik) slots of an atom with z bonds in the bond-order tile kernels: its

@@ -54,6 +54,7 @@ int eam_upload(EamTables &t);
 struct Outputs {
   // Device pointers (accumulated into); NULL when not requested.
   double *f = nullptr;
+  bool f_set = false;  // f is written (every atom), not accumulated into
   double *epot_per_at = nullptr;
   double *wpot_per_at = nullptr;
   double *epot_per_bond = nullptr;

@@ -220,3 +220,47 @@ def test_new_force_array_every_call_stays_eager(gpu):
         e, _, _ = pot.energy_and_forces(p, nl, forces=f)
         assert not pot.last_replayed()
         assert e == e0 and torch.equal(f, fe)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_pinned_host_forces_written_directly(gpu, graph):
+    # forces written (not accumulated) into page-locked host memory go there
+    # straight from the gather; equal to the device-array result, also after
+    # the array held other values
+    import torch
+    s = rattled_diamond("Si", 5.431, (3, 3, 3), 0.1, 23)
+    dev = torch.device("cuda", 0)
+    pe, nle, pote = _setup(s, "Tersoff", "mixed", False)
+    fe = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+    e0, _, w0 = pote.energy_and_forces(pe, nle, forces=fe)
+    p, nl, pot = _setup(s, "Tersoff", "mixed", graph)
+    fh = torch.full((len(s), 3), 7.0, dtype=torch.float64).pin_memory()
+    fn = fh.numpy()
+    for call in range(3):
+        fn[...] = 7.0
+        e, _, w = pot.energy_and_forces(p, nl, forces=fn, accumulate=False)
+        assert e == e0 and np.array_equal(fn, fe.cpu().numpy()), call
+        assert np.array_equal(np.asarray(w), np.asarray(w0))
+    assert pot.last_replayed() == graph
+
+
+def test_eam_forces_written_for_skipped_atoms(gpu, tmp_path):
+    # store mode: atoms of elements the potential skips get zero forces even
+    # when the array held other values
+    import torch
+    from atomistica_gb300 import io as gio
+    from atomistica_gb300 import native
+    fn_ = gio.analytic_alloy_setfl(str(tmp_path / "a.setfl"), ["Cu", "Ag"], seed=4)
+    s = S.fcc("Cu", 3.7, (3, 3, 3))
+    s.numbers[::5] = 14  # not in the file
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    pot = native.TabulatedAlloyEAM(fn_)
+    pot.bind_to(p, nl)
+    dev = torch.device("cuda", 0)
+    f0 = torch.zeros((len(s), 3), dtype=torch.float64, device=dev)
+    pot.energy_and_forces(p, nl, forces=f0)
+    f1 = torch.full((len(s), 3), 3.0, dtype=torch.float64, device=dev)
+    pot.energy_and_forces(p, nl, forces=f1, accumulate=False)
+    assert torch.equal(f1, f0)
+    assert torch.all(f1[::5] == 0)
