@@ -259,6 +259,7 @@ void drop_graph(Batch &b) {
   b.graph = nullptr;
   b.graph_kernels = 0;
   b.graph_bufs.clear();
+  b.graph_fout = nullptr;
 }
 
 // Device buffers a captured evaluation writes or reads (their addresses are
@@ -316,8 +317,23 @@ int batch_forces(Batch &b, Potential &pot, double *fdev, cudaStream_t s, BopSyst
   return 0;
 }
 
-// epot set, wpot accumulated, per structure (as energy_and_forces).
-int batch_finish(Batch &b, Potential &pot, double *epot, double *wpot) {
+// Device outputs of batch_finish: epot[q] = row q's energy, wpot[q] += its
+// virial (rows of 10: energy, then the virial in Fortran order).
+__global__ void seg_results(int nseg, const double *__restrict__ rows, double *__restrict__ epot,
+                            double *__restrict__ wpot) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 10 * nseg) return;
+  const int q = k / 10, c = k % 10;
+  if (c == 0)
+    epot[q] = rows[k];
+  else
+    wpot[9 * (size_t)q + c - 1] += rows[k];
+}
+
+// epot set, wpot accumulated, per structure (as energy_and_forces).  Device
+// arrays are written on the stream from the device rows (no host copy);
+// host arrays from the page-locked copy of the rows.
+int batch_finish(Batch &b, Potential &pot, double *epot, double *wpot, cudaStream_t s) {
   const double *hs = b.hseg.as<double>();
   const double *hr = pot.hred.as<double>();
   const int st = reinterpret_cast<const int *>(hr + 12)[0];
@@ -329,6 +345,14 @@ int batch_finish(Batch &b, Potential &pot, double *epot, double *wpot) {
     return GB_ERROR_UNSPECIFIED;
   }
   const bool ed = is_device_ptr(epot), wd = is_device_ptr(wpot);
+  if (ed && wd) {
+    seg_results<<<(10 * b.nstruct + 255) / 256, 256, 0, s>>>(b.nstruct, b.red_seg.as<double>(),
+                                                             epot, wpot);
+    note_launch();
+    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cudaStreamSynchronize(s));  // results complete on return, as for host arrays
+    return 0;
+  }
   std::vector<double> e(b.nstruct), w(9 * (size_t)b.nstruct);
   if (wd)
     GB_CUDA(cudaMemcpy(w.data(), wpot, sizeof(double) * w.size(), cudaMemcpyDeviceToHost));
@@ -391,7 +415,8 @@ int batch_choose_budget(Batch &b, Potential &pot, cudaStream_t s) {
 // has sized everything; failures leave the eager path in use.
 // kind 0: one evaluation into gf; kind 1: a whole velocity-Verlet step of
 // time step dt (step1, gf = 0, evaluation, checked step2 into md_v / md_f).
-void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, double dt = 0.0) {
+void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, double dt = 0.0,
+                   double *fcall = nullptr) {
   drop_graph(b);
   const int cap = b.nl.stage_cap;
   if (cap <= 0 || b.nat == 0) return;
@@ -433,7 +458,22 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, doubl
     clear_error();
     return;
   }
+  // One evaluation for a device force array: the graph's gather adds into
+  // that array, and only when the replay is valid (the gather checks the
+  // list build's and the tile kernel's status words on the device), so an
+  // overflowed replay leaves the caller's forces untouched.
+  double *fout = b.gf.as<double>();
+  b.graph_fout = nullptr;
   BopSystem sys = batch_system(b);
+  if (kind == 0 && fcall && !b.graph_direct_off && is_device_ptr(fcall) &&
+      !pot.red.ensure(sizeof(double) * 16)) {
+    fout = fcall;
+    b.graph_fout = fcall;
+    sys.check.nl = nl.stats.as<int>();
+    sys.check.tile = reinterpret_cast<int *>(pot.red.as<double>() + 12);
+    sys.check.cap = cap;
+  }
+  clear_error();
   sys.capture = true;
   sys.nb_capacity = capacity;
   sys.max_nbt = max_nbt;
@@ -463,7 +503,7 @@ void batch_capture(Batch &b, Potential &pot, cudaStream_t s, int kind = 0, doubl
   if (rc == 0)
     rc = nl_build(nl, b.nat, b.r.as<double>(), dummy, b.bps.as<BinParams>(), b.sid.as<int>(),
                   b.ncells, s, true);
-  if (rc == 0) rc = batch_forces(b, pot, b.gf.as<double>(), s, sys);
+  if (rc == 0) rc = batch_forces(b, pot, fout, s, sys);
   if (rc == 0 && kind == 1) {
     md_kick<<<nbk, T, 0, s>>>(b.nat, b.md_v.as<double>(), b.gf.as<double>(), b.md_m.as<double>(),
                               dt, b.md_f.as<double>(), nl.stats.as<int>(),
@@ -530,13 +570,21 @@ int batch_replay(Batch &b, Potential &pot, double *epot, double *f, double *wpot
                  cudaStream_t s, bool &done) {
   done = false;
   const size_t nf = 3 * (size_t)b.nat;
-  GB_CUDA(cudaMemcpyAsync(b.gf.p, f, sizeof(double) * nf, cudaMemcpyDefault, s));
+  const bool direct = b.graph_fout != nullptr;
+  if (direct && f != b.graph_fout) {
+    // another force array: this graph would add into the old one
+    drop_graph(b);
+    b.graph_direct_off = true;
+    return 0;
+  }
+  if (!direct)
+    GB_CUDA(cudaMemcpyAsync(b.gf.p, f, sizeof(double) * nf, cudaMemcpyDefault, s));
   GB_CUDA(cudaGraphLaunch(b.graph_exec, s));
   GB_CUDA(cudaStreamSynchronize(s));
   note_launch(b.graph_kernels);
   const int *hs = b.nl.hstats.as<int>();
   const int *st = reinterpret_cast<const int *>(pot.hred.as<double>() + 12);
-  const bool ok = hs[0] <= b.graph_cap && (hs[1] & (1 | 2)) == 0 && (hs[5] & 4) == 0 &&
+  const bool ok = hs[0] <= b.graph_cap && (hs[1] & (1 | 2 | 8)) == 0 && (hs[5] & 4) == 0 &&
                   (st[0] & 2) == 0;
   if (!ok) {
     drop_graph(b);
@@ -550,8 +598,8 @@ int batch_replay(Batch &b, Potential &pot, double *epot, double *f, double *wpot
   b.nl.rev_pending = false;
   b.nl.posff_valid = b.nl.want_posff;
   b.built_pos = b.pos_rev;
-  GB_CUDA(cudaMemcpy(f, b.gf.p, sizeof(double) * nf, cudaMemcpyDefault));
-  GB_CHECK(batch_finish(b, pot, epot, wpot));
+  if (!direct) GB_CUDA(cudaMemcpy(f, b.gf.p, sizeof(double) * nf, cudaMemcpyDefault));
+  GB_CHECK(batch_finish(b, pot, epot, wpot, s));
   done = true;
   return 0;
 }
@@ -631,7 +679,7 @@ int batch_eager(Batch &b, Potential &pot, double *epot, double *f, double *wpot,
   cudaEventElapsedTime(&ms[3], pot.kev[0], pot.kev[1]);
   cudaGetLastError();
   for (int q = 0; q < 4; q++) pot.timing[q] = ms[q];
-  GB_CHECK(batch_finish(b, pot, epot, wpot));
+  GB_CHECK(batch_finish(b, pot, epot, wpot, s));
   b.info[1] = b.tiles_apt;
   b.info[3] = b.tune_candidates;
   return 0;
@@ -647,7 +695,8 @@ int batch_replay_md(Batch &b, Potential &pot, cudaStream_t s, bool &ok) {
   b.pos_rev++;  // the step moved the atoms
   const int *hs = b.nl.hstats.as<int>();
   const int *st = reinterpret_cast<const int *>(pot.hred.as<double>() + 12);
-  ok = hs[0] <= b.graph_cap && (hs[1] & (1 | 2)) == 0 && (hs[5] & 4) == 0 && (st[0] & 2) == 0;
+  ok = hs[0] <= b.graph_cap && (hs[1] & (1 | 2 | 8)) == 0 && (hs[5] & 4) == 0 &&
+       (st[0] & 2) == 0;
   if (!ok) {
     drop_graph(b);
     b.nl.valid = false;
@@ -687,7 +736,7 @@ int batch_energy_and_forces(Batch &b, Potential &pot, double *epot, double *f, d
     }
   }
   GB_CHECK(batch_eager(b, pot, epot, f, wpot, s, cutoff));
-  if (b.use_graph && !b.graph_failed && !graph_current(b, pot)) batch_capture(b, pot, s);
+  if (b.use_graph && !b.graph_failed && !graph_current(b, pot)) batch_capture(b, pot, s, 0, 0.0, f);
   b.info[2] = b.graph_kernels;
   return 0;
 }
@@ -739,7 +788,7 @@ int batch_md_run(Batch &b, Potential &pot, double dt, int nsteps, double *epot, 
       GB_CHECK(batch_replay_md(b, pot, s, ok));
       if (ok) {
         std::fill(b.md_w.begin(), b.md_w.end(), 0.0);
-        GB_CHECK(batch_finish(b, pot, b.md_e.data(), b.md_w.data()));
+        GB_CHECK(batch_finish(b, pot, b.md_e.data(), b.md_w.data(), s));
         b.info[0] = 1;
         continue;
       }

@@ -62,6 +62,11 @@ struct Batch {
   std::vector<double> md_e, md_w;  // per-structure energies / virials of the last step
   std::vector<const void *> graph_bufs;
   DevBuf gf;  // forces accumulated by the graph
+  // A graph of one evaluation captured for a device force array of the
+  // caller accumulates into that array directly (graph_fout); a call with
+  // another array drops such a graph, and later graphs use gf.
+  double *graph_fout = nullptr;
+  bool graph_direct_off = false;
   int64_t info[4] = {0, 0, 0, 0};  // last call: replayed, bonds/tile, kernels in graph, tuned
   ~Batch();
 };

@@ -176,3 +176,63 @@ def test_batch_eager_after_capture_same_positions(gpu):
     b.set_options(graph=False)
     e2, f2, w2 = b.energy_and_forces(pot)   # eager on the same positions
     assert np.array_equal(f2, f1) and np.array_equal(e2, e1) and np.array_equal(w2, w1)
+
+
+def test_batch_graph_device_arrays(gpu):
+    # Device force arrays: the graph captured for the caller's array adds into
+    # it directly (no staging copies); energies and virials are written on the
+    # device.  An overflowed replay must leave the array untouched before the
+    # eager redo, and another array must not be written through the old graph.
+    import torch
+    from atomistica_gb300 import native
+    structs = S.si_batch(24, seed=46)
+    r0 = np.concatenate([s.positions for s in structs])
+    nat = len(r0)
+    pot = native.Tersoff(precision="mixed")
+
+    def reference(r):
+        ref = native.Batch(structs)
+        ref.set_positions(r)
+        fr = torch.full((nat, 3), 0.5, dtype=torch.float64, device="cuda")
+        e, _, w = ref.energy_and_forces(pot, forces=fr)
+        return e.cpu().numpy(), fr.cpu().numpy(), w.cpu().numpy()
+
+    def call(b, f):
+        f.fill_(0.5)
+        e, _, w = b.energy_and_forces(pot, forces=f)
+        return e.cpu().numpy(), f.cpu().numpy(), w.cpu().numpy(), b.last_info()["replayed"]
+
+    e0, f0, w0 = reference(r0)
+    b = native.Batch(structs)
+    b.set_options(graph=True)
+    f = torch.zeros((nat, 3), dtype=torch.float64, device="cuda")
+    for k in range(3):  # eager (then captured), then replays into the same array
+        e, fg, w, rep = call(b, f)
+        assert rep == (k > 0)
+        assert np.array_equal(fg, f0) and np.array_equal(e, e0) and np.array_equal(w, w0)
+    dense = r0.copy()
+    sl = slice(int(b.offsets[0]), int(b.offsets[1]))
+    c = dense[sl].mean(axis=0)
+    dense[sl] = c + 0.6 * (dense[sl] - c)
+    ed, fd, wd = reference(dense)
+    b.set_positions(dense)
+    e, fg, w, rep = call(b, f)
+    assert not rep
+    assert np.array_equal(fg, fd) and np.array_equal(e, ed) and np.array_equal(w, wd)
+    # (the dense configuration re-cut the tiles: from here on the energies and
+    # virials may differ from the reference by the rounding of the tile sums;
+    # the forces do not depend on the tiles)
+    b.set_positions(r0)
+    call(b, f)
+    e, fg, w, rep = call(b, f)
+    assert rep and np.array_equal(fg, f0)
+    f2 = torch.zeros((nat, 3), dtype=torch.float64, device="cuda")
+    e, fg, w, rep = call(b, f2)  # another array: not through the old graph
+    assert not rep and np.array_equal(fg, f0)
+    # (the mixed form adds virials in FP32 per tile)
+    assert np.allclose(e, e0, rtol=1e-12, atol=0)
+    assert np.max(np.abs(w - w0)) <= 1e-5 * np.max(np.abs(w0))
+    for arr in (f2, f, f2):  # later graphs stage through their own buffer
+        e1, fg, w1, rep = call(b, arr)
+        assert rep and np.array_equal(fg, f0)
+        assert np.array_equal(e1, e) and np.array_equal(w1, w)

@@ -26,6 +26,44 @@ def _nl_check(s, cutoff, got):
     assert np.array_equal(sorted_triples(seed, j, dc), ref.triples())
 
 
+def _strained(s, eps):
+    s = s.copy()
+    F = np.eye(3) + np.asarray(eps)
+    s.positions = s.positions @ F.T
+    s.cell = s.cell @ F.T
+    return s
+
+
+# Structures above the small-structure size of the pair search (one thread,
+# or one warp-flattened walk, per atom): cubic boxes (rows and cells beyond
+# the cutoff skipped), a slab, a sheared box and atoms outside the box.
+LARGE_NL = {
+    "amorphous_65536": lambda: S.tersoff_si_amorphous(65536, seed=5),
+    "amorphous_262144": lambda: S.tersoff_si_amorphous(262144, seed=6, sigma=0.4),
+    "slab_65536": lambda: _nopbc(S.tersoff_si_amorphous(65536, seed=7), [True, True, False]),
+    "sheared_65536": lambda: _strained(S.tersoff_si_amorphous(65536, seed=8),
+                                       [[0, 0.03, 0], [0, 0, 0], [0.02, 0, 0]]),
+    "outside_65536": lambda: _rattle(S.tersoff_si_amorphous(65536, seed=9), 2.0, 10),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LARGE_NL))
+def test_neighbour_list_large(gpu, name):
+    # First build (count and fill passes), then a rebuild on moved positions
+    # (single pass with staged entries): both bit-exact and in the
+    # reference's per-atom order.
+    from atomistica_gb300 import native
+    s = LARGE_NL[name]()
+    p = native.from_atoms(s)
+    nl = native.Neighbors(100)
+    nl.request_interaction_range(3.0)
+    _nl_check(s, 3.0, nl.get_list(p))
+    s2 = _rattle(s.copy(), 0.05, 11)
+    p.coordinates[:] = s2.positions
+    p.I_changed_positions()
+    _nl_check(s2, 3.0, nl.get_list(p))
+
+
 CASES = {
     "si_4096": lambda: S.tersoff_si_4096(),
     "si_rattled": lambda: rattled_diamond(amp=0.4, seed=1),
