@@ -678,6 +678,35 @@ __device__ __forceinline__ bool pair_test(const BinParams &bp, const float4 &pi,
   return accept;
 }
 
+// Shortcuts of the candidate loops.  A warp runs a candidate step for all
+// its lanes at once, so the common cases are kept short and the band test of
+// pair_test is left to the rare ones:
+//   d2' = |(p_i + A s) - p_j|^2 in FP32 (the run's image offset added to p_i
+//         first), for a j without own wrap (its image offset is the run's);
+//   reject  d2' > thi (about nine candidates in ten), or j = i in a run
+//           without image shift;
+//   accept  d2' < tlo;
+//   otherwise (the FP32 band around the cutoff, a wrapped j) pair_test.
+// thi and tlo are where pair_test's band test (d2f -+ B against chi / clo,
+// B = a d2f + b, a = 3.47 E + 12 u, b = 3.47 E + 18 E^2) starts to reject /
+// still accepts: thi = (chi + b) / (1 - a) raised and tlo = (clo - b) /
+// (1 + a) lowered by a relative 1e-6.  Each component error of the lean
+// evaluation is within the same E as pair_test's order for every pair
+// closer than the cutoff (u (3X + 4T + |d|) <= E), so both shortcuts make
+// the reference's decision.
+__device__ __forceinline__ void band_thresholds(float clo, float chi, float E, float &tlo,
+                                                float &thi) {
+  const float u = 5.9604645e-8f;
+  const float a = 3.47f * E + 12.0f * u, b = 3.47f * E + 18.0f * E * E;
+  thi = (chi + b) / (1.0f - a) * (1.0f + 1e-6f);
+  tlo = (clo - b) / (1.0f + a) * (1.0f - 1e-6f);
+}
+// Whether a packed image shift is outside the packed range.
+__device__ __forceinline__ bool shift_out_of_range(int sx, int sy, int sz) {
+  return sx > kMaxShift || sx < -kMaxShift || sy > kMaxShift || sy < -kMaxShift ||
+         sz > kMaxShift || sz < -kMaxShift;
+}
+
 // An accepted entry number pos of atom i, as kMode stores it.
 template <int kMode>
 __device__ __forceinline__ void pair_store(int i, int pos, int j, int packed, bool range_bad,
@@ -696,9 +725,9 @@ __device__ __forceinline__ void pair_store(int i, int pos, int j, int packed, bo
 
 // The whole stencil of atom i (sorted slot t, cell (cx0, cy0, cz0), wrap q)
 // walked on one thread in the reference's order; returns its entry count.
-template <int kMode>
-__device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const float4 &pi, int cx0,
-                                          int cy0, int cz0, int q0, int q1, int q2, float Ebase,
+template <int kMode, bool kLean>
+__device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, int t, const float4 &pi,
+                                          int cx0, int cy0, int cz0, int q0, int q1, int q2, float Ebase,
                                           float eA, const Pos4 *__restrict__ pos4,
                                           const float4 *__restrict__ spos,
                                           const int *__restrict__ swrap,
@@ -706,6 +735,7 @@ __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const floa
                                           int *__restrict__ nbr, int *__restrict__ shift,
                                           int2 *__restrict__ stage, int cap,
                                           int *__restrict__ status) {
+  const int kZeroWrap = pack_shift(0, 0, 0);
   int cnt = 0;
   bool have_ri = false;
   Pos4 ri;
@@ -738,11 +768,38 @@ __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const floa
           Erun += eA * (fabsf(fx) + fabsf(fy) + fabsf(fz));
         }
         const int packed1 = pack_shift(sx, sy, sz);
+        if (!kLean) {
+          for (int jq = js; jq < je; jq++) {
+            int j, packed;
+            bool range_bad;
+            if (pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz, Erun,
+                          Ebase, eA, packed1, clo, chi, have_ri, ri, j, packed, range_bad)) {
+              pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
+                                status);
+              cnt++;
+            }
+          }
+          continue;
+        }
+        const bool run_bad = shift_out_of_range(sx, sy, sz);
+        float tlo, thi;
+        band_thresholds(clo, chi, Erun, tlo, thi);
+        const float px = pi.x + ox, py = pi.y + oy, pz = pi.z + oz;
+        const int self_slot = s1zero ? t : -1;
         for (int jq = js; jq < je; jq++) {
-          int j, packed;
-          bool range_bad;
-          if (pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz, Erun,
-                        Ebase, eA, packed1, clo, chi, have_ri, ri, j, packed, range_bad)) {
+          const float4 pj = spos[jq];
+          const int wj = swrap[jq];
+          const float dx = px - pj.x, dy = py - pj.y, dz = pz - pj.z;
+          const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          const bool plain = wj == kZeroWrap;
+          if (plain && (d2 > thi || jq == self_slot)) continue;
+          int j = __float_as_int(pj.w), packed = packed1;
+          bool range_bad = run_bad;
+          bool acc = plain && d2 < tlo;
+          if (!acc)
+            acc = pair_test(bp, pi, i, jq, spos, swrap, pos4, sx, sy, sz, s1zero, ox, oy, oz, Erun,
+                            Ebase, eA, packed1, clo, chi, have_ri, ri, j, packed, range_bad);
+          if (acc) {
             pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
                               status);
             cnt++;
@@ -754,8 +811,18 @@ __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, const floa
   return cnt;
 }
 
+// Resident blocks per SM asked of the compiler: the pair search is bound by
+// the latency of its candidate loads, and more resident warps (fewer
+// registers, a few spilled) hide more of it (measured at 1,048,576 atoms).
+#ifndef GB_PAIRS_MIN_BLOCKS
+#define GB_PAIRS_MIN_BLOCKS 12
+#endif
+#ifndef GB_PAIRS_MIN_BLOCKS_BATCH
+#define GB_PAIRS_MIN_BLOCKS_BATCH 8
+#endif
+
 template <int kMode, bool kBatch>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, kBatch ? GB_PAIRS_MIN_BLOCKS_BATCH : GB_PAIRS_MIN_BLOCKS)
     nl_pairs(int nat, BinParams bp0, const BinParams *__restrict__ bps,
              const int *__restrict__ sid, const Pos4 *__restrict__ pos4,
              const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
@@ -795,6 +862,8 @@ __global__ void __launch_bounds__(128)
   if (__all_sync(active, deep)) {
     const int kZeroWrap = pack_shift(0, 0, 0);
     const float clo = bp.cutoff_sq_lo, chi = bp.cutoff_sq_hi;
+    float tlo0, thi0;
+    band_thresholds(clo, chi, Ebase, tlo0, thi0);
     bool have_ri = false;
     Pos4 ri;
     for (int x = -bp.dx; x <= bp.dx; x++) {
@@ -802,10 +871,20 @@ __global__ void __launch_bounds__(128)
         const int row = cell_linear(bp, cx0 + x, cy0 + y, 0);
         const int js = cell_start[row + cz0 - bp.dz], je = cell_start[row + cz0 + bp.dz + 1];
         for (int jq = js; jq < je; jq++) {
-          int j, packed;
-          bool range_bad;
-          if (pair_test(bp, pi, i, jq, spos, swrap, pos4, 0, 0, 0, true, 0.0f, 0.0f, 0.0f, Ebase,
-                        Ebase, eA, kZeroWrap, clo, chi, have_ri, ri, j, packed, range_bad)) {
+          const float4 pj = spos[jq];
+          const int wj = swrap[jq];
+          const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+          const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          const bool plain = wj == kZeroWrap;
+          if (plain && (d2 > thi0 || jq == t)) continue;
+          int j = __float_as_int(pj.w), packed = kZeroWrap;
+          bool range_bad = false;
+          bool acc = plain && d2 < tlo0;
+          if (!acc)
+            acc = pair_test(bp, pi, i, jq, spos, swrap, pos4, 0, 0, 0, true, 0.0f, 0.0f, 0.0f,
+                            Ebase, Ebase, eA, kZeroWrap, clo, chi, have_ri, ri, j, packed,
+                            range_bad);
+          if (acc) {
             pair_store<kMode>(i, cnt, j, packed, range_bad, seed_i, nbr, shift, stage, cap,
                               status);
             cnt++;
@@ -814,8 +893,9 @@ __global__ void __launch_bounds__(128)
       }
     }
   } else {
-    cnt = pairs_walk<kMode>(bp, i, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4, spos, swrap,
-                            cell_start, seed_i, nbr, shift, stage, cap, status);
+    cnt = pairs_walk<kMode, kBatch>(bp, i, t, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4,
+                                    spos, swrap, cell_start, seed_i, nbr, shift, stage, cap,
+                                    status);
   }
   if (kMode != kPairsFill) {
     // clamp: the staged single pass without a host check (captured graphs)
@@ -984,8 +1064,9 @@ __global__ void __launch_bounds__(128)
         cnt += __popc(mine);
       }
     } else if (g == 0) {
-      cnt = pairs_walk<kMode>(bp, i, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4, spos, swrap,
-                              cell_start, seed_i, nbr, shift, stage, cap, status);
+      cnt = pairs_walk<kMode, false>(bp, i, t, pi, cx0, cy0, cz0, q0, q1, q2, Ebase, eA, pos4,
+                                     spos, swrap, cell_start, seed_i, nbr, shift, stage, cap,
+                                     status);
     }
     cnt = __shfl_sync(gmask, cnt, 0, G);
   }
