@@ -811,18 +811,24 @@ __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, int t, con
   return cnt;
 }
 
-// Resident blocks per SM asked of the compiler: the pair search is bound by
-// the latency of its candidate loads, and more resident warps (fewer
-// registers, a few spilled) hide more of it (measured at 1,048,576 atoms).
+// Threads per block and resident threads per SM asked of the compiler (1536
+// for a single structure, 1024 for batches): the pair search is bound by the
+// latency of its candidate loads, and more resident warps (fewer registers,
+// a few spilled) hide more of it (measured at 1,048,576 atoms).
+#ifndef GB_PAIRS_THREADS
+#define GB_PAIRS_THREADS 128
+#endif
 #ifndef GB_PAIRS_MIN_BLOCKS
-#define GB_PAIRS_MIN_BLOCKS 12
+#define GB_PAIRS_MIN_BLOCKS (1536 / GB_PAIRS_THREADS)
 #endif
 #ifndef GB_PAIRS_MIN_BLOCKS_BATCH
-#define GB_PAIRS_MIN_BLOCKS_BATCH 8
+#define GB_PAIRS_MIN_BLOCKS_BATCH (1024 / GB_PAIRS_THREADS)
 #endif
+constexpr int kPairsThreads = GB_PAIRS_THREADS;
 
 template <int kMode, bool kBatch>
-__global__ void __launch_bounds__(128, kBatch ? GB_PAIRS_MIN_BLOCKS_BATCH : GB_PAIRS_MIN_BLOCKS)
+__global__ void __launch_bounds__(kPairsThreads,
+                                  kBatch ? GB_PAIRS_MIN_BLOCKS_BATCH : GB_PAIRS_MIN_BLOCKS)
     nl_pairs(int nat, BinParams bp0, const BinParams *__restrict__ bps,
              const int *__restrict__ sid, const Pos4 *__restrict__ pos4,
              const int *__restrict__ atom_cell, const float4 *__restrict__ spos,
@@ -1367,7 +1373,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
                    int2 *stage, int cap, int clamp = 0) {
     constexpr int kMode = decltype(mode_tag)::value;
     if (batch)
-      nl_pairs<kMode, true><<<(nat + 127) / 128, 128, 0, stream>>>(
+      nl_pairs<kMode, true><<<(nat + kPairsThreads - 1) / kPairsThreads, kPairsThreads, 0,
+                              stream>>>(
           nat, bp0, bps, sid, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(), nl.spos.as<float4>(),
           nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr, shift, stage, cap,
           clamp, status);
@@ -1378,7 +1385,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
                                       nl.cell_start.as<int>(), counts, seed, nbr, shift, stage,
                                       cap, clamp, status);
     else
-      nl_pairs<kMode, false><<<(nat + 127) / 128, 128, 0, stream>>>(
+      nl_pairs<kMode, false><<<(nat + kPairsThreads - 1) / kPairsThreads, kPairsThreads, 0,
+                               stream>>>(
           nat, bp0, nullptr, nullptr, nl.pos4.as<Pos4>(), nl.atom_cell.as<int>(),
           nl.spos.as<float4>(), nl.swrap.as<int>(), nl.cell_start.as<int>(), counts, seed, nbr,
           shift, stage, cap, clamp, status);

@@ -90,3 +90,49 @@ def test_md_energy_conservation(gpu):
     drift = abs((e1.sum() + k1) - (e0.sum() + k0)) / n
     assert drift < 1e-4, drift
     assert abs(k1 - k0) / n > 1e-6  # the system did move
+
+
+def _md_states(structs, v, m, prec, graph, plan):
+    from atomistica_gb300 import native
+    b = native.Batch(structs)
+    b.set_options(graph=graph)
+    b.md_set_state(v, m)
+    pot = native.Tersoff(precision=prec)
+    for item in plan:
+        if isinstance(item, int):
+            e, w = b.md_run(pot, DT, item)
+        else:
+            b.set_positions(item)
+    return (e, w) + b.md_get_state()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_md_overflow_falls_back(gpu, prec):
+    # A captured step that outgrows the captured list capacity leaves the
+    # second half kick undone and is redone eagerly.  Two ways to get there:
+    # positions compressed between runs (the first replayed step overflows),
+    # and a cluster driven inward so that its coordination grows during the
+    # run.  Either way the trajectory equals the eager one bitwise.
+    structs, v, m = _system(64)
+    r0 = np.concatenate([s.positions for s in structs])
+    dense = r0.copy()
+    n0 = len(structs[0])
+    c = dense[:n0].mean(axis=0)
+    dense[:n0] = c + 0.75 * (dense[:n0] - c)
+    plan = [12, dense, 21]
+    a = _md_states(structs, v, m, prec, False, plan)
+    g = _md_states(structs, v, m, prec, True, plan)
+    for x, y in zip(a, g):
+        assert np.array_equal(x, y)
+
+    cl = rattled_diamond("Si", 5.431 * 1.15, (2, 2, 2), 0.05, 65)
+    cl.cell = cl.cell * 2.0  # a cluster in vacuum
+    cl.positions = cl.positions + 0.25 * np.diag(cl.cell)
+    centre = cl.positions.mean(axis=0)
+    vin = -0.35 * (cl.positions - centre)
+    mc = np.full(len(cl), M_SI)
+    a = _md_states([cl], vin, mc, prec, False, [40])
+    g = _md_states([cl], vin, mc, prec, True, [40])
+    for x, y in zip(a, g):
+        assert np.array_equal(x, y)
+    assert np.all(np.isfinite(g[2]))
