@@ -725,10 +725,13 @@ __device__ __forceinline__ void pair_store(int i, int pos, int j, int packed, bo
 
 // The whole stencil of atom i (sorted slot t, cell (cx0, cy0, cz0), wrap q)
 // walked on one thread in the reference's order; returns its entry count.
+// kLean: the candidate steps take the shortcuts above (the batch walk); else
+// every candidate takes pair_test (the single-structure walk, where the
+// shortcuts' extra registers cost more than they save).
 template <int kMode, bool kLean>
 __device__ __forceinline__ int pairs_walk(const BinParams &bp, int i, int t, const float4 &pi,
-                                          int cx0, int cy0, int cz0, int q0, int q1, int q2, float Ebase,
-                                          float eA, const Pos4 *__restrict__ pos4,
+                                          int cx0, int cy0, int cz0, int q0, int q1, int q2,
+                                          float Ebase, float eA, const Pos4 *__restrict__ pos4,
                                           const float4 *__restrict__ spos,
                                           const int *__restrict__ swrap,
                                           const int *__restrict__ cell_start, int seed_i,
@@ -859,8 +862,9 @@ __global__ void __launch_bounds__(kPairsThreads,
   // Inside the cell grid (no row of the stencil needs a periodic wrap, the
   // atom is not wrapped): every row is one run of 2 dz + 1 cells with a zero
   // image shift, so a whole warp of such atoms takes a lean walk (the same
-  // rows, runs, candidates and decisions as pairs_walk; a wrapped j still
-  // brings its own shift through pair_test).
+  // rows, runs, candidates and decisions as pairs_walk, with the shortcut
+  // candidate steps; a wrapped j still brings its own shift through
+  // pair_test).
   const bool deep = !kBatch && (q0 | q1 | q2) == 0 && cx0 >= bp.dx &&
                     cx0 < bp.n[0] - bp.dx && cy0 >= bp.dy && cy0 < bp.n[1] - bp.dy &&
                     cz0 >= bp.dz && cz0 < bp.n[2] - bp.dz;
