@@ -551,7 +551,7 @@ std::vector<const void *> single_graph_buffers(const Potential &pot, const Parti
           nl.spos.p,      nl.swrap.p,     nl.seed.p,      nl.nbr.p,      nl.shift.p,
           nl.rev.p,       nl.stage.p,     nl.scan_tmp.p,  nl.stats.p,    nl.hstats.p,
           pot.bond_G.p,   pot.bond_e.p,   pot.tile_part.p, pot.red.p,    pot.hred.p,
-          pot.red_stage.p, pot.out_f.p};
+          pot.red_stage.p, pot.out_f.p, pot.eam_cache.p};
 }
 
 bool single_graph_current(const Potential &pot, const Particles &p, const Neighbors &nl,
@@ -603,6 +603,9 @@ void single_capture(Potential &pot, Particles &p, Neighbors &nl, double *fd, boo
       clear_error();
       return;
     }
+  } else if (eam_cache_ensure(pot, capacity)) {
+    clear_error();
+    return;
   }
   // every buffer at its captured size now: nothing may be allocated inside
   // (the EAM kernels' per-atom and per-block buffers depend on nat only and

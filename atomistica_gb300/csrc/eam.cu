@@ -325,6 +325,12 @@ struct EamArgs {
   int *status;
   ReplayCheck chk;        // a replayed evaluation writes no forces when invalid
   int fset;               // f is written for every atom (1) or accumulated into (0)
+  // Per-entry cache written by the density pass and read by the force pass
+  // (tables on one shared r grid): spline coordinate B, 1/r, and the
+  // interval as 2 k + (coordinate out of the table ? 1 : 0), or -1 for an
+  // entry the force pass skips (unknown element, beyond the cutoff).
+  double *cB, *cRinv;
+  int *cK;
 };
 
 // simple_spline_f_and_df with extrapolate=.true. (:536-614).
@@ -453,7 +459,7 @@ __device__ __forceinline__ double rsqrt_nr(double r2) {
   return fma(y, e, y);
 }
 
-template <bool kFuncfl>
+template <bool kFuncfl, bool kCache>
 __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
   const int gt = blockIdx.x * kEamThreads + threadIdx.x;
   const int i = gt / kEamLanes, sub = gt % kEamLanes;
@@ -465,13 +471,19 @@ __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
   }
   double rho = 0.0;
   bool bad = false;
-  if (on) {
+  // kCache: every entry of an atom of a known element (the force pass visits
+  // them whether or not the atom is in the mask) gets its cache row; the
+  // density itself only for atoms in the mask.
+  if (kCache ? eli >= 0 : on) {
     const Pos4 pi = a.pos[i];
     const int s = a.seed[i], e = a.seed[i + 1];
     for (int b = s + sub; b < e; b += kEamLanes) {
       const int j = a.nbr[b];
       const int elj = a.el[j];
-      if (elj < 0) continue;
+      if (elj < 0) {
+        if (kCache) a.cK[b] = -1;
+        continue;
+      }
       double d[3];
       get_drj(a, pi, a.pos[j], a.shift[b], d);
       const double r2 = norm2_ref(d);
@@ -483,8 +495,17 @@ __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
           inline_interval(a.rho[elj], sqrt(r2), B, k, ok);
         else
           r_interval(a.rho[elj], sqrt(r2), B, k, ok);
-        bad |= !ok;
-        rho += interval_f(a.rho[elj], k, B);
+        if (kCache) {
+          a.cB[b] = B;
+          a.cRinv[b] = rsqrt_nr(r2);
+          a.cK[b] = 2 * k + (ok ? 0 : 1);
+        }
+        if (on) {
+          bad |= !ok;
+          rho += interval_f(a.rho[elj], k, B);
+        }
+      } else if (kCache) {
+        a.cK[b] = -1;
       }
     }
   }
@@ -516,7 +537,7 @@ __device__ __forceinline__ int sym_index(int c2, int c) {
   return c2 == c ? c : 2 + c2 + c;  // (0,1) -> 3, (0,2) -> 4, (1,2) -> 5
 }
 
-template <bool kEpa, bool kWat, bool kFuncfl>
+template <bool kEpa, bool kWat, bool kFuncfl, bool kCache>
 __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
   __shared__ double sred[kEamThreads / 32][7];
   const int gt = blockIdx.x * kEamThreads + threadIdx.x;
@@ -535,31 +556,45 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
     const int s = a.seed[i], e = a.seed[i + 1];
     for (int b = s + sub; b < e; b += kEamLanes) {
       const int j = a.nbr[b];
-      const int elj = a.el[j];
-      if (elj < 0) continue;
-      double d[3];
-      get_drj(a, pi, a.pos[j], a.shift[b], d);
-      const double r2 = norm2_ref(d);
-      if (!(r2 < a.cutoff_sq)) continue;
-      const bool mj = !(a.mask && a.mask[j] == 0);
-      const double r = sqrt(r2);  // rounded as the reference's (table coordinate)
-      const double rinv = rsqrt_nr(r2);
       // rho and phi share the r grid: one interval for all three splines
-      const SplineDev &sp = a.phi[eli * a.nel + elj];
-      double B;
-      int k;
+      double B, rinv;
+      int k, elj;
       bool ok;
+      double d[3];
+      if (kCache) {
+        // the density pass's coordinate, 1/r and interval of this entry
+        const int kk = a.cK[b];
+        if (kk < 0) continue;
+        elj = a.el[j];
+        get_drj(a, pi, a.pos[j], a.shift[b], d);
+        B = a.cB[b];
+        rinv = a.cRinv[b];
+        k = kk >> 1;
+        ok = (kk & 1) == 0;
+      } else {
+        elj = a.el[j];
+        if (elj < 0) continue;
+        get_drj(a, pi, a.pos[j], a.shift[b], d);
+        const double r2 = norm2_ref(d);
+        if (!(r2 < a.cutoff_sq)) continue;
+        const double r = sqrt(r2);  // rounded as the reference's (table coordinate)
+        rinv = rsqrt_nr(r2);
+        if (kFuncfl)
+          inline_interval(a.phi[eli * a.nel + elj], r, B, k, ok);
+        else
+          r_interval(a.phi[eli * a.nel + elj], r, B, k, ok);
+      }
+      const bool mj = !(a.mask && a.mask[j] == 0);
+      const SplineDev &sp = a.phi[eli * a.nel + elj];
       double phi, dphi, pair;
       if (kFuncfl) {
         // Z(r): pair energy Z^2 / r, its derivative 2 Z Z' / r - Z^2 / r^2
         // (tabulated_eam.f90:301-304)
-        inline_interval(sp, r, B, k, ok);
         double z, dz;
         interval_fdf(sp, k, B, z, dz);
         phi = z * z * rinv;
         pair = 2 * z * dz * rinv - phi * rinv;
       } else {
-        r_interval(sp, r, B, k, ok);
         interval_fdf(sp, k, B, phi, dphi);
         pair = (dphi - phi * rinv) * rinv;
         phi = phi * rinv;
@@ -654,6 +689,26 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
 
 }  // namespace
 
+// Whether every rho and phi table of the file lies on one r grid (the
+// density pass's interval of an entry is then the force pass's too).
+static bool eam_shared_grid(const EamTables &t) {
+  if (t.drho.empty()) return false;
+  const SplineDev &g = t.drho[0];
+  auto same = [&](const SplineDev &q) {
+    return q.n == g.n && q.x0 == g.x0 && q.dx == g.dx && q.rdx == g.rdx && q.cut == g.cut;
+  };
+  for (const auto &q : t.drho)
+    if (!same(q)) return false;
+  for (const auto &q : t.dphi)
+    if (!same(q)) return false;
+  return true;
+}
+
+int eam_cache_ensure(Potential &pot, int64_t entries) {
+  if (entries < 0) entries = 0;
+  return pot.eam_cache.ensure(20 * (size_t)std::max<int64_t>(entries, 1));
+}
+
 int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
                 bool want_wat, ReplayCheck chk, bool capture) {
   cudaStream_t s = pot.stream;
@@ -696,18 +751,39 @@ int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs
   a.chk = chk;
   a.fset = o.f_set ? 1 : 0;
   const bool ff = t.funcfl;
+  // The per-entry cache needs one r grid for every rho and phi table (true
+  // of setfl and funcfl files) and room for the list: its entries now, or the
+  // captured capacity (sized before the capture began).
+  const int64_t entries = capture ? (int64_t)nat * nl.stage_cap : (int64_t)nl.nentries;
+  const bool cache = eam_shared_grid(t) && eam_cache_ensure(pot, entries) == 0;
+  clear_error();
+  a.cB = nullptr;
+  a.cRinv = nullptr;
+  a.cK = nullptr;
+  if (cache) {
+    const size_t cap = pot.eam_cache.bytes / 20;
+    a.cB = pot.eam_cache.as<double>();
+    a.cRinv = a.cB + cap;
+    a.cK = reinterpret_cast<int *>(a.cRinv + cap);
+  }
   if (ff)
-    eam_density<true><<<blocks, kEamThreads, 0, s>>>(a);
+    cache ? eam_density<true, true><<<blocks, kEamThreads, 0, s>>>(a)
+          : eam_density<true, false><<<blocks, kEamThreads, 0, s>>>(a);
   else
-    eam_density<false><<<blocks, kEamThreads, 0, s>>>(a);
+    cache ? eam_density<false, true><<<blocks, kEamThreads, 0, s>>>(a)
+          : eam_density<false, false><<<blocks, kEamThreads, 0, s>>>(a);
   note_launch();
   const bool epa = o.epot_per_at != nullptr;
   // the funcfl kernel of the reference leaves wpot_per_at untouched
   const bool wat = want_wat && !ff;
   if (!capture) GB_CUDA(cudaEventRecord(pot.kev[0], s));
   auto pair = [&](auto epa_t, auto wat_t, auto ff_t) {
-    eam_pair<decltype(epa_t)::value, decltype(wat_t)::value, decltype(ff_t)::value>
-        <<<blocks, kEamThreads, 0, s>>>(a);
+    if (cache)
+      eam_pair<decltype(epa_t)::value, decltype(wat_t)::value, decltype(ff_t)::value, true>
+          <<<blocks, kEamThreads, 0, s>>>(a);
+    else
+      eam_pair<decltype(epa_t)::value, decltype(wat_t)::value, decltype(ff_t)::value, false>
+          <<<blocks, kEamThreads, 0, s>>>(a);
     note_launch();
   };
   using T = std::true_type;

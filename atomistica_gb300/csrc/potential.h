@@ -95,6 +95,7 @@ struct Potential {
   // Scratch.
   DevBuf bond_G, bond_e, bond_w, bond_fr, tile_part, red;
   DevBuf atom_dF;
+  DevBuf eam_cache;  // per list entry: spline coordinate, 1/r, interval (EAM density pass)
   DevBuf red_stage;  // first-stage sums of the tile partials
   DevBuf out_f, out_epa, out_wpa, out_epb, out_fpb, out_wpb, mask_d;
   // Ghost-atom calls (a caller's list over local + ghost atoms, no image
@@ -145,6 +146,9 @@ double bop_pair_range(const Potential &pot, int t);
 int bop_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
                 bool want_wat, bool want_per_bond);
 // (chk, capture: a captured evaluation, see ReplayCheck; no event records)
+// Per-entry cache of the EAM density pass (spline coordinate, 1/r and
+// interval of each list entry, 20 bytes), sized for `entries` list entries.
+int eam_cache_ensure(Potential &pot, int64_t entries);
 int eam_compute(Potential &pot, const Particles &p, Neighbors &nl, const Outputs &o,
                 bool want_wat, ReplayCheck chk = ReplayCheck{}, bool capture = false);
 // Element count / atomic number of element q of the potential; its stream.
