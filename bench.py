@@ -248,19 +248,19 @@ def cpu_baseline(structure, params, runs, nthreads=None):
 
 
 def _gpu_step_ms(pot, p, nl, d_pos, d_f, steps=20):
-    """Mean device time (ms) of set_positions + energy_and_forces."""
+    """Mean device time (ms) of set_positions + energy_and_forces (forces
+    written into d_f, as the reference's call without a forces argument
+    returns a fresh array)."""
     import torch
     for _ in range(3):
-        d_f.zero_()
         p.set_positions(d_pos)
-        pot.energy_and_forces(p, nl, forces=d_f)
+        pot.energy_and_forces(p, nl, forces=d_f, accumulate=False)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(steps):
-        d_f.zero_()
         p.set_positions(d_pos)
-        pot.energy_and_forces(p, nl, forces=d_f)
+        pot.energy_and_forces(p, nl, forces=d_f, accumulate=False)
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / steps
@@ -745,10 +745,10 @@ def run_ours(args):
 
     def step(pot):
         pp, nn = next(where[k] for k, v in pots.items() if v is pot)
-        with torch.cuda.stream(stream):
-            d_f.zero_()
         pp.set_positions(d_pos)   # marks positions changed -> full neighbour rebuild
-        return pot.energy_and_forces(pp, nn, forces=d_f)
+        # forces written (every atom), as the reference's call without a
+        # forces argument returns a fresh array
+        return pot.energy_and_forces(pp, nn, forces=d_f, accumulate=False)
 
     def timed(pot, k, sampler=None):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -900,7 +900,8 @@ def run_ours(args):
                    "potential": "Tersoff_PRB_39_5566_Si_C", "parallelism": "replicas" if ws > 1
                    else "single GPU", "l2": "flushed between steps (256 MB write outside the "
                                             "timed events)",
-                   "step": "set_positions (D2D) + energy_and_forces incl. full neighbour "
+                   "step": "set_positions (D2D) + energy_and_forces (forces written, "
+                           "accumulate=False) incl. full neighbour "
                            "rebuild, replayed as one CUDA graph (Tersoff.set_graph(True), "
                            "gb_potential_set_graph; results equal the eager path's bit for "
                            "bit, checked below)"},
