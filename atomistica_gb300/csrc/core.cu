@@ -1126,32 +1126,45 @@ __global__ void nl_compact(int nat, int cap, const int *__restrict__ seed,
 // (j, s) at stage[i cap + k], goes to nbr / shift at seed[i] + k, and its
 // reverse (j -> i, -s) is looked up among j's staged entries instead of in the
 // compacted arrays: rev = seed[j] + its position.  Four entries of i at a
-// time, so that their loads (seed[j], then the first 32-byte sector of j's
-// staged row: its first four entries; cap is a multiple of 4) overlap.
+// time per thread, so that their loads (seed[j], then the first 32-byte
+// sector of j's staged row: its first four entries; cap is a multiple of 4)
+// overlap.
+#ifndef GB_COMPACT_LANES
+#define GB_COMPACT_LANES 2
+#endif
+constexpr int kCompactLanes = GB_COMPACT_LANES;  // threads per atom
+
 __global__ void nl_compact_reverse(int nat, int cap, const int *__restrict__ seed,
                                    const int2 *__restrict__ stage, int *__restrict__ nbr,
                                    int *__restrict__ shift, int *__restrict__ rev,
                                    int *__restrict__ status) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // kCompactLanes threads per atom take its entries in turn (entry k on lane
+  // k mod kCompactLanes), four at a time
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / kCompactLanes, lane = t % kCompactLanes;
   if (i >= nat) return;
   const int s = seed[i], n = seed[i + 1] - s;
   const int2 *src = stage + (size_t)i * cap;
-  for (int k0 = 0; k0 < n; k0 += 4) {
+  for (int k0 = lane; k0 < n; k0 += 4 * kCompactLanes) {
     int2 v[4];
     int want[4], cj[4], nj[4], found[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) v[q] = k0 + q < n ? src[k0 + q] : make_int2(i, 0);
+    for (int q = 0; q < 4; q++) {
+      const int k = k0 + q * kCompactLanes;
+      v[q] = k < n ? src[k] : make_int2(i, 0);
+    }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      if (k0 + q < n) {
-        nbr[s + k0 + q] = v[q].x;
-        shift[s + k0 + q] = v[q].y;
+      const int k = k0 + q * kCompactLanes;
+      if (k < n) {
+        nbr[s + k] = v[q].x;
+        shift[s + k] = v[q].y;
       }
       int s0, s1, s2;
       unpack_shift(v[q].y, s0, s1, s2);
       want[q] = pack_shift(-s0, -s1, -s2);
       cj[q] = seed[v[q].x];
-      nj[q] = k0 + q < n ? seed[v[q].x + 1] - cj[q] : 0;
+      nj[q] = k < n ? seed[v[q].x + 1] - cj[q] : 0;
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -1167,14 +1180,15 @@ __global__ void nl_compact_reverse(int nat, int cap, const int *__restrict__ see
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      if (k0 + q >= n) continue;
+      const int k = k0 + q * kCompactLanes;
+      if (k >= n) continue;
       const int2 *row = stage + (size_t)v[q].x * cap;
       for (int c = 4; c < nj[q] && found[q] < 0; c++) {
         const int2 e = row[c];
         if (e.x == i && e.y == want[q]) found[q] = c;
       }
       if (found[q] < 0) atomicOr(&status[1], 4);
-      rev[s + k0 + q] = found[q] < 0 ? -1 : cj[q] + found[q];
+      rev[s + k] = found[q] < 0 ? -1 : cj[q] + found[q];
     }
   }
 }
@@ -1427,7 +1441,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
     // the status words in hstats for the caller to check after the replay.
     if (nat > 0 && nl.want_rev && nl.stage_cap <= 32) {
       // (rev sized for nat * cap entries by the caller, like nbr and shift)
-      nl_compact_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(
+      nl_compact_reverse<<<(unsigned)(((int64_t)nat * kCompactLanes + 127) / 128), 128, 0,
+                           stream>>>(
           nat, nl.stage_cap, nl.seed.as<int>(), nl.stage.as<int2>(), nl.nbr.as<int>(),
           nl.shift.as<int>(), nl.rev.as<int>(), status + 3);
       note_launch();
@@ -1489,7 +1504,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
       // compaction and reverse index together (the symmetry flag is read
       // by the caller's next synchronisation, as after neighbors_build_reverse)
       GB_CHECK(nl.rev.ensure(sizeof(int) * std::max<int64_t>(total, 1)));
-      nl_compact_reverse<<<(nat + 127) / 128, 128, 0, stream>>>(
+      nl_compact_reverse<<<(unsigned)(((int64_t)nat * kCompactLanes + 127) / 128), 128, 0,
+                           stream>>>(
           nat, nl.stage_cap, nl.seed.as<int>(), nl.stage.as<int2>(), nl.nbr.as<int>(),
           nl.shift.as<int>(), nl.rev.as<int>(), status + 3);
       note_launch();
