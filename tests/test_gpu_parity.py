@@ -280,6 +280,7 @@ def test_mixed_precision_amorphous_workload(gpu, natoms):
     ref = oracle.bop_compute("tersoff", TERSOFF, s)
     g64 = gpu_bop("tersoff", s, per_at=False)
     gmx = gpu_bop("tersoff", s, precision="mixed", per_at=False)
+    _nl_check(s, 3.0, g64["nl"])  # the full pair set, in the reference's order
     assert np.max(np.abs(g64["f"] - ref["f"])) < 1e-9
     assert abs(g64["epot"] - ref["epot"]) / natoms < 1e-10
     dfm = np.max(np.abs(gmx["f"] - ref["f"]))
