@@ -97,6 +97,7 @@ SIGNATURES = [
                                               _P]),
     ("gb_kernel_launches", ctypes.c_uint64, []),
     ("gb_bench_fma_peak", _I, [_I, _P]),
+    ("gb_diag_sqrt_check", _I, [ctypes.c_int64, ctypes.c_double, ctypes.c_double, _P]),
 ]
 
 

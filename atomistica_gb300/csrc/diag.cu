@@ -58,8 +58,46 @@ int measure(double *tflops) {
   return 0;
 }
 
+// sqrt_from_rsqrt against the correctly rounded sqrt for n arguments drawn
+// uniformly from [lo, hi] (a counter-based hash, argument k for index k).
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void sqrt_check(int64_t n, double lo, double hi, unsigned long long *bad) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long mine = 0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += stride) {
+    const double u = (double)(mix64((uint64_t)k) >> 11) * (1.0 / 9007199254740992.0);
+    const double x = lo + (hi - lo) * u;
+    mine += sqrt_from_rsqrt(x, rsqrt_refined(x)) != sqrt(x);
+  }
+  if (mine) atomicAdd(bad, mine);
+}
+
 }  // namespace
 }  // namespace gb
+
+extern "C" int gb_diag_sqrt_check(int64_t n, double lo, double hi, int64_t *mismatches) {
+  gb::clear_error();
+  if (!mismatches || n < 0 || !(lo > 0.0) || !(hi >= lo)) return GB_ERROR_ARGUMENT;
+  unsigned long long *bad = nullptr;
+  GB_CUDA(cudaMalloc(&bad, sizeof(unsigned long long)));
+  GB_CUDA(cudaMemset(bad, 0, sizeof(unsigned long long)));
+  int dev = 0, sms = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  gb::sqrt_check<<<sms * 8, 256>>>(n, lo, hi, bad);
+  gb::note_launch();
+  unsigned long long h = 0;
+  const cudaError_t e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  GB_CUDA(e);
+  *mismatches = (int64_t)h;
+  return 0;
+}
 
 extern "C" int gb_bench_fma_peak(int fp64, double *tflops) {
   gb::clear_error();

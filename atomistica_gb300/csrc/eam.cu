@@ -451,13 +451,6 @@ __device__ __forceinline__ double interval_df(const SplineDev &s, int k, double 
   return c.x + B * (c.y + B * d.x);
 }
 
-// 1/sqrt(r2) to about an ulp: the hardware reciprocal square root refined by
-// one Newton step, y (1 + (1/2 - r2/2 y^2)).
-__device__ __forceinline__ double rsqrt_nr(double r2) {
-  const double y = rsqrt(r2);
-  const double e = fma(-0.5 * r2 * y, y, 0.5);
-  return fma(y, e, y);
-}
 
 template <bool kFuncfl, bool kCache>
 __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
@@ -491,13 +484,17 @@ __global__ void __launch_bounds__(kEamThreads) eam_density(const EamArgs a) {
         double B;
         int k;
         bool ok;
+        // kCache: 1/r is cached as well, and r derived from it (the correctly
+        // rounded square root, see sqrt_from_rsqrt)
+        const double rinv = kCache ? rsqrt_refined(r2) : 0.0;
+        const double r = kCache ? sqrt_from_rsqrt(r2, rinv) : sqrt(r2);
         if (kFuncfl)
-          inline_interval(a.rho[elj], sqrt(r2), B, k, ok);
+          inline_interval(a.rho[elj], r, B, k, ok);
         else
-          r_interval(a.rho[elj], sqrt(r2), B, k, ok);
+          r_interval(a.rho[elj], r, B, k, ok);
         if (kCache) {
           a.cB[b] = B;
-          a.cRinv[b] = rsqrt_nr(r2);
+          a.cRinv[b] = rinv;
           a.cK[b] = 2 * k + (ok ? 0 : 1);
         }
         if (on) {
@@ -578,7 +575,7 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
         const double r2 = norm2_ref(d);
         if (!(r2 < a.cutoff_sq)) continue;
         const double r = sqrt(r2);  // rounded as the reference's (table coordinate)
-        rinv = rsqrt_nr(r2);
+        rinv = rsqrt_refined(r2);
         if (kFuncfl)
           inline_interval(a.phi[eli * a.nel + elj], r, B, k, ok);
         else

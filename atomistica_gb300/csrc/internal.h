@@ -118,6 +118,24 @@ __device__ __forceinline__ bool replay_invalid(const ReplayCheck &c) {
                    (c.tile[0] & 2) == 0);
 }
 
+// 1/sqrt(x) to about an ulp: the hardware reciprocal square root refined by
+// one Newton step, y (1 + (1/2 - x/2 y^2)).
+__device__ __forceinline__ double rsqrt_refined(double x) {
+  const double y = rsqrt(x);
+  const double e = fma(-0.5 * x * y, y, 0.5);
+  return fma(y, e, y);
+}
+// sqrt(x) from y = rsqrt_refined(x): s = x y and one correction with the
+// residual x - s^2 computed by an FMA (Markstein's method); it equals the
+// correctly rounded square root for every argument the tests draw (see
+// gb_diag_sqrt_check), so a kernel that needs both sqrt(x) and 1/sqrt(x)
+// pays for one hardware approximation.
+__device__ __forceinline__ double sqrt_from_rsqrt(double x, double y) {
+  const double s = x * y;
+  const double e = fma(-s, s, x);
+  return fma(e, 0.5 * y, s);
+}
+
 // A block's per-atom forces (3 doubles per atom; atom blockIdx.x * kThreads +
 // threadIdx.x) written out through shared memory, so that consecutive
 // threads store consecutive doubles: coalesced lines in device memory, and

@@ -507,6 +507,11 @@ uint64_t gb_kernel_launches(void);
 /* FMA-chain microbenchmark on the current device: sustained FP64 (fp64=1)
  * or FP32 (fp64=0) throughput in TFLOP/s (2 flops per FMA). */
 int gb_bench_fma_peak(int fp64, double *tflops);
+/* Device check of the square root the EAM density pass derives from its
+ * refined reciprocal square root: *mismatches = how many of n arguments,
+ * drawn uniformly from [lo, hi] (lo > 0), differ from the correctly rounded
+ * sqrt.  Diagnostic; no counterpart in the reference. */
+int gb_diag_sqrt_check(int64_t n, double lo, double hi, int64_t *mismatches);
 /* Host-only generator of the random workload structures: nat uniform
  * positions (pos: nat x 3, Cartesian) in the cell (rows = lattice vectors)
  * with every pair, over all periodic images, at least dmin apart (random

@@ -256,6 +256,21 @@ def test_eam_fp64(gpu, tmp_path, size, sigma):
     _nl_check(s, 5.0, got["nl"])
 
 
+def test_derived_sqrt_is_correctly_rounded(gpu):
+    # The EAM density pass derives r from its refined 1/sqrt(r^2) (one FMA
+    # residual correction) instead of a separate square root; near a setfl
+    # table's zero padding the interval coordinate needs r rounded exactly as
+    # the correctly rounded sqrt.  2^27 arguments per range: the squared
+    # distances of the tables and a wider range.
+    import ctypes
+    from atomistica_gb300 import _lib
+    L = _lib.load()
+    for lo, hi in ((1e-2, 1.0), (1.0, 100.0), (1e-6, 1e6)):
+        bad = ctypes.c_int64(-1)
+        assert L.gb_diag_sqrt_check(1 << 27, lo, hi, ctypes.byref(bad)) == 0
+        assert bad.value == 0, (lo, hi, bad.value)
+
+
 def test_eam_mask(gpu, tmp_path):
     fn = _cu_setfl(tmp_path, nr=2000, nrho=2000)
     rng = np.random.default_rng(71)
