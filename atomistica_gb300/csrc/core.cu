@@ -242,28 +242,33 @@ size_t scan_tmp_ints(int n) {
 
 }  // namespace
 
-// Small inputs (n <= 16384): one block of 1024 threads, 16 consecutive
-// elements each, and the total out[n]: one launch.
+// Small inputs (n <= 16384): one block of 1024 threads and the total out[n],
+// one launch.  Warp w scans elements [512 w, 512 w + 512) as 16 rows of 32
+// (coalesced loads and stores, 16 independent shuffle scans per warp), then
+// the 32 warp totals are scanned and added.
 constexpr int kScanSmallThreads = 1024, kScanSmallPer = 16;
 __global__ void __launch_bounds__(kScanSmallThreads)
     scan_small(const int *__restrict__ in, int *__restrict__ out, int n) {
   __shared__ int warp_tot[kScanSmallThreads / 32];
-  const int base = threadIdx.x * kScanSmallPer;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int base = wid * (32 * kScanSmallPer) + lane;
   int v[kScanSmallPer];
-  int s = 0;
+#pragma unroll
+  for (int q = 0; q < kScanSmallPer; q++) v[q] = base + 32 * q < n ? in[base + 32 * q] : 0;
+  int run = 0;
 #pragma unroll
   for (int q = 0; q < kScanSmallPer; q++) {
-    v[q] = base + q < n ? in[base + q] : 0;
-    s += v[q];
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int incl = s;
+    int x = v[q];
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    const int row = __shfl_sync(0xffffffffu, x, 31);
+    v[q] = run + x - v[q];  // exclusive within the warp's chunk
+    run += row;
   }
-  if (lane == 31) warp_tot[wid] = incl;
+  if (lane == 0) warp_tot[wid] = run;
   __syncthreads();
   if (wid == 0) {
     int w = warp_tot[lane];
@@ -275,13 +280,11 @@ __global__ void __launch_bounds__(kScanSmallThreads)
     warp_tot[lane] = w;
   }
   __syncthreads();
-  int run = incl - s + (wid > 0 ? warp_tot[wid - 1] : 0);
+  const int off = wid > 0 ? warp_tot[wid - 1] : 0;
 #pragma unroll
-  for (int q = 0; q < kScanSmallPer; q++) {
-    if (base + q < n) out[base + q] = run;
-    run += v[q];
-  }
-  if (threadIdx.x == kScanSmallThreads - 1) out[n] = run;
+  for (int q = 0; q < kScanSmallPer; q++)
+    if (base + 32 * q < n) out[base + 32 * q] = v[q] + off;
+  if (threadIdx.x == 0) out[n] = warp_tot[kScanSmallThreads / 32 - 1];
 }
 
 int exclusive_scan_i32(const int *in, int *out, int n, DevBuf &tmp, cudaStream_t stream) {
@@ -1100,26 +1103,40 @@ __global__ void __launch_bounds__(128)
 }
 
 // CSR from the staged entries (every atom has at most cap of them).
+// Staged entries to the CSR: G consecutive lanes per atom take its entries k
+// = lane, lane + G, ..., so that a group's loads of the staged row and its
+// stores to nbr / shift are contiguous runs (one thread per atom wrote each
+// entry to a different sector of its warp's stores).
+template <int G>
 __global__ void nl_compact(int nat, int cap, const int *__restrict__ seed,
                            const int2 *__restrict__ stage, int *__restrict__ nbr,
                            int *__restrict__ shift) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t / G), lane = (int)(t % G);
   if (i >= nat) return;
   const int s = seed[i], n = seed[i + 1] - s;
   const int2 *src = stage + (size_t)i * cap;
-  // four independent loads in flight per thread
-  for (int k = 0; k < n; k += 4) {
-    int2 v[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      if (k + q < n) v[q] = src[k + q];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      if (k + q < n) {
-        nbr[s + k + q] = v[q].x;
-        shift[s + k + q] = v[q].y;
-      }
+  for (int k = lane; k < n; k += G) {
+    const int2 v = src[k];
+    nbr[s + k] = v.x;
+    shift[s + k] = v.y;
   }
+}
+
+// Lanes per atom for nl_compact from the staging capacity (an upper bound of
+// the entries per atom, 1.25 x the previous maximum + 4).
+cudaError_t launch_compact(int nat, int cap, const int *seed, const int2 *stage, int *nbr,
+                           int *shift, cudaStream_t stream) {
+  const int g = cap <= 16 ? 4 : cap <= 48 ? 8 : 16;
+  const unsigned blocks = (unsigned)(((int64_t)nat * g + 127) / 128);
+  if (g == 4)
+    nl_compact<4><<<blocks, 128, 0, stream>>>(nat, cap, seed, stage, nbr, shift);
+  else if (g == 8)
+    nl_compact<8><<<blocks, 128, 0, stream>>>(nat, cap, seed, stage, nbr, shift);
+  else
+    nl_compact<16><<<blocks, 128, 0, stream>>>(nat, cap, seed, stage, nbr, shift);
+  note_launch();
+  return cudaGetLastError();
 }
 
 // nl_compact and the reverse index in one pass: entry k of atom i, staged as
@@ -1449,10 +1466,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
       GB_CUDA(cudaMemcpyAsync(hs + 5, status + 4, sizeof(int), cudaMemcpyDeviceToHost, stream));
       nl.rev_pending = true;
     } else if (nat > 0) {
-      nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
-                                                        nl.stage.as<int2>(), nl.nbr.as<int>(),
-                                                        nl.shift.as<int>());
-      note_launch();
+      GB_CUDA(launch_compact(nat, nl.stage_cap, nl.seed.as<int>(), nl.stage.as<int2>(),
+                             nl.nbr.as<int>(), nl.shift.as<int>(), stream));
     }
     GB_CUDA(cudaMemcpyAsync(hs, status, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream));
     GB_CUDA(cudaMemcpyAsync(hs + 4, nl.seed.as<int>() + nat, sizeof(int), cudaMemcpyDeviceToHost,
@@ -1512,10 +1527,8 @@ int nl_build(Neighbors &nl, int nat, const double *r, const BinParams &bp0,
       GB_CUDA(cudaMemcpyAsync(hs + 5, status + 4, sizeof(int), cudaMemcpyDeviceToHost, stream));
       nl.rev_pending = true;
     } else if (nl.stage_cap > 0 && maxz <= nl.stage_cap) {
-      nl_compact<<<(nat + 127) / 128, 128, 0, stream>>>(nat, nl.stage_cap, nl.seed.as<int>(),
-                                                        nl.stage.as<int2>(), nl.nbr.as<int>(),
-                                                        nl.shift.as<int>());
-      note_launch();
+      GB_CUDA(launch_compact(nat, nl.stage_cap, nl.seed.as<int>(), nl.stage.as<int2>(),
+                             nl.nbr.as<int>(), nl.shift.as<int>(), stream));
     } else {
       pairs(std::integral_constant<int, kPairsFill>(), nullptr, nl.seed.as<int>(),
             nl.nbr.as<int>(), nl.shift.as<int>(), nullptr, 0);

@@ -263,6 +263,11 @@ def _gpu_step_ms(pot, p, nl, d_pos, d_f, steps=20):
         pot.energy_and_forces(p, nl, forces=d_f, accumulate=False)
     e1.record()
     torch.cuda.synchronize()
+    # whether the timed steps were graph replays: one more step with the
+    # same arguments (the flag of a call is only visible after it)
+    p.set_positions(d_pos)
+    pot.energy_and_forces(p, nl, forces=d_f, accumulate=False)
+    _gpu_step_ms.replayed = pot.last_replayed()
     return e0.elapsed_time(e1) / steps
 
 
@@ -303,6 +308,7 @@ def other_configs(dev, oracle):
         if "graph" in name:
             pot.set_graph(True)
         ms = _gpu_step_ms(pot, pq, nq, d_pos, d_f)
+        replayed = _gpu_step_ms.replayed
         d_f.zero_()
         pq.set_positions(d_pos)
         e, _, w = pot.energy_and_forces(pq, nq, forces=d_f)
@@ -311,7 +317,7 @@ def other_configs(dev, oracle):
                        "max_abs_dF": float(np.max(np.abs(f - ref["f"]))),
                        "abs_dE_per_atom": abs(e - ref["epot"]) / len(s)}
         if "graph" in name:
-            entry[name]["replayed"] = pot.last_replayed()
+            entry[name]["replayed"] = replayed
     out["tersoff_si_4096"] = entry
     out["tersoff_scr"] = screened_config(dev, oracle, nth, cpu_time)
     out["md_si_4096"] = md_config()
@@ -364,11 +370,12 @@ def eam_config(dev, oracle, nth, cpu_time):
         potg.bind_to(pg, nlg)
         potg.set_graph(True)
         ms_g = _gpu_step_ms(potg, pg, nlg, d_pos, d_f)
+        replayed_g = _gpu_step_ms.replayed
         d_f.zero_()
         pg.set_positions(d_pos)
         e_g, _, _ = potg.energy_and_forces(pg, nlg, forces=d_f)
         graph = {"value": len(s) / (ms_g * 1e-3), "ms_per_step": ms_g,
-                 "replayed": potg.last_replayed(),
+                 "replayed": replayed_g,
                  "equals_eager": bool(e_g == e and np.array_equal(d_f.cpu().numpy(), f))}
     from atomistica_gb300 import _lib
     fp64_peak = _peak(_lib.load(), True)
