@@ -410,8 +410,9 @@ __device__ __forceinline__ void r_interval(const SplineDev &s, double r, double 
   double q = u * s.rdx;
   q = fma(fma(-q, s.dx, u), s.rdx, q);
   const double xf = q + 1.0;
-  const double fl = floor(xf);
-  int i = (int)fmin(fmax(fl, -1.0e9), 1.0e9);
+  // floor as one rounding-down conversion (r is finite and below the cutoff
+  // at every call, and the conversion saturates)
+  int i = __double2int_rd(xf);
   ok = i >= 1 && (i < s.n || r <= s.cut);
   i = min(max(i, 1), s.n - 1);
   B = xf - i;
@@ -597,6 +598,9 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
         phi = phi * rinv;
       }
       double fac_i = 0.0;
+      // f_i += (sc_i + sc_j) d: the i-side term df = sc_i d and the j-side
+      // term of the mirror entry, -df' = sc_j d, added as one coefficient
+      double sc_f = 0.0;
       if (mi) {
         // i-side of entry (i->j), :577-607: df = sc d, f_i += df,
         // w += -d (x) df
@@ -604,10 +608,8 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
         fac_i = interval_df(a.rho[elj], k, B);
         const double sc = -(dFi * fac_i + pair) * rinv;
         Ei += phi;
+        sc_f = sc;
         const double df[3] = {sc * d[0], sc * d[1], sc * d[2]};
-        F3[0] += df[0];
-        F3[1] += df[1];
-        F3[2] += df[2];
         const double w[6] = {-d[0] * df[0], -d[1] * df[1], -d[2] * df[2],
                              -d[0] * df[1], -d[0] * df[2], -d[1] * df[2]};
 #pragma unroll
@@ -621,11 +623,9 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
         bad |= !ok;
         const double fac_j = (mi && elj == eli) ? fac_i : interval_df(a.rho[eli], k, B);
         const double sc = -(a.dFi[j] * fac_j + pair) * rinv;
-        const double dfp[3] = {-sc * d[0], -sc * d[1], -sc * d[2]};
-        F3[0] -= dfp[0];
-        F3[1] -= dfp[1];
-        F3[2] -= dfp[2];
+        sc_f += sc;
         if (kWat) {
+          const double dfp[3] = {-sc * d[0], -sc * d[1], -sc * d[2]};
           Wa[0] += 0.5 * (d[0] * dfp[0]);
           Wa[1] += 0.5 * (d[1] * dfp[1]);
           Wa[2] += 0.5 * (d[2] * dfp[2]);
@@ -634,6 +634,9 @@ __global__ void __launch_bounds__(kEamThreads) eam_pair(const EamArgs a) {
           Wa[5] += 0.5 * (d[1] * dfp[2]);
         }
       }
+      F3[0] = fma(sc_f, d[0], F3[0]);
+      F3[1] = fma(sc_f, d[1], F3[1]);
+      F3[2] = fma(sc_f, d[2], F3[2]);
     }
     if (bad) atomicOr(a.status, 1);
   }
